@@ -1,0 +1,356 @@
+#!/usr/bin/env python
+"""Benchmark of SharpRay's render hot path on GB300: path samples/s at 1080p.
+
+Workload (one step): the 1920x1080, 64 spp, depth-8, fog 0.02 scene (871,200-triangle fBm sphere
++ 64 instanced 5,000-triangle rocks, 2048x1024 HDR env, 512x512 albedo texture; seed 2), rendered
+and composited (denoise + tonemap) once.  Synthetic seeded data stands in for the reference's
+LFS-only assets.
+
+Lines printed (rank 0, one JSON line):
+* ours (default):   `value` = path samples/s with the scene resident in HBM and AOVs/image written
+  to device memory (CUDA events on the launching stream); `e2e` = the same metric through the
+  public render+compose call with host (pinned) outputs, D2H copies inside the timed region;
+  `roofline` for the path-tracing kernel; `cpu_baseline` = the CPU oracle on a bounded row sample.
+* --impl reference: the CPU restatement of the reference render path (the oracle; the C# reference
+  cannot be built or run here: no .NET SDK/runtime on either machine) on all host cores.
+
+Multi-GPU (torchrun): replicas only -- every rank renders its own full frame (weak scaling), no
+data-path collective; the barrier and max-over-ranks timing use torch.distributed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "path samples/s at 1080p (1920x1080, 64 spp, depth 8, fog)"
+UNIT = "samples/s"
+H2D_PARAM_BYTES = 48 + 32 + 44  # SrView + SrRenderParams + SrComposeParams per call
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the oracle sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            j = json.loads(p.read_text())
+            return float(j["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.lines, self.proc = device, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(c: dict, pixels: int) -> int:
+    """Bytes the reference algorithm must touch per render (data-structure sizes of the reference):
+    32 B per BVH node test, 36 B per triangle test, 40 B per instance test, 108 B per inflated hit,
+    48 B per bilinear texture sample (4 float3 texels), 4 B per CDF probe, 56 B AOV write per pixel."""
+    return int(32 * (c["tlas_node"] + c["blas_node"]) + 36 * c["blas_shape"] + 40 * c["tlas_shape"]
+               + 108 * c["hit_inflate"] + 48 * c["tex_sample"] + 4 * c["cdf_probe"] + 56 * pixels)
+
+
+def cpu_oracle_sample(desc, target_s: float, threads: int):
+    """Times the CPU oracle on a row band of the workload sized for ~target_s seconds."""
+    from oracle import oracle
+    from sharpray_gb300 import render_params
+    scene = oracle.instantiate(desc)
+    view, params = desc.view.to_c(), render_params(*desc.render_args())
+    mid = desc.height // 2
+    t0 = time.perf_counter()
+    scene.render(view, params, threads, rows=(mid, mid + 2))
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rows = int(max(2, min(desc.height, round(2 * target_s / dt))))
+    y0 = max(0, mid - rows // 2)
+    t0 = time.perf_counter()
+    aovs, _ = scene.render(view, params, threads, rows=(y0, y0 + rows))
+    dt = time.perf_counter() - t0
+    samples = rows * desc.width * desc.spp
+    return samples / dt, rows, dt
+
+
+def run_reference(args):
+    rank, _, world = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle
+    from sharpray_gb300 import render_params, synth
+    desc = synth.config_c2(args.width, args.height, args.spp)
+    threads = os.cpu_count() or 1
+    scene = oracle.instantiate(desc)
+    view, params = desc.view.to_c(), render_params(*desc.render_args())
+    # calibrate a row band of ~2 s per step so the whole run stays within minutes
+    mid = desc.height // 2
+    t0 = time.perf_counter()
+    scene.render(view, params, threads, rows=(mid, mid + 1))
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rows = int(max(1, min(desc.height, round(2.0 / dt))))
+    for _ in range(args.warmup):
+        scene.render(view, params, threads, rows=(mid, mid + 1))
+    times = []
+    for s in range(args.steps):
+        y0 = (mid - rows // 2 + s * rows) % max(1, desc.height - rows)
+        t0 = time.perf_counter()
+        scene.render(view, params, threads, rows=(y0, y0 + rows))
+        times.append(time.perf_counter() - t0)
+    samples = rows * desc.width * desc.spp * args.steps
+    value = samples / sum(times)
+    sample_desc = f"{rows} image rows x {desc.width} px x {desc.spp} spp per step (of {desc.height} rows)"
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded), CPU",
+        "config": {"workload": desc.name, "width": desc.width, "height": desc.height, "spp": desc.spp,
+                   "bounces": desc.bounces, "sample": sample_desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample_desc,
+                         "note": "C++ restatement of the reference C# CPU path (oracle/); the C# reference "
+                                 "cannot run here (no .NET SDK or runtime)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    rank, local, world = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from sharpray_gb300 import Context, Compositor, _abi, render_params, synth
+    from sharpray_gb300.api import Aovs
+
+    t_setup = time.perf_counter()
+    desc = synth.config_c2(args.width, args.height, args.spp)
+    ctx = Context(local)
+    scene = desc.instantiate(ctx)
+    scene.build()
+    setup_s = time.perf_counter() - t_setup
+    lib = ctx._lib
+    W, H = desc.width, desc.height
+    n = W * H
+    view, params = desc.view.to_c(), render_params(*desc.render_args())
+    comp = Compositor()
+    cparams = comp.to_c()
+
+    dev = {k: torch.empty(n * c, dtype=torch.float32 if k != "samples" else torch.int32, device="cuda")
+           for k, c in [("radiance", 3), ("radiance_fog", 3), ("normals", 3), ("uv", 2), ("depth", 1),
+                        ("samples", 1), ("variance", 1)]}
+    rgb = torch.empty(n * 3, dtype=torch.uint8, device="cuda")
+    aovs = _abi.SrAovs(*[dev[k].data_ptr() for k in ("radiance", "radiance_fog", "normals", "uv", "depth",
+                                                      "samples", "variance")])
+    stream = torch.cuda.current_stream()
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def render():
+        _abi.check(lib.sr_render_device(scene.handle, C.byref(view), C.byref(params), C.byref(aovs), sp))
+
+    def compose():
+        _abi.check(lib.sr_compose_device(ctx.handle, C.byref(aovs), W, H, C.byref(cparams),
+                                         C.c_void_p(rgb.data_ptr()), sp))
+
+    # work counters of one render (untimed) -> algorithmic bytes per launch
+    scene.set_counting(True)
+    render()
+    torch.cuda.synchronize()
+    counters = scene.counters()
+    scene.set_counting(False)
+    samples_per_step = counters["sample"]
+
+    for _ in range(args.warmup):
+        render()
+        compose()
+    torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for a, b, c in ev:
+            a.record(stream)
+            render()
+            b.record(stream)
+            compose()
+            c.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [a.elapsed_time(c) for a, _, c in ev]
+    render_ms = [a.elapsed_time(b) for a, b, _ in ev]
+    total_s = sum(step_ms) / 1000.0
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = samples_per_step * args.steps * world / total_s
+
+    # end to end through the public API with pinned host outputs
+    host = Aovs(W, H)
+    pinned = {}
+    for k in ("radiance", "radiance_fog", "normals", "uv", "depth", "samples", "variance"):
+        arr = getattr(host, k)
+        t = torch.empty(arr.shape, dtype=torch.int32 if k == "samples" else torch.float32).pin_memory()
+        pinned[k] = t
+        setattr(host, k, t.numpy().view(arr.dtype))
+    img_t = torch.empty((H, W, 3), dtype=torch.uint8).pin_memory()
+    img = img_t.numpy()
+    from sharpray_gb300 import render_compose
+    render_compose(scene, desc.view, *desc.render_args(), comp, aovs=host, image=img)  # warm
+    e2e_steps = max(1, args.e2e_steps)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        render_compose(scene, desc.view, *desc.render_args(), comp, aovs=host, image=img)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = samples_per_step * e2e_steps * world / e2e_s
+    d2h = n * (12 + 12 + 12 + 8 + 4 + 4 + 4) + n * 3
+
+    peak, peak_kind = measured_peaks()
+    alg = algorithmic_bytes(counters, n)
+    kern_s = statistics.mean(render_ms) / 1000.0
+    achieved = alg / kern_s / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "render_c2_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, rows, dt = cpu_oracle_sample(desc, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{rows} rows x {W} px x {desc.spp} spp of the same frame ({dt:.1f} s)"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generators; reference assets are LFS pointers)",
+            "config": {"workload": desc.name, "width": W, "height": H, "spp": desc.spp, "bounces": desc.bounces,
+                       "fog_density": 0.02, "triangles": desc.triangle_count, "instances": len(desc.objects) - 1,
+                       "env": "2048x1024", "step": "render + compose (denoise, fog blur, tonemap)",
+                       "l2": "inputs larger than L2: scene ~%.0f MB + AOVs %.0f MB resident" % (
+                           (desc.triangle_count * 192 + 2048 * 1024 * 24) / 1e6, n * 56 / 1e6),
+                       "parallelism": "replicas" if world > 1 else "single", "setup_s": round(setup_s, 2),
+                       "wall_s_timed": round(wall, 3)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": H2D_PARAM_BYTES,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "kernel": "k_render_pixels",
+                         "kernel_ms": 1000 * kern_s, "alg_bytes_per_launch": alg, "peak_source": peak_kind},
+            "cpu_baseline": cpu,
+            "gpu_launches": 3 * args.steps,
+            "clocks": clocks.summary(),
+            "counters_per_step": counters,
+        }
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

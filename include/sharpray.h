@@ -1,0 +1,283 @@
+/*
+ * sharpray.h — C ABI of the GB300 (sm_103a) render hot path of SharpRay.
+ *
+ * The library replaces the CPU render call of the C# reference: scene construction
+ * (Scene/Object/Mesh/Texture/SkyTexture/Fog), the Renderer (per-pixel path loop with
+ * adaptive sampling and seven AOVs) and the Compositor (joint bilateral denoise, fog blur,
+ * tonemap).  Every entry point is plain C: blittable structs, raw pointers and sizes,
+ * int status codes (SR_OK == 0) and a thread-local message from sr_last_error_message().
+ *
+ * Each declaration names the reference interface it replaces (file:line within the
+ * SharpRay project).  Struct layouts are fixed (all fields 4 bytes) so that a C# host can
+ * mirror them with [StructLayout(LayoutKind.Sequential)].
+ *
+ * Threading: one SrContext per host thread.  All device work of a context runs on the
+ * context's CUDA stream unless a *_device entry point is given an explicit stream.
+ */
+#ifndef SHARPRAY_H
+#define SHARPRAY_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SR_API __attribute__((visibility("default")))
+#else
+#define SR_API
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+enum {
+    SR_OK = 0,
+    SR_ERR_INVALID_ARG = 1,   /* bad pointer, size or id (reference: Debug.Assert)        */
+    SR_ERR_STATE = 2,         /* build-state misuse (reference: InvalidOperationException)*/
+    SR_ERR_CUDA = 3,          /* a CUDA runtime call failed                                */
+    SR_ERR_OUT_OF_MEMORY = 4, /* device allocation failed                                  */
+    SR_ERR_DEVICE = 5,        /* a kernel reported an error word (e.g. traversal stack)   */
+    SR_ERR_IO = 6             /* asset parse failure (reference: Exception in obj/image)  */
+};
+
+/* ---- handles ------------------------------------------------------------------------- */
+typedef struct SrContext SrContext;
+typedef struct SrScene SrScene;
+
+/* ---- plain data ---------------------------------------------------------------------- */
+
+/* One triangle exactly as Mesh(IReadOnlyList<Triangle>) consumes it: the lean form
+ * (PosA, PosB-PosA, PosC-PosA) and the per-corner attributes.
+ * Reference: Triangle math.cs:1491-1528, TriangleLean math.cs:1336-1344, mesh.cs:6-11. */
+typedef struct SrTriangle {
+    float pos_a[3], ab[3], ac[3];
+    float norm_a[3], norm_b[3], norm_c[3];
+    float tan_a[4], tan_b[4], tan_c[4]; /* xyz tangent, w bitangent handedness */
+    float uv_a[2], uv_b[2], uv_c[2];
+} SrTriangle;
+
+/* Reference: Transform math.cs:773-879 (Pos, Rot quaternion x,y,z,w, Scale). */
+typedef struct SrTransform {
+    float pos[3];
+    float rot[4];
+    float scale[3];
+} SrTransform;
+
+/* Reference: Material scene.cs:161-187.  Texture ids are from sr_texture_create, -1 = none. */
+typedef struct SrMaterial {
+    float albedo[3];
+    float roughness;
+    float metallic;
+    float transparency;
+    float ior;
+    float radiance[3];
+    int32_t color_texture;
+    int32_t roughness_texture;
+    int32_t metallic_texture;
+    int32_t normal_texture;
+} SrMaterial;
+
+enum { SR_SHAPE_MESH = 0, SR_SHAPE_SPHERE = 1, SR_SHAPE_AABOX = 2 };
+
+/* Reference: IShape implementations Mesh (mesh.cs:4), Sphere (math.cs:1179), AABox (math.cs:936).
+ * sphere: params = {cx, cy, cz, radius}; aabox: params = {minx, miny, minz, maxx, maxy, maxz}. */
+typedef struct SrShape {
+    int32_t kind;
+    int32_t mesh;
+    float params[6];
+} SrShape;
+
+/* Reference: Fog scene.cs:438-442 (exponential height fog; height_falloff must be > 0). */
+typedef struct SrFog {
+    float density;
+    float color[3];
+    float anisotropy;
+    float height_falloff;
+} SrFog;
+
+/* Reference: SkyProcedural ctor scene.cs:341-354 + SunProcedural scene.cs:281-298. */
+typedef struct SrSkyProcedural {
+    float top[3];
+    float middle[3];
+    float bottom[3];
+    float sun_dir[3];
+    float sun_radiance[3];
+    float sun_angle;
+} SrSkyProcedural;
+
+/* Reference: View math.cs:1582-1611 (fov in radians, near plane distance). */
+typedef struct SrView {
+    SrTransform transform;
+    float fov;
+    float near_plane;
+} SrView;
+
+/* Reference: Renderer ctor arguments renderer.cs:40-51. */
+typedef struct SrRenderParams {
+    uint32_t width;
+    uint32_t height;
+    uint32_t block_size;
+    uint32_t min_samples;
+    uint32_t max_samples;
+    float variance_threshold;
+    uint32_t bounces;
+    float indirect_clamp;
+} SrRenderParams;
+
+/* The seven AOV planes of Renderer (renderer.cs:14-20), width*height entries each:
+ * radiance/radiance_fog/normals float3, uv float2, depth float (+inf = none),
+ * samples uint32, variance float.  Host or device pointers depending on the entry point. */
+typedef struct SrAovs {
+    float* radiance;
+    float* radiance_fog;
+    float* normals;
+    float* uv;
+    float* depth;
+    uint32_t* samples;
+    float* variance;
+} SrAovs;
+
+enum { SR_TONEMAP_REINHARD = 0, SR_TONEMAP_LINEAR_SMOOTH = 1 };
+
+/* Reference: Compositor ctor compose.cs:22-48. */
+typedef struct SrComposeParams {
+    int32_t tonemapper;
+    float exposure;
+    float denoise_radius;
+    float denoise_strength;
+    float denoise_strength_max;
+    float denoise_luminance_boost;
+    float denoise_luminance_limit;
+    float denoise_normal_limit;
+    float denoise_depth_limit;
+    float denoise_fog_radius;
+    float denoise_fog_strength;
+} SrComposeParams;
+
+/* Work counters of one render (reference Counters.Type, counters.cs:24-79), collected only
+ * when requested.  Index names: */
+enum {
+    SR_COUNTER_SAMPLE = 0,        /* Scene.Sample calls                 (scene.cs:640)   */
+    SR_COUNTER_SAMPLE_BOUNCE,     /* path segments                      (scene.cs:652)   */
+    SR_COUNTER_SCENE_TRACE,       /* closest-hit rays                   (scene.cs:606)   */
+    SR_COUNTER_SCENE_OCCLUDE,     /* shadow rays                        (scene.cs:581)   */
+    SR_COUNTER_TLAS_NODE,         /* scene BVH box tests                (bvh.cs:189)     */
+    SR_COUNTER_TLAS_SHAPE,        /* object tests                       (bvh.cs:203)     */
+    SR_COUNTER_BLAS_NODE,         /* mesh BVH box tests                 (bvh.cs:189)     */
+    SR_COUNTER_BLAS_SHAPE,        /* triangle tests                     (bvh.cs:203)     */
+    SR_COUNTER_HIT_INFLATE,       /* closest hits inflated              (mesh.cs:57)     */
+    SR_COUNTER_TEX_SAMPLE,        /* Texture.Sample calls               (texture.cs:39)  */
+    SR_COUNTER_CDF_PROBE,         /* Cdf1 binary-search probes          (cdf.cs:40-52)   */
+    SR_COUNTER_COUNT
+};
+
+/* ---- errors / version ----------------------------------------------------------------- */
+SR_API const char* sr_version(void);
+/* Message of the last failed call on this host thread ("" if none). */
+SR_API const char* sr_last_error_message(void);
+
+/* ---- context ---------------------------------------------------------------------------- */
+/* Binds CUDA device `device` and creates the context's stream.  No reference counterpart
+ * (the reference has no device); owns every texture/mesh/scene created from it.
+ * device == -1 creates a host-only context: meshes, BVH builds/exports and scene BVH builds
+ * work, every entry point that needs the GPU returns SR_ERR_STATE. */
+SR_API int sr_ctx_create(int device, SrContext** out_ctx);
+SR_API int sr_ctx_destroy(SrContext* ctx);
+
+/* ---- host-side ingest (no device work) --------------------------------------------------- */
+/* Builds `count` SrTriangles from triangle-corner positions (count*9 floats), optional
+ * corner uvs (count*6, NULL = (0,0),(1,0),(0,1)) and optional corner normals (count*9, NULL =
+ * face normal), then, if smooth_normals != 0 and normals == NULL, replaces the normals by
+ * area-weighted vertex normals.  Replaces the Triangle constructors (math.cs:1498-1527) as
+ * TriangulateFace uses them (obj.cs:403-443) followed by Mesh.ComputeSmoothNormals
+ * (mesh.cs:99-123), i.e. the ObjLoader BuildObject path (obj.cs:170-190). */
+SR_API int sr_triangles_from_corners(const float* positions, const float* uvs, const float* normals,
+                                     uint32_t count, int32_t smooth_normals, SrTriangle* out);
+
+/* ---- textures ---------------------------------------------------------------------------- */
+/* Float3 texels (width*height*3, row-major, row 0 = top), filter 0 = bilinear, 1 = point.
+ * Replaces Texture (texture.cs:6-37) as built by FromSrgb/FromLinear/FromHdr (texture.cs:138-163). */
+SR_API int sr_texture_create(SrContext* ctx, const float* texels_rgb, uint32_t width, uint32_t height,
+                             int32_t filter, float tiling_x, float tiling_y, int32_t* out_id);
+
+/* ---- meshes ------------------------------------------------------------------------------ */
+/* Builds the mesh BVH on the host (binned SAH, 8 bins, intersect cost 0.5; node order and item
+ * permutation identical to bvh.cs) and uploads triangles + attributes.  Replaces
+ * Mesh(IReadOnlyList<Triangle>) mesh.cs:18-45. */
+SR_API int sr_mesh_create(SrContext* ctx, const SrTriangle* triangles, uint32_t count, int32_t* out_id);
+/* Node count of a mesh BVH (for sizing sr_mesh_bvh_export buffers). */
+SR_API int sr_mesh_bvh_size(SrContext* ctx, int32_t mesh, uint32_t* node_count, uint32_t* item_count);
+/* Exports the BVH exactly as bvh.cs stores it: per node {min xyz, max xyz} floats (6 per node)
+ * and {child, shapeCount} ints (2 per node), plus the item permutation.  Replaces the private
+ * Bvh._nodes/_items arrays (bvh.cs:53-55); used by parity tests. */
+SR_API int sr_mesh_bvh_export(SrContext* ctx, int32_t mesh, float* node_bounds, int32_t* node_links,
+                              int32_t* items);
+
+/* ---- scenes ------------------------------------------------------------------------------ */
+/* Replaces `new Scene()` (scene.cs:507). */
+SR_API int sr_scene_create(SrContext* ctx, SrScene** out_scene);
+SR_API int sr_scene_destroy(SrScene* scene);
+/* Replaces Scene.SetSky(new SkyTexture(texture, multiplier, rotYaw)) scene.cs:543-551,389-404. */
+SR_API int sr_scene_set_sky_texture(SrScene* scene, int32_t texture, float multiplier, float rot_yaw);
+/* Replaces Scene.SetSky(new SkyProcedural(...)) scene.cs:543-551,334-356. */
+SR_API int sr_scene_set_sky_procedural(SrScene* scene, const SrSkyProcedural* sky);
+/* Replaces Scene.SetFog(Fog) scene.cs:553-561. */
+SR_API int sr_scene_set_fog(SrScene* scene, const SrFog* fog);
+/* Replaces Scene.AddObject(new Object(name, transform, material, shape)) scene.cs:563-571,214-225.
+ * out_index receives the object index (the order of AddObject calls). */
+SR_API int sr_scene_add_object(SrScene* scene, const SrTransform* transform, const SrMaterial* material,
+                               const SrShape* shape, int32_t* out_index);
+/* Builds the scene BVH over objects (32 bins, intersect cost 10) and uploads the scene.
+ * Replaces Scene.Build scene.cs:517-541 (same errors: a sky is required). */
+SR_API int sr_scene_build(SrScene* scene);
+SR_API int sr_scene_bvh_size(SrScene* scene, uint32_t* node_count, uint32_t* item_count);
+SR_API int sr_scene_bvh_export(SrScene* scene, float* node_bounds, int32_t* node_links, int32_t* items);
+
+/* Closest hit of `count` world rays (origin xyz, dir xyz; dir unit length) on the GPU, host
+ * buffers in and out.  Outputs per ray: object index (-1 = miss), triangle index within the
+ * object's mesh (-1 for analytic shapes), world distance, barycentric u, v.  Replaces the
+ * traversal of Scene.Trace (scene.cs:602-625 -> Bvh.Intersect bvh.cs:165-216 ->
+ * Mesh.Intersect mesh.cs:51-62 -> TriangleLean.Intersect math.cs:1407-1435); used for the
+ * bit-exact hit parity test. */
+SR_API int sr_scene_trace(SrScene* scene, const float* rays, uint32_t count, int32_t* out_object,
+                          int32_t* out_triangle, float* out_dist, float* out_uv);
+
+/* ---- rendering --------------------------------------------------------------------------- */
+/* Renders the full image and copies the AOVs into the caller's host arrays (any of the seven
+ * pointers may be NULL to skip that plane).  Replaces `new Renderer(...)` + the Tick() loop
+ * until Step == Total (renderer.cs:40-151) and reading its public AOV arrays. */
+SR_API int sr_render(SrScene* scene, const SrView* view, const SrRenderParams* params, const SrAovs* host_out);
+/* Same, writing device arrays (all seven required, each width*height entries) on `stream`
+ * (a cudaStream_t, NULL = the context stream).  Asynchronous: returns after the launches. */
+SR_API int sr_render_device(SrScene* scene, const SrView* view, const SrRenderParams* params,
+                            const SrAovs* device_out, void* stream);
+/* Render + Compose in one call, the program.cs flow (program.cs:159-202 then 276-282): renders on
+ * the device, denoises/tonemaps there, and copies back the RGB8 image (host_rgb8, width*height*3
+ * bytes, may be NULL) and whichever AOV planes host_aovs requests (host_aovs or any plane may be
+ * NULL).  Replaces `new Renderer(...)`, the Tick() loop and Compositor.Compose. */
+SR_API int sr_render_compose(SrScene* scene, const SrView* view, const SrRenderParams* params,
+                             const SrComposeParams* compose, const SrAovs* host_aovs, uint8_t* host_rgb8);
+/* Reads the work counters of the last render on this scene (device counting is enabled by
+ * sr_scene_set_counting); counters_out has SR_COUNTER_COUNT entries. */
+SR_API int sr_scene_set_counting(SrScene* scene, int32_t enabled);
+SR_API int sr_scene_counters(SrScene* scene, uint64_t* counters_out);
+
+/* ---- compositing ------------------------------------------------------------------------- */
+/* Joint bilateral denoise + fog blur + tonemap to RGB8 (width*height*3 bytes), host AOVs in,
+ * host pixels out.  Replaces Compositor.Compose compose.cs:74-99 (Filter :101-204,
+ * FilterFog :206-245, Tonemap :247-266, Color.ToPixel math.cs:127-136). */
+SR_API int sr_compose(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height,
+                      const SrComposeParams* params, uint8_t* host_rgb8);
+/* Same on device buffers (radiance, radiance_fog, normals, depth, variance are read) on `stream`. */
+SR_API int sr_compose_device(SrContext* ctx, const SrAovs* device_aovs, uint32_t width, uint32_t height,
+                             const SrComposeParams* params, uint8_t* device_rgb8, void* stream);
+/* Tonemap of radiance + radiance_fog without denoise.  Replaces Compositor.Preview compose.cs:57-65. */
+SR_API int sr_preview(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height,
+                      const SrComposeParams* params, uint8_t* host_rgb8);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHARPRAY_H */

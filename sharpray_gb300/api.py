@@ -1,0 +1,545 @@
+"""Python host API over the C ABI, mirroring the C# reference's render-path classes.
+
+Names, argument meanings and error behaviour follow the reference:
+
+=========================  ==========================================================
+reference (C#)             here
+=========================  ==========================================================
+``Texture`` texture.cs     :class:`Texture` (``from_srgb`` / ``from_linear`` / ``from_hdr``)
+``Mesh`` mesh.cs           :class:`Mesh` (``from_corners`` = ObjLoader triangle path)
+``Sphere``/``AABox``       :class:`Sphere`, :class:`AABox`
+``Material`` scene.cs      :class:`Material`
+``Transform``/``Quat``     :class:`Transform`, :class:`Quat`
+``Object`` scene.cs        :class:`Object`
+``SkyTexture``/``SkyProcedural``  :class:`SkyTexture`, :class:`SkyProcedural`
+``Fog`` scene.cs           :class:`Fog`
+``Scene`` scene.cs         :class:`Scene` (``set_sky``/``set_fog``/``add_object``/``build``)
+``View`` math.cs           :class:`View`
+``Renderer`` renderer.cs   :class:`Renderer` (renders on construction; ``tick`` + AOV arrays)
+``Compositor`` compose.cs  :class:`Compositor` (``compose`` / ``preview``)
+=========================  ==========================================================
+
+Build-state misuse raises :class:`StateError` (the reference's InvalidOperationException).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+from enum import IntEnum
+from typing import Optional, Sequence, Union
+
+import numpy as np
+
+from . import _abi
+from ._abi import (SharpRayError, SrAovs, SrComposeParams, SrFog, SrMaterial, SrRenderParams, SrShape,
+                   SrSkyProcedural, SrTransform, SrView, StateError, check, ptr)
+
+__all__ = [
+    "Context", "Texture", "TextureFilter", "Mesh", "Sphere", "AABox", "Material", "Quat", "Transform", "Object",
+    "SkyTexture", "SkyProcedural", "Fog", "Scene", "View", "Renderer", "Compositor", "Tonemapper",
+    "SharpRayError", "StateError",
+]
+
+
+def _f32(v) -> np.float32:
+    return np.float32(v)
+
+
+class Context:
+    """One CUDA device + stream; owns textures, meshes and scenes (no reference counterpart)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _abi.load()
+        h = C.c_void_p()
+        check(self._lib.sr_ctx_create(device, C.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.sr_ctx_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TextureFilter(IntEnum):
+    Bilinear = 0
+    Point = 1
+
+
+class Texture:
+    """Float RGB texels, repeat-wrapped with tiling (texture.cs:6-69)."""
+
+    def __init__(self, ctx: Context, texels: np.ndarray, filter: TextureFilter = TextureFilter.Bilinear,
+                 tiling: Sequence[float] = (1.0, 1.0)):
+        t = np.ascontiguousarray(texels, dtype=np.float32)
+        if t.ndim != 3 or t.shape[2] != 3:
+            raise ValueError("texels must be (height, width, 3)")
+        self.ctx, self.texels = ctx, t
+        self.height, self.width = t.shape[:2]
+        self.filter, self.tiling = TextureFilter(filter), (float(tiling[0]), float(tiling[1]))
+        out = C.c_int32()
+        check(ctx._lib.sr_texture_create(ctx.handle, ptr(t), self.width, self.height, int(self.filter),
+                                         self.tiling[0], self.tiling[1], C.byref(out)))
+        self.id = out.value
+
+    # Color.FromPixel(Pixel) math.cs:184-191: sRGB decode pow(x/255, 2.2333).
+    @staticmethod
+    def srgb_to_linear(pixels: np.ndarray) -> np.ndarray:
+        p = np.asarray(pixels)[..., :3].astype(np.float32) / np.float32(255.0)
+        return np.power(p, np.float32(2.233333333), dtype=np.float32)
+
+    @classmethod
+    def from_srgb(cls, ctx: Context, pixels: np.ndarray, **kw) -> "Texture":
+        """Texture.FromSrgb texture.cs:138-144 (RGB8/RGBA8 pixels, alpha dropped)."""
+        return cls(ctx, cls.srgb_to_linear(pixels), **kw)
+
+    @classmethod
+    def from_linear(cls, ctx: Context, pixels: np.ndarray, **kw) -> "Texture":
+        """Texture.FromLinear texture.cs:146-152."""
+        p = np.asarray(pixels)[..., :3].astype(np.float32) / np.float32(255.0)
+        return cls(ctx, p, **kw)
+
+    @staticmethod
+    def rgbe_to_linear(rgbe: np.ndarray, max_luminance: float = float(np.finfo(np.float32).max)) -> np.ndarray:
+        """Color.FromPixel(PixelHdr) math.cs:196-202 + ClampLuminance math.cs:118-122."""
+        rgbe = np.asarray(rgbe, dtype=np.uint8)
+        e = rgbe[..., 3].astype(np.int32)
+        scale = (np.ldexp(np.float32(1.0), e - 128).astype(np.float32) / np.float32(256.0)).astype(np.float32)
+        c = rgbe[..., :3].astype(np.float32) * scale[..., None]
+        c[e == 0] = 0.0
+        lum = (np.float32(0.2126) * c[..., 0] + np.float32(0.7152) * c[..., 1]) + np.float32(0.0722) * c[..., 2]
+        m = np.float32(max_luminance)
+        over = lum > m
+        if np.any(over):
+            c[over] = c[over] * (m / lum[over])[:, None]
+        return c.astype(np.float32)
+
+    @classmethod
+    def from_hdr(cls, ctx: Context, rgbe: np.ndarray, max_luminance: float = float(np.finfo(np.float32).max),
+                 **kw) -> "Texture":
+        """Texture.FromHdr texture.cs:154-163 from RGBE pixels (H, W, 4) uint8."""
+        return cls(ctx, cls.rgbe_to_linear(rgbe, max_luminance), **kw)
+
+
+class Mesh:
+    """Triangle mesh with its own binned-SAH BVH built on the host (mesh.cs:18-45)."""
+
+    def __init__(self, ctx: Context, triangles: np.ndarray):
+        tris = np.ascontiguousarray(triangles, dtype=np.float32).reshape(-1, _abi.TRIANGLE_FLOATS)
+        self.ctx, self.triangles = ctx, tris
+        out = C.c_int32()
+        check(ctx._lib.sr_mesh_create(ctx.handle, ptr(tris), tris.shape[0], C.byref(out)))
+        self.id = out.value
+
+    @staticmethod
+    def triangles_from_corners(ctx: Context, positions: np.ndarray, uvs: Optional[np.ndarray] = None,
+                               normals: Optional[np.ndarray] = None, smooth_normals: bool = True) -> np.ndarray:
+        """Triangle ctors + Mesh.ComputeSmoothNormals, the ObjLoader path (obj.cs:170-190, 403-443)."""
+        p = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
+        u = None if uvs is None else np.ascontiguousarray(uvs, dtype=np.float32).reshape(-1, 6)
+        n = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
+        out = np.zeros((p.shape[0], _abi.TRIANGLE_FLOATS), np.float32)
+        check(ctx._lib.sr_triangles_from_corners(ptr(p), ptr(u), ptr(n), p.shape[0], int(smooth_normals), ptr(out)))
+        return out
+
+    @classmethod
+    def from_corners(cls, ctx: Context, positions, uvs=None, normals=None, smooth_normals: bool = True) -> "Mesh":
+        return cls(ctx, cls.triangles_from_corners(ctx, positions, uvs, normals, smooth_normals))
+
+    def bvh(self):
+        """(node bounds (M,6), node links (M,2) = child/shapeCount, item permutation (N,))."""
+        lib, h = self.ctx._lib, self.ctx.handle
+        nn, ni = C.c_uint32(), C.c_uint32()
+        check(lib.sr_mesh_bvh_size(h, self.id, C.byref(nn), C.byref(ni)))
+        b = np.zeros((nn.value, 6), np.float32)
+        l = np.zeros((nn.value, 2), np.int32)
+        it = np.zeros(ni.value, np.int32)
+        check(lib.sr_mesh_bvh_export(h, self.id, ptr(b), ptr(l), ptr(it)))
+        return b, l, it
+
+
+@dataclass
+class Sphere:
+    """Analytic sphere shape (math.cs:1179-1234)."""
+    center: Sequence[float]
+    radius: float
+
+
+@dataclass
+class AABox:
+    """Analytic axis-aligned box shape (math.cs:936-1059)."""
+    min: Sequence[float]
+    max: Sequence[float]
+
+
+Shape = Union[Mesh, Sphere, AABox]
+
+
+@dataclass
+class Material:
+    """scene.cs:161-187.  Textures multiply the scalar values."""
+    albedo: Sequence[float]
+    roughness: float
+    metallic: float = 0.0
+    transparency: float = 0.0
+    ior: float = 1.5
+    radiance: Sequence[float] = (0.0, 0.0, 0.0)
+    color_texture: Optional[Texture] = None
+    roughness_texture: Optional[Texture] = None
+    metallic_texture: Optional[Texture] = None
+    normal_texture: Optional[Texture] = None
+
+    def to_c(self) -> SrMaterial:
+        tid = lambda t: -1 if t is None else t.id
+        m = SrMaterial()
+        m.albedo[:] = [float(x) for x in self.albedo]
+        m.roughness, m.metallic, m.transparency, m.ior = (float(self.roughness), float(self.metallic),
+                                                          float(self.transparency), float(self.ior))
+        m.radiance[:] = [float(x) for x in self.radiance]
+        m.color_texture, m.roughness_texture = tid(self.color_texture), tid(self.roughness_texture)
+        m.metallic_texture, m.normal_texture = tid(self.metallic_texture), tid(self.normal_texture)
+        return m
+
+
+@dataclass
+class Quat:
+    """Rotation quaternion (x, y, z, w) in float32 (math.cs:551-667)."""
+    x: float = 0.0
+    y: float = 0.0
+    z: float = 0.0
+    w: float = 1.0
+
+    @staticmethod
+    def identity() -> "Quat":
+        return Quat(0.0, 0.0, 0.0, 1.0)
+
+    @staticmethod
+    def angle_axis(angle: float, axis: Sequence[float]) -> "Quat":
+        """Quat.AngleAxis math.cs:620-625 (float32 arithmetic)."""
+        half = _f32(angle) * _f32(0.5)
+        s = _f32(math.sin(half))
+        a = [_f32(v) * s for v in axis]
+        return Quat(float(a[0]), float(a[1]), float(a[2]), float(_f32(math.cos(half))))
+
+    def __mul__(self, b: "Quat") -> "Quat":
+        a = self
+        ax, ay, az, aw = map(_f32, (a.x, a.y, a.z, a.w))
+        bx, by, bz, bw = map(_f32, (b.x, b.y, b.z, b.w))
+        return Quat(float(aw * bx + ax * bw + ay * bz - az * by), float(aw * by + ay * bw + az * bx - ax * bz),
+                    float(aw * bz + az * bw + ax * by - ay * bx), float(aw * bw - ax * bx - ay * by - az * bz))
+
+    def as_tuple(self):
+        return (self.x, self.y, self.z, self.w)
+
+
+@dataclass
+class Transform:
+    """Position, rotation, scale (math.cs:773-879)."""
+    pos: Sequence[float] = (0.0, 0.0, 0.0)
+    rot: Quat = field(default_factory=Quat.identity)
+    scale: Sequence[float] = (1.0, 1.0, 1.0)
+
+    @staticmethod
+    def identity() -> "Transform":
+        return Transform()
+
+    def to_c(self) -> SrTransform:
+        t = SrTransform()
+        t.pos[:] = [float(v) for v in self.pos]
+        t.rot[:] = [float(v) for v in self.rot.as_tuple()]
+        t.scale[:] = [float(v) for v in self.scale]
+        return t
+
+
+@dataclass
+class Object:
+    """A shape placed in the scene with a material (scene.cs:204-225)."""
+    name: str
+    trans: Transform
+    material: Material
+    shape: Shape
+
+    def shape_c(self) -> SrShape:
+        s = SrShape()
+        if isinstance(self.shape, Mesh):
+            s.kind, s.mesh = _abi.SR_SHAPE_MESH, self.shape.id
+        elif isinstance(self.shape, Sphere):
+            s.kind, s.mesh = _abi.SR_SHAPE_SPHERE, -1
+            s.params[:4] = [*map(float, self.shape.center), float(self.shape.radius)]
+        elif isinstance(self.shape, AABox):
+            s.kind, s.mesh = _abi.SR_SHAPE_AABOX, -1
+            s.params[:] = [*map(float, self.shape.min), *map(float, self.shape.max)]
+        else:
+            raise TypeError(f"unsupported shape {type(self.shape).__name__}")
+        return s
+
+
+@dataclass
+class SkyTexture:
+    """Equirectangular HDR sky with CDF importance sampling (scene.cs:379-435)."""
+    texture: Texture
+    multiplier: float = 1.0
+    rot_yaw: float = 0.0
+
+
+@dataclass
+class SkyProcedural:
+    """Three-band gradient sky with a cone sun (scene.cs:281-377)."""
+    radiance_top: Sequence[float]
+    radiance_middle: Sequence[float]
+    radiance_bottom: Sequence[float]
+    sun_dir: Sequence[float]
+    sun_radiance: Sequence[float]
+    sun_angle: float
+
+    def to_c(self) -> SrSkyProcedural:
+        s = SrSkyProcedural()
+        s.top[:], s.middle[:], s.bottom[:] = (list(map(float, self.radiance_top)),
+                                              list(map(float, self.radiance_middle)),
+                                              list(map(float, self.radiance_bottom)))
+        s.sun_dir[:], s.sun_radiance[:] = list(map(float, self.sun_dir)), list(map(float, self.sun_radiance))
+        s.sun_angle = float(self.sun_angle)
+        return s
+
+
+@dataclass
+class Fog:
+    """Exponential height fog (scene.cs:438-505).  ``height_falloff`` must be > 0."""
+    density: float
+    color: Sequence[float]
+    anisotropy: float
+    height_falloff: float
+
+    def to_c(self) -> SrFog:
+        f = SrFog()
+        f.density, f.anisotropy, f.height_falloff = float(self.density), float(self.anisotropy), float(self.height_falloff)
+        f.color[:] = [float(c) for c in self.color]
+        return f
+
+
+class Scene:
+    """Objects + sky + optional fog; ``build`` makes the scene BVH and uploads (scene.cs:507-571)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        h = C.c_void_p()
+        check(self._lib.sr_scene_create(ctx.handle, C.byref(h)))
+        self.handle = h
+        self.objects: list[Object] = []
+        self.sky = None
+        self.fog: Optional[Fog] = None
+        self.built = False
+
+    def set_sky(self, sky) -> None:
+        if isinstance(sky, SkyTexture):
+            check(self._lib.sr_scene_set_sky_texture(self.handle, sky.texture.id, float(sky.multiplier),
+                                                     float(sky.rot_yaw)))
+        elif isinstance(sky, SkyProcedural):
+            c = sky.to_c()
+            check(self._lib.sr_scene_set_sky_procedural(self.handle, C.byref(c)))
+        else:
+            raise TypeError("sky must be SkyTexture or SkyProcedural")
+        self.sky = sky
+
+    def set_fog(self, fog: Fog) -> None:
+        c = fog.to_c()
+        check(self._lib.sr_scene_set_fog(self.handle, C.byref(c)))
+        self.fog = fog
+
+    def add_object(self, obj: Object) -> int:
+        t, m, s = obj.trans.to_c(), obj.material.to_c(), obj.shape_c()
+        idx = C.c_int32()
+        check(self._lib.sr_scene_add_object(self.handle, C.byref(t), C.byref(m), C.byref(s), C.byref(idx)))
+        self.objects.append(obj)
+        return idx.value
+
+    def build(self) -> None:
+        check(self._lib.sr_scene_build(self.handle))
+        self.built = True
+
+    def bvh(self):
+        nn, ni = C.c_uint32(), C.c_uint32()
+        check(self._lib.sr_scene_bvh_size(self.handle, C.byref(nn), C.byref(ni)))
+        b = np.zeros((nn.value, 6), np.float32)
+        l = np.zeros((nn.value, 2), np.int32)
+        it = np.zeros(ni.value, np.int32)
+        check(self._lib.sr_scene_bvh_export(self.handle, ptr(b), ptr(l), ptr(it)))
+        return b, l, it
+
+    def trace(self, rays: np.ndarray) -> dict:
+        """Closest hit of world rays (N, 6) = origin, unit dir; on the GPU."""
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        n = r.shape[0]
+        obj = np.empty(n, np.int32)
+        tri = np.empty(n, np.int32)
+        dist = np.empty(n, np.float32)
+        uv = np.empty((n, 2), np.float32)
+        check(self._lib.sr_scene_trace(self.handle, ptr(r), n, ptr(obj), ptr(tri), ptr(dist), ptr(uv)))
+        return {"object": obj, "triangle": tri, "dist": dist, "uv": uv}
+
+    def set_counting(self, enabled: bool) -> None:
+        check(self._lib.sr_scene_set_counting(self.handle, int(enabled)))
+
+    def counters(self) -> dict:
+        out = np.zeros(_abi.SR_COUNTER_COUNT, np.uint64)
+        check(self._lib.sr_scene_counters(self.handle, ptr(out)))
+        return dict(zip(_abi.COUNTER_NAMES, (int(v) for v in out)))
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.sr_scene_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class View:
+    """Pinhole camera (math.cs:1582-1636): fov in radians, horizontal when aspect >= 1."""
+    trans: Transform = field(default_factory=Transform.identity)
+    fov: float = math.radians(60.0)
+    near: float = 0.1
+
+    def to_c(self) -> SrView:
+        v = SrView()
+        v.transform = self.trans.to_c()
+        v.fov, v.near_plane = float(self.fov), float(self.near)
+        return v
+
+
+def render_params(width, height, block_size, min_samples, max_samples, variance_threshold, bounces,
+                  indirect_clamp) -> SrRenderParams:
+    p = SrRenderParams()
+    p.width, p.height, p.block_size = int(width), int(height), int(block_size)
+    p.min_samples, p.max_samples = int(min_samples), int(max_samples)
+    p.variance_threshold, p.bounces, p.indirect_clamp = float(variance_threshold), int(bounces), float(indirect_clamp)
+    return p
+
+
+class Aovs:
+    """The seven AOV planes of a render as numpy arrays (renderer.cs:14-20)."""
+
+    def __init__(self, width: int, height: int):
+        n = width * height
+        self.width, self.height = width, height
+        self.radiance = np.zeros((n, 3), np.float32)
+        self.radiance_fog = np.zeros((n, 3), np.float32)
+        self.normals = np.zeros((n, 3), np.float32)
+        self.uv = np.zeros((n, 2), np.float32)
+        self.depth = np.zeros(n, np.float32)
+        self.samples = np.zeros(n, np.uint32)
+        self.variance = np.zeros(n, np.float32)
+
+    def to_c(self) -> SrAovs:
+        a = SrAovs()
+        a.radiance, a.radiance_fog, a.normals = ptr(self.radiance), ptr(self.radiance_fog), ptr(self.normals)
+        a.uv, a.depth, a.samples, a.variance = ptr(self.uv), ptr(self.depth), ptr(self.samples), ptr(self.variance)
+        return a
+
+
+class Renderer:
+    """Renders the whole image on construction (the GPU finishes all tiles in one call).
+
+    ``tick()`` returns ``(Step, Total)`` like renderer.cs:98-105 and is always complete; the AOV arrays
+    ``radiance``, ``radiance_fog``, ``normals``, ``uv``, ``depth``, ``samples``, ``variance`` match
+    renderer.cs:14-20 (flattened row-major, one entry per pixel).
+    """
+
+    def __init__(self, scene: Scene, view: View, width: int, height: int, block_size: int, min_samples: int,
+                 max_samples: int, variance_threshold: float, bounces: int, indirect_clamp: float):
+        if not scene.built:
+            scene.build()  # the reference's ctor calls scene.Build (renderer.cs:77)
+        self.scene, self.view = scene, view
+        self.width, self.height = int(width), int(height)
+        self.params = render_params(width, height, block_size, min_samples, max_samples, variance_threshold,
+                                    bounces, indirect_clamp)
+        self.aovs = Aovs(self.width, self.height)
+        v, a = view.to_c(), self.aovs.to_c()
+        check(scene._lib.sr_render(scene.handle, C.byref(v), C.byref(self.params), C.byref(a)))
+        bx = (self.width + block_size - 1) // block_size
+        by = (self.height + block_size - 1) // block_size
+        self._total = bx * by
+
+    def tick(self):
+        return (self._total, self._total)
+
+    def __getattr__(self, name):
+        if name in ("radiance", "radiance_fog", "normals", "uv", "depth", "samples", "variance"):
+            return getattr(self.aovs, name)
+        raise AttributeError(name)
+
+
+class Tonemapper(IntEnum):
+    Reinhard = _abi.SR_TONEMAP_REINHARD
+    LinearSmooth = _abi.SR_TONEMAP_LINEAR_SMOOTH
+
+
+@dataclass
+class Compositor:
+    """Denoise + tonemap (compose.cs:22-48); defaults are program.cs:29-40."""
+    tonemapper: Tonemapper = Tonemapper.LinearSmooth
+    exposure: float = 1.0
+    denoise_radius: float = 0.0075
+    denoise_strength: float = 0.1
+    denoise_strength_max: float = 1.75
+    denoise_luminance_boost: float = 0.25
+    denoise_luminance_limit: float = 2.0
+    denoise_normal_limit: float = 0.125
+    denoise_depth_limit: float = 0.2
+    denoise_fog_radius: float = 0.002
+    denoise_fog_strength: float = 0.05
+
+    def to_c(self) -> SrComposeParams:
+        p = SrComposeParams()
+        p.tonemapper, p.exposure = int(self.tonemapper), float(self.exposure)
+        p.denoise_radius, p.denoise_strength = float(self.denoise_radius), float(self.denoise_strength)
+        p.denoise_strength_max = float(self.denoise_strength_max)
+        p.denoise_luminance_boost = float(self.denoise_luminance_boost)
+        p.denoise_luminance_limit = float(self.denoise_luminance_limit)
+        p.denoise_normal_limit, p.denoise_depth_limit = float(self.denoise_normal_limit), float(self.denoise_depth_limit)
+        p.denoise_fog_radius, p.denoise_fog_strength = float(self.denoise_fog_radius), float(self.denoise_fog_strength)
+        return p
+
+    def compose(self, rend: Renderer) -> np.ndarray:
+        """Compositor.Compose compose.cs:74-99 -> (H, W, 3) uint8."""
+        out = np.zeros((rend.height, rend.width, 3), np.uint8)
+        a, p = rend.aovs.to_c(), self.to_c()
+        ctx = rend.scene.ctx
+        check(ctx._lib.sr_compose(ctx.handle, C.byref(a), rend.width, rend.height, C.byref(p), ptr(out)))
+        return out
+
+    def preview(self, rend: Renderer) -> np.ndarray:
+        """Compositor.Preview compose.cs:57-65 (tonemap without denoise)."""
+        out = np.zeros((rend.height, rend.width, 3), np.uint8)
+        a, p = rend.aovs.to_c(), self.to_c()
+        ctx = rend.scene.ctx
+        check(ctx._lib.sr_preview(ctx.handle, C.byref(a), rend.width, rend.height, C.byref(p), ptr(out)))
+        return out
+
+
+def render_compose(scene: Scene, view: View, width: int, height: int, block_size: int, min_samples: int,
+                   max_samples: int, variance_threshold: float, bounces: int, indirect_clamp: float,
+                   compositor: Compositor, aovs: Optional[Aovs] = None, image: Optional[np.ndarray] = None):
+    """Render + Compose in one native call (sr_render_compose); returns (image, aovs)."""
+    if not scene.built:
+        scene.build()
+    p = render_params(width, height, block_size, min_samples, max_samples, variance_threshold, bounces,
+                      indirect_clamp)
+    v, cp = view.to_c(), compositor.to_c()
+    if image is None:
+        image = np.zeros((height, width, 3), np.uint8)
+    a = C.byref(aovs.to_c()) if aovs is not None else None
+    check(scene._lib.sr_render_compose(scene.handle, C.byref(v), C.byref(p), C.byref(cp), a, ptr(image)))
+    return image, aovs

@@ -1,0 +1,959 @@
+// sr_device.cuh — device-side scene layout and the per-path arithmetic of SharpRay's hot path.
+//
+// Everything here is compiled with -fmad=false and IEEE division/sqrt so that every float
+// operation matches the C# reference's single-precision evaluation order (left to right, no
+// FMA contraction).  Integer work (RNG, BVH indices) is exact by construction; the BVH
+// traversal is bit-exact, so closest-hit results equal the reference's.  The transcendental
+// calls (sinf, cosf, expf, logf, powf, atan2f, asinf) are CUDA's, which differ from the C
+// runtime by at most a few ulp; images are therefore compared statistically.
+#pragma once
+
+#include <cstdint>
+
+#include "sr_layout.h"
+
+namespace sr {
+
+#define SR_DEV __device__ __forceinline__
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// ---- small vector types ------------------------------------------------------------------------
+struct V2 {
+    float x, y;
+};
+struct V3 {
+    float x, y, z;
+};
+struct V4 {
+    float x, y, z, w;
+};
+struct Col {
+    float r, g, b;
+};
+
+SR_DEV V2 operator+(V2 a, V2 b) { return {a.x + b.x, a.y + b.y}; }
+SR_DEV V2 operator*(V2 v, float s) { return {v.x * s, v.y * s}; }
+SR_DEV V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+SR_DEV V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+SR_DEV V3 operator-(V3 v) { return {-v.x, -v.y, -v.z}; }
+SR_DEV V3 operator*(V3 a, float b) { return {a.x * b, a.y * b, a.z * b}; }
+SR_DEV V3 operator*(float a, V3 b) { return {a * b.x, a * b.y, a * b.z}; }
+SR_DEV V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+SR_DEV V3 operator/(V3 a, float b) { return {a.x / b, a.y / b, a.z / b}; }
+SR_DEV V3 operator/(V3 a, V3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+SR_DEV float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+SR_DEV V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+SR_DEV float mag_sqr(V3 v) { return dot(v, v); }
+SR_DEV float magnitude(V3 v) { return sqrtf(mag_sqr(v)); }
+SR_DEV V3 normalize(V3 v) { return v / magnitude(v); }
+SR_DEV V3 normalize_or(V3 v, V3 fb) {
+    float m = mag_sqr(v);
+    return m >= 1e-12f ? v / sqrtf(m) : fb;
+}
+SR_DEV V3 up3() { return {0.f, 1.f, 0.f}; }
+SR_DEV V3 right3() { return {1.f, 0.f, 0.f}; }
+SR_DEV V4 operator+(V4 a, V4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+SR_DEV V4 operator*(V4 a, float b) { return {a.x * b, a.y * b, a.z * b, a.w * b}; }
+SR_DEV V3 xyz(V4 v) { return {v.x, v.y, v.z}; }
+SR_DEV V3 v3(float4 f) { return {f.x, f.y, f.z}; }
+
+SR_DEV Col operator+(Col a, Col b) { return {a.r + b.r, a.g + b.g, a.b + b.b}; }
+SR_DEV Col operator-(Col a, Col b) { return {a.r - b.r, a.g - b.g, a.b - b.b}; }
+SR_DEV Col operator*(Col a, Col b) { return {a.r * b.r, a.g * b.g, a.b * b.b}; }
+SR_DEV Col operator*(Col c, float s) { return {c.r * s, c.g * s, c.b * s}; }
+SR_DEV Col operator*(float s, Col c) { return {c.r * s, c.g * s, c.b * s}; }
+SR_DEV Col operator/(Col c, float s) { return {c.r / s, c.g / s, c.b / s}; }
+SR_DEV Col operator/(Col a, Col b) { return {a.r / b.r, a.g / b.g, a.b / b.b}; }
+SR_DEV Col gray(float v) { return {v, v, v}; }
+SR_DEV Col black() { return {0.f, 0.f, 0.f}; }
+SR_DEV Col white() { return {1.f, 1.f, 1.f}; }
+SR_DEV float luminance(Col c) { return 0.2126f * c.r + 0.7152f * c.g + 0.0722f * c.b; }
+SR_DEV float max_component(Col c) { return fmaxf(c.r, fmaxf(c.g, c.b)); }
+SR_DEV Col clamp_luminance(Col c, float max) {
+    float lum = luminance(c);
+    return lum > max ? c * (max / lum) : c;
+}
+SR_DEV Col lerp(Col a, Col b, float t) { return {a.r + (b.r - a.r) * t, a.g + (b.g - a.g) * t, a.b + (b.b - a.b) * t}; }
+SR_DEV Col bilerp(Col c1, Col c2, Col c3, Col c4, float tx, float ty) { return lerp(lerp(c1, c2, tx), lerp(c3, c4, tx), ty); }
+SR_DEV float clampf(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+SR_DEV Col col3(float4 f) { return {f.x, f.y, f.z}; }
+
+// ---- quaternions (Quat * Vec3, math.cs:609-617) ------------------------------------------------
+SR_DEV V3 quat_rotate(float4 q, V3 v) {
+    V3 axis{q.x, q.y, q.z};
+    float sqr = mag_sqr(axis);
+    V3 a = axis * (dot(axis, v) * 2.0f);
+    V3 b = v * (q.w * q.w - sqr);
+    V3 c = cross(axis, v) * (q.w * 2.0f);
+    return a + b + c;
+}
+SR_DEV float4 quat_inverse(float4 q) { return make_float4(-q.x, -q.y, -q.z, q.w); }
+
+// ---- rays (Ray ctor math.cs:846-857) -------------------------------------------------------------
+struct Ray {
+    V3 o, d, inv;
+};
+SR_DEV float safe_comp(float d) { return fabsf(d) >= 1e-8f ? d : copysignf(1e-8f, d); }
+SR_DEV Ray make_ray(V3 o, V3 d) {
+    Ray r;
+    r.o = o;
+    r.d = d;
+    r.inv = {1.0f / safe_comp(d.x), 1.0f / safe_comp(d.y), 1.0f / safe_comp(d.z)};
+    return r;
+}
+SR_DEV V3 ray_at(const Ray& r, float t) { return r.o + r.d * t; }
+
+// ---- RNG: xorwow-style generator seeded by splitmix64 (math.cs:1665-1743) -------------------------
+struct Rng {
+    uint32_t s0, s1, s2, s3, s4;
+};
+SR_DEV uint64_t split_mix64(uint64_t& state) {
+    uint64_t r = state += 0x9e3779b97f4a7c15ULL;
+    r = (r ^ (r >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    r = (r ^ (r >> 27)) * 0x94d049bb133111ebULL;
+    return r ^ (r >> 31);
+}
+SR_DEV Rng rng_seed(uint32_t a, uint32_t b) {
+    uint64_t seed = ((uint64_t)a << 32) | b;
+    uint64_t v1 = split_mix64(seed);
+    uint64_t v2 = split_mix64(seed);
+    return {(uint32_t)v1, (uint32_t)(v1 >> 32), (uint32_t)v2, (uint32_t)(v2 >> 32), 0u};
+}
+SR_DEV uint32_t rng_uint(Rng& r) {
+    uint32_t t = r.s3;
+    uint32_t s = r.s0;
+    r.s3 = r.s2;
+    r.s2 = r.s1;
+    r.s1 = s;
+    t ^= t >> 2;
+    t ^= t << 1;
+    t ^= s ^ (s << 4);
+    r.s0 = t;
+    r.s4 += 362437u;
+    return t + r.s4;
+}
+SR_DEV float rng_float(Rng& r) {
+    const float to_float = 1.0f / (4294967296.0f + 512.0f);
+    return __uint2float_rn(rng_uint(r)) * to_float;
+}
+SR_DEV float rng_exponential(Rng& r) {
+    float u;
+    do {
+        u = rng_float(r);
+    } while (u <= 1e-8f);
+    return -logf(u);
+}
+SR_DEV void rng_gauss(Rng& r, float& a_out, float& b_out) {
+    float a;
+    do {
+        a = rng_float(r);
+    } while (a <= 1e-8f);
+    float b = (kPi * 2.0f) * rng_float(r);
+    float mag = sqrtf(-2.0f * logf(a));
+    float sb, cb;
+    sincosf(b, &sb, &cb);
+    a_out = mag * cb;
+    b_out = mag * sb;
+}
+SR_DEV V2 rand_v2(Rng& r) {
+    float x = rng_float(r);
+    float y = rng_float(r);
+    return {x, y};
+}
+SR_DEV V3 rand_on_sphere(Rng& r) {
+    while (true) {
+        float x, y, z, unused;
+        rng_gauss(r, x, y);
+        rng_gauss(r, z, unused);
+        float m = x * x + y * y + z * z;
+        if (m > 1e-6f) return V3{x, y, z} / sqrtf(m);
+    }
+}
+
+// ---- work counters (per thread, flushed once per warp) --------------------------------------------
+struct Ctr {
+    uint32_t v[SR_COUNTER_COUNT];
+};
+#define SR_COUNT(c, idx, n)            \
+    do {                               \
+        if (COUNT) (c).v[(idx)] += (n); \
+    } while (0)
+
+// ---- AABB slab test (AABox.IntersectDist math.cs:983-1004) ----------------------------------------
+SR_DEV bool slab(float4 lo, float4 hi, const Ray& r, float& t_out) {
+    float t1 = (lo.x - r.o.x) * r.inv.x;
+    float t2 = (hi.x - r.o.x) * r.inv.x;
+    float t3 = (lo.y - r.o.y) * r.inv.y;
+    float t4 = (hi.y - r.o.y) * r.inv.y;
+    float t5 = (lo.z - r.o.z) * r.inv.z;
+    float t6 = (hi.z - r.o.z) * r.inv.z;
+    float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
+    float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
+    if (tmax < 0.0f || tmin > tmax) return false;
+    t_out = fmaxf(0.0f, tmin);
+    return true;
+}
+
+// ---- Moller-Trumbore (TriangleLean.Intersect math.cs:1407-1435) ------------------------------------
+SR_DEV bool tri_hit(V3 a, V3 ab, V3 ac, const Ray& r, float& t_out, float& u_out, float& v_out) {
+    V3 h = cross(r.d, ac);
+    float det = dot(ab, h);
+    if (fabsf(det) <= 1e-7f) return false;
+    float inv_det = 1.0f / det;
+    const float eps = 1e-7f;
+    V3 ao = r.o - a;
+    float u = dot(ao, h) * inv_det;
+    if (u < -eps || u > (1.0f + eps)) return false;
+    V3 q = cross(ao, ab);
+    float v = dot(r.d, q) * inv_det;
+    if (v < -eps || (u + v) > (1.0f + eps)) return false;
+    float t = dot(ac, q) * inv_det;
+    if (t < 0.0f) return false;
+    t_out = t;
+    u_out = u;
+    v_out = v;
+    return true;
+}
+
+// Traversal stack entry: the pushed node's own (child, count) record and its entry distance.
+struct StackEntry {
+    int child;
+    int count;
+    float t;
+};
+constexpr int kStackSize = 128;  // bvh.cs:172 stackalloc size; depth cap 64 keeps use <= 65.
+// Upper bound on node pops of one traversal.  A well-formed tree of N nodes needs at most N pops;
+// the cap only turns a malformed tree into an error word instead of a hang.
+constexpr uint32_t kMaxPops = 1u << 24;
+
+SR_DEV float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Bvh<TriangleLean>.Intersect (bvh.cs:165-216) over one mesh BVH in the object's local space.
+// Returns the accepted triangle position (index into the reordered triangle array) or -1.
+template <bool COUNT>
+SR_DEV int blas_closest(const DevScene& S, int root, const Ray& r, float& t_best, float& u_best, float& v_best,
+                        Ctr& c, uint32_t* err) {
+    if (root < 0) return -1;  // empty mesh: Bvh.Intersect returns null
+    StackEntry stack[kStackSize];
+    uint32_t pops = 0;
+    float4 rn1 = ldg4(S.nodes + 2 * root + 1);
+    float4 rn0 = ldg4(S.nodes + 2 * root);
+    int sp = 0;
+    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+    float best = __int_as_float(0x7f800000);
+    int best_pos = -1;
+    while (sp > 0) {
+        StackEntry e = stack[--sp];
+        if (++pops > kMaxPops) {
+            atomicOr(err, SR_DEVERR_LOOP);
+            break;
+        }
+        if (e.t >= best) continue;
+        if (e.count == 0) {
+            SR_COUNT(c, SR_COUNTER_BLAS_NODE, 2);
+            const float4* n = S.nodes + 2 * e.child;
+            float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
+            float ta = 0.f, tb = 0.f;
+            bool pa = slab(a0, a1, r, ta) && ta <= best;
+            bool pb = slab(b0, b1, r, tb) && tb <= best;
+            if (sp + 2 > kStackSize) {
+                atomicOr(err, SR_DEVERR_STACK);
+                return -1;
+            }
+            StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
+            StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
+            if (pa && pb) {
+                if (ta < tb) {
+                    stack[sp++] = eb;
+                    stack[sp++] = ea;
+                } else {
+                    stack[sp++] = ea;
+                    stack[sp++] = eb;
+                }
+            } else if (pa) {
+                stack[sp++] = ea;
+            } else if (pb) {
+                stack[sp++] = eb;
+            }
+        } else {
+            SR_COUNT(c, SR_COUNTER_BLAS_SHAPE, (uint32_t)e.count);
+            for (int i = 0; i < e.count; ++i) {
+                const float4* tp = S.tris + 3 * (e.child + i);
+                float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
+                float t, u, v;
+                if (tri_hit(v3(q0), v3(q1), v3(q2), r, t, u, v) && t < best) {
+                    best = t;
+                    best_pos = e.child + i;
+                    u_best = u;
+                    v_best = v;
+                }
+            }
+        }
+    }
+    t_best = best;
+    return best_pos;
+}
+
+// Any-hit over one mesh BVH: true iff the closest-hit traversal above would return a hit.
+// Visiting order and node predicate are the reference's; only the search stops at the first hit.
+template <bool COUNT>
+SR_DEV bool blas_any(const DevScene& S, int root, const Ray& r, Ctr& c, uint32_t* err) {
+    if (root < 0) return false;
+    StackEntry stack[kStackSize];
+    uint32_t pops = 0;
+    float4 rn0 = ldg4(S.nodes + 2 * root);
+    float4 rn1 = ldg4(S.nodes + 2 * root + 1);
+    int sp = 0;
+    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+    while (sp > 0) {
+        StackEntry e = stack[--sp];
+        if (++pops > kMaxPops) {
+            atomicOr(err, SR_DEVERR_LOOP);
+            break;
+        }
+        if (e.count == 0) {
+            SR_COUNT(c, SR_COUNTER_BLAS_NODE, 2);
+            const float4* n = S.nodes + 2 * e.child;
+            float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
+            float ta = 0.f, tb = 0.f;
+            bool pa = slab(a0, a1, r, ta);
+            bool pb = slab(b0, b1, r, tb);
+            if (sp + 2 > kStackSize) {
+                atomicOr(err, SR_DEVERR_STACK);
+                return false;
+            }
+            StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
+            StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
+            if (pa && pb) {
+                if (ta < tb) {
+                    stack[sp++] = eb;
+                    stack[sp++] = ea;
+                } else {
+                    stack[sp++] = ea;
+                    stack[sp++] = eb;
+                }
+            } else if (pa) {
+                stack[sp++] = ea;
+            } else if (pb) {
+                stack[sp++] = eb;
+            }
+        } else {
+            SR_COUNT(c, SR_COUNTER_BLAS_SHAPE, (uint32_t)e.count);
+            for (int i = 0; i < e.count; ++i) {
+                const float4* tp = S.tris + 3 * (e.child + i);
+                float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
+                float t, u, v;
+                if (tri_hit(v3(q0), v3(q1), v3(q2), r, t, u, v)) return true;
+            }
+        }
+    }
+    return false;
+}
+
+// ---- shape hits ---------------------------------------------------------------------------------
+struct ShapeHit {
+    float dist;
+    V3 norm, norm_geo;
+    V4 tan;
+    V2 uv;
+};
+
+// Transform.TransformRayInv math.cs:816-822.
+SR_DEV Ray to_local(const DevObject& o, const Ray& r, float& scale) {
+    float4 inv = quat_inverse(o.rot);
+    V3 s = v3(o.scale_root);
+    V3 origin = quat_rotate(inv, r.o - v3(o.pos_kind)) / s;
+    V3 dir_raw = quat_rotate(inv, r.d) / s;
+    scale = magnitude(dir_raw);
+    return make_ray(origin, dir_raw / scale);
+}
+
+// Sphere.Intersect math.cs:1210-1234.
+SR_DEV bool sphere_hit(float4 sc, const Ray& r, ShapeHit& h, bool full) {
+    V3 c = v3(sc);
+    float rad = sc.w;
+    V3 tc = c - r.o;
+    float ds = mag_sqr(tc);
+    float a = dot(tc, r.d);
+    float disc = rad * rad - ds + a * a;
+    if (disc < 0.0f) return false;
+    float f = sqrtf(disc);
+    float t = ds < rad * rad ? a + f : a - f;
+    if (t < 0.0f) return false;
+    h.dist = t;
+    if (full) {
+        V3 n = normalize(ray_at(r, t) - c);
+        V3 txyz = normalize_or(V3{-n.z, 0.0f, n.x}, right3());
+        h.norm = n;
+        h.norm_geo = n;
+        h.tan = {txyz.x, txyz.y, txyz.z, 1.0f};
+        h.uv = {0.5f + atan2f(n.z, n.x) / (2.0f * kPi), 0.5f - asinf(clampf(n.y, -1.0f, 1.0f)) / kPi};
+    }
+    return true;
+}
+
+// AABox.Intersect math.cs:1006-1059.
+SR_DEV bool box_hit(float4 lo, float4 hi, const Ray& r, ShapeHit& h, bool full) {
+    float t1 = (lo.x - r.o.x) * r.inv.x;
+    float t2 = (hi.x - r.o.x) * r.inv.x;
+    float t3 = (lo.y - r.o.y) * r.inv.y;
+    float t4 = (hi.y - r.o.y) * r.inv.y;
+    float t5 = (lo.z - r.o.z) * r.inv.z;
+    float t6 = (hi.z - r.o.z) * r.inv.z;
+    float mina = fminf(t1, t2), minb = fminf(t3, t4), minc = fminf(t5, t6);
+    float maxa = fmaxf(t1, t2), maxb = fmaxf(t3, t4), maxc = fmaxf(t5, t6);
+    float tmin = fmaxf(fmaxf(mina, minb), minc);
+    float tmax = fminf(fminf(maxa, maxb), maxc);
+    if (tmax < 0.0f || tmin > tmax) return false;
+    bool inside = tmin < 0.0f;
+    float t = inside ? tmax : tmin;
+    h.dist = t;
+    if (full) {
+        V3 p = ray_at(r, t);
+        V3 n;
+        V4 tan;
+        V2 face;
+        if (mina >= minb && mina >= minc) {
+            bool neg = t1 <= t2;
+            n = neg ? V3{-1.f, 0.f, 0.f} : V3{1.f, 0.f, 0.f};
+            tan = {0.f, 1.f, 0.f, neg ? -1.0f : 1.0f};
+            face = {(p.y - lo.y) / (hi.y - lo.y), (p.z - lo.z) / (hi.z - lo.z)};
+        } else if (minb >= mina && minb >= minc) {
+            bool neg = t3 <= t4;
+            n = neg ? V3{0.f, -1.f, 0.f} : V3{0.f, 1.f, 0.f};
+            tan = {1.f, 0.f, 0.f, neg ? 1.0f : -1.0f};
+            face = {(p.x - lo.x) / (hi.x - lo.x), (p.z - lo.z) / (hi.z - lo.z)};
+        } else {
+            bool neg = t5 <= t6;
+            n = neg ? V3{0.f, 0.f, -1.f} : V3{0.f, 0.f, 1.f};
+            tan = {1.f, 0.f, 0.f, neg ? -1.0f : 1.0f};
+            face = {(p.x - lo.x) / (hi.x - lo.x), (p.y - lo.y) / (hi.y - lo.y)};
+        }
+        V3 nn = inside ? -n : n;
+        h.norm = nn;
+        h.norm_geo = nn;
+        h.tan = tan;
+        h.uv = face;
+    }
+    return true;
+}
+
+// TriangleLean.Inflate math.cs:1437-1459 for the triangle at reordered position `pos`.
+SR_DEV ShapeHit inflate(const DevScene& S, int pos, float dist, float u, float v) {
+    const float4* tp = S.tris + 3 * pos;
+    V3 ab = v3(ldg4(tp + 1)), ac = v3(ldg4(tp + 2));
+    const float4* ap = S.attrs + 7 * pos;
+    float4 q0 = ldg4(ap), q1 = ldg4(ap + 1), q2 = ldg4(ap + 2), q3 = ldg4(ap + 3), q4 = ldg4(ap + 4), q5 = ldg4(ap + 5),
+           q6 = ldg4(ap + 6);
+    // attribute record: na.xyz nb.x | nb.yz nc.xy | nc.z ta.xyz | ta.w tb.xyz | tb.w tc.xyz | tc.w uva.xy uvb.x | uvb.y uvc.xy -
+    V3 na{q0.x, q0.y, q0.z}, nb{q0.w, q1.x, q1.y}, nc{q1.z, q1.w, q2.x};
+    V4 ta{q2.y, q2.z, q2.w, q3.x}, tb{q3.y, q3.z, q3.w, q4.x}, tc{q4.y, q4.z, q4.w, q5.x};
+    V2 uva{q5.y, q5.z}, uvb{q5.w, q6.x}, uvc{q6.y, q6.z};
+    float w = 1.0f - u - v;
+    V3 face = normalize_or(cross(ab, ac), up3());
+    V3 ni = na * w + nb * u + nc * v;
+    V3 norm = mag_sqr(ni) >= 1e-12f ? normalize(ni) : face;
+    V4 ti = ta * w + tb * u + tc * v;
+    V3 txyz = xyz(ti);
+    V3 tan_xyz = normalize_or(txyz - dot(txyz, norm) * norm, right3());
+    ShapeHit h;
+    h.dist = dist;
+    h.norm = norm;
+    h.norm_geo = face;
+    h.tan = {tan_xyz.x, tan_xyz.y, tan_xyz.z, ti.w >= 0.0f ? 1.0f : -1.0f};
+    h.uv = uva * w + uvb * u + uvc * v;
+    return h;
+}
+
+// Result of a scene closest-hit query before inflation.
+struct Hit {
+    int obj;     // position of the object in the scene-BVH item order, -1 = miss
+    int tri;     // reordered triangle position (meshes), -1 otherwise
+    float dist;  // world distance (hit.Dist / localRayScale)
+    float tl;    // local distance (meshes)
+    float u, v;  // barycentrics (meshes)
+};
+
+// Scene.Trace's Bvh<Object>.Intersect (bvh.cs:165-216) with Object.Intersect at the leaves
+// (ShapeExtensions.Intersect math.cs:67-79).  Each object is intersected with an unpruned local
+// search exactly as the reference does; only the inflation of the winning hit is deferred.
+template <bool COUNT>
+SR_DEV Hit scene_closest(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err) {
+    Hit best{-1, -1, __int_as_float(0x7f800000), 0.f, 0.f, 0.f};
+    if (S.tlas_root < 0) return best;
+    StackEntry stack[kStackSize];
+    uint32_t pops = 0;
+    float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
+    float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
+    int sp = 0;
+    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+    while (sp > 0) {
+        StackEntry e = stack[--sp];
+        if (++pops > kMaxPops) {
+            atomicOr(err, SR_DEVERR_LOOP);
+            break;
+        }
+        if (e.t >= best.dist) continue;
+        if (e.count == 0) {
+            SR_COUNT(c, SR_COUNTER_TLAS_NODE, 2);
+            const float4* n = S.nodes + 2 * e.child;
+            float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
+            float ta = 0.f, tb = 0.f;
+            bool pa = slab(a0, a1, r, ta) && ta <= best.dist;
+            bool pb = slab(b0, b1, r, tb) && tb <= best.dist;
+            if (sp + 2 > kStackSize) {
+                atomicOr(err, SR_DEVERR_STACK);
+                return best;
+            }
+            StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
+            StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
+            if (pa && pb) {
+                if (ta < tb) {
+                    stack[sp++] = eb;
+                    stack[sp++] = ea;
+                } else {
+                    stack[sp++] = ea;
+                    stack[sp++] = eb;
+                }
+            } else if (pa) {
+                stack[sp++] = ea;
+            } else if (pb) {
+                stack[sp++] = eb;
+            }
+        } else {
+            SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
+            for (int i = 0; i < e.count; ++i) {
+                const DevObject& o = S.objects[e.child + i];
+                float scale;
+                Ray lr = to_local(o, r, scale);
+                int kind = __float_as_int(o.pos_kind.w);
+                if (kind == SR_SHAPE_MESH) {
+                    float t, u, v;
+                    int pos = blas_closest<COUNT>(S, __float_as_int(o.scale_root.w), lr, t, u, v, c, err);
+                    if (pos >= 0) {
+                        float d = t / scale;
+                        if (d < best.dist) best = {e.child + i, pos, d, t, u, v};
+                    }
+                } else {
+                    ShapeHit h;
+                    bool ok = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, lr, h, false)
+                                                      : box_hit(o.shape0, o.shape1, lr, h, false);
+                    if (ok) {
+                        float d = h.dist / scale;
+                        if (d < best.dist) best = {e.child + i, -1, d, 0.f, 0.f, 0.f};
+                    }
+                }
+            }
+        }
+    }
+    return best;
+}
+
+// Occlusion test for all-opaque scenes: true iff scene_closest would report a hit.
+template <bool COUNT>
+SR_DEV bool scene_any(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err) {
+    if (S.tlas_root < 0) return false;
+    StackEntry stack[kStackSize];
+    uint32_t pops = 0;
+    float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
+    float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
+    int sp = 0;
+    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+    while (sp > 0) {
+        StackEntry e = stack[--sp];
+        if (++pops > kMaxPops) {
+            atomicOr(err, SR_DEVERR_LOOP);
+            break;
+        }
+        if (e.count == 0) {
+            SR_COUNT(c, SR_COUNTER_TLAS_NODE, 2);
+            const float4* n = S.nodes + 2 * e.child;
+            float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
+            float ta = 0.f, tb = 0.f;
+            bool pa = slab(a0, a1, r, ta);
+            bool pb = slab(b0, b1, r, tb);
+            if (sp + 2 > kStackSize) {
+                atomicOr(err, SR_DEVERR_STACK);
+                return false;
+            }
+            StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
+            StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
+            if (pa && pb) {
+                if (ta < tb) {
+                    stack[sp++] = eb;
+                    stack[sp++] = ea;
+                } else {
+                    stack[sp++] = ea;
+                    stack[sp++] = eb;
+                }
+            } else if (pa) {
+                stack[sp++] = ea;
+            } else if (pb) {
+                stack[sp++] = eb;
+            }
+        } else {
+            SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
+            for (int i = 0; i < e.count; ++i) {
+                const DevObject& o = S.objects[e.child + i];
+                float scale;
+                Ray lr = to_local(o, r, scale);
+                int kind = __float_as_int(o.pos_kind.w);
+                bool hit;
+                if (kind == SR_SHAPE_MESH) {
+                    hit = blas_any<COUNT>(S, __float_as_int(o.scale_root.w), lr, c, err);
+                } else {
+                    ShapeHit h;
+                    hit = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, lr, h, false)
+                                                  : box_hit(o.shape0, o.shape1, lr, h, false);
+                }
+                if (hit) return true;
+            }
+        }
+    }
+    return false;
+}
+
+// The world-space ShapeHit of a scene hit (ShapeExtensions.Intersect math.cs:67-79).
+template <bool COUNT>
+SR_DEV ShapeHit world_hit(const DevScene& S, const Ray& r, const Hit& hit, Ctr& c) {
+    const DevObject& o = S.objects[hit.obj];
+    float scale;
+    Ray lr = to_local(o, r, scale);
+    int kind = __float_as_int(o.pos_kind.w);
+    ShapeHit h;
+    if (kind == SR_SHAPE_MESH) {
+        SR_COUNT(c, SR_COUNTER_HIT_INFLATE, 1);
+        h = inflate(S, hit.tri, hit.tl, hit.u, hit.v);
+    } else if (kind == SR_SHAPE_SPHERE) {
+        sphere_hit(o.shape0, lr, h, true);
+    } else {
+        box_hit(o.shape0, o.shape1, lr, h, true);
+    }
+    V3 s = v3(o.scale_root);
+    V3 wn = normalize(quat_rotate(o.rot, h.norm / s));
+    V3 wng = normalize(quat_rotate(o.rot, h.norm_geo / s));
+    V3 wt = normalize(quat_rotate(o.rot, xyz(h.tan)));
+    ShapeHit w;
+    w.dist = h.dist / scale;
+    w.norm = wn;
+    w.norm_geo = wng;
+    w.tan = {wt.x, wt.y, wt.z, h.tan.w};
+    w.uv = h.uv;
+    return w;
+}
+
+// ---- textures (Texture.Sample texture.cs:39-69) ----------------------------------------------------
+template <bool COUNT>
+SR_DEV Col tex_sample(const DevScene& S, int id, V2 coord, Ctr& c) {
+    SR_COUNT(c, SR_COUNTER_TEX_SAMPLE, 1);
+    const DevTexture& t = S.textures[id];
+    float u = coord.x * t.tiling_x;
+    u -= floorf(u);
+    float v = coord.y * t.tiling_y;
+    v -= floorf(v);
+    const float4* tx = S.texels + t.offset;
+    uint32_t w = t.width, hgt = t.height;
+    if (t.filter == 1) {
+        uint32_t x = (uint32_t)(u * (float)w) % w;
+        uint32_t y = (uint32_t)(v * (float)hgt) % hgt;
+        return col3(ldg4(tx + (size_t)y * w + x));
+    }
+    float fx = u * (float)(w - 1);
+    float fy = v * (float)(hgt - 1);
+    uint32_t x0 = (uint32_t)fx;
+    uint32_t y0 = (uint32_t)fy;
+    uint32_t x1 = (x0 + 1) % w;
+    uint32_t y1 = (y0 + 1) % hgt;
+    float txf = fx - (float)x0;
+    float tyf = fy - (float)y0;
+    return bilerp(col3(ldg4(tx + (size_t)y0 * w + x0)), col3(ldg4(tx + (size_t)y0 * w + x1)),
+                  col3(ldg4(tx + (size_t)y1 * w + x0)), col3(ldg4(tx + (size_t)y1 * w + x1)), txf, tyf);
+}
+
+// ---- sky ----------------------------------------------------------------------------------------
+SR_DEV V2 equirect_uv(V3 d) {
+    float u = atan2f(d.z, d.x) / (kPi * 2.0f) + 0.5f;
+    float v = 0.5f - asinf(clampf(d.y, -1.0f, 1.0f)) / kPi;
+    return {u, v};
+}
+SR_DEV V3 from_equirect_uv(V2 uv) {
+    float phi = (uv.x - 0.5f) * 2.0f * kPi;
+    float st, ct, sp, cp;
+    sincosf(kPi * uv.y, &st, &ct);
+    sincosf(phi, &sp, &cp);
+    return {st * cp, ct, st * sp};
+}
+
+template <bool COUNT>
+SR_DEV Col sky_radiance(const DevScene& S, V3 dir, Ctr& c) {
+    const DevSky& k = S.sky;
+    if (k.kind == 0) return tex_sample<COUNT>(S, k.texture, equirect_uv(quat_rotate(k.rot_inv, dir)), c) * k.multiplier;
+    const float bias = 0.0001f;
+    float top_b = 1.0f - powf(fminf(1.0f, 1.0f + bias - dir.y), 4.0f);
+    float bot_b = 1.0f - powf(fminf(1.0f, 1.0f + bias + dir.y), 40.0f);
+    float mid_b = 1.0f - top_b - bot_b;
+    Col ambient = col3(k.top) * top_b + col3(k.middle) * mid_b + col3(k.bottom) * bot_b;
+    float blend = fmaxf(0.0f, (dot(dir, v3(k.sun_dir)) - k.sun_cos) / (1.0f - k.sun_cos));
+    return ambient + col3(k.sun_radiance) * blend;
+}
+
+// SkyTexture.LightDir / SunProcedural.LightDir (point-lookup pdf for MIS); 0 = null.
+SR_DEV float sky_light_pdf(const DevScene& S, V3 dir) {
+    const DevSky& k = S.sky;
+    if (k.kind == 0) {
+        if (k.cdf_total <= 0.0f) return 0.0f;
+        V2 uv = equirect_uv(quat_rotate(k.rot_inv, dir));
+        const DevTexture& t = S.textures[k.texture];
+        int cx = (int)(uv.x * (float)t.width) % (int)t.width;
+        int cy = (int)(uv.y * (float)t.height) % (int)t.height;
+        cx = min(max(cx, 0), (int)t.width - 1);  // in range for every finite direction; guards NaN input
+        cy = min(max(cy, 0), (int)t.height - 1);
+        float pdf = luminance(col3(ldg4(S.texels + t.offset + (size_t)cy * t.width + cx))) * k.pdf_scale;
+        return pdf > 0.0f ? pdf : 0.0f;
+    }
+    float ct = dot(dir, v3(k.sun_dir));
+    if (ct < k.sun_cos) return 0.0f;
+    float blend = (ct - k.sun_cos) / (1.0f - k.sun_cos);
+    return blend / k.sun_pdf_denom;
+}
+
+// Cdf1.Sample cdf.cs:37-55 over cdf[0..n].
+template <bool COUNT>
+SR_DEV uint32_t cdf_sample(const float* cdf, uint32_t n, float norm, Ctr& c) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        SR_COUNT(c, SR_COUNTER_CDF_PROBE, 1);
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(cdf + mid + 1) <= norm)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return min(lo, n - 1);
+}
+
+// ISky.LightDirRand (SkyTexture scene.cs:408-416, SunProcedural scene.cs:314-323).
+template <bool COUNT>
+SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr& c) {
+    const DevSky& k = S.sky;
+    if (k.kind == 0) {
+        if (k.cdf_total <= 0.0f) return false;
+        V2 u = rand_v2(rng);
+        const DevTexture& t = S.textures[k.texture];
+        uint32_t y = cdf_sample<COUNT>(k.cdf_marginal, t.height, u.y, c);
+        uint32_t x = cdf_sample<COUNT>(k.cdf_cond + (size_t)y * (t.width + 1), t.width, u.x, c);
+        V2 uv{((float)(int)x + 0.5f) / (float)(int)t.width, ((float)(int)y + 0.5f) / (float)(int)t.height};
+        dir = quat_rotate(k.rot, from_equirect_uv(uv));
+        pdf = luminance(col3(ldg4(S.texels + t.offset + (size_t)y * t.width + x))) * k.pdf_scale;
+        return pdf > 0.0f;
+    }
+    float phi = (kPi * 2.0f) * rng_float(rng);
+    float blend = sqrtf(rng_float(rng));
+    float z = k.sun_cos + (1.0f - k.sun_cos) * blend;
+    float st = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    dir = quat_rotate(k.sun_rot, V3{cp * st, sp * st, z});
+    pdf = blend / k.sun_pdf_denom;
+    return true;
+}
+
+// ---- fog (scene.cs:445-496) -----------------------------------------------------------------------
+SR_DEV float fog_density_at(const DevScene& S, float y) { return S.fog_density * expf(-S.fog_falloff * y); }
+SR_DEV float fog_transmittance_inf(const DevScene& S, const Ray& r) {
+    // OpticalDepth over [0, +inf).
+    float hd = r.d.y;
+    float inf = __int_as_float(0x7f800000);
+    float hs = r.o.y + 0.0f * hd;
+    float he = r.o.y + inf * hd;
+    float ds = fog_density_at(S, hs);
+    float de = fog_density_at(S, he);
+    float od = fabsf(hd) < 1e-6f ? ds * (inf - 0.0f) : (ds - de) / (S.fog_falloff * hd);
+    return expf(-od);
+}
+SR_DEV bool fog_scatter_distance(const DevScene& S, const Ray& r, float end, Rng& rng, float& t_out) {
+    float hd = r.d.y;
+    float ho = r.o.y;
+    float hs = ho + 0.0f * hd;
+    float u = rng_exponential(rng);
+    float t;
+    if (fabsf(hd) < 1e-6f) {
+        float ds = fog_density_at(S, hs);
+        if (ds <= 0.0f) return false;
+        t = 0.0f + u / ds;
+    } else {
+        float rhs = expf(-S.fog_falloff * hs) - u * S.fog_falloff * hd / S.fog_density;
+        if (rhs <= 0.0f) return false;
+        float yt = -logf(rhs) / S.fog_falloff;
+        t = (yt - ho) / hd;
+    }
+    if (t < end) {
+        t_out = t;
+        return true;
+    }
+    return false;
+}
+
+// ---- BRDF (brdf.cs) ----------------------------------------------------------------------------------
+SR_DEV Col base_reflectivity(float f0, Col albedo, float metallic) { return lerp(gray(f0), albedo, metallic); }
+SR_DEV Col fresnel(float n_dot_v, Col base) {
+    float x = 1.0f - n_dot_v;
+    float x2 = x * x;
+    float x5 = x2 * x2 * x;
+    return base + (white() - base) * x5;
+}
+SR_DEV float ggx_d(float n_dot_h, float rs) {
+    float a2 = rs * rs;
+    float nh2 = n_dot_h * n_dot_h;
+    float d = (1.0f - nh2) + nh2 * a2;
+    return a2 / (kPi * d * d);
+}
+SR_DEV float smith_g1(float n_dot_x, float rs) {
+    float k = rs / 2.0f;
+    return n_dot_x / (n_dot_x * (1.0f - k) + k);
+}
+SR_DEV V3 ggx_sample_local(float rs, V2 u) {
+    float ct = sqrtf((1.0f - u.x) / (u.x * (rs * rs - 1.0f) + 1.0f));
+    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    float phi = (2.0f * kPi) * u.y;
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    return {st * cp, st * sp, ct};
+}
+SR_DEV float power_heuristic(float p1, float p2) {
+    float a = p1 * p1;
+    float b = p2 * p2;
+    return a + b > 0.0f ? a / (a + b) : 0.0f;
+}
+SR_DEV float hg_pdf(float r_dot_l, float g) {
+    float gs = g * g;
+    float d = 1.0f + gs - 2.0f * g * r_dot_l;
+    return (1.0f - gs) / ((4.0f * kPi) * d * sqrtf(d));
+}
+SR_DEV bool refract(V3 in, V3 n, float ratio, V3& out) {
+    float ci = -dot(in, n);
+    float s2t = ratio * ratio * (1.0f - ci * ci);
+    if (s2t >= 1.0f) return false;
+    float ctt = sqrtf(1.0f - s2t);
+    out = ratio * in + (ratio * ci - ctt) * n;
+    return true;
+}
+SR_DEV Col beer_law(Col a, float dist) {
+    return {powf(fmaxf(a.r, 0.0f), dist), powf(fmaxf(a.g, 0.0f), dist), powf(fmaxf(a.b, 0.0f), dist)};
+}
+SR_DEV V3 perp(V3 v) {
+    V3 up = fabsf(v.y) < 0.9f ? up3() : right3();
+    return normalize(cross(up, v));
+}
+SR_DEV V3 hg_scatter_dir(V3 fwd, float g, Rng& rng) {
+    V2 u = rand_v2(rng);
+    float ct;
+    if (fabsf(g) < 1e-3f) {
+        ct = 1.0f - 2.0f * u.x;
+    } else {
+        float s = (1.0f - g * g) / (1.0f - g + 2.0f * g * u.x);
+        ct = (1.0f + g * g - s * s) / (2.0f * g);
+    }
+    ct = clampf(ct, -1.0f, 1.0f);
+    float st = sqrtf(1.0f - ct * ct);
+    float phi = (2.0f * kPi) * u.y;
+    V3 t = perp(fwd);
+    V3 b = cross(fwd, t);
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    return ct * fwd + (st * cp) * t + (st * sp) * b;
+}
+SR_DEV V3 from_tangent_space(V3 d, V4 tangent, V3 n) {
+    V3 t = xyz(tangent);
+    V3 b = tangent.w * cross(n, t);
+    return d.x * t + d.y * b + d.z * n;
+}
+SR_DEV V3 reflect(V3 v, V3 n) { return v - (2.0f * dot(v, n)) * n; }
+
+// ---- Surface (scene.cs:15-151) --------------------------------------------------------------------
+struct Surface {
+    Col radiance, albedo;
+    float roughness, metallic, transparency, ior, f0;
+    V3 normal, normal_geo;
+    V4 tangent;
+    V2 uv;
+};
+struct Scatter {
+    V3 dir;
+    Col weight;
+    bool has_pdf;
+    float pdf;
+    bool refracted;
+};
+
+SR_DEV V3 clamp_to_geo_side(const Surface& s, V3 dir, V3 side) {
+    float d = dot(dir, s.normal_geo);
+    if (d * dot(side, s.normal_geo) < 0.0f) dir = normalize_or(dir - (2.0f * d) * s.normal_geo, side);
+    return dir;
+}
+SR_DEV float specular_probability(const Surface& s, V3 view) {
+    float ndv = fmaxf(1e-4f, dot(s.normal, view));
+    float f = luminance(fresnel(ndv, base_reflectivity(s.f0, s.albedo, s.metallic)));
+    return clampf(fmaxf(f, s.metallic), 0.001f, 0.999f);
+}
+SR_DEV Col opaque_eval(const Surface& s, V3 view, V3 light) {
+    float ndl = dot(s.normal, light);
+    if (ndl <= 0.0f) return black();
+    float ndv = fmaxf(1e-4f, dot(s.normal, view));
+    float rs = fmaxf(s.roughness * s.roughness, 1e-4f);
+    Col base = base_reflectivity(s.f0, s.albedo, s.metallic);
+    V3 half = normalize_or(view + light, s.normal);
+    float ndh = dot(s.normal, half);
+    float hdv = dot(half, view);
+    Col f = fresnel(hdv, base);
+    float g = smith_g1(ndv, rs) * smith_g1(ndl, rs);
+    Col spec = ggx_d(ndh, rs) * f * g / (4.0f * ndv);
+    Col diff = (white() - fresnel(ndv, base)) * s.albedo * (1.0f - s.metallic) * (ndl / kPi);
+    return (spec + diff) * (1.0f - s.transparency);
+}
+SR_DEV float opaque_pdf(const Surface& s, V3 view, V3 light, float spec_p) {
+    float ndl = dot(s.normal, light);
+    if (ndl <= 0.0f) return 0.0f;
+    V3 half = normalize_or(view + light, s.normal);
+    float ndh = fmaxf(0.0f, dot(s.normal, half));
+    float hdv = fmaxf(1e-6f, dot(half, view));
+    float rs = fmaxf(s.roughness * s.roughness, 1e-4f);
+    float ps = ggx_d(ndh, rs) * ndh / (4.0f * hdv);
+    float pd = ndl / kPi;
+    return (spec_p * ps + (1.0f - spec_p) * pd) * (1.0f - s.transparency);
+}
+SR_DEV Scatter surface_scatter(const Surface& s, V3 in, V3 view, Rng& rng) {
+    if (rng_float(rng) < s.transparency) {
+        // TransparentScatter scene.cs:119-144
+        bool entering = dot(in, s.normal_geo) < 0.0f;
+        V3 rn = entering ? s.normal_geo : -s.normal_geo;
+        float ratio = entering ? 1.0f / s.ior : s.ior;
+        float rs = fmaxf(s.roughness * s.roughness, 1e-4f);
+        V3 half = from_tangent_space(ggx_sample_local(rs, rand_v2(rng)), s.tangent, s.normal);
+        if (!entering) half = -half;
+        if (dot(in, half) > 0.0f) half = rn;
+        float hdv = fmaxf(1e-4f, dot(half, view));
+        float f = luminance(fresnel(hdv, base_reflectivity(s.f0, s.albedo, s.metallic)));
+        V3 rdir;
+        if (rng_float(rng) >= f && refract(in, half, ratio, rdir))
+            return {clamp_to_geo_side(s, rdir, -rn), white(), false, 0.0f, true};
+        return {clamp_to_geo_side(s, reflect(in, half), rn), white(), false, 0.0f, false};
+    }
+    // OpaqueScatter scene.cs:103-117
+    float spec_p = specular_probability(s, view);
+    V3 dir;
+    if (rng_float(rng) < spec_p) {
+        float rs = fmaxf(s.roughness * s.roughness, 1e-4f);
+        V3 hl = ggx_sample_local(rs, rand_v2(rng));
+        V3 hw = from_tangent_space(hl, s.tangent, s.normal);
+        dir = reflect(in, hw);
+    } else {
+        dir = normalize_or(s.normal + rand_on_sphere(rng), s.normal);
+    }
+    dir = clamp_to_geo_side(s, dir, s.normal_geo);
+    float pdf = opaque_pdf(s, view, dir, spec_p);
+    return {dir, opaque_eval(s, view, dir) / fmaxf(pdf, 1e-6f), true, pdf, false};
+}
+
+}  // namespace sr

@@ -1,0 +1,891 @@
+// sr_host.cpp — the C ABI (include/sharpray.h): contexts, textures, meshes, scene build and
+// upload, render and compose entry points.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/sharpray.h"
+#include "sr_bvh.h"
+#include "sr_kernels.h"
+#include "sr_layout.h"
+
+using namespace sr;
+using namespace sr::host;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    int code = e == cudaErrorMemoryAllocation ? SR_ERR_OUT_OF_MEMORY : SR_ERR_CUDA;
+    return fail(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SR_CUDA(call, what)                          \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+// Owning device buffer.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    template <typename T>
+    T* as() const {
+        return (T*)ptr;
+    }
+};
+
+cudaError_t upload(DevBuf& buf, const void* src, size_t bytes, cudaStream_t s) {
+    cudaError_t e = buf.reserve(bytes > 0 ? bytes : 16);
+    if (e != cudaSuccess) return e;
+    if (bytes) e = cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyHostToDevice, s);
+    return e;
+}
+
+struct TextureHost {
+    uint32_t width, height;
+    int32_t filter;
+    float tiling_x, tiling_y;
+    std::vector<float> texels;  // rgb
+    float texel_lum(uint32_t x, uint32_t y) const {
+        const float* t = &texels[((size_t)y * width + x) * 3];
+        return 0.2126f * t[0] + 0.7152f * t[1] + 0.0722f * t[2];
+    }
+};
+
+struct MeshHost {
+    std::vector<SrTriangle> tris;
+    BvhHost bvh;
+    Box bounds;
+};
+
+}  // namespace
+
+struct SrContext {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<std::unique_ptr<TextureHost>> textures;
+    std::vector<std::unique_ptr<MeshHost>> meshes;
+    // compose resources
+    DevBuf compose_scratch, compose_tables, compose_io;
+    std::vector<float> table_host;
+};
+
+struct SrScene {
+    SrContext* ctx;
+    // description
+    struct Obj {
+        SrTransform tr;
+        SrMaterial mat;
+        SrShape shape;
+        Box bounds;
+    };
+    std::vector<Obj> objects;
+    int sky_kind = -1;
+    int32_t sky_texture = -1;
+    float sky_multiplier = 1, sky_yaw = 0;
+    SrSkyProcedural sky_proc{};
+    bool has_fog = false;
+    SrFog fog{};
+    bool built = false;
+    BvhHost tlas;
+    // device state
+    DevScene dev{};
+    DevBuf nodes, tris, attrs, objs, mats, texs, texels, cdf_marginal, cdf_cond;
+    DevBuf err, counters;
+    DevBuf aovs;  // staging for sr_render
+    DevBuf rays_io;
+    bool counting = false;
+    uint64_t last_counters[SR_COUNTER_COUNT] = {};
+};
+
+namespace {
+
+F3 f3(const float* p) { return {p[0], p[1], p[2]}; }
+Quat quat(const float* p) { return {p[0], p[1], p[2], p[3]}; }
+float4 mk4(float x, float y, float z, float w) {
+    float4 r;
+    r.x = x, r.y = y, r.z = z, r.w = w;
+    return r;
+}
+float ibits(int32_t v) {
+    float f;
+    std::memcpy(&f, &v, 4);
+    return f;
+}
+
+// Bounds of a triangle from its lean form (TriangleLean.Bounds math.cs:1356-1362).
+Box tri_bounds(const SrTriangle& t) {
+    F3 a = f3(t.pos_a), b = a + f3(t.ab), c = a + f3(t.ac);
+    return {{net_min(a.x, net_min(b.x, c.x)), net_min(a.y, net_min(b.y, c.y)), net_min(a.z, net_min(b.z, c.z))},
+            {net_max(a.x, net_max(b.x, c.x)), net_max(a.y, net_max(b.y, c.y)), net_max(a.z, net_max(b.z, c.z))}};
+}
+
+// Object world bounds: AABox.Transform -> Box, then Box.Bounds (scene.cs:219-220,
+// math.cs:960-961,1100-1113).
+Box object_bounds(const SrTransform& tr, const Box& local) {
+    F3 pos = f3(tr.pos), scale = f3(tr.scale);
+    Quat rot = quat(tr.rot);
+    F3 center = pos + rotate(rot, local.center() * scale);
+    F3 size = local.size() * scale;
+    Box oriented{center - size * 0.5f, center + size * 0.5f};
+    F3 c = oriented.center();
+    F3 h = oriented.size() * 0.5f;
+    F3 ax = rotate(rot, {h.x, 0, 0}), ay = rotate(rot, {0, h.y, 0}), az = rotate(rot, {0, 0, h.z});
+    F3 ext{std::fabs(ax.x) + std::fabs(ay.x) + std::fabs(az.x), std::fabs(ax.y) + std::fabs(ay.y) + std::fabs(az.y),
+           std::fabs(ax.z) + std::fabs(ay.z) + std::fabs(az.z)};
+    F3 full = ext * 2.0f;
+    return {c - full * 0.5f, c + full * 0.5f};
+}
+
+void export_bvh(const BvhHost& b, float* bounds, int32_t* links, int32_t* items) {
+    for (int i = 0; i < b.node_count; ++i) {
+        const BvhNodeHost& n = b.nodes[i];
+        float* o = bounds + (size_t)i * 6;
+        o[0] = n.bounds.lo.x, o[1] = n.bounds.lo.y, o[2] = n.bounds.lo.z;
+        o[3] = n.bounds.hi.x, o[4] = n.bounds.hi.y, o[5] = n.bounds.hi.z;
+        if (links) links[2 * i] = n.child, links[2 * i + 1] = n.count;
+    }
+    if (items) std::memcpy(items, b.items.data(), b.items.size() * sizeof(int32_t));
+}
+
+// Appends one tree to the node slot array.  Slot base is kept even so node pairs (c, c+1) with c
+// odd land on 64-byte boundaries; node i goes to slot base + 1 + i.  Leaves point at
+// `leaf_base + child`, interior nodes (count == 0, including the zero-count leaves the reference
+// can create) at `base + 1 + child`.  Returns the root slot.
+int32_t append_tree(std::vector<float4>& slots, const BvhHost& b, int32_t leaf_base) {
+    if (slots.size() % 4 != 0) slots.resize(slots.size() + 2);  // keep (base) even in node units
+    int32_t base = (int32_t)(slots.size() / 2);
+    slots.resize(slots.size() + 2);  // padding slot
+    for (const BvhNodeHost& n : b.nodes) {
+        int32_t child = n.count > 0 ? leaf_base + n.child : base + 1 + n.child;
+        slots.push_back(mk4(n.bounds.lo.x, n.bounds.lo.y, n.bounds.lo.z, ibits(child)));
+        slots.push_back(mk4(n.bounds.hi.x, n.bounds.hi.y, n.bounds.hi.z, ibits(n.count)));
+    }
+    return b.node_count > 0 ? base + 1 : -1;
+}
+
+bool valid_texture(SrContext* ctx, int32_t id) { return id == -1 || (id >= 0 && id < (int32_t)ctx->textures.size()); }
+
+}  // namespace
+
+extern "C" {
+
+SR_API const char* sr_version(void) { return "sharpray-gb300 0.1 (sm_103a)"; }
+SR_API const char* sr_last_error_message(void) { return g_error.c_str(); }
+
+SR_API int sr_ctx_create(int device, SrContext** out_ctx) {
+    if (!out_ctx) return fail(SR_ERR_INVALID_ARG, "sr_ctx_create: out_ctx is NULL");
+    if (device == -1) {  // host-only context: ingest and BVH builds, no device work
+        auto ctx = std::make_unique<SrContext>();
+        ctx->device = -1;
+        *out_ctx = ctx.release();
+        return SR_OK;
+    }
+    int n = 0;
+    SR_CUDA(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (device < 0 || device >= n) return fail(SR_ERR_INVALID_ARG, "sr_ctx_create: device %d out of range (%d)", device, n);
+    SR_CUDA(cudaSetDevice(device), "cudaSetDevice");
+    auto ctx = std::make_unique<SrContext>();
+    ctx->device = device;
+    SR_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    *out_ctx = ctx.release();
+    return SR_OK;
+}
+
+SR_API int sr_ctx_destroy(SrContext* ctx) {
+    if (!ctx) return SR_OK;
+    if (ctx->device >= 0) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return SR_OK;
+}
+
+SR_API int sr_triangles_from_corners(const float* positions, const float* uvs, const float* normals, uint32_t count,
+                                     int32_t smooth_normals, SrTriangle* out) {
+    if ((!positions || !out) && count) return fail(SR_ERR_INVALID_ARG, "sr_triangles_from_corners: NULL array");
+    triangles_from_corners(positions, uvs, normals, count, smooth_normals != 0, out);
+    return SR_OK;
+}
+
+SR_API int sr_texture_create(SrContext* ctx, const float* texels_rgb, uint32_t width, uint32_t height, int32_t filter,
+                             float tiling_x, float tiling_y, int32_t* out_id) {
+    if (!ctx || !texels_rgb || !out_id) return fail(SR_ERR_INVALID_ARG, "sr_texture_create: NULL argument");
+    if (width == 0 || height == 0) return fail(SR_ERR_INVALID_ARG, "sr_texture_create: empty texture");
+    if (filter != 0 && filter != 1) return fail(SR_ERR_INVALID_ARG, "sr_texture_create: bad filter %d", filter);
+    auto t = std::make_unique<TextureHost>();
+    t->width = width;
+    t->height = height;
+    t->filter = filter;
+    t->tiling_x = tiling_x;
+    t->tiling_y = tiling_y;
+    t->texels.assign(texels_rgb, texels_rgb + (size_t)width * height * 3);
+    ctx->textures.push_back(std::move(t));
+    *out_id = (int32_t)ctx->textures.size() - 1;
+    return SR_OK;
+}
+
+SR_API int sr_mesh_create(SrContext* ctx, const SrTriangle* triangles, uint32_t count, int32_t* out_id) {
+    if (!ctx || (!triangles && count) || !out_id) return fail(SR_ERR_INVALID_ARG, "sr_mesh_create: NULL argument");
+    auto m = std::make_unique<MeshHost>();
+    m->tris.assign(triangles, triangles + count);
+    std::vector<Box> bounds(count);
+    for (uint32_t i = 0; i < count; ++i) bounds[i] = tri_bounds(m->tris[i]);
+    m->bvh = build_bvh(bounds, 1.0f, 0.5f, 8);  // mesh.cs:40-41
+    m->bounds = m->bvh.node_count > 0 ? m->bvh.nodes[0].bounds : Box::inverted();
+    ctx->meshes.push_back(std::move(m));
+    *out_id = (int32_t)ctx->meshes.size() - 1;
+    return SR_OK;
+}
+
+SR_API int sr_mesh_bvh_size(SrContext* ctx, int32_t mesh, uint32_t* node_count, uint32_t* item_count) {
+    if (!ctx || mesh < 0 || mesh >= (int32_t)ctx->meshes.size()) return fail(SR_ERR_INVALID_ARG, "bad mesh id");
+    if (node_count) *node_count = (uint32_t)ctx->meshes[mesh]->bvh.node_count;
+    if (item_count) *item_count = (uint32_t)ctx->meshes[mesh]->bvh.items.size();
+    return SR_OK;
+}
+
+SR_API int sr_mesh_bvh_export(SrContext* ctx, int32_t mesh, float* node_bounds, int32_t* node_links, int32_t* items) {
+    if (!ctx || mesh < 0 || mesh >= (int32_t)ctx->meshes.size()) return fail(SR_ERR_INVALID_ARG, "bad mesh id");
+    if (!node_bounds) return fail(SR_ERR_INVALID_ARG, "node_bounds is NULL");
+    export_bvh(ctx->meshes[mesh]->bvh, node_bounds, node_links, items);
+    return SR_OK;
+}
+
+SR_API int sr_scene_create(SrContext* ctx, SrScene** out_scene) {
+    if (!ctx || !out_scene) return fail(SR_ERR_INVALID_ARG, "sr_scene_create: NULL argument");
+    SrScene* s = new SrScene();
+    s->ctx = ctx;
+    *out_scene = s;
+    return SR_OK;
+}
+
+SR_API int sr_scene_destroy(SrScene* scene) {
+    if (!scene) return SR_OK;
+    if (scene->ctx->device >= 0) {
+        cudaSetDevice(scene->ctx->device);
+        cudaStreamSynchronize(scene->ctx->stream);
+    }
+    delete scene;
+    return SR_OK;
+}
+
+SR_API int sr_scene_set_sky_texture(SrScene* s, int32_t texture, float multiplier, float rot_yaw) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    if (s->built) return fail(SR_ERR_STATE, "Scene already built");
+    if (texture < 0 || texture >= (int32_t)s->ctx->textures.size()) return fail(SR_ERR_INVALID_ARG, "bad texture id");
+    s->sky_kind = 0;
+    s->sky_texture = texture;
+    s->sky_multiplier = multiplier;
+    s->sky_yaw = rot_yaw;
+    return SR_OK;
+}
+
+SR_API int sr_scene_set_sky_procedural(SrScene* s, const SrSkyProcedural* sky) {
+    if (!s || !sky) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (s->built) return fail(SR_ERR_STATE, "Scene already built");
+    s->sky_kind = 1;
+    s->sky_proc = *sky;
+    return SR_OK;
+}
+
+SR_API int sr_scene_set_fog(SrScene* s, const SrFog* fog) {
+    if (!s || !fog) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (s->built) return fail(SR_ERR_STATE, "Scene already built");
+    if (!(fog->height_falloff > 0.0f))
+        return fail(SR_ERR_INVALID_ARG, "Fog height_falloff must be > 0 (the reference divides by it)");
+    if (!(fog->anisotropy > -1.0f && fog->anisotropy < 1.0f))
+        return fail(SR_ERR_INVALID_ARG, "Fog anisotropy must be in (-1, 1)");
+    s->has_fog = true;
+    s->fog = *fog;
+    return SR_OK;
+}
+
+SR_API int sr_scene_add_object(SrScene* s, const SrTransform* tr, const SrMaterial* mat, const SrShape* shape,
+                               int32_t* out_index) {
+    if (!s || !tr || !mat || !shape) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (s->built) return fail(SR_ERR_STATE, "Scene already built");
+    SrContext* ctx = s->ctx;
+    if (!valid_texture(ctx, mat->color_texture) || !valid_texture(ctx, mat->roughness_texture) ||
+        !valid_texture(ctx, mat->metallic_texture) || !valid_texture(ctx, mat->normal_texture))
+        return fail(SR_ERR_INVALID_ARG, "material references an unknown texture");
+    if (tr->scale[0] == 0.0f || tr->scale[1] == 0.0f || tr->scale[2] == 0.0f)
+        return fail(SR_ERR_INVALID_ARG, "Scale cannot be zero");
+    Box local;
+    switch (shape->kind) {
+        case SR_SHAPE_MESH:
+            if (shape->mesh < 0 || shape->mesh >= (int32_t)ctx->meshes.size()) return fail(SR_ERR_INVALID_ARG, "bad mesh id");
+            local = ctx->meshes[shape->mesh]->bounds;
+            break;
+        case SR_SHAPE_SPHERE: {
+            if (!(shape->params[3] > 0.0f)) return fail(SR_ERR_INVALID_ARG, "Radius must be positive");
+            F3 c = f3(shape->params), r{shape->params[3], shape->params[3], shape->params[3]};
+            local = {c - r, c + r};
+            break;
+        }
+        case SR_SHAPE_AABOX:
+            local = {f3(shape->params), f3(shape->params + 3)};
+            break;
+        default:
+            return fail(SR_ERR_INVALID_ARG, "unknown shape kind %d", shape->kind);
+    }
+    s->objects.push_back({*tr, *mat, *shape, object_bounds(*tr, local)});
+    if (out_index) *out_index = (int32_t)s->objects.size() - 1;
+    return SR_OK;
+}
+
+SR_API int sr_scene_build(SrScene* s) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    if (s->built) return SR_OK;
+    if (s->sky_kind < 0) return fail(SR_ERR_STATE, "Scene sky is required");
+    SrContext* ctx = s->ctx;
+
+    // Scene BVH over the objects (scene.cs:530-532).
+    std::vector<Box> ob(s->objects.size());
+    for (size_t i = 0; i < ob.size(); ++i) ob[i] = s->objects[i].bounds;
+    s->tlas = build_bvh(ob, 1.0f, 10.0f, 32);
+    if (ctx->device < 0) {  // host-only context: the BVH is inspectable, nothing is uploaded
+        s->built = true;
+        return SR_OK;
+    }
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+
+    // Meshes used by the scene, each uploaded once however many objects instance it.
+    std::vector<int32_t> mesh_slot(ctx->meshes.size(), -2), mesh_root(ctx->meshes.size(), -1);
+    std::vector<float4> node_slots, tri_rec, attr_rec;
+    for (const auto& o : s->objects) {
+        if (o.shape.kind != SR_SHAPE_MESH || mesh_slot[o.shape.mesh] != -2) continue;
+        const MeshHost& m = *ctx->meshes[o.shape.mesh];
+        int32_t tri_base = (int32_t)(tri_rec.size() / 3);
+        mesh_slot[o.shape.mesh] = tri_base;
+        for (int32_t j = 0; j < (int32_t)m.bvh.items.size(); ++j) {
+            int32_t idx = m.bvh.items[j];
+            const SrTriangle& t = m.tris[idx];
+            tri_rec.push_back(mk4(t.pos_a[0], t.pos_a[1], t.pos_a[2], ibits(idx)));
+            tri_rec.push_back(mk4(t.ab[0], t.ab[1], t.ab[2], 0.0f));
+            tri_rec.push_back(mk4(t.ac[0], t.ac[1], t.ac[2], 0.0f));
+            const float a[28] = {t.norm_a[0], t.norm_a[1], t.norm_a[2], t.norm_b[0], t.norm_b[1], t.norm_b[2],
+                                 t.norm_c[0], t.norm_c[1], t.norm_c[2], t.tan_a[0],  t.tan_a[1],  t.tan_a[2],
+                                 t.tan_a[3],  t.tan_b[0],  t.tan_b[1],  t.tan_b[2],  t.tan_b[3],  t.tan_c[0],
+                                 t.tan_c[1],  t.tan_c[2],  t.tan_c[3],  t.uv_a[0],   t.uv_a[1],   t.uv_b[0],
+                                 t.uv_b[1],   t.uv_c[0],   t.uv_c[1],   0.0f};
+            for (int k = 0; k < 7; ++k) attr_rec.push_back(mk4(a[4 * k], a[4 * k + 1], a[4 * k + 2], a[4 * k + 3]));
+        }
+        mesh_root[o.shape.mesh] = append_tree(node_slots, m.bvh, tri_base);
+    }
+    // Objects in scene-BVH leaf order.
+    std::vector<DevObject> objs(s->objects.size());
+    std::vector<DevMaterial> mats(s->objects.size());
+    bool has_transparent = false;
+    for (size_t p = 0; p < s->objects.size(); ++p) {
+        int32_t idx = s->tlas.items[p];
+        const SrScene::Obj& o = s->objects[idx];
+        DevObject& d = objs[p];
+        std::memset(&d, 0, sizeof(d));
+        d.pos_kind = mk4(o.tr.pos[0], o.tr.pos[1], o.tr.pos[2], ibits(o.shape.kind));
+        d.rot = mk4(o.tr.rot[0], o.tr.rot[1], o.tr.rot[2], o.tr.rot[3]);
+        int32_t root = o.shape.kind == SR_SHAPE_MESH ? mesh_root[o.shape.mesh] : -1;
+        d.scale_root = mk4(o.tr.scale[0], o.tr.scale[1], o.tr.scale[2], ibits(root));
+        d.shape0 = mk4(o.shape.params[0], o.shape.params[1], o.shape.params[2], o.shape.params[3]);
+        d.shape1 = mk4(o.shape.params[3], o.shape.params[4], o.shape.params[5], 0.0f);
+        d.index = idx;
+        if (o.shape.kind == SR_SHAPE_AABOX) d.shape0.w = 0.0f;
+    }
+    for (size_t i = 0; i < s->objects.size(); ++i) {
+        const SrMaterial& m = s->objects[i].mat;
+        DevMaterial& d = mats[i];
+        float r = (m.ior - 1.0f) / (m.ior + 1.0f);
+        float f0 = std::pow(r, 2.0f);  // Brdf.BaseReflectivity brdf.cs:12-16
+        d.albedo_rough = mk4(m.albedo[0], m.albedo[1], m.albedo[2], m.roughness);
+        d.params = mk4(m.metallic, m.transparency, m.ior, f0);
+        d.radiance = mk4(m.radiance[0], m.radiance[1], m.radiance[2], 0.0f);
+        d.tex[0] = m.color_texture, d.tex[1] = m.roughness_texture, d.tex[2] = m.metallic_texture, d.tex[3] = m.normal_texture;
+        if (m.transparency > 0.0f) has_transparent = true;
+    }
+    int32_t tlas_root = append_tree(node_slots, s->tlas, 0);
+
+    // Textures (all of the context's, so ids stay valid).
+    std::vector<DevTexture> texs(ctx->textures.size());
+    std::vector<float4> texels;
+    for (size_t i = 0; i < ctx->textures.size(); ++i) {
+        const TextureHost& t = *ctx->textures[i];
+        DevTexture& d = texs[i];
+        std::memset(&d, 0, sizeof(d));
+        d.width = t.width, d.height = t.height, d.filter = t.filter, d.tiling_x = t.tiling_x, d.tiling_y = t.tiling_y;
+        d.offset = texels.size();
+        for (size_t k = 0; k < (size_t)t.width * t.height; ++k)
+            texels.push_back(mk4(t.texels[3 * k], t.texels[3 * k + 1], t.texels[3 * k + 2], 0.0f));
+    }
+
+    // Sky (SkyTexture ctor scene.cs:389-404 builds a Cdf2 with sin(theta) weights, cdf.cs:62-84).
+    DevSky sky;
+    std::memset(&sky, 0, sizeof(sky));
+    sky.kind = s->sky_kind;
+    std::vector<float> marginal, cond;
+    const float pi = 3.14159265358979323846f;
+    if (s->sky_kind == 0) {
+        const TextureHost& t = *ctx->textures[s->sky_texture];
+        uint32_t w = t.width, h = t.height;
+        cond.assign((size_t)h * (w + 1), 0.0f);
+        std::vector<float> row_w(h);
+        for (uint32_t y = 0; y < h; ++y) {
+            float* c = &cond[(size_t)y * (w + 1)];
+            float sin_w = std::sin(pi * ((float)(int)y + 0.5f) / (float)(int)h);
+            c[0] = 0.0f;
+            for (uint32_t x = 0; x < w; ++x) c[x + 1] = c[x] + t.texel_lum(x, y) * sin_w;
+            float total = c[w];
+            if (total > 0.0f)
+                for (uint32_t x = 1; x <= w; ++x) c[x] /= total;
+            row_w[y] = total;
+        }
+        marginal.assign(h + 1, 0.0f);
+        for (uint32_t y = 0; y < h; ++y) marginal[y + 1] = marginal[y] + row_w[y];
+        float total = marginal[h];
+        if (total > 0.0f)
+            for (uint32_t y = 1; y <= h; ++y) marginal[y] /= total;
+        sky.texture = s->sky_texture;
+        sky.multiplier = s->sky_multiplier;
+        sky.cdf_total = total;
+        sky.pdf_scale = (float)(int)(w * h) / (total * 2.0f * pi * pi);
+        float half = s->sky_yaw * 0.5f;
+        float sh = std::sin(half);
+        Quat q{0.0f * sh, 1.0f * sh, 0.0f * sh, std::cos(half)};  // Quat.AngleAxis(yaw, Up)
+        sky.rot = mk4(q.x, q.y, q.z, q.w);
+        sky.rot_inv = mk4(-q.x, -q.y, -q.z, q.w);
+    } else {
+        const SrSkyProcedural& p = s->sky_proc;
+        sky.top = mk4(p.top[0], p.top[1], p.top[2], 0);
+        sky.middle = mk4(p.middle[0], p.middle[1], p.middle[2], 0);
+        sky.bottom = mk4(p.bottom[0], p.bottom[1], p.bottom[2], 0);
+        sky.sun_dir = mk4(p.sun_dir[0], p.sun_dir[1], p.sun_dir[2], 0);
+        sky.sun_radiance = mk4(p.sun_radiance[0], p.sun_radiance[1], p.sun_radiance[2], 0);
+        sky.sun_cos = std::cos(p.sun_angle);
+        sky.sun_pdf_denom = pi * (1.0f - sky.sun_cos);
+        // Quat.Look(dir, Up) = FromMat4(Mat4.RotateLook(dir, Up)) (math.cs:641-665, 736-751).
+        F3 c0{1, 0, 0}, c1{0, 1, 0}, c2{0, 0, 1};
+        F3 fwd_in = f3(p.sun_dir), up{0, 1, 0};
+        if (!(mag_sqr(fwd_in) <= 1e-6f)) {
+            F3 fwd = normalize(fwd_in);
+            F3 right = cross(up, fwd);
+            right = mag_sqr(right) > 1e-6f ? normalize(right) : F3{1, 0, 0};
+            c0 = right, c1 = cross(fwd, right), c2 = fwd;
+        }
+        float trace = c0.x + c1.y + c2.z;
+        Quat q;
+        if (trace > 1e-6f) {
+            float sq = std::sqrt(trace + 1) * 2;
+            q = {(c1.z - c2.y) / sq, (c2.x - c0.z) / sq, (c0.y - c1.x) / sq, sq * 0.25f};
+        } else if (c0.x > c1.y && c0.x > c2.z) {
+            float sq = std::sqrt(1 + c0.x - c1.y - c2.z) * 2;
+            q = {sq * 0.25f, (c1.x + c0.y) / sq, (c2.x + c0.z) / sq, (c1.z - c2.y) / sq};
+        } else if (c1.y > c2.z) {
+            float sq = std::sqrt(1 + c1.y - c0.x - c2.z) * 2;
+            q = {(c1.x + c0.y) / sq, sq * 0.25f, (c2.y + c1.z) / sq, (c2.x - c0.z) / sq};
+        } else {
+            float sq = std::sqrt(1 + c2.z - c0.x - c1.y) * 2;
+            q = {(c2.x + c0.z) / sq, (c2.y + c1.z) / sq, sq * 0.25f, (c0.y - c1.x) / sq};
+        }
+        sky.sun_rot = mk4(q.x, q.y, q.z, q.w);
+        sky.rot = mk4(0, 0, 0, 1);
+        sky.rot_inv = mk4(0, 0, 0, 1);
+    }
+
+    SR_CUDA(upload(s->nodes, node_slots.data(), node_slots.size() * sizeof(float4), st), "upload nodes");
+    SR_CUDA(upload(s->tris, tri_rec.data(), tri_rec.size() * sizeof(float4), st), "upload triangles");
+    SR_CUDA(upload(s->attrs, attr_rec.data(), attr_rec.size() * sizeof(float4), st), "upload attributes");
+    SR_CUDA(upload(s->objs, objs.data(), objs.size() * sizeof(DevObject), st), "upload objects");
+    SR_CUDA(upload(s->mats, mats.data(), mats.size() * sizeof(DevMaterial), st), "upload materials");
+    SR_CUDA(upload(s->texs, texs.data(), texs.size() * sizeof(DevTexture), st), "upload textures");
+    SR_CUDA(upload(s->texels, texels.data(), texels.size() * sizeof(float4), st), "upload texels");
+    SR_CUDA(upload(s->cdf_marginal, marginal.data(), marginal.size() * sizeof(float), st), "upload cdf");
+    SR_CUDA(upload(s->cdf_cond, cond.data(), cond.size() * sizeof(float), st), "upload cdf");
+    SR_CUDA(s->err.reserve(sizeof(uint32_t)), "alloc error word");
+    SR_CUDA(cudaMemsetAsync(s->err.ptr, 0, sizeof(uint32_t), st), "clear error word");
+    SR_CUDA(s->counters.reserve(SR_COUNTER_COUNT * sizeof(unsigned long long)), "alloc counters");
+    SR_CUDA(cudaStreamSynchronize(st), "scene upload");
+
+    sky.cdf_marginal = s->cdf_marginal.as<float>();
+    sky.cdf_cond = s->cdf_cond.as<float>();
+    DevScene& d = s->dev;
+    std::memset(&d, 0, sizeof(d));
+    d.nodes = s->nodes.as<float4>();
+    d.tris = s->tris.as<float4>();
+    d.attrs = s->attrs.as<float4>();
+    d.objects = s->objs.as<DevObject>();
+    d.materials = s->mats.as<DevMaterial>();
+    d.textures = s->texs.as<DevTexture>();
+    d.texels = s->texels.as<float4>();
+    d.sky = sky;
+    d.tlas_root = tlas_root;
+    d.has_fog = s->has_fog ? 1 : 0;
+    d.has_transparent = has_transparent ? 1 : 0;
+    d.object_count = (int32_t)s->objects.size();
+    if (s->has_fog) {
+        d.fog_density = s->fog.density;
+        d.fog_falloff = s->fog.height_falloff;
+        d.fog_g = s->fog.anisotropy;
+        d.fog_color = mk4(s->fog.color[0], s->fog.color[1], s->fog.color[2], 0);
+    }
+    s->built = true;
+    return SR_OK;
+}
+
+SR_API int sr_scene_bvh_size(SrScene* s, uint32_t* node_count, uint32_t* item_count) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    if (!s->built) return fail(SR_ERR_STATE, "Scene not built");
+    if (node_count) *node_count = (uint32_t)s->tlas.node_count;
+    if (item_count) *item_count = (uint32_t)s->tlas.items.size();
+    return SR_OK;
+}
+
+SR_API int sr_scene_bvh_export(SrScene* s, float* node_bounds, int32_t* node_links, int32_t* items) {
+    if (!s || !node_bounds) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!s->built) return fail(SR_ERR_STATE, "Scene not built");
+    export_bvh(s->tlas, node_bounds, node_links, items);
+    return SR_OK;
+}
+
+static int need_device(SrScene* s) {
+    if (!s->built) return fail(SR_ERR_STATE, "Scene not built");
+    if (s->ctx->device < 0) return fail(SR_ERR_STATE, "host-only context (device -1) cannot run device work");
+    return SR_OK;
+}
+
+static int check_device_error(SrScene* s) {
+    uint32_t word = 0;
+    SR_CUDA(cudaMemcpy(&word, s->err.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read error word");
+    if (word) {
+        cudaMemset(s->err.ptr, 0, sizeof(uint32_t));
+        return fail(SR_ERR_DEVICE, "kernel error word 0x%x (1 = traversal stack overflow, 2 = loop cap)", word);
+    }
+    return SR_OK;
+}
+
+SR_API int sr_scene_trace(SrScene* s, const float* rays, uint32_t count, int32_t* out_object, int32_t* out_triangle,
+                          float* out_dist, float* out_uv) {
+    if (!s || (!rays && count) || !out_object || !out_triangle || !out_dist || !out_uv)
+        return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    size_t in_b = (size_t)count * 6 * 4, out_b = (size_t)count * 5 * 4;
+    SR_CUDA(s->rays_io.reserve(in_b + out_b + 64), "alloc ray buffers");
+    char* base = s->rays_io.as<char>();
+    float* d_rays = (float*)base;
+    int32_t* d_obj = (int32_t*)(base + in_b);
+    int32_t* d_tri = d_obj + count;
+    float* d_dist = (float*)(d_tri + count);
+    float* d_uv = d_dist + count;
+    SR_CUDA(cudaMemcpyAsync(d_rays, rays, in_b, cudaMemcpyHostToDevice, st), "copy rays");
+    SR_CUDA(launch_trace(s->dev, d_rays, count, d_obj, d_tri, d_dist, d_uv, s->err.as<uint32_t>(), st), "trace launch");
+    SR_CUDA(cudaMemcpyAsync(out_object, d_obj, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
+    SR_CUDA(cudaMemcpyAsync(out_triangle, d_tri, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
+    SR_CUDA(cudaMemcpyAsync(out_dist, d_dist, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
+    SR_CUDA(cudaMemcpyAsync(out_uv, d_uv, count * 8, cudaMemcpyDeviceToHost, st), "copy hits");
+    SR_CUDA(cudaStreamSynchronize(st), "trace");
+    return check_device_error(s);
+}
+
+static int make_view(const SrView* v, const SrRenderParams* p, DevView& dv, DevParams& dp) {
+    if (!v || !p) return fail(SR_ERR_INVALID_ARG, "NULL view or params");
+    if (p->width == 0 || p->height == 0) return fail(SR_ERR_INVALID_ARG, "width and height must be > 0");
+    if (p->min_samples == 0 || p->min_samples > p->max_samples)
+        return fail(SR_ERR_INVALID_ARG, "need 0 < min_samples <= max_samples");
+    if (!(v->fov > 0.0f && v->fov < 3.14159265f)) return fail(SR_ERR_INVALID_ARG, "Invalid fov");
+    if (!(v->near_plane > 0.0f)) return fail(SR_ERR_INVALID_ARG, "Invalid near plane");
+    float aspect = (float)p->width / (float)p->height;
+    float th, tv;
+    if (aspect >= 1.0f) {
+        th = std::tan(v->fov * 0.5f);
+        tv = th / aspect;
+    } else {
+        tv = std::tan(v->fov * 0.5f);
+        th = tv * aspect;
+    }
+    Quat rot = quat(v->transform.rot);
+    F3 origin = f3(v->transform.pos) + rotate(rot, F3{0.0f, 0.0f, v->near_plane});
+    dv.origin = mk4(origin.x, origin.y, origin.z, 0);
+    dv.rot = mk4(rot.x, rot.y, rot.z, rot.w);
+    dv.tan_h = th;
+    dv.tan_v = tv;
+    dv.pad0 = dv.pad1 = 0;
+    dp.width = p->width;
+    dp.height = p->height;
+    dp.min_samples = p->min_samples;
+    dp.max_samples = p->max_samples;
+    dp.bounces = p->bounces;
+    dp.variance_threshold = p->variance_threshold;
+    dp.indirect_clamp = p->indirect_clamp;
+    dp.aspect = aspect;
+    return SR_OK;
+}
+
+static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t h, const SrComposeParams* p,
+                        bool denoise, uint8_t* rgb8, cudaStream_t st);
+
+static int render_into(SrScene* s, const SrView* view, const SrRenderParams* params, const DevAovs& out, cudaStream_t st) {
+    DevView dv;
+    DevParams dp;
+    int rc = make_view(view, params, dv, dp);
+    if (rc) return rc;
+    unsigned long long* ctr = nullptr;
+    if (s->counting) {
+        ctr = s->counters.as<unsigned long long>();
+        SR_CUDA(cudaMemsetAsync(ctr, 0, SR_COUNTER_COUNT * sizeof(unsigned long long), st), "clear counters");
+    }
+    SR_CUDA(launch_render(s->dev, dv, dp, out, ctr, s->err.as<uint32_t>(), st), "render launch");
+    return SR_OK;
+}
+
+SR_API int sr_render_device(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* out,
+                            void* stream) {
+    if (!s || !out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    if (!out->radiance || !out->radiance_fog || !out->normals || !out->uv || !out->depth || !out->samples || !out->variance)
+        return fail(SR_ERR_INVALID_ARG, "sr_render_device needs all seven AOV planes");
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    DevAovs d{out->radiance, out->radiance_fog, out->normals, out->uv, out->depth, out->samples, out->variance};
+    return render_into(s, view, params, d, st);
+}
+
+// Device AOV planes (56 B per pixel) plus an RGB8 image, cached on the scene.
+static cudaError_t stage_aovs(SrScene* s, size_t n, DevAovs& d, uint8_t** rgb) {
+    cudaError_t e = s->aovs.reserve(n * 59 + 256);
+    if (e != cudaSuccess) return e;
+    char* b = s->aovs.as<char>();
+    d.radiance = (float*)b;
+    d.radiance_fog = d.radiance + 3 * n;
+    d.normals = d.radiance_fog + 3 * n;
+    d.uv = d.normals + 3 * n;
+    d.depth = d.uv + 2 * n;
+    d.samples = (uint32_t*)(d.depth + n);
+    d.variance = (float*)(d.samples + n);
+    if (rgb) *rgb = (uint8_t*)(d.variance + n);
+    return cudaSuccess;
+}
+
+static int copy_aovs_to_host(const DevAovs& d, size_t n, const SrAovs& host_out, cudaStream_t st) {
+    struct Plane {
+        void* dst;
+        const void* src;
+        size_t bytes;
+    } planes[] = {{host_out.radiance, d.radiance, n * 12},  {host_out.radiance_fog, d.radiance_fog, n * 12},
+                  {host_out.normals, d.normals, n * 12},    {host_out.uv, d.uv, n * 8},
+                  {host_out.depth, d.depth, n * 4},         {host_out.samples, d.samples, n * 4},
+                  {host_out.variance, d.variance, n * 4}};
+    for (const Plane& p : planes)
+        if (p.dst) SR_CUDA(cudaMemcpyAsync(p.dst, p.src, p.bytes, cudaMemcpyDeviceToHost, st), "copy AOVs");
+    return SR_OK;
+}
+
+SR_API int sr_render(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* host_out) {
+    if (!s || !host_out || !params) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    size_t n = (size_t)params->width * params->height;
+    DevAovs d;
+    SR_CUDA(stage_aovs(s, n, d, nullptr), "alloc AOVs");
+    int rc = render_into(s, view, params, d, st);
+    if (rc) return rc;
+    rc = copy_aovs_to_host(d, n, *host_out, st);
+    if (rc) return rc;
+    SR_CUDA(cudaStreamSynchronize(st), "render");
+    if (s->counting)
+        SR_CUDA(cudaMemcpy(s->last_counters, s->counters.ptr, sizeof(s->last_counters), cudaMemcpyDeviceToHost),
+                "read counters");
+    return check_device_error(s);
+}
+
+SR_API int sr_scene_set_counting(SrScene* s, int32_t enabled) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    s->counting = enabled != 0;
+    return SR_OK;
+}
+
+SR_API int sr_scene_counters(SrScene* s, uint64_t* counters_out) {
+    if (!s || !counters_out) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    SR_CUDA(cudaDeviceSynchronize(), "sync");
+    SR_CUDA(cudaMemcpy(counters_out, s->counters.ptr, SR_COUNTER_COUNT * sizeof(uint64_t), cudaMemcpyDeviceToHost),
+            "read counters");
+    return check_device_error(s);
+}
+
+// ---- compose ------------------------------------------------------------------------------------
+static void build_table(std::vector<float>& out, int radius, float inv, float scale) {
+    // (2R+1)^2 spatial weights scale*exp(-d^2*inv), then per-row half widths.
+    int side = 2 * radius + 1;
+    size_t base = out.size();
+    out.resize(base + (size_t)side * side + side);
+    for (int ky = -radius; ky <= radius; ++ky)
+        for (int kx = -radius; kx <= radius; ++kx) {
+            float kd = (float)(kx * kx + ky * ky);
+            out[base + (size_t)(ky + radius) * side + (kx + radius)] = scale * std::exp(-kd * inv);
+        }
+    for (int ky = -radius; ky <= radius; ++ky) {
+        int hw = 0;
+        while ((hw + 1) * (hw + 1) + ky * ky <= radius * radius) ++hw;
+        out[base + (size_t)side * side + (ky + radius)] = (float)hw;
+    }
+}
+
+static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t h, const SrComposeParams* p,
+                        bool denoise, uint8_t* rgb8, cudaStream_t st) {
+    if (!p) return fail(SR_ERR_INVALID_ARG, "params is NULL");
+    if (ctx->device < 0) return fail(SR_ERR_STATE, "host-only context (device -1) cannot run device work");
+    if (w == 0 || h == 0) return fail(SR_ERR_INVALID_ARG, "empty image");
+    if (p->tonemapper != SR_TONEMAP_REINHARD && p->tonemapper != SR_TONEMAP_LINEAR_SMOOTH)
+        return fail(SR_ERR_INVALID_ARG, "Unknown tonemapper: %d", p->tonemapper);
+    ComposeConsts k;
+    k.tonemapper = p->tonemapper;
+    k.exposure = p->exposure;
+    k.strength = p->denoise_strength;
+    k.strength_max = p->denoise_strength_max;
+    k.lum_boost = p->denoise_luminance_boost;
+    k.lum_limit_inv = 1.0f / (p->denoise_luminance_limit * p->denoise_luminance_limit * 2.0f);
+    k.normal_limit_inv = 1.0f / (p->denoise_normal_limit * p->denoise_normal_limit * 2.0f);
+    k.depth_limit_inv = 1.0f / (p->denoise_depth_limit * p->denoise_depth_limit * 2.0f);
+    // Filter / FilterFog radii (compose.cs:112-115, 210-213).
+    float area_sqrt = std::sqrt((float)(int)(w * h));
+    float rp = p->denoise_radius * area_sqrt;
+    float rp_inv = 1.0f / (rp * rp * 2.0f);
+    float rpf = p->denoise_fog_radius * area_sqrt;
+    float rpf_inv = 1.0f / (rpf * rpf * 2.0f);
+    k.radius = (int)std::ceil(rp * 3.0f);
+    k.fog_radius = (int)std::ceil(rpf * 3.0f);
+    if (k.radius < 0 || k.fog_radius < 0 || k.radius > 4096 || k.fog_radius > 4096)
+        return fail(SR_ERR_INVALID_ARG, "denoise radius out of range");
+    std::vector<float>& tab = ctx->table_host;
+    tab.clear();
+    build_table(tab, k.radius, rp_inv, 1.0f);
+    size_t fog_off = tab.size();
+    build_table(tab, k.fog_radius, rpf_inv, p->denoise_fog_strength);
+    SR_CUDA(upload(ctx->compose_tables, tab.data(), tab.size() * sizeof(float), st), "upload tables");
+    size_t n = (size_t)w * h;
+    SR_CUDA(ctx->compose_scratch.reserve(n * 3 * sizeof(float4)), "alloc compose scratch");
+    const float* d_tab = ctx->compose_tables.as<float>();
+    SR_CUDA(launch_compose(in, w, h, k, d_tab, d_tab + fog_off, denoise, rgb8, ctx->compose_scratch.as<float4>(), st),
+            "compose launch");
+    return SR_OK;
+}
+
+SR_API int sr_compose_device(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p,
+                             uint8_t* device_rgb8, void* stream) {
+    if (!ctx || !a || !device_rgb8) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!a->radiance || !a->radiance_fog || !a->normals || !a->depth || !a->variance)
+        return fail(SR_ERR_INVALID_ARG, "compose needs radiance, radiance_fog, normals, depth and variance");
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    DevAovs d{a->radiance, a->radiance_fog, a->normals, a->uv, a->depth, a->samples, a->variance};
+    return compose_impl(ctx, d, w, h, p, true, device_rgb8, st);
+}
+
+static int compose_host(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p,
+                        uint8_t* rgb, bool denoise) {
+    if (!ctx || !a || !rgb || !a->radiance || !a->radiance_fog) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (denoise && (!a->normals || !a->depth || !a->variance))
+        return fail(SR_ERR_INVALID_ARG, "compose needs radiance, radiance_fog, normals, depth and variance");
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    size_t n = (size_t)w * h;
+    SR_CUDA(ctx->compose_io.reserve(n * (12 + 12 + 12 + 4 + 4 + 3) + 256), "alloc compose io");
+    char* b = ctx->compose_io.as<char>();
+    DevAovs d{};
+    d.radiance = (float*)b;
+    d.radiance_fog = d.radiance + 3 * n;
+    d.normals = d.radiance_fog + 3 * n;
+    d.depth = d.normals + 3 * n;
+    d.variance = d.depth + n;
+    uint8_t* d_rgb = (uint8_t*)(d.variance + n);
+    SR_CUDA(cudaMemcpyAsync(d.radiance, a->radiance, n * 12, cudaMemcpyHostToDevice, st), "copy AOVs");
+    SR_CUDA(cudaMemcpyAsync(d.radiance_fog, a->radiance_fog, n * 12, cudaMemcpyHostToDevice, st), "copy AOVs");
+    if (denoise) {
+        SR_CUDA(cudaMemcpyAsync(d.normals, a->normals, n * 12, cudaMemcpyHostToDevice, st), "copy AOVs");
+        SR_CUDA(cudaMemcpyAsync(d.depth, a->depth, n * 4, cudaMemcpyHostToDevice, st), "copy AOVs");
+        SR_CUDA(cudaMemcpyAsync(d.variance, a->variance, n * 4, cudaMemcpyHostToDevice, st), "copy AOVs");
+    } else {
+        SR_CUDA(cudaMemsetAsync(d.normals, 0, n * 20, st), "clear AOVs");
+    }
+    int rc = compose_impl(ctx, d, w, h, p, denoise, d_rgb, st);
+    if (rc) return rc;
+    SR_CUDA(cudaMemcpyAsync(rgb, d_rgb, n * 3, cudaMemcpyDeviceToHost, st), "copy pixels");
+    SR_CUDA(cudaStreamSynchronize(st), "compose");
+    return SR_OK;
+}
+
+SR_API int sr_compose(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p, uint8_t* rgb) {
+    return compose_host(ctx, a, w, h, p, rgb, true);
+}
+
+SR_API int sr_render_compose(SrScene* s, const SrView* view, const SrRenderParams* params, const SrComposeParams* cp,
+                             const SrAovs* host_out, uint8_t* host_rgb8) {
+    if (!s || !params || !cp) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    size_t n = (size_t)params->width * params->height;
+    DevAovs d;
+    uint8_t* d_rgb;
+    SR_CUDA(stage_aovs(s, n, d, &d_rgb), "alloc AOVs");
+    int rc = render_into(s, view, params, d, st);
+    if (rc) return rc;
+    rc = compose_impl(s->ctx, d, params->width, params->height, cp, true, d_rgb, st);
+    if (rc) return rc;
+    if (host_out) {
+        rc = copy_aovs_to_host(d, n, *host_out, st);
+        if (rc) return rc;
+    }
+    if (host_rgb8) SR_CUDA(cudaMemcpyAsync(host_rgb8, d_rgb, n * 3, cudaMemcpyDeviceToHost, st), "copy pixels");
+    SR_CUDA(cudaStreamSynchronize(st), "render_compose");
+    if (s->counting)
+        SR_CUDA(cudaMemcpy(s->last_counters, s->counters.ptr, sizeof(s->last_counters), cudaMemcpyDeviceToHost),
+                "read counters");
+    return check_device_error(s);
+}
+
+SR_API int sr_preview(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p, uint8_t* rgb) {
+    return compose_host(ctx, a, w, h, p, rgb, false);
+}
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// sr_kernels.h — host-callable launchers of the CUDA kernels (implemented in the .cu files).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sr_layout.h"
+
+namespace sr {
+
+struct DevAovs {
+    float* radiance;
+    float* radiance_fog;
+    float* normals;
+    float* uv;
+    float* depth;
+    uint32_t* samples;
+    float* variance;
+};
+
+// Path loop over every pixel (sr_render.cu).
+cudaError_t launch_render(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& out,
+                          unsigned long long* counters, uint32_t* err, cudaStream_t stream);
+
+// Closest hit per world ray (sr_render.cu).
+cudaError_t launch_trace(const DevScene& S, const float* rays, uint32_t n, int32_t* obj, int32_t* tri, float* dist,
+                         float* uv, uint32_t* err, cudaStream_t stream);
+
+// Denoise + fog blur + tonemap (sr_compose.cu).  `spatial` holds the (2r+1)^2 surface weights
+// dw-independent exp(-d^2/(2 r^2)) and `fog_spatial` the fog weights strength*exp(...), both
+// evaluated on the host.  `denoise` = false gives Compositor.Preview.
+struct ComposeConsts {
+    int32_t tonemapper;
+    float exposure;
+    float strength, strength_max, lum_boost;
+    float lum_limit_inv, normal_limit_inv, depth_limit_inv;
+    int32_t radius, fog_radius;
+};
+cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, const ComposeConsts& k,
+                           const float* spatial, const float* fog_spatial, bool denoise, uint8_t* rgb8,
+                           float4* scratch, cudaStream_t stream);
+
+}  // namespace sr

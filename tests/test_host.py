@@ -1,0 +1,102 @@
+"""Host-side logic of the product (CPU, host-only context): triangle ingest and the binned-SAH BVH
+builds must be bit-identical to the oracle's restatement of bvh.cs / mesh.cs / math.cs."""
+import numpy as np
+import pytest
+
+from sharpray_gb300 import Mesh, synth
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def _same_bvh(a, b):
+    return all(np.array_equal(_bits(x), _bits(y)) for x, y in zip(a, b))
+
+
+MESHES = {
+    "icosphere_s4": lambda: synth.displaced_icosphere(4, 0.1, seed=1),
+    "uv_sphere_40": lambda: synth.uv_sphere(40, 40, amplitude=0.2, seed=3),
+    "ground": lambda: synth.ground_quad(5.0, -1.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MESHES))
+@pytest.mark.parametrize("smooth", [True, False])
+def test_ingest_bit_exact(host_ctx, oracle_mod, name, smooth):
+    pos, uv = MESHES[name]()
+    ours = Mesh.triangles_from_corners(host_ctx, pos, uv, None, smooth)
+    ref = oracle_mod.triangles_from_corners(pos, uv, None, smooth)
+    assert np.array_equal(_bits(ours), _bits(ref))
+
+
+def test_ingest_with_normals_and_default_uvs(host_ctx, oracle_mod):
+    pos, _ = synth.uv_sphere(8, 8)
+    rng = np.random.default_rng(0)
+    n = rng.normal(size=pos.shape).astype(np.float32)
+    ours = Mesh.triangles_from_corners(host_ctx, pos, None, n, True)
+    ref = oracle_mod.triangles_from_corners(pos, None, n, True)
+    assert np.array_equal(_bits(ours), _bits(ref))
+
+
+@pytest.mark.parametrize("name", sorted(MESHES))
+def test_mesh_bvh_bit_exact(host_ctx, oracle_mod, name):
+    pos, uv = MESHES[name]()
+    tris = Mesh.triangles_from_corners(host_ctx, pos, uv)
+    ours = Mesh(host_ctx, tris).bvh()
+    s = oracle_mod.OracleScene()
+    ref = s.mesh_bvh(s.mesh(tris))
+    assert ours[0].shape == ref[0].shape
+    assert _same_bvh(ours, ref)
+    # structural invariants of bvh.cs: children consecutive, leaves cover every item once
+    bounds, links, items = ours
+    assert sorted(items.tolist()) == list(range(len(tris)))
+
+
+def test_degenerate_and_clustered_meshes(host_ctx, oracle_mod):
+    """Edge cases: duplicate triangles, zero-area triangles, a cluster of nearly coincident
+    centroids far from the origin (where the split position can round onto the minimum)."""
+    rng = np.random.default_rng(11)
+    base = rng.normal(size=(50, 3, 3)).astype(np.float32)
+    dup = np.repeat(base[:5], 4, axis=0)
+    flat = base[5:10].copy()
+    flat[:, 2] = flat[:, 0]  # zero area
+    cluster = (np.float32(1000.0) + rng.normal(scale=1e-4, size=(40, 3, 3))).astype(np.float32)
+    pos = np.concatenate([base, dup, flat, cluster]).astype(np.float32)
+    tris = Mesh.triangles_from_corners(host_ctx, pos, None, None, True)
+    assert np.array_equal(_bits(tris), _bits(oracle_mod.triangles_from_corners(pos, None, None, True)))
+    ours = Mesh(host_ctx, tris).bvh()
+    s = oracle_mod.OracleScene()
+    assert _same_bvh(ours, s.mesh_bvh(s.mesh(tris)))
+
+
+def test_empty_and_single_triangle_mesh(host_ctx, oracle_mod):
+    s = oracle_mod.OracleScene()
+    for n in (0, 1):
+        pos = np.zeros((n, 3, 3), np.float32)
+        if n:
+            pos[0] = [[0, 0, 0], [1, 0, 0], [0, 1, 0]]
+        tris = Mesh.triangles_from_corners(host_ctx, pos)
+        ours = Mesh(host_ctx, tris).bvh()
+        assert _same_bvh(ours, s.mesh_bvh(s.mesh(tris)))
+        assert ours[0].shape[0] == n
+
+
+def test_scene_bvh_bit_exact(host_ctx, oracle_mod):
+    d = synth.config_features()
+    ours = d.instantiate(host_ctx)
+    ours.build()
+    ref = oracle_mod.instantiate(d)
+    assert _same_bvh(ours.bvh(), ref.bvh())
+    for i in range(len(d.meshes)):
+        assert _same_bvh(ours._keepalive[1][i].bvh(), ref.mesh_bvh(i))
+
+
+def test_c2_scene_bvh_reduced(host_ctx, oracle_mod):
+    """The 65-object C2 layout (meshes reduced so the check stays fast): the 32-bin scene BVH over
+    rotated/scaled instance bounds is bit-identical."""
+    d = synth.config_c2(64, 36, 1, rings=40, rock_rings=10, env=(64, 32))
+    ours = d.instantiate(host_ctx)
+    ours.build()
+    ref = oracle_mod.instantiate(d)
+    assert _same_bvh(ours.bvh(), ref.bvh())
