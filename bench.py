@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the oracle sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--mode", type=int, default=0, help="render mode: 0 auto, 1 megakernel, 2 wavefront, 3 graph")
+    ap.add_argument("--variants", action="store_true", help="also time every render mode once")
     return ap.parse_args()
 
 
@@ -222,8 +224,10 @@ def run_ours(args):
     rgb = torch.empty(n * 3, dtype=torch.uint8, device="cuda")
     aovs = _abi.SrAovs(*[dev[k].data_ptr() for k in ("radiance", "radiance_fog", "normals", "uv", "depth",
                                                       "samples", "variance")])
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sp = C.c_void_p(stream.cuda_stream)
+    scene.set_render_mode(args.mode)
 
     def render():
         _abi.check(lib.sr_render_device(scene.handle, C.byref(view), C.byref(params), C.byref(aovs), sp))
@@ -271,6 +275,21 @@ def run_ours(args):
         total_s = float(t.item())
     value = samples_per_step * args.steps * world / total_s
 
+    variants = None
+    if args.variants:
+        variants = {}
+        for mode, label in ((1, "megakernel"), (2, "wavefront_host_loop"), (3, "wavefront_graph")):
+            scene.set_render_mode(mode)
+            render()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            render()
+            b.record(stream)
+            torch.cuda.synchronize()
+            variants[label] = samples_per_step / (a.elapsed_time(b) / 1000.0)
+        scene.set_render_mode(args.mode)
+
     # end to end through the public API with pinned host outputs
     host = Aovs(W, H)
     pinned = {}
@@ -297,6 +316,9 @@ def run_ours(args):
     e2e_value = samples_per_step * e2e_steps * world / e2e_s
     d2h = n * (12 + 12 + 12 + 8 + 4 + 4 + 4) + n * 3
 
+    # kernels of one timed step: the render's own launches (reported by the library) + compose (2)
+    info = scene.render_info()
+    launches = (info["kernel_launches"] + 2) * args.steps
     peak, peak_kind = measured_peaks()
     alg = algorithmic_bytes(counters, n)
     kern_s = statistics.mean(render_ms) / 1000.0
@@ -335,9 +357,13 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": traffic, "kernel": "k_render_pixels",
                          "kernel_ms": 1000 * kern_s, "alg_bytes_per_launch": alg, "peak_source": peak_kind},
             "cpu_baseline": cpu,
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": launches,
+            "render_mode": {0: "auto (wavefront graph)", 1: "megakernel", 2: "wavefront host loop",
+                            3: "wavefront graph"}[args.mode],
+            "variants_samples_per_s": variants,
             "clocks": clocks.summary(),
             "counters_per_step": counters,
+            "bounce_iterations": info["bounce_iterations"],
         }
         print(json.dumps(out), flush=True)
     if world > 1:

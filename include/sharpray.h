@@ -168,7 +168,8 @@ enum {
     SR_COUNTER_BLAS_SHAPE,        /* triangle tests                     (bvh.cs:203)     */
     SR_COUNTER_HIT_INFLATE,       /* closest hits inflated              (mesh.cs:57)     */
     SR_COUNTER_TEX_SAMPLE,        /* Texture.Sample calls               (texture.cs:39)  */
-    SR_COUNTER_CDF_PROBE,         /* Cdf1 binary-search probes          (cdf.cs:40-52)   */
+    SR_COUNTER_CDF_PROBE,         /* Cdf1 search probes performed       (cdf.cs:40-52)   */
+    SR_COUNTER_LIGHT_SAMPLE,      /* sky-texture light samples (Cdf2)   (scene.cs:408)   */
     SR_COUNTER_COUNT
 };
 
@@ -258,6 +259,16 @@ SR_API int sr_render_device(SrScene* scene, const SrView* view, const SrRenderPa
  * NULL).  Replaces `new Renderer(...)`, the Tick() loop and Compositor.Compose. */
 SR_API int sr_render_compose(SrScene* scene, const SrView* view, const SrRenderParams* params,
                              const SrComposeParams* compose, const SrAovs* host_aovs, uint8_t* host_rgb8);
+/* Render implementation used by this scene's renders (no reference counterpart; all produce the
+ * same image): SR_RENDER_MEGAKERNEL = one thread per pixel running the whole sample loop;
+ * SR_RENDER_WAVEFRONT = per-bounce extend/shade/resolve kernels driven by a host loop;
+ * SR_RENDER_WAVEFRONT_GRAPH = the same kernels repeated on the device by a CUDA-graph
+ * conditional loop (no host round trip per bounce).  SR_RENDER_AUTO picks the fastest (graph). */
+enum { SR_RENDER_AUTO = 0, SR_RENDER_MEGAKERNEL = 1, SR_RENDER_WAVEFRONT = 2, SR_RENDER_WAVEFRONT_GRAPH = 3 };
+SR_API int sr_scene_set_render_mode(SrScene* scene, int32_t mode);
+/* Kernel launches and wavefront bounce iterations of the last completed render on this scene
+ * (synchronises with it).  No reference counterpart. */
+SR_API int sr_scene_render_info(SrScene* scene, uint32_t* kernel_launches, uint32_t* bounce_iterations);
 /* Reads the work counters of the last render on this scene (device counting is enabled by
  * sr_scene_set_counting); counters_out has SR_COUNTER_COUNT entries. */
 SR_API int sr_scene_set_counting(SrScene* scene, int32_t enabled);

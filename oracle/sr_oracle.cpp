@@ -895,6 +895,7 @@ struct Sky {
     std::optional<SampleLight> light_dir_rand(Rng& rng, Counters* ctr) const {
         if (kind == 0) {
             if (cdf.marginal.total <= 0.0f) return std::nullopt;
+            if (ctr) ctr->add(SR_COUNTER_LIGHT_SAMPLE);
             V2 c = rand_v2(rng);
             int y = (int)cdf.marginal.sample(c.y, ctr);
             int x = (int)cdf.conditionals[y].sample(c.x, ctr);

@@ -24,12 +24,17 @@ SR_SHAPE_MESH = 0
 SR_SHAPE_SPHERE = 1
 SR_SHAPE_AABOX = 2
 
+SR_RENDER_AUTO = 0
+SR_RENDER_MEGAKERNEL = 1
+SR_RENDER_WAVEFRONT = 2
+SR_RENDER_WAVEFRONT_GRAPH = 3
+
 SR_TONEMAP_REINHARD = 0
 SR_TONEMAP_LINEAR_SMOOTH = 1
 
 COUNTER_NAMES = [
     "sample", "sample_bounce", "scene_trace", "scene_occlude", "tlas_node", "tlas_shape", "blas_node",
-    "blas_shape", "hit_inflate", "tex_sample", "cdf_probe",
+    "blas_shape", "hit_inflate", "tex_sample", "cdf_probe", "light_sample",
 ]
 SR_COUNTER_COUNT = len(COUNTER_NAMES)
 
@@ -125,6 +130,8 @@ PROTOTYPES = {
     "sr_render_device": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P]),
     "sr_render_compose": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrComposeParams),
                                C.POINTER(SrAovs), _P]),
+    "sr_scene_set_render_mode": (_I, [_P, C.c_int32]),
+    "sr_scene_render_info": (_I, [_P, C.POINTER(_U), C.POINTER(_U)]),
     "sr_scene_set_counting": (_I, [_P, C.c_int32]),
     "sr_scene_counters": (_I, [_P, _P]),
     "sr_compose": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P]),

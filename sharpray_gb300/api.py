@@ -385,6 +385,16 @@ class Scene:
         check(self._lib.sr_scene_trace(self.handle, ptr(r), n, ptr(obj), ptr(tri), ptr(dist), ptr(uv)))
         return {"object": obj, "triangle": tri, "dist": dist, "uv": uv}
 
+    def set_render_mode(self, mode: int) -> None:
+        """0 auto, 1 megakernel, 2 wavefront (host loop), 3 wavefront (device graph loop)."""
+        check(self._lib.sr_scene_set_render_mode(self.handle, int(mode)))
+
+    def render_info(self) -> dict:
+        """Kernel launches and wavefront bounce iterations of the last render."""
+        k, b = C.c_uint32(), C.c_uint32()
+        check(self._lib.sr_scene_render_info(self.handle, C.byref(k), C.byref(b)))
+        return {"kernel_launches": k.value, "bounce_iterations": b.value}
+
     def set_counting(self, enabled: bool) -> None:
         check(self._lib.sr_scene_set_counting(self.handle, int(enabled)))
 

@@ -229,128 +229,6 @@ constexpr uint32_t kMaxPops = 1u << 24;
 
 SR_DEV float4 ldg4(const float4* p) { return __ldg(p); }
 
-// Bvh<TriangleLean>.Intersect (bvh.cs:165-216) over one mesh BVH in the object's local space.
-// Returns the accepted triangle position (index into the reordered triangle array) or -1.
-template <bool COUNT>
-SR_DEV int blas_closest(const DevScene& S, int root, const Ray& r, float& t_best, float& u_best, float& v_best,
-                        Ctr& c, uint32_t* err) {
-    if (root < 0) return -1;  // empty mesh: Bvh.Intersect returns null
-    StackEntry stack[kStackSize];
-    uint32_t pops = 0;
-    float4 rn1 = ldg4(S.nodes + 2 * root + 1);
-    float4 rn0 = ldg4(S.nodes + 2 * root);
-    int sp = 0;
-    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
-    float best = __int_as_float(0x7f800000);
-    int best_pos = -1;
-    while (sp > 0) {
-        StackEntry e = stack[--sp];
-        if (++pops > kMaxPops) {
-            atomicOr(err, SR_DEVERR_LOOP);
-            break;
-        }
-        if (e.t >= best) continue;
-        if (e.count == 0) {
-            SR_COUNT(c, SR_COUNTER_BLAS_NODE, 2);
-            const float4* n = S.nodes + 2 * e.child;
-            float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
-            float ta = 0.f, tb = 0.f;
-            bool pa = slab(a0, a1, r, ta) && ta <= best;
-            bool pb = slab(b0, b1, r, tb) && tb <= best;
-            if (sp + 2 > kStackSize) {
-                atomicOr(err, SR_DEVERR_STACK);
-                return -1;
-            }
-            StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
-            StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
-            if (pa && pb) {
-                if (ta < tb) {
-                    stack[sp++] = eb;
-                    stack[sp++] = ea;
-                } else {
-                    stack[sp++] = ea;
-                    stack[sp++] = eb;
-                }
-            } else if (pa) {
-                stack[sp++] = ea;
-            } else if (pb) {
-                stack[sp++] = eb;
-            }
-        } else {
-            SR_COUNT(c, SR_COUNTER_BLAS_SHAPE, (uint32_t)e.count);
-            for (int i = 0; i < e.count; ++i) {
-                const float4* tp = S.tris + 3 * (e.child + i);
-                float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
-                float t, u, v;
-                if (tri_hit(v3(q0), v3(q1), v3(q2), r, t, u, v) && t < best) {
-                    best = t;
-                    best_pos = e.child + i;
-                    u_best = u;
-                    v_best = v;
-                }
-            }
-        }
-    }
-    t_best = best;
-    return best_pos;
-}
-
-// Any-hit over one mesh BVH: true iff the closest-hit traversal above would return a hit.
-// Visiting order and node predicate are the reference's; only the search stops at the first hit.
-template <bool COUNT>
-SR_DEV bool blas_any(const DevScene& S, int root, const Ray& r, Ctr& c, uint32_t* err) {
-    if (root < 0) return false;
-    StackEntry stack[kStackSize];
-    uint32_t pops = 0;
-    float4 rn0 = ldg4(S.nodes + 2 * root);
-    float4 rn1 = ldg4(S.nodes + 2 * root + 1);
-    int sp = 0;
-    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
-    while (sp > 0) {
-        StackEntry e = stack[--sp];
-        if (++pops > kMaxPops) {
-            atomicOr(err, SR_DEVERR_LOOP);
-            break;
-        }
-        if (e.count == 0) {
-            SR_COUNT(c, SR_COUNTER_BLAS_NODE, 2);
-            const float4* n = S.nodes + 2 * e.child;
-            float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
-            float ta = 0.f, tb = 0.f;
-            bool pa = slab(a0, a1, r, ta);
-            bool pb = slab(b0, b1, r, tb);
-            if (sp + 2 > kStackSize) {
-                atomicOr(err, SR_DEVERR_STACK);
-                return false;
-            }
-            StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
-            StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
-            if (pa && pb) {
-                if (ta < tb) {
-                    stack[sp++] = eb;
-                    stack[sp++] = ea;
-                } else {
-                    stack[sp++] = ea;
-                    stack[sp++] = eb;
-                }
-            } else if (pa) {
-                stack[sp++] = ea;
-            } else if (pb) {
-                stack[sp++] = eb;
-            }
-        } else {
-            SR_COUNT(c, SR_COUNTER_BLAS_SHAPE, (uint32_t)e.count);
-            for (int i = 0; i < e.count; ++i) {
-                const float4* tp = S.tris + 3 * (e.child + i);
-                float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
-                float t, u, v;
-                if (tri_hit(v3(q0), v3(q1), v3(q2), r, t, u, v)) return true;
-            }
-        }
-    }
-    return false;
-}
-
 // ---- shape hits ---------------------------------------------------------------------------------
 struct ShapeHit {
     float dist;
@@ -475,40 +353,120 @@ struct Hit {
     float u, v;  // barycentrics (meshes)
 };
 
-// Scene.Trace's Bvh<Object>.Intersect (bvh.cs:165-216) with Object.Intersect at the leaves
-// (ShapeExtensions.Intersect math.cs:67-79).  Each object is intersected with an unpruned local
-// search exactly as the reference does; only the inflation of the winning hit is deferred.
-template <bool COUNT>
-SR_DEV Hit scene_closest(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err) {
-    Hit best{-1, -1, __int_as_float(0x7f800000), 0.f, 0.f, 0.f};
+// Scene-level closest hit (ANY = false) or occlusion test (ANY = true) as ONE loop over a shared
+// stack.  The reference nests two traversals: Bvh<Object>.Intersect (bvh.cs:165-216) calls, for each
+// object of a scene-BVH leaf, Object.Intersect (math.cs:67-79) which runs a complete, unpruned mesh
+// BVH traversal in the object's local space.  Here the mesh traversal of the current object pushes
+// its entries above the scene entries (above `blas_base`); the loop swaps the traversal ray and the
+// pruning distance when it enters and leaves an object, so every iteration is one node-pair test or
+// one leaf, whichever level a lane is in, and lanes of a warp stay in the same loop.  Visit order,
+// pruning (`t >= best`, `t <= best`), tie-breaking (first strictly closer hit) and the per-object
+// comparison `hit.Dist / localRayScale < bestDist` are the reference's, so results are bit-exact.
+// With ANY the search stops at the first hit found and prunes nothing, which gives the same yes/no
+// answer as the closest-hit query.
+constexpr int kSceneStack = 192;  // scene (<= 65) + mesh (<= 65) entries, with margin
+
+template <bool COUNT, bool ANY>
+SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* err) {
+    const float inf = __int_as_float(0x7f800000);
+    Hit best{-1, -1, inf, 0.f, 0.f, 0.f};
     if (S.tlas_root < 0) return best;
-    StackEntry stack[kStackSize];
+    StackEntry stack[kSceneStack];
+    {
+        float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
+        float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
+        stack[0] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+    }
+    int sp = 1;
+    // current traversal ray (world or the current object's local ray) and pruning distance
+    V3 ro = wr.o, rinv = wr.inv;
+    float cur_best = inf;
+    bool in_mesh = false;
+    int mesh_base = 0;
+    int leaf_next = 0, leaf_left = 0;  // objects of the current scene leaf still to test
+    Ray lr = wr;                       // local ray of the current object
+    float lscale = 1.0f;
+    int obj_pos = -1;
+    int ob_tri = -1;
+    float ob_u = 0.f, ob_v = 0.f;
     uint32_t pops = 0;
-    float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
-    float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
-    int sp = 0;
-    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
-    while (sp > 0) {
-        StackEntry e = stack[--sp];
+    for (;;) {
         if (++pops > kMaxPops) {
             atomicOr(err, SR_DEVERR_LOOP);
             break;
         }
-        if (e.t >= best.dist) continue;
+        if (in_mesh && sp == mesh_base) {
+            // the object's mesh traversal is complete: Bvh<Object> leaf comparison (bvh.cs:207)
+            if (ob_tri >= 0) {
+                float d = cur_best / lscale;
+                if (d < best.dist) best = {obj_pos, ob_tri, d, cur_best, ob_u, ob_v};
+            }
+            in_mesh = false;
+            ro = wr.o;
+            rinv = wr.inv;
+            cur_best = ANY ? inf : best.dist;
+        }
+        if (!in_mesh && leaf_left > 0) {
+            const DevObject& o = S.objects[leaf_next];
+            obj_pos = leaf_next;
+            ++leaf_next;
+            --leaf_left;
+            Ray l = to_local(o, wr, lscale);
+            int kind = __float_as_int(o.pos_kind.w);
+            if (kind == SR_SHAPE_MESH) {
+                int root = __float_as_int(o.scale_root.w);
+                if (root < 0) continue;  // empty mesh never hits
+                float4 rn0 = ldg4(S.nodes + 2 * root);
+                float4 rn1 = ldg4(S.nodes + 2 * root + 1);
+                if (sp >= kSceneStack) {
+                    atomicOr(err, SR_DEVERR_STACK);
+                    break;
+                }
+                mesh_base = sp;
+                stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+                in_mesh = true;
+                lr = l;
+                ro = l.o;
+                rinv = l.inv;
+                cur_best = inf;
+                ob_tri = -1;
+            } else {
+                ShapeHit h;
+                bool ok = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, l, h, false)
+                                                  : box_hit(o.shape0, o.shape1, l, h, false);
+                if (ok) {
+                    if (ANY) return {obj_pos, -1, 0.f, 0.f, 0.f, 0.f};
+                    float d = h.dist / lscale;
+                    if (d < best.dist) best = {obj_pos, -1, d, 0.f, 0.f, 0.f};
+                    cur_best = best.dist;
+                }
+            }
+            continue;
+        }
+        if (sp == 0) break;
+        StackEntry e = stack[--sp];
+        if (!ANY && e.t >= cur_best) continue;
         if (e.count == 0) {
-            SR_COUNT(c, SR_COUNTER_TLAS_NODE, 2);
+            if (in_mesh)
+                SR_COUNT(c, SR_COUNTER_BLAS_NODE, 2);
+            else
+                SR_COUNT(c, SR_COUNTER_TLAS_NODE, 2);
             const float4* n = S.nodes + 2 * e.child;
             float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
+            Ray rr;
+            rr.o = ro;
+            rr.inv = rinv;
             float ta = 0.f, tb = 0.f;
-            bool pa = slab(a0, a1, r, ta) && ta <= best.dist;
-            bool pb = slab(b0, b1, r, tb) && tb <= best.dist;
-            if (sp + 2 > kStackSize) {
+            bool pa = slab(a0, a1, rr, ta) && (ANY || ta <= cur_best);
+            bool pb = slab(b0, b1, rr, tb) && (ANY || tb <= cur_best);
+            if (sp + 2 > kSceneStack) {
                 atomicOr(err, SR_DEVERR_STACK);
-                return best;
+                break;
             }
             StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
             StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
             if (pa && pb) {
+                // the nearer child is popped first; on a tie the second child is (bvh.cs:196-197)
                 if (ta < tb) {
                     stack[sp++] = eb;
                     stack[sp++] = ea;
@@ -521,97 +479,37 @@ SR_DEV Hit scene_closest(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err)
             } else if (pb) {
                 stack[sp++] = eb;
             }
-        } else {
-            SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
+        } else if (in_mesh) {
+            SR_COUNT(c, SR_COUNTER_BLAS_SHAPE, (uint32_t)e.count);
             for (int i = 0; i < e.count; ++i) {
-                const DevObject& o = S.objects[e.child + i];
-                float scale;
-                Ray lr = to_local(o, r, scale);
-                int kind = __float_as_int(o.pos_kind.w);
-                if (kind == SR_SHAPE_MESH) {
-                    float t, u, v;
-                    int pos = blas_closest<COUNT>(S, __float_as_int(o.scale_root.w), lr, t, u, v, c, err);
-                    if (pos >= 0) {
-                        float d = t / scale;
-                        if (d < best.dist) best = {e.child + i, pos, d, t, u, v};
-                    }
-                } else {
-                    ShapeHit h;
-                    bool ok = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, lr, h, false)
-                                                      : box_hit(o.shape0, o.shape1, lr, h, false);
-                    if (ok) {
-                        float d = h.dist / scale;
-                        if (d < best.dist) best = {e.child + i, -1, d, 0.f, 0.f, 0.f};
-                    }
+                const float4* tp = S.tris + 3 * (e.child + i);
+                float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
+                float t, u, v;
+                if (tri_hit(v3(q0), v3(q1), v3(q2), lr, t, u, v) && (ANY || t < cur_best)) {
+                    if (ANY) return {obj_pos, e.child + i, 0.f, 0.f, 0.f, 0.f};
+                    cur_best = t;
+                    ob_tri = e.child + i;
+                    ob_u = u;
+                    ob_v = v;
                 }
             }
+        } else {
+            SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
+            leaf_next = e.child;
+            leaf_left = e.count;
         }
     }
     return best;
 }
 
-// Occlusion test for all-opaque scenes: true iff scene_closest would report a hit.
+template <bool COUNT>
+SR_DEV Hit scene_closest(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err) {
+    return scene_traverse<COUNT, false>(S, r, c, err);
+}
+
 template <bool COUNT>
 SR_DEV bool scene_any(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err) {
-    if (S.tlas_root < 0) return false;
-    StackEntry stack[kStackSize];
-    uint32_t pops = 0;
-    float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
-    float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
-    int sp = 0;
-    stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
-    while (sp > 0) {
-        StackEntry e = stack[--sp];
-        if (++pops > kMaxPops) {
-            atomicOr(err, SR_DEVERR_LOOP);
-            break;
-        }
-        if (e.count == 0) {
-            SR_COUNT(c, SR_COUNTER_TLAS_NODE, 2);
-            const float4* n = S.nodes + 2 * e.child;
-            float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
-            float ta = 0.f, tb = 0.f;
-            bool pa = slab(a0, a1, r, ta);
-            bool pb = slab(b0, b1, r, tb);
-            if (sp + 2 > kStackSize) {
-                atomicOr(err, SR_DEVERR_STACK);
-                return false;
-            }
-            StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
-            StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
-            if (pa && pb) {
-                if (ta < tb) {
-                    stack[sp++] = eb;
-                    stack[sp++] = ea;
-                } else {
-                    stack[sp++] = ea;
-                    stack[sp++] = eb;
-                }
-            } else if (pa) {
-                stack[sp++] = ea;
-            } else if (pb) {
-                stack[sp++] = eb;
-            }
-        } else {
-            SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
-            for (int i = 0; i < e.count; ++i) {
-                const DevObject& o = S.objects[e.child + i];
-                float scale;
-                Ray lr = to_local(o, r, scale);
-                int kind = __float_as_int(o.pos_kind.w);
-                bool hit;
-                if (kind == SR_SHAPE_MESH) {
-                    hit = blas_any<COUNT>(S, __float_as_int(o.scale_root.w), lr, c, err);
-                } else {
-                    ShapeHit h;
-                    hit = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, lr, h, false)
-                                                  : box_hit(o.shape0, o.shape1, lr, h, false);
-                }
-                if (hit) return true;
-            }
-        }
-    }
-    return false;
+    return scene_traverse<COUNT, true>(S, r, c, err).obj >= 0;
 }
 
 // The world-space ShapeHit of a scene hit (ShapeExtensions.Intersect math.cs:67-79).
@@ -718,10 +616,16 @@ SR_DEV float sky_light_pdf(const DevScene& S, V3 dir) {
     return blend / k.sun_pdf_denom;
 }
 
-// Cdf1.Sample cdf.cs:37-55 over cdf[0..n].
+// Cdf1.Sample cdf.cs:37-55 over cdf[0..n], accelerated by a bucket guide.  The reference's loop is
+// a lower bound over the non-decreasing cdf[1..n] (prefix sums of non-negative weights divided by
+// their total), i.e. r(u) = #{j : cdf[j+1] <= u}, clamped to n-1.  guide[k] holds r() at the
+// smallest float u that falls into bucket k = (int)(u * n), so for any u in bucket k the answer
+// lies in [guide[k], guide[k+1]]; bisecting that range with the same predicate returns exactly
+// the reference's index while touching ~1-2 cdf entries instead of ~log2(n).
 template <bool COUNT>
-SR_DEV uint32_t cdf_sample(const float* cdf, uint32_t n, float norm, Ctr& c) {
-    uint32_t lo = 0, hi = n;
+SR_DEV uint32_t cdf_sample(const float* cdf, const uint32_t* guide, uint32_t n, float norm, Ctr& c) {
+    uint32_t k = min((uint32_t)(int)(norm * (float)n), n - 1);
+    uint32_t lo = __ldg(guide + k), hi = __ldg(guide + k + 1);
     while (lo < hi) {
         SR_COUNT(c, SR_COUNTER_CDF_PROBE, 1);
         uint32_t mid = (lo + hi) >> 1;
@@ -741,8 +645,10 @@ SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr
         if (k.cdf_total <= 0.0f) return false;
         V2 u = rand_v2(rng);
         const DevTexture& t = S.textures[k.texture];
-        uint32_t y = cdf_sample<COUNT>(k.cdf_marginal, t.height, u.y, c);
-        uint32_t x = cdf_sample<COUNT>(k.cdf_cond + (size_t)y * (t.width + 1), t.width, u.x, c);
+        SR_COUNT(c, SR_COUNTER_LIGHT_SAMPLE, 1);
+        uint32_t y = cdf_sample<COUNT>(k.cdf_marginal, k.guide_marginal, t.height, u.y, c);
+        size_t row = (size_t)y * (t.width + 1);
+        uint32_t x = cdf_sample<COUNT>(k.cdf_cond + row, k.guide_cond + row, t.width, u.x, c);
         V2 uv{((float)(int)x + 0.5f) / (float)(int)t.width, ((float)(int)y + 0.5f) / (float)(int)t.height};
         dir = quat_rotate(k.rot, from_equirect_uv(uv));
         pdf = luminance(col3(ldg4(S.texels + t.offset + (size_t)y * t.width + x))) * k.pdf_scale;

@@ -14,6 +14,7 @@
 #include "sr_bvh.h"
 #include "sr_kernels.h"
 #include "sr_layout.h"
+#include "sr_wavefront.h"
 
 using namespace sr;
 using namespace sr::host;
@@ -125,12 +126,29 @@ struct SrScene {
     BvhHost tlas;
     // device state
     DevScene dev{};
-    DevBuf nodes, tris, attrs, objs, mats, texs, texels, cdf_marginal, cdf_cond;
+    DevBuf nodes, tris, attrs, objs, mats, texs, texels, cdf_marginal, cdf_cond, guide_marginal, guide_cond;
     DevBuf err, counters;
     DevBuf aovs;  // staging for sr_render
     DevBuf rays_io;
     bool counting = false;
     uint64_t last_counters[SR_COUNTER_COUNT] = {};
+    // wavefront renderer state
+    int32_t render_mode = SR_RENDER_AUTO;
+    DevBuf wave;
+    uint32_t wave_slots = 0;
+    WaveState ws{};
+    cudaStream_t capture_stream = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    WaveLaunch graph_launch{};  // launch parameters baked into graph_exec
+    uint32_t* counts_host = nullptr;  // pinned
+    int sms = 0;
+    int last_mode = 0;                // render mode of the last render
+    uint32_t last_host_iters = 0;     // bounces run by the host loop
+    ~SrScene() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+        if (counts_host) cudaFreeHost(counts_host);
+    }
 };
 
 namespace {
@@ -197,6 +215,33 @@ int32_t append_tree(std::vector<float4>& slots, const BvhHost& b, int32_t leaf_b
         slots.push_back(mk4(n.bounds.hi.x, n.bounds.hi.y, n.bounds.hi.z, ibits(n.count)));
     }
     return b.node_count > 0 ? base + 1 : -1;
+}
+
+// Reference search (Cdf1.Sample cdf.cs:37-55) without the final clamp: #{j : cdf[j+1] <= u}.
+uint32_t cdf_lower_bound(const float* cdf, uint32_t n, float u) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (cdf[mid + 1] <= u)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+// Bucket guide of one Cdf1 for the device search: guide[k] = lower bound at the smallest float u
+// with (int)(u * n) >= k; guide[n] = n.
+void build_guide(const float* cdf, uint32_t n, uint32_t* guide) {
+    const float fn = (float)n;
+    guide[0] = cdf_lower_bound(cdf, n, 0.0f);
+    for (uint32_t k = 1; k < n; ++k) {
+        float f = (float)((double)k / (double)n);
+        while (f > 0.0f && (int)(f * fn) >= (int)k) f = std::nextafter(f, 0.0f);
+        while ((int)(f * fn) < (int)k) f = std::nextafter(f, 2.0f);
+        guide[k] = cdf_lower_bound(cdf, n, f);
+    }
+    guide[n] = n;
 }
 
 bool valid_texture(SrContext* ctx, int32_t id) { return id == -1 || (id >= 0 && id < (int32_t)ctx->textures.size()); }
@@ -460,6 +505,7 @@ SR_API int sr_scene_build(SrScene* s) {
     std::memset(&sky, 0, sizeof(sky));
     sky.kind = s->sky_kind;
     std::vector<float> marginal, cond;
+    std::vector<uint32_t> gmarginal, gcond;
     const float pi = 3.14159265358979323846f;
     if (s->sky_kind == 0) {
         const TextureHost& t = *ctx->textures[s->sky_texture];
@@ -481,6 +527,10 @@ SR_API int sr_scene_build(SrScene* s) {
         float total = marginal[h];
         if (total > 0.0f)
             for (uint32_t y = 1; y <= h; ++y) marginal[y] /= total;
+        gmarginal.resize(h + 1);
+        build_guide(marginal.data(), h, gmarginal.data());
+        gcond.resize((size_t)h * (w + 1));
+        for (uint32_t y = 0; y < h; ++y) build_guide(&cond[(size_t)y * (w + 1)], w, &gcond[(size_t)y * (w + 1)]);
         sky.texture = s->sky_texture;
         sky.multiplier = s->sky_multiplier;
         sky.cdf_total = total;
@@ -537,6 +587,8 @@ SR_API int sr_scene_build(SrScene* s) {
     SR_CUDA(upload(s->texels, texels.data(), texels.size() * sizeof(float4), st), "upload texels");
     SR_CUDA(upload(s->cdf_marginal, marginal.data(), marginal.size() * sizeof(float), st), "upload cdf");
     SR_CUDA(upload(s->cdf_cond, cond.data(), cond.size() * sizeof(float), st), "upload cdf");
+    SR_CUDA(upload(s->guide_marginal, gmarginal.data(), gmarginal.size() * sizeof(uint32_t), st), "upload cdf guide");
+    SR_CUDA(upload(s->guide_cond, gcond.data(), gcond.size() * sizeof(uint32_t), st), "upload cdf guide");
     SR_CUDA(s->err.reserve(sizeof(uint32_t)), "alloc error word");
     SR_CUDA(cudaMemsetAsync(s->err.ptr, 0, sizeof(uint32_t), st), "clear error word");
     SR_CUDA(s->counters.reserve(SR_COUNTER_COUNT * sizeof(unsigned long long)), "alloc counters");
@@ -544,6 +596,8 @@ SR_API int sr_scene_build(SrScene* s) {
 
     sky.cdf_marginal = s->cdf_marginal.as<float>();
     sky.cdf_cond = s->cdf_cond.as<float>();
+    sky.guide_marginal = s->guide_marginal.as<uint32_t>();
+    sky.guide_cond = s->guide_cond.as<uint32_t>();
     DevScene& d = s->dev;
     std::memset(&d, 0, sizeof(d));
     d.nodes = s->nodes.as<float4>();
@@ -661,6 +715,109 @@ static int make_view(const SrView* v, const SrRenderParams* p, DevView& dv, DevP
 static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t h, const SrComposeParams* p,
                         bool denoise, uint8_t* rgb8, cudaStream_t st);
 
+// Allocates the wavefront path state for `slots` pixel slots (one block, carved into the arrays).
+static int wave_reserve(SrScene* s, uint32_t slots) {
+    if (s->wave_slots >= slots && s->wave.ptr) return SR_OK;
+    const size_t n = slots;
+    // 16-byte planes: rng, ray_o, ray_d, rad, fog, energy, medium, prim, acc0..5, hit, sh0..3 (21)
+    // 8-byte planes: prim_uv, hit_uv; 4-byte planes: rng_c, q_active x2, q_resolve; + 4 counters
+    size_t bytes = n * (21 * 16 + 2 * 8 + 4 * 4) + 256;
+    SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
+    char* p = s->wave.as<char>();
+    auto take = [&](size_t elem) {
+        char* r = p;
+        p += n * elem;
+        return r;
+    };
+    WaveState& w = s->ws;
+    w.rng = (uint4*)take(16);
+    w.ray_o = (float4*)take(16);
+    w.ray_d = (float4*)take(16);
+    w.rad = (float4*)take(16);
+    w.fog = (float4*)take(16);
+    w.energy = (float4*)take(16);
+    w.medium = (float4*)take(16);
+    w.prim = (float4*)take(16);
+    w.acc0 = (float4*)take(16);
+    w.acc1 = (float4*)take(16);
+    w.acc2 = (float4*)take(16);
+    w.acc3 = (float4*)take(16);
+    w.acc4 = (float4*)take(16);
+    w.acc5 = (float4*)take(16);
+    w.hit = (float4*)take(16);
+    w.sh0 = (float4*)take(16);
+    w.sh1 = (float4*)take(16);
+    w.sh2 = (float4*)take(16);
+    w.sh3 = (float4*)take(16);
+    take(16);  // spare plane keeps the 8-byte planes aligned
+    take(16);
+    w.prim_uv = (float2*)take(8);
+    w.hit_uv = (float2*)take(8);
+    w.rng_c = (uint32_t*)take(4);
+    w.q_active[0] = (uint32_t*)take(4);
+    w.q_active[1] = (uint32_t*)take(4);
+    w.q_resolve = (uint32_t*)take(4);
+    w.counts = (uint32_t*)p;
+    s->wave_slots = slots;
+    // request flags start clear; resolve clears them after use
+    SR_CUDA(cudaMemset(w.sh0, 0, n * 16), "clear wavefront state");
+    return SR_OK;
+}
+
+static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& out,
+                            unsigned long long* ctr, cudaStream_t st, bool graph) {
+    uint32_t tiles_x = (dp.width + 7) / 8, tiles_y = (dp.height + 3) / 4;
+    uint32_t slots = tiles_x * tiles_y * 32;
+    int rc = wave_reserve(s, slots);
+    if (rc) return rc;
+    s->ws.slots = slots;
+    s->ws.tiles_x = tiles_x;
+    if (!s->sms) {
+        SR_CUDA(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->ctx->device), "device query");
+    }
+    WaveLaunch L;
+    std::memset(&L, 0, sizeof(L));  // padding bytes take part in the graph-reuse comparison
+    L.W = s->ws;
+    L.S = s->dev;
+    L.V = dv;
+    L.P = dp;
+    L.out = out;
+    L.err = s->err.as<uint32_t>();
+    L.counters = ctr;
+    wave_grid_sizes(L, s->sms);
+    uint64_t cap = (uint64_t)dp.max_samples * (dp.bounces + 1) + 4;
+    L.max_iters = (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap);
+    SR_CUDA(wave_init(L, st), "wavefront init");
+    if (graph) {
+        if (!s->capture_stream) SR_CUDA(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking), "stream");
+        if (s->graph_exec && std::memcmp(&s->graph_launch, &L, sizeof(L)) != 0) {
+            SR_CUDA(cudaStreamSynchronize(st), "sync before graph rebuild");
+            cudaGraphExecDestroy(s->graph_exec);
+            s->graph_exec = nullptr;
+        }
+        if (!s->graph_exec) {
+            SR_CUDA(wave_build_graph(L, s->capture_stream, &s->graph_exec), "build bounce-loop graph");
+            std::memcpy(&s->graph_launch, &L, sizeof(L));
+        }
+        SR_CUDA(cudaGraphLaunch(s->graph_exec, st), "launch bounce-loop graph");
+        return SR_OK;
+    }
+    if (!s->counts_host) SR_CUDA(cudaMallocHost(&s->counts_host, 4 * sizeof(uint32_t)), "pinned alloc");
+    for (uint32_t it = 0;; ++it) {
+        if (it >= L.max_iters) return fail(SR_ERR_DEVICE, "wavefront loop exceeded %u bounces", L.max_iters);
+        int cur = (int)(it & 1u);
+        SR_CUDA(wave_bounce(L, cur, st), "wavefront bounce");
+        SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws.counts + (cur ^ 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                "read live count");
+        SR_CUDA(cudaStreamSynchronize(st), "wavefront bounce");
+        if (s->counts_host[0] == 0) {
+            s->last_host_iters = it + 1;
+            break;
+        }
+    }
+    return SR_OK;
+}
+
 static int render_into(SrScene* s, const SrView* view, const SrRenderParams* params, const DevAovs& out, cudaStream_t st) {
     DevView dv;
     DevParams dp;
@@ -671,8 +828,13 @@ static int render_into(SrScene* s, const SrView* view, const SrRenderParams* par
         ctr = s->counters.as<unsigned long long>();
         SR_CUDA(cudaMemsetAsync(ctr, 0, SR_COUNTER_COUNT * sizeof(unsigned long long), st), "clear counters");
     }
-    SR_CUDA(launch_render(s->dev, dv, dp, out, ctr, s->err.as<uint32_t>(), st), "render launch");
-    return SR_OK;
+    int mode = s->render_mode == SR_RENDER_AUTO ? SR_RENDER_WAVEFRONT_GRAPH : s->render_mode;
+    s->last_mode = mode;
+    if (mode == SR_RENDER_MEGAKERNEL) {
+        SR_CUDA(launch_render(s->dev, dv, dp, out, ctr, s->err.as<uint32_t>(), st), "render launch");
+        return SR_OK;
+    }
+    return render_wavefront(s, dv, dp, out, ctr, st, mode == SR_RENDER_WAVEFRONT_GRAPH);
 }
 
 SR_API int sr_render_device(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* out,
@@ -734,6 +896,34 @@ SR_API int sr_render(SrScene* s, const SrView* view, const SrRenderParams* param
         SR_CUDA(cudaMemcpy(s->last_counters, s->counters.ptr, sizeof(s->last_counters), cudaMemcpyDeviceToHost),
                 "read counters");
     return check_device_error(s);
+}
+
+SR_API int sr_scene_set_render_mode(SrScene* s, int32_t mode) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    if (mode < SR_RENDER_AUTO || mode > SR_RENDER_WAVEFRONT_GRAPH) return fail(SR_ERR_INVALID_ARG, "bad render mode %d", mode);
+    s->render_mode = mode;
+    return SR_OK;
+}
+
+SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t* bounce_iterations) {
+    if (!s || !kernel_launches || !bounce_iterations) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    SR_CUDA(cudaDeviceSynchronize(), "sync");
+    if (s->last_mode == SR_RENDER_MEGAKERNEL) {
+        *kernel_launches = 1;
+        *bounce_iterations = 0;
+        return SR_OK;
+    }
+    uint32_t iters = s->last_host_iters;
+    if (s->last_mode == SR_RENDER_WAVEFRONT_GRAPH) {
+        SR_CUDA(cudaMemcpy(&iters, s->ws.counts + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
+        *kernel_launches = 1 + 3 * iters + iters / 2;  // init, 3 per bounce, loop condition per 2 bounces
+    } else {
+        *kernel_launches = 1 + 3 * iters;
+    }
+    *bounce_iterations = iters;
+    return SR_OK;
 }
 
 SR_API int sr_scene_set_counting(SrScene* s, int32_t enabled) {

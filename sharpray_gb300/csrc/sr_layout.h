@@ -67,8 +67,10 @@ struct SR_ALIGN16 DevSky {
     float sun_pdf_denom;
     float pad;
     float4 rot, rot_inv;
-    const float* cdf_marginal;  // height + 1 floats
-    const float* cdf_cond;      // height * (width + 1) floats
+    const float* cdf_marginal;       // height + 1 floats
+    const float* cdf_cond;           // height * (width + 1) floats
+    const uint32_t* guide_marginal;  // height + 1 bucket bounds of the marginal search
+    const uint32_t* guide_cond;      // height * (width + 1) bucket bounds of the row searches
     float4 top, middle, bottom, sun_dir, sun_radiance, sun_rot;
 };
 

@@ -197,9 +197,20 @@ def sky_env(width: int, height: int, seed: int, sun_peak: float = 50.0, sun_sigm
     t_dn = np.clip(-y * 4.0, 0.0, 1.0)
     sky = sky * (1.0 - t_dn[..., None]) + ground * t_dn[..., None]
     if lognormal_sigma > 0.0:
-        f = fbm3(d * 3.0, seed + 101, 5)
+        # smooth unit-variance field (fBm on the sphere, evaluated on a coarse grid and bilinearly
+        # upsampled), exponentiated: a lognormal luminance field with the requested sigma
+        cw, ch = max(4, width // 8), max(2, height // 8)
+        f = fbm3(_equirect_dirs(cw, ch) * 3.0, seed + 101, 5)
         z = (f - f.mean()) / max(f.std(), 1e-12)
-        sky = sky * np.exp(lognormal_sigma * z - 0.5 * lognormal_sigma ** 2)[..., None]
+        gx = (np.arange(width) + 0.5) / width * cw - 0.5
+        gy = (np.arange(height) + 0.5) / height * ch - 0.5
+        x0 = np.clip(np.floor(gx).astype(int), 0, cw - 1)
+        y0 = np.clip(np.floor(gy).astype(int), 0, ch - 1)
+        x1, y1 = np.clip(x0 + 1, 0, cw - 1), np.clip(y0 + 1, 0, ch - 1)
+        tx = np.clip(gx - x0, 0.0, 1.0)[None, :]
+        ty = np.clip(gy - y0, 0.0, 1.0)[:, None]
+        zz = ((z[y0][:, x0] * (1 - tx) + z[y0][:, x1] * tx) * (1 - ty) + (z[y1][:, x0] * (1 - tx) + z[y1][:, x1] * tx) * ty)
+        sky = sky * np.exp(lognormal_sigma * zz - 0.5 * lognormal_sigma ** 2)[..., None]
     elev = math.radians(rng.uniform(25.0, 55.0))
     azim = rng.uniform(0.0, 2.0 * math.pi)
     sun = np.array([math.cos(elev) * math.cos(azim), math.sin(elev), math.cos(elev) * math.sin(azim)])

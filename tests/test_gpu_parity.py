@@ -183,6 +183,41 @@ def test_counters_track_oracle(built):
     g.set_counting(False)
     _, oc = o.render(d.view.to_c(), render_params(*d.render_args()), counters=True)
     assert c["sample"] == oc["sample"] == d.width * d.height * d.spp
-    # (node/triangle counts differ by design: shadow rays stop at the first hit on the GPU)
-    for k in ("sample_bounce", "scene_trace", "scene_occlude", "cdf_probe"):
+    # Node/triangle counts differ by design: shadow rays stop at the first hit on the GPU, and the
+    # wavefront skips the shadow ray of a light sample that fails the normal-side tests (the
+    # reference traces it, then discards the result).
+    for k in ("sample_bounce", "scene_trace"):
         assert abs(c[k] - oc[k]) <= 0.02 * oc[k], (k, c[k], oc[k])
+    assert c["scene_occlude"] <= oc["scene_occlude"]
+
+
+@pytest.mark.parametrize("name", ["c1", "features", "c2_reduced"])
+def test_render_modes_identical(built, name):
+    """Megakernel, wavefront (host loop) and wavefront (device graph loop) run the same per-path
+    arithmetic in the same order, so their AOVs are bit-identical."""
+    from sharpray_gb300 import _abi
+    d, g, _ = built(name)
+    outs = {}
+    for mode in (_abi.SR_RENDER_MEGAKERNEL, _abi.SR_RENDER_WAVEFRONT, _abi.SR_RENDER_WAVEFRONT_GRAPH):
+        g.set_render_mode(mode)
+        outs[mode] = Renderer(g, d.view, *d.render_args())
+    g.set_render_mode(_abi.SR_RENDER_AUTO)
+    ref = outs[_abi.SR_RENDER_MEGAKERNEL]
+    for mode, r in outs.items():
+        for plane in ("radiance", "radiance_fog", "normals", "uv", "depth", "samples", "variance"):
+            a, b = getattr(r, plane), getattr(ref, plane)
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (mode, plane)
+
+
+def test_adaptive_sampling_wavefront(built, oracle_mod):
+    """Adaptive stop (minSamples < maxSamples) through the wavefront loop matches the oracle."""
+    d, g, o = built("c1")
+    args = (d.width, d.height, 32, 2, 16, 0.2, 4, 10.0)
+    rend = Renderer(g, d.view, *args)
+    ref, _ = o.render(d.view.to_c(), render_params(*args))
+    assert (rend.samples == ref.samples).mean() >= 0.97
+    assert rend.samples.min() >= 2 and rend.samples.max() <= 17
+    assert len(np.unique(rend.samples)) > 2, "threshold should stop some pixels early"
+    tot, tref = rend.radiance + rend.radiance_fog, ref.radiance + ref.radiance_fog
+    err = np.abs(tot - tref).max(axis=1) / np.maximum(np.abs(tref).max(axis=1), 1e-3)
+    assert (err < 1e-3).mean() >= 0.95
