@@ -39,22 +39,28 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError(f"build step failed ({proc.returncode}):\n{' '.join(cmd)}\n{proc.stdout}\n{proc.stderr}")
 
 
-def build_library(verbose: bool = False, ptxas_info: bool = False) -> Path:
-    """Compile every translation unit and link the shared library.  Returns its path."""
+def build_library(verbose: bool = False, ptxas_info: bool = False, defines: tuple = (), out: Path | None = None,
+                  build_dir: Path | None = None) -> Path:
+    """Compile every translation unit and link the shared library.  Returns its path.
+
+    `defines` are extra -D tuning macros (SR_REFILL, SR_TRACE_MIN_BLOCKS, SR_LEAF_LOOP); `out` and
+    `build_dir` redirect the outputs (defaults: the in-tree library)."""
     cuda = cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
-    BUILD.mkdir(exist_ok=True)
-    inc = [f"-I{ROOT / 'include'}", f"-I{CSRC}", f"-I{cuda / 'include'}"]
+    bdir = build_dir or BUILD
+    lib = out or LIB
+    bdir.mkdir(parents=True, exist_ok=True)
+    inc = [f"-I{ROOT / 'include'}", f"-I{CSRC}", f"-I{cuda / 'include'}"] + [f"-D{d}" for d in defines]
     jobs = []
     for src in CUDA_SOURCES:
-        obj = BUILD / (src + ".o")
+        obj = bdir / (src + ".o")
         cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
                "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", *inc, "-c", str(CSRC / src), "-o", str(obj)]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         jobs.append((cmd, obj))
     for src in HOST_SOURCES:
-        obj = BUILD / (src + ".o")
+        obj = bdir / (src + ".o")
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-fvisibility=hidden",
                "-Wall", *inc, "-c", str(CSRC / src), "-o", str(obj)]
         jobs.append((cmd, obj))
@@ -62,14 +68,14 @@ def build_library(verbose: bool = False, ptxas_info: bool = False) -> Path:
         futures = [ex.submit(_run, cmd) for cmd, _ in jobs]
         for f in futures:
             f.result()
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib.with_suffix(".so.tmp")
     link = [nvcc, *ARCH, "-shared", "-Xcompiler", "-fPIC", "-cudart", "static", *[str(o) for _, o in jobs],
             "-o", str(tmp)]
     _run(link)
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":

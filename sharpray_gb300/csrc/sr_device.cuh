@@ -18,6 +18,16 @@ namespace sr {
 
 constexpr float kPi = 3.14159265358979323846f;
 
+// Transcendentals go through one non-inlined copy each: inlining every call site multiplies the
+// kernels' machine code (the shading kernel exceeded the instruction cache), while the calls are
+// few per path segment.  The functions are CUDA's own sinf/cosf/expf/logf/powf/atan2f/asinf.
+static __device__ __noinline__ void sr_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
+static __device__ __noinline__ float sr_exp(float x) { return expf(x); }
+static __device__ __noinline__ float sr_log(float x) { return logf(x); }
+static __device__ __noinline__ float sr_pow(float x, float y) { return powf(x, y); }
+static __device__ __noinline__ float sr_atan2(float y, float x) { return atan2f(y, x); }
+static __device__ __noinline__ float sr_asin(float x) { return asinf(x); }
+
 // ---- small vector types ------------------------------------------------------------------------
 struct V2 {
     float x, y;
@@ -142,7 +152,7 @@ SR_DEV float rng_exponential(Rng& r) {
     do {
         u = rng_float(r);
     } while (u <= 1e-8f);
-    return -logf(u);
+    return -sr_log(u);
 }
 SR_DEV void rng_gauss(Rng& r, float& a_out, float& b_out) {
     float a;
@@ -150,9 +160,9 @@ SR_DEV void rng_gauss(Rng& r, float& a_out, float& b_out) {
         a = rng_float(r);
     } while (a <= 1e-8f);
     float b = (kPi * 2.0f) * rng_float(r);
-    float mag = sqrtf(-2.0f * logf(a));
+    float mag = sqrtf(-2.0f * sr_log(a));
     float sb, cb;
-    sincosf(b, &sb, &cb);
+    sr_sincos(b, &sb, &cb);
     a_out = mag * cb;
     b_out = mag * sb;
 }
@@ -266,7 +276,7 @@ SR_DEV bool sphere_hit(float4 sc, const Ray& r, ShapeHit& h, bool full) {
         h.norm = n;
         h.norm_geo = n;
         h.tan = {txyz.x, txyz.y, txyz.z, 1.0f};
-        h.uv = {0.5f + atan2f(n.z, n.x) / (2.0f * kPi), 0.5f - asinf(clampf(n.y, -1.0f, 1.0f)) / kPi};
+        h.uv = {0.5f + sr_atan2(n.z, n.x) / (2.0f * kPi), 0.5f - sr_asin(clampf(n.y, -1.0f, 1.0f)) / kPi};
     }
     return true;
 }
@@ -354,7 +364,7 @@ struct Hit {
 };
 
 // Scene-level closest hit (ANY = false) or occlusion test (ANY = true) as ONE loop over a shared
-// stack.  The reference nests two traversals: Bvh<Object>.Intersect (bvh.cs:165-216) calls, for each
+// stack (SceneQuery below).  The reference nests two traversals: Bvh<Object>.Intersect (bvh.cs:165-216) calls, for each
 // object of a scene-BVH leaf, Object.Intersect (math.cs:67-79) which runs a complete, unpruned mesh
 // BVH traversal in the object's local space.  Here the mesh traversal of the current object pushes
 // its entries above the scene entries (above `blas_base`); the loop swaps the traversal ray and the
@@ -364,36 +374,78 @@ struct Hit {
 // comparison `hit.Dist / localRayScale < bestDist` are the reference's, so results are bit-exact.
 // With ANY the search stops at the first hit found and prunes nothing, which gives the same yes/no
 // answer as the closest-hit query.
-constexpr int kSceneStack = 192;  // scene (<= 65) + mesh (<= 65) entries, with margin
+constexpr int kSceneStack = 192;
+// SR_LEAF_LOOP = 1 tests a whole mesh leaf in one step; 0 tests one triangle per step (more uniform
+// step lengths across the lanes of a warp).
+#ifndef SR_LEAF_LOOP
+#define SR_LEAF_LOOP 1
+#endif  // scene (<= 65) + mesh (<= 65) entries, with margin
 
-template <bool COUNT, bool ANY>
-SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* err) {
-    const float inf = __int_as_float(0x7f800000);
-    Hit best{-1, -1, inf, 0.f, 0.f, 0.f};
-    if (S.tlas_root < 0) return best;
-    StackEntry stack[kSceneStack];
-    {
-        float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
-        float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
-        stack[0] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+// Resumable traversal state: init() starts a ray, step() performs one loop iteration (one node-pair
+// test, one triangle test, or entering an object) and returns true when the query is answered
+// (`best` then holds the result).  Callers either run it to completion or interleave rays on a lane
+// (persistent kernels replace a finished ray at once).  GENERAL = false compiles only what scenes of
+// meshes need (no analytic shapes).
+template <bool ANY, bool GENERAL>
+struct SceneQuery {
+    // The traversal stack lives outside the struct (a separate local array passed to init/step):
+    // keeping the dynamically indexed array out lets the scalar state stay in registers.
+    Ray wr;              // world ray
+    Ray cr;              // ray of the current level (world, or the current object's local ray)
+    float cur_best;      // pruning distance of the current level
+    float lscale;        // local-ray scale of the current object
+    float ob_u, ob_v;    // best hit inside the current object
+    Hit best;
+    int sp, mesh_base, leaf_next, leaf_left, tri_next, tri_left, obj_pos, ob_tri;
+    uint32_t pops;
+    bool in_mesh;
+
+    SR_DEV void init(const DevScene& S, const Ray& r, StackEntry* stack) {
+        const float inf = __int_as_float(0x7f800000);
+        best = Hit{-1, -1, inf, 0.f, 0.f, 0.f};
+        wr = r;
+        cr = r;
+        cur_best = inf;
+        lscale = 1.0f;
+        ob_u = ob_v = 0.f;
+        mesh_base = leaf_next = leaf_left = tri_next = tri_left = 0;
+        obj_pos = ob_tri = -1;
+        pops = 0;
+        in_mesh = false;
+        sp = 0;
+        if (S.tlas_root >= 0) {
+            float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
+            float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
+            stack[0] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+            sp = 1;
+        }
     }
-    int sp = 1;
-    // current traversal ray (world or the current object's local ray) and pruning distance
-    V3 ro = wr.o, rinv = wr.inv;
-    float cur_best = inf;
-    bool in_mesh = false;
-    int mesh_base = 0;
-    int leaf_next = 0, leaf_left = 0;  // objects of the current scene leaf still to test
-    Ray lr = wr;                       // local ray of the current object
-    float lscale = 1.0f;
-    int obj_pos = -1;
-    int ob_tri = -1;
-    float ob_u = 0.f, ob_v = 0.f;
-    uint32_t pops = 0;
-    for (;;) {
+
+    template <bool COUNT>
+    SR_DEV bool step(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
+        const float inf = __int_as_float(0x7f800000);
         if (++pops > kMaxPops) {
             atomicOr(err, SR_DEVERR_LOOP);
-            break;
+            return true;
+        }
+        if (tri_left > 0) {
+            // one triangle of the current mesh leaf, in leaf order (bvh.cs:203-212)
+            const float4* tp = S.tris + 3 * tri_next;
+            float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
+            float t, u, v;
+            if (tri_hit(v3(q0), v3(q1), v3(q2), cr, t, u, v) && (ANY || t < cur_best)) {
+                if (ANY) {
+                    best = {obj_pos, tri_next, 0.f, 0.f, 0.f, 0.f};
+                    return true;
+                }
+                cur_best = t;
+                ob_tri = tri_next;
+                ob_u = u;
+                ob_v = v;
+            }
+            ++tri_next;
+            --tri_left;
+            return false;
         }
         if (in_mesh && sp == mesh_base) {
             // the object's mesh traversal is complete: Bvh<Object> leaf comparison (bvh.cs:207)
@@ -402,8 +454,7 @@ SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* er
                 if (d < best.dist) best = {obj_pos, ob_tri, d, cur_best, ob_u, ob_v};
             }
             in_mesh = false;
-            ro = wr.o;
-            rinv = wr.inv;
+            cr = wr;
             cur_best = ANY ? inf : best.dist;
         }
         if (!in_mesh && leaf_left > 0) {
@@ -412,40 +463,41 @@ SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* er
             ++leaf_next;
             --leaf_left;
             Ray l = to_local(o, wr, lscale);
-            int kind = __float_as_int(o.pos_kind.w);
+            int kind = GENERAL ? __float_as_int(o.pos_kind.w) : SR_SHAPE_MESH;
             if (kind == SR_SHAPE_MESH) {
                 int root = __float_as_int(o.scale_root.w);
-                if (root < 0) continue;  // empty mesh never hits
-                float4 rn0 = ldg4(S.nodes + 2 * root);
-                float4 rn1 = ldg4(S.nodes + 2 * root + 1);
+                if (root < 0) return false;  // empty mesh never hits
                 if (sp >= kSceneStack) {
                     atomicOr(err, SR_DEVERR_STACK);
-                    break;
+                    return true;
                 }
+                float4 rn0 = ldg4(S.nodes + 2 * root);
+                float4 rn1 = ldg4(S.nodes + 2 * root + 1);
                 mesh_base = sp;
                 stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
                 in_mesh = true;
-                lr = l;
-                ro = l.o;
-                rinv = l.inv;
+                cr = l;
                 cur_best = inf;
                 ob_tri = -1;
-            } else {
+            } else if (GENERAL) {
                 ShapeHit h;
                 bool ok = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, l, h, false)
                                                   : box_hit(o.shape0, o.shape1, l, h, false);
                 if (ok) {
-                    if (ANY) return {obj_pos, -1, 0.f, 0.f, 0.f, 0.f};
+                    if (ANY) {
+                        best = {obj_pos, -1, 0.f, 0.f, 0.f, 0.f};
+                        return true;
+                    }
                     float d = h.dist / lscale;
                     if (d < best.dist) best = {obj_pos, -1, d, 0.f, 0.f, 0.f};
                     cur_best = best.dist;
                 }
             }
-            continue;
+            return false;
         }
-        if (sp == 0) break;
+        if (sp == 0) return true;
         StackEntry e = stack[--sp];
-        if (!ANY && e.t >= cur_best) continue;
+        if (!ANY && e.t >= cur_best) return false;
         if (e.count == 0) {
             if (in_mesh)
                 SR_COUNT(c, SR_COUNTER_BLAS_NODE, 2);
@@ -453,15 +505,12 @@ SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* er
                 SR_COUNT(c, SR_COUNTER_TLAS_NODE, 2);
             const float4* n = S.nodes + 2 * e.child;
             float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
-            Ray rr;
-            rr.o = ro;
-            rr.inv = rinv;
             float ta = 0.f, tb = 0.f;
-            bool pa = slab(a0, a1, rr, ta) && (ANY || ta <= cur_best);
-            bool pb = slab(b0, b1, rr, tb) && (ANY || tb <= cur_best);
+            bool pa = slab(a0, a1, cr, ta) && (ANY || ta <= cur_best);
+            bool pb = slab(b0, b1, cr, tb) && (ANY || tb <= cur_best);
             if (sp + 2 > kSceneStack) {
                 atomicOr(err, SR_DEVERR_STACK);
-                break;
+                return true;
             }
             StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
             StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
@@ -481,46 +530,65 @@ SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* er
             }
         } else if (in_mesh) {
             SR_COUNT(c, SR_COUNTER_BLAS_SHAPE, (uint32_t)e.count);
-            for (int i = 0; i < e.count; ++i) {
-                const float4* tp = S.tris + 3 * (e.child + i);
+            tri_next = e.child;
+            tri_left = e.count;
+#if SR_LEAF_LOOP
+            // whole leaf in this step (bvh.cs:203-212)
+            for (; tri_left > 0; ++tri_next, --tri_left) {
+                const float4* tp = S.tris + 3 * tri_next;
                 float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
                 float t, u, v;
-                if (tri_hit(v3(q0), v3(q1), v3(q2), lr, t, u, v) && (ANY || t < cur_best)) {
-                    if (ANY) return {obj_pos, e.child + i, 0.f, 0.f, 0.f, 0.f};
+                if (tri_hit(v3(q0), v3(q1), v3(q2), cr, t, u, v) && (ANY || t < cur_best)) {
+                    if (ANY) {
+                        best = {obj_pos, tri_next, 0.f, 0.f, 0.f, 0.f};
+                        tri_left = 0;
+                        return true;
+                    }
                     cur_best = t;
-                    ob_tri = e.child + i;
+                    ob_tri = tri_next;
                     ob_u = u;
                     ob_v = v;
                 }
             }
+#endif
         } else {
             SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
             leaf_next = e.child;
             leaf_left = e.count;
         }
+        return false;
     }
-    return best;
+};
+
+template <bool COUNT, bool ANY, bool GENERAL = true>
+SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* err) {
+    StackEntry stack[kSceneStack];
+    SceneQuery<ANY, GENERAL> q;
+    q.init(S, wr, stack);
+    while (!q.template step<COUNT>(S, stack, c, err)) {
+    }
+    return q.best;
 }
 
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 SR_DEV Hit scene_closest(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err) {
-    return scene_traverse<COUNT, false>(S, r, c, err);
+    return scene_traverse<COUNT, false, GENERAL>(S, r, c, err);
 }
 
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 SR_DEV bool scene_any(const DevScene& S, const Ray& r, Ctr& c, uint32_t* err) {
-    return scene_traverse<COUNT, true>(S, r, c, err).obj >= 0;
+    return scene_traverse<COUNT, true, GENERAL>(S, r, c, err).obj >= 0;
 }
 
 // The world-space ShapeHit of a scene hit (ShapeExtensions.Intersect math.cs:67-79).
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 SR_DEV ShapeHit world_hit(const DevScene& S, const Ray& r, const Hit& hit, Ctr& c) {
     const DevObject& o = S.objects[hit.obj];
     float scale;
     Ray lr = to_local(o, r, scale);
-    int kind = __float_as_int(o.pos_kind.w);
+    int kind = GENERAL ? __float_as_int(o.pos_kind.w) : SR_SHAPE_MESH;
     ShapeHit h;
-    if (kind == SR_SHAPE_MESH) {
+    if (!GENERAL || kind == SR_SHAPE_MESH) {
         SR_COUNT(c, SR_COUNTER_HIT_INFLATE, 1);
         h = inflate(S, hit.tri, hit.tl, hit.u, hit.v);
     } else if (kind == SR_SHAPE_SPHERE) {
@@ -571,25 +639,25 @@ SR_DEV Col tex_sample(const DevScene& S, int id, V2 coord, Ctr& c) {
 
 // ---- sky ----------------------------------------------------------------------------------------
 SR_DEV V2 equirect_uv(V3 d) {
-    float u = atan2f(d.z, d.x) / (kPi * 2.0f) + 0.5f;
-    float v = 0.5f - asinf(clampf(d.y, -1.0f, 1.0f)) / kPi;
+    float u = sr_atan2(d.z, d.x) / (kPi * 2.0f) + 0.5f;
+    float v = 0.5f - sr_asin(clampf(d.y, -1.0f, 1.0f)) / kPi;
     return {u, v};
 }
 SR_DEV V3 from_equirect_uv(V2 uv) {
     float phi = (uv.x - 0.5f) * 2.0f * kPi;
     float st, ct, sp, cp;
-    sincosf(kPi * uv.y, &st, &ct);
-    sincosf(phi, &sp, &cp);
+    sr_sincos(kPi * uv.y, &st, &ct);
+    sr_sincos(phi, &sp, &cp);
     return {st * cp, ct, st * sp};
 }
 
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 SR_DEV Col sky_radiance(const DevScene& S, V3 dir, Ctr& c) {
     const DevSky& k = S.sky;
-    if (k.kind == 0) return tex_sample<COUNT>(S, k.texture, equirect_uv(quat_rotate(k.rot_inv, dir)), c) * k.multiplier;
+    if (!GENERAL || k.kind == 0) return tex_sample<COUNT>(S, k.texture, equirect_uv(quat_rotate(k.rot_inv, dir)), c) * k.multiplier;
     const float bias = 0.0001f;
-    float top_b = 1.0f - powf(fminf(1.0f, 1.0f + bias - dir.y), 4.0f);
-    float bot_b = 1.0f - powf(fminf(1.0f, 1.0f + bias + dir.y), 40.0f);
+    float top_b = 1.0f - sr_pow(fminf(1.0f, 1.0f + bias - dir.y), 4.0f);
+    float bot_b = 1.0f - sr_pow(fminf(1.0f, 1.0f + bias + dir.y), 40.0f);
     float mid_b = 1.0f - top_b - bot_b;
     Col ambient = col3(k.top) * top_b + col3(k.middle) * mid_b + col3(k.bottom) * bot_b;
     float blend = fmaxf(0.0f, (dot(dir, v3(k.sun_dir)) - k.sun_cos) / (1.0f - k.sun_cos));
@@ -597,9 +665,10 @@ SR_DEV Col sky_radiance(const DevScene& S, V3 dir, Ctr& c) {
 }
 
 // SkyTexture.LightDir / SunProcedural.LightDir (point-lookup pdf for MIS); 0 = null.
+template <bool GENERAL = true>
 SR_DEV float sky_light_pdf(const DevScene& S, V3 dir) {
     const DevSky& k = S.sky;
-    if (k.kind == 0) {
+    if (!GENERAL || k.kind == 0) {
         if (k.cdf_total <= 0.0f) return 0.0f;
         V2 uv = equirect_uv(quat_rotate(k.rot_inv, dir));
         const DevTexture& t = S.textures[k.texture];
@@ -638,10 +707,10 @@ SR_DEV uint32_t cdf_sample(const float* cdf, const uint32_t* guide, uint32_t n, 
 }
 
 // ISky.LightDirRand (SkyTexture scene.cs:408-416, SunProcedural scene.cs:314-323).
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr& c) {
     const DevSky& k = S.sky;
-    if (k.kind == 0) {
+    if (!GENERAL || k.kind == 0) {
         if (k.cdf_total <= 0.0f) return false;
         V2 u = rand_v2(rng);
         const DevTexture& t = S.textures[k.texture];
@@ -659,14 +728,14 @@ SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr
     float z = k.sun_cos + (1.0f - k.sun_cos) * blend;
     float st = sqrtf(fmaxf(0.0f, 1.0f - z * z));
     float sp, cp;
-    sincosf(phi, &sp, &cp);
+    sr_sincos(phi, &sp, &cp);
     dir = quat_rotate(k.sun_rot, V3{cp * st, sp * st, z});
     pdf = blend / k.sun_pdf_denom;
     return true;
 }
 
 // ---- fog (scene.cs:445-496) -----------------------------------------------------------------------
-SR_DEV float fog_density_at(const DevScene& S, float y) { return S.fog_density * expf(-S.fog_falloff * y); }
+SR_DEV float fog_density_at(const DevScene& S, float y) { return S.fog_density * sr_exp(-S.fog_falloff * y); }
 SR_DEV float fog_transmittance_inf(const DevScene& S, const Ray& r) {
     // OpticalDepth over [0, +inf).
     float hd = r.d.y;
@@ -676,7 +745,7 @@ SR_DEV float fog_transmittance_inf(const DevScene& S, const Ray& r) {
     float ds = fog_density_at(S, hs);
     float de = fog_density_at(S, he);
     float od = fabsf(hd) < 1e-6f ? ds * (inf - 0.0f) : (ds - de) / (S.fog_falloff * hd);
-    return expf(-od);
+    return sr_exp(-od);
 }
 SR_DEV bool fog_scatter_distance(const DevScene& S, const Ray& r, float end, Rng& rng, float& t_out) {
     float hd = r.d.y;
@@ -689,9 +758,9 @@ SR_DEV bool fog_scatter_distance(const DevScene& S, const Ray& r, float end, Rng
         if (ds <= 0.0f) return false;
         t = 0.0f + u / ds;
     } else {
-        float rhs = expf(-S.fog_falloff * hs) - u * S.fog_falloff * hd / S.fog_density;
+        float rhs = sr_exp(-S.fog_falloff * hs) - u * S.fog_falloff * hd / S.fog_density;
         if (rhs <= 0.0f) return false;
-        float yt = -logf(rhs) / S.fog_falloff;
+        float yt = -sr_log(rhs) / S.fog_falloff;
         t = (yt - ho) / hd;
     }
     if (t < end) {
@@ -724,7 +793,7 @@ SR_DEV V3 ggx_sample_local(float rs, V2 u) {
     float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
     float phi = (2.0f * kPi) * u.y;
     float sp, cp;
-    sincosf(phi, &sp, &cp);
+    sr_sincos(phi, &sp, &cp);
     return {st * cp, st * sp, ct};
 }
 SR_DEV float power_heuristic(float p1, float p2) {
@@ -746,7 +815,7 @@ SR_DEV bool refract(V3 in, V3 n, float ratio, V3& out) {
     return true;
 }
 SR_DEV Col beer_law(Col a, float dist) {
-    return {powf(fmaxf(a.r, 0.0f), dist), powf(fmaxf(a.g, 0.0f), dist), powf(fmaxf(a.b, 0.0f), dist)};
+    return {sr_pow(fmaxf(a.r, 0.0f), dist), sr_pow(fmaxf(a.g, 0.0f), dist), sr_pow(fmaxf(a.b, 0.0f), dist)};
 }
 SR_DEV V3 perp(V3 v) {
     V3 up = fabsf(v.y) < 0.9f ? up3() : right3();
@@ -767,7 +836,7 @@ SR_DEV V3 hg_scatter_dir(V3 fwd, float g, Rng& rng) {
     V3 t = perp(fwd);
     V3 b = cross(fwd, t);
     float sp, cp;
-    sincosf(phi, &sp, &cp);
+    sr_sincos(phi, &sp, &cp);
     return ct * fwd + (st * cp) * t + (st * sp) * b;
 }
 SR_DEV V3 from_tangent_space(V3 d, V4 tangent, V3 n) {
@@ -829,8 +898,9 @@ SR_DEV float opaque_pdf(const Surface& s, V3 view, V3 light, float spec_p) {
     float pd = ndl / kPi;
     return (spec_p * ps + (1.0f - spec_p) * pd) * (1.0f - s.transparency);
 }
+template <bool GENERAL = true>
 SR_DEV Scatter surface_scatter(const Surface& s, V3 in, V3 view, Rng& rng) {
-    if (rng_float(rng) < s.transparency) {
+    if (rng_float(rng) < s.transparency && GENERAL) {
         // TransparentScatter scene.cs:119-144
         bool entering = dot(in, s.normal_geo) < 0.0f;
         V3 rn = entering ? s.normal_geo : -s.normal_geo;

@@ -612,6 +612,10 @@ SR_API int sr_scene_build(SrScene* s) {
     d.has_fog = s->has_fog ? 1 : 0;
     d.has_transparent = has_transparent ? 1 : 0;
     d.object_count = (int32_t)s->objects.size();
+    bool general = has_transparent || s->sky_kind != 0;
+    for (const auto& o : s->objects)
+        if (o.shape.kind != SR_SHAPE_MESH || o.mat.normal_texture >= 0) general = true;
+    d.general = general ? 1 : 0;
     if (s->has_fog) {
         d.fog_density = s->fog.density;
         d.fog_falloff = s->fog.height_falloff;
@@ -720,8 +724,8 @@ static int wave_reserve(SrScene* s, uint32_t slots) {
     if (s->wave_slots >= slots && s->wave.ptr) return SR_OK;
     const size_t n = slots;
     // 16-byte planes: rng, ray_o, ray_d, rad, fog, energy, medium, prim, acc0..5, hit, sh0..3 (21)
-    // 8-byte planes: prim_uv, hit_uv; 4-byte planes: rng_c, q_active x2, q_resolve; + 4 counters
-    size_t bytes = n * (21 * 16 + 2 * 8 + 4 * 4) + 256;
+    // 8-byte planes: prim_uv, hit_uv; 4-byte planes: rng_c, q_active x2, q_resolve, q_shadow; + 8 counters
+    size_t bytes = n * (21 * 16 + 2 * 8 + 5 * 4) + 256;
     SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
     char* p = s->wave.as<char>();
     auto take = [&](size_t elem) {
@@ -757,6 +761,7 @@ static int wave_reserve(SrScene* s, uint32_t slots) {
     w.q_active[0] = (uint32_t*)take(4);
     w.q_active[1] = (uint32_t*)take(4);
     w.q_resolve = (uint32_t*)take(4);
+    w.q_shadow = (uint32_t*)take(4);
     w.counts = (uint32_t*)p;
     s->wave_slots = slots;
     // request flags start clear; resolve clears them after use
@@ -784,6 +789,7 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
     L.out = out;
     L.err = s->err.as<uint32_t>();
     L.counters = ctr;
+    L.general = s->dev.general;
     wave_grid_sizes(L, s->sms);
     uint64_t cap = (uint64_t)dp.max_samples * (dp.bounces + 1) + 4;
     L.max_iters = (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap);
@@ -918,9 +924,9 @@ SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t*
     uint32_t iters = s->last_host_iters;
     if (s->last_mode == SR_RENDER_WAVEFRONT_GRAPH) {
         SR_CUDA(cudaMemcpy(&iters, s->ws.counts + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
-        *kernel_launches = 1 + 3 * iters + iters / 2;  // init, 3 per bounce, loop condition per 2 bounces
+        *kernel_launches = 1 + 4 * iters + iters / 2;  // init, 4 per bounce, loop condition per 2 bounces
     } else {
-        *kernel_launches = 1 + 3 * iters;
+        *kernel_launches = 1 + 4 * iters;
     }
     *bounce_iterations = iters;
     return SR_OK;

@@ -87,6 +87,9 @@ struct SR_ALIGN16 DevScene {
     int32_t has_fog;
     int32_t has_transparent;
     int32_t object_count;
+    int32_t general;  // needs the general kernels (analytic shapes, transparency, normal maps,
+                      // procedural sky); 0 = meshes + texture sky only
+    int32_t pad1[3];
     float fog_density, fog_falloff, fog_g, pad;
     float4 fog_color;
 };

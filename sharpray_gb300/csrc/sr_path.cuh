@@ -23,10 +23,10 @@ struct SurfHit {
 
 // The Surface of a scene hit: Scene.Trace after the BVH query (scene.cs:608-621): inflate the
 // winning hit, then the material's texture lookups, normal map and re-orthogonalised tangent.
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 __device__ __forceinline__ void surface_from_hit(const DevScene& S, const Ray& ray, const Hit& hit, SurfHit& out,
                                                  Ctr& c) {
-    ShapeHit h = world_hit<COUNT>(S, ray, hit, c);
+    ShapeHit h = world_hit<COUNT, GENERAL>(S, ray, hit, c);
     const DevObject& o = S.objects[hit.obj];
     const DevMaterial& m = S.materials[o.index];
     float4 ar = m.albedo_rough;
@@ -35,7 +35,7 @@ __device__ __forceinline__ void surface_from_hit(const DevScene& S, const Ray& r
     float roughness = (m.tex[1] >= 0 ? tex_sample<COUNT>(S, m.tex[1], h.uv, c).r : 1.0f) * ar.w;
     float metallic = (m.tex[2] >= 0 ? tex_sample<COUNT>(S, m.tex[2], h.uv, c).r : 1.0f) * mp.x;
     V3 normal = h.norm;
-    if (m.tex[3] >= 0) {
+    if (GENERAL && m.tex[3] >= 0) {
         Col nc = tex_sample<COUNT>(S, m.tex[3], h.uv, c);
         V3 tn = normalize_or(V3{nc.r * 2.0f - 1.0f, -(nc.g * 2.0f - 1.0f), nc.b * 2.0f - 1.0f}, up3());
         normal = normalize_or(from_tangent_space(tn, h.tan, h.norm), h.norm);
@@ -58,22 +58,22 @@ __device__ __forceinline__ void surface_from_hit(const DevScene& S, const Ray& r
 }
 
 // Scene.Trace scene.cs:602-625.
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 __device__ bool trace_surface(const DevScene& S, const Ray& ray, SurfHit& out, Ctr& c, uint32_t* err) {
     SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-    Hit hit = scene_closest<COUNT>(S, ray, c, err);
+    Hit hit = scene_closest<COUNT, GENERAL>(S, ray, c, err);
     if (hit.obj < 0) return false;
-    surface_from_hit<COUNT>(S, ray, hit, out, c);
+    surface_from_hit<COUNT, GENERAL>(S, ray, hit, out, c);
     return true;
 }
 
 // Scene.ShadowTransmittance scene.cs:576-600.  In scenes without transparent materials the first
 // hit is always opaque, so the answer is "any hit -> black, else white".
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 __device__ Col shadow_transmittance(const DevScene& S, Ray ray, Ctr& c, uint32_t* err) {
-    if (!S.has_transparent) {
+    if (!GENERAL || !S.has_transparent) {
         SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
-        return scene_any<COUNT>(S, ray, c, err) ? black() : white();
+        return scene_any<COUNT, GENERAL>(S, ray, c, err) ? black() : white();
     }
     Col tr = white();
     int steps = 0;

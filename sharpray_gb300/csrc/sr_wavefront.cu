@@ -1,13 +1,18 @@
 // sr_wavefront.cu — wavefront form of the per-pixel path loop.
 //
-// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into three
+// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into four
 // kernels per bounce over structure-of-arrays path state, one slot per pixel:
 //
-//   extend  : closest hit of every live path ray            (Scene.Trace -> Bvh.Intersect)
-//   shade   : surface/fog/miss logic of one segment, light sample, Russian roulette, scatter;
-//             the NEE shadow ray and the end of a sample are deferred to `resolve`
-//   resolve : shadow ray (ShadowTransmittance) and its contribution, then, for finished samples,
-//             the pixel statistics, the adaptive stop, and the next camera ray or the AOV write
+//   extend   : closest hit of every live path ray            (Scene.Trace -> Bvh.Intersect)
+//   shade    : surface/fog/miss logic of one segment, light sample, Russian roulette, scatter;
+//              the NEE shadow ray and the end of a sample are deferred
+//   shadow   : shadow rays (ShadowTransmittance, scene.cs:576-600) times the fog transmittance
+//   finalize : NEE contributions, then, for finished samples, the pixel statistics, the adaptive
+//              stop, and the next camera ray or the AOV write
+//
+// extend and shadow are persistent: a lane that finishes its ray takes the next one from the
+// queue at once (refilled per warp with one atomic), so warps stay full although ray lengths
+// differ by orders of magnitude.
 //
 // Live paths are compacted between kernels with warp-aggregated atomics (ballot + popc), so every
 // launch works on dense queues.  Every per-path operation -- RNG draws, float operation order,
@@ -89,33 +94,122 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
     push(W.q_active[0], &W.counts[0], s, valid);
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_wave_extend(WaveState W, DevScene S, int cur, uint32_t* err,
+// A warp refills its idle lanes once at least this many are idle (or all are).
+#ifndef SR_REFILL
+#define SR_REFILL 8
+#endif
+constexpr int kRefill = SR_REFILL;
+// Minimum resident blocks per SM requested for the traversal kernels (caps their registers).
+#ifndef SR_TRACE_MIN_BLOCKS
+#define SR_TRACE_MIN_BLOCKS 6
+#endif
+
+// Persistent ray loop shared by extend and shadow: lanes take queue entries [fetch counter) until
+// the queue is exhausted; `start(slot)` begins a query, `finish(slot)` stores its answer.
+template <bool COUNT, bool ANY, bool GENERAL, typename Start, typename Finish>
+__device__ __forceinline__ void persistent_queries(const DevScene& S, const uint32_t* q, uint32_t n, uint32_t* fetch,
+                                                   Ctr& c, uint32_t* err, Start start, Finish finish) {
+    StackEntry stack[kSceneStack];
+    SceneQuery<ANY, GENERAL> sq;
+    bool busy = false, exhausted = false;
+    uint32_t slot = 0;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned idle = __ballot_sync(0xffffffffu, !busy);
+        int nidle = __popc(idle);
+        if (!exhausted && nidle >= kRefill) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(fetch, (uint32_t)nidle);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + (uint32_t)nidle >= n) exhausted = true;
+            if (!busy) {
+                uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+                if (idx < n) {
+                    slot = q[idx];
+                    sq.init(S, start(slot), stack);
+                    busy = true;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, busy)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (busy && sq.template step<COUNT>(S, stack, c, err)) {
+            finish(slot, sq.best);
+            busy = false;
+        }
+    }
+}
+
+template <bool COUNT, bool GENERAL>
+__global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveState W, DevScene S, int cur, uint32_t* err,
                                                      unsigned long long* counters) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        W.counts[2] = 0;        // resolve queue of this bounce starts empty
+        W.counts[2] = 0;        // deferred-work queue of this bounce starts empty
+        W.counts[6] = 0;        // shadow queue of this bounce starts empty
         W.counts[cur ^ 1] = 0;  // next live queue starts empty
     }
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
-    const uint32_t n = W.counts[cur];
-    const uint32_t* q = W.q_active[cur];
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        uint32_t s = q[k];
-        float4 o = W.ray_o[s], d = W.ray_d[s];
-        Ray ray = make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
-        SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-        Hit h = scene_closest<COUNT>(S, ray, c, err);
-        W.hit[s] = make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl);
-        W.hit_uv[s] = make_float2(h.u, h.v);
+    persistent_queries<COUNT, false, GENERAL>(
+        S, W.q_active[cur], W.counts[cur], &W.counts[4], c, err,
+        [&](uint32_t s) {
+            SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
+            float4 o = W.ray_o[s], d = W.ray_d[s];
+            return make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
+        },
+        [&](uint32_t s, const Hit& h) {
+            W.hit[s] = make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl);
+            W.hit_uv[s] = make_float2(h.u, h.v);
+        });
+    flush_counters<COUNT>(c, counters);
+}
+
+// Shadow rays of the bounce: transmittance (any hit -> black in opaque scenes) times the fog
+// transmittance, as SampleSkyLight forms it (scene.cs:758-772); written over the ray origin.
+template <bool COUNT, bool GENERAL>
+__global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveState W, DevScene S, uint32_t* err,
+                                                     unsigned long long* counters) {
+    Ctr c;
+#pragma unroll
+    for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
+    if (!GENERAL || !S.has_transparent) {
+        persistent_queries<COUNT, true, GENERAL>(
+            S, W.q_shadow, W.counts[6], &W.counts[5], c, err,
+            [&](uint32_t s) {
+                SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
+                float4 o = W.sh0[s], d = W.sh1[s];
+                return make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
+            },
+            [&](uint32_t s, const Hit& h) {
+                float4 o = W.sh0[s], d = W.sh1[s];
+                float tr = 0.0f;
+                if (h.obj < 0) {
+                    tr = 1.0f;
+                    if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}));
+                }
+                W.sh0[s] = make_float4(tr, tr, tr, o.w);
+            });
+    } else {
+        const uint32_t n = W.counts[6];
+        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+            uint32_t s = W.q_shadow[k];
+            float4 o = W.sh0[s], d = W.sh1[s];
+            Ray shadow = make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
+            Col tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
+            if (max_component(tr) > 0.0f && S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
+            W.sh0[s] = make_float4(tr.r, tr.g, tr.b, o.w);
+        }
     }
     flush_counters<COUNT>(c, counters);
 }
 
-template <bool COUNT>
+template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, uint32_t* err,
                                                     unsigned long long* counters) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[5] = 0;  // shadow kernel's fetch counter
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
@@ -145,7 +239,7 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
             Hit hit{__float_as_int(h0.x), __float_as_int(h0.y), h0.z, h0.w, huv.x, huv.y};
             bool has_hit = hit.obj >= 0;
             SurfHit sh;
-            if (has_hit) surface_from_hit<COUNT>(S, ray, hit, sh, c);
+            if (has_hit) surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
             float sdist;
             if (S.has_fog && fog_scatter_distance(S, ray, has_hit ? sh.dist : inf, rng, sdist)) {
                 // fog scatter: NEE toward the sky is deferred to resolve (scene.cs:659-683)
@@ -153,7 +247,7 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                 V3 pos = ray_at(ray, sdist);
                 V3 ldir;
                 float lpdf;
-                if (sky_light_rand<COUNT>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
+                if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
                     float fog_pdf = hg_pdf(dot(ray.d, ldir), S.fog_g);
                     float mis = power_heuristic(lpdf, fog_pdf);
                     rflags |= RF_SHADOW | (bounce == 0 ? RF_FOG : 0u);
@@ -177,7 +271,7 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                 V3 view = -ray.d;
                 float bias = fmaxf(1e-4f, dist * 1e-4f);
                 V3 pos = ray_at(ray, dist - bias);
-                if (pflags & PF_MEDIUM) energy = energy * beer_law(col3(W.medium[s]), dist);
+                if (GENERAL && (pflags & PF_MEDIUM)) energy = energy * beer_law(col3(W.medium[s]), dist);
                 radiance = radiance + su.radiance * energy;
                 if (bounce == 0) {
                     pflags |= PF_PRIMARY;
@@ -186,7 +280,7 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                 }
                 V3 ldir;
                 float lpdf;
-                if (sky_light_rand<COUNT>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
+                if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
                     V3 nn = dot(su.normal, view) >= 0.0f ? su.normal : -su.normal;
                     V3 ng = dot(su.normal_geo, view) >= 0.0f ? su.normal_geo : -su.normal_geo;
                     if (dot(nn, ldir) > 0.0f && dot(ng, ldir) > 0.0f) {
@@ -203,11 +297,11 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                 if (russian_roulette(energy, bounce, rng)) {
                     rflags |= RF_TERMINATE;
                 } else {
-                    Scatter sc = surface_scatter(su, ray.d, view, rng);
+                    Scatter sc = surface_scatter<GENERAL>(su, ray.d, view, rng);
                     energy = energy * sc.weight;
                     energy = clamp_luminance(energy, P.indirect_clamp);
                     bool enter = dot(sc.dir, su.normal_geo) < 0.0f;
-                    if (sc.refracted) {
+                    if (GENERAL && sc.refracted) {
                         if (enter) {
                             pflags |= PF_MEDIUM;
                             W.medium[s] = make_float4(su.albedo.r, su.albedo.g, su.albedo.b, 0.f);
@@ -223,8 +317,8 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                 }
             } else {
                 // miss: sky radiance with the MIS weight of the last scatter (scene.cs:728-738)
-                float mis = (pflags & PF_SPDF) ? power_heuristic(spdf, sky_light_pdf(S, ray.d)) : 1.0f;
-                radiance = radiance + sky_radiance<COUNT>(S, ray.d, c) * mis * energy;
+                float mis = (pflags & PF_SPDF) ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
+                radiance = radiance + sky_radiance<COUNT, GENERAL>(S, ray.d, c) * mis * energy;
                 rflags |= RF_TERMINATE;
             }
             if (!(rflags & RF_TERMINATE) && ++bounce == P.bounces + 1) rflags |= RF_TERMINATE;
@@ -237,13 +331,15 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
         }
         push(W.q_active[nxt], &W.counts[nxt], s, valid && rflags == 0);
         push(W.q_resolve, &W.counts[2], s, valid && rflags != 0);
+        push(W.q_shadow, &W.counts[6], s, valid && (rflags & RF_SHADOW));
     }
     flush_counters<COUNT>(c, counters);
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_wave_resolve(WaveState W, DevScene S, DevView V, DevParams P, DevAovs out,
-                                                      int cur, uint32_t* err, unsigned long long* counters) {
+template <bool COUNT, bool GENERAL>
+__global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, DevView V, DevParams P, DevAovs out,
+                                                       int cur, uint32_t* err, unsigned long long* counters) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[4] = 0;  // next extend's fetch counter
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
@@ -259,14 +355,13 @@ __global__ void __launch_bounds__(128) k_wave_resolve(WaveState W, DevScene S, D
             float4 s0 = W.sh0[s];
             uint32_t rflags = (uint32_t)__float_as_int(s0.w);
             if (rflags & RF_SHADOW) {
-                // ShadowTransmittance + the rest of SampleSkyDirect / SampleSkyDirectFog (scene.cs:758-810)
-                float4 s1 = W.sh1[s], s2 = W.sh2[s], s3 = W.sh3[s];
-                V3 ldir{s1.x, s1.y, s1.z};
-                Ray shadow = make_ray(V3{s0.x, s0.y, s0.z}, ldir);
-                Col tr = shadow_transmittance<COUNT>(S, shadow, c, err);
+                // the rest of SampleSkyDirect / SampleSkyDirectFog (scene.cs:774-810) once the
+                // shadow kernel has left the transmittance (incl. fog) in sh0.xyz
+                Col tr = col3(s0);
                 if (max_component(tr) > 0.0f) {
-                    if (S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
-                    Col contrib = sky_radiance<COUNT>(S, ldir, c) * tr * col3(s2) * s2.w / s1.w;
+                    float4 s1 = W.sh1[s], s2 = W.sh2[s], s3 = W.sh3[s];
+                    V3 ldir{s1.x, s1.y, s1.z};
+                    Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * col3(s2) * s2.w / s1.w;
                     Col add = contrib * col3(s3);
                     if (rflags & RF_FOG) {
                         float4 f = W.fog[s];
@@ -363,35 +458,53 @@ __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* cou
 }
 
 // ---- launchers ------------------------------------------------------------------------------------
-template <bool COUNT>
+template <bool COUNT, bool GENERAL>
 static void launch_bounce(const WaveLaunch& L, int cur, cudaStream_t st) {
-    k_wave_extend<COUNT><<<L.grid_extend, 128, 0, st>>>(L.W, L.S, cur, L.err, L.counters);
-    k_wave_shade<COUNT><<<L.grid_shade, 128, 0, st>>>(L.W, L.S, L.P, cur, L.err, L.counters);
-    k_wave_resolve<COUNT><<<L.grid_resolve, 128, 0, st>>>(L.W, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
+    k_wave_extend<COUNT, GENERAL><<<L.grid_extend, 128, 0, st>>>(L.W, L.S, cur, L.err, L.counters);
+    k_wave_shade<COUNT, GENERAL><<<L.grid_shade, 128, 0, st>>>(L.W, L.S, L.P, cur, L.err, L.counters);
+    k_wave_shadow<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(L.W, L.S, L.err, L.counters);
+    k_wave_finalize<COUNT, GENERAL><<<L.grid_resolve, 128, 0, st>>>(L.W, L.S, L.V, L.P, L.out, cur, L.err,
+                                                                    L.counters);
 }
 
 void wave_grid_sizes(WaveLaunch& L, int sms) {
-    int b0 = 0, b1 = 0, b2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_wave_extend<false>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_wave_shade<false>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_wave_resolve<false>, 128, 0);
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+    if (L.general) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_wave_extend<false, true>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_wave_shade<false, true>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_wave_finalize<false, true>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_wave_shadow<false, true>, 128, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_wave_extend<false, false>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_wave_shade<false, false>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_wave_finalize<false, false>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_wave_shadow<false, false>, 128, 0);
+    }
     L.grid_extend = sms * (b0 > 0 ? b0 : 1);
     L.grid_shade = sms * (b1 > 0 ? b1 : 1);
     L.grid_resolve = sms * (b2 > 0 ? b2 : 1);
+    L.grid_shadow = sms * (b3 > 0 ? b3 : 1);
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(L.W.counts, 0, 4 * sizeof(uint32_t), st);
+    cudaError_t e = cudaMemsetAsync(L.W.counts, 0, 8 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     k_wave_init<<<(L.W.slots + 127) / 128, 128, 0, st>>>(L.W, L.V, L.P);
     return cudaGetLastError();
 }
 
 cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st) {
-    if (L.counters)
-        launch_bounce<true>(L, cur, st);
-    else
-        launch_bounce<false>(L, cur, st);
+    if (L.general) {
+        if (L.counters)
+            launch_bounce<true, true>(L, cur, st);
+        else
+            launch_bounce<false, true>(L, cur, st);
+    } else {
+        if (L.counters)
+            launch_bounce<true, false>(L, cur, st);
+        else
+            launch_bounce<false, false>(L, cur, st);
+    }
     return cudaGetLastError();
 }
 

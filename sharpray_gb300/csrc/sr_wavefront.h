@@ -30,13 +30,15 @@ struct WaveState {
     float4* acc5;      // pixel: first uv, has-uv flag
     float4* hit;       // closest hit: object, triangle (int bits), world distance, local distance
     float2* hit_uv;    // closest hit barycentrics
-    float4* sh0;       // deferred work: shadow origin, request flags (int bits)
+    float4* sh0;       // deferred work: shadow origin (then its transmittance), request flags (int bits)
     float4* sh1;       // shadow direction, light pdf
     float4* sh2;       // reflectance (or phase pdf) rgb, MIS weight
     float4* sh3;       // throughput at the light sample
     uint32_t* q_active[2];  // live-path queues (ping-pong)
-    uint32_t* q_resolve;    // deferred-work queue
-    uint32_t* counts;       // [0],[1] live counts, [2] resolve count, [3] bounce counter
+    uint32_t* q_resolve;    // deferred-work queue (shadow requests and finished samples)
+    uint32_t* q_shadow;     // shadow-ray queue
+    uint32_t* counts;       // [0],[1] live counts, [2] deferred count, [3] bounce counter,
+                            // [4] extend fetch, [5] shadow fetch, [6] shadow count
 };
 
 struct WaveLaunch {
@@ -47,7 +49,8 @@ struct WaveLaunch {
     DevAovs out;
     uint32_t* err;
     unsigned long long* counters;
-    int grid_extend, grid_shade, grid_resolve;
+    int grid_extend, grid_shade, grid_resolve, grid_shadow;
+    int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
 };
 
