@@ -283,6 +283,19 @@ SR_API int sr_compose(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, u
 /* Same on device buffers (radiance, radiance_fog, normals, depth, variance are read) on `stream`. */
 SR_API int sr_compose_device(SrContext* ctx, const SrAovs* device_aovs, uint32_t width, uint32_t height,
                              const SrComposeParams* params, uint8_t* device_rgb8, void* stream);
+/* sr_compose_device that allocates no device memory: for hosts that cannot allocate when they
+ * composite (a service whose device memory is fully committed to its own pools under a quota, a
+ * latency-critical loop that cannot afford cudaMalloc's device-wide synchronisation).  No
+ * counterpart in the reference.  Its scratch is a fixed
+ * 32 MiB device array that every GPU loading the library holds until the process exits; the image
+ * is filtered in row bands, and a call fails with SR_ERR_INVALID_ARG when one band with its filter
+ * halo does not fit, i.e. when (2 * max(radius, fog radius) + 2) * width * 48 bytes > 32 MiB.
+ * The first call on a device looks up the array's address there (make that first call before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU race and corrupt each
+ * other's images, so run them one after another.  Spatial weights are evaluated per tap on the
+ * device, so results can differ from sr_compose_device by one code value in rare pixels. */
+SR_API int sr_compose_device_static(SrContext* ctx, const SrAovs* device_aovs, uint32_t width, uint32_t height,
+                                    const SrComposeParams* params, uint8_t* device_rgb8, void* stream);
 /* Tonemap of radiance + radiance_fog without denoise.  Replaces Compositor.Preview compose.cs:57-65. */
 SR_API int sr_preview(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height,
                       const SrComposeParams* params, uint8_t* host_rgb8);

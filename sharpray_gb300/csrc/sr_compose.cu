@@ -151,4 +151,172 @@ cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, c
     return cudaGetLastError();
 }
 
+// ---- compositing without allocations ----------------------------------------------------------
+//
+// Some hosts cannot allocate device memory at the moment they want to composite: a render service
+// whose device memory is already committed to its own frame pools under a hard quota, or a
+// latency-critical loop that must not call cudaMalloc because an allocation can synchronise the
+// whole device and stall its other streams.  For them sr_compose_device_static runs the same filter
+// as sr_compose_device but keeps its packed planes in the fixed array below instead of a context
+// buffer, and evaluates the spatial weights inline instead of uploading a weight table.
+//
+// Limits: the array is kStaticScratchBytes (32 MiB) on every GPU that loads the library, held until
+// the process exits.  The image is filtered in bands of rows, each band packed together with its
+// filter halo; a call fails when even a one-row band with its halo does not fit, i.e. when
+// (2 * max(radius, fog radius) + 2) * width * 48 bytes exceeds 32 MiB.  All calls share the array:
+// two calls that overlap on the GPU (e.g. on different streams) overwrite each other's bands and
+// produce wrong images, so serialise them.  Every band is packed before it is read, so the array
+// needs no clearing between calls.
+static constexpr size_t kStaticScratchBytes = size_t(32) << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+// Device address of g_static_scratch, resolved once per device with that device current.
+static constexpr int kMaxDevices = 64;
+static float4* g_static_scratch_addr[kMaxDevices];
+
+static cudaError_t static_scratch(int device, float4** out) {
+    if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+    if (!g_static_scratch_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return e;
+        g_static_scratch_addr[device] = (float4*)p;
+    }
+    *out = g_static_scratch_addr[device];
+    return cudaSuccess;
+}
+
+// Packs image rows [row0, row0 + rows) into band-local planes.
+__global__ void k_pack_band(DevAovs in, uint32_t width, uint32_t row0, uint32_t rows, float4* p_rad, float4* p_geo,
+                            float4* p_fog) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= width * rows) return;
+    size_t g = (size_t)row0 * width + i;
+    Col r{in.radiance[3 * g], in.radiance[3 * g + 1], in.radiance[3 * g + 2]};
+    p_rad[i] = make_float4(r.r, r.g, r.b, luminance(r));
+    p_geo[i] = make_float4(in.normals[3 * g], in.normals[3 * g + 1], in.normals[3 * g + 2], in.depth[g]);
+    p_fog[i] = make_float4(in.radiance_fog[3 * g], in.radiance_fog[3 * g + 1], in.radiance_fog[3 * g + 2], 0.0f);
+}
+
+// Largest |kx| with kx^2 + ky^2 <= r^2 (the circular-kernel test of compose.cs:147-148).
+__device__ __forceinline__ int half_width(int r, int ky) {
+    int hw = (int)sqrtf((float)(r * r - ky * ky));
+    while (hw > 0 && hw * hw + ky * ky > r * r) --hw;
+    while ((hw + 1) * (hw + 1) + ky * ky <= r * r) ++hw;
+    return hw;
+}
+
+// k_compose for output rows [y0, y1) reading band planes that start at image row `prow0`; spatial
+// weights are evaluated per tap as the reference does (compose.cs:160, 236).
+__global__ void __launch_bounds__(128) k_compose_band(const float4* __restrict__ p_rad, const float4* __restrict__ p_geo,
+                                                      const float4* __restrict__ p_fog, const float* __restrict__ variance,
+                                                      uint32_t width, uint32_t height, uint32_t y0, uint32_t y1,
+                                                      uint32_t prow0, ComposeConsts k, float rp_inv, float rpf_inv,
+                                                      float fog_strength, uint8_t* rgb8) {
+    int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    int y = (int)y0 + blockIdx.y * 4 + (threadIdx.x >> 5);
+    if (x >= (int)width || y >= (int)y1) return;
+    size_t li = (size_t)(y - (int)prow0) * width + x;
+    float4 c0 = __ldg(p_rad + li);
+    Col main = col3(c0);
+    Col fog = col3(__ldg(p_fog + li));
+    float4 c1 = __ldg(p_geo + li);
+    V3 cn = v3(c1);
+    float cd = c1.w;
+    bool has_n = mag_sqr(cn) > 0.0f;
+    bool has_d = !isinf(cd);
+    float lum = c0.w;
+    float boost = 1.0f + lum * k.lum_boost;
+    float dw = fminf(__ldg(variance + (size_t)y * width + x) * boost * k.strength, k.strength_max);
+    if (!(dw < 1e-4f)) {
+        int R = k.radius;
+        float wsum = 1.0f;
+        Col rsum = main;
+        int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
+        for (int ky = ky0; ky <= ky1; ++ky) {
+            int hw = half_width(R, ky);
+            int kx0 = max(-hw, -x), kx1 = min(hw, (int)width - 1 - x);
+            const float4* prow = p_rad + (size_t)(y + ky - (int)prow0) * width + x;
+            const float4* grow = p_geo + (size_t)(y + ky - (int)prow0) * width + x;
+            for (int kx = kx0; kx <= kx1; ++kx) {
+                if (kx == 0 && ky == 0) continue;
+                float4 q1 = __ldg(grow + kx);
+                V3 nn = v3(q1);
+                bool nh_n = mag_sqr(nn) > 0.0f;
+                bool nh_d = !isinf(q1.w);
+                if (has_n != nh_n || has_d != nh_d) continue;
+                float4 q0 = __ldg(prow + kx);
+                float kd = (float)(kx * kx + ky * ky);
+                float w = dw * sr_exp(-kd * rp_inv);
+                if (has_n && w > 0.0f) {
+                    V3 nd = cn - nn;
+                    w *= sr_exp(-mag_sqr(nd) * k.normal_limit_inv);
+                }
+                if (has_d && w > 0.0f) {
+                    float dd = cd - q1.w;
+                    w *= sr_exp(-(dd * dd) * k.depth_limit_inv);
+                }
+                if (w > 0.0f) {
+                    float ld = fmaxf(0.0f, q0.w - lum);
+                    w *= sr_exp(-(ld * ld) * k.lum_limit_inv);
+                }
+                wsum += w;
+                rsum = rsum + col3(q0) * w;
+            }
+        }
+        main = rsum / wsum;
+    }
+    {
+        int R = k.fog_radius;
+        float wsum = 1.0f;
+        Col rsum = fog;
+        int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
+        for (int ky = ky0; ky <= ky1; ++ky) {
+            int hw = half_width(R, ky);
+            int kx0 = max(-hw, -x), kx1 = min(hw, (int)width - 1 - x);
+            const float4* frow = p_fog + (size_t)(y + ky - (int)prow0) * width + x;
+            for (int kx = kx0; kx <= kx1; ++kx) {
+                if (kx == 0 && ky == 0) continue;
+                float kd = (float)(kx * kx + ky * ky);
+                float w = fog_strength * sr_exp(-kd * rpf_inv);
+                wsum += w;
+                rsum = rsum + col3(__ldg(frow + kx)) * w;
+            }
+        }
+        fog = rsum / wsum;
+    }
+    tonemap(k, main + fog, rgb8 + ((size_t)y * width + x) * 3);
+}
+
+cudaError_t launch_compose_static(int device, const DevAovs& in, uint32_t width, uint32_t height,
+                                  const ComposeConsts& k, float rp_inv, float rpf_inv, float fog_strength,
+                                  uint8_t* rgb8, cudaStream_t stream, size_t* needed_bytes) {
+    uint32_t halo = (uint32_t)(k.radius > k.fog_radius ? k.radius : k.fog_radius);
+    const size_t row_bytes = (size_t)width * 3 * sizeof(float4);
+    size_t rows_cap = kStaticScratchBytes / row_bytes;
+    *needed_bytes = (size_t)(2 * halo + 2) * row_bytes;
+    if (rows_cap < 2 * (size_t)halo + 2) return cudaErrorInvalidValue;  // caller reports the limit
+    float4* base = nullptr;
+    cudaError_t e = static_scratch(device, &base);
+    if (e != cudaSuccess) return e;
+    uint32_t band = (uint32_t)(rows_cap - 2 * halo);
+    for (uint32_t y0 = 0; y0 < height; y0 += band) {
+        uint32_t y1 = y0 + band < height ? y0 + band : height;
+        uint32_t p0 = y0 > halo ? y0 - halo : 0;
+        uint32_t p1 = y1 + halo < height ? y1 + halo : height;
+        uint32_t prows = p1 - p0;
+        size_t plane = (size_t)prows * width;
+        float4* p_rad = base;
+        float4* p_geo = base + plane;
+        float4* p_fog = base + 2 * plane;
+        k_pack_band<<<(unsigned)((plane + 255) / 256), 256, 0, stream>>>(in, width, p0, prows, p_rad, p_geo, p_fog);
+        dim3 grid((width + 31) / 32, (y1 - y0 + 3) / 4);
+        k_compose_band<<<grid, 128, 0, stream>>>(p_rad, p_geo, p_fog, in.variance, width, height, y0, y1, p0, k,
+                                                 rp_inv, rpf_inv, fog_strength, rgb8);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 }  // namespace sr

@@ -1017,6 +1017,46 @@ SR_API int sr_compose_device(SrContext* ctx, const SrAovs* a, uint32_t w, uint32
     return compose_impl(ctx, d, w, h, p, true, device_rgb8, st);
 }
 
+SR_API int sr_compose_device_static(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p,
+                                    uint8_t* device_rgb8, void* stream) {
+    if (!ctx || !a || !p || !device_rgb8) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!a->radiance || !a->radiance_fog || !a->normals || !a->depth || !a->variance)
+        return fail(SR_ERR_INVALID_ARG, "compose needs radiance, radiance_fog, normals, depth and variance");
+    if (ctx->device < 0) return fail(SR_ERR_STATE, "host-only context (device -1) cannot run device work");
+    if (w == 0 || h == 0) return fail(SR_ERR_INVALID_ARG, "empty image");
+    if (p->tonemapper != SR_TONEMAP_REINHARD && p->tonemapper != SR_TONEMAP_LINEAR_SMOOTH)
+        return fail(SR_ERR_INVALID_ARG, "Unknown tonemapper: %d", p->tonemapper);
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    ComposeConsts k;
+    k.tonemapper = p->tonemapper;
+    k.exposure = p->exposure;
+    k.strength = p->denoise_strength;
+    k.strength_max = p->denoise_strength_max;
+    k.lum_boost = p->denoise_luminance_boost;
+    k.lum_limit_inv = 1.0f / (p->denoise_luminance_limit * p->denoise_luminance_limit * 2.0f);
+    k.normal_limit_inv = 1.0f / (p->denoise_normal_limit * p->denoise_normal_limit * 2.0f);
+    k.depth_limit_inv = 1.0f / (p->denoise_depth_limit * p->denoise_depth_limit * 2.0f);
+    float area_sqrt = std::sqrt((float)(int)(w * h));
+    float rp = p->denoise_radius * area_sqrt;
+    float rpf = p->denoise_fog_radius * area_sqrt;
+    k.radius = (int)std::ceil(rp * 3.0f);
+    k.fog_radius = (int)std::ceil(rpf * 3.0f);
+    if (k.radius < 0 || k.fog_radius < 0 || k.radius > 4096 || k.fog_radius > 4096)
+        return fail(SR_ERR_INVALID_ARG, "denoise radius out of range");
+    DevAovs d{a->radiance, a->radiance_fog, a->normals, a->uv, a->depth, a->samples, a->variance};
+    size_t needed = 0;
+    cudaError_t e = launch_compose_static(ctx->device, d, w, h, k, 1.0f / (rp * rp * 2.0f), 1.0f / (rpf * rpf * 2.0f),
+                                          p->denoise_fog_strength, device_rgb8, st, &needed);
+    if (e == cudaErrorInvalidValue)
+        return fail(SR_ERR_INVALID_ARG,
+                    "sr_compose_device_static: a %u-pixel-wide image with filter radius %d needs %zu bytes of "
+                    "scratch per band, more than the fixed 33554432-byte scratch array",
+                    w, k.radius > k.fog_radius ? k.radius : k.fog_radius, needed);
+    SR_CUDA(e, "compose (static scratch)");
+    return SR_OK;
+}
+
 static int compose_host(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p,
                         uint8_t* rgb, bool denoise) {
     if (!ctx || !a || !rgb || !a->radiance || !a->radiance_fog) return fail(SR_ERR_INVALID_ARG, "NULL argument");

@@ -39,4 +39,11 @@ cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, c
                            const float* spatial, const float* fog_spatial, bool denoise, uint8_t* rgb8,
                            float4* scratch, cudaStream_t stream);
 
+// Compositing that allocates nothing: packed planes live in a fixed device array of sr_compose.cu
+// (bands of rows); spatial weights are evaluated per tap.  Returns cudaErrorInvalidValue when the
+// image is too wide for the array (needed_bytes then holds the size one band would need).
+cudaError_t launch_compose_static(int device, const DevAovs& in, uint32_t width, uint32_t height,
+                                  const ComposeConsts& k, float rp_inv, float rpf_inv, float fog_strength,
+                                  uint8_t* rgb8, cudaStream_t stream, size_t* needed_bytes);
+
 }  // namespace sr
