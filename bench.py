@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=0, help="render mode: 0 auto, 1 megakernel, 2 wavefront, 3 graph")
     ap.add_argument("--variants", action="store_true", help="also time every render mode once")
+    ap.add_argument("--profile-once", action="store_true",
+                    help="set up, render + compose exactly once, exit (for ncu captures)")
     return ap.parse_args()
 
 
@@ -121,6 +123,13 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def aggregate(samples_per_rank_step: int, steps: int, world: int, rank_seconds: float, reduce_max=None) -> tuple:
+    """Whole-job throughput of `world` replicas that each render `steps` frames: the slowest rank's
+    time (max over ranks via `reduce_max`) over all ranks' samples.  Returns (value, seconds)."""
+    t = reduce_max(rank_seconds) if (reduce_max is not None and world > 1) else rank_seconds
+    return samples_per_rank_step * steps * world / t, t
 
 
 def algorithmic_bytes(c: dict, pixels: int) -> int:
@@ -236,6 +245,14 @@ def run_ours(args):
         _abi.check(lib.sr_compose_device(ctx.handle, C.byref(aovs), W, H, C.byref(cparams),
                                          C.c_void_p(rgb.data_ptr()), sp))
 
+    if args.profile_once:
+        render()
+        compose()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
     # work counters of one render (untimed) -> algorithmic bytes per launch
     scene.set_counting(True)
     render()
@@ -268,12 +285,13 @@ def run_ours(args):
         torch.distributed.barrier()
     step_ms = [a.elapsed_time(c) for a, _, c in ev]
     render_ms = [a.elapsed_time(b) for a, b, _ in ev]
-    total_s = sum(step_ms) / 1000.0
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda")
+
+    def reduce_max(x: float) -> float:
+        t = torch.tensor([x], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    value = samples_per_step * args.steps * world / total_s
+        return float(t.item())
+
+    value, total_s = aggregate(samples_per_step, args.steps, world, sum(step_ms) / 1000.0, reduce_max)
 
     variants = None
     if args.variants:
@@ -308,12 +326,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         render_compose(scene, desc.view, *desc.render_args(), comp, aovs=host, image=img)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = samples_per_step * e2e_steps * world / e2e_s
+    e2e_value, e2e_s = aggregate(samples_per_step, e2e_steps, world, time.perf_counter() - t0, reduce_max)
     d2h = n * (12 + 12 + 12 + 8 + 4 + 4 + 4) + n * 3
 
     # kernels of one timed step: the render's own launches (reported by the library) + compose (2)
@@ -324,10 +337,10 @@ def run_ours(args):
     kern_s = statistics.mean(render_ms) / 1000.0
     achieved = alg / kern_s / 1e9
     traffic = None
-    tf = ROOT / "profiles" / "render_c2_traffic.json"
-    if tf.exists():
+    tf = ROOT / "profiles" / "path_tracer_c2_traffic.json"
+    if tf.exists() and (W, H, desc.spp) == (1920, 1080, 64):
         try:
-            traffic = json.loads(tf.read_text()).get("traffic_bytes_per_launch")
+            traffic = json.loads(tf.read_text()).get("traffic_bytes_per_frame")
         except Exception:
             traffic = None
 
@@ -354,8 +367,12 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": H2D_PARAM_BYTES,
                     "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "kernel": "k_render_pixels",
-                         "kernel_ms": 1000 * kern_s, "alg_bytes_per_launch": alg, "peak_source": peak_kind},
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": ("path tracer: k_render_pixels" if args.mode == 1 else
+                                    "path tracer: k_wave_extend/shade/shadow/finalize (one frame)"),
+                         "kernel_ms": 1000 * kern_s, "alg_bytes_per_launch": alg, "peak_source": peak_kind,
+                         "note": "per frame of the path tracer; alg bytes from the kernels' own work "
+                                 "counters sized by the reference's records"},
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "render_mode": {0: "auto (wavefront graph)", 1: "megakernel", 2: "wavefront host loop",

@@ -28,6 +28,20 @@ static __device__ __noinline__ float sr_pow(float x, float y) { return powf(x, y
 static __device__ __noinline__ float sr_atan2(float y, float x) { return atan2f(y, x); }
 static __device__ __noinline__ float sr_asin(float x) { return asinf(x); }
 
+// IEEE division and square root expand to ~17 instructions per call site; with SR_OUTLINE_DIV the
+// vector helpers below share one out-of-line copy of each (same correctly rounded results), which
+// keeps the shading kernels' machine code small enough for the instruction cache.
+#ifndef SR_OUTLINE_DIV
+#define SR_OUTLINE_DIV 0
+#endif
+#if SR_OUTLINE_DIV
+static __device__ __noinline__ float sr_fdiv(float a, float b) { return a / b; }
+static __device__ __noinline__ float sr_fsqrt(float a) { return sqrtf(a); }
+#else
+static __device__ __forceinline__ float sr_fdiv(float a, float b) { return a / b; }
+static __device__ __forceinline__ float sr_fsqrt(float a) { return sqrtf(a); }
+#endif
+
 // ---- small vector types ------------------------------------------------------------------------
 struct V2 {
     float x, y;
@@ -50,16 +64,16 @@ SR_DEV V3 operator-(V3 v) { return {-v.x, -v.y, -v.z}; }
 SR_DEV V3 operator*(V3 a, float b) { return {a.x * b, a.y * b, a.z * b}; }
 SR_DEV V3 operator*(float a, V3 b) { return {a * b.x, a * b.y, a * b.z}; }
 SR_DEV V3 operator*(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-SR_DEV V3 operator/(V3 a, float b) { return {a.x / b, a.y / b, a.z / b}; }
-SR_DEV V3 operator/(V3 a, V3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+SR_DEV V3 operator/(V3 a, float b) { return {sr_fdiv(a.x, b), sr_fdiv(a.y, b), sr_fdiv(a.z, b)}; }
+SR_DEV V3 operator/(V3 a, V3 b) { return {sr_fdiv(a.x, b.x), sr_fdiv(a.y, b.y), sr_fdiv(a.z, b.z)}; }
 SR_DEV float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 SR_DEV V3 cross(V3 a, V3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
 SR_DEV float mag_sqr(V3 v) { return dot(v, v); }
-SR_DEV float magnitude(V3 v) { return sqrtf(mag_sqr(v)); }
+SR_DEV float magnitude(V3 v) { return sr_fsqrt(mag_sqr(v)); }
 SR_DEV V3 normalize(V3 v) { return v / magnitude(v); }
 SR_DEV V3 normalize_or(V3 v, V3 fb) {
     float m = mag_sqr(v);
-    return m >= 1e-12f ? v / sqrtf(m) : fb;
+    return m >= 1e-12f ? v / sr_fsqrt(m) : fb;
 }
 SR_DEV V3 up3() { return {0.f, 1.f, 0.f}; }
 SR_DEV V3 right3() { return {1.f, 0.f, 0.f}; }
@@ -73,8 +87,8 @@ SR_DEV Col operator-(Col a, Col b) { return {a.r - b.r, a.g - b.g, a.b - b.b}; }
 SR_DEV Col operator*(Col a, Col b) { return {a.r * b.r, a.g * b.g, a.b * b.b}; }
 SR_DEV Col operator*(Col c, float s) { return {c.r * s, c.g * s, c.b * s}; }
 SR_DEV Col operator*(float s, Col c) { return {c.r * s, c.g * s, c.b * s}; }
-SR_DEV Col operator/(Col c, float s) { return {c.r / s, c.g / s, c.b / s}; }
-SR_DEV Col operator/(Col a, Col b) { return {a.r / b.r, a.g / b.g, a.b / b.b}; }
+SR_DEV Col operator/(Col c, float s) { return {sr_fdiv(c.r, s), sr_fdiv(c.g, s), sr_fdiv(c.b, s)}; }
+SR_DEV Col operator/(Col a, Col b) { return {sr_fdiv(a.r, b.r), sr_fdiv(a.g, b.g), sr_fdiv(a.b, b.b)}; }
 SR_DEV Col gray(float v) { return {v, v, v}; }
 SR_DEV Col black() { return {0.f, 0.f, 0.f}; }
 SR_DEV Col white() { return {1.f, 1.f, 1.f}; }
@@ -872,7 +886,20 @@ SR_DEV float specular_probability(const Surface& s, V3 view) {
     float f = luminance(fresnel(ndv, base_reflectivity(s.f0, s.albedo, s.metallic)));
     return clampf(fmaxf(f, s.metallic), 0.001f, 0.999f);
 }
-SR_DEV Col opaque_eval(const Surface& s, V3 view, V3 light) {
+// Surface.OpaqueEval / OpaquePdf are evaluated for the light sample and again for the scattered
+// direction.  SR_NOINLINE_BRDF = 1 compiles one out-of-line copy each (smaller shading kernels);
+// it stays off: with it the megakernel recorded wrong primary-hit depths in a transparent/fog
+// scene on this toolchain (caught by the render-mode identity test), while the inlined build
+// matches the oracle bit for bit.
+#ifndef SR_NOINLINE_BRDF
+#define SR_NOINLINE_BRDF 0
+#endif
+#if SR_NOINLINE_BRDF
+#define SR_BRDF static __device__ __noinline__
+#else
+#define SR_BRDF SR_DEV
+#endif
+SR_BRDF Col opaque_eval(const Surface& s, V3 view, V3 light) {
     float ndl = dot(s.normal, light);
     if (ndl <= 0.0f) return black();
     float ndv = fmaxf(1e-4f, dot(s.normal, view));
@@ -887,7 +914,7 @@ SR_DEV Col opaque_eval(const Surface& s, V3 view, V3 light) {
     Col diff = (white() - fresnel(ndv, base)) * s.albedo * (1.0f - s.metallic) * (ndl / kPi);
     return (spec + diff) * (1.0f - s.transparency);
 }
-SR_DEV float opaque_pdf(const Surface& s, V3 view, V3 light, float spec_p) {
+SR_BRDF float opaque_pdf(const Surface& s, V3 view, V3 light, float spec_p) {
     float ndl = dot(s.normal, light);
     if (ndl <= 0.0f) return 0.0f;
     V3 half = normalize_or(view + light, s.normal);

@@ -241,61 +241,66 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
             SurfHit sh;
             if (has_hit) surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
             float sdist;
-            if (S.has_fog && fog_scatter_distance(S, ray, has_hit ? sh.dist : inf, rng, sdist)) {
-                // fog scatter: NEE toward the sky is deferred to resolve (scene.cs:659-683)
-                energy = energy * col3(S.fog_color);
-                V3 pos = ray_at(ray, sdist);
-                V3 ldir;
-                float lpdf;
-                if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
-                    float fog_pdf = hg_pdf(dot(ray.d, ldir), S.fog_g);
-                    float mis = power_heuristic(lpdf, fog_pdf);
-                    rflags |= RF_SHADOW | (bounce == 0 ? RF_FOG : 0u);
-                    W.sh0[s] = make_float4(pos.x, pos.y, pos.z, 0.f);
-                    W.sh1[s] = make_float4(ldir.x, ldir.y, ldir.z, lpdf);
-                    W.sh2[s] = make_float4(fog_pdf, fog_pdf, fog_pdf, mis);
-                    W.sh3[s] = make_float4(energy.r, energy.g, energy.b, 0.f);
-                }
-                if (russian_roulette(energy, bounce, rng)) {
-                    rflags |= RF_TERMINATE;
-                } else {
-                    V3 sdir = hg_scatter_dir(ray.d, S.fog_g, rng);
-                    pflags |= PF_SPDF;
-                    spdf = hg_pdf(dot(ray.d, sdir), S.fog_g);
-                    ray = make_ray(ray_at(ray, sdist), sdir);
-                }
-            } else if (has_hit) {
-                // surface (scene.cs:684-727)
+            // Event of this segment (scene.cs:654-738): fog scatter (free-flight distance drawn first
+            // when fog is set), surface hit, or miss.  Fog and surface events share one light sample,
+            // one Russian-roulette draw and then scatter, in that RNG order, so those calls exist once.
+            bool fog_event = S.has_fog && fog_scatter_distance(S, ray, has_hit ? sh.dist : inf, rng, sdist);
+            if (fog_event || has_hit) {
                 const Surface& su = sh.surf;
-                float dist = sh.dist;
-                V3 view = -ray.d;
-                float bias = fmaxf(1e-4f, dist * 1e-4f);
-                V3 pos = ray_at(ray, dist - bias);
-                if (GENERAL && (pflags & PF_MEDIUM)) energy = energy * beer_law(col3(W.medium[s]), dist);
-                radiance = radiance + su.radiance * energy;
-                if (bounce == 0) {
-                    pflags |= PF_PRIMARY;
-                    W.prim[s] = make_float4(su.normal.x, su.normal.y, su.normal.z, dist);
-                    W.prim_uv[s] = make_float2(su.uv.x, su.uv.y);
+                const float dist = sh.dist;
+                const V3 view = -ray.d;
+                float bias = 0.0f;
+                V3 pos;
+                if (fog_event) {
+                    energy = energy * col3(S.fog_color);
+                    pos = ray_at(ray, sdist);
+                } else {
+                    bias = fmaxf(1e-4f, dist * 1e-4f);
+                    pos = ray_at(ray, dist - bias);
+                    if (GENERAL && (pflags & PF_MEDIUM)) energy = energy * beer_law(col3(W.medium[s]), dist);
+                    radiance = radiance + su.radiance * energy;
+                    if (bounce == 0) {
+                        pflags |= PF_PRIMARY;
+                        W.prim[s] = make_float4(su.normal.x, su.normal.y, su.normal.z, dist);
+                        W.prim_uv[s] = make_float2(su.uv.x, su.uv.y);
+                    }
                 }
+                // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
+                // the shadow ray and the contribution are deferred
                 V3 ldir;
                 float lpdf;
                 if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
-                    V3 nn = dot(su.normal, view) >= 0.0f ? su.normal : -su.normal;
-                    V3 ng = dot(su.normal_geo, view) >= 0.0f ? su.normal_geo : -su.normal_geo;
-                    if (dot(nn, ldir) > 0.0f && dot(ng, ldir) > 0.0f) {
-                        Col refl = opaque_eval(su, view, ldir);
-                        float sp = opaque_pdf(su, view, ldir, specular_probability(su, view));
-                        float mis = power_heuristic(lpdf, sp);
-                        rflags |= RF_SHADOW;
+                    bool emit = true;
+                    Col w3;
+                    float mis;
+                    if (fog_event) {
+                        float fog_pdf = hg_pdf(dot(ray.d, ldir), S.fog_g);
+                        mis = power_heuristic(lpdf, fog_pdf);
+                        w3 = gray(fog_pdf);
+                    } else {
+                        V3 nn = dot(su.normal, view) >= 0.0f ? su.normal : -su.normal;
+                        V3 ng = dot(su.normal_geo, view) >= 0.0f ? su.normal_geo : -su.normal_geo;
+                        emit = dot(nn, ldir) > 0.0f && dot(ng, ldir) > 0.0f;
+                        if (emit) {
+                            w3 = opaque_eval(su, view, ldir);
+                            mis = power_heuristic(lpdf, opaque_pdf(su, view, ldir, specular_probability(su, view)));
+                        }
+                    }
+                    if (emit) {
+                        rflags |= RF_SHADOW | ((fog_event && bounce == 0) ? RF_FOG : 0u);
                         W.sh0[s] = make_float4(pos.x, pos.y, pos.z, 0.f);
                         W.sh1[s] = make_float4(ldir.x, ldir.y, ldir.z, lpdf);
-                        W.sh2[s] = make_float4(refl.r, refl.g, refl.b, mis);
+                        W.sh2[s] = make_float4(w3.r, w3.g, w3.b, mis);
                         W.sh3[s] = make_float4(energy.r, energy.g, energy.b, 0.f);
                     }
                 }
                 if (russian_roulette(energy, bounce, rng)) {
                     rflags |= RF_TERMINATE;
+                } else if (fog_event) {
+                    V3 sdir = hg_scatter_dir(ray.d, S.fog_g, rng);
+                    pflags |= PF_SPDF;
+                    spdf = hg_pdf(dot(ray.d, sdir), S.fog_g);
+                    ray = make_ray(pos, sdir);
                 } else {
                     Scatter sc = surface_scatter<GENERAL>(su, ray.d, view, rng);
                     energy = energy * sc.weight;
