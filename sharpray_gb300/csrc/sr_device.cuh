@@ -378,31 +378,34 @@ struct Hit {
 };
 
 // Scene-level closest hit (ANY = false) or occlusion test (ANY = true) as ONE loop over a shared
-// stack (SceneQuery below).  The reference nests two traversals: Bvh<Object>.Intersect (bvh.cs:165-216) calls, for each
-// object of a scene-BVH leaf, Object.Intersect (math.cs:67-79) which runs a complete, unpruned mesh
-// BVH traversal in the object's local space.  Here the mesh traversal of the current object pushes
-// its entries above the scene entries (above `blas_base`); the loop swaps the traversal ray and the
-// pruning distance when it enters and leaves an object, so every iteration is one node-pair test or
-// one leaf, whichever level a lane is in, and lanes of a warp stay in the same loop.  Visit order,
-// pruning (`t >= best`, `t <= best`), tie-breaking (first strictly closer hit) and the per-object
-// comparison `hit.Dist / localRayScale < bestDist` are the reference's, so results are bit-exact.
-// With ANY the search stops at the first hit found and prunes nothing, which gives the same yes/no
-// answer as the closest-hit query.
-constexpr int kSceneStack = 192;
-// SR_LEAF_LOOP = 1 tests a whole mesh leaf in one step; 0 tests one triangle per step (more uniform
-// step lengths across the lanes of a warp).
-#ifndef SR_LEAF_LOOP
-#define SR_LEAF_LOOP 1
-#endif  // scene (<= 65) + mesh (<= 65) entries, with margin
+// stack (SceneQuery below).  The reference nests two traversals: Bvh<Object>.Intersect
+// (bvh.cs:165-216) calls, for each object of a scene-BVH leaf, Object.Intersect (math.cs:67-79)
+// which runs a complete, unpruned mesh BVH traversal in the object's local space.  Here the mesh
+// traversal of the current object pushes its entries above the scene entries (above `mesh_base`);
+// the query swaps the traversal ray and the pruning distance when it enters and leaves an object.
+// Visit order, pruning (`t >= best` on pop, `t <= best` on push), tie-breaking (first strictly
+// closer hit) and the per-object comparison `hit.Dist / localRayScale < bestDist` are the
+// reference's, so results are bit-exact.  With ANY the search stops at the first hit found and
+// prunes nothing, which gives the same yes/no answer as the closest-hit query.
+constexpr int kSceneStack = 192;  // scene (<= 65) + mesh (<= 65) entries, with margin
 
-// Resumable traversal state: init() starts a ray, step() performs one loop iteration (one node-pair
-// test, one triangle test, or entering an object) and returns true when the query is answered
-// (`best` then holds the result).  Callers either run it to completion or interleave rays on a lane
-// (persistent kernels replace a finished ray at once).  GENERAL = false compiles only what scenes of
-// meshes need (no analytic shapes).
+// Resumable traversal state.  init() starts a ray; the query is then a sequence of actions, each
+// chosen by `state`:
+//   QS_NODE : visit the next node -- the nearer child kept from the last visit (the reference
+//             pushes it last and pops it next, so it never needs to go through the stack) or the
+//             stack top; an interior node tests its two children, a leaf moves to QS_TRI / QS_OBJ
+//   QS_TRI  : test the triangles of a mesh leaf (bvh.cs:203-212)
+//   QS_OBJ  : enter the next object of a scene leaf (to its local ray and mesh root)
+//   QS_EXIT : an object's mesh traversal is complete: compare its hit with the scene's best
+//   QS_DONE : `best` holds the answer
+// Node actions and leaf actions are separate so that persistent kernels can run the node actions
+// of all lanes together and batch the (long, divergent) leaf actions.  GENERAL = false compiles
+// only what scenes of meshes need (no analytic shapes).
+enum : int { QS_NODE = 0, QS_TRI = 1, QS_OBJ = 2, QS_EXIT = 3, QS_DONE = 4 };
+
 template <bool ANY, bool GENERAL>
 struct SceneQuery {
-    // The traversal stack lives outside the struct (a separate local array passed to init/step):
+    // The traversal stack lives outside the struct (a separate local array passed to the actions):
     // keeping the dynamically indexed array out lets the scalar state stay in registers.
     Ray wr;              // world ray
     Ray cr;              // ray of the current level (world, or the current object's local ray)
@@ -410,11 +413,13 @@ struct SceneQuery {
     float lscale;        // local-ray scale of the current object
     float ob_u, ob_v;    // best hit inside the current object
     Hit best;
+    StackEntry node;     // next node to visit when has_node (instead of the stack top)
     int sp, mesh_base, leaf_next, leaf_left, tri_next, tri_left, obj_pos, ob_tri;
     uint32_t pops;
-    bool in_mesh;
+    int state;
+    bool in_mesh, has_node;
 
-    SR_DEV void init(const DevScene& S, const Ray& r, StackEntry* stack) {
+    SR_DEV void init(const DevScene& S, const Ray& r) {
         const float inf = __int_as_float(0x7f800000);
         best = Hit{-1, -1, inf, 0.f, 0.f, 0.f};
         wr = r;
@@ -427,91 +432,46 @@ struct SceneQuery {
         pops = 0;
         in_mesh = false;
         sp = 0;
+        has_node = false;
+        state = QS_DONE;
         if (S.tlas_root >= 0) {
             float4 rn0 = ldg4(S.nodes + 2 * S.tlas_root);
             float4 rn1 = ldg4(S.nodes + 2 * S.tlas_root + 1);
-            stack[0] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
-            sp = 1;
+            node = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+            has_node = true;
+            state = QS_NODE;
         }
     }
 
-    template <bool COUNT>
-    SR_DEV bool step(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
-        const float inf = __int_as_float(0x7f800000);
+    // The action after the current one, in the reference's order: finish the current mesh, then
+    // the remaining objects of the current scene leaf, then the stack.
+    SR_DEV void next_state() {
+        if (in_mesh)
+            state = (has_node || sp > mesh_base) ? QS_NODE : QS_EXIT;
+        else if (leaf_left > 0)
+            state = QS_OBJ;
+        else
+            state = (has_node || sp > 0) ? QS_NODE : QS_DONE;
+    }
+
+    SR_DEV bool count_action(uint32_t* err) {
         if (++pops > kMaxPops) {
             atomicOr(err, SR_DEVERR_LOOP);
-            return true;
-        }
-        if (tri_left > 0) {
-            // one triangle of the current mesh leaf, in leaf order (bvh.cs:203-212)
-            const float4* tp = S.tris + 3 * tri_next;
-            float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
-            float t, u, v;
-            if (tri_hit(v3(q0), v3(q1), v3(q2), cr, t, u, v) && (ANY || t < cur_best)) {
-                if (ANY) {
-                    best = {obj_pos, tri_next, 0.f, 0.f, 0.f, 0.f};
-                    return true;
-                }
-                cur_best = t;
-                ob_tri = tri_next;
-                ob_u = u;
-                ob_v = v;
-            }
-            ++tri_next;
-            --tri_left;
+            state = QS_DONE;
             return false;
         }
-        if (in_mesh && sp == mesh_base) {
-            // the object's mesh traversal is complete: Bvh<Object> leaf comparison (bvh.cs:207)
-            if (ob_tri >= 0) {
-                float d = cur_best / lscale;
-                if (d < best.dist) best = {obj_pos, ob_tri, d, cur_best, ob_u, ob_v};
-            }
-            in_mesh = false;
-            cr = wr;
-            cur_best = ANY ? inf : best.dist;
+        return true;
+    }
+
+    template <bool COUNT>
+    SR_DEV void node_action(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
+        if (!count_action(err)) return;
+        StackEntry e = has_node ? node : stack[--sp];
+        has_node = false;
+        if (!ANY && e.t >= cur_best) {
+            next_state();
+            return;
         }
-        if (!in_mesh && leaf_left > 0) {
-            const DevObject& o = S.objects[leaf_next];
-            obj_pos = leaf_next;
-            ++leaf_next;
-            --leaf_left;
-            Ray l = to_local(o, wr, lscale);
-            int kind = GENERAL ? __float_as_int(o.pos_kind.w) : SR_SHAPE_MESH;
-            if (kind == SR_SHAPE_MESH) {
-                int root = __float_as_int(o.scale_root.w);
-                if (root < 0) return false;  // empty mesh never hits
-                if (sp >= kSceneStack) {
-                    atomicOr(err, SR_DEVERR_STACK);
-                    return true;
-                }
-                float4 rn0 = ldg4(S.nodes + 2 * root);
-                float4 rn1 = ldg4(S.nodes + 2 * root + 1);
-                mesh_base = sp;
-                stack[sp++] = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
-                in_mesh = true;
-                cr = l;
-                cur_best = inf;
-                ob_tri = -1;
-            } else if (GENERAL) {
-                ShapeHit h;
-                bool ok = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, l, h, false)
-                                                  : box_hit(o.shape0, o.shape1, l, h, false);
-                if (ok) {
-                    if (ANY) {
-                        best = {obj_pos, -1, 0.f, 0.f, 0.f, 0.f};
-                        return true;
-                    }
-                    float d = h.dist / lscale;
-                    if (d < best.dist) best = {obj_pos, -1, d, 0.f, 0.f, 0.f};
-                    cur_best = best.dist;
-                }
-            }
-            return false;
-        }
-        if (sp == 0) return true;
-        StackEntry e = stack[--sp];
-        if (!ANY && e.t >= cur_best) return false;
         if (e.count == 0) {
             if (in_mesh)
                 SR_COUNT(c, SR_COUNTER_BLAS_NODE, 2);
@@ -522,32 +482,43 @@ struct SceneQuery {
             float ta = 0.f, tb = 0.f;
             bool pa = slab(a0, a1, cr, ta) && (ANY || ta <= cur_best);
             bool pb = slab(b0, b1, cr, tb) && (ANY || tb <= cur_best);
-            if (sp + 2 > kSceneStack) {
-                atomicOr(err, SR_DEVERR_STACK);
-                return true;
-            }
             StackEntry ea{__float_as_int(a0.w), __float_as_int(a1.w), ta};
             StackEntry eb{__float_as_int(b0.w), __float_as_int(b1.w), tb};
             if (pa && pb) {
-                // the nearer child is popped first; on a tie the second child is (bvh.cs:196-197)
-                if (ta < tb) {
-                    stack[sp++] = eb;
-                    stack[sp++] = ea;
-                } else {
-                    stack[sp++] = ea;
-                    stack[sp++] = eb;
+                // the nearer child is visited first; on a tie the second child is (bvh.cs:196-197)
+                if (sp + 1 > kSceneStack) {
+                    atomicOr(err, SR_DEVERR_STACK);
+                    state = QS_DONE;
+                    return;
                 }
-            } else if (pa) {
-                stack[sp++] = ea;
-            } else if (pb) {
-                stack[sp++] = eb;
+                bool a_first = ta < tb;
+                stack[sp++] = a_first ? eb : ea;
+                node = a_first ? ea : eb;
+                has_node = true;
+            } else if (pa || pb) {
+                node = pa ? ea : eb;
+                has_node = true;
             }
+            next_state();
         } else if (in_mesh) {
             SR_COUNT(c, SR_COUNTER_BLAS_SHAPE, (uint32_t)e.count);
             tri_next = e.child;
             tri_left = e.count;
-#if SR_LEAF_LOOP
-            // whole leaf in this step (bvh.cs:203-212)
+            state = QS_TRI;
+        } else {
+            SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
+            leaf_next = e.child;
+            leaf_left = e.count;
+            next_state();
+        }
+    }
+
+    template <bool COUNT>
+    SR_DEV void leaf_action(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
+        const float inf = __int_as_float(0x7f800000);
+        if (!count_action(err)) return;
+        if (state == QS_TRI) {
+            // the whole mesh leaf, in leaf order (bvh.cs:203-212)
             for (; tri_left > 0; ++tri_next, --tri_left) {
                 const float4* tp = S.tris + 3 * tri_next;
                 float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
@@ -556,7 +527,8 @@ struct SceneQuery {
                     if (ANY) {
                         best = {obj_pos, tri_next, 0.f, 0.f, 0.f, 0.f};
                         tri_left = 0;
-                        return true;
+                        state = QS_DONE;
+                        return;
                     }
                     cur_best = t;
                     ob_tri = tri_next;
@@ -564,21 +536,91 @@ struct SceneQuery {
                     ob_v = v;
                 }
             }
-#endif
-        } else {
-            SR_COUNT(c, SR_COUNTER_TLAS_SHAPE, (uint32_t)e.count);
-            leaf_next = e.child;
-            leaf_left = e.count;
+            next_state();
+        } else if (state == QS_EXIT) {
+            // the object's mesh traversal is complete: Bvh<Object> leaf comparison (bvh.cs:207)
+            if (ob_tri >= 0) {
+                float d = cur_best / lscale;
+                if (d < best.dist) best = {obj_pos, ob_tri, d, cur_best, ob_u, ob_v};
+            }
+            in_mesh = false;
+            cr = wr;
+            cur_best = ANY ? inf : best.dist;
+            next_state();
+        } else if (state == QS_OBJ) {
+            const DevObject& o = S.objects[leaf_next];
+            obj_pos = leaf_next;
+            ++leaf_next;
+            --leaf_left;
+            Ray l = to_local(o, wr, lscale);
+            int kind = GENERAL ? __float_as_int(o.pos_kind.w) : SR_SHAPE_MESH;
+            if (kind == SR_SHAPE_MESH) {
+                int root = __float_as_int(o.scale_root.w);
+                if (root >= 0) {  // an empty mesh never hits
+                    float4 rn0 = ldg4(S.nodes + 2 * root);
+                    float4 rn1 = ldg4(S.nodes + 2 * root + 1);
+                    mesh_base = sp;
+                    node = {__float_as_int(rn0.w), __float_as_int(rn1.w), 0.0f};
+                    has_node = true;
+                    in_mesh = true;
+                    cr = l;
+                    cur_best = inf;
+                    ob_tri = -1;
+                }
+            } else if (GENERAL) {
+                ShapeHit h;
+                bool ok = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, l, h, false)
+                                                  : box_hit(o.shape0, o.shape1, l, h, false);
+                if (ok) {
+                    if (ANY) {
+                        best = {obj_pos, -1, 0.f, 0.f, 0.f, 0.f};
+                        state = QS_DONE;
+                        return;
+                    }
+                    float d = h.dist / lscale;
+                    if (d < best.dist) best = {obj_pos, -1, d, 0.f, 0.f, 0.f};
+                    cur_best = best.dist;
+                }
+            }
+            next_state();
         }
-        return false;
+    }
+
+    // One action of whatever kind is next; true when the query is answered.
+    template <bool COUNT>
+    SR_DEV bool step(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
+        if (state == QS_NODE)
+            node_action<COUNT>(S, stack, c, err);
+        else if (state != QS_DONE)
+            leaf_action<COUNT>(S, stack, c, err);
+        return state == QS_DONE;
     }
 };
+
+// True when a query's first step -- the two children of the scene BVH's root -- already decides it
+// (neither box is hit, so there is no hit), without a traversal; counts what that step counts.
+// False when the root is a leaf or a child box is hit.
+template <bool COUNT, bool ANY>
+SR_DEV bool misses_scene(const DevScene& S, const Ray& r, Ctr& c) {
+    if (S.tlas_root < 0) return true;
+    const float4* root = S.nodes + 2 * S.tlas_root;
+    float4 rn0 = ldg4(root), rn1 = ldg4(root + 1);
+    if (__float_as_int(rn1.w) != 0) return false;
+    SR_COUNT(c, SR_COUNTER_TLAS_NODE, 2);
+    const float4* n = S.nodes + 2 * __float_as_int(rn0.w);
+    float4 a0 = ldg4(n), a1 = ldg4(n + 1), b0 = ldg4(n + 2), b1 = ldg4(n + 3);
+    const float inf = __int_as_float(0x7f800000);
+    float ta = 0.f, tb = 0.f;
+    bool pa = slab(a0, a1, r, ta) && (ANY || ta <= inf);
+    bool pb = slab(b0, b1, r, tb) && (ANY || tb <= inf);
+    return !pa && !pb;
+}
 
 template <bool COUNT, bool ANY, bool GENERAL = true>
 SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* err) {
     StackEntry stack[kSceneStack];
     SceneQuery<ANY, GENERAL> q;
-    q.init(S, wr, stack);
+    q.init(S, wr);
     while (!q.template step<COUNT>(S, stack, c, err)) {
     }
     return q.best;

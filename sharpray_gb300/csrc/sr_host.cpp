@@ -723,49 +723,30 @@ static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t 
 static int wave_reserve(SrScene* s, uint32_t slots) {
     if (s->wave_slots >= slots && s->wave.ptr) return SR_OK;
     const size_t n = slots;
-    // 16-byte planes: rng, ray_o, ray_d, rad, fog, energy, medium, prim, acc0..5, hit, sh0..3 (21)
-    // 8-byte planes: prim_uv, hit_uv; 4-byte planes: rng_c, q_active x2, q_resolve, q_shadow; + 8 counters
-    size_t bytes = n * (21 * 16 + 2 * 8 + 5 * 4) + 256;
+    // 32-byte sectors: path records (6 per slot), pixel records (4 per slot); 16-byte medium;
+    // 4-byte queues: live x2, trace x2, event x3, resolve, shadow; each array starts on 256 bytes
+    const size_t rec = sizeof(Rec);
+    size_t bytes = n * (10 * rec + 16 + 9 * 4) + 16 * 256 + kWaveCounters * sizeof(uint32_t);
     SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
     char* p = s->wave.as<char>();
-    auto take = [&](size_t elem) {
+    auto take = [&](size_t elem_bytes) {
         char* r = p;
-        p += n * elem;
+        p += (n * elem_bytes + 255) & ~(size_t)255;
         return r;
     };
     WaveState& w = s->ws;
-    w.rng = (uint4*)take(16);
-    w.ray_o = (float4*)take(16);
-    w.ray_d = (float4*)take(16);
-    w.rad = (float4*)take(16);
-    w.fog = (float4*)take(16);
-    w.energy = (float4*)take(16);
+    w.rec = (Rec*)take(6 * rec);
+    w.pix = (Rec*)take(4 * rec);
     w.medium = (float4*)take(16);
-    w.prim = (float4*)take(16);
-    w.acc0 = (float4*)take(16);
-    w.acc1 = (float4*)take(16);
-    w.acc2 = (float4*)take(16);
-    w.acc3 = (float4*)take(16);
-    w.acc4 = (float4*)take(16);
-    w.acc5 = (float4*)take(16);
-    w.hit = (float4*)take(16);
-    w.sh0 = (float4*)take(16);
-    w.sh1 = (float4*)take(16);
-    w.sh2 = (float4*)take(16);
-    w.sh3 = (float4*)take(16);
-    take(16);  // spare plane keeps the 8-byte planes aligned
-    take(16);
-    w.prim_uv = (float2*)take(8);
-    w.hit_uv = (float2*)take(8);
-    w.rng_c = (uint32_t*)take(4);
     w.q_active[0] = (uint32_t*)take(4);
     w.q_active[1] = (uint32_t*)take(4);
+    w.q_trace[0] = (uint32_t*)take(4);
+    w.q_trace[1] = (uint32_t*)take(4);
+    w.q_event = (uint32_t*)take(3 * 4);
     w.q_resolve = (uint32_t*)take(4);
     w.q_shadow = (uint32_t*)take(4);
     w.counts = (uint32_t*)p;
     s->wave_slots = slots;
-    // request flags start clear; resolve clears them after use
-    SR_CUDA(cudaMemset(w.sh0, 0, n * 16), "clear wavefront state");
     return SR_OK;
 }
 
@@ -924,9 +905,10 @@ SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t*
     uint32_t iters = s->last_host_iters;
     if (s->last_mode == SR_RENDER_WAVEFRONT_GRAPH) {
         SR_CUDA(cudaMemcpy(&iters, s->ws.counts + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
-        *kernel_launches = 1 + 4 * iters + iters / 2;  // init, 4 per bounce, loop condition per 2 bounces
+        // init, the bounce kernels, one loop condition per 2 bounces
+        *kernel_launches = 1 + kWaveKernelsPerBounce * iters + iters / 2;
     } else {
-        *kernel_launches = 1 + 4 * iters;
+        *kernel_launches = 1 + kWaveKernelsPerBounce * iters;
     }
     *bounce_iterations = iters;
     return SR_OK;

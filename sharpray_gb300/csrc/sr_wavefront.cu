@@ -1,24 +1,32 @@
 // sr_wavefront.cu — wavefront form of the per-pixel path loop.
 //
-// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into four
-// kernels per bounce over structure-of-arrays path state, one slot per pixel:
+// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into five
+// kernels per bounce over per-path state records, one slot per pixel:
 //
 //   extend   : closest hit of every live path ray            (Scene.Trace -> Bvh.Intersect)
-//   shade    : surface/fog/miss logic of one segment, light sample, Russian roulette, scatter;
-//              the NEE shadow ray and the end of a sample are deferred
+//              that enters the root boxes of the scene BVH (the others are decided when the ray
+//              is made: in foggy scenes most rays start far outside the scene and leave it)
+//   classify : the segment's event -- fog scatter (the free-flight distance is drawn here, the
+//              first RNG draw of the segment), surface hit or miss -- and one queue per event
+//   shade    : first the NEE contribution of the previous segment (its shadow ray has been traced
+//              since), then the event's logic: light sample, Russian roulette, scatter
 //   shadow   : shadow rays (ShadowTransmittance, scene.cs:576-600) times the fog transmittance
-//   finalize : NEE contributions, then, for finished samples, the pixel statistics, the adaptive
-//              stop, and the next camera ray or the AOV write
+//   finalize : finished samples only: the last NEE contribution, the pixel statistics, the
+//              adaptive stop, and the next camera ray or the AOV write
+//
+// Sorting paths by event makes every shade warp run one branch: fog scatter, surface and miss
+// logic differ completely, and in foggy scenes most segments end in the fog while a few hit
+// surfaces, so unsorted warps nearly always ran all three.
 //
 // extend and shadow are persistent: a lane that finishes its ray takes the next one from the
 // queue at once (refilled per warp with one atomic), so warps stay full although ray lengths
 // differ by orders of magnitude.
 //
-// Live paths are compacted between kernels with warp-aggregated atomics (ballot + popc), so every
-// launch works on dense queues.  Every per-path operation -- RNG draws, float operation order,
+// Live paths are compacted between kernels with block-aggregated atomics (ballot + popc per warp,
+// one atomic per block and queue), so every launch works on dense queues.  Every per-path operation -- RNG draws, float operation order,
 // the order in which contributions are added -- is the megakernel's (sr_path.cuh), so the two
-// forms produce identical images; the wavefront form keeps each kernel's register footprint
-// small so the latency-bound traversals run at high occupancy.
+// forms produce identical images: a segment's NEE contribution is added before anything of the
+// next segment touches the radiance, exactly where the megakernel adds it.
 //
 // The bounce loop runs either as a host loop (one launch per kernel per bounce, the host reads the
 // live-path count after every bounce) or as a CUDA graph whose conditional WHILE node repeats the
@@ -30,8 +38,38 @@
 
 namespace sr {
 
-enum : uint32_t { PF_SPDF = 1u, PF_MEDIUM = 2u, PF_PRIMARY = 4u };
-enum : uint32_t { RF_SHADOW = 1u, RF_TERMINATE = 2u, RF_FOG = 4u };
+// path flags (Rec path.b.w)
+enum : uint32_t {
+    PF_SPDF = 1u,      // the last scatter has a pdf (MIS on a later sky hit)
+    PF_MEDIUM = 2u,    // inside a refractive medium
+    PF_PRIMARY = 4u,   // the sample's primary hit is recorded in `prim`
+    PF_NEE = 8u,       // a traced shadow ray's contribution is pending
+    PF_NEE_FOG = 16u,  // ... and it goes to the fog radiance (primary-segment fog scatter)
+};
+// segment events (queue index)
+enum : int { EV_FOG = 0, EV_MISS = 1, EV_SURF = 2 };
+// WaveState::counts
+enum : int {
+    kCountLive = 0,          // [0], [1]: live-queue lengths (ping-pong)
+    kCountResolve = 2,       // finished samples of this bounce
+    kCountIter = 3,          // bounces run by the device loop
+    kCountExtendFetch = 4,   // extend's fetch cursor
+    kCountShadowFetch = 5,   // shadow's fetch cursor
+    kCountShadow = 6,        // shadow rays of this bounce
+    kCountEvent = 8,         // [8..10]: event-queue lengths
+    kCountTrace = 11,        // [11], [12]: trace-queue lengths (ping-pong)
+};
+
+// Sectors of a slot's path record (WaveState::rec, six per slot, 192 bytes on 64-byte boundaries:
+// {ray, hit}, {path, rng} and the shadow request each fill one 64-byte DRAM burst) and of its pixel
+// record (WaveState::pix, four per slot).
+enum : int { R_RAY = 0, R_HIT = 1, R_PATH = 2, R_RNG = 3, R_SH0 = 4, R_SH1 = 5 };
+enum : int { X_PRIM = 0, X_ACC = 1 };
+__device__ __forceinline__ size_t rix(uint32_t s, int k) { return 6 * (size_t)s + k; }
+__device__ __forceinline__ size_t pix(uint32_t s, int k) { return 4 * (size_t)s + k; }
+
+__device__ __forceinline__ uint32_t ibits(float f) { return (uint32_t)__float_as_int(f); }
+__device__ __forceinline__ float fbits(uint32_t u) { return __int_as_float((int)u); }
 
 __device__ __forceinline__ void slot_pixel(const WaveState& W, uint32_t slot, uint32_t& x, uint32_t& y) {
     // slots are laid out in 8x4 pixel tiles so that a warp's primary rays are neighbours
@@ -40,37 +78,59 @@ __device__ __forceinline__ void slot_pixel(const WaveState& W, uint32_t slot, ui
     y = (tile / W.tiles_x) * 4u + (lane >> 3);
 }
 
-// Warp-aggregated append of `value` to queue q when pred holds (all 32 lanes must call).
-__device__ __forceinline__ void push(uint32_t* q, uint32_t* count, uint32_t value, bool pred) {
-    unsigned mask = __ballot_sync(0xffffffffu, pred);
-    if (!mask) return;
-    int lane = threadIdx.x & 31;
-    int leader = __ffs(mask) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (pred) q[base + __popc(mask & ((1u << lane) - 1u))] = value;
+// Appends of one grid-stride round to NQ queues (value to queue i where pred[i] holds), aggregated
+// per block: one atomic per queue and block.  The queue lengths are single words that every block
+// appends to; their atomics serialise in L2, so per-warp appends made them a bottleneck.  All
+// threads of the 128-thread block call it in block-uniform control flow, passing shared scratch
+// sh[2][NQ][5] and the round's parity (the scratch alternates so a round needs two barriers).
+constexpr int kBlockWarps = 4;
+template <int NQ>
+__device__ __forceinline__ void push_block(uint32_t* const (&q)[NQ], uint32_t* const (&count)[NQ], uint32_t value,
+                                           const bool (&pred)[NQ], uint32_t (*sh)[NQ][kBlockWarps + 1],
+                                           uint32_t round) {
+    uint32_t(&b)[NQ][kBlockWarps + 1] = sh[round & 1u];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned mask[NQ];
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        mask[i] = __ballot_sync(0xffffffffu, pred[i]);
+        if (lane == 0) b[i][warp] = (uint32_t)__popc(mask[i]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        if (threadIdx.x == (unsigned)i) {
+            uint32_t tot = b[i][0] + b[i][1] + b[i][2] + b[i][3];
+            b[i][kBlockWarps] = tot ? atomicAdd(count[i], tot) : 0u;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        if (pred[i]) {
+            uint32_t off = b[i][kBlockWarps];
+            for (int w = 0; w < warp; ++w) off += b[i][w];
+            q[i][off + (uint32_t)__popc(mask[i] & ((1u << lane) - 1u))] = value;
+        }
+    }
 }
 
-__device__ __forceinline__ Rng load_rng(const WaveState& W, uint32_t s) {
-    uint4 a = W.rng[s];
-    return {a.x, a.y, a.z, a.w, W.rng_c[s]};
+__device__ __forceinline__ Rng rng_of(const Rec& g) {
+    return {ibits(g.a.x), ibits(g.a.y), ibits(g.a.z), ibits(g.a.w), ibits(g.b.x)};
 }
-__device__ __forceinline__ void store_rng(const WaveState& W, uint32_t s, const Rng& r) {
-    W.rng[s] = make_uint4(r.s0, r.s1, r.s2, r.s3);
-    W.rng_c[s] = r.s4;
+__device__ __forceinline__ Rec rng_rec(const Rng& r, Col fog) {
+    return {make_float4(fbits(r.s0), fbits(r.s1), fbits(r.s2), fbits(r.s3)), make_float4(fbits(r.s4), fog.r, fog.g, fog.b)};
 }
 
 // Start of a sample: the camera ray and a reset path (scene.cs:633-638).
-__device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, const Ray& ray) {
-    W.ray_o[s] = make_float4(ray.o.x, ray.o.y, ray.o.z, __int_as_float(0));
-    W.ray_d[s] = make_float4(ray.d.x, ray.d.y, ray.d.z, __int_as_float(0));
-    W.rad[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-    W.fog[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-    W.energy[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+__device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, const Ray& ray, const Rng& rng) {
+    W.rec[rix(s, R_RAY)] = {make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)};
+    W.rec[rix(s, R_PATH)] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(1.f, 1.f, 1.f, fbits(0u))};
+    W.rec[rix(s, R_RNG)] = rng_rec(rng, black());
 }
 
 __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevParams P) {
+    __shared__ uint32_t sh[2][2][kBlockWarps + 1];
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = false;
     if (s < W.slots) {
@@ -80,18 +140,27 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
         if (valid) {
             Rng rng = rng_seed(x, y);
             Ray ray = camera_ray(V, P, x, y, rng);
-            store_rng(W, s, rng);
-            begin_sample(W, s, ray);
+            begin_sample(W, s, ray, rng);
             float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-            W.acc0[s] = z;
-            W.acc1[s] = z;
-            W.acc2[s] = z;
-            W.acc3[s] = z;
-            W.acc4[s] = z;  // depth sum, normal count, depth count, sample index (int bits 0)
-            W.acc5[s] = z;  // first uv, has-uv flag
+            W.pix[pix(s, X_ACC)] = {z, z};
+            W.pix[pix(s, X_ACC + 1)] = {z, z};
+            W.pix[pix(s, X_ACC + 2)] = {z, z};  // counts and sample index start at 0 (int bits)
         }
     }
-    push(W.q_active[0], &W.counts[0], s, valid);
+    push_block<2>({W.q_active[0], W.q_trace[0]}, {&W.counts[kCountLive], &W.counts[kCountTrace]}, s, {valid, valid}, sh,
+                  0u);
+}
+
+// A new path ray (scatter or camera ray): it needs the next extend's traversal unless it misses
+// both root children of the scene BVH, the first thing the traversal tests; then its empty
+// closest hit is written here, as extend would write it.
+template <bool COUNT>
+__device__ __forceinline__ bool needs_trace(const WaveState& W, const DevScene& S, uint32_t s, const Ray& ray, Ctr& c) {
+    if (!misses_scene<COUNT, false>(S, ray, c)) return true;
+    SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
+    W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(-1), __int_as_float(-1), __int_as_float(0x7f800000), 0.f),
+                make_float4(0.f, 0.f, 0.f, 0.f)};
+    return false;
 }
 
 // A warp refills its idle lanes once at least this many are idle (or all are).
@@ -103,9 +172,24 @@ constexpr int kRefill = SR_REFILL;
 #ifndef SR_TRACE_MIN_BLOCKS
 #define SR_TRACE_MIN_BLOCKS 6
 #endif
+// Node phase of the persistent loop: at most SR_NODE_BURST node visits per round, ended early
+// once SR_LEAF_WAIT lanes wait for a leaf action (triangles, entering or leaving an object) or
+// are done.  1 / 1 runs one action of each lane per round.
+#ifndef SR_NODE_BURST
+#define SR_NODE_BURST 8
+#endif
+#ifndef SR_LEAF_WAIT
+#define SR_LEAF_WAIT 8
+#endif
+constexpr int kNodeBurst = SR_NODE_BURST;
+constexpr int kLeafWait = SR_LEAF_WAIT;
 
 // Persistent ray loop shared by extend and shadow: lanes take queue entries [fetch counter) until
-// the queue is exhausted; `start(slot)` begins a query, `finish(slot)` stores its answer.
+// the queue is exhausted; `start(slot)` begins a query, `finish(slot, hit, ray)` stores its answer.
+// Each round runs the node visits of all lanes together (up to kNodeBurst), then one leaf action
+// of each lane that waits for one: leaf actions are long and differ between lanes, so batching
+// them keeps warps from running each one with a single lane.  Every lane's own sequence of actions
+// is unchanged, so results are those of a plain loop over SceneQuery::step.
 template <bool COUNT, bool ANY, bool GENERAL, typename Start, typename Finish>
 __device__ __forceinline__ void persistent_queries(const DevScene& S, const uint32_t* q, uint32_t n, uint32_t* fetch,
                                                    Ctr& c, uint32_t* err, Start start, Finish finish) {
@@ -126,7 +210,7 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const uint
                 uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (idx < n) {
                     slot = q[idx];
-                    sq.init(S, start(slot), stack);
+                    sq.init(S, start(slot));
                     busy = true;
                 }
             }
@@ -135,8 +219,16 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const uint
             if (exhausted) break;
             continue;
         }
-        if (busy && sq.template step<COUNT>(S, stack, c, err)) {
-            finish(slot, sq.best);
+#pragma unroll 1
+        for (int k = 0; k < kNodeBurst; ++k) {
+            bool nodework = busy && sq.state == QS_NODE;
+            if (!__any_sync(0xffffffffu, nodework)) break;
+            if (nodework) sq.template node_action<COUNT>(S, stack, c, err);
+            if (__popc(__ballot_sync(0xffffffffu, busy && sq.state != QS_NODE)) >= kLeafWait) break;
+        }
+        if (busy && sq.state != QS_NODE && sq.state != QS_DONE) sq.template leaf_action<COUNT>(S, stack, c, err);
+        if (busy && sq.state == QS_DONE) {
+            finish(slot, sq.best, sq.wr);
             busy = false;
         }
     }
@@ -146,25 +238,68 @@ template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveState W, DevScene S, int cur, uint32_t* err,
                                                      unsigned long long* counters) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        W.counts[2] = 0;        // deferred-work queue of this bounce starts empty
-        W.counts[6] = 0;        // shadow queue of this bounce starts empty
-        W.counts[cur ^ 1] = 0;  // next live queue starts empty
+        W.counts[kCountResolve] = 0;  // finished samples of this bounce
+        W.counts[kCountShadow] = 0;   // shadow queue of this bounce starts empty
+        W.counts[cur ^ 1] = 0;        // next live queue starts empty
+        W.counts[kCountTrace + (cur ^ 1)] = 0;
+        W.counts[kCountEvent + EV_FOG] = 0;
+        W.counts[kCountEvent + EV_MISS] = 0;
+        W.counts[kCountEvent + EV_SURF] = 0;
     }
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     persistent_queries<COUNT, false, GENERAL>(
-        S, W.q_active[cur], W.counts[cur], &W.counts[4], c, err,
+        S, W.q_trace[cur], W.counts[kCountTrace + cur], &W.counts[kCountExtendFetch], c, err,
         [&](uint32_t s) {
             SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-            float4 o = W.ray_o[s], d = W.ray_d[s];
-            return make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
+            Rec r = W.rec[rix(s, R_RAY)];
+            return make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
         },
-        [&](uint32_t s, const Hit& h) {
-            W.hit[s] = make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl);
-            W.hit_uv[s] = make_float2(h.u, h.v);
+        [&](uint32_t s, const Hit& h, const Ray&) {
+            W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
+                        make_float4(h.u, h.v, 0.f, 0.f)};
         });
     flush_counters<COUNT>(c, counters);
+}
+
+// The event of each live segment (scene.cs:654-738 decides in this order): with fog set, the
+// free-flight distance is drawn first and wins if it is shorter than the hit; else a hit is a
+// surface event and no hit a miss.  The world distance of the closest hit is the one the surface
+// lookup reports (both divide the local distance by the same object-space scale).
+__global__ void __launch_bounds__(128) k_wave_classify(WaveState W, DevScene S, int cur) {
+    __shared__ uint32_t sh[2][3][kBlockWarps + 1];
+    uint32_t round = 0;
+    const uint32_t n = W.counts[cur];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const float inf = __int_as_float(0x7f800000);
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        uint32_t k = base + threadIdx.x;
+        bool valid = k < n;
+        uint32_t s = valid ? W.q_active[cur][k] : 0u;
+        int ev = EV_MISS;
+        if (valid) {
+            Rec h = W.rec[rix(s, R_HIT)];
+            bool has_hit = __float_as_int(h.a.x) >= 0;
+            ev = has_hit ? EV_SURF : EV_MISS;
+            if (S.has_fog) {
+                Rec r = W.rec[rix(s, R_RAY)];
+                Rec g = W.rec[rix(s, R_RNG)];
+                Rng rng = rng_of(g);
+                Ray ray{V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z}, V3{0.f, 0.f, 0.f}};
+                float sdist;
+                if (fog_scatter_distance(S, ray, has_hit ? h.a.z : inf, rng, sdist)) {
+                    ev = EV_FOG;
+                    W.rec[rix(s, R_HIT)].b = make_float4(h.b.x, h.b.y, sdist, 0.f);
+                }
+                W.rec[rix(s, R_RNG)] = rng_rec(rng, Col{g.b.y, g.b.z, g.b.w});
+            }
+        }
+        push_block<3>({W.q_event + (size_t)EV_FOG * W.slots, W.q_event + (size_t)EV_MISS * W.slots,
+                       W.q_event + (size_t)EV_SURF * W.slots},
+                      {&W.counts[kCountEvent + EV_FOG], &W.counts[kCountEvent + EV_MISS], &W.counts[kCountEvent + EV_SURF]},
+                      s, {valid && ev == EV_FOG, valid && ev == EV_MISS, valid && ev == EV_SURF}, sh, round++);
+    }
 }
 
 // Shadow rays of the bounce: transmittance (any hit -> black in opaque scenes) times the fog
@@ -177,75 +312,110 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     if (!GENERAL || !S.has_transparent) {
         persistent_queries<COUNT, true, GENERAL>(
-            S, W.q_shadow, W.counts[6], &W.counts[5], c, err,
+            S, W.q_shadow, W.counts[kCountShadow], &W.counts[kCountShadowFetch], c, err,
             [&](uint32_t s) {
                 SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
-                float4 o = W.sh0[s], d = W.sh1[s];
-                return make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
+                Rec r = W.rec[rix(s, R_SH0)];
+                return make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
             },
-            [&](uint32_t s, const Hit& h) {
-                float4 o = W.sh0[s], d = W.sh1[s];
+            [&](uint32_t s, const Hit& h, const Ray& ray) {
                 float tr = 0.0f;
                 if (h.obj < 0) {
                     tr = 1.0f;
-                    if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z}));
+                    if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, ray);
                 }
-                W.sh0[s] = make_float4(tr, tr, tr, o.w);
+                W.rec[rix(s, R_SH0)].a = make_float4(tr, tr, tr, 0.f);
             });
     } else {
-        const uint32_t n = W.counts[6];
+        const uint32_t n = W.counts[kCountShadow];
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
             uint32_t s = W.q_shadow[k];
-            float4 o = W.sh0[s], d = W.sh1[s];
-            Ray shadow = make_ray(V3{o.x, o.y, o.z}, V3{d.x, d.y, d.z});
+            Rec r = W.rec[rix(s, R_SH0)];
+            Ray shadow = make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
             Col tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
             if (max_component(tr) > 0.0f && S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
-            W.sh0[s] = make_float4(tr.r, tr.g, tr.b, o.w);
+            W.rec[rix(s, R_SH0)].a = make_float4(tr.r, tr.g, tr.b, 0.f);
         }
     }
     flush_counters<COUNT>(c, counters);
 }
 
+// The rest of SampleSkyDirect / SampleSkyDirectFog (scene.cs:774-810) once the shadow kernel has
+// left the transmittance (incl. fog) in the request record: the contribution of the light sample.
+template <bool COUNT, bool GENERAL>
+__device__ __forceinline__ void add_nee(const WaveState& W, const DevScene& S, uint32_t s, uint32_t pflags,
+                                        Col& radiance, Col& fog, Ctr& c) {
+    Rec r0 = W.rec[rix(s, R_SH0)];
+    Col tr = col3(r0.a);
+    if (max_component(tr) > 0.0f) {
+        Rec r1 = W.rec[rix(s, R_SH1)];
+        V3 ldir{r0.b.x, r0.b.y, r0.b.z};
+        Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * col3(r1.a) * r1.a.w / r0.b.w;
+        Col add = contrib * col3(r1.b);
+        if (pflags & PF_NEE_FOG)
+            fog = fog + add;
+        else
+            radiance = radiance + add;
+    }
+}
+
+// One segment of every live path, warps sorted by event: the index space is the fog queue, then
+// the miss queue, then the surface queue, the first two padded to whole warps, so every warp
+// runs one event's logic.
 template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, uint32_t* err,
                                                     unsigned long long* counters) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[5] = 0;  // shadow kernel's fetch counter
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountShadowFetch] = 0;
+    __shared__ uint32_t sh[2][4][kBlockWarps + 1];
+    uint32_t round = 0;
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     const int nxt = cur ^ 1;
-    const uint32_t n = W.counts[cur];
+    const uint32_t nfog = W.counts[kCountEvent + EV_FOG], nmiss = W.counts[kCountEvent + EV_MISS],
+                   nsurf = W.counts[kCountEvent + EV_SURF];
+    const uint32_t pfog = (nfog + 31u) & ~31u, pmiss = (nmiss + 31u) & ~31u;
+    const uint32_t total = pfog + pmiss + nsurf;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const float inf = __int_as_float(0x7f800000);
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        uint32_t k = base + threadIdx.x;
-        bool valid = k < n;
-        uint32_t s = valid ? W.q_active[cur][k] : 0u;
-        uint32_t rflags = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += stride) {
+        const uint32_t k = base + threadIdx.x;
+        int ev;
+        uint32_t i, cnt;
+        if (k < pfog) {
+            ev = EV_FOG, i = k, cnt = nfog;
+        } else if (k < pfog + pmiss) {
+            ev = EV_MISS, i = k - pfog, cnt = nmiss;
+        } else {
+            ev = EV_SURF, i = k - pfog - pmiss, cnt = nsurf;
+        }
+        const bool valid = i < cnt;
+        const uint32_t s = valid ? W.q_event[(size_t)ev * W.slots + i] : 0u;
+        bool live = false, shadow_req = false, trace = false;
         if (valid) {
             SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
-            Rng rng = load_rng(W, s);
-            float4 o4 = W.ray_o[s], d4 = W.ray_d[s];
-            uint32_t bounce = (uint32_t)__float_as_int(o4.w);
-            uint32_t pflags = (uint32_t)__float_as_int(d4.w);
+            Rec rr = W.rec[rix(s, R_RAY)], pr = W.rec[rix(s, R_PATH)], gr = W.rec[rix(s, R_RNG)];
+            Rng rng = rng_of(gr);
+            Col fog{gr.b.y, gr.b.z, gr.b.w};
+            uint32_t bounce = ibits(rr.a.w);
+            uint32_t pflags = ibits(pr.b.w);
             if (bounce == 0) SR_COUNT(c, SR_COUNTER_SAMPLE, 1);
-            Ray ray = make_ray(V3{o4.x, o4.y, o4.z}, V3{d4.x, d4.y, d4.z});
-            float4 rad4 = W.rad[s];
-            Col radiance{rad4.x, rad4.y, rad4.z};
-            float spdf = rad4.w;
-            Col energy = col3(W.energy[s]);
-            float4 h0 = W.hit[s];
-            float2 huv = W.hit_uv[s];
-            Hit hit{__float_as_int(h0.x), __float_as_int(h0.y), h0.z, h0.w, huv.x, huv.y};
-            bool has_hit = hit.obj >= 0;
-            SurfHit sh;
-            if (has_hit) surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
-            float sdist;
-            // Event of this segment (scene.cs:654-738): fog scatter (free-flight distance drawn first
-            // when fog is set), surface hit, or miss.  Fog and surface events share one light sample,
-            // one Russian-roulette draw and then scatter, in that RNG order, so those calls exist once.
-            bool fog_event = S.has_fog && fog_scatter_distance(S, ray, has_hit ? sh.dist : inf, rng, sdist);
-            if (fog_event || has_hit) {
+            Ray ray = make_ray(V3{rr.a.x, rr.a.y, rr.a.z}, V3{rr.b.x, rr.b.y, rr.b.z});
+            Col radiance = col3(pr.a);
+            float spdf = pr.a.w;
+            Col energy = col3(pr.b);
+            if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, fog, c);
+            pflags &= ~(PF_NEE | PF_NEE_FOG);
+            bool terminate = false;
+            if (ev != EV_MISS) {
+                // Fog and surface events share one light sample, one Russian-roulette draw and then
+                // scatter, in that RNG order (scene.cs:654-726).
+                const bool fog_event = ev == EV_FOG;
+                const Rec hr = W.rec[rix(s, R_HIT)];
+                SurfHit sh;
+                if (!fog_event) {
+                    Hit hit{__float_as_int(hr.a.x), __float_as_int(hr.a.y), hr.a.z, hr.a.w, hr.b.x, hr.b.y};
+                    surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
+                }
                 const Surface& su = sh.surf;
                 const float dist = sh.dist;
                 const V3 view = -ray.d;
@@ -253,7 +423,7 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                 V3 pos;
                 if (fog_event) {
                     energy = energy * col3(S.fog_color);
-                    pos = ray_at(ray, sdist);
+                    pos = ray_at(ray, hr.b.z);
                 } else {
                     bias = fmaxf(1e-4f, dist * 1e-4f);
                     pos = ray_at(ray, dist - bias);
@@ -261,12 +431,12 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                     radiance = radiance + su.radiance * energy;
                     if (bounce == 0) {
                         pflags |= PF_PRIMARY;
-                        W.prim[s] = make_float4(su.normal.x, su.normal.y, su.normal.z, dist);
-                        W.prim_uv[s] = make_float2(su.uv.x, su.uv.y);
+                        W.pix[pix(s, X_PRIM)] = {make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
+                                     make_float4(su.uv.x, su.uv.y, 0.f, 0.f)};
                     }
                 }
                 // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
-                // the shadow ray and the contribution are deferred
+                // the shadow ray is traced by the shadow kernel, the contribution added next segment
                 V3 ldir;
                 float lpdf;
                 if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
@@ -287,15 +457,27 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                         }
                     }
                     if (emit) {
-                        rflags |= RF_SHADOW | ((fog_event && bounce == 0) ? RF_FOG : 0u);
-                        W.sh0[s] = make_float4(pos.x, pos.y, pos.z, 0.f);
-                        W.sh1[s] = make_float4(ldir.x, ldir.y, ldir.z, lpdf);
-                        W.sh2[s] = make_float4(w3.r, w3.g, w3.b, mis);
-                        W.sh3[s] = make_float4(energy.r, energy.g, energy.b, 0.f);
+                        pflags |= PF_NEE | ((fog_event && bounce == 0) ? PF_NEE_FOG : 0u);
+                        // a shadow ray that misses the scene's root boxes is unoccluded: its
+                        // transmittance is the fog's alone, formed here as the shadow kernel would
+                        Ray shadow = make_ray(pos, ldir);
+                        float4 head = make_float4(pos.x, pos.y, pos.z, 0.f);
+                        const bool any = !GENERAL || !S.has_transparent;
+                        if (any ? misses_scene<COUNT, true>(S, shadow, c) : misses_scene<COUNT, false>(S, shadow, c)) {
+                            SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
+                            float tr = 1.0f;
+                            if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, shadow);
+                            head = make_float4(tr, tr, tr, 0.f);
+                        } else {
+                            shadow_req = true;
+                        }
+                        W.rec[rix(s, R_SH0)] = {head, make_float4(ldir.x, ldir.y, ldir.z, lpdf)};
+                        W.rec[rix(s, R_SH1)] = {make_float4(w3.r, w3.g, w3.b, mis),
+                                                       make_float4(energy.r, energy.g, energy.b, 0.f)};
                     }
                 }
                 if (russian_roulette(energy, bounce, rng)) {
-                    rflags |= RF_TERMINATE;
+                    terminate = true;
                 } else if (fog_event) {
                     V3 sdir = hg_scatter_dir(ray.d, S.fog_g, rng);
                     pflags |= PF_SPDF;
@@ -324,127 +506,112 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
                 // miss: sky radiance with the MIS weight of the last scatter (scene.cs:728-738)
                 float mis = (pflags & PF_SPDF) ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
                 radiance = radiance + sky_radiance<COUNT, GENERAL>(S, ray.d, c) * mis * energy;
-                rflags |= RF_TERMINATE;
+                terminate = true;
             }
-            if (!(rflags & RF_TERMINATE) && ++bounce == P.bounces + 1) rflags |= RF_TERMINATE;
-            store_rng(W, s, rng);
-            W.ray_o[s] = make_float4(ray.o.x, ray.o.y, ray.o.z, __int_as_float((int)bounce));
-            W.ray_d[s] = make_float4(ray.d.x, ray.d.y, ray.d.z, __int_as_float((int)pflags));
-            W.rad[s] = make_float4(radiance.r, radiance.g, radiance.b, spdf);
-            W.energy[s] = make_float4(energy.r, energy.g, energy.b, 0.f);
-            if (rflags) W.sh0[s].w = __int_as_float((int)rflags);
+            if (!terminate && ++bounce == P.bounces + 1) terminate = true;
+            live = !terminate;
+            W.rec[rix(s, R_PATH)] = {make_float4(radiance.r, radiance.g, radiance.b, spdf),
+                         make_float4(energy.r, energy.g, energy.b, fbits(pflags))};
+            W.rec[rix(s, R_RNG)] = rng_rec(rng, fog);
+            if (live) {
+                W.rec[rix(s, R_RAY)] = {make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                            make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)};
+                trace = needs_trace<COUNT>(W, S, s, ray, c);
+            }
         }
-        push(W.q_active[nxt], &W.counts[nxt], s, valid && rflags == 0);
-        push(W.q_resolve, &W.counts[2], s, valid && rflags != 0);
-        push(W.q_shadow, &W.counts[6], s, valid && (rflags & RF_SHADOW));
+        push_block<4>({W.q_active[nxt], W.q_trace[nxt], W.q_resolve, W.q_shadow},
+                      {&W.counts[nxt], &W.counts[kCountTrace + nxt], &W.counts[kCountResolve], &W.counts[kCountShadow]},
+                      s, {valid && live, valid && trace, valid && !live, valid && shadow_req}, sh, round++);
     }
     flush_counters<COUNT>(c, counters);
 }
 
+// Finished samples: the pending NEE contribution of the last segment, then the pixel statistics
+// and the adaptive stop (renderer.cs:173-212), then the next camera ray or the AOV write.
 template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, DevView V, DevParams P, DevAovs out,
                                                        int cur, uint32_t* err, unsigned long long* counters) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[4] = 0;  // next extend's fetch counter
+    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountExtendFetch] = 0;  // next extend's fetch cursor
+    __shared__ uint32_t sh[2][2][kBlockWarps + 1];
+    uint32_t round = 0;
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     const int nxt = cur ^ 1;
-    const uint32_t n = W.counts[2];
+    const uint32_t n = W.counts[kCountResolve];
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         uint32_t k = base + threadIdx.x;
         bool valid = k < n;
         uint32_t s = valid ? W.q_resolve[k] : 0u;
-        bool live = false;
+        bool live = false, trace = false;
         if (valid) {
-            float4 s0 = W.sh0[s];
-            uint32_t rflags = (uint32_t)__float_as_int(s0.w);
-            if (rflags & RF_SHADOW) {
-                // the rest of SampleSkyDirect / SampleSkyDirectFog (scene.cs:774-810) once the
-                // shadow kernel has left the transmittance (incl. fog) in sh0.xyz
-                Col tr = col3(s0);
-                if (max_component(tr) > 0.0f) {
-                    float4 s1 = W.sh1[s], s2 = W.sh2[s], s3 = W.sh3[s];
-                    V3 ldir{s1.x, s1.y, s1.z};
-                    Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * col3(s2) * s2.w / s1.w;
-                    Col add = contrib * col3(s3);
-                    if (rflags & RF_FOG) {
-                        float4 f = W.fog[s];
-                        W.fog[s] = make_float4(f.x + add.r, f.y + add.g, f.z + add.b, f.w);
-                    } else {
-                        float4 r = W.rad[s];
-                        W.rad[s] = make_float4(r.x + add.r, r.y + add.g, r.z + add.b, r.w);
-                    }
-                }
+            Rec pr = W.rec[rix(s, R_PATH)], gr = W.rec[rix(s, R_RNG)];
+            uint32_t pflags = ibits(pr.b.w);
+            Col radiance = col3(pr.a);
+            Col radiance_fog{gr.b.y, gr.b.z, gr.b.w};
+            if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, radiance_fog, c);
+            Rec c0 = W.pix[pix(s, X_ACC)], c1 = W.pix[pix(s, X_ACC + 1)], c2 = W.pix[pix(s, X_ACC + 2)];
+            float4 a0 = c0.a, a1 = c0.b, a2 = c1.a, a3 = c1.b, a4 = c2.a, a5 = c2.b;
+            a0.x += radiance.r, a0.y += radiance.g, a0.z += radiance.b;
+            a1.x += radiance_fog.r, a1.y += radiance_fog.g, a1.z += radiance_fog.b;
+            float lum = luminance(radiance) + luminance(radiance_fog);
+            a0.w += lum;
+            a1.w += lum * lum;
+            float ls = luminance(radiance);
+            a2.w += ls;
+            a3.w += ls * ls;
+            uint32_t ncount = ibits(a4.y), dcount = ibits(a4.z);
+            uint32_t si = ibits(a4.w);
+            if (pflags & PF_PRIMARY) {
+                Rec pm = W.pix[pix(s, X_PRIM)];
+                float4 pn = pm.a;
+                a2.x += pn.x, a2.y += pn.y, a2.z += pn.z;
+                a3.x = pn.x, a3.y = pn.y, a3.z = pn.z;
+                ncount++;
+                a4.x += pn.w;
+                dcount++;
+                if (ibits(a5.z) == 0u) a5 = make_float4(pm.b.x, pm.b.y, fbits(1u), 0.f);
             }
-            // clear the request flags so a later bounce without a request is not re-resolved
-            W.sh0[s].w = __int_as_float(0);
-            live = !(rflags & RF_TERMINATE);
-            if (!live) {
-                // end of a sample: pixel statistics and the adaptive stop (renderer.cs:173-212)
-                Col radiance = col3(W.rad[s]);
-                Col radiance_fog = col3(W.fog[s]);
-                uint32_t pflags = (uint32_t)__float_as_int(W.ray_d[s].w);
-                float4 a0 = W.acc0[s], a1 = W.acc1[s], a2 = W.acc2[s], a3 = W.acc3[s], a4 = W.acc4[s], a5 = W.acc5[s];
-                a0.x += radiance.r, a0.y += radiance.g, a0.z += radiance.b;
-                a1.x += radiance_fog.r, a1.y += radiance_fog.g, a1.z += radiance_fog.b;
-                float lum = luminance(radiance) + luminance(radiance_fog);
-                a0.w += lum;
-                a1.w += lum * lum;
-                float ls = luminance(radiance);
-                a2.w += ls;
-                a3.w += ls * ls;
-                uint32_t ncount = (uint32_t)__float_as_int(a4.y), dcount = (uint32_t)__float_as_int(a4.z);
-                uint32_t si = (uint32_t)__float_as_int(a4.w);
-                if (pflags & PF_PRIMARY) {
-                    float4 pr = W.prim[s];
-                    a2.x += pr.x, a2.y += pr.y, a2.z += pr.z;
-                    a3.x = pr.x, a3.y = pr.y, a3.z = pr.z;
-                    ncount++;
-                    a4.x += pr.w;
-                    dcount++;
-                    if (__float_as_int(a5.z) == 0) {
-                        float2 uv = W.prim_uv[s];
-                        a5 = make_float4(uv.x, uv.y, __int_as_float(1), 0.f);
-                    }
-                }
-                bool done = false;
-                uint32_t count = 0;
-                if (si >= P.min_samples - 1 && relative_std_err(a0.w, a1.w, si + 1) < P.variance_threshold) {
-                    done = true;
-                    count = si + 1;
-                } else if (++si == P.max_samples) {
-                    done = true;
-                    count = si + 1;  // loop ran out: normalised by maxSamples + 1 (renderer.cs:215)
-                }
-                uint32_t x, y;
-                slot_pixel(W, s, x, y);
-                if (done) {
-                    float var = relative_std_err(a2.w, a3.w, count);
-                    Col r = col3(a0) / (float)count;
-                    Col f = col3(a1) / (float)count;
-                    V3 nsum{a2.x, a2.y, a2.z}, nfb{a3.x, a3.y, a3.z};
-                    V3 nrm = ncount > 0 ? normalize_or(nsum, nfb) : V3{0.f, 0.f, 0.f};
-                    size_t i = (size_t)y * P.width + x;
-                    out.radiance[3 * i] = r.r, out.radiance[3 * i + 1] = r.g, out.radiance[3 * i + 2] = r.b;
-                    out.radiance_fog[3 * i] = f.r, out.radiance_fog[3 * i + 1] = f.g, out.radiance_fog[3 * i + 2] = f.b;
-                    out.normals[3 * i] = nrm.x, out.normals[3 * i + 1] = nrm.y, out.normals[3 * i + 2] = nrm.z;
-                    out.uv[2 * i] = a5.x, out.uv[2 * i + 1] = a5.y;
-                    out.depth[i] = dcount > 0 ? a4.x / (float)dcount : __int_as_float(0x7f800000);
-                    out.samples[i] = count;
-                    out.variance[i] = var;
-                } else {
-                    Rng rng = load_rng(W, s);
-                    Ray ray = camera_ray(V, P, x, y, rng);
-                    store_rng(W, s, rng);
-                    begin_sample(W, s, ray);
-                    live = true;
-                }
-                a4.y = __int_as_float((int)ncount), a4.z = __int_as_float((int)dcount), a4.w = __int_as_float((int)si);
-                W.acc0[s] = a0, W.acc1[s] = a1, W.acc2[s] = a2, W.acc3[s] = a3, W.acc4[s] = a4, W.acc5[s] = a5;
+            bool done = false;
+            uint32_t count = 0;
+            if (si >= P.min_samples - 1 && relative_std_err(a0.w, a1.w, si + 1) < P.variance_threshold) {
+                done = true;
+                count = si + 1;
+            } else if (++si == P.max_samples) {
+                done = true;
+                count = si + 1;  // loop ran out: normalised by maxSamples + 1 (renderer.cs:215)
             }
+            uint32_t x, y;
+            slot_pixel(W, s, x, y);
+            if (done) {
+                float var = relative_std_err(a2.w, a3.w, count);
+                Col r = col3(a0) / (float)count;
+                Col f = col3(a1) / (float)count;
+                V3 nsum{a2.x, a2.y, a2.z}, nfb{a3.x, a3.y, a3.z};
+                V3 nrm = ncount > 0 ? normalize_or(nsum, nfb) : V3{0.f, 0.f, 0.f};
+                size_t i = (size_t)y * P.width + x;
+                out.radiance[3 * i] = r.r, out.radiance[3 * i + 1] = r.g, out.radiance[3 * i + 2] = r.b;
+                out.radiance_fog[3 * i] = f.r, out.radiance_fog[3 * i + 1] = f.g, out.radiance_fog[3 * i + 2] = f.b;
+                out.normals[3 * i] = nrm.x, out.normals[3 * i + 1] = nrm.y, out.normals[3 * i + 2] = nrm.z;
+                out.uv[2 * i] = a5.x, out.uv[2 * i + 1] = a5.y;
+                out.depth[i] = dcount > 0 ? a4.x / (float)dcount : __int_as_float(0x7f800000);
+                out.samples[i] = count;
+                out.variance[i] = var;
+            } else {
+                Rng rng = rng_of(gr);
+                Ray ray = camera_ray(V, P, x, y, rng);
+                begin_sample(W, s, ray, rng);
+                live = true;
+                trace = needs_trace<COUNT>(W, S, s, ray, c);
+            }
+            a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
+            W.pix[pix(s, X_ACC)] = {a0, a1};
+            W.pix[pix(s, X_ACC + 1)] = {a2, a3};
+            W.pix[pix(s, X_ACC + 2)] = {a4, a5};
         }
-        push(W.q_active[nxt], &W.counts[nxt], s, valid && live);
+        push_block<2>({W.q_active[nxt], W.q_trace[nxt]}, {&W.counts[nxt], &W.counts[kCountTrace + nxt]}, s,
+                      {valid && live, valid && trace}, sh, round++);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -452,9 +619,9 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
 // Condition of the device-side bounce loop: continue while paths are live and the bounce cap
 // (max_samples * (bounces + 1) per pixel, plus slack) is not reached.
 __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, uint32_t max_iters, uint32_t* err) {
-    uint32_t it = counts[3] + 2;  // two bounces per loop body
-    counts[3] = it;
-    bool more = counts[0] > 0;
+    uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
+    counts[kCountIter] = it;
+    bool more = counts[kCountLive] > 0;
     if (more && it >= max_iters) {
         atomicOr(err, SR_DEVERR_LOOP);
         more = false;
@@ -466,33 +633,38 @@ __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* cou
 template <bool COUNT, bool GENERAL>
 static void launch_bounce(const WaveLaunch& L, int cur, cudaStream_t st) {
     k_wave_extend<COUNT, GENERAL><<<L.grid_extend, 128, 0, st>>>(L.W, L.S, cur, L.err, L.counters);
+    k_wave_classify<<<L.grid_classify, 128, 0, st>>>(L.W, L.S, cur);
     k_wave_shade<COUNT, GENERAL><<<L.grid_shade, 128, 0, st>>>(L.W, L.S, L.P, cur, L.err, L.counters);
     k_wave_shadow<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(L.W, L.S, L.err, L.counters);
-    k_wave_finalize<COUNT, GENERAL><<<L.grid_resolve, 128, 0, st>>>(L.W, L.S, L.V, L.P, L.out, cur, L.err,
-                                                                    L.counters);
+    k_wave_finalize<COUNT, GENERAL><<<L.grid_finalize, 128, 0, st>>>(L.W, L.S, L.V, L.P, L.out, cur, L.err,
+                                                                     L.counters);
+}
+
+template <bool GENERAL>
+static void occupancy(int* b) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_wave_extend<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_classify, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_shade<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shadow<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_wave_finalize<false, GENERAL>, 128, 0);
 }
 
 void wave_grid_sizes(WaveLaunch& L, int sms) {
-    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-    if (L.general) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_wave_extend<false, true>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_wave_shade<false, true>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_wave_finalize<false, true>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_wave_shadow<false, true>, 128, 0);
-    } else {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b0, k_wave_extend<false, false>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b1, k_wave_shade<false, false>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_wave_finalize<false, false>, 128, 0);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, k_wave_shadow<false, false>, 128, 0);
-    }
-    L.grid_extend = sms * (b0 > 0 ? b0 : 1);
-    L.grid_shade = sms * (b1 > 0 ? b1 : 1);
-    L.grid_resolve = sms * (b2 > 0 ? b2 : 1);
-    L.grid_shadow = sms * (b3 > 0 ? b3 : 1);
+    int b[5] = {0, 0, 0, 0, 0};
+    if (L.general)
+        occupancy<true>(b);
+    else
+        occupancy<false>(b);
+    for (int& v : b) v = sms * (v > 0 ? v : 1);
+    L.grid_extend = b[0];
+    L.grid_classify = b[1];
+    L.grid_shade = b[2];
+    L.grid_shadow = b[3];
+    L.grid_finalize = b[4];
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(L.W.counts, 0, 8 * sizeof(uint32_t), st);
+    cudaError_t e = cudaMemsetAsync(L.W.counts, 0, kWaveCounters * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     k_wave_init<<<(L.W.slots + 127) / 128, 128, 0, st>>>(L.W, L.V, L.P);
     return cudaGetLastError();

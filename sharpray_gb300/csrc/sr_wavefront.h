@@ -8,38 +8,43 @@
 
 namespace sr {
 
-// Structure-of-arrays path state, one slot per pixel (slots in 8x4 pixel tiles).
+// One 32-byte sector.  Path state is stored as records of fields that the kernels read and write
+// together, so that a lane touching a path moves whole DRAM bursts: the slots a warp visits are
+// scattered (queues are compacted in arrival order), and 16-byte fields in separate planes would
+// waste most of every burst read and turn every write into a partial write.
+struct alignas(32) Rec {
+    float4 a, b;
+};
+
+// Path state, one slot per pixel (slots in 8x4 pixel tiles).
 struct WaveState {
     uint32_t slots;    // tiles_x * tiles_y * 32
     uint32_t tiles_x;  // ceil(width / 8)
-    uint4* rng;        // RNG words s0..s3
-    uint32_t* rng_c;   // RNG Weyl counter s4
-    float4* ray_o;     // ray origin, w = bounce index (int bits)
-    float4* ray_d;     // ray direction, w = path flags (int bits)
-    float4* rad;       // path radiance, w = pdf of the last scatter
-    float4* fog;       // path fog radiance (primary-segment fog scatter)
-    float4* energy;    // path throughput
-    float4* medium;    // albedo of the medium the path is inside
-    float4* prim;      // primary-hit normal, depth
-    float2* prim_uv;   // primary-hit uv
-    float4* acc0;      // pixel: radiance sum, luminance sum
-    float4* acc1;      // pixel: fog radiance sum, luminance^2 sum
-    float4* acc2;      // pixel: normal sum, surface luminance sum
-    float4* acc3;      // pixel: last normal, surface luminance^2 sum
-    float4* acc4;      // pixel: depth sum, normal count, depth count, sample index (int bits)
-    float4* acc5;      // pixel: first uv, has-uv flag
-    float4* hit;       // closest hit: object, triangle (int bits), world distance, local distance
-    float2* hit_uv;    // closest hit barycentrics
-    float4* sh0;       // deferred work: shadow origin (then its transmittance), request flags (int bits)
-    float4* sh1;       // shadow direction, light pdf
-    float4* sh2;       // reflectance (or phase pdf) rgb, MIS weight
-    float4* sh3;       // throughput at the light sample
+    Rec* rec;          // path records, six sectors per slot (192 bytes, 64-byte aligned):
+                       //   ray  a: origin, bounce index (int bits)      b: direction, -
+                       //   hit  a: object, triangle (int bits), world distance, local distance
+                       //        b: barycentric u, v, fog scatter distance, -
+                       //   path a: radiance, pdf of the last scatter    b: throughput, path flags (int bits)
+                       //   rng  a: RNG words s0..s3 (bits)              b: RNG counter s4 (bits), fog radiance
+                       //   sh0  a: shadow origin (then transmittance)   b: shadow direction, light pdf
+                       //   sh1  a: reflectance or phase pdf, MIS weight b: throughput at the light sample
+    Rec* pix;          // pixel records, four sectors per slot:
+                       //   prim a: primary-hit normal, depth            b: primary-hit uv, -, -
+                       //   acc0 a: radiance sum, luminance sum          b: fog radiance sum, luminance^2 sum
+                       //   acc1 a: normal sum, surface lum sum          b: last normal, surface lum^2 sum
+                       //   acc2 a: depth sum, normal count, depth count, sample index (int bits)
+                       //        b: first uv, has-uv flag, -
+    float4* medium;    // albedo of the medium the path is inside (scenes with refraction only)
     uint32_t* q_active[2];  // live-path queues (ping-pong)
-    uint32_t* q_resolve;    // deferred-work queue (shadow requests and finished samples)
+    uint32_t* q_trace[2];   // the live paths whose ray needs a traversal (ping-pong)
+    uint32_t* q_event;      // three queues of `slots` entries: fog scatter, miss, surface hit
+    uint32_t* q_resolve;    // finished samples
     uint32_t* q_shadow;     // shadow-ray queue
-    uint32_t* counts;       // [0],[1] live counts, [2] deferred count, [3] bounce counter,
-                            // [4] extend fetch, [5] shadow fetch, [6] shadow count
+    uint32_t* counts;       // see kCount* in sr_wavefront.cu
 };
+
+// Number of 32-bit counters at WaveState::counts.
+constexpr int kWaveCounters = 16;
 
 struct WaveLaunch {
     WaveState W;
@@ -49,10 +54,13 @@ struct WaveLaunch {
     DevAovs out;
     uint32_t* err;
     unsigned long long* counters;
-    int grid_extend, grid_shade, grid_resolve, grid_shadow;
+    int grid_extend, grid_classify, grid_shade, grid_shadow, grid_finalize;
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
 };
+
+// Kernels launched per bounce (extend, classify, shade, shadow, finalize).
+constexpr int kWaveKernelsPerBounce = 5;
 
 void wave_grid_sizes(WaveLaunch& L, int sms);
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st);
