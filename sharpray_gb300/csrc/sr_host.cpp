@@ -724,9 +724,9 @@ static int wave_reserve(SrScene* s, uint32_t slots) {
     if (s->wave_slots >= slots && s->wave.ptr) return SR_OK;
     const size_t n = slots;
     // 32-byte sectors: path records (6 per slot), pixel records (4 per slot); 16-byte medium;
-    // 4-byte queues: live x2, trace x2, event x3, resolve, shadow; each array starts on 256 bytes
+    // 4-byte queues: trace x2, event 3 x2, resolve, shadow; each array starts on 256 bytes
     const size_t rec = sizeof(Rec);
-    size_t bytes = n * (10 * rec + 16 + 9 * 4) + 16 * 256 + kWaveCounters * sizeof(uint32_t);
+    size_t bytes = n * (10 * rec + 16 + 10 * 4) + 16 * 256 + kWaveCounters * sizeof(uint32_t);
     SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
     char* p = s->wave.as<char>();
     auto take = [&](size_t elem_bytes) {
@@ -738,11 +738,10 @@ static int wave_reserve(SrScene* s, uint32_t slots) {
     w.rec = (Rec*)take(6 * rec);
     w.pix = (Rec*)take(4 * rec);
     w.medium = (float4*)take(16);
-    w.q_active[0] = (uint32_t*)take(4);
-    w.q_active[1] = (uint32_t*)take(4);
     w.q_trace[0] = (uint32_t*)take(4);
     w.q_trace[1] = (uint32_t*)take(4);
-    w.q_event = (uint32_t*)take(3 * 4);
+    w.q_event[0] = (uint32_t*)take(3 * 4);
+    w.q_event[1] = (uint32_t*)take(3 * 4);
     w.q_resolve = (uint32_t*)take(4);
     w.q_shadow = (uint32_t*)take(4);
     w.counts = (uint32_t*)p;
@@ -789,15 +788,15 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
         SR_CUDA(cudaGraphLaunch(s->graph_exec, st), "launch bounce-loop graph");
         return SR_OK;
     }
-    if (!s->counts_host) SR_CUDA(cudaMallocHost(&s->counts_host, 4 * sizeof(uint32_t)), "pinned alloc");
+    if (!s->counts_host) SR_CUDA(cudaMallocHost(&s->counts_host, kWaveCounters * sizeof(uint32_t)), "pinned alloc");
     for (uint32_t it = 0;; ++it) {
         if (it >= L.max_iters) return fail(SR_ERR_DEVICE, "wavefront loop exceeded %u bounces", L.max_iters);
         int cur = (int)(it & 1u);
         SR_CUDA(wave_bounce(L, cur, st), "wavefront bounce");
-        SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws.counts + (cur ^ 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+        SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws.counts, kWaveCounters * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
                 "read live count");
         SR_CUDA(cudaStreamSynchronize(st), "wavefront bounce");
-        if (s->counts_host[0] == 0) {
+        if (wave_live(s->counts_host, cur ^ 1) == 0) {
             s->last_host_iters = it + 1;
             break;
         }
@@ -904,7 +903,7 @@ SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t*
     }
     uint32_t iters = s->last_host_iters;
     if (s->last_mode == SR_RENDER_WAVEFRONT_GRAPH) {
-        SR_CUDA(cudaMemcpy(&iters, s->ws.counts + 3, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
+        SR_CUDA(cudaMemcpy(&iters, s->ws.counts + kCountIter, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
         // init, the bounce kernels, one loop condition per 2 bounces
         *kernel_launches = 1 + kWaveKernelsPerBounce * iters + iters / 2;
     } else {

@@ -159,14 +159,15 @@ __device__ __forceinline__ float relative_std_err(float sum, float sum_sqr, uint
 
 template <bool COUNT>
 __device__ __forceinline__ void flush_counters(Ctr& c, unsigned long long* counters) {
-    if (!COUNT) return;
+    if constexpr (COUNT) {
 #pragma unroll
-    for (int i = 0; i < SR_COUNTER_COUNT; ++i) {
-        unsigned long long v = c.v[i];
-        // warp reduction keeps the atomics to one per warp and counter
-        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-        if ((threadIdx.x & 31) == 0 && v) atomicAdd(counters + i, v);
-        c.v[i] = 0;
+        for (int i = 0; i < SR_COUNTER_COUNT; ++i) {
+            unsigned long long v = c.v[i];
+            // warp reduction keeps the atomics to one per warp and counter
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if ((threadIdx.x & 31) == 0 && v) atomicAdd(counters + i, v);
+            c.v[i] = 0;
+        }
     }
 }
 

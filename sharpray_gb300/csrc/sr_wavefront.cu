@@ -1,13 +1,14 @@
 // sr_wavefront.cu — wavefront form of the per-pixel path loop.
 //
-// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into five
+// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into four
 // kernels per bounce over per-path state records, one slot per pixel:
 //
 //   extend   : closest hit of every live path ray            (Scene.Trace -> Bvh.Intersect)
-//              that enters the root boxes of the scene BVH (the others are decided when the ray
-//              is made: in foggy scenes most rays start far outside the scene and leave it)
-//   classify : the segment's event -- fog scatter (the free-flight distance is drawn here, the
-//              first RNG draw of the segment), surface hit or miss -- and one queue per event
+//              that enters the root boxes of the scene BVH, then the segment's event -- fog
+//              scatter (the free-flight distance is drawn here, the segment's first RNG draw),
+//              surface hit or miss -- and one queue per event.  A ray that misses the root boxes
+//              gets its event where it is made (in foggy scenes most rays start far outside the
+//              scene and leave it)
 //   shade    : first the NEE contribution of the previous segment (its shadow ray has been traced
 //              since), then the event's logic: light sample, Russian roulette, scatter
 //   shadow   : shadow rays (ShadowTransmittance, scene.cs:576-600) times the fog transmittance
@@ -22,8 +23,9 @@
 // queue at once (refilled per warp with one atomic), so warps stay full although ray lengths
 // differ by orders of magnitude.
 //
-// Live paths are compacted between kernels with block-aggregated atomics (ballot + popc per warp,
-// one atomic per block and queue), so every launch works on dense queues.  Every per-path operation -- RNG draws, float operation order,
+// Paths are compacted into queues between kernels with aggregated atomics (per block in the
+// grid-stride kernels, per warp and 32 entries in the persistent ones), so every launch works on
+// dense queues.  Every per-path operation -- RNG draws, float operation order,
 // the order in which contributions are added -- is the megakernel's (sr_path.cuh), so the two
 // forms produce identical images: a segment's NEE contribution is added before anything of the
 // next segment touches the radiance, exactly where the megakernel adds it.
@@ -48,17 +50,6 @@ enum : uint32_t {
 };
 // segment events (queue index)
 enum : int { EV_FOG = 0, EV_MISS = 1, EV_SURF = 2 };
-// WaveState::counts
-enum : int {
-    kCountLive = 0,          // [0], [1]: live-queue lengths (ping-pong)
-    kCountResolve = 2,       // finished samples of this bounce
-    kCountIter = 3,          // bounces run by the device loop
-    kCountExtendFetch = 4,   // extend's fetch cursor
-    kCountShadowFetch = 5,   // shadow's fetch cursor
-    kCountShadow = 6,        // shadow rays of this bounce
-    kCountEvent = 8,         // [8..10]: event-queue lengths
-    kCountTrace = 11,        // [11], [12]: trace-queue lengths (ping-pong)
-};
 
 // Sectors of a slot's path record (WaveState::rec, six per slot, 192 bytes on 64-byte boundaries:
 // {ray, hit}, {path, rng} and the shadow request each fill one 64-byte DRAM burst) and of its pixel
@@ -130,7 +121,7 @@ __device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, con
 }
 
 __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevParams P) {
-    __shared__ uint32_t sh[2][2][kBlockWarps + 1];
+    __shared__ uint32_t sh[2][1][kBlockWarps + 1];
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = false;
     if (s < W.slots) {
@@ -147,21 +138,84 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
             W.pix[pix(s, X_ACC + 2)] = {z, z};  // counts and sample index start at 0 (int bits)
         }
     }
-    push_block<2>({W.q_active[0], W.q_trace[0]}, {&W.counts[kCountLive], &W.counts[kCountTrace]}, s, {valid, valid}, sh,
-                  0u);
+    push_block<1>({W.q_trace[0]}, {&W.counts[kCountTrace]}, s, {valid}, sh, 0u);
 }
 
-// A new path ray (scatter or camera ray): it needs the next extend's traversal unless it misses
-// both root children of the scene BVH, the first thing the traversal tests; then its empty
-// closest hit is written here, as extend would write it.
-template <bool COUNT>
-__device__ __forceinline__ bool needs_trace(const WaveState& W, const DevScene& S, uint32_t s, const Ray& ray, Ctr& c) {
-    if (!misses_scene<COUNT, false>(S, ray, c)) return true;
-    SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-    W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(-1), __int_as_float(-1), __int_as_float(0x7f800000), 0.f),
-                make_float4(0.f, 0.f, 0.f, 0.f)};
-    return false;
+// The event of a segment whose closest hit is known (scene.cs:654-738 decides in this order):
+// with fog set, the free-flight distance is drawn first -- the segment's first RNG draw -- and wins
+// if it is shorter than the hit; else a hit is a surface event and no hit a miss.
+__device__ __forceinline__ int segment_event(const DevScene& S, const Ray& ray, bool has_hit, float hit_dist, Rng& rng,
+                                             float& sdist) {
+    sdist = 0.f;
+    if (S.has_fog && fog_scatter_distance(S, ray, has_hit ? hit_dist : __int_as_float(0x7f800000), rng, sdist))
+        return EV_FOG;
+    return has_hit ? EV_SURF : EV_MISS;
 }
+
+// A new path ray (scatter or camera ray): -1 when it needs the next extend's traversal; when it
+// misses both root children of the scene BVH -- the first thing the traversal tests -- its empty
+// closest hit is written here, as extend would write it, and its segment's event is returned.
+template <bool COUNT>
+__device__ __forceinline__ int next_segment(const WaveState& W, const DevScene& S, uint32_t s, const Ray& ray, Rng& rng,
+                                            Ctr& c) {
+    if (!misses_scene<COUNT, false>(S, ray, c)) return -1;
+    SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
+    float sdist;
+    int ev = segment_event(S, ray, false, 0.f, rng, sdist);
+    W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(-1), __int_as_float(-1), __int_as_float(0x7f800000), 0.f),
+                            make_float4(0.f, 0.f, sdist, 0.f)};
+    return ev;
+}
+
+// Per-warp staging of the persistent loop's appends to NQ queues: entries collect in a shared
+// ring of 64 per queue and go out 32 at a time (one atomic and one coalesced write per 32
+// entries).  All 32 lanes call add() and flush() together.
+template <int NQ>
+struct WarpStage {
+    uint32_t* buf;  // this warp's [NQ][64] shared ring
+    uint32_t head[NQ], cnt[NQ];
+
+    __device__ __forceinline__ void init(uint32_t* ring) {
+        buf = ring;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) head[k] = cnt[k] = 0;
+    }
+    // value goes to queue `which` (-1: nothing)
+    __device__ __forceinline__ void add(uint32_t* const (&q)[NQ], uint32_t* const (&count)[NQ], uint32_t value,
+                                        int which) {
+        const int lane = threadIdx.x & 31;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+            unsigned m = __ballot_sync(0xffffffffu, which == k);
+            if (!m) continue;
+            if (which == k) buf[k * 64 + ((head[k] + cnt[k] + (uint32_t)__popc(m & ((1u << lane) - 1u))) & 63u)] = value;
+            cnt[k] += (uint32_t)__popc(m);
+            if (cnt[k] >= 32u) {
+                __syncwarp();
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(count[k], 32u);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                q[k][base + lane] = buf[k * 64 + ((head[k] + lane) & 63u)];
+                __syncwarp();
+                head[k] = (head[k] + 32u) & 63u;
+                cnt[k] -= 32u;
+            }
+        }
+    }
+    __device__ __forceinline__ void flush(uint32_t* const (&q)[NQ], uint32_t* const (&count)[NQ]) {
+        const int lane = threadIdx.x & 31;
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+            if (!cnt[k]) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(count[k], cnt[k]);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if ((uint32_t)lane < cnt[k]) q[k][base + lane] = buf[k * 64 + ((head[k] + lane) & 63u)];
+            cnt[k] = 0;
+        }
+    }
+};
 
 // A warp refills its idle lanes once at least this many are idle (or all are).
 #ifndef SR_REFILL
@@ -179,28 +233,42 @@ constexpr int kRefill = SR_REFILL;
 #define SR_NODE_BURST 8
 #endif
 #ifndef SR_LEAF_WAIT
-#define SR_LEAF_WAIT 8
+#define SR_LEAF_WAIT 16
+#endif
+// Minimum resident blocks per SM requested for the shading kernel (caps its registers).
+#ifndef SR_SHADE_MIN_BLOCKS
+#define SR_SHADE_MIN_BLOCKS 5
 #endif
 constexpr int kNodeBurst = SR_NODE_BURST;
 constexpr int kLeafWait = SR_LEAF_WAIT;
 
 // Persistent ray loop shared by extend and shadow: lanes take queue entries [fetch counter) until
-// the queue is exhausted; `start(slot)` begins a query, `finish(slot, hit, ray)` stores its answer.
+// the queue is exhausted; `start(slot)` begins a query, `finish(slot, hit, ray)` stores its answer
+// and returns an output code that `emit(slot, code)` (all lanes together, -1 = none) passes on.
 // Each round runs the node visits of all lanes together (up to kNodeBurst), then one leaf action
 // of each lane that waits for one: leaf actions are long and differ between lanes, so batching
-// them keeps warps from running each one with a single lane.  Every lane's own sequence of actions
-// is unchanged, so results are those of a plain loop over SceneQuery::step.
-template <bool COUNT, bool ANY, bool GENERAL, typename Start, typename Finish>
+// them keeps warps from running each one with a single lane.  Finished lanes are answered in a
+// batch when the warp refills.  Every lane's own sequence of actions is unchanged, so results are
+// those of a plain loop over SceneQuery::step.
+template <bool COUNT, bool ANY, bool GENERAL, typename Start, typename Finish, typename Emit>
 __device__ __forceinline__ void persistent_queries(const DevScene& S, const uint32_t* q, uint32_t n, uint32_t* fetch,
-                                                   Ctr& c, uint32_t* err, Start start, Finish finish) {
+                                                   Ctr& c, uint32_t* err, Start start, Finish finish, Emit emit) {
     StackEntry stack[kSceneStack];
     SceneQuery<ANY, GENERAL> sq;
-    bool busy = false, exhausted = false;
+    bool busy = false, pending = false, exhausted = false;
     uint32_t slot = 0;
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned idle = __ballot_sync(0xffffffffu, !busy);
         int nidle = __popc(idle);
+        if (nidle >= kRefill || (exhausted && idle == 0xffffffffu)) {
+            int code = -1;
+            if (pending) {
+                code = finish(slot, sq.best, sq.wr);
+                pending = false;
+            }
+            emit(slot, code);
+        }
         if (!exhausted && nidle >= kRefill) {
             uint32_t base = 0;
             if (lane == 0) base = atomicAdd(fetch, (uint32_t)nidle);
@@ -228,8 +296,8 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const uint
         }
         if (busy && sq.state != QS_NODE && sq.state != QS_DONE) sq.template leaf_action<COUNT>(S, stack, c, err);
         if (busy && sq.state == QS_DONE) {
-            finish(slot, sq.best, sq.wr);
             busy = false;
+            pending = true;
         }
     }
 }
@@ -237,15 +305,22 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const uint
 template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveState W, DevScene S, int cur, uint32_t* err,
                                                      unsigned long long* counters) {
+    const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        W.counts[kCountResolve] = 0;  // finished samples of this bounce
-        W.counts[kCountShadow] = 0;   // shadow queue of this bounce starts empty
-        W.counts[cur ^ 1] = 0;        // next live queue starts empty
-        W.counts[kCountTrace + (cur ^ 1)] = 0;
-        W.counts[kCountEvent + EV_FOG] = 0;
-        W.counts[kCountEvent + EV_MISS] = 0;
-        W.counts[kCountEvent + EV_SURF] = 0;
+        W.counts[kCountResolve] = 0;      // finished samples of this bounce
+        W.counts[kCountShadow] = 0;       // shadow queue of this bounce starts empty
+        W.counts[kCountTrace + nxt] = 0;  // the next bounce's queues start empty
+        W.counts[kCountEvent + 3 * nxt + EV_FOG] = 0;
+        W.counts[kCountEvent + 3 * nxt + EV_MISS] = 0;
+        W.counts[kCountEvent + 3 * nxt + EV_SURF] = 0;
     }
+    __shared__ uint32_t ring[kBlockWarps][3 * 64];
+    WarpStage<3> stage;
+    stage.init(ring[threadIdx.x >> 5]);
+    uint32_t* const eq[3] = {W.q_event[cur] + (size_t)EV_FOG * W.slots, W.q_event[cur] + (size_t)EV_MISS * W.slots,
+                             W.q_event[cur] + (size_t)EV_SURF * W.slots};
+    uint32_t* const ec[3] = {&W.counts[kCountEvent + 3 * cur + EV_FOG], &W.counts[kCountEvent + 3 * cur + EV_MISS],
+                             &W.counts[kCountEvent + 3 * cur + EV_SURF]};
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
@@ -256,50 +331,22 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveSt
             Rec r = W.rec[rix(s, R_RAY)];
             return make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
         },
-        [&](uint32_t s, const Hit& h, const Ray&) {
-            W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
-                        make_float4(h.u, h.v, 0.f, 0.f)};
-        });
-    flush_counters<COUNT>(c, counters);
-}
-
-// The event of each live segment (scene.cs:654-738 decides in this order): with fog set, the
-// free-flight distance is drawn first and wins if it is shorter than the hit; else a hit is a
-// surface event and no hit a miss.  The world distance of the closest hit is the one the surface
-// lookup reports (both divide the local distance by the same object-space scale).
-__global__ void __launch_bounds__(128) k_wave_classify(WaveState W, DevScene S, int cur) {
-    __shared__ uint32_t sh[2][3][kBlockWarps + 1];
-    uint32_t round = 0;
-    const uint32_t n = W.counts[cur];
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const float inf = __int_as_float(0x7f800000);
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        uint32_t k = base + threadIdx.x;
-        bool valid = k < n;
-        uint32_t s = valid ? W.q_active[cur][k] : 0u;
-        int ev = EV_MISS;
-        if (valid) {
-            Rec h = W.rec[rix(s, R_HIT)];
-            bool has_hit = __float_as_int(h.a.x) >= 0;
-            ev = has_hit ? EV_SURF : EV_MISS;
+        [&](uint32_t s, const Hit& h, const Ray& ray) {
+            float sdist = 0.f;
+            int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
             if (S.has_fog) {
-                Rec r = W.rec[rix(s, R_RAY)];
                 Rec g = W.rec[rix(s, R_RNG)];
                 Rng rng = rng_of(g);
-                Ray ray{V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z}, V3{0.f, 0.f, 0.f}};
-                float sdist;
-                if (fog_scatter_distance(S, ray, has_hit ? h.a.z : inf, rng, sdist)) {
-                    ev = EV_FOG;
-                    W.rec[rix(s, R_HIT)].b = make_float4(h.b.x, h.b.y, sdist, 0.f);
-                }
+                ev = segment_event(S, ray, h.obj >= 0, h.dist, rng, sdist);
                 W.rec[rix(s, R_RNG)] = rng_rec(rng, Col{g.b.y, g.b.z, g.b.w});
             }
-        }
-        push_block<3>({W.q_event + (size_t)EV_FOG * W.slots, W.q_event + (size_t)EV_MISS * W.slots,
-                       W.q_event + (size_t)EV_SURF * W.slots},
-                      {&W.counts[kCountEvent + EV_FOG], &W.counts[kCountEvent + EV_MISS], &W.counts[kCountEvent + EV_SURF]},
-                      s, {valid && ev == EV_FOG, valid && ev == EV_MISS, valid && ev == EV_SURF}, sh, round++);
-    }
+            W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
+                                    make_float4(h.u, h.v, sdist, 0.f)};
+            return ev;
+        },
+        [&](uint32_t s, int ev) { stage.add(eq, ec, s, ev); });
+    stage.flush(eq, ec);
+    flush_counters<COUNT>(c, counters);
 }
 
 // Shadow rays of the bounce: transmittance (any hit -> black in opaque scenes) times the fog
@@ -325,7 +372,9 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
                     if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, ray);
                 }
                 W.rec[rix(s, R_SH0)].a = make_float4(tr, tr, tr, 0.f);
-            });
+                return -1;
+            },
+            [](uint32_t, int) {});
     } else {
         const uint32_t n = W.counts[kCountShadow];
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
@@ -363,17 +412,17 @@ __device__ __forceinline__ void add_nee(const WaveState& W, const DevScene& S, u
 // the miss queue, then the surface queue, the first two padded to whole warps, so every warp
 // runs one event's logic.
 template <bool COUNT, bool GENERAL>
-__global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, uint32_t* err,
+__global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, uint32_t* err,
                                                     unsigned long long* counters) {
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountShadowFetch] = 0;
-    __shared__ uint32_t sh[2][4][kBlockWarps + 1];
+    __shared__ uint32_t sh[2][5][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     const int nxt = cur ^ 1;
-    const uint32_t nfog = W.counts[kCountEvent + EV_FOG], nmiss = W.counts[kCountEvent + EV_MISS],
-                   nsurf = W.counts[kCountEvent + EV_SURF];
+    const uint32_t* ecount = W.counts + kCountEvent + 3 * cur;
+    const uint32_t nfog = ecount[EV_FOG], nmiss = ecount[EV_MISS], nsurf = ecount[EV_SURF];
     const uint32_t pfog = (nfog + 31u) & ~31u, pmiss = (nmiss + 31u) & ~31u;
     const uint32_t total = pfog + pmiss + nsurf;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -389,8 +438,9 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
             ev = EV_SURF, i = k - pfog - pmiss, cnt = nsurf;
         }
         const bool valid = i < cnt;
-        const uint32_t s = valid ? W.q_event[(size_t)ev * W.slots + i] : 0u;
-        bool live = false, shadow_req = false, trace = false;
+        const uint32_t s = valid ? W.q_event[cur][(size_t)ev * W.slots + i] : 0u;
+        bool live = false, shadow_req = false;
+        int next = -1;  // next segment: -1 traced, else its event
         if (valid) {
             SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
             Rec rr = W.rec[rix(s, R_RAY)], pr = W.rec[rix(s, R_PATH)], gr = W.rec[rix(s, R_RNG)];
@@ -512,16 +562,22 @@ __global__ void __launch_bounds__(128) k_wave_shade(WaveState W, DevScene S, Dev
             live = !terminate;
             W.rec[rix(s, R_PATH)] = {make_float4(radiance.r, radiance.g, radiance.b, spdf),
                          make_float4(energy.r, energy.g, energy.b, fbits(pflags))};
-            W.rec[rix(s, R_RNG)] = rng_rec(rng, fog);
             if (live) {
                 W.rec[rix(s, R_RAY)] = {make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                            make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)};
-                trace = needs_trace<COUNT>(W, S, s, ray, c);
+                                        make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)};
+                next = next_segment<COUNT>(W, S, s, ray, rng, c);
             }
+            W.rec[rix(s, R_RNG)] = rng_rec(rng, fog);
         }
-        push_block<4>({W.q_active[nxt], W.q_trace[nxt], W.q_resolve, W.q_shadow},
-                      {&W.counts[nxt], &W.counts[kCountTrace + nxt], &W.counts[kCountResolve], &W.counts[kCountShadow]},
-                      s, {valid && live, valid && trace, valid && !live, valid && shadow_req}, sh, round++);
+        uint32_t* eq = W.q_event[nxt];
+        push_block<5>({W.q_trace[nxt], eq + (size_t)EV_FOG * W.slots, eq + (size_t)EV_MISS * W.slots, W.q_resolve,
+                       W.q_shadow},
+                      {&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
+                       &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve], &W.counts[kCountShadow]},
+                      s,
+                      {valid && live && next < 0, valid && live && next == EV_FOG, valid && live && next == EV_MISS,
+                       valid && !live, valid && shadow_req},
+                      sh, round++);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -532,7 +588,7 @@ template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, DevView V, DevParams P, DevAovs out,
                                                        int cur, uint32_t* err, unsigned long long* counters) {
     if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountExtendFetch] = 0;  // next extend's fetch cursor
-    __shared__ uint32_t sh[2][2][kBlockWarps + 1];
+    __shared__ uint32_t sh[2][3][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
 #pragma unroll
@@ -544,7 +600,8 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
         uint32_t k = base + threadIdx.x;
         bool valid = k < n;
         uint32_t s = valid ? W.q_resolve[k] : 0u;
-        bool live = false, trace = false;
+        bool live = false;
+        int next = -1;
         if (valid) {
             Rec pr = W.rec[rix(s, R_PATH)], gr = W.rec[rix(s, R_RNG)];
             uint32_t pflags = ibits(pr.b.w);
@@ -601,17 +658,21 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
             } else {
                 Rng rng = rng_of(gr);
                 Ray ray = camera_ray(V, P, x, y, rng);
+                next = next_segment<COUNT>(W, S, s, ray, rng, c);
                 begin_sample(W, s, ray, rng);
                 live = true;
-                trace = needs_trace<COUNT>(W, S, s, ray, c);
             }
             a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
             W.pix[pix(s, X_ACC)] = {a0, a1};
             W.pix[pix(s, X_ACC + 1)] = {a2, a3};
             W.pix[pix(s, X_ACC + 2)] = {a4, a5};
         }
-        push_block<2>({W.q_active[nxt], W.q_trace[nxt]}, {&W.counts[nxt], &W.counts[kCountTrace + nxt]}, s,
-                      {valid && live, valid && trace}, sh, round++);
+        uint32_t* eq = W.q_event[nxt];
+        push_block<3>({W.q_trace[nxt], eq + (size_t)EV_FOG * W.slots, eq + (size_t)EV_MISS * W.slots},
+                      {&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
+                       &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
+                      s, {valid && live && next < 0, valid && live && next == EV_FOG, valid && live && next == EV_MISS},
+                      sh, round++);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -621,7 +682,7 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
 __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, uint32_t max_iters, uint32_t* err) {
     uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
     counts[kCountIter] = it;
-    bool more = counts[kCountLive] > 0;
+    bool more = wave_live(counts, 0) > 0;  // the body's second bounce has parity 1
     if (more && it >= max_iters) {
         atomicOr(err, SR_DEVERR_LOOP);
         more = false;
@@ -633,7 +694,6 @@ __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* cou
 template <bool COUNT, bool GENERAL>
 static void launch_bounce(const WaveLaunch& L, int cur, cudaStream_t st) {
     k_wave_extend<COUNT, GENERAL><<<L.grid_extend, 128, 0, st>>>(L.W, L.S, cur, L.err, L.counters);
-    k_wave_classify<<<L.grid_classify, 128, 0, st>>>(L.W, L.S, cur);
     k_wave_shade<COUNT, GENERAL><<<L.grid_shade, 128, 0, st>>>(L.W, L.S, L.P, cur, L.err, L.counters);
     k_wave_shadow<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(L.W, L.S, L.err, L.counters);
     k_wave_finalize<COUNT, GENERAL><<<L.grid_finalize, 128, 0, st>>>(L.W, L.S, L.V, L.P, L.out, cur, L.err,
@@ -643,24 +703,22 @@ static void launch_bounce(const WaveLaunch& L, int cur, cudaStream_t st) {
 template <bool GENERAL>
 static void occupancy(int* b) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_wave_extend<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_classify, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_shade<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shadow<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_wave_finalize<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_shade<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_shadow<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_finalize<false, GENERAL>, 128, 0);
 }
 
 void wave_grid_sizes(WaveLaunch& L, int sms) {
-    int b[5] = {0, 0, 0, 0, 0};
+    int b[4] = {0, 0, 0, 0};
     if (L.general)
         occupancy<true>(b);
     else
         occupancy<false>(b);
     for (int& v : b) v = sms * (v > 0 ? v : 1);
     L.grid_extend = b[0];
-    L.grid_classify = b[1];
-    L.grid_shade = b[2];
-    L.grid_shadow = b[3];
-    L.grid_finalize = b[4];
+    L.grid_shade = b[1];
+    L.grid_shadow = b[2];
+    L.grid_finalize = b[3];
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {

@@ -35,16 +35,33 @@ struct WaveState {
                        //   acc2 a: depth sum, normal count, depth count, sample index (int bits)
                        //        b: first uv, has-uv flag, -
     float4* medium;    // albedo of the medium the path is inside (scenes with refraction only)
-    uint32_t* q_active[2];  // live-path queues (ping-pong)
-    uint32_t* q_trace[2];   // the live paths whose ray needs a traversal (ping-pong)
-    uint32_t* q_event;      // three queues of `slots` entries: fog scatter, miss, surface hit
+    uint32_t* q_trace[2];   // paths whose next ray needs a traversal (ping-pong by bounce parity)
+    uint32_t* q_event[2];   // paths whose next segment's event is known, three queues of `slots`
+                            // entries each: fog scatter, miss, surface hit (ping-pong)
     uint32_t* q_resolve;    // finished samples
     uint32_t* q_shadow;     // shadow-ray queue
-    uint32_t* counts;       // see kCount* in sr_wavefront.cu
+    uint32_t* counts;       // kCount* below
 };
 
-// Number of 32-bit counters at WaveState::counts.
+// Number of 32-bit counters at WaveState::counts, and their layout.
 constexpr int kWaveCounters = 16;
+enum : int {
+    kCountResolve = 0,       // finished samples of this bounce
+    kCountIter = 1,          // bounces run by the device loop
+    kCountExtendFetch = 2,   // extend's fetch cursor
+    kCountShadowFetch = 3,   // shadow's fetch cursor
+    kCountShadow = 4,        // shadow rays of this bounce
+    kCountTrace = 6,         // + parity: trace-queue length
+    kCountEvent = 8,         // + 3 * parity + event: event-queue lengths
+};
+// Paths alive for the bounce of the given parity: queued for a traversal or with a known event.
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline uint32_t wave_live(const uint32_t* counts, int parity) {
+    return counts[kCountTrace + parity] + counts[kCountEvent + 3 * parity] + counts[kCountEvent + 3 * parity + 1] +
+           counts[kCountEvent + 3 * parity + 2];
+}
 
 struct WaveLaunch {
     WaveState W;
@@ -54,13 +71,13 @@ struct WaveLaunch {
     DevAovs out;
     uint32_t* err;
     unsigned long long* counters;
-    int grid_extend, grid_classify, grid_shade, grid_shadow, grid_finalize;
+    int grid_extend, grid_shade, grid_shadow, grid_finalize;
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
 };
 
-// Kernels launched per bounce (extend, classify, shade, shadow, finalize).
-constexpr int kWaveKernelsPerBounce = 5;
+// Kernels launched per bounce (extend, shade, shadow, finalize).
+constexpr int kWaveKernelsPerBounce = 4;
 
 void wave_grid_sizes(WaveLaunch& L, int sms);
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st);
