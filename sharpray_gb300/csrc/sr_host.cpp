@@ -136,8 +136,10 @@ struct SrScene {
     int32_t render_mode = SR_RENDER_AUTO;
     DevBuf wave;
     uint32_t wave_slots = 0;
-    WaveState ws{};
+    WaveState ws[kWaveGroups]{};
     cudaStream_t capture_stream = nullptr;
+    cudaStream_t side_streams[kWaveGroups > 1 ? kWaveGroups - 1 : 1] = {};  // groups 1.. of a bounce
+    cudaEvent_t fork_events[kWaveGroups] = {};                              // fork, then joins
     cudaGraphExec_t graph_exec = nullptr;
     WaveLaunch graph_launch{};  // launch parameters baked into graph_exec
     uint32_t* counts_host = nullptr;  // pinned
@@ -147,6 +149,10 @@ struct SrScene {
     ~SrScene() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (capture_stream) cudaStreamDestroy(capture_stream);
+        for (cudaStream_t& st : side_streams)
+            if (st) cudaStreamDestroy(st);
+        for (cudaEvent_t& e : fork_events)
+            if (e) cudaEventDestroy(e);
         if (counts_host) cudaFreeHost(counts_host);
     }
 };
@@ -719,50 +725,69 @@ static int make_view(const SrView* v, const SrRenderParams* p, DevView& dv, DevP
 static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t h, const SrComposeParams* p,
                         bool denoise, uint8_t* rgb8, cudaStream_t st);
 
-// Allocates the wavefront path state for `slots` pixel slots (one block, carved into the arrays).
-static int wave_reserve(SrScene* s, uint32_t slots) {
-    if (s->wave_slots >= slots && s->wave.ptr) return SR_OK;
-    const size_t n = slots;
-    // 32-byte sectors: path records (6 per slot), pixel records (4 per slot); 16-byte medium;
-    // 4-byte queues: trace x2, event 3 x2, resolve, shadow; each array starts on 256 bytes
-    const size_t rec = sizeof(Rec);
-    size_t bytes = n * (10 * rec + 16 + 10 * 4) + 16 * 256 + kWaveCounters * sizeof(uint32_t);
-    SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
+// Allocates the wavefront path state for a tiles_x x tiles_y grid of 8x4 slot tiles: the records
+// of every slot, then each group's queues, then every group's counters (one block, carved).
+static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
+    const uint32_t tiles = tiles_x * tiles_y;
+    const size_t n = (size_t)tiles * 32;
+    uint32_t group_slots[kWaveGroups];
+    for (int g = 0; g < kWaveGroups; ++g) group_slots[g] = (uint32_t)(tiles > (uint32_t)g ? (tiles - g + kWaveGroups - 1) / kWaveGroups : 0) * 32;
+    if (s->wave_slots < n || !s->wave.ptr) {
+        // 32-byte sectors: path records (6 per slot), pixel records (4 per slot); 16-byte medium;
+        // 4-byte queues: trace x2, event 3 x2, resolve, shadow per group slot; arrays start on 256 bytes
+        const size_t rec = sizeof(Rec);
+        size_t bytes = n * (10 * rec + 16 + 10 * 4) + (3 + 6 * kWaveGroups) * 256 +
+                       kWaveGroups * kWaveCounters * sizeof(uint32_t);
+        SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
+        s->wave_slots = (uint32_t)n;
+    }
     char* p = s->wave.as<char>();
-    auto take = [&](size_t elem_bytes) {
+    auto take = [&](size_t count, size_t elem_bytes) {
         char* r = p;
-        p += (n * elem_bytes + 255) & ~(size_t)255;
+        p += (count * elem_bytes + 255) & ~(size_t)255;
         return r;
     };
-    WaveState& w = s->ws;
-    w.rec = (Rec*)take(6 * rec);
-    w.pix = (Rec*)take(4 * rec);
-    w.medium = (float4*)take(16);
-    w.q_trace[0] = (uint32_t*)take(4);
-    w.q_trace[1] = (uint32_t*)take(4);
-    w.q_event[0] = (uint32_t*)take(3 * 4);
-    w.q_event[1] = (uint32_t*)take(3 * 4);
-    w.q_resolve = (uint32_t*)take(4);
-    w.q_shadow = (uint32_t*)take(4);
-    w.counts = (uint32_t*)p;
-    s->wave_slots = slots;
+    const size_t rec = sizeof(Rec);
+    Rec* recs = (Rec*)take(n, 6 * rec);
+    Rec* pix = (Rec*)take(n, 4 * rec);
+    float4* medium = (float4*)take(n, 16);
+    for (int g = 0; g < kWaveGroups; ++g) {
+        WaveState& w = s->ws[g];
+        const size_t m = group_slots[g];
+        w.slots = group_slots[g];
+        w.tiles_x = tiles_x;
+        w.group = (uint32_t)g;
+        w.groups = kWaveGroups;
+        w.rec = recs;
+        w.pix = pix;
+        w.medium = medium;
+        w.q_trace[0] = (uint32_t*)take(m, 4);
+        w.q_trace[1] = (uint32_t*)take(m, 4);
+        w.q_event[0] = (uint32_t*)take(m, 3 * 4);
+        w.q_event[1] = (uint32_t*)take(m, 3 * 4);
+        w.q_resolve = (uint32_t*)take(m, 4);
+        w.q_shadow = (uint32_t*)take(m, 4);
+    }
+    for (int g = 0; g < kWaveGroups; ++g) s->ws[g].counts = (uint32_t*)p + g * kWaveCounters;
     return SR_OK;
 }
 
 static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& out,
                             unsigned long long* ctr, cudaStream_t st, bool graph) {
     uint32_t tiles_x = (dp.width + 7) / 8, tiles_y = (dp.height + 3) / 4;
-    uint32_t slots = tiles_x * tiles_y * 32;
-    int rc = wave_reserve(s, slots);
+    int rc = wave_reserve(s, tiles_x, tiles_y);
     if (rc) return rc;
-    s->ws.slots = slots;
-    s->ws.tiles_x = tiles_x;
+    for (int g = 0; g + 1 < kWaveGroups; ++g)
+        if (!s->side_streams[g]) SR_CUDA(cudaStreamCreateWithFlags(&s->side_streams[g], cudaStreamNonBlocking), "stream");
+    for (cudaEvent_t& e : s->fork_events)
+        if (!e) SR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
     if (!s->sms) {
         SR_CUDA(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->ctx->device), "device query");
     }
     WaveLaunch L;
     std::memset(&L, 0, sizeof(L));  // padding bytes take part in the graph-reuse comparison
-    L.W = s->ws;
+    for (int g = 0; g < kWaveGroups; ++g) L.W[g] = s->ws[g];
+    L.groups = kWaveGroups;
     L.S = s->dev;
     L.V = dv;
     L.P = dp;
@@ -782,21 +807,24 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
             s->graph_exec = nullptr;
         }
         if (!s->graph_exec) {
-            SR_CUDA(wave_build_graph(L, s->capture_stream, &s->graph_exec), "build bounce-loop graph");
+            SR_CUDA(wave_build_graph(L, s->capture_stream, s->side_streams, s->fork_events, &s->graph_exec),
+                    "build bounce-loop graph");
             std::memcpy(&s->graph_launch, &L, sizeof(L));
         }
         SR_CUDA(cudaGraphLaunch(s->graph_exec, st), "launch bounce-loop graph");
         return SR_OK;
     }
-    if (!s->counts_host) SR_CUDA(cudaMallocHost(&s->counts_host, kWaveCounters * sizeof(uint32_t)), "pinned alloc");
+    const size_t count_bytes = kWaveGroups * kWaveCounters * sizeof(uint32_t);
+    if (!s->counts_host) SR_CUDA(cudaMallocHost(&s->counts_host, count_bytes), "pinned alloc");
     for (uint32_t it = 0;; ++it) {
         if (it >= L.max_iters) return fail(SR_ERR_DEVICE, "wavefront loop exceeded %u bounces", L.max_iters);
         int cur = (int)(it & 1u);
-        SR_CUDA(wave_bounce(L, cur, st), "wavefront bounce");
-        SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws.counts, kWaveCounters * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
-                "read live count");
+        SR_CUDA(wave_bounce(L, cur, st, s->side_streams, s->fork_events), "wavefront bounce");
+        SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws[0].counts, count_bytes, cudaMemcpyDeviceToHost, st), "read live count");
         SR_CUDA(cudaStreamSynchronize(st), "wavefront bounce");
-        if (wave_live(s->counts_host, cur ^ 1) == 0) {
+        uint32_t live = 0;
+        for (int g = 0; g < kWaveGroups; ++g) live += wave_live(s->counts_host + g * kWaveCounters, cur ^ 1);
+        if (live == 0) {
             s->last_host_iters = it + 1;
             break;
         }
@@ -903,11 +931,11 @@ SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t*
     }
     uint32_t iters = s->last_host_iters;
     if (s->last_mode == SR_RENDER_WAVEFRONT_GRAPH) {
-        SR_CUDA(cudaMemcpy(&iters, s->ws.counts + kCountIter, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
+        SR_CUDA(cudaMemcpy(&iters, s->ws[0].counts + kCountIter, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
         // init, the bounce kernels, one loop condition per 2 bounces
-        *kernel_launches = 1 + kWaveKernelsPerBounce * iters + iters / 2;
+        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + iters / 2;
     } else {
-        *kernel_launches = 1 + kWaveKernelsPerBounce * iters;
+        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters);
     }
     *bounce_iterations = iters;
     return SR_OK;

@@ -122,9 +122,10 @@ __device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, con
 
 __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevParams P) {
     __shared__ uint32_t sh[2][1][kBlockWarps + 1];
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;  // index among this group's slots
+    const uint32_t s = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);
     bool valid = false;
-    if (s < W.slots) {
+    if (li < W.slots) {
         uint32_t x, y;
         slot_pixel(W, s, x, y);
         valid = x < P.width && y < P.height;
@@ -677,12 +678,16 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
     flush_counters<COUNT>(c, counters);
 }
 
-// Condition of the device-side bounce loop: continue while paths are live and the bounce cap
-// (max_samples * (bounces + 1) per pixel, plus slack) is not reached.
-__global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, uint32_t max_iters, uint32_t* err) {
+// Condition of the device-side bounce loop: continue while paths of any group are live and the
+// bounce cap (max_samples * (bounces + 1) per pixel, plus slack) is not reached.  `counts` holds
+// the groups' counters one after another.
+__global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, int groups, uint32_t max_iters,
+                                uint32_t* err) {
     uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
     counts[kCountIter] = it;
-    bool more = wave_live(counts, 0) > 0;  // the body's second bounce has parity 1
+    uint32_t live = 0;
+    for (int g = 0; g < groups; ++g) live += wave_live(counts + g * kWaveCounters, 0);  // next bounce: parity 0
+    bool more = live > 0;
     if (more && it >= max_iters) {
         atomicOr(err, SR_DEVERR_LOOP);
         more = false;
@@ -692,12 +697,45 @@ __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* cou
 
 // ---- launchers ------------------------------------------------------------------------------------
 template <bool COUNT, bool GENERAL>
-static void launch_bounce(const WaveLaunch& L, int cur, cudaStream_t st) {
-    k_wave_extend<COUNT, GENERAL><<<L.grid_extend, 128, 0, st>>>(L.W, L.S, cur, L.err, L.counters);
-    k_wave_shade<COUNT, GENERAL><<<L.grid_shade, 128, 0, st>>>(L.W, L.S, L.P, cur, L.err, L.counters);
-    k_wave_shadow<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(L.W, L.S, L.err, L.counters);
-    k_wave_finalize<COUNT, GENERAL><<<L.grid_finalize, 128, 0, st>>>(L.W, L.S, L.V, L.P, L.out, cur, L.err,
-                                                                     L.counters);
+static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st) {
+    k_wave_extend<COUNT, GENERAL><<<L.grid_extend, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
+    k_wave_shade<COUNT, GENERAL><<<L.grid_shade, 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
+    k_wave_shadow<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, L.err, L.counters);
+    k_wave_finalize<COUNT, GENERAL><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
+}
+
+static void launch_group_bounces(const WaveLaunch& L, const WaveState& W, int cur, int n, cudaStream_t st) {
+    for (int i = 0; i < n; ++i, cur ^= 1) {
+        if (L.general) {
+            if (L.counters)
+                launch_bounce<true, true>(L, W, cur, st);
+            else
+                launch_bounce<false, true>(L, W, cur, st);
+        } else {
+            if (L.counters)
+                launch_bounce<true, false>(L, W, cur, st);
+            else
+                launch_bounce<false, false>(L, W, cur, st);
+        }
+    }
+}
+
+// n bounces of every group starting at parity cur: group 0 on st, group g on side[g - 1], forked
+// from st by fork[0] and joined back by fork[g].
+static cudaError_t launch_bounces(const WaveLaunch& L, int cur, int n, cudaStream_t st, const cudaStream_t* side,
+                                  const cudaEvent_t* fork) {
+    cudaError_t e = cudaSuccess;
+    if (L.groups > 1) {
+        e = cudaEventRecord(fork[0], st);
+        for (int g = 1; g < L.groups && e == cudaSuccess; ++g) e = cudaStreamWaitEvent(side[g - 1], fork[0], 0);
+        if (e != cudaSuccess) return e;
+    }
+    for (int g = 0; g < L.groups; ++g) launch_group_bounces(L, L.W[g], cur, n, g == 0 ? st : side[g - 1]);
+    for (int g = 1; g < L.groups && e == cudaSuccess; ++g) {
+        e = cudaEventRecord(fork[g], side[g - 1]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, fork[g], 0);
+    }
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template <bool GENERAL>
@@ -722,28 +760,19 @@ void wave_grid_sizes(WaveLaunch& L, int sms) {
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(L.W.counts, 0, kWaveCounters * sizeof(uint32_t), st);
+    cudaError_t e = cudaMemsetAsync(L.W[0].counts, 0, (size_t)L.groups * kWaveCounters * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    k_wave_init<<<(L.W.slots + 127) / 128, 128, 0, st>>>(L.W, L.V, L.P);
+    for (int g = 0; g < L.groups; ++g)
+        if (L.W[g].slots) k_wave_init<<<(L.W[g].slots + 127) / 128, 128, 0, st>>>(L.W[g], L.V, L.P);
     return cudaGetLastError();
 }
 
-cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st) {
-    if (L.general) {
-        if (L.counters)
-            launch_bounce<true, true>(L, cur, st);
-        else
-            launch_bounce<false, true>(L, cur, st);
-    } else {
-        if (L.counters)
-            launch_bounce<true, false>(L, cur, st);
-        else
-            launch_bounce<false, false>(L, cur, st);
-    }
-    return cudaGetLastError();
+cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st, const cudaStream_t* side, const cudaEvent_t* fork) {
+    return launch_bounces(L, cur, 1, st, side, fork);
 }
 
-cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, cudaGraphExec_t* exec_out) {
+cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, const cudaStream_t* side,
+                             const cudaEvent_t* fork, cudaGraphExec_t* exec_out) {
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaGraphCreate(&graph, 0);
     if (e != cudaSuccess) return e;
@@ -761,12 +790,12 @@ cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, c
             cudaGraph_t body = cp.conditional.phGraph_out[0];
             e = cudaStreamBeginCaptureToGraph(capture_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
             if (e == cudaSuccess) {
-                wave_bounce(L, 0, capture_stream);
-                wave_bounce(L, 1, capture_stream);
-                k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W.counts, L.max_iters, L.err);
+                // two bounces per group on parallel branches, joined before the loop condition
+                cudaError_t e1 = launch_bounces(L, 0, 2, capture_stream, side, fork);
+                k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.max_iters, L.err);
                 cudaGraph_t captured = nullptr;
                 cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
-                e = e2 != cudaSuccess ? e2 : cudaGetLastError();
+                e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : cudaGetLastError());
             }
         }
     }

@@ -16,10 +16,22 @@ struct alignas(32) Rec {
     float4 a, b;
 };
 
-// Path state, one slot per pixel (slots in 8x4 pixel tiles).
+// The pixel slots are split into independent groups (tile t belongs to group t % groups), each a
+// complete wavefront with its own queues and counters.  The groups' bounce kernels run on parallel
+// branches of the graph, so that while one group's kernel drains (its last long rays occupy a few
+// warps) the other group's kernel fills the idle SMs.
+#ifndef SR_WAVE_GROUPS
+#define SR_WAVE_GROUPS 2
+#endif
+constexpr int kWaveGroups = SR_WAVE_GROUPS;
+
+// Path state of one group, one slot per pixel (slots in 8x4 pixel tiles).
 struct WaveState {
-    uint32_t slots;    // tiles_x * tiles_y * 32
+    uint32_t slots;    // this group's slots: its tiles x 32 (queue capacity)
     uint32_t tiles_x;  // ceil(width / 8)
+    uint32_t group;    // this group's index
+    uint32_t groups;   // number of groups
+    // records of all groups, indexed by the global slot (tile * 32 + lane)
     Rec* rec;          // path records, six sectors per slot (192 bytes, 64-byte aligned):
                        //   ray  a: origin, bounce index (int bits)      b: direction, -
                        //   hit  a: object, triangle (int bits), world distance, local distance
@@ -40,7 +52,7 @@ struct WaveState {
                             // entries each: fog scatter, miss, surface hit (ping-pong)
     uint32_t* q_resolve;    // finished samples
     uint32_t* q_shadow;     // shadow-ray queue
-    uint32_t* counts;       // kCount* below
+    uint32_t* counts;       // this group's counters, kCount* below
 };
 
 // Number of 32-bit counters at WaveState::counts, and their layout.
@@ -64,7 +76,8 @@ inline uint32_t wave_live(const uint32_t* counts, int parity) {
 }
 
 struct WaveLaunch {
-    WaveState W;
+    WaveState W[kWaveGroups];
+    int groups;
     DevScene S;
     DevView V;
     DevParams P;
@@ -80,8 +93,12 @@ struct WaveLaunch {
 constexpr int kWaveKernelsPerBounce = 4;
 
 void wave_grid_sizes(WaveLaunch& L, int sms);
+// Counters of every group (contiguous, kWaveCounters per group) cleared, first camera rays.
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st);
-cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st);
-cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, cudaGraphExec_t* exec_out);
+// One bounce of every group: group 0 on `st`, the others on `side` streams forked from and
+// joined back to `st` with the events in `fork` (one per group).
+cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st, const cudaStream_t* side, const cudaEvent_t* fork);
+cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, const cudaStream_t* side,
+                             const cudaEvent_t* fork, cudaGraphExec_t* exec_out);
 
 }  // namespace sr
