@@ -251,7 +251,41 @@ constexpr int kStackSize = 128;  // bvh.cs:172 stackalloc size; depth cap 64 kee
 // the cap only turns a malformed tree into an error word instead of a hang.
 constexpr uint32_t kMaxPops = 1u << 24;
 
+// Read-only scene data (BVH nodes, triangles, attributes, texels, CDF tables) goes through the
+// non-coherent path.  SR_SCENE_HINT = 1 adds the L2 eviction priority evict_last so that the path
+// state streaming through L2 every bounce evicts it last; measured on GB300 at 1080p it did not
+// help (the traversal is latency-bound on L1/L2 hits already), so it is off by default.
+#ifndef SR_SCENE_HINT
+#define SR_SCENE_HINT 0
+#endif
+#if SR_SCENE_HINT
+SR_DEV uint64_t scene_policy() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+SR_DEV float4 ldg4(const float4* ptr) {
+    float4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(ptr), "l"(scene_policy()));
+    return v;
+}
+SR_DEV float ldg1(const float* ptr) {
+    float v;
+    asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(ptr), "l"(scene_policy()));
+    return v;
+}
+SR_DEV uint32_t ldgu(const uint32_t* ptr) {
+    uint32_t v;
+    asm("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(scene_policy()));
+    return v;
+}
+#else
 SR_DEV float4 ldg4(const float4* p) { return __ldg(p); }
+SR_DEV float ldg1(const float* p) { return __ldg(p); }
+SR_DEV uint32_t ldgu(const uint32_t* p) { return __ldg(p); }
+#endif
 
 // ---- shape hits ---------------------------------------------------------------------------------
 struct ShapeHit {
@@ -750,11 +784,11 @@ SR_DEV float sky_light_pdf(const DevScene& S, V3 dir) {
 template <bool COUNT>
 SR_DEV uint32_t cdf_sample(const float* cdf, const uint32_t* guide, uint32_t n, float norm, Ctr& c) {
     uint32_t k = min((uint32_t)(int)(norm * (float)n), n - 1);
-    uint32_t lo = __ldg(guide + k), hi = __ldg(guide + k + 1);
+    uint32_t lo = ldgu(guide + k), hi = ldgu(guide + k + 1);
     while (lo < hi) {
         SR_COUNT(c, SR_COUNTER_CDF_PROBE, 1);
         uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(cdf + mid + 1) <= norm)
+        if (ldg1(cdf + mid + 1) <= norm)
             lo = mid + 1;
         else
             hi = mid;

@@ -59,6 +59,11 @@ enum : int { X_PRIM = 0, X_ACC = 1 };
 __device__ __forceinline__ size_t rix(uint32_t s, int k) { return 6 * (size_t)s + k; }
 __device__ __forceinline__ size_t pix(uint32_t s, int k) { return 4 * (size_t)s + k; }
 
+// Record loads and stores (one place to change how path state is moved).
+__device__ __forceinline__ Rec ld_rec(const Rec* p) { return *p; }
+__device__ __forceinline__ void st_rec(Rec* p, const Rec& v) { *p = v; }
+__device__ __forceinline__ void st4(float4* p, float4 v) { *p = v; }
+
 __device__ __forceinline__ uint32_t ibits(float f) { return (uint32_t)__float_as_int(f); }
 __device__ __forceinline__ float fbits(uint32_t u) { return __int_as_float((int)u); }
 
@@ -115,9 +120,9 @@ __device__ __forceinline__ Rec rng_rec(const Rng& r, Col fog) {
 
 // Start of a sample: the camera ray and a reset path (scene.cs:633-638).
 __device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, const Ray& ray, const Rng& rng) {
-    W.rec[rix(s, R_RAY)] = {make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)};
-    W.rec[rix(s, R_PATH)] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(1.f, 1.f, 1.f, fbits(0u))};
-    W.rec[rix(s, R_RNG)] = rng_rec(rng, black());
+    st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
+    st_rec(&W.rec[rix(s, R_PATH)], Rec{make_float4(0.f, 0.f, 0.f, 0.f), make_float4(1.f, 1.f, 1.f, fbits(0u))});
+    st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, black()));
 }
 
 __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevParams P) {
@@ -134,9 +139,9 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
             Ray ray = camera_ray(V, P, x, y, rng);
             begin_sample(W, s, ray, rng);
             float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-            W.pix[pix(s, X_ACC)] = {z, z};
-            W.pix[pix(s, X_ACC + 1)] = {z, z};
-            W.pix[pix(s, X_ACC + 2)] = {z, z};  // counts and sample index start at 0 (int bits)
+            st_rec(&W.pix[pix(s, X_ACC)], Rec{z, z});
+            st_rec(&W.pix[pix(s, X_ACC + 1)], Rec{z, z});
+            st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{z, z});  // counts and sample index start at 0 (int bits)
         }
     }
     push_block<1>({W.q_trace[0]}, {&W.counts[kCountTrace]}, s, {valid}, sh, 0u);
@@ -163,8 +168,8 @@ __device__ __forceinline__ int next_segment(const WaveState& W, const DevScene& 
     SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
     float sdist;
     int ev = segment_event(S, ray, false, 0.f, rng, sdist);
-    W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(-1), __int_as_float(-1), __int_as_float(0x7f800000), 0.f),
-                            make_float4(0.f, 0.f, sdist, 0.f)};
+    st_rec(&W.rec[rix(s, R_HIT)], Rec{make_float4(__int_as_float(-1), __int_as_float(-1), __int_as_float(0x7f800000), 0.f),
+                            make_float4(0.f, 0.f, sdist, 0.f)});
     return ev;
 }
 
@@ -329,20 +334,20 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveSt
         S, W.q_trace[cur], W.counts[kCountTrace + cur], &W.counts[kCountExtendFetch], c, err,
         [&](uint32_t s) {
             SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-            Rec r = W.rec[rix(s, R_RAY)];
+            Rec r = ld_rec(&W.rec[rix(s, R_RAY)]);
             return make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
         },
         [&](uint32_t s, const Hit& h, const Ray& ray) {
             float sdist = 0.f;
             int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
             if (S.has_fog) {
-                Rec g = W.rec[rix(s, R_RNG)];
+                Rec g = ld_rec(&W.rec[rix(s, R_RNG)]);
                 Rng rng = rng_of(g);
                 ev = segment_event(S, ray, h.obj >= 0, h.dist, rng, sdist);
-                W.rec[rix(s, R_RNG)] = rng_rec(rng, Col{g.b.y, g.b.z, g.b.w});
+                st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, Col{g.b.y, g.b.z, g.b.w}));
             }
-            W.rec[rix(s, R_HIT)] = {make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
-                                    make_float4(h.u, h.v, sdist, 0.f)};
+            st_rec(&W.rec[rix(s, R_HIT)], Rec{make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
+                                    make_float4(h.u, h.v, sdist, 0.f)});
             return ev;
         },
         [&](uint32_t s, int ev) { stage.add(eq, ec, s, ev); });
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
             S, W.q_shadow, W.counts[kCountShadow], &W.counts[kCountShadowFetch], c, err,
             [&](uint32_t s) {
                 SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
-                Rec r = W.rec[rix(s, R_SH0)];
+                Rec r = ld_rec(&W.rec[rix(s, R_SH0)]);
                 return make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
             },
             [&](uint32_t s, const Hit& h, const Ray& ray) {
@@ -372,7 +377,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
                     tr = 1.0f;
                     if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, ray);
                 }
-                W.rec[rix(s, R_SH0)].a = make_float4(tr, tr, tr, 0.f);
+                st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr, tr, tr, 0.f));
                 return -1;
             },
             [](uint32_t, int) {});
@@ -380,11 +385,11 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
         const uint32_t n = W.counts[kCountShadow];
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
             uint32_t s = W.q_shadow[k];
-            Rec r = W.rec[rix(s, R_SH0)];
+            Rec r = ld_rec(&W.rec[rix(s, R_SH0)]);
             Ray shadow = make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
             Col tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
             if (max_component(tr) > 0.0f && S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
-            W.rec[rix(s, R_SH0)].a = make_float4(tr.r, tr.g, tr.b, 0.f);
+            st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr.r, tr.g, tr.b, 0.f));
         }
     }
     flush_counters<COUNT>(c, counters);
@@ -395,10 +400,10 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
 template <bool COUNT, bool GENERAL>
 __device__ __forceinline__ void add_nee(const WaveState& W, const DevScene& S, uint32_t s, uint32_t pflags,
                                         Col& radiance, Col& fog, Ctr& c) {
-    Rec r0 = W.rec[rix(s, R_SH0)];
+    Rec r0 = ld_rec(&W.rec[rix(s, R_SH0)]);
     Col tr = col3(r0.a);
     if (max_component(tr) > 0.0f) {
-        Rec r1 = W.rec[rix(s, R_SH1)];
+        Rec r1 = ld_rec(&W.rec[rix(s, R_SH1)]);
         V3 ldir{r0.b.x, r0.b.y, r0.b.z};
         Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * col3(r1.a) * r1.a.w / r0.b.w;
         Col add = contrib * col3(r1.b);
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
         int next = -1;  // next segment: -1 traced, else its event
         if (valid) {
             SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
-            Rec rr = W.rec[rix(s, R_RAY)], pr = W.rec[rix(s, R_PATH)], gr = W.rec[rix(s, R_RNG)];
+            Rec rr = ld_rec(&W.rec[rix(s, R_RAY)]), pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
             Rng rng = rng_of(gr);
             Col fog{gr.b.y, gr.b.z, gr.b.w};
             uint32_t bounce = ibits(rr.a.w);
@@ -461,7 +466,7 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
                 // Fog and surface events share one light sample, one Russian-roulette draw and then
                 // scatter, in that RNG order (scene.cs:654-726).
                 const bool fog_event = ev == EV_FOG;
-                const Rec hr = W.rec[rix(s, R_HIT)];
+                const Rec hr = ld_rec(&W.rec[rix(s, R_HIT)]);
                 SurfHit sh;
                 if (!fog_event) {
                     Hit hit{__float_as_int(hr.a.x), __float_as_int(hr.a.y), hr.a.z, hr.a.w, hr.b.x, hr.b.y};
@@ -482,8 +487,8 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
                     radiance = radiance + su.radiance * energy;
                     if (bounce == 0) {
                         pflags |= PF_PRIMARY;
-                        W.pix[pix(s, X_PRIM)] = {make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
-                                     make_float4(su.uv.x, su.uv.y, 0.f, 0.f)};
+                        st_rec(&W.pix[pix(s, X_PRIM)], Rec{make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
+                                     make_float4(su.uv.x, su.uv.y, 0.f, 0.f)});
                     }
                 }
                 // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
@@ -522,9 +527,9 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
                         } else {
                             shadow_req = true;
                         }
-                        W.rec[rix(s, R_SH0)] = {head, make_float4(ldir.x, ldir.y, ldir.z, lpdf)};
-                        W.rec[rix(s, R_SH1)] = {make_float4(w3.r, w3.g, w3.b, mis),
-                                                       make_float4(energy.r, energy.g, energy.b, 0.f)};
+                        st_rec(&W.rec[rix(s, R_SH0)], Rec{head, make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
+                        st_rec(&W.rec[rix(s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
+                                                       make_float4(energy.r, energy.g, energy.b, 0.f)});
                     }
                 }
                 if (russian_roulette(energy, bounce, rng)) {
@@ -561,14 +566,14 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
             }
             if (!terminate && ++bounce == P.bounces + 1) terminate = true;
             live = !terminate;
-            W.rec[rix(s, R_PATH)] = {make_float4(radiance.r, radiance.g, radiance.b, spdf),
-                         make_float4(energy.r, energy.g, energy.b, fbits(pflags))};
+            st_rec(&W.rec[rix(s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
+                         make_float4(energy.r, energy.g, energy.b, fbits(pflags))});
             if (live) {
-                W.rec[rix(s, R_RAY)] = {make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                        make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)};
+                st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                                        make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
                 next = next_segment<COUNT>(W, S, s, ray, rng, c);
             }
-            W.rec[rix(s, R_RNG)] = rng_rec(rng, fog);
+            st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, fog));
         }
         uint32_t* eq = W.q_event[nxt];
         push_block<5>({W.q_trace[nxt], eq + (size_t)EV_FOG * W.slots, eq + (size_t)EV_MISS * W.slots, W.q_resolve,
@@ -604,12 +609,12 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
         bool live = false;
         int next = -1;
         if (valid) {
-            Rec pr = W.rec[rix(s, R_PATH)], gr = W.rec[rix(s, R_RNG)];
+            Rec pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
             uint32_t pflags = ibits(pr.b.w);
             Col radiance = col3(pr.a);
             Col radiance_fog{gr.b.y, gr.b.z, gr.b.w};
             if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, radiance_fog, c);
-            Rec c0 = W.pix[pix(s, X_ACC)], c1 = W.pix[pix(s, X_ACC + 1)], c2 = W.pix[pix(s, X_ACC + 2)];
+            Rec c0 = ld_rec(&W.pix[pix(s, X_ACC)]), c1 = ld_rec(&W.pix[pix(s, X_ACC + 1)]), c2 = ld_rec(&W.pix[pix(s, X_ACC + 2)]);
             float4 a0 = c0.a, a1 = c0.b, a2 = c1.a, a3 = c1.b, a4 = c2.a, a5 = c2.b;
             a0.x += radiance.r, a0.y += radiance.g, a0.z += radiance.b;
             a1.x += radiance_fog.r, a1.y += radiance_fog.g, a1.z += radiance_fog.b;
@@ -622,7 +627,7 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
             uint32_t ncount = ibits(a4.y), dcount = ibits(a4.z);
             uint32_t si = ibits(a4.w);
             if (pflags & PF_PRIMARY) {
-                Rec pm = W.pix[pix(s, X_PRIM)];
+                Rec pm = ld_rec(&W.pix[pix(s, X_PRIM)]);
                 float4 pn = pm.a;
                 a2.x += pn.x, a2.y += pn.y, a2.z += pn.z;
                 a3.x = pn.x, a3.y = pn.y, a3.z = pn.z;
@@ -664,9 +669,9 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
                 live = true;
             }
             a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
-            W.pix[pix(s, X_ACC)] = {a0, a1};
-            W.pix[pix(s, X_ACC + 1)] = {a2, a3};
-            W.pix[pix(s, X_ACC + 2)] = {a4, a5};
+            st_rec(&W.pix[pix(s, X_ACC)], Rec{a0, a1});
+            st_rec(&W.pix[pix(s, X_ACC + 1)], Rec{a2, a3});
+            st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{a4, a5});
         }
         uint32_t* eq = W.q_event[nxt];
         push_block<3>({W.q_trace[nxt], eq + (size_t)EV_FOG * W.slots, eq + (size_t)EV_MISS * W.slots},
