@@ -734,9 +734,10 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
     for (int g = 0; g < kWaveGroups; ++g) group_slots[g] = (uint32_t)(tiles > (uint32_t)g ? (tiles - g + kWaveGroups - 1) / kWaveGroups : 0) * 32;
     if (s->wave_slots < n || !s->wave.ptr) {
         // 32-byte sectors: path records (6 per slot), pixel records (4 per slot); 16-byte medium;
-        // 4-byte queues: trace x2, event 3 x2, resolve, shadow per group slot; arrays start on 256 bytes
+        // queues per group slot: ray entries (32 B) trace x2 + shadow, 4-byte event 3 x2 + resolve;
+        // arrays start on 256 bytes
         const size_t rec = sizeof(Rec);
-        size_t bytes = n * (10 * rec + 16 + 10 * 4) + (3 + 6 * kWaveGroups) * 256 +
+        size_t bytes = n * (10 * rec + 16 + 3 * rec + 7 * 4) + (3 + 6 * kWaveGroups) * 256 +
                        kWaveGroups * kWaveCounters * sizeof(uint32_t);
         SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
         s->wave_slots = (uint32_t)n;
@@ -761,12 +762,12 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         w.rec = recs;
         w.pix = pix;
         w.medium = medium;
-        w.q_trace[0] = (uint32_t*)take(m, 4);
-        w.q_trace[1] = (uint32_t*)take(m, 4);
+        w.q_trace[0] = (Rec*)take(m, rec);
+        w.q_trace[1] = (Rec*)take(m, rec);
         w.q_event[0] = (uint32_t*)take(m, 3 * 4);
         w.q_event[1] = (uint32_t*)take(m, 3 * 4);
         w.q_resolve = (uint32_t*)take(m, 4);
-        w.q_shadow = (uint32_t*)take(m, 4);
+        w.q_shadow = (Rec*)take(m, rec);
     }
     for (int g = 0; g < kWaveGroups; ++g) s->ws[g].counts = (uint32_t*)p + g * kWaveCounters;
     return SR_OK;

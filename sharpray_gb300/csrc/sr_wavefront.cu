@@ -81,9 +81,9 @@ __device__ __forceinline__ void slot_pixel(const WaveState& W, uint32_t slot, ui
 // sh[2][NQ][5] and the round's parity (the scratch alternates so a round needs two barriers).
 constexpr int kBlockWarps = 4;
 template <int NQ>
-__device__ __forceinline__ void push_block(uint32_t* const (&q)[NQ], uint32_t* const (&count)[NQ], uint32_t value,
-                                           const bool (&pred)[NQ], uint32_t (*sh)[NQ][kBlockWarps + 1],
-                                           uint32_t round) {
+__device__ __forceinline__ void block_offsets(uint32_t* const (&count)[NQ], const bool (&pred)[NQ],
+                                              uint32_t (*sh)[NQ][kBlockWarps + 1], uint32_t round,
+                                              uint32_t (&off)[NQ]) {
     uint32_t(&b)[NQ][kBlockWarps + 1] = sh[round & 1u];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned mask[NQ];
@@ -103,12 +103,27 @@ __device__ __forceinline__ void push_block(uint32_t* const (&q)[NQ], uint32_t* c
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < NQ; ++i) {
-        if (pred[i]) {
-            uint32_t off = b[i][kBlockWarps];
-            for (int w = 0; w < warp; ++w) off += b[i][w];
-            q[i][off + (uint32_t)__popc(mask[i] & ((1u << lane) - 1u))] = value;
-        }
+        uint32_t o = b[i][kBlockWarps];
+        for (int w = 0; w < warp; ++w) o += b[i][w];
+        off[i] = o + (uint32_t)__popc(mask[i] & ((1u << lane) - 1u));
     }
+}
+// block_offsets, then `value` written to queue i where pred[i] holds.
+template <int NQ>
+__device__ __forceinline__ void push_block(uint32_t* const (&q)[NQ], uint32_t* const (&count)[NQ], uint32_t value,
+                                           const bool (&pred)[NQ], uint32_t (*sh)[NQ][kBlockWarps + 1],
+                                           uint32_t round) {
+    uint32_t off[NQ];
+    block_offsets<NQ>(count, pred, sh, round, off);
+#pragma unroll
+    for (int i = 0; i < NQ; ++i)
+        if (pred[i]) q[i][off[i]] = value;
+}
+
+// Ray-queue entries carry the ray itself (origin + slot, direction), so that a traversal kernel
+// starts a ray with one coalesced load instead of a queue load followed by a scattered record load.
+__device__ __forceinline__ Rec ray_entry(uint32_t slot, V3 o, V3 d) {
+    return {make_float4(o.x, o.y, o.z, __int_as_float((int)slot)), make_float4(d.x, d.y, d.z, 0.f)};
 }
 
 __device__ __forceinline__ Rng rng_of(const Rec& g) {
@@ -144,7 +159,12 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
             st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{z, z});  // counts and sample index start at 0 (int bits)
         }
     }
-    push_block<1>({W.q_trace[0]}, {&W.counts[kCountTrace]}, s, {valid}, sh, 0u);
+    uint32_t off[1];
+    block_offsets<1>({&W.counts[kCountTrace]}, {valid}, sh, 0u, off);
+    if (valid) {
+        Rec r = ld_rec(&W.rec[rix(s, R_RAY)]);
+        W.q_trace[0][off[0]] = ray_entry(s, V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
+    }
 }
 
 // The event of a segment whose closest hit is known (scene.cs:654-738 decides in this order):
@@ -241,23 +261,33 @@ constexpr int kRefill = SR_REFILL;
 #ifndef SR_LEAF_WAIT
 #define SR_LEAF_WAIT 16
 #endif
-// Minimum resident blocks per SM requested for the shading kernel (caps its registers).
+// Shading runs as one kernel per event (SR_SPLIT_SHADE = 1): fog scatter, the most frequent
+// event in foggy scenes, then needs far fewer registers than surface shading and runs at higher
+// occupancy.  Minimum resident blocks per SM requested for each (caps their registers).
+#ifndef SR_SPLIT_SHADE
+#define SR_SPLIT_SHADE 1
+#endif
 #ifndef SR_SHADE_MIN_BLOCKS
 #define SR_SHADE_MIN_BLOCKS 5
 #endif
+#ifndef SR_SHADE_FOG_MIN_BLOCKS
+#define SR_SHADE_FOG_MIN_BLOCKS 8
+#endif
+constexpr int shade_min_blocks(int ev) { return ev == 0 || ev == 1 ? SR_SHADE_FOG_MIN_BLOCKS : SR_SHADE_MIN_BLOCKS; }
 constexpr int kNodeBurst = SR_NODE_BURST;
 constexpr int kLeafWait = SR_LEAF_WAIT;
 
-// Persistent ray loop shared by extend and shadow: lanes take queue entries [fetch counter) until
-// the queue is exhausted; `start(slot)` begins a query, `finish(slot, hit, ray)` stores its answer
-// and returns an output code that `emit(slot, code)` (all lanes together, -1 = none) passes on.
+// Persistent ray loop shared by extend and shadow: lanes take ray-queue entries [fetch counter)
+// until the queue is exhausted; `start()` is called as a query begins, `finish(slot, hit, ray)`
+// stores its answer and returns an output code that `emit(slot, code)` (all lanes together, -1 =
+// none) passes on.
 // Each round runs the node visits of all lanes together (up to kNodeBurst), then one leaf action
 // of each lane that waits for one: leaf actions are long and differ between lanes, so batching
 // them keeps warps from running each one with a single lane.  Finished lanes are answered in a
 // batch when the warp refills.  Every lane's own sequence of actions is unchanged, so results are
 // those of a plain loop over SceneQuery::step.
 template <bool COUNT, bool ANY, bool GENERAL, typename Start, typename Finish, typename Emit>
-__device__ __forceinline__ void persistent_queries(const DevScene& S, const uint32_t* q, uint32_t n, uint32_t* fetch,
+__device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec* q, uint32_t n, uint32_t* fetch,
                                                    Ctr& c, uint32_t* err, Start start, Finish finish, Emit emit) {
     StackEntry stack[kSceneStack];
     SceneQuery<ANY, GENERAL> sq;
@@ -283,8 +313,10 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const uint
             if (!busy) {
                 uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (idx < n) {
-                    slot = q[idx];
-                    sq.init(S, start(slot));
+                    Rec e = q[idx];
+                    slot = (uint32_t)__float_as_int(e.a.w);
+                    start();
+                    sq.init(S, make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z}));
                     busy = true;
                 }
             }
@@ -332,11 +364,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveSt
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     persistent_queries<COUNT, false, GENERAL>(
         S, W.q_trace[cur], W.counts[kCountTrace + cur], &W.counts[kCountExtendFetch], c, err,
-        [&](uint32_t s) {
-            SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-            Rec r = ld_rec(&W.rec[rix(s, R_RAY)]);
-            return make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
-        },
+        [&]() { SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1); },
         [&](uint32_t s, const Hit& h, const Ray& ray) {
             float sdist = 0.f;
             int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
@@ -366,11 +394,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
     if (!GENERAL || !S.has_transparent) {
         persistent_queries<COUNT, true, GENERAL>(
             S, W.q_shadow, W.counts[kCountShadow], &W.counts[kCountShadowFetch], c, err,
-            [&](uint32_t s) {
-                SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
-                Rec r = ld_rec(&W.rec[rix(s, R_SH0)]);
-                return make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
-            },
+            [&]() { SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1); },
             [&](uint32_t s, const Hit& h, const Ray& ray) {
                 float tr = 0.0f;
                 if (h.obj < 0) {
@@ -384,9 +408,9 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
     } else {
         const uint32_t n = W.counts[kCountShadow];
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-            uint32_t s = W.q_shadow[k];
-            Rec r = ld_rec(&W.rec[rix(s, R_SH0)]);
-            Ray shadow = make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
+            Rec e = W.q_shadow[k];
+            uint32_t s = (uint32_t)__float_as_int(e.a.w);
+            Ray shadow = make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z});
             Col tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
             if (max_component(tr) > 0.0f && S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
             st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr.r, tr.g, tr.b, 0.f));
@@ -414,13 +438,13 @@ __device__ __forceinline__ void add_nee(const WaveState& W, const DevScene& S, u
     }
 }
 
-// One segment of every live path, warps sorted by event: the index space is the fog queue, then
-// the miss queue, then the surface queue, the first two padded to whole warps, so every warp
-// runs one event's logic.
-template <bool COUNT, bool GENERAL>
-__global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, uint32_t* err,
-                                                    unsigned long long* counters) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountShadowFetch] = 0;
+// One segment of every live path with event EVK, or of all live paths (EVK = -1) with warps
+// sorted by event: the index space is then the fog queue, the miss queue and the surface queue,
+// the first two padded to whole warps, so every warp runs one event's logic.
+template <bool COUNT, bool GENERAL, int EVK>
+__global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveState W, DevScene S, DevParams P, int cur,
+                                                                          uint32_t* err, unsigned long long* counters) {
+    if (EVK <= 0 && blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountShadowFetch] = 0;
     __shared__ uint32_t sh[2][5][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
@@ -430,13 +454,15 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
     const uint32_t* ecount = W.counts + kCountEvent + 3 * cur;
     const uint32_t nfog = ecount[EV_FOG], nmiss = ecount[EV_MISS], nsurf = ecount[EV_SURF];
     const uint32_t pfog = (nfog + 31u) & ~31u, pmiss = (nmiss + 31u) & ~31u;
-    const uint32_t total = pfog + pmiss + nsurf;
+    const uint32_t total = EVK >= 0 ? ecount[EVK] : pfog + pmiss + nsurf;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += stride) {
         const uint32_t k = base + threadIdx.x;
         int ev;
         uint32_t i, cnt;
-        if (k < pfog) {
+        if (EVK >= 0) {
+            ev = EVK, i = k, cnt = total;
+        } else if (k < pfog) {
             ev = EV_FOG, i = k, cnt = nfog;
         } else if (k < pfog + pmiss) {
             ev = EV_MISS, i = k - pfog, cnt = nmiss;
@@ -447,6 +473,8 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
         const uint32_t s = valid ? W.q_event[cur][(size_t)ev * W.slots + i] : 0u;
         bool live = false, shadow_req = false;
         int next = -1;  // next segment: -1 traced, else its event
+        V3 sh_o{0.f, 0.f, 0.f}, sh_d{0.f, 0.f, 0.f};  // the shadow ray, when traced
+        V3 nx_o{0.f, 0.f, 0.f}, nx_d{0.f, 0.f, 0.f};  // the next path ray, when traced
         if (valid) {
             SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
             Rec rr = ld_rec(&W.rec[rix(s, R_RAY)]), pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
@@ -526,6 +554,8 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
                             head = make_float4(tr, tr, tr, 0.f);
                         } else {
                             shadow_req = true;
+                            sh_o = pos;
+                            sh_d = ldir;
                         }
                         st_rec(&W.rec[rix(s, R_SH0)], Rec{head, make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
                         st_rec(&W.rec[rix(s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
@@ -572,18 +602,23 @@ __global__ void __launch_bounds__(128, SR_SHADE_MIN_BLOCKS) k_wave_shade(WaveSta
                 st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
                                         make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
                 next = next_segment<COUNT>(W, S, s, ray, rng, c);
+                nx_o = ray.o;
+                nx_d = ray.d;
             }
             st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, fog));
         }
         uint32_t* eq = W.q_event[nxt];
-        push_block<5>({W.q_trace[nxt], eq + (size_t)EV_FOG * W.slots, eq + (size_t)EV_MISS * W.slots, W.q_resolve,
-                       W.q_shadow},
-                      {&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
-                       &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve], &W.counts[kCountShadow]},
-                      s,
-                      {valid && live && next < 0, valid && live && next == EV_FOG, valid && live && next == EV_MISS,
-                       valid && !live, valid && shadow_req},
-                      sh, round++);
+        const bool pred[5] = {valid && live && next < 0, valid && live && next == EV_FOG,
+                              valid && live && next == EV_MISS, valid && !live, valid && shadow_req};
+        uint32_t off[5];
+        block_offsets<5>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
+                          &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve], &W.counts[kCountShadow]},
+                         pred, sh, round++, off);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, nx_o, nx_d);
+        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
+        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
+        if (pred[3]) W.q_resolve[off[3]] = s;
+        if (pred[4]) W.q_shadow[off[4]] = ray_entry(s, sh_o, sh_d);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -608,6 +643,7 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
         uint32_t s = valid ? W.q_resolve[k] : 0u;
         bool live = false;
         int next = -1;
+        V3 nx_o{0.f, 0.f, 0.f}, nx_d{0.f, 0.f, 0.f};  // the new camera ray, when traced
         if (valid) {
             Rec pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
             uint32_t pflags = ibits(pr.b.w);
@@ -667,6 +703,8 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
                 next = next_segment<COUNT>(W, S, s, ray, rng, c);
                 begin_sample(W, s, ray, rng);
                 live = true;
+                nx_o = ray.o;
+                nx_d = ray.d;
             }
             a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
             st_rec(&W.pix[pix(s, X_ACC)], Rec{a0, a1});
@@ -674,11 +712,15 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
             st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{a4, a5});
         }
         uint32_t* eq = W.q_event[nxt];
-        push_block<3>({W.q_trace[nxt], eq + (size_t)EV_FOG * W.slots, eq + (size_t)EV_MISS * W.slots},
-                      {&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
-                       &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
-                      s, {valid && live && next < 0, valid && live && next == EV_FOG, valid && live && next == EV_MISS},
-                      sh, round++);
+        const bool pred[3] = {valid && live && next < 0, valid && live && next == EV_FOG,
+                              valid && live && next == EV_MISS};
+        uint32_t off[3];
+        block_offsets<3>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
+                          &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
+                         pred, sh, round++, off);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, nx_o, nx_d);
+        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
+        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -704,7 +746,13 @@ __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* cou
 template <bool COUNT, bool GENERAL>
 static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st) {
     k_wave_extend<COUNT, GENERAL><<<L.grid_extend, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
-    k_wave_shade<COUNT, GENERAL><<<L.grid_shade, 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
+    if (SR_SPLIT_SHADE) {
+        k_wave_shade<COUNT, GENERAL, EV_FOG><<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
+        k_wave_shade<COUNT, GENERAL, EV_MISS><<<L.grid_shade[1], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
+        k_wave_shade<COUNT, GENERAL, EV_SURF><<<L.grid_shade[2], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
+    } else {
+        k_wave_shade<COUNT, GENERAL, -1><<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
+    }
     k_wave_shadow<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, L.err, L.counters);
     k_wave_finalize<COUNT, GENERAL><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
 }
@@ -746,22 +794,30 @@ static cudaError_t launch_bounces(const WaveLaunch& L, int cur, int n, cudaStrea
 template <bool GENERAL>
 static void occupancy(int* b) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_wave_extend<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_shade<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_shadow<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_finalize<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_shadow<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_finalize<false, GENERAL>, 128, 0);
+    if (SR_SPLIT_SHADE) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shade<false, GENERAL, EV_FOG>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_wave_shade<false, GENERAL, EV_MISS>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[5], k_wave_shade<false, GENERAL, EV_SURF>, 128, 0);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shade<false, GENERAL, -1>, 128, 0);
+    }
 }
 
 void wave_grid_sizes(WaveLaunch& L, int sms) {
-    int b[4] = {0, 0, 0, 0};
+    int b[6] = {0, 0, 0, 0, 0, 0};
     if (L.general)
         occupancy<true>(b);
     else
         occupancy<false>(b);
     for (int& v : b) v = sms * (v > 0 ? v : 1);
     L.grid_extend = b[0];
-    L.grid_shade = b[1];
-    L.grid_shadow = b[2];
-    L.grid_finalize = b[3];
+    L.grid_shadow = b[1];
+    L.grid_finalize = b[2];
+    L.grid_shade[0] = b[3];
+    L.grid_shade[1] = b[4];
+    L.grid_shade[2] = b[5];
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {

@@ -47,11 +47,12 @@ struct WaveState {
                        //   acc2 a: depth sum, normal count, depth count, sample index (int bits)
                        //        b: first uv, has-uv flag, -
     float4* medium;    // albedo of the medium the path is inside (scenes with refraction only)
-    uint32_t* q_trace[2];   // paths whose next ray needs a traversal (ping-pong by bounce parity)
+    Rec* q_trace[2];        // rays that need a traversal (ping-pong by bounce parity): entries
+                            // {origin, slot (int bits)}, {direction, -}
     uint32_t* q_event[2];   // paths whose next segment's event is known, three queues of `slots`
                             // entries each: fog scatter, miss, surface hit (ping-pong)
     uint32_t* q_resolve;    // finished samples
-    uint32_t* q_shadow;     // shadow-ray queue
+    Rec* q_shadow;          // shadow rays, entries as q_trace
     uint32_t* counts;       // this group's counters, kCount* below
 };
 
@@ -84,13 +85,17 @@ struct WaveLaunch {
     DevAovs out;
     uint32_t* err;
     unsigned long long* counters;
-    int grid_extend, grid_shade, grid_shadow, grid_finalize;
+    int grid_extend, grid_shadow, grid_finalize;
+    int grid_shade[3];  // per event kernel (fog, miss, surface), or [0] for the sorted kernel
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
 };
 
-// Kernels launched per bounce (extend, shade, shadow, finalize).
-constexpr int kWaveKernelsPerBounce = 4;
+// Kernels launched per bounce and group (extend, shade per event, shadow, finalize).
+#ifndef SR_SPLIT_SHADE
+#define SR_SPLIT_SHADE 1
+#endif
+constexpr int kWaveKernelsPerBounce = SR_SPLIT_SHADE ? 6 : 4;
 
 void wave_grid_sizes(WaveLaunch& L, int sms);
 // Counters of every group (contiguous, kWaveCounters per group) cleared, first camera rays.
