@@ -146,6 +146,7 @@ struct SrScene {
     int sms = 0;
     int last_mode = 0;                // render mode of the last render
     uint32_t last_host_iters = 0;     // bounces run by the host loop
+    bool last_tail = false;           // the host loop launched the tail kernel
     ~SrScene() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (capture_stream) cudaStreamDestroy(capture_stream);
@@ -799,6 +800,9 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
     wave_grid_sizes(L, s->sms);
     uint64_t cap = (uint64_t)dp.max_samples * (dp.bounces + 1) + 4;
     L.max_iters = (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap);
+    uint32_t all_slots = 0;
+    for (int g = 0; g < kWaveGroups; ++g) all_slots += s->ws[g].slots;
+    L.tail_paths = SR_TAIL_DIV > 0 ? all_slots / SR_TAIL_DIV : 0;
     SR_CUDA(wave_init(L, st), "wavefront init");
     if (graph) {
         if (!s->capture_stream) SR_CUDA(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking), "stream");
@@ -825,8 +829,10 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
         SR_CUDA(cudaStreamSynchronize(st), "wavefront bounce");
         uint32_t live = 0;
         for (int g = 0; g < kWaveGroups; ++g) live += wave_live(s->counts_host + g * kWaveCounters, cur ^ 1);
-        if (live == 0) {
+        if (live <= L.tail_paths) {
             s->last_host_iters = it + 1;
+            s->last_tail = live > 0;
+            if (live > 0) SR_CUDA(wave_tail(L, cur ^ 1, st), "wavefront tail");
             break;
         }
     }
@@ -934,9 +940,10 @@ SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t*
     if (s->last_mode == SR_RENDER_WAVEFRONT_GRAPH) {
         SR_CUDA(cudaMemcpy(&iters, s->ws[0].counts + kCountIter, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
         // init, the bounce kernels, one loop condition per 2 bounces
-        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + iters / 2;
+        // init and bounce kernels per group, one loop condition per 2 bounces, the tail kernel
+        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + iters / 2 + 1;
     } else {
-        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters);
+        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + (s->last_tail ? 1 : 0);
     }
     *bounce_iterations = iters;
     return SR_OK;

@@ -340,6 +340,22 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
     }
 }
 
+// The closest hit of slot s's ray is known: store it and decide the segment's event.
+__device__ __forceinline__ int extend_answer(const WaveState& W, const DevScene& S, uint32_t s, const Hit& h,
+                                             const Ray& ray) {
+    float sdist = 0.f;
+    int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
+    if (S.has_fog) {
+        Rec g = ld_rec(&W.rec[rix(s, R_RNG)]);
+        Rng rng = rng_of(g);
+        ev = segment_event(S, ray, h.obj >= 0, h.dist, rng, sdist);
+        st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, Col{g.b.y, g.b.z, g.b.w}));
+    }
+    st_rec(&W.rec[rix(s, R_HIT)], Rec{make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
+                                      make_float4(h.u, h.v, sdist, 0.f)});
+    return ev;
+}
+
 template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveState W, DevScene S, int cur, uint32_t* err,
                                                      unsigned long long* counters) {
@@ -365,22 +381,20 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveSt
     persistent_queries<COUNT, false, GENERAL>(
         S, W.q_trace[cur], W.counts[kCountTrace + cur], &W.counts[kCountExtendFetch], c, err,
         [&]() { SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1); },
-        [&](uint32_t s, const Hit& h, const Ray& ray) {
-            float sdist = 0.f;
-            int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
-            if (S.has_fog) {
-                Rec g = ld_rec(&W.rec[rix(s, R_RNG)]);
-                Rng rng = rng_of(g);
-                ev = segment_event(S, ray, h.obj >= 0, h.dist, rng, sdist);
-                st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, Col{g.b.y, g.b.z, g.b.w}));
-            }
-            st_rec(&W.rec[rix(s, R_HIT)], Rec{make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
-                                    make_float4(h.u, h.v, sdist, 0.f)});
-            return ev;
-        },
+        [&](uint32_t s, const Hit& h, const Ray& ray) { return extend_answer(W, S, s, h, ray); },
         [&](uint32_t s, int ev) { stage.add(eq, ec, s, ev); });
     stage.flush(eq, ec);
     flush_counters<COUNT>(c, counters);
+}
+
+// The transmittance of slot s's shadow ray by the closest-hit loop (ShadowTransmittance,
+// scene.cs:576-600), times the fog transmittance, written over the request's origin.
+template <bool COUNT, bool GENERAL>
+__device__ __forceinline__ void shadow_trace(const WaveState& W, const DevScene& S, uint32_t s, const Ray& shadow,
+                                             Ctr& c, uint32_t* err) {
+    Col tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
+    if (max_component(tr) > 0.0f && S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
+    st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr.r, tr.g, tr.b, 0.f));
 }
 
 // Shadow rays of the bounce: transmittance (any hit -> black in opaque scenes) times the fog
@@ -409,11 +423,8 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
         const uint32_t n = W.counts[kCountShadow];
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
             Rec e = W.q_shadow[k];
-            uint32_t s = (uint32_t)__float_as_int(e.a.w);
-            Ray shadow = make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z});
-            Col tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
-            if (max_component(tr) > 0.0f && S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
-            st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr.r, tr.g, tr.b, 0.f));
+            shadow_trace<COUNT, GENERAL>(W, S, (uint32_t)__float_as_int(e.a.w),
+                                         make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z}), c, err);
         }
     }
     flush_counters<COUNT>(c, counters);
@@ -436,6 +447,154 @@ __device__ __forceinline__ void add_nee(const WaveState& W, const DevScene& S, u
         else
             radiance = radiance + add;
     }
+}
+
+// The outcome of one path step: whether the path goes on, whether a shadow ray must be traced,
+// and the next segment (its event, or -1 when its ray needs a traversal) with the rays to queue.
+struct SegOut {
+    bool live = false, shadow = false;
+    int next = -1;
+    V3 sh_o{0.f, 0.f, 0.f}, sh_d{0.f, 0.f, 0.f};  // the shadow ray, when traced
+    V3 nx_o{0.f, 0.f, 0.f}, nx_d{0.f, 0.f, 0.f};  // the next ray, when traced
+};
+
+// One segment of path slot s whose event is ev (scene.cs:640-738): first the NEE contribution of
+// the previous segment, then the event's logic; the new path state is stored.
+template <bool COUNT, bool GENERAL>
+__device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevScene& S, const DevParams& P, uint32_t s,
+                                                int ev, Ctr& c) {
+    SegOut o;
+        SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
+        Rec rr = ld_rec(&W.rec[rix(s, R_RAY)]), pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
+        Rng rng = rng_of(gr);
+        Col fog{gr.b.y, gr.b.z, gr.b.w};
+        uint32_t bounce = ibits(rr.a.w);
+        uint32_t pflags = ibits(pr.b.w);
+        if (bounce == 0) SR_COUNT(c, SR_COUNTER_SAMPLE, 1);
+        Ray ray = make_ray(V3{rr.a.x, rr.a.y, rr.a.z}, V3{rr.b.x, rr.b.y, rr.b.z});
+        Col radiance = col3(pr.a);
+        float spdf = pr.a.w;
+        Col energy = col3(pr.b);
+        if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, fog, c);
+        pflags &= ~(PF_NEE | PF_NEE_FOG);
+        bool terminate = false;
+        if (ev != EV_MISS) {
+            // Fog and surface events share one light sample, one Russian-roulette draw and then
+            // scatter, in that RNG order (scene.cs:654-726).
+            const bool fog_event = ev == EV_FOG;
+            const Rec hr = ld_rec(&W.rec[rix(s, R_HIT)]);
+            SurfHit sh;
+            if (!fog_event) {
+                Hit hit{__float_as_int(hr.a.x), __float_as_int(hr.a.y), hr.a.z, hr.a.w, hr.b.x, hr.b.y};
+                surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
+            }
+            const Surface& su = sh.surf;
+            const float dist = sh.dist;
+            const V3 view = -ray.d;
+            float bias = 0.0f;
+            V3 pos;
+            if (fog_event) {
+                energy = energy * col3(S.fog_color);
+                pos = ray_at(ray, hr.b.z);
+            } else {
+                bias = fmaxf(1e-4f, dist * 1e-4f);
+                pos = ray_at(ray, dist - bias);
+                if (GENERAL && (pflags & PF_MEDIUM)) energy = energy * beer_law(col3(W.medium[s]), dist);
+                radiance = radiance + su.radiance * energy;
+                if (bounce == 0) {
+                    pflags |= PF_PRIMARY;
+                    st_rec(&W.pix[pix(s, X_PRIM)], Rec{make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
+                                 make_float4(su.uv.x, su.uv.y, 0.f, 0.f)});
+                }
+            }
+            // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
+            // the shadow ray is traced by the shadow kernel, the contribution added next segment
+            V3 ldir;
+            float lpdf;
+            if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
+                bool emit = true;
+                Col w3;
+                float mis;
+                if (fog_event) {
+                    float fog_pdf = hg_pdf(dot(ray.d, ldir), S.fog_g);
+                    mis = power_heuristic(lpdf, fog_pdf);
+                    w3 = gray(fog_pdf);
+                } else {
+                    V3 nn = dot(su.normal, view) >= 0.0f ? su.normal : -su.normal;
+                    V3 ng = dot(su.normal_geo, view) >= 0.0f ? su.normal_geo : -su.normal_geo;
+                    emit = dot(nn, ldir) > 0.0f && dot(ng, ldir) > 0.0f;
+                    if (emit) {
+                        w3 = opaque_eval(su, view, ldir);
+                        mis = power_heuristic(lpdf, opaque_pdf(su, view, ldir, specular_probability(su, view)));
+                    }
+                }
+                if (emit) {
+                    pflags |= PF_NEE | ((fog_event && bounce == 0) ? PF_NEE_FOG : 0u);
+                    // a shadow ray that misses the scene's root boxes is unoccluded: its
+                    // transmittance is the fog's alone, formed here as the shadow kernel would
+                    Ray shadow = make_ray(pos, ldir);
+                    float4 head = make_float4(pos.x, pos.y, pos.z, 0.f);
+                    const bool any = !GENERAL || !S.has_transparent;
+                    if (any ? misses_scene<COUNT, true>(S, shadow, c) : misses_scene<COUNT, false>(S, shadow, c)) {
+                        SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
+                        float tr = 1.0f;
+                        if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, shadow);
+                        head = make_float4(tr, tr, tr, 0.f);
+                    } else {
+                        o.shadow = true;
+                        o.sh_o = pos;
+                        o.sh_d = ldir;
+                    }
+                    st_rec(&W.rec[rix(s, R_SH0)], Rec{head, make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
+                    st_rec(&W.rec[rix(s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
+                                                   make_float4(energy.r, energy.g, energy.b, 0.f)});
+                }
+            }
+            if (russian_roulette(energy, bounce, rng)) {
+                terminate = true;
+            } else if (fog_event) {
+                V3 sdir = hg_scatter_dir(ray.d, S.fog_g, rng);
+                pflags |= PF_SPDF;
+                spdf = hg_pdf(dot(ray.d, sdir), S.fog_g);
+                ray = make_ray(pos, sdir);
+            } else {
+                Scatter sc = surface_scatter<GENERAL>(su, ray.d, view, rng);
+                energy = energy * sc.weight;
+                energy = clamp_luminance(energy, P.indirect_clamp);
+                bool enter = dot(sc.dir, su.normal_geo) < 0.0f;
+                if (GENERAL && sc.refracted) {
+                    if (enter) {
+                        pflags |= PF_MEDIUM;
+                        W.medium[s] = make_float4(su.albedo.r, su.albedo.g, su.albedo.b, 0.f);
+                    } else {
+                        pflags &= ~PF_MEDIUM;
+                    }
+                } else if (!enter) {
+                    pflags &= ~PF_MEDIUM;
+                }
+                pflags = sc.has_pdf ? (pflags | PF_SPDF) : (pflags & ~PF_SPDF);
+                spdf = sc.pdf;
+                ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
+            }
+        } else {
+            // miss: sky radiance with the MIS weight of the last scatter (scene.cs:728-738)
+            float mis = (pflags & PF_SPDF) ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
+            radiance = radiance + sky_radiance<COUNT, GENERAL>(S, ray.d, c) * mis * energy;
+            terminate = true;
+        }
+        if (!terminate && ++bounce == P.bounces + 1) terminate = true;
+        o.live = !terminate;
+        st_rec(&W.rec[rix(s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
+                     make_float4(energy.r, energy.g, energy.b, fbits(pflags))});
+        if (o.live) {
+            st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                                    make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
+            o.next = next_segment<COUNT>(W, S, s, ray, rng, c);
+            o.nx_o = ray.o;
+            o.nx_d = ray.d;
+        }
+        st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, fog));
+    return o;
 }
 
 // One segment of every live path with event EVK, or of all live paths (EVK = -1) with warps
@@ -471,156 +630,98 @@ __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveS
         }
         const bool valid = i < cnt;
         const uint32_t s = valid ? W.q_event[cur][(size_t)ev * W.slots + i] : 0u;
-        bool live = false, shadow_req = false;
-        int next = -1;  // next segment: -1 traced, else its event
-        V3 sh_o{0.f, 0.f, 0.f}, sh_d{0.f, 0.f, 0.f};  // the shadow ray, when traced
-        V3 nx_o{0.f, 0.f, 0.f}, nx_d{0.f, 0.f, 0.f};  // the next path ray, when traced
+        SegOut o;
         if (valid) {
-            SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
-            Rec rr = ld_rec(&W.rec[rix(s, R_RAY)]), pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
-            Rng rng = rng_of(gr);
-            Col fog{gr.b.y, gr.b.z, gr.b.w};
-            uint32_t bounce = ibits(rr.a.w);
-            uint32_t pflags = ibits(pr.b.w);
-            if (bounce == 0) SR_COUNT(c, SR_COUNTER_SAMPLE, 1);
-            Ray ray = make_ray(V3{rr.a.x, rr.a.y, rr.a.z}, V3{rr.b.x, rr.b.y, rr.b.z});
-            Col radiance = col3(pr.a);
-            float spdf = pr.a.w;
-            Col energy = col3(pr.b);
-            if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, fog, c);
-            pflags &= ~(PF_NEE | PF_NEE_FOG);
-            bool terminate = false;
-            if (ev != EV_MISS) {
-                // Fog and surface events share one light sample, one Russian-roulette draw and then
-                // scatter, in that RNG order (scene.cs:654-726).
-                const bool fog_event = ev == EV_FOG;
-                const Rec hr = ld_rec(&W.rec[rix(s, R_HIT)]);
-                SurfHit sh;
-                if (!fog_event) {
-                    Hit hit{__float_as_int(hr.a.x), __float_as_int(hr.a.y), hr.a.z, hr.a.w, hr.b.x, hr.b.y};
-                    surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
-                }
-                const Surface& su = sh.surf;
-                const float dist = sh.dist;
-                const V3 view = -ray.d;
-                float bias = 0.0f;
-                V3 pos;
-                if (fog_event) {
-                    energy = energy * col3(S.fog_color);
-                    pos = ray_at(ray, hr.b.z);
-                } else {
-                    bias = fmaxf(1e-4f, dist * 1e-4f);
-                    pos = ray_at(ray, dist - bias);
-                    if (GENERAL && (pflags & PF_MEDIUM)) energy = energy * beer_law(col3(W.medium[s]), dist);
-                    radiance = radiance + su.radiance * energy;
-                    if (bounce == 0) {
-                        pflags |= PF_PRIMARY;
-                        st_rec(&W.pix[pix(s, X_PRIM)], Rec{make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
-                                     make_float4(su.uv.x, su.uv.y, 0.f, 0.f)});
-                    }
-                }
-                // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
-                // the shadow ray is traced by the shadow kernel, the contribution added next segment
-                V3 ldir;
-                float lpdf;
-                if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
-                    bool emit = true;
-                    Col w3;
-                    float mis;
-                    if (fog_event) {
-                        float fog_pdf = hg_pdf(dot(ray.d, ldir), S.fog_g);
-                        mis = power_heuristic(lpdf, fog_pdf);
-                        w3 = gray(fog_pdf);
-                    } else {
-                        V3 nn = dot(su.normal, view) >= 0.0f ? su.normal : -su.normal;
-                        V3 ng = dot(su.normal_geo, view) >= 0.0f ? su.normal_geo : -su.normal_geo;
-                        emit = dot(nn, ldir) > 0.0f && dot(ng, ldir) > 0.0f;
-                        if (emit) {
-                            w3 = opaque_eval(su, view, ldir);
-                            mis = power_heuristic(lpdf, opaque_pdf(su, view, ldir, specular_probability(su, view)));
-                        }
-                    }
-                    if (emit) {
-                        pflags |= PF_NEE | ((fog_event && bounce == 0) ? PF_NEE_FOG : 0u);
-                        // a shadow ray that misses the scene's root boxes is unoccluded: its
-                        // transmittance is the fog's alone, formed here as the shadow kernel would
-                        Ray shadow = make_ray(pos, ldir);
-                        float4 head = make_float4(pos.x, pos.y, pos.z, 0.f);
-                        const bool any = !GENERAL || !S.has_transparent;
-                        if (any ? misses_scene<COUNT, true>(S, shadow, c) : misses_scene<COUNT, false>(S, shadow, c)) {
-                            SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
-                            float tr = 1.0f;
-                            if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, shadow);
-                            head = make_float4(tr, tr, tr, 0.f);
-                        } else {
-                            shadow_req = true;
-                            sh_o = pos;
-                            sh_d = ldir;
-                        }
-                        st_rec(&W.rec[rix(s, R_SH0)], Rec{head, make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
-                        st_rec(&W.rec[rix(s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
-                                                       make_float4(energy.r, energy.g, energy.b, 0.f)});
-                    }
-                }
-                if (russian_roulette(energy, bounce, rng)) {
-                    terminate = true;
-                } else if (fog_event) {
-                    V3 sdir = hg_scatter_dir(ray.d, S.fog_g, rng);
-                    pflags |= PF_SPDF;
-                    spdf = hg_pdf(dot(ray.d, sdir), S.fog_g);
-                    ray = make_ray(pos, sdir);
-                } else {
-                    Scatter sc = surface_scatter<GENERAL>(su, ray.d, view, rng);
-                    energy = energy * sc.weight;
-                    energy = clamp_luminance(energy, P.indirect_clamp);
-                    bool enter = dot(sc.dir, su.normal_geo) < 0.0f;
-                    if (GENERAL && sc.refracted) {
-                        if (enter) {
-                            pflags |= PF_MEDIUM;
-                            W.medium[s] = make_float4(su.albedo.r, su.albedo.g, su.albedo.b, 0.f);
-                        } else {
-                            pflags &= ~PF_MEDIUM;
-                        }
-                    } else if (!enter) {
-                        pflags &= ~PF_MEDIUM;
-                    }
-                    pflags = sc.has_pdf ? (pflags | PF_SPDF) : (pflags & ~PF_SPDF);
-                    spdf = sc.pdf;
-                    ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
-                }
-            } else {
-                // miss: sky radiance with the MIS weight of the last scatter (scene.cs:728-738)
-                float mis = (pflags & PF_SPDF) ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
-                radiance = radiance + sky_radiance<COUNT, GENERAL>(S, ray.d, c) * mis * energy;
-                terminate = true;
-            }
-            if (!terminate && ++bounce == P.bounces + 1) terminate = true;
-            live = !terminate;
-            st_rec(&W.rec[rix(s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
-                         make_float4(energy.r, energy.g, energy.b, fbits(pflags))});
-            if (live) {
-                st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                        make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
-                next = next_segment<COUNT>(W, S, s, ray, rng, c);
-                nx_o = ray.o;
-                nx_d = ray.d;
-            }
-            st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, fog));
+            o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
         }
         uint32_t* eq = W.q_event[nxt];
-        const bool pred[5] = {valid && live && next < 0, valid && live && next == EV_FOG,
-                              valid && live && next == EV_MISS, valid && !live, valid && shadow_req};
+        const bool pred[5] = {valid && o.live && o.next < 0, valid && o.live && o.next == EV_FOG,
+                              valid && o.live && o.next == EV_MISS, valid && !o.live, valid && o.shadow};
         uint32_t off[5];
         block_offsets<5>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve], &W.counts[kCountShadow]},
                          pred, sh, round++, off);
-        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, nx_o, nx_d);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d);
         if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
         if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
         if (pred[3]) W.q_resolve[off[3]] = s;
-        if (pred[4]) W.q_shadow[off[4]] = ray_entry(s, sh_o, sh_d);
+        if (pred[4]) W.q_shadow[off[4]] = ray_entry(s, o.sh_o, o.sh_d);
     }
     flush_counters<COUNT>(c, counters);
+}
+
+// End of the sample in slot s: the pending NEE contribution of its last segment, the pixel
+// statistics and the adaptive stop (renderer.cs:173-212), then the next camera ray or the AOVs.
+template <bool COUNT, bool GENERAL>
+__device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevScene& S, const DevView& V,
+                                                  const DevParams& P, const DevAovs& out, uint32_t s, Ctr& c) {
+    SegOut o;
+        Rec pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
+        uint32_t pflags = ibits(pr.b.w);
+        Col radiance = col3(pr.a);
+        Col radiance_fog{gr.b.y, gr.b.z, gr.b.w};
+        if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, radiance_fog, c);
+        Rec c0 = ld_rec(&W.pix[pix(s, X_ACC)]), c1 = ld_rec(&W.pix[pix(s, X_ACC + 1)]), c2 = ld_rec(&W.pix[pix(s, X_ACC + 2)]);
+        float4 a0 = c0.a, a1 = c0.b, a2 = c1.a, a3 = c1.b, a4 = c2.a, a5 = c2.b;
+        a0.x += radiance.r, a0.y += radiance.g, a0.z += radiance.b;
+        a1.x += radiance_fog.r, a1.y += radiance_fog.g, a1.z += radiance_fog.b;
+        float lum = luminance(radiance) + luminance(radiance_fog);
+        a0.w += lum;
+        a1.w += lum * lum;
+        float ls = luminance(radiance);
+        a2.w += ls;
+        a3.w += ls * ls;
+        uint32_t ncount = ibits(a4.y), dcount = ibits(a4.z);
+        uint32_t si = ibits(a4.w);
+        if (pflags & PF_PRIMARY) {
+            Rec pm = ld_rec(&W.pix[pix(s, X_PRIM)]);
+            float4 pn = pm.a;
+            a2.x += pn.x, a2.y += pn.y, a2.z += pn.z;
+            a3.x = pn.x, a3.y = pn.y, a3.z = pn.z;
+            ncount++;
+            a4.x += pn.w;
+            dcount++;
+            if (ibits(a5.z) == 0u) a5 = make_float4(pm.b.x, pm.b.y, fbits(1u), 0.f);
+        }
+        bool done = false;
+        uint32_t count = 0;
+        if (si >= P.min_samples - 1 && relative_std_err(a0.w, a1.w, si + 1) < P.variance_threshold) {
+            done = true;
+            count = si + 1;
+        } else if (++si == P.max_samples) {
+            done = true;
+            count = si + 1;  // loop ran out: normalised by maxSamples + 1 (renderer.cs:215)
+        }
+        uint32_t x, y;
+        slot_pixel(W, s, x, y);
+        if (done) {
+            float var = relative_std_err(a2.w, a3.w, count);
+            Col r = col3(a0) / (float)count;
+            Col f = col3(a1) / (float)count;
+            V3 nsum{a2.x, a2.y, a2.z}, nfb{a3.x, a3.y, a3.z};
+            V3 nrm = ncount > 0 ? normalize_or(nsum, nfb) : V3{0.f, 0.f, 0.f};
+            size_t i = (size_t)y * P.width + x;
+            out.radiance[3 * i] = r.r, out.radiance[3 * i + 1] = r.g, out.radiance[3 * i + 2] = r.b;
+            out.radiance_fog[3 * i] = f.r, out.radiance_fog[3 * i + 1] = f.g, out.radiance_fog[3 * i + 2] = f.b;
+            out.normals[3 * i] = nrm.x, out.normals[3 * i + 1] = nrm.y, out.normals[3 * i + 2] = nrm.z;
+            out.uv[2 * i] = a5.x, out.uv[2 * i + 1] = a5.y;
+            out.depth[i] = dcount > 0 ? a4.x / (float)dcount : __int_as_float(0x7f800000);
+            out.samples[i] = count;
+            out.variance[i] = var;
+        } else {
+            Rng rng = rng_of(gr);
+            Ray ray = camera_ray(V, P, x, y, rng);
+            o.next = next_segment<COUNT>(W, S, s, ray, rng, c);
+            begin_sample(W, s, ray, rng);
+            o.live = true;
+            o.nx_o = ray.o;
+            o.nx_d = ray.d;
+        }
+        a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
+        st_rec(&W.pix[pix(s, X_ACC)], Rec{a0, a1});
+        st_rec(&W.pix[pix(s, X_ACC + 1)], Rec{a2, a3});
+        st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{a4, a5});
+    return o;
 }
 
 // Finished samples: the pending NEE contribution of the last segment, then the pixel statistics
@@ -641,100 +742,94 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
         uint32_t k = base + threadIdx.x;
         bool valid = k < n;
         uint32_t s = valid ? W.q_resolve[k] : 0u;
-        bool live = false;
-        int next = -1;
-        V3 nx_o{0.f, 0.f, 0.f}, nx_d{0.f, 0.f, 0.f};  // the new camera ray, when traced
+        SegOut o;
         if (valid) {
-            Rec pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
-            uint32_t pflags = ibits(pr.b.w);
-            Col radiance = col3(pr.a);
-            Col radiance_fog{gr.b.y, gr.b.z, gr.b.w};
-            if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, radiance_fog, c);
-            Rec c0 = ld_rec(&W.pix[pix(s, X_ACC)]), c1 = ld_rec(&W.pix[pix(s, X_ACC + 1)]), c2 = ld_rec(&W.pix[pix(s, X_ACC + 2)]);
-            float4 a0 = c0.a, a1 = c0.b, a2 = c1.a, a3 = c1.b, a4 = c2.a, a5 = c2.b;
-            a0.x += radiance.r, a0.y += radiance.g, a0.z += radiance.b;
-            a1.x += radiance_fog.r, a1.y += radiance_fog.g, a1.z += radiance_fog.b;
-            float lum = luminance(radiance) + luminance(radiance_fog);
-            a0.w += lum;
-            a1.w += lum * lum;
-            float ls = luminance(radiance);
-            a2.w += ls;
-            a3.w += ls * ls;
-            uint32_t ncount = ibits(a4.y), dcount = ibits(a4.z);
-            uint32_t si = ibits(a4.w);
-            if (pflags & PF_PRIMARY) {
-                Rec pm = ld_rec(&W.pix[pix(s, X_PRIM)]);
-                float4 pn = pm.a;
-                a2.x += pn.x, a2.y += pn.y, a2.z += pn.z;
-                a3.x = pn.x, a3.y = pn.y, a3.z = pn.z;
-                ncount++;
-                a4.x += pn.w;
-                dcount++;
-                if (ibits(a5.z) == 0u) a5 = make_float4(pm.b.x, pm.b.y, fbits(1u), 0.f);
-            }
-            bool done = false;
-            uint32_t count = 0;
-            if (si >= P.min_samples - 1 && relative_std_err(a0.w, a1.w, si + 1) < P.variance_threshold) {
-                done = true;
-                count = si + 1;
-            } else if (++si == P.max_samples) {
-                done = true;
-                count = si + 1;  // loop ran out: normalised by maxSamples + 1 (renderer.cs:215)
-            }
-            uint32_t x, y;
-            slot_pixel(W, s, x, y);
-            if (done) {
-                float var = relative_std_err(a2.w, a3.w, count);
-                Col r = col3(a0) / (float)count;
-                Col f = col3(a1) / (float)count;
-                V3 nsum{a2.x, a2.y, a2.z}, nfb{a3.x, a3.y, a3.z};
-                V3 nrm = ncount > 0 ? normalize_or(nsum, nfb) : V3{0.f, 0.f, 0.f};
-                size_t i = (size_t)y * P.width + x;
-                out.radiance[3 * i] = r.r, out.radiance[3 * i + 1] = r.g, out.radiance[3 * i + 2] = r.b;
-                out.radiance_fog[3 * i] = f.r, out.radiance_fog[3 * i + 1] = f.g, out.radiance_fog[3 * i + 2] = f.b;
-                out.normals[3 * i] = nrm.x, out.normals[3 * i + 1] = nrm.y, out.normals[3 * i + 2] = nrm.z;
-                out.uv[2 * i] = a5.x, out.uv[2 * i + 1] = a5.y;
-                out.depth[i] = dcount > 0 ? a4.x / (float)dcount : __int_as_float(0x7f800000);
-                out.samples[i] = count;
-                out.variance[i] = var;
-            } else {
-                Rng rng = rng_of(gr);
-                Ray ray = camera_ray(V, P, x, y, rng);
-                next = next_segment<COUNT>(W, S, s, ray, rng, c);
-                begin_sample(W, s, ray, rng);
-                live = true;
-                nx_o = ray.o;
-                nx_d = ray.d;
-            }
-            a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
-            st_rec(&W.pix[pix(s, X_ACC)], Rec{a0, a1});
-            st_rec(&W.pix[pix(s, X_ACC + 1)], Rec{a2, a3});
-            st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{a4, a5});
+            o = finalize_sample<COUNT, GENERAL>(W, S, V, P, out, s, c);
         }
         uint32_t* eq = W.q_event[nxt];
-        const bool pred[3] = {valid && live && next < 0, valid && live && next == EV_FOG,
-                              valid && live && next == EV_MISS};
+        const bool pred[3] = {valid && o.live && o.next < 0, valid && o.live && o.next == EV_FOG,
+                              valid && o.live && o.next == EV_MISS};
         uint32_t off[3];
         block_offsets<3>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
                          pred, sh, round++, off);
-        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, nx_o, nx_d);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d);
         if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
         if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
     }
     flush_counters<COUNT>(c, counters);
 }
 
-// Condition of the device-side bounce loop: continue while paths of any group are live and the
-// bounce cap (max_samples * (bounces + 1) per pixel, plus slack) is not reached.  `counts` holds
-// the groups' counters one after another.
-__global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, int groups, uint32_t max_iters,
-                                uint32_t* err) {
+// The last paths of a frame, one thread per slot run to completion.  When few paths are left the
+// bounce kernels are bound by the latency of their few longest paths plus the launch gaps of
+// every bounce, while one thread per slot runs the same steps back to back -- traversal, event,
+// shading, shadow ray, end of sample -- in the same order, so results are identical.  The live
+// slots of parity `cur` are those of every group's trace queue and event queues.
+template <bool COUNT, bool GENERAL>
+__global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, DevView V, DevParams P, DevAovs out,
+                                                   int cur, uint32_t* err, unsigned long long* counters) {
+    Ctr c;
+#pragma unroll
+    for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    int group = -1, ev = -1;
+    uint32_t s = 0;
+    for (int g = 0; g < G.groups && group < 0; ++g) {
+        const WaveState& Wg = G.W[g];
+        const uint32_t nt = Wg.counts[kCountTrace + cur];
+        if (k < nt) {
+            group = g;
+            s = (uint32_t)__float_as_int(Wg.q_trace[cur][k].a.w);
+            break;
+        }
+        k -= nt;
+        for (int e = 0; e < 3; ++e) {
+            const uint32_t ne = Wg.counts[kCountEvent + 3 * cur + e];
+            if (k < ne) {
+                group = g, ev = e;
+                s = Wg.q_event[cur][(size_t)e * Wg.slots + k];
+                break;
+            }
+            k -= ne;
+        }
+    }
+    if (group >= 0) {
+        const WaveState W = G.W[group];
+        // every step advances a segment or ends a sample, so this bounds a well-formed frame
+        const uint64_t cap = ((uint64_t)P.max_samples + 1) * ((uint64_t)P.bounces + 2) * 2 + 8;
+        for (uint64_t step = 0;; ++step) {
+            if (step > cap) {
+                atomicOr(err, SR_DEVERR_LOOP);
+                break;
+            }
+            if (ev < 0) {
+                Rec r = ld_rec(&W.rec[rix(s, R_RAY)]);
+                Ray ray = make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
+                SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
+                ev = extend_answer(W, S, s, scene_closest<COUNT, GENERAL>(S, ray, c, err), ray);
+            }
+            SegOut o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
+            if (o.shadow) shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(o.sh_o, o.sh_d), c, err);
+            if (!o.live) {
+                o = finalize_sample<COUNT, GENERAL>(W, S, V, P, out, s, c);
+                if (!o.live) break;
+            }
+            ev = o.next;
+        }
+    }
+    flush_counters<COUNT>(c, counters);
+}
+
+// Condition of the device-side bounce loop: continue while more than `tail` paths of all groups
+// are live (the rest go to the tail kernel) and the bounce cap (max_samples * (bounces + 1) per
+// pixel, plus slack) is not reached.  `counts` holds the groups' counters one after another.
+__global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, int groups, uint32_t tail,
+                                uint32_t max_iters, uint32_t* err) {
     uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
     counts[kCountIter] = it;
     uint32_t live = 0;
     for (int g = 0; g < groups; ++g) live += wave_live(counts + g * kWaveCounters, 0);  // next bounce: parity 0
-    bool more = live > 0;
+    bool more = live > tail;
     if (more && it >= max_iters) {
         atomicOr(err, SR_DEVERR_LOOP);
         more = false;
@@ -832,6 +927,26 @@ cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st, const cud
     return launch_bounces(L, cur, 1, st, side, fork);
 }
 
+cudaError_t wave_tail(const WaveLaunch& L, int cur, cudaStream_t st) {
+    WaveGroups G;
+    for (int g = 0; g < kWaveGroups; ++g) G.W[g] = L.W[g];
+    G.groups = L.groups;
+    const int grid = (int)((L.tail_paths + 127) / 128);
+    if (grid == 0) return cudaSuccess;
+    if (L.general) {
+        if (L.counters)
+            k_wave_tail<true, true><<<grid, 128, 0, st>>>(G, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
+        else
+            k_wave_tail<false, true><<<grid, 128, 0, st>>>(G, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
+    } else {
+        if (L.counters)
+            k_wave_tail<true, false><<<grid, 128, 0, st>>>(G, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
+        else
+            k_wave_tail<false, false><<<grid, 128, 0, st>>>(G, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, const cudaStream_t* side,
                              const cudaEvent_t* fork, cudaGraphExec_t* exec_out) {
     cudaGraph_t graph = nullptr;
@@ -853,10 +968,21 @@ cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, c
             if (e == cudaSuccess) {
                 // two bounces per group on parallel branches, joined before the loop condition
                 cudaError_t e1 = launch_bounces(L, 0, 2, capture_stream, side, fork);
-                k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.max_iters, L.err);
+                k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.tail_paths, L.max_iters,
+                                                             L.err);
                 cudaGraph_t captured = nullptr;
                 cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
                 e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : cudaGetLastError());
+            }
+            if (e == cudaSuccess) {
+                // after the loop: the tail kernel over the paths left (parity 0 after whole bodies)
+                e = cudaStreamBeginCaptureToGraph(capture_stream, graph, &node, nullptr, 1, cudaStreamCaptureModeRelaxed);
+                if (e == cudaSuccess) {
+                    cudaError_t e1 = wave_tail(L, 0, capture_stream);
+                    cudaGraph_t captured = nullptr;
+                    cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
+                    e = e1 != cudaSuccess ? e1 : e2;
+                }
             }
         }
     }

@@ -89,7 +89,20 @@ struct WaveLaunch {
     int grid_shade[3];  // per event kernel (fog, miss, surface), or [0] for the sorted kernel
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
+    uint32_t tail_paths;  // the bounce loop stops when at most this many paths are live; the tail
+                          // kernel then finishes them, one thread per slot
 };
+
+// Every group's state, as one kernel argument.
+struct WaveGroups {
+    WaveState W[kWaveGroups];
+    int groups;
+};
+
+// The bounce loop hands over to the tail kernel at slots / SR_TAIL_DIV live paths (0: never).
+#ifndef SR_TAIL_DIV
+#define SR_TAIL_DIV 16
+#endif
 
 // Kernels launched per bounce and group (extend, shade per event, shadow, finalize).
 #ifndef SR_SPLIT_SHADE
@@ -103,6 +116,8 @@ cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st);
 // One bounce of every group: group 0 on `st`, the others on `side` streams forked from and
 // joined back to `st` with the events in `fork` (one per group).
 cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st, const cudaStream_t* side, const cudaEvent_t* fork);
+// The tail kernel over the live paths of parity `cur` (at most L.tail_paths of them).
+cudaError_t wave_tail(const WaveLaunch& L, int cur, cudaStream_t st);
 cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, const cudaStream_t* side,
                              const cudaEvent_t* fork, cudaGraphExec_t* exec_out);
 
