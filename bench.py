@@ -140,21 +140,32 @@ def algorithmic_bytes(c: dict, pixels: int) -> int:
                + 108 * c["hit_inflate"] + 48 * c["tex_sample"] + 4 * c["cdf_probe"] + 56 * pixels)
 
 
+def oracle_bands(scene, view, params, threads: int, height: int, rows_per_band: int, bands: int = 16,
+                 shift: int = 0):
+    """Renders `bands` evenly spaced bands of `rows_per_band` image rows with the CPU oracle (a
+    stratified sample of the frame: rows differ widely in cost, sky vs. geometry).  Returns the
+    rows rendered and the seconds taken."""
+    r = max(1, min(rows_per_band, height // bands))
+    spans = []
+    for b in range(bands):
+        y0 = int((b + 0.5) * height / bands) - r // 2 + shift * r
+        y0 = max(0, min(height - r, y0))
+        spans.append((y0, y0 + r))
+    t0 = time.perf_counter()
+    for y0, y1 in spans:
+        scene.render(view, params, threads, rows=(y0, y1))
+    return r * len(spans), time.perf_counter() - t0
+
+
 def cpu_oracle_sample(desc, target_s: float, threads: int):
-    """Times the CPU oracle on a row band of the workload sized for ~target_s seconds."""
+    """Times the CPU oracle on a stratified row sample of the workload sized for ~target_s seconds."""
     from oracle import oracle
     from sharpray_gb300 import render_params
     scene = oracle.instantiate(desc)
     view, params = desc.view.to_c(), render_params(*desc.render_args())
-    mid = desc.height // 2
-    t0 = time.perf_counter()
-    scene.render(view, params, threads, rows=(mid, mid + 2))
-    dt = max(time.perf_counter() - t0, 1e-3)
-    rows = int(max(2, min(desc.height, round(2 * target_s / dt))))
-    y0 = max(0, mid - rows // 2)
-    t0 = time.perf_counter()
-    aovs, _ = scene.render(view, params, threads, rows=(y0, y0 + rows))
-    dt = time.perf_counter() - t0
+    rows1, dt1 = oracle_bands(scene, view, params, threads, desc.height, 1)
+    per_band = int(max(1, round(target_s / max(dt1, 1e-3))))
+    rows, dt = oracle_bands(scene, view, params, threads, desc.height, per_band)
     samples = rows * desc.width * desc.spp
     return samples / dt, rows, dt
 
@@ -169,23 +180,19 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     scene = oracle.instantiate(desc)
     view, params = desc.view.to_c(), render_params(*desc.render_args())
-    # calibrate a row band of ~2 s per step so the whole run stays within minutes
-    mid = desc.height // 2
-    t0 = time.perf_counter()
-    scene.render(view, params, threads, rows=(mid, mid + 1))
-    dt = max(time.perf_counter() - t0, 1e-3)
-    rows = int(max(1, min(desc.height, round(2.0 / dt))))
+    # calibrate a stratified row sample of ~2 s per step so the whole run stays within minutes
+    rows1, dt1 = oracle_bands(scene, view, params, threads, desc.height, 1)
+    per_band = int(max(1, round(2.0 / max(dt1, 1e-3))))
     for _ in range(args.warmup):
-        scene.render(view, params, threads, rows=(mid, mid + 1))
-    times = []
+        oracle_bands(scene, view, params, threads, desc.height, 1)
+    times, rows = [], 0
     for s in range(args.steps):
-        y0 = (mid - rows // 2 + s * rows) % max(1, desc.height - rows)
-        t0 = time.perf_counter()
-        scene.render(view, params, threads, rows=(y0, y0 + rows))
-        times.append(time.perf_counter() - t0)
+        rows, dt = oracle_bands(scene, view, params, threads, desc.height, per_band, shift=s % 2)
+        times.append(dt)
     samples = rows * desc.width * desc.spp * args.steps
     value = samples / sum(times)
-    sample_desc = f"{rows} image rows x {desc.width} px x {desc.spp} spp per step (of {desc.height} rows)"
+    sample_desc = (f"{rows} image rows per step in 16 evenly spaced bands x {desc.width} px x {desc.spp} spp "
+                   f"(of {desc.height} rows)")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
@@ -349,7 +356,8 @@ def run_ours(args):
         threads = os.cpu_count() or 1
         v, rows, dt = cpu_oracle_sample(desc, args.cpu_seconds, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{rows} rows x {W} px x {desc.spp} spp of the same frame ({dt:.1f} s)"}
+               "sample": f"{rows} rows in 16 evenly spaced bands x {W} px x {desc.spp} spp of the same frame "
+                         f"({dt:.1f} s)"}
 
     if rank == 0:
         out = {
@@ -369,7 +377,8 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": ("path tracer: k_render_pixels" if args.mode == 1 else
-                                    "path tracer: k_wave_extend/shade/shadow/finalize (one frame)"),
+                                    "path tracer: k_wave_extend/shade(fog,miss,surface)/shadow/finalize "
+                                    "+ k_wave_tail (one frame)"),
                          "kernel_ms": 1000 * kern_s, "alg_bytes_per_launch": alg, "peak_source": peak_kind,
                          "note": "per frame of the path tracer; alg bytes from the kernels' own work "
                                  "counters sized by the reference's records"},
@@ -380,6 +389,8 @@ def run_ours(args):
             "variants_samples_per_s": variants,
             "clocks": clocks.summary(),
             "counters_per_step": counters,
+            # closest-hit + shadow queries per second (SceneTrace + SceneOcclude counters)
+            "rays_per_s": (counters["scene_trace"] + counters["scene_occlude"]) * value / max(1, samples_per_step),
             "bounce_iterations": info["bounce_iterations"],
         }
         print(json.dumps(out), flush=True)

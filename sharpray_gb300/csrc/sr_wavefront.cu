@@ -9,8 +9,9 @@
 //              surface hit or miss -- and one queue per event.  A ray that misses the root boxes
 //              gets its event where it is made (in foggy scenes most rays start far outside the
 //              scene and leave it)
-//   shade    : first the NEE contribution of the previous segment (its shadow ray has been traced
-//              since), then the event's logic: light sample, Russian roulette, scatter
+//   shade    : first the NEE contribution of the previous segment if its shadow ray was traced
+//              since, then the event's logic: light sample (a shadow ray that misses the scene's
+//              root boxes contributes at once), Russian roulette, scatter
 //   shadow   : shadow rays (ShadowTransmittance, scene.cs:576-600) times the fog transmittance
 //   finalize : finished samples only: the last NEE contribution, the pixel statistics, the
 //              adaptive stop, and the next camera ray or the AOV write
@@ -120,10 +121,12 @@ __device__ __forceinline__ void push_block(uint32_t* const (&q)[NQ], uint32_t* c
         if (pred[i]) q[i][off[i]] = value;
 }
 
-// Ray-queue entries carry the ray itself (origin + slot, direction), so that a traversal kernel
-// starts a ray with one coalesced load instead of a queue load followed by a scattered record load.
-__device__ __forceinline__ Rec ray_entry(uint32_t slot, V3 o, V3 d) {
-    return {make_float4(o.x, o.y, o.z, __int_as_float((int)slot)), make_float4(d.x, d.y, d.z, 0.f)};
+// Ray-queue entries carry the ray itself (origin + slot, direction + bounce index), so that a
+// traversal kernel starts a ray with one coalesced load instead of a queue load followed by a
+// scattered record load.
+__device__ __forceinline__ Rec ray_entry(uint32_t slot, V3 o, V3 d, uint32_t bounce) {
+    return {make_float4(o.x, o.y, o.z, __int_as_float((int)slot)),
+            make_float4(d.x, d.y, d.z, __int_as_float((int)bounce))};
 }
 
 __device__ __forceinline__ Rng rng_of(const Rec& g) {
@@ -163,7 +166,7 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
     block_offsets<1>({&W.counts[kCountTrace]}, {valid}, sh, 0u, off);
     if (valid) {
         Rec r = ld_rec(&W.rec[rix(s, R_RAY)]);
-        W.q_trace[0][off[0]] = ray_entry(s, V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
+        W.q_trace[0][off[0]] = ray_entry(s, V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z}, 0u);
     }
 }
 
@@ -278,8 +281,8 @@ constexpr int kNodeBurst = SR_NODE_BURST;
 constexpr int kLeafWait = SR_LEAF_WAIT;
 
 // Persistent ray loop shared by extend and shadow: lanes take ray-queue entries [fetch counter)
-// until the queue is exhausted; `start()` is called as a query begins, `finish(slot, hit, ray)`
-// stores its answer and returns an output code that `emit(slot, code)` (all lanes together, -1 =
+// until the queue is exhausted; `start()` is called as a query begins, `finish(slot, tag, hit,
+// ray)` (tag: the entry's bounce index) stores its answer and returns an output code that `emit(slot, code)` (all lanes together, -1 =
 // none) passes on.
 // Each round runs the node visits of all lanes together (up to kNodeBurst), then one leaf action
 // of each lane that waits for one: leaf actions are long and differ between lanes, so batching
@@ -292,7 +295,7 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
     StackEntry stack[kSceneStack];
     SceneQuery<ANY, GENERAL> sq;
     bool busy = false, pending = false, exhausted = false;
-    uint32_t slot = 0;
+    uint32_t slot = 0, tag = 0;
     const int lane = threadIdx.x & 31;
     for (;;) {
         unsigned idle = __ballot_sync(0xffffffffu, !busy);
@@ -300,7 +303,7 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
         if (nidle >= kRefill || (exhausted && idle == 0xffffffffu)) {
             int code = -1;
             if (pending) {
-                code = finish(slot, sq.best, sq.wr);
+                code = finish(slot, tag, sq.best, sq.wr);
                 pending = false;
             }
             emit(slot, code);
@@ -315,6 +318,7 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
                 if (idx < n) {
                     Rec e = q[idx];
                     slot = (uint32_t)__float_as_int(e.a.w);
+                    tag = (uint32_t)__float_as_int(e.b.w);
                     start();
                     sq.init(S, make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z}));
                     busy = true;
@@ -340,9 +344,10 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
     }
 }
 
-// The closest hit of slot s's ray is known: store it and decide the segment's event.
+// The closest hit of slot s's ray (at bounce index `bounce`) is known: store the ray and its hit
+// (one whole 64-byte record pair) and decide the segment's event.
 __device__ __forceinline__ int extend_answer(const WaveState& W, const DevScene& S, uint32_t s, const Hit& h,
-                                             const Ray& ray) {
+                                             const Ray& ray, uint32_t bounce) {
     float sdist = 0.f;
     int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
     if (S.has_fog) {
@@ -351,6 +356,8 @@ __device__ __forceinline__ int extend_answer(const WaveState& W, const DevScene&
         ev = segment_event(S, ray, h.obj >= 0, h.dist, rng, sdist);
         st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, Col{g.b.y, g.b.z, g.b.w}));
     }
+    st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                                      make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
     st_rec(&W.rec[rix(s, R_HIT)], Rec{make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
                                       make_float4(h.u, h.v, sdist, 0.f)});
     return ev;
@@ -381,7 +388,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveSt
     persistent_queries<COUNT, false, GENERAL>(
         S, W.q_trace[cur], W.counts[kCountTrace + cur], &W.counts[kCountExtendFetch], c, err,
         [&]() { SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1); },
-        [&](uint32_t s, const Hit& h, const Ray& ray) { return extend_answer(W, S, s, h, ray); },
+        [&](uint32_t s, uint32_t bounce, const Hit& h, const Ray& ray) { return extend_answer(W, S, s, h, ray, bounce); },
         [&](uint32_t s, int ev) { stage.add(eq, ec, s, ev); });
     stage.flush(eq, ec);
     flush_counters<COUNT>(c, counters);
@@ -409,7 +416,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveSt
         persistent_queries<COUNT, true, GENERAL>(
             S, W.q_shadow, W.counts[kCountShadow], &W.counts[kCountShadowFetch], c, err,
             [&]() { SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1); },
-            [&](uint32_t s, const Hit& h, const Ray& ray) {
+            [&](uint32_t s, uint32_t, const Hit& h, const Ray& ray) {
                 float tr = 0.0f;
                 if (h.obj < 0) {
                     tr = 1.0f;
@@ -456,6 +463,7 @@ struct SegOut {
     int next = -1;
     V3 sh_o{0.f, 0.f, 0.f}, sh_d{0.f, 0.f, 0.f};  // the shadow ray, when traced
     V3 nx_o{0.f, 0.f, 0.f}, nx_d{0.f, 0.f, 0.f};  // the next ray, when traced
+    uint32_t nx_bounce = 0;                        // ... and its bounce index
 };
 
 // One segment of path slot s whose event is ev (scene.cs:640-738): first the NEE contribution of
@@ -508,7 +516,8 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
                 }
             }
             // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
-            // the shadow ray is traced by the shadow kernel, the contribution added next segment
+            // a shadow ray that needs a traversal goes to the shadow kernel and its contribution is
+            // added next segment (before anything of that segment touches the radiance)
             V3 ldir;
             float lpdf;
             if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
@@ -529,25 +538,36 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
                     }
                 }
                 if (emit) {
-                    pflags |= PF_NEE | ((fog_event && bounce == 0) ? PF_NEE_FOG : 0u);
-                    // a shadow ray that misses the scene's root boxes is unoccluded: its
-                    // transmittance is the fog's alone, formed here as the shadow kernel would
+                    const bool to_fog = fog_event && bounce == 0;
                     Ray shadow = make_ray(pos, ldir);
-                    float4 head = make_float4(pos.x, pos.y, pos.z, 0.f);
                     const bool any = !GENERAL || !S.has_transparent;
                     if (any ? misses_scene<COUNT, true>(S, shadow, c) : misses_scene<COUNT, false>(S, shadow, c)) {
+                        // a shadow ray that misses the scene's root boxes is unoccluded: its
+                        // transmittance is the fog's alone, and the light sample's contribution is
+                        // added at once, as SampleSkyDirect(Fog) forms it
                         SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
-                        float tr = 1.0f;
-                        if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, shadow);
-                        head = make_float4(tr, tr, tr, 0.f);
+                        float t = 1.0f;
+                        if (S.has_fog) t = 1.0f * fog_transmittance_inf(S, shadow);
+                        Col tr = gray(t);
+                        if (max_component(tr) > 0.0f) {
+                            Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * w3 * mis / lpdf;
+                            Col add = contrib * energy;
+                            if (to_fog)
+                                fog = fog + add;
+                            else
+                                radiance = radiance + add;
+                        }
                     } else {
+                        // traced by the shadow kernel; the contribution is added next segment
+                        pflags |= PF_NEE | (to_fog ? PF_NEE_FOG : 0u);
                         o.shadow = true;
                         o.sh_o = pos;
                         o.sh_d = ldir;
+                        st_rec(&W.rec[rix(s, R_SH0)], Rec{make_float4(pos.x, pos.y, pos.z, 0.f),
+                                                          make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
+                        st_rec(&W.rec[rix(s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
+                                                          make_float4(energy.r, energy.g, energy.b, 0.f)});
                     }
-                    st_rec(&W.rec[rix(s, R_SH0)], Rec{head, make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
-                    st_rec(&W.rec[rix(s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
-                                                   make_float4(energy.r, energy.g, energy.b, 0.f)});
                 }
             }
             if (russian_roulette(energy, bounce, rng)) {
@@ -587,11 +607,14 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
         st_rec(&W.rec[rix(s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
                      make_float4(energy.r, energy.g, energy.b, fbits(pflags))});
         if (o.live) {
-            st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                    make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
             o.next = next_segment<COUNT>(W, S, s, ray, rng, c);
             o.nx_o = ray.o;
             o.nx_d = ray.d;
+            o.nx_bounce = bounce;
+            // a traced ray's record is written by extend together with its hit
+            if (o.next >= 0)
+                st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                                                  make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
         }
         st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, fog));
     return o;
@@ -641,11 +664,11 @@ __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveS
         block_offsets<5>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve], &W.counts[kCountShadow]},
                          pred, sh, round++, off);
-        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_bounce);
         if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
         if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
         if (pred[3]) W.q_resolve[off[3]] = s;
-        if (pred[4]) W.q_shadow[off[4]] = ray_entry(s, o.sh_o, o.sh_d);
+        if (pred[4]) W.q_shadow[off[4]] = ray_entry(s, o.sh_o, o.sh_d, 0u);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -753,7 +776,7 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
         block_offsets<3>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
                          pred, sh, round++, off);
-        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, 0u);
         if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
         if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
     }
@@ -773,13 +796,18 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     int group = -1, ev = -1;
-    uint32_t s = 0;
+    uint32_t s = 0, bounce = 0;
+    V3 ro{0.f, 0.f, 0.f}, rd{0.f, 0.f, 0.f};  // the ray of a segment that needs a traversal
     for (int g = 0; g < G.groups && group < 0; ++g) {
         const WaveState& Wg = G.W[g];
         const uint32_t nt = Wg.counts[kCountTrace + cur];
         if (k < nt) {
             group = g;
-            s = (uint32_t)__float_as_int(Wg.q_trace[cur][k].a.w);
+            Rec e = Wg.q_trace[cur][k];
+            s = (uint32_t)__float_as_int(e.a.w);
+            bounce = (uint32_t)__float_as_int(e.b.w);
+            ro = V3{e.a.x, e.a.y, e.a.z};
+            rd = V3{e.b.x, e.b.y, e.b.z};
             break;
         }
         k -= nt;
@@ -803,10 +831,9 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
                 break;
             }
             if (ev < 0) {
-                Rec r = ld_rec(&W.rec[rix(s, R_RAY)]);
-                Ray ray = make_ray(V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z});
+                Ray ray = make_ray(ro, rd);
                 SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-                ev = extend_answer(W, S, s, scene_closest<COUNT, GENERAL>(S, ray, c, err), ray);
+                ev = extend_answer(W, S, s, scene_closest<COUNT, GENERAL>(S, ray, c, err), ray, bounce);
             }
             SegOut o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
             if (o.shadow) shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(o.sh_o, o.sh_d), c, err);
@@ -815,6 +842,7 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
                 if (!o.live) break;
             }
             ev = o.next;
+            ro = o.nx_o, rd = o.nx_d, bounce = o.nx_bounce;
         }
     }
     flush_counters<COUNT>(c, counters);
