@@ -434,10 +434,13 @@ constexpr int kSceneStack = 192;  // scene (<= 65) + mesh (<= 65) entries, with 
 //   QS_DONE : `best` holds the answer
 // Node actions and leaf actions are separate so that persistent kernels can run the node actions
 // of all lanes together and batch the (long, divergent) leaf actions.  GENERAL = false compiles
-// only what scenes of meshes need (no analytic shapes).
+// only what scenes of meshes need (no analytic shapes).  DYN = true (with ANY = false) makes the
+// query kind a run-time choice (init's `any`), so one loop can serve closest-hit and occlusion
+// queries: an occlusion query keeps its pruning distance at +inf, which makes every node test and
+// push/pop decision the same as the ANY form's, and stops at its first hit.
 enum : int { QS_NODE = 0, QS_TRI = 1, QS_OBJ = 2, QS_EXIT = 3, QS_DONE = 4 };
 
-template <bool ANY, bool GENERAL>
+template <bool ANY, bool GENERAL, bool DYN = false>
 struct SceneQuery {
     // The traversal stack lives outside the struct (a separate local array passed to the actions):
     // keeping the dynamically indexed array out lets the scalar state stay in registers.
@@ -452,8 +455,12 @@ struct SceneQuery {
     uint32_t pops;
     int state;
     bool in_mesh, has_node;
+    bool any_hit;  // DYN: this query is an occlusion query
 
-    SR_DEV void init(const DevScene& S, const Ray& r) {
+    SR_DEV bool is_any() const { return ANY || (DYN && any_hit); }
+
+    SR_DEV void init(const DevScene& S, const Ray& r, bool any = false) {
+        any_hit = any;
         const float inf = __int_as_float(0x7f800000);
         best = Hit{-1, -1, inf, 0.f, 0.f, 0.f};
         wr = r;
@@ -557,8 +564,8 @@ struct SceneQuery {
                 const float4* tp = S.tris + 3 * tri_next;
                 float4 q0 = ldg4(tp), q1 = ldg4(tp + 1), q2 = ldg4(tp + 2);
                 float t, u, v;
-                if (tri_hit(v3(q0), v3(q1), v3(q2), cr, t, u, v) && (ANY || t < cur_best)) {
-                    if (ANY) {
+                if (tri_hit(v3(q0), v3(q1), v3(q2), cr, t, u, v) && (is_any() || t < cur_best)) {
+                    if (is_any()) {
                         best = {obj_pos, tri_next, 0.f, 0.f, 0.f, 0.f};
                         tri_left = 0;
                         state = QS_DONE;
@@ -579,7 +586,7 @@ struct SceneQuery {
             }
             in_mesh = false;
             cr = wr;
-            cur_best = ANY ? inf : best.dist;
+            cur_best = is_any() ? inf : best.dist;
             next_state();
         } else if (state == QS_OBJ) {
             const DevObject& o = S.objects[leaf_next];
@@ -606,7 +613,7 @@ struct SceneQuery {
                 bool ok = kind == SR_SHAPE_SPHERE ? sphere_hit(o.shape0, l, h, false)
                                                   : box_hit(o.shape0, o.shape1, l, h, false);
                 if (ok) {
-                    if (ANY) {
+                    if (is_any()) {
                         best = {obj_pos, -1, 0.f, 0.f, 0.f, 0.f};
                         state = QS_DONE;
                         return;

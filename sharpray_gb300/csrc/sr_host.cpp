@@ -735,10 +735,10 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
     for (int g = 0; g < kWaveGroups; ++g) group_slots[g] = (uint32_t)(tiles > (uint32_t)g ? (tiles - g + kWaveGroups - 1) / kWaveGroups : 0) * 32;
     if (s->wave_slots < n || !s->wave.ptr) {
         // 32-byte sectors: path records (6 per slot), pixel records (4 per slot); 16-byte medium;
-        // queues per group slot: ray entries (32 B) trace x2 + shadow, 4-byte event 3 x2 + resolve;
-        // arrays start on 256 bytes
+        // queues per group slot: ray entries (32 B) trace x2 + shadow x2, 4-byte event 3 x2 + late x2 +
+        // resolve; arrays start on 256 bytes
         const size_t rec = sizeof(Rec);
-        size_t bytes = n * (10 * rec + 16 + 3 * rec + 7 * 4) + (3 + 6 * kWaveGroups) * 256 +
+        size_t bytes = n * (10 * rec + 16 + 4 * rec + 9 * 4) + (3 + 9 * kWaveGroups) * 256 +
                        kWaveGroups * kWaveCounters * sizeof(uint32_t);
         SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
         s->wave_slots = (uint32_t)n;
@@ -768,7 +768,10 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         w.q_event[0] = (uint32_t*)take(m, 3 * 4);
         w.q_event[1] = (uint32_t*)take(m, 3 * 4);
         w.q_resolve = (uint32_t*)take(m, 4);
-        w.q_shadow = (Rec*)take(m, rec);
+        w.q_shadow[0] = (Rec*)take(m, rec);
+        w.q_shadow[1] = (Rec*)take(m, rec);
+        w.q_late[0] = (uint32_t*)take(m, 4);
+        w.q_late[1] = (uint32_t*)take(m, 4);
     }
     for (int g = 0; g < kWaveGroups; ++g) s->ws[g].counts = (uint32_t*)p + g * kWaveCounters;
     return SR_OK;

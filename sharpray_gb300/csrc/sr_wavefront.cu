@@ -1,39 +1,44 @@
 // sr_wavefront.cu — wavefront form of the per-pixel path loop.
 //
-// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into four
-// kernels per bounce over per-path state records, one slot per pixel:
+// Renderer.Render (renderer.cs:153-229) + Scene.Sample (scene.cs:627-741) are split into kernels
+// over per-path state records, one slot per pixel.  Per bounce:
 //
-//   extend   : closest hit of every live path ray            (Scene.Trace -> Bvh.Intersect)
-//              that enters the root boxes of the scene BVH, then the segment's event -- fog
-//              scatter (the free-flight distance is drawn here, the segment's first RNG draw),
-//              surface hit or miss -- and one queue per event.  A ray that misses the root boxes
-//              gets its event where it is made (in foggy scenes most rays start far outside the
-//              scene and leave it)
-//   shade    : first the NEE contribution of the previous segment if its shadow ray was traced
-//              since, then the event's logic: light sample (a shadow ray that misses the scene's
-//              root boxes contributes at once), Russian roulette, scatter
-//   shadow   : shadow rays (ShadowTransmittance, scene.cs:576-600) times the fog transmittance
-//   finalize : finished samples only: the last NEE contribution, the pixel statistics, the
-//              adaptive stop, and the next camera ray or the AOV write
+//   trace    : one persistent traversal loop over two ray queues: the closest hit of every path
+//              ray that enters the root boxes of the scene BVH (Scene.Trace -> Bvh.Intersect),
+//              followed by its segment's event -- fog scatter (the free-flight distance is drawn
+//              here, the segment's first RNG draw), surface hit or miss -- into one queue per
+//              event; and the shadow rays of the previous bounce's light samples
+//              (ShadowTransmittance scene.cs:576-600 x fog transmittance).  A ray that misses the
+//              root boxes is decided where it is made: in foggy scenes most rays start far outside
+//              the scene and leave it
+//   late     : samples that finished last bounce with a shadow ray still to trace: its
+//              contribution, the pixel statistics, the adaptive stop, the next camera ray
+//   shade    : one kernel per event: first the NEE contribution of the previous segment if its
+//              shadow ray was traced since, then the event's logic: light sample (a shadow ray that
+//              misses the root boxes contributes at once, others are queued), Russian roulette,
+//              scatter
+//   finalize : samples that finished this bounce without a shadow ray to trace: pixel statistics,
+//              adaptive stop, next camera ray or the AOV write
 //
 // Sorting paths by event makes every shade warp run one branch: fog scatter, surface and miss
 // logic differ completely, and in foggy scenes most segments end in the fog while a few hit
 // surfaces, so unsorted warps nearly always ran all three.
 //
-// extend and shadow are persistent: a lane that finishes its ray takes the next one from the
-// queue at once (refilled per warp with one atomic), so warps stay full although ray lengths
-// differ by orders of magnitude.
+// The trace loop is persistent: a lane that finishes its ray takes the next one from the queues
+// at once (refilled per warp with one atomic), so warps stay full although ray lengths differ by
+// orders of magnitude, and shadow rays fill the SMs while the last long path rays finish.
 //
 // Paths are compacted into queues between kernels with aggregated atomics (per block in the
 // grid-stride kernels, per warp and 32 entries in the persistent ones), so every launch works on
-// dense queues.  Every per-path operation -- RNG draws, float operation order,
-// the order in which contributions are added -- is the megakernel's (sr_path.cuh), so the two
-// forms produce identical images: a segment's NEE contribution is added before anything of the
-// next segment touches the radiance, exactly where the megakernel adds it.
+// dense queues.  Every per-path operation -- RNG draws, float operation order, the order in
+// which contributions are added -- is the megakernel's (sr_path.cuh), so the two forms produce
+// identical images: a segment's NEE contribution is added before anything of the next segment
+// (or the end of its sample) touches the radiance, exactly where the megakernel adds it.
 //
 // The bounce loop runs either as a host loop (one launch per kernel per bounce, the host reads the
 // live-path count after every bounce) or as a CUDA graph whose conditional WHILE node repeats the
-// bounce kernels on the device until no path is left (no host round trip per bounce).
+// bounce kernels on the device (no host round trip per bounce).  Either hands the last few live
+// paths to a tail kernel that runs each to completion.
 #include <cuda_runtime.h>
 
 #include "sr_path.cuh"
@@ -181,9 +186,10 @@ __device__ __forceinline__ int segment_event(const DevScene& S, const Ray& ray, 
     return has_hit ? EV_SURF : EV_MISS;
 }
 
-// A new path ray (scatter or camera ray): -1 when it needs the next extend's traversal; when it
-// misses both root children of the scene BVH -- the first thing the traversal tests -- its empty
-// closest hit is written here, as extend would write it, and its segment's event is returned.
+// A new path ray (scatter or camera ray): -1 when it needs the next trace kernel's traversal; when
+// it misses both root children of the scene BVH -- the first thing the traversal tests -- its
+// empty closest hit is written here, as the trace kernel would write it, and its segment's event
+// is returned.
 template <bool COUNT>
 __device__ __forceinline__ int next_segment(const WaveState& W, const DevScene& S, uint32_t s, const Ray& ray, Rng& rng,
                                             Ctr& c) {
@@ -280,20 +286,23 @@ constexpr int shade_min_blocks(int ev) { return ev == 0 || ev == 1 ? SR_SHADE_FO
 constexpr int kNodeBurst = SR_NODE_BURST;
 constexpr int kLeafWait = SR_LEAF_WAIT;
 
-// Persistent ray loop shared by extend and shadow: lanes take ray-queue entries [fetch counter)
-// until the queue is exhausted; `start()` is called as a query begins, `finish(slot, tag, hit,
-// ray)` (tag: the entry's bounce index) stores its answer and returns an output code that `emit(slot, code)` (all lanes together, -1 =
+// Persistent ray loop: lanes take entries [fetch counter) of the concatenation of two ray queues
+// -- q0 closest-hit queries, q1 occlusion queries -- until both are exhausted; `start(any)` is
+// called as a query begins, `finish(slot, tag, any, hit, ray)` (tag: the entry's bounce index)
+// stores its answer and returns an output code that `emit(slot, code)` (all lanes together, -1 =
 // none) passes on.
 // Each round runs the node visits of all lanes together (up to kNodeBurst), then one leaf action
 // of each lane that waits for one: leaf actions are long and differ between lanes, so batching
 // them keeps warps from running each one with a single lane.  Finished lanes are answered in a
 // batch when the warp refills.  Every lane's own sequence of actions is unchanged, so results are
 // those of a plain loop over SceneQuery::step.
-template <bool COUNT, bool ANY, bool GENERAL, typename Start, typename Finish, typename Emit>
-__device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec* q, uint32_t n, uint32_t* fetch,
-                                                   Ctr& c, uint32_t* err, Start start, Finish finish, Emit emit) {
+template <bool COUNT, bool GENERAL, typename Start, typename Finish, typename Emit>
+__device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec* q0, uint32_t n0, const Rec* q1,
+                                                   uint32_t n1, uint32_t* fetch, Ctr& c, uint32_t* err, Start start,
+                                                   Finish finish, Emit emit) {
     StackEntry stack[kSceneStack];
-    SceneQuery<ANY, GENERAL> sq;
+    SceneQuery<false, GENERAL, true> sq;
+    const uint32_t n = n0 + n1;
     bool busy = false, pending = false, exhausted = false;
     uint32_t slot = 0, tag = 0;
     const int lane = threadIdx.x & 31;
@@ -303,7 +312,7 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
         if (nidle >= kRefill || (exhausted && idle == 0xffffffffu)) {
             int code = -1;
             if (pending) {
-                code = finish(slot, tag, sq.best, sq.wr);
+                code = finish(slot, tag, sq.any_hit, sq.best, sq.wr);
                 pending = false;
             }
             emit(slot, code);
@@ -316,11 +325,12 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
             if (!busy) {
                 uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (idx < n) {
-                    Rec e = q[idx];
+                    const bool any = idx >= n0;
+                    Rec e = any ? q1[idx - n0] : q0[idx];
                     slot = (uint32_t)__float_as_int(e.a.w);
                     tag = (uint32_t)__float_as_int(e.b.w);
-                    start();
-                    sq.init(S, make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z}));
+                    start(any);
+                    sq.init(S, make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z}), any);
                     busy = true;
                 }
             }
@@ -363,14 +373,20 @@ __device__ __forceinline__ int extend_answer(const WaveState& W, const DevScene&
     return ev;
 }
 
-template <bool COUNT, bool GENERAL>
-__global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveState W, DevScene S, int cur, uint32_t* err,
-                                                     unsigned long long* counters) {
+// Traversals of the bounce: the closest hit of every queued path ray, then its segment's event
+// (one event queue each), and -- WITH_SHADOW -- the shadow rays of the previous bounce's light
+// samples in the same persistent loop (any hit -> black in opaque scenes, else the fog
+// transmittance, written over the request's origin; SampleSkyLight scene.cs:758-772).  One loop
+// for both keeps the SMs busy while either kind's last long rays finish.
+template <bool COUNT, bool GENERAL, bool WITH_SHADOW>
+__global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveState W, DevScene S, int cur,
+                                                                          uint32_t* err, unsigned long long* counters) {
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        W.counts[kCountResolve] = 0;      // finished samples of this bounce
-        W.counts[kCountShadow] = 0;       // shadow queue of this bounce starts empty
-        W.counts[kCountTrace + nxt] = 0;  // the next bounce's queues start empty
+        W.counts[kCountResolve] = 0;  // the next bounce's queues start empty
+        W.counts[kCountTrace + nxt] = 0;
+        W.counts[kCountShadow + nxt] = 0;
+        W.counts[kCountLate + nxt] = 0;
         W.counts[kCountEvent + 3 * nxt + EV_FOG] = 0;
         W.counts[kCountEvent + 3 * nxt + EV_MISS] = 0;
         W.counts[kCountEvent + 3 * nxt + EV_SURF] = 0;
@@ -385,10 +401,20 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_extend(WaveSt
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
-    persistent_queries<COUNT, false, GENERAL>(
-        S, W.q_trace[cur], W.counts[kCountTrace + cur], &W.counts[kCountExtendFetch], c, err,
-        [&]() { SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1); },
-        [&](uint32_t s, uint32_t bounce, const Hit& h, const Ray& ray) { return extend_answer(W, S, s, h, ray, bounce); },
+    persistent_queries<COUNT, GENERAL>(
+        S, W.q_trace[cur], W.counts[kCountTrace + cur], W.q_shadow[cur], WITH_SHADOW ? W.counts[kCountShadow + cur] : 0u,
+        &W.counts[kCountTraceFetch], c, err,
+        [&](bool any) { SR_COUNT(c, any ? SR_COUNTER_SCENE_OCCLUDE : SR_COUNTER_SCENE_TRACE, 1); },
+        [&](uint32_t s, uint32_t bounce, bool any, const Hit& h, const Ray& ray) {
+            if (!any) return extend_answer(W, S, s, h, ray, bounce);
+            float tr = 0.0f;
+            if (h.obj < 0) {
+                tr = 1.0f;
+                if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, ray);
+            }
+            st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr, tr, tr, 0.f));
+            return -1;
+        },
         [&](uint32_t s, int ev) { stage.add(eq, ec, s, ev); });
     stage.flush(eq, ec);
     flush_counters<COUNT>(c, counters);
@@ -404,35 +430,19 @@ __device__ __forceinline__ void shadow_trace(const WaveState& W, const DevScene&
     st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr.r, tr.g, tr.b, 0.f));
 }
 
-// Shadow rays of the bounce: transmittance (any hit -> black in opaque scenes) times the fog
-// transmittance, as SampleSkyLight forms it (scene.cs:758-772); written over the ray origin.
+// Shadow rays of the previous bounce in scenes with transparent materials, where a shadow ray is a
+// closest-hit loop through the transparent objects it meets.
 template <bool COUNT, bool GENERAL>
-__global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_shadow(WaveState W, DevScene S, uint32_t* err,
-                                                     unsigned long long* counters) {
+__global__ void __launch_bounds__(128) k_wave_shadow_loop(WaveState W, DevScene S, int cur, uint32_t* err,
+                                                         unsigned long long* counters) {
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
-    if (!GENERAL || !S.has_transparent) {
-        persistent_queries<COUNT, true, GENERAL>(
-            S, W.q_shadow, W.counts[kCountShadow], &W.counts[kCountShadowFetch], c, err,
-            [&]() { SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1); },
-            [&](uint32_t s, uint32_t, const Hit& h, const Ray& ray) {
-                float tr = 0.0f;
-                if (h.obj < 0) {
-                    tr = 1.0f;
-                    if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, ray);
-                }
-                st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr, tr, tr, 0.f));
-                return -1;
-            },
-            [](uint32_t, int) {});
-    } else {
-        const uint32_t n = W.counts[kCountShadow];
-        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-            Rec e = W.q_shadow[k];
-            shadow_trace<COUNT, GENERAL>(W, S, (uint32_t)__float_as_int(e.a.w),
-                                         make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z}), c, err);
-        }
+    const uint32_t n = W.counts[kCountShadow + cur];
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        Rec e = W.q_shadow[cur][k];
+        shadow_trace<COUNT, GENERAL>(W, S, (uint32_t)__float_as_int(e.a.w),
+                                     make_ray(V3{e.a.x, e.a.y, e.a.z}, V3{e.b.x, e.b.y, e.b.z}), c, err);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -611,7 +621,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
             o.nx_o = ray.o;
             o.nx_d = ray.d;
             o.nx_bounce = bounce;
-            // a traced ray's record is written by extend together with its hit
+            // a traced ray's record is written by the trace kernel together with its hit
             if (o.next >= 0)
                 st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
                                                   make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
@@ -626,8 +636,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
 template <bool COUNT, bool GENERAL, int EVK>
 __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveState W, DevScene S, DevParams P, int cur,
                                                                           uint32_t* err, unsigned long long* counters) {
-    if (EVK <= 0 && blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountShadowFetch] = 0;
-    __shared__ uint32_t sh[2][5][kBlockWarps + 1];
+    __shared__ uint32_t sh[2][6][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
 #pragma unroll
@@ -658,17 +667,21 @@ __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveS
             o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
         }
         uint32_t* eq = W.q_event[nxt];
-        const bool pred[5] = {valid && o.live && o.next < 0, valid && o.live && o.next == EV_FOG,
-                              valid && o.live && o.next == EV_MISS, valid && !o.live, valid && o.shadow};
-        uint32_t off[5];
-        block_offsets<5>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
-                          &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve], &W.counts[kCountShadow]},
+        // finished samples wait for their last shadow ray (traced next bounce) when it has one
+        const bool pred[6] = {valid && o.live && o.next < 0, valid && o.live && o.next == EV_FOG,
+                              valid && o.live && o.next == EV_MISS, valid && !o.live && !o.shadow,
+                              valid && !o.live && o.shadow, valid && o.shadow};
+        uint32_t off[6];
+        block_offsets<6>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
+                          &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve],
+                          &W.counts[kCountLate + nxt], &W.counts[kCountShadow + nxt]},
                          pred, sh, round++, off);
         if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_bounce);
         if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
         if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
         if (pred[3]) W.q_resolve[off[3]] = s;
-        if (pred[4]) W.q_shadow[off[4]] = ray_entry(s, o.sh_o, o.sh_d, 0u);
+        if (pred[4]) W.q_late[nxt][off[4]] = s;
+        if (pred[5]) W.q_shadow[nxt][off[5]] = ray_entry(s, o.sh_o, o.sh_d, 0u);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -749,22 +762,25 @@ __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevS
 
 // Finished samples: the pending NEE contribution of the last segment, then the pixel statistics
 // and the adaptive stop (renderer.cs:173-212), then the next camera ray or the AOV write.
-template <bool COUNT, bool GENERAL>
+// LATE: the samples that finished last bounce with a shadow ray, traced since by this bounce's
+// trace kernel; else the samples finished this bounce without one.
+template <bool COUNT, bool GENERAL, bool LATE>
 __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, DevView V, DevParams P, DevAovs out,
                                                        int cur, uint32_t* err, unsigned long long* counters) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountExtendFetch] = 0;  // next extend's fetch cursor
+    if (!LATE && blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountTraceFetch] = 0;  // next trace's fetch cursor
     __shared__ uint32_t sh[2][3][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     const int nxt = cur ^ 1;
-    const uint32_t n = W.counts[kCountResolve];
+    const uint32_t n = LATE ? W.counts[kCountLate + cur] : W.counts[kCountResolve];
+    const uint32_t* q = LATE ? W.q_late[cur] : W.q_resolve;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         uint32_t k = base + threadIdx.x;
         bool valid = k < n;
-        uint32_t s = valid ? W.q_resolve[k] : 0u;
+        uint32_t s = valid ? q[k] : 0u;
         SegOut o;
         if (valid) {
             o = finalize_sample<COUNT, GENERAL>(W, S, V, P, out, s, c);
@@ -783,11 +799,14 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
     flush_counters<COUNT>(c, counters);
 }
 
+constexpr int kTailFinalize = 16;  // tail-kernel state: the slot's sample is finished
+
 // The last paths of a frame, one thread per slot run to completion.  When few paths are left the
 // bounce kernels are bound by the latency of their few longest paths plus the launch gaps of
 // every bounce, while one thread per slot runs the same steps back to back -- traversal, event,
 // shading, shadow ray, end of sample -- in the same order, so results are identical.  The live
-// slots of parity `cur` are those of every group's trace queue and event queues.
+// slots of parity `cur` are those of every group's trace, event and late queues; a slot's shadow
+// ray still queued is traced first.
 template <bool COUNT, bool GENERAL>
 __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, DevView V, DevParams P, DevAovs out,
                                                    int cur, uint32_t* err, unsigned long long* counters) {
@@ -811,7 +830,7 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
             break;
         }
         k -= nt;
-        for (int e = 0; e < 3; ++e) {
+        for (int e = 0; e < 3 && group < 0; ++e) {
             const uint32_t ne = Wg.counts[kCountEvent + 3 * cur + e];
             if (k < ne) {
                 group = g, ev = e;
@@ -820,9 +839,23 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
             }
             k -= ne;
         }
+        if (group >= 0) break;
+        const uint32_t nl = Wg.counts[kCountLate + cur];
+        if (k < nl) {
+            group = g, ev = kTailFinalize;
+            s = Wg.q_late[cur][k];
+            break;
+        }
+        k -= nl;
     }
     if (group >= 0) {
         const WaveState W = G.W[group];
+        // the slot's shadow ray queued for the next bounce, if any: traced first
+        if (ibits(ld_rec(&W.rec[rix(s, R_PATH)]).b.w) & PF_NEE) {
+            Rec r0 = ld_rec(&W.rec[rix(s, R_SH0)]);
+            shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(V3{r0.a.x, r0.a.y, r0.a.z}, V3{r0.b.x, r0.b.y, r0.b.z}), c,
+                                         err);
+        }
         // every step advances a segment or ends a sample, so this bounds a well-formed frame
         const uint64_t cap = ((uint64_t)P.max_samples + 1) * ((uint64_t)P.bounces + 2) * 2 + 8;
         for (uint64_t step = 0;; ++step) {
@@ -830,13 +863,18 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
                 atomicOr(err, SR_DEVERR_LOOP);
                 break;
             }
-            if (ev < 0) {
-                Ray ray = make_ray(ro, rd);
-                SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-                ev = extend_answer(W, S, s, scene_closest<COUNT, GENERAL>(S, ray, c, err), ray, bounce);
+            SegOut o;
+            if (ev == kTailFinalize) {
+                o.live = false;
+            } else {
+                if (ev < 0) {
+                    Ray ray = make_ray(ro, rd);
+                    SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
+                    ev = extend_answer(W, S, s, scene_closest<COUNT, GENERAL>(S, ray, c, err), ray, bounce);
+                }
+                o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
+                if (o.shadow) shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(o.sh_o, o.sh_d), c, err);
             }
-            SegOut o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
-            if (o.shadow) shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(o.sh_o, o.sh_d), c, err);
             if (!o.live) {
                 o = finalize_sample<COUNT, GENERAL>(W, S, V, P, out, s, c);
                 if (!o.live) break;
@@ -868,7 +906,15 @@ __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* cou
 // ---- launchers ------------------------------------------------------------------------------------
 template <bool COUNT, bool GENERAL>
 static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st) {
-    k_wave_extend<COUNT, GENERAL><<<L.grid_extend, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
+    const bool loop_shadows = GENERAL && L.S.has_transparent;
+    if (loop_shadows) {
+        k_wave_trace<COUNT, GENERAL, false><<<L.grid_trace, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
+        k_wave_shadow_loop<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
+    } else {
+        k_wave_trace<COUNT, GENERAL, true><<<L.grid_trace, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
+    }
+    k_wave_finalize<COUNT, GENERAL, true><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
+                                                                           L.counters);
     if (SR_SPLIT_SHADE) {
         k_wave_shade<COUNT, GENERAL, EV_FOG><<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
         k_wave_shade<COUNT, GENERAL, EV_MISS><<<L.grid_shade[1], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
@@ -876,8 +922,8 @@ static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cuda
     } else {
         k_wave_shade<COUNT, GENERAL, -1><<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
     }
-    k_wave_shadow<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, L.err, L.counters);
-    k_wave_finalize<COUNT, GENERAL><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err, L.counters);
+    k_wave_finalize<COUNT, GENERAL, false><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
+                                                                            L.counters);
 }
 
 static void launch_group_bounces(const WaveLaunch& L, const WaveState& W, int cur, int n, cudaStream_t st) {
@@ -916,9 +962,9 @@ static cudaError_t launch_bounces(const WaveLaunch& L, int cur, int n, cudaStrea
 
 template <bool GENERAL>
 static void occupancy(int* b) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_wave_extend<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_shadow<false, GENERAL>, 128, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_finalize<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[0], k_wave_trace<false, GENERAL, true>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_shadow_loop<false, GENERAL>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_finalize<false, GENERAL, false>, 128, 0);
     if (SR_SPLIT_SHADE) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shade<false, GENERAL, EV_FOG>, 128, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_wave_shade<false, GENERAL, EV_MISS>, 128, 0);
@@ -935,7 +981,7 @@ void wave_grid_sizes(WaveLaunch& L, int sms) {
     else
         occupancy<false>(b);
     for (int& v : b) v = sms * (v > 0 ? v : 1);
-    L.grid_extend = b[0];
+    L.grid_trace = b[0];
     L.grid_shadow = b[1];
     L.grid_finalize = b[2];
     L.grid_shade[0] = b[3];

@@ -51,29 +51,31 @@ struct WaveState {
                             // {origin, slot (int bits)}, {direction, -}
     uint32_t* q_event[2];   // paths whose next segment's event is known, three queues of `slots`
                             // entries each: fog scatter, miss, surface hit (ping-pong)
-    uint32_t* q_resolve;    // finished samples
-    Rec* q_shadow;          // shadow rays, entries as q_trace
+    Rec* q_shadow[2];       // shadow rays (ping-pong), entries as q_trace
+    uint32_t* q_late[2];    // finished samples whose last shadow ray is still to trace (ping-pong)
+    uint32_t* q_resolve;    // finished samples without a shadow ray to trace
     uint32_t* counts;       // this group's counters, kCount* below
 };
 
 // Number of 32-bit counters at WaveState::counts, and their layout.
 constexpr int kWaveCounters = 16;
 enum : int {
-    kCountResolve = 0,       // finished samples of this bounce
-    kCountIter = 1,          // bounces run by the device loop
-    kCountExtendFetch = 2,   // extend's fetch cursor
-    kCountShadowFetch = 3,   // shadow's fetch cursor
-    kCountShadow = 4,        // shadow rays of this bounce
-    kCountTrace = 6,         // + parity: trace-queue length
-    kCountEvent = 8,         // + 3 * parity + event: event-queue lengths
+    kCountResolve = 0,     // samples finished this bounce without a shadow ray to trace
+    kCountIter = 1,        // bounces run by the device loop
+    kCountTraceFetch = 2,  // the trace kernel's fetch cursor
+    kCountTrace = 4,       // + parity: trace-queue length
+    kCountShadow = 6,      // + parity: shadow-queue length
+    kCountLate = 8,        // + parity: late finished samples
+    kCountEvent = 10,      // + 3 * parity + event: event-queue lengths
 };
-// Paths alive for the bounce of the given parity: queued for a traversal or with a known event.
+// Paths alive for the bounce of the given parity: queued for a traversal, with a known event, or
+// finished with their last shadow ray still to trace.
 #if defined(__CUDACC__)
 __host__ __device__
 #endif
 inline uint32_t wave_live(const uint32_t* counts, int parity) {
     return counts[kCountTrace + parity] + counts[kCountEvent + 3 * parity] + counts[kCountEvent + 3 * parity + 1] +
-           counts[kCountEvent + 3 * parity + 2];
+           counts[kCountEvent + 3 * parity + 2] + counts[kCountLate + parity];
 }
 
 struct WaveLaunch {
@@ -85,7 +87,7 @@ struct WaveLaunch {
     DevAovs out;
     uint32_t* err;
     unsigned long long* counters;
-    int grid_extend, grid_shadow, grid_finalize;
+    int grid_trace, grid_shadow, grid_finalize;
     int grid_shade[3];  // per event kernel (fog, miss, surface), or [0] for the sorted kernel
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
@@ -104,7 +106,8 @@ struct WaveGroups {
 #define SR_TAIL_DIV 16
 #endif
 
-// Kernels launched per bounce and group (extend, shade per event, shadow, finalize).
+// Kernels launched per bounce and group: trace, late finalize, shade per event, finalize (plus a
+// shadow-loop kernel in scenes with transparent materials).
 #ifndef SR_SPLIT_SHADE
 #define SR_SPLIT_SHADE 1
 #endif
