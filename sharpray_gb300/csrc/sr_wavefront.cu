@@ -259,7 +259,7 @@ struct WarpStage {
 constexpr int kRefill = SR_REFILL;
 // Minimum resident blocks per SM requested for the traversal kernels (caps their registers).
 #ifndef SR_TRACE_MIN_BLOCKS
-#define SR_TRACE_MIN_BLOCKS 6
+#define SR_TRACE_MIN_BLOCKS 7
 #endif
 // Node phase of the persistent loop: at most SR_NODE_BURST node visits per round, ended early
 // once SR_LEAF_WAIT lanes wait for a leaf action (triangles, entering or leaving an object) or

@@ -16,12 +16,13 @@ struct alignas(32) Rec {
     float4 a, b;
 };
 
-// The pixel slots are split into independent groups (tile t belongs to group t % groups), each a
-// complete wavefront with its own queues and counters.  The groups' bounce kernels run on parallel
-// branches of the graph, so that while one group's kernel drains (its last long rays occupy a few
-// warps) the other group's kernel fills the idle SMs.
+// The pixel slots can be split into independent groups (tile t belongs to group t % groups), each
+// a complete wavefront with its own queues and counters whose bounce kernels run on parallel
+// branches of the graph, so that while one group's kernel drains the other's fills the idle SMs.
+// With shadow rays traced in the same persistent loop as path rays one group measured best
+// (C2 1080p on GB300: 1 group 413, 2 groups 400 M samples/s).
 #ifndef SR_WAVE_GROUPS
-#define SR_WAVE_GROUPS 2
+#define SR_WAVE_GROUPS 1
 #endif
 constexpr int kWaveGroups = SR_WAVE_GROUPS;
 

@@ -3,9 +3,9 @@
 Bars:
 * closest hit (object, triangle, distance bits, barycentric bits): bit-exact on seeded ray sets;
 * RNG-driven AOVs: the sample counts and primary-hit planes match wherever the per-pixel random
-  stream has not diverged; radiance statistically equal: relMSE(GPU, oracle) below the Monte-Carlo
-  noise floor and per-pixel relative error < 1e-3 on most pixels (the two sides evaluate
-  sin/cos/exp/log/pow with different ulp-accurate libraries, so a rare path forks);
+  stream has not diverged; radiance: relMSE(GPU, oracle) < 1e-4 and per-pixel relative error
+  < 1e-3 on >= 99.5 % of pixels (the two sides evaluate sin/cos/exp/log/pow with different
+  ulp-accurate libraries, so a rare path forks);
 * compositor: RGB8 within 1 code value on >= 99.9 % of pixels for identical input AOVs.
 """
 import math
@@ -100,9 +100,11 @@ def test_render_matches_oracle(built, name):
     tot = rend.radiance + rend.radiance_fog
     tref = ref.radiance + ref.radiance_fog
     err = np.abs(tot - tref).max(axis=1) / np.maximum(np.abs(tref).max(axis=1), 1e-3)
+    # image tolerance of the project: per-pixel relative error < 1e-3 on >= 99.5 % of pixels and
+    # relMSE < 1e-4 at equal seeds and spp
     frac = float((err < 1e-3).mean())
-    assert frac >= 0.95, f"only {frac:.4f} of pixels within 1e-3"
-    assert rel_mse(tot, tref) < 5e-3
+    assert frac >= 0.995, f"only {frac:.4f} of pixels within 1e-3"
+    assert rel_mse(tot, tref) < 1e-4
 
 
 def test_render_device_api_matches_host_api(built, gpu_ctx):
