@@ -377,7 +377,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": ("path tracer: k_render_pixels" if args.mode == 1 else
-                                    "path tracer: k_wave_extend/shade(fog,miss,surface)/shadow/finalize "
+                                    "path tracer: k_wave_trace/finalize(late)/shade(fog,miss,surface)/finalize "
                                     "+ k_wave_tail (one frame)"),
                          "kernel_ms": 1000 * kern_s, "alg_bytes_per_launch": alg, "peak_source": peak_kind,
                          "note": "per frame of the path tracer; alg bytes from the kernels' own work "
