@@ -80,6 +80,9 @@ typedef struct SrMaterial {
 
 enum { SR_SHAPE_MESH = 0, SR_SHAPE_SPHERE = 1, SR_SHAPE_AABOX = 2 };
 
+/* Where BVHs are built (sr_ctx_set_bvh_build, sr_bvh_build). */
+enum { SR_BVH_BUILD_HOST = 0, SR_BVH_BUILD_DEVICE = 1 };
+
 /* Reference: IShape implementations Mesh (mesh.cs:4), Sphere (math.cs:1179), AABox (math.cs:936).
  * sphere: params = {cx, cy, cz, radius}; aabox: params = {minx, miny, minz, maxx, maxy, maxz}. */
 typedef struct SrShape {
@@ -207,6 +210,18 @@ SR_API int sr_texture_create(SrContext* ctx, const float* texels_rgb, uint32_t w
  * permutation identical to bvh.cs) and uploads triangles + attributes.  Replaces
  * Mesh(IReadOnlyList<Triangle>) mesh.cs:18-45. */
 SR_API int sr_mesh_create(SrContext* ctx, const SrTriangle* triangles, uint32_t count, int32_t* out_id);
+/* Where sr_mesh_create and sr_scene_build build their BVHs: SR_BVH_BUILD_HOST (default) or
+ * SR_BVH_BUILD_DEVICE (level by level on the context's GPU; node order, item permutation and bounds
+ * bit-identical to the host build).  No counterpart in the reference, which builds on the CPU
+ * (bvh.cs:58-75). */
+SR_API int sr_ctx_set_bvh_build(SrContext* ctx, int32_t where);
+/* The reference's Bvh over arbitrary shape bounds (Bvh ctor bvh.cs:58-75 with InsertRoot/Subdivide
+ * :285-459): `bounds` holds {min xyz, max xyz} per shape; built on the host or, with
+ * SR_BVH_BUILD_DEVICE, on the context's GPU.  Outputs as sr_mesh_bvh_export, sized for 2*count
+ * nodes (node_links and items may be NULL); `node_count` receives the nodes used. */
+SR_API int sr_bvh_build(SrContext* ctx, const float* bounds, uint32_t count, float cost_traverse,
+                        float cost_intersect, int32_t bins, int32_t where, float* node_bounds, int32_t* node_links,
+                        int32_t* items, uint32_t* node_count);
 /* Node count of a mesh BVH (for sizing sr_mesh_bvh_export buffers). */
 SR_API int sr_mesh_bvh_size(SrContext* ctx, int32_t mesh, uint32_t* node_count, uint32_t* item_count);
 /* Exports the BVH exactly as bvh.cs stores it: per node {min xyz, max xyz} floats (6 per node)

@@ -24,6 +24,9 @@ SR_SHAPE_MESH = 0
 SR_SHAPE_SPHERE = 1
 SR_SHAPE_AABOX = 2
 
+SR_BVH_BUILD_HOST = 0
+SR_BVH_BUILD_DEVICE = 1
+
 SR_RENDER_AUTO = 0
 SR_RENDER_MEGAKERNEL = 1
 SR_RENDER_WAVEFRONT = 2
@@ -113,6 +116,8 @@ PROTOTYPES = {
     "sr_triangles_from_corners": (_I, [_P, _P, _P, _U, C.c_int32, _P]),
     "sr_texture_create": (_I, [_P, _P, _U, _U, C.c_int32, _F, _F, C.POINTER(C.c_int32)]),
     "sr_mesh_create": (_I, [_P, _P, _U, C.POINTER(C.c_int32)]),
+    "sr_ctx_set_bvh_build": (_I, [_P, C.c_int32]),
+    "sr_bvh_build": (_I, [_P, _P, _U, _F, _F, C.c_int32, C.c_int32, _P, _P, _P, C.POINTER(_U)]),
     "sr_mesh_bvh_size": (_I, [_P, C.c_int32, C.POINTER(_U), C.POINTER(_U)]),
     "sr_mesh_bvh_export": (_I, [_P, C.c_int32, _P, _P, _P]),
     "sr_scene_create": (_I, [_P, C.POINTER(_P)]),

@@ -56,6 +56,26 @@ class Context:
         self.handle = h
         self.device = device
 
+    def set_bvh_build(self, where: int) -> None:
+        """Where meshes and scenes build their BVHs: _abi.SR_BVH_BUILD_HOST (default) or
+        SR_BVH_BUILD_DEVICE (bit-identical result; no reference counterpart)."""
+        check(self._lib.sr_ctx_set_bvh_build(self.handle, int(where)))
+
+    def build_bvh(self, bounds: np.ndarray, cost_traverse: float, cost_intersect: float, bins: int,
+                  where: int = _abi.SR_BVH_BUILD_HOST):
+        """The reference's Bvh over arbitrary shape bounds (N, 6) = min xyz, max xyz (bvh.cs:58-75).
+        Returns (node bounds (M,6), node links (M,2) = child/shapeCount, item permutation (N,))."""
+        b = np.ascontiguousarray(bounds, dtype=np.float32).reshape(-1, 6)
+        n = b.shape[0]
+        nb = np.zeros((max(2 * n, 1), 6), np.float32)
+        nl = np.zeros((max(2 * n, 1), 2), np.int32)
+        it = np.zeros(n, np.int32)
+        cnt = C.c_uint32()
+        check(self._lib.sr_bvh_build(self.handle, ptr(b), n, float(cost_traverse), float(cost_intersect), int(bins),
+                                     int(where), ptr(nb), ptr(nl), ptr(it), C.byref(cnt)))
+        m = cnt.value
+        return nb[:m], nl[:m], it
+
     def close(self) -> None:
         if self.handle:
             self._lib.sr_ctx_destroy(self.handle)

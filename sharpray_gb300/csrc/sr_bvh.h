@@ -92,6 +92,7 @@ struct BvhHost {
     std::vector<BvhNodeHost> nodes;  // size max(2N, 1); nodes past node_count stay zero
     std::vector<int32_t> items;
     int32_t node_count = 0;
+    bool overflow = false;  // more than 2N nodes were needed (the reference throws); tree unusable
 };
 
 // Builds over `n` shapes with the given bounds.  Reference parameters: meshes use

@@ -130,6 +130,12 @@ struct Builder {
             int axis;
             float pos;
             if (!pick(out.nodes[w.node], axis, pos)) continue;
+            if (out.node_count + 2 > (int)out.nodes.size()) {
+                // a split whose partition sends every item to one side repeats until the depth
+                // cap and can outgrow the reference's 2N node array (bvh.cs would throw)
+                out.overflow = true;
+                return;
+            }
             int p = partition(out.nodes[w.node], axis, pos);
             BvhNodeHost& node = out.nodes[w.node];
             int count_a = p - node.child;

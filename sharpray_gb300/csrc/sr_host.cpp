@@ -12,6 +12,7 @@
 
 #include "../../include/sharpray.h"
 #include "sr_bvh.h"
+#include "sr_bvh_build.h"
 #include "sr_kernels.h"
 #include "sr_layout.h"
 #include "sr_wavefront.h"
@@ -99,6 +100,7 @@ struct MeshHost {
 struct SrContext {
     int device = 0;
     cudaStream_t stream = nullptr;
+    int32_t bvh_build = SR_BVH_BUILD_HOST;
     std::vector<std::unique_ptr<TextureHost>> textures;
     std::vector<std::unique_ptr<MeshHost>> meshes;
     // compose resources
@@ -290,6 +292,46 @@ SR_API int sr_ctx_destroy(SrContext* ctx) {
     return SR_OK;
 }
 
+// A BVH built where `where` says (device builds need a device context); bit-identical either way.
+static int build_tree(SrContext* ctx, const std::vector<Box>& bounds, float ct, float ci, int bins, int32_t where,
+                      BvhHost& out) {
+    if (where == SR_BVH_BUILD_DEVICE) {
+        if (ctx->device < 0) return fail(SR_ERR_STATE, "device BVH build on a host-only context");
+        SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+        SR_CUDA(build_bvh_device(bounds, ct, ci, bins, ctx->stream, out), "device BVH build");
+    } else {
+        out = build_bvh(bounds, ct, ci, bins);
+    }
+    if (out.overflow) return fail(SR_ERR_INVALID_ARG, "BVH needs more than 2N nodes (degenerate bounds)");
+    return SR_OK;
+}
+
+SR_API int sr_ctx_set_bvh_build(SrContext* ctx, int32_t where) {
+    if (!ctx) return fail(SR_ERR_INVALID_ARG, "context is NULL");
+    if (where != SR_BVH_BUILD_HOST && where != SR_BVH_BUILD_DEVICE) return fail(SR_ERR_INVALID_ARG, "bad BVH build %d", where);
+    if (where == SR_BVH_BUILD_DEVICE && ctx->device < 0) return fail(SR_ERR_STATE, "host-only context has no device");
+    ctx->bvh_build = where;
+    return SR_OK;
+}
+
+SR_API int sr_bvh_build(SrContext* ctx, const float* bounds, uint32_t count, float cost_traverse, float cost_intersect,
+                        int32_t bins, int32_t where, float* node_bounds, int32_t* node_links, int32_t* items,
+                        uint32_t* node_count) {
+    if (!ctx || (!bounds && count) || !node_bounds || !node_count) return fail(SR_ERR_INVALID_ARG, "sr_bvh_build: NULL argument");
+    if (bins < 2 || bins > 32) return fail(SR_ERR_INVALID_ARG, "sr_bvh_build: bins must be 2..32");
+    if (where != SR_BVH_BUILD_HOST && where != SR_BVH_BUILD_DEVICE) return fail(SR_ERR_INVALID_ARG, "bad BVH build %d", where);
+    std::vector<Box> b(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* p = bounds + 6 * (size_t)i;
+        b[i] = {{p[0], p[1], p[2]}, {p[3], p[4], p[5]}};
+    }
+    BvhHost t;
+    if (int rc = build_tree(ctx, b, cost_traverse, cost_intersect, bins, where, t)) return rc;
+    export_bvh(t, node_bounds, node_links, items);
+    *node_count = (uint32_t)t.node_count;
+    return SR_OK;
+}
+
 SR_API int sr_triangles_from_corners(const float* positions, const float* uvs, const float* normals, uint32_t count,
                                      int32_t smooth_normals, SrTriangle* out) {
     if ((!positions || !out) && count) return fail(SR_ERR_INVALID_ARG, "sr_triangles_from_corners: NULL array");
@@ -320,7 +362,7 @@ SR_API int sr_mesh_create(SrContext* ctx, const SrTriangle* triangles, uint32_t 
     m->tris.assign(triangles, triangles + count);
     std::vector<Box> bounds(count);
     for (uint32_t i = 0; i < count; ++i) bounds[i] = tri_bounds(m->tris[i]);
-    m->bvh = build_bvh(bounds, 1.0f, 0.5f, 8);  // mesh.cs:40-41
+    if (int rc = build_tree(ctx, bounds, 1.0f, 0.5f, 8, ctx->bvh_build, m->bvh)) return rc;  // mesh.cs:40-41
     m->bounds = m->bvh.node_count > 0 ? m->bvh.nodes[0].bounds : Box::inverted();
     ctx->meshes.push_back(std::move(m));
     *out_id = (int32_t)ctx->meshes.size() - 1;
@@ -432,7 +474,7 @@ SR_API int sr_scene_build(SrScene* s) {
     // Scene BVH over the objects (scene.cs:530-532).
     std::vector<Box> ob(s->objects.size());
     for (size_t i = 0; i < ob.size(); ++i) ob[i] = s->objects[i].bounds;
-    s->tlas = build_bvh(ob, 1.0f, 10.0f, 32);
+    if (int rc = build_tree(ctx, ob, 1.0f, 10.0f, 32, ctx->bvh_build, s->tlas)) return rc;
     if (ctx->device < 0) {  // host-only context: the BVH is inspectable, nothing is uploaded
         s->built = true;
         return SR_OK;

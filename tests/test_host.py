@@ -100,3 +100,21 @@ def test_c2_scene_bvh_reduced(host_ctx, oracle_mod):
     ours.build()
     ref = oracle_mod.instantiate(d)
     assert _same_bvh(ours.bvh(), ref.bvh())
+
+
+def test_bvh_build_entry_matches_mesh_build(host_ctx):
+    """sr_bvh_build over a mesh's triangle bounds gives the mesh's own tree (host build)."""
+    pos, uv = synth.uv_sphere(24, 24, amplitude=0.2, seed=7)
+    tris = Mesh.triangles_from_corners(host_ctx, pos, uv)
+    a, ab, ac = tris[:, 0:3], tris[:, 0:3] + tris[:, 3:6], tris[:, 0:3] + tris[:, 6:9]
+    b = np.concatenate([np.minimum(np.minimum(a, ab), ac), np.maximum(np.maximum(a, ab), ac)], 1)
+    assert _same_bvh(host_ctx.build_bvh(b, 1.0, 0.5, 8), Mesh(host_ctx, tris).bvh())
+
+
+def test_device_bvh_build_needs_a_device(host_ctx):
+    from sharpray_gb300 import _abi
+    from sharpray_gb300._abi import StateError
+    with pytest.raises(StateError):
+        host_ctx.set_bvh_build(_abi.SR_BVH_BUILD_DEVICE)
+    with pytest.raises(StateError):
+        host_ctx.build_bvh(np.zeros((4, 6), np.float32), 1.0, 0.5, 8, where=_abi.SR_BVH_BUILD_DEVICE)
