@@ -224,6 +224,7 @@ def run_ours(args):
     t_setup = time.perf_counter()
     desc = synth.config_c2(args.width, args.height, args.spp)
     ctx = Context(local)
+    ctx.set_bvh_build(_abi.SR_BVH_BUILD_DEVICE)  # bit-identical to the host build
     scene = desc.instantiate(ctx)
     scene.build()
     setup_s = time.perf_counter() - t_setup
@@ -259,6 +260,17 @@ def run_ours(args):
         if world > 1:
             torch.distributed.destroy_process_group()
         return
+
+    # BVH build of the largest mesh, host vs device (identical trees; setup, not in the metric)
+    from sharpray_gb300 import Mesh
+    tris = Mesh.triangles_from_corners(ctx, desc.meshes[0].positions, desc.meshes[0].uvs)
+    pa, pb, pc = tris[:, 0:3], tris[:, 0:3] + tris[:, 3:6], tris[:, 0:3] + tris[:, 6:9]
+    tb = np.concatenate([np.minimum(np.minimum(pa, pb), pc), np.maximum(np.maximum(pa, pb), pc)], 1)
+    bvh_s = {"triangles": int(len(tris))}
+    for where, label in ((_abi.SR_BVH_BUILD_HOST, "host"), (_abi.SR_BVH_BUILD_DEVICE, "device")):
+        t0 = time.perf_counter()
+        ctx.build_bvh(tb, 1.0, 0.5, 8, where=where)
+        bvh_s[label + "_s"] = round(time.perf_counter() - t0, 4)
 
     # work counters of one render (untimed) -> algorithmic bytes per launch
     scene.set_counting(True)
@@ -371,6 +383,7 @@ def run_ours(args):
                        "l2": "inputs larger than L2: scene ~%.0f MB + AOVs %.0f MB resident" % (
                            (desc.triangle_count * 192 + 2048 * 1024 * 24) / 1e6, n * 56 / 1e6),
                        "parallelism": "replicas" if world > 1 else "single", "setup_s": round(setup_s, 2),
+                       "bvh_build": bvh_s,
                        "wall_s_timed": round(wall, 3)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": H2D_PARAM_BYTES,
                     "d2h_bytes_per_step": d2h},
