@@ -80,6 +80,10 @@ typedef struct SrMaterial {
 
 enum { SR_SHAPE_MESH = 0, SR_SHAPE_SPHERE = 1, SR_SHAPE_AABOX = 2 };
 
+/* Texel encodings of image files (sr_texture_load): Texture.FromSrgb, FromLinear (Image.Load .tga),
+ * FromHdr (ImageHdr.Load .hdr) texture.cs:138-163. */
+enum { SR_TEXTURE_SRGB = 0, SR_TEXTURE_LINEAR = 1, SR_TEXTURE_HDR = 2 };
+
 /* Where BVHs are built (sr_ctx_set_bvh_build, sr_bvh_build). */
 enum { SR_BVH_BUILD_HOST = 0, SR_BVH_BUILD_DEVICE = 1 };
 
@@ -314,6 +318,33 @@ SR_API int sr_compose_device_static(SrContext* ctx, const SrAovs* device_aovs, u
 /* Tonemap of radiance + radiance_fog without denoise.  Replaces Compositor.Preview compose.cs:57-65. */
 SR_API int sr_preview(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height,
                       const SrComposeParams* params, uint8_t* host_rgb8);
+
+/* ---- asset ingest (host-side file parsing) ------------------------------------------------- */
+/* Image.Load (image.cs:214-273: uncompressed 24-bit TrueColor / 8-bit Grayscale .tga, rows top-down)
+ * or ImageHdr.Load (image.cs:307-382: Radiance .hdr, "-Y h +X w", new-style RLE or flat): sizes
+ * always; pixels (RGB8, or RGBE8 for .hdr: `channels` 3 or 4) when `pixels` is non-NULL and
+ * `capacity` suffices.  Parse failures return SR_ERR_IO with the reference's message. */
+SR_API int sr_image_load(const char* path, uint32_t* width, uint32_t* height, uint32_t* channels, uint8_t* pixels,
+                         uint64_t capacity);
+/* Texture.FromSrgb / FromLinear (Image.Load(path)) or FromHdr(ImageHdr.Load(path), max_luminance)
+ * (texture.cs:138-163) as a texture of the context (filter and tiling as sr_texture_create). */
+SR_API int sr_texture_load(SrContext* ctx, const char* path, int32_t encoding, float max_luminance, int32_t filter,
+                           float tiling_x, float tiling_y, int32_t* out_id);
+/* ObjLoader.Load(path, scene, config) obj.cs:139-259: parses the OBJ and its mtllib files (MTL
+ * textures via sr_texture_load rules), makes one mesh + object per `o`/`g`/`usemtl` group with the
+ * reference's names ("<file>_<name>" or "<file>_<n>"), triangle fans, V flipped, smooth normals
+ * when the file has no `vn` and smooth_normals is set.  `transform` NULL = identity; `material`
+ * NULL = Material(White, 1) for groups without an MTL material.  Unlike the reference, a parse error
+ * adds nothing to the scene. */
+SR_API int sr_obj_load(SrScene* scene, const char* path, const SrTransform* transform, const SrMaterial* material,
+                       int32_t smooth_normals, uint32_t* objects_added);
+/* Inspection (no reference counterpart): a texture's texels (3 floats each), a mesh's triangles,
+ * a scene object's description and name (objects from sr_obj_load are named). */
+SR_API int sr_texture_export(SrContext* ctx, int32_t texture, uint32_t* width, uint32_t* height, float* texels);
+SR_API int sr_mesh_export(SrContext* ctx, int32_t mesh, uint32_t* count, SrTriangle* triangles);
+SR_API int sr_scene_object_count(SrScene* scene, uint32_t* count);
+SR_API int sr_scene_object_info(SrScene* scene, uint32_t index, SrTransform* transform, SrMaterial* material,
+                                SrShape* shape, char* name, uint32_t name_capacity);
 
 #ifdef __cplusplus
 }

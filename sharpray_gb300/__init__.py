@@ -6,6 +6,6 @@ Compositor classes (see :mod:`sharpray_gb300.api`).
 """
 from .api import (AABox, Aovs, Compositor, Context, Fog, Material, Mesh, Object, Quat, Renderer, Scene,
                   SharpRayError, SkyProcedural, SkyTexture, Sphere, StateError, Texture, TextureFilter, Tonemapper,
-                  Transform, View, render_compose, render_params)
+                  Transform, View, load_image, mesh_triangles, render_compose, render_params)
 
 __version__ = "0.1.0"

@@ -24,6 +24,10 @@ SR_SHAPE_MESH = 0
 SR_SHAPE_SPHERE = 1
 SR_SHAPE_AABOX = 2
 
+SR_TEXTURE_SRGB = 0
+SR_TEXTURE_LINEAR = 1
+SR_TEXTURE_HDR = 2
+
 SR_BVH_BUILD_HOST = 0
 SR_BVH_BUILD_DEVICE = 1
 
@@ -119,6 +123,13 @@ PROTOTYPES = {
     "sr_ctx_set_bvh_build": (_I, [_P, C.c_int32]),
     "sr_bvh_build": (_I, [_P, _P, _U, _F, _F, C.c_int32, C.c_int32, _P, _P, _P, C.POINTER(_U)]),
     "sr_mesh_bvh_size": (_I, [_P, C.c_int32, C.POINTER(_U), C.POINTER(_U)]),
+    "sr_image_load": (_I, [C.c_char_p, C.POINTER(_U), C.POINTER(_U), C.POINTER(_U), _P, C.c_uint64]),
+    "sr_texture_load": (_I, [_P, C.c_char_p, C.c_int32, _F, C.c_int32, _F, _F, C.POINTER(C.c_int32)]),
+    "sr_obj_load": (_I, [_P, C.c_char_p, _P, _P, C.c_int32, C.POINTER(_U)]),
+    "sr_texture_export": (_I, [_P, C.c_int32, C.POINTER(_U), C.POINTER(_U), _P]),
+    "sr_mesh_export": (_I, [_P, C.c_int32, C.POINTER(_U), _P]),
+    "sr_scene_object_count": (_I, [_P, C.POINTER(_U)]),
+    "sr_scene_object_info": (_I, [_P, _U, _P, _P, _P, C.c_char_p, _U]),
     "sr_mesh_bvh_export": (_I, [_P, C.c_int32, _P, _P, _P]),
     "sr_scene_create": (_I, [_P, C.POINTER(_P)]),
     "sr_scene_destroy": (_I, [_P]),

@@ -38,12 +38,27 @@ from ._abi import (SharpRayError, SrAovs, SrComposeParams, SrFog, SrMaterial, Sr
 __all__ = [
     "Context", "Texture", "TextureFilter", "Mesh", "Sphere", "AABox", "Material", "Quat", "Transform", "Object",
     "SkyTexture", "SkyProcedural", "Fog", "Scene", "View", "Renderer", "Compositor", "Tonemapper",
-    "SharpRayError", "StateError",
+    "SharpRayError", "StateError", "load_image", "mesh_triangles",
 ]
 
 
 def _f32(v) -> np.float32:
     return np.float32(v)
+
+
+_SRGB_TABLE = None
+
+
+def _srgb_table() -> np.ndarray:
+    global _SRGB_TABLE
+    if _SRGB_TABLE is None:
+        import ctypes.util
+        libm = C.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+        libm.powf.restype, libm.powf.argtypes = C.c_float, [C.c_float, C.c_float]
+        g = float(np.float32(2.233333333))
+        _SRGB_TABLE = np.array([libm.powf(float(np.float32(i) / np.float32(255.0)), g) for i in range(256)],
+                               np.float32)
+    return _SRGB_TABLE
 
 
 class Context:
@@ -109,11 +124,36 @@ class Texture:
                                          self.tiling[0], self.tiling[1], C.byref(out)))
         self.id = out.value
 
+    @classmethod
+    def load(cls, ctx: Context, path, encoding: int = _abi.SR_TEXTURE_SRGB,
+             max_luminance: float = float(np.finfo(np.float32).max), filter: TextureFilter = TextureFilter.Bilinear,
+             tiling: Sequence[float] = (1.0, 1.0)) -> "Texture":
+        """Texture.FromSrgb/FromLinear(Image.Load(path)) for .tga or FromHdr(ImageHdr.Load(path)) for
+        .hdr (texture.cs:138-163), parsed by the library."""
+        out = C.c_int32()
+        check(ctx._lib.sr_texture_load(ctx.handle, str(path).encode(), int(encoding), float(max_luminance), int(filter),
+                                       float(tiling[0]), float(tiling[1]), C.byref(out)))
+        return cls.from_id(ctx, out.value, filter, tiling)
+
+    @classmethod
+    def from_id(cls, ctx: Context, tid: int, filter: TextureFilter = TextureFilter.Bilinear,
+                tiling: Sequence[float] = (1.0, 1.0)) -> "Texture":
+        """A texture the library created (e.g. from an MTL map), with its texels read back."""
+        w, h = C.c_uint32(), C.c_uint32()
+        check(ctx._lib.sr_texture_export(ctx.handle, int(tid), C.byref(w), C.byref(h), None))
+        t = np.zeros((h.value, w.value, 3), np.float32)
+        check(ctx._lib.sr_texture_export(ctx.handle, int(tid), C.byref(w), C.byref(h), ptr(t)))
+        obj = cls.__new__(cls)
+        obj.ctx, obj.texels, obj.height, obj.width = ctx, t, h.value, w.value
+        obj.filter, obj.tiling, obj.id = TextureFilter(filter), (float(tiling[0]), float(tiling[1])), int(tid)
+        return obj
+
     # Color.FromPixel(Pixel) math.cs:184-191: sRGB decode pow(x/255, 2.2333).
     @staticmethod
     def srgb_to_linear(pixels: np.ndarray) -> np.ndarray:
-        p = np.asarray(pixels)[..., :3].astype(np.float32) / np.float32(255.0)
-        return np.power(p, np.float32(2.233333333), dtype=np.float32)
+        """MathF.Pow(c / 255f, 2.233333333f) per channel: the C runtime's powf, as the library's
+        file loader (sr_texture_load) uses it."""
+        return _srgb_table()[np.asarray(pixels)[..., :3]]
 
     @classmethod
     def from_srgb(cls, ctx: Context, pixels: np.ndarray, **kw) -> "Texture":
@@ -385,6 +425,28 @@ class Scene:
         check(self._lib.sr_scene_build(self.handle))
         self.built = True
 
+    def load_obj(self, path, transform: Optional["Transform"] = None, material: Optional["Material"] = None,
+                 smooth_normals: bool = True) -> int:
+        """ObjLoader.Load(path, scene, config) obj.cs:139-259: adds one object per OBJ group; returns
+        the number added."""
+        t = C.byref(transform.to_c()) if transform is not None else None
+        m = C.byref(material.to_c()) if material is not None else None
+        n = C.c_uint32()
+        check(self._lib.sr_obj_load(self.handle, str(path).encode(), t, m, int(smooth_normals), C.byref(n)))
+        return n.value
+
+    def object_count(self) -> int:
+        n = C.c_uint32()
+        check(self._lib.sr_scene_object_count(self.handle, C.byref(n)))
+        return n.value
+
+    def object_info(self, index: int) -> dict:
+        """Name, transform, material and shape of object `index` as the library holds them."""
+        t, m, sh = _abi.SrTransform(), _abi.SrMaterial(), _abi.SrShape()
+        name = C.create_string_buffer(512)
+        check(self._lib.sr_scene_object_info(self.handle, int(index), C.byref(t), C.byref(m), C.byref(sh), name, 512))
+        return {"name": name.value.decode(), "transform": t, "material": m, "shape": sh}
+
     def bvh(self):
         nn, ni = C.c_uint32(), C.c_uint32()
         check(self._lib.sr_scene_bvh_size(self.handle, C.byref(nn), C.byref(ni)))
@@ -573,3 +635,22 @@ def render_compose(scene: Scene, view: View, width: int, height: int, block_size
     a = C.byref(aovs.to_c()) if aovs is not None else None
     check(scene._lib.sr_render_compose(scene.handle, C.byref(v), C.byref(p), C.byref(cp), a, ptr(image)))
     return image, aovs
+
+
+def load_image(path) -> np.ndarray:
+    """Image.Load (.tga: RGB8) or ImageHdr.Load (.hdr: RGBE8) as parsed by the library; (H, W, C)."""
+    lib = _abi.load()
+    w, h, ch = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    check(lib.sr_image_load(str(path).encode(), C.byref(w), C.byref(h), C.byref(ch), None, 0))
+    out = np.zeros((h.value, w.value, ch.value), np.uint8)
+    check(lib.sr_image_load(str(path).encode(), C.byref(w), C.byref(h), C.byref(ch), ptr(out), out.nbytes))
+    return out
+
+
+def mesh_triangles(ctx: Context, mesh_id: int) -> np.ndarray:
+    """The SrTriangles (N, 36) of a library mesh."""
+    n = C.c_uint32()
+    check(ctx._lib.sr_mesh_export(ctx.handle, int(mesh_id), C.byref(n), None))
+    out = np.zeros((n.value, _abi.TRIANGLE_FLOATS), np.float32)
+    check(ctx._lib.sr_mesh_export(ctx.handle, int(mesh_id), C.byref(n), ptr(out)))
+    return out

@@ -20,7 +20,7 @@ LIB = PKG / "libsharpray_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["sr_render.cu", "sr_wavefront.cu", "sr_compose.cu", "sr_bvh_build.cu"]
-HOST_SOURCES = ["sr_host.cpp", "sr_geometry.cpp"]
+HOST_SOURCES = ["sr_host.cpp", "sr_geometry.cpp", "sr_ingest.cpp"]
 
 
 def cuda_home() -> Path:

@@ -103,6 +103,12 @@ BvhHost build_bvh(const std::vector<Box>& shape_bounds, float cost_traverse, flo
 // sr_triangles_from_corners in sharpray.h.  `out` is an array of SrTriangle.
 void triangles_from_corners(const float* positions, const float* uvs, const float* normals, uint32_t count,
                             bool smooth_normals, void* out);
+// Mesh.ComputeSmoothNormals mesh.cs:99-123 over `count` SrTriangles in place.
+void compute_smooth_normals(void* tris, uint32_t count);
+// One SrTriangle from its corners (Triangle ctors math.cs:1510-1531); `normals` NULL gives the face
+// normal at every corner.
+void make_triangle_corners(const float* pa, const float* pb, const float* pc, const float* normals, const float* uva,
+                           const float* uvb, const float* uvc, void* out);
 
 }  // namespace host
 }  // namespace sr

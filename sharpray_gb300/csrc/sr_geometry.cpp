@@ -206,6 +206,13 @@ void make_triangle(F3 pa, F3 pb, F3 pc, const F3* normals, const float* uva, con
 
 }  // namespace
 
+void make_triangle_corners(const float* pa, const float* pb, const float* pc, const float* normals, const float* uva,
+                           const float* uvb, const float* uvc, void* out) {
+    F3 ns[3];
+    if (normals) ns[0] = get3(normals), ns[1] = get3(normals + 3), ns[2] = get3(normals + 6);
+    make_triangle(get3(pa), get3(pb), get3(pc), normals ? ns : nullptr, uva, uvb, uvc, *(SrTriangle*)out);
+}
+
 BvhHost build_bvh(const std::vector<Box>& shape_bounds, float cost_traverse, float cost_intersect, int bins) {
     Builder b(shape_bounds, cost_traverse, cost_intersect, bins);
     b.run();
@@ -229,7 +236,12 @@ void triangles_from_corners(const float* positions, const float* uvs, const floa
         make_triangle(get3(p), get3(p + 3), get3(p + 6), normals ? ns : nullptr, ua, ub, uc, out[i]);
     }
     if (!smooth_normals || normals || count == 0) return;
+    compute_smooth_normals(out, count);
+}
 
+void compute_smooth_normals(void* tris_v, uint32_t count) {
+    SrTriangle* out = (SrTriangle*)tris_v;
+    if (count == 0) return;
     // Mesh.ComputeSmoothNormals mesh.cs:99-123.  Corner positions are grouped by the quantised key
     // of Vec3Comparer(1e-6) (math.cs:396-403); each group's area-weighted face normals are summed in
     // corner order (triangle order, then A, B, C), which is the order the reference's dictionary

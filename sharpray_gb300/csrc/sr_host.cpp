@@ -13,6 +13,7 @@
 #include "../../include/sharpray.h"
 #include "sr_bvh.h"
 #include "sr_bvh_build.h"
+#include "sr_ingest.h"
 #include "sr_kernels.h"
 #include "sr_layout.h"
 #include "sr_wavefront.h"
@@ -118,6 +119,7 @@ struct SrScene {
         Box bounds;
     };
     std::vector<Obj> objects;
+    std::vector<std::string> object_names;  // names of objects from sr_obj_load (others empty)
     int sky_kind = -1;
     int32_t sky_texture = -1;
     float sky_multiplier = 1, sky_yaw = 0;
@@ -1187,3 +1189,151 @@ SR_API int sr_preview(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, c
 }
 
 }  // extern "C"
+
+// ---- asset ingest (sr_ingest.cpp) ------------------------------------------------------------------
+
+SR_API int sr_image_load(const char* path, uint32_t* width, uint32_t* height, uint32_t* channels, uint8_t* pixels,
+                         uint64_t capacity) {
+    if (!path || !width || !height || !channels) return fail(SR_ERR_INVALID_ARG, "sr_image_load: NULL argument");
+    try {
+        std::string p(path);
+        std::vector<uint8_t> data;
+        uint32_t w = 0, h = 0, ch = 3;
+        size_t dot = p.find_last_of('.');
+        if (dot != std::string::npos && p.substr(dot) == ".hdr") {
+            load_hdr(p, w, h, data);
+            ch = 4;
+        } else {
+            load_image(p, w, h, data);
+        }
+        *width = w, *height = h, *channels = ch;
+        if (pixels) {
+            if (capacity < data.size()) return fail(SR_ERR_INVALID_ARG, "sr_image_load: buffer of %llu bytes, need %zu",
+                                                    (unsigned long long)capacity, data.size());
+            std::memcpy(pixels, data.data(), data.size());
+        }
+    } catch (const IngestError& e) {
+        return fail(SR_ERR_IO, "%s", e.what());
+    }
+    return SR_OK;
+}
+
+static int texture_from_file(SrContext* ctx, const std::string& path, int32_t encoding, float max_luminance,
+                             int32_t filter, float tiling_x, float tiling_y, int32_t* out_id) {
+    std::vector<uint8_t> data;
+    uint32_t w = 0, h = 0;
+    std::vector<float> texels;
+    if (encoding == SR_TEXTURE_HDR) {
+        load_hdr(path, w, h, data);
+        texels.resize((size_t)w * h * 3);
+        rgbe_to_texels(data.data(), (size_t)w * h, max_luminance, texels.data());
+    } else {
+        load_image(path, w, h, data);
+        texels.resize((size_t)w * h * 3);
+        rgb8_to_texels(data.data(), (size_t)w * h, encoding == SR_TEXTURE_SRGB, texels.data());
+    }
+    return sr_texture_create(ctx, texels.data(), w, h, filter, tiling_x, tiling_y, out_id);
+}
+
+SR_API int sr_texture_load(SrContext* ctx, const char* path, int32_t encoding, float max_luminance, int32_t filter,
+                           float tiling_x, float tiling_y, int32_t* out_id) {
+    if (!ctx || !path || !out_id) return fail(SR_ERR_INVALID_ARG, "sr_texture_load: NULL argument");
+    if (encoding != SR_TEXTURE_SRGB && encoding != SR_TEXTURE_LINEAR && encoding != SR_TEXTURE_HDR)
+        return fail(SR_ERR_INVALID_ARG, "sr_texture_load: bad encoding %d", encoding);
+    try {
+        return texture_from_file(ctx, path, encoding, max_luminance, filter, tiling_x, tiling_y, out_id);
+    } catch (const IngestError& e) {
+        return fail(SR_ERR_IO, "%s", e.what());
+    }
+}
+
+SR_API int sr_obj_load(SrScene* s, const char* path, const SrTransform* transform, const SrMaterial* material,
+                       int32_t smooth_normals, uint32_t* objects_added) {
+    if (!s || !path) return fail(SR_ERR_INVALID_ARG, "sr_obj_load: NULL argument");
+    if (s->built) return fail(SR_ERR_STATE, "Scene already built");
+    SrContext* ctx = s->ctx;
+    const SrTransform identity{{0, 0, 0}, {0, 0, 0, 1}, {1, 1, 1}};
+    const SrMaterial fallback{{1, 1, 1}, 1.0f, 0.0f, 0.0f, 1.5f, {0, 0, 0}, -1, -1, -1, -1};  // Material(White, 1)
+    const SrTransform& tr = transform ? *transform : identity;
+    ObjResult r;
+    std::vector<SrMaterial> mats;  // per object
+    try {
+        r = parse_obj(path, smooth_normals != 0);
+        std::map<const ObjImage*, int32_t> uploaded;  // one texture per decoded map
+        for (const ObjObject& o : r.objects) {
+            const ObjMaterial& m = o.material;
+            SrMaterial sm = material ? *material : fallback;
+            if (o.has_material) {
+                sm = SrMaterial{{m.albedo[0], m.albedo[1], m.albedo[2]}, m.roughness, m.metallic, m.transparency, m.ior,
+                                {m.radiance[0], m.radiance[1], m.radiance[2]}, -1, -1, -1, -1};
+                const ObjImagePtr* maps[4] = {&m.color_map, &m.roughness_map, &m.metallic_map, &m.normal_map};
+                int32_t* ids[4] = {&sm.color_texture, &sm.roughness_texture, &sm.metallic_texture, &sm.normal_texture};
+                for (int k = 0; k < 4; ++k) {
+                    const ObjImage* img = maps[k]->get();
+                    if (!img) continue;
+                    auto it = uploaded.find(img);
+                    if (it == uploaded.end()) {
+                        int32_t id = -1;  // Texture defaults: bilinear, tiling (1, 1) (texture.cs:17-30)
+                        if (int rc = sr_texture_create(ctx, img->texels.data(), img->width, img->height, 0, 1.0f, 1.0f, &id))
+                            return rc;
+                        it = uploaded.emplace(img, id).first;
+                    }
+                    *ids[k] = it->second;
+                }
+            }
+            mats.push_back(sm);
+        }
+    } catch (const IngestError& e) {
+        return fail(SR_ERR_IO, "%s", e.what());
+    }
+    uint32_t added = 0;
+    for (const ObjObject& o : r.objects) {
+        int32_t mesh = -1, index = -1;
+        if (int rc = sr_mesh_create(ctx, o.triangles.data(), (uint32_t)o.triangles.size(), &mesh)) return rc;
+        SrShape shape{SR_SHAPE_MESH, mesh, {0, 0, 0, 0, 0, 0}};
+        if (int rc = sr_scene_add_object(s, &tr, &mats[added], &shape, &index)) return rc;
+        s->object_names.resize(s->objects.size());
+        s->object_names[index] = o.name;
+        ++added;
+    }
+    if (objects_added) *objects_added = added;
+    return SR_OK;
+}
+
+SR_API int sr_texture_export(SrContext* ctx, int32_t id, uint32_t* width, uint32_t* height, float* texels) {
+    if (!ctx || !valid_texture(ctx, id) || id < 0) return fail(SR_ERR_INVALID_ARG, "bad texture id");
+    const TextureHost& t = *ctx->textures[id];
+    if (width) *width = t.width;
+    if (height) *height = t.height;
+    if (texels) std::memcpy(texels, t.texels.data(), t.texels.size() * sizeof(float));
+    return SR_OK;
+}
+
+SR_API int sr_mesh_export(SrContext* ctx, int32_t mesh, uint32_t* count, SrTriangle* triangles) {
+    if (!ctx || mesh < 0 || mesh >= (int32_t)ctx->meshes.size()) return fail(SR_ERR_INVALID_ARG, "bad mesh id");
+    const MeshHost& m = *ctx->meshes[mesh];
+    if (count) *count = (uint32_t)m.tris.size();
+    if (triangles) std::memcpy(triangles, m.tris.data(), m.tris.size() * sizeof(SrTriangle));
+    return SR_OK;
+}
+
+SR_API int sr_scene_object_info(SrScene* s, uint32_t index, SrTransform* transform, SrMaterial* material,
+                                SrShape* shape, char* name, uint32_t name_capacity) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    if (index >= s->objects.size()) return fail(SR_ERR_INVALID_ARG, "object index %u of %zu", index, s->objects.size());
+    const SrScene::Obj& o = s->objects[index];
+    if (transform) *transform = o.tr;
+    if (material) *material = o.mat;
+    if (shape) *shape = o.shape;
+    if (name && name_capacity) {
+        std::string n = index < s->object_names.size() ? s->object_names[index] : std::string();
+        std::snprintf(name, name_capacity, "%s", n.c_str());
+    }
+    return SR_OK;
+}
+
+SR_API int sr_scene_object_count(SrScene* s, uint32_t* count) {
+    if (!s || !count) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    *count = (uint32_t)s->objects.size();
+    return SR_OK;
+}
