@@ -346,6 +346,65 @@ SR_API int sr_scene_object_count(SrScene* scene, uint32_t* count);
 SR_API int sr_scene_object_info(SrScene* scene, uint32_t index, SrTransform* transform, SrMaterial* material,
                                 SrShape* shape, char* name, uint32_t name_capacity);
 
+/* ---- AOV images, debug overlay, image files ------------------------------------------------ */
+/* AOV visualisations of program.cs:211-263 (the normal.bmp / depth.bmp / variance.bmp /
+ * samples.bmp / uv.bmp dumps) as RGB8: normal (n * 0.5 + 0.5) * 255; depth clamp(d / 25) * 255 grey,
+ * red where infinite; variance clamp(v / (2 * variance_threshold)) * 255 grey; samples
+ * log2(s / min) / log2(max / min) * 255 grey; uv |uv mod 1| * 255 in red and green.  Float to byte
+ * conversions follow .NET 8: truncation, low 8 bits, 0 for NaN and values outside the int range. */
+enum { SR_AOV_NORMAL = 0, SR_AOV_DEPTH = 1, SR_AOV_VARIANCE = 2, SR_AOV_SAMPLES = 3, SR_AOV_UV = 4 };
+typedef struct SrAovImageParams {
+    float variance_threshold; /* SR_AOV_VARIANCE */
+    uint32_t min_samples;     /* SR_AOV_SAMPLES */
+    uint32_t max_samples;
+} SrAovImageParams;
+SR_API int sr_aov_image(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height, int32_t kind,
+                        const SrAovImageParams* params, uint8_t* host_rgb8);
+SR_API int sr_aov_image_device(SrContext* ctx, const SrAovs* device_aovs, uint32_t width, uint32_t height,
+                               int32_t kind, const SrAovImageParams* params, uint8_t* device_rgb8, void* stream);
+
+/* Overlay.Draw (overlay.cs:54-96): world-space lines (Bresenham, perspective-correct depth test
+ * against the render's depth with a relative bias, overlay.cs:102-149) and text (8x8 bitmap font,
+ * '\n' separated lines, top-left or centred, overlay.cs:151-196) drawn into an RGB8 image.  The
+ * reference's draw order holds: every line, then every world-space text, then every screen-space
+ * text, each in array order; later entries overwrite earlier ones.  Text is one byte per character;
+ * characters outside the font's range are skipped but count for centring.  The font is the
+ * caller's: `glyphs` holds 8 bytes per character from first_char to last_char, one byte per row
+ * top to bottom, the most significant bit leftmost (the reference's Font table layout; no font
+ * ships with the library).  Lines whose projected end points lie outside the int range or that
+ * span more than 2^24 pixels fail with SR_ERR_INVALID_ARG. */
+enum { SR_ALIGN_TOP_LEFT = 0, SR_ALIGN_CENTER = 1 };
+typedef struct SrOverlayLine {
+    float a[3], b[3];
+    float color[3];     /* linear colour, encoded with Color.ToPixel */
+    int32_t depth_test; /* 1: hidden behind nearer surfaces of the depth plane */
+    float depth_bias;   /* fraction of the depth pulled towards the camera (reference default 0.005) */
+} SrOverlayLine;
+typedef struct SrOverlayText {
+    const char* text;      /* NUL-terminated */
+    int32_t in_world;      /* 1: world_pos projected through the view; 0: screen_pos in pixels */
+    float world_pos[3];
+    int32_t screen_pos[2];
+    float color[3];
+    int32_t align;         /* SR_ALIGN_*; the reference defaults to centred in world, top-left on screen */
+} SrOverlayText;
+typedef struct SrFont {
+    const uint8_t* glyphs;
+    int32_t first_char, last_char;
+} SrFont;
+SR_API int sr_overlay_draw(SrContext* ctx, uint8_t* host_rgb8, uint32_t width, uint32_t height, const SrView* view,
+                           const float* host_depth, const SrOverlayLine* lines, uint32_t line_count,
+                           const SrOverlayText* texts, uint32_t text_count, const SrFont* font);
+/* Same on a device image and depth plane (depth may be NULL: no depth test) on `stream`. */
+SR_API int sr_overlay_draw_device(SrContext* ctx, uint8_t* device_rgb8, uint32_t width, uint32_t height,
+                                  const SrView* view, const float* device_depth, const SrOverlayLine* lines,
+                                  uint32_t line_count, const SrOverlayText* texts, uint32_t text_count,
+                                  const SrFont* font, void* stream);
+/* Image.Save (image.cs:88-212): RGB8 rows top-down written as .tga (24-bit, top-left origin), .ppm
+ * (P6) or .bmp (24-bit, top-down, rows padded to 4 bytes) by the path's extension; other
+ * extensions or write failures return SR_ERR_IO. */
+SR_API int sr_image_save(const char* path, uint32_t width, uint32_t height, const uint8_t* rgb8);
+
 #ifdef __cplusplus
 }
 #endif

@@ -561,3 +561,28 @@ def parse_obj(path: str, smooth_normals: bool = True) -> list:
     if not objects:
         raise IngestError("OBJ: no objects found")
     return objects
+
+
+# ---- image files (Image.WriteTga / WritePpm / WriteBmp image.cs:95-196) -------------------------
+
+def image_bytes(ext: str, rgb: np.ndarray) -> bytes:
+    """The bytes Image.Save writes for an (H, W, 3) RGB8 image and an extension."""
+    h, w = rgb.shape[:2]
+    if ext == ".tga":
+        head = bytes([0, 0, 2]) + bytes(9) + (w & 0xFFFF).to_bytes(2, "little") + (h & 0xFFFF).to_bytes(2, "little")
+        return head + bytes([24, 0x20]) + rgb[:, :, ::-1].tobytes()
+    if ext == ".ppm":
+        return f"P6\n{w} {h}\n255\n".encode("ascii") + rgb.tobytes()
+    if ext == ".bmp":
+        stride = (w * 3 + 3) & ~3
+        size = stride * h
+        out = bytearray(b"BM")
+        for v in (14 + 40 + size, 0, 54, 40, w, (-h) & 0xFFFFFFFF):
+            out += int(v).to_bytes(4, "little")
+        out += (1).to_bytes(2, "little") + (24).to_bytes(2, "little")
+        out += (0).to_bytes(4, "little") + size.to_bytes(4, "little") + bytes(16)
+        pad = bytes(stride - w * 3)
+        for y in range(h):
+            out += rgb[y, :, ::-1].tobytes() + pad
+        return bytes(out)
+    raise IngestError(f"Image: Unsupported file format '{ext}'")

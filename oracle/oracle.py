@@ -22,8 +22,9 @@ SRC = HERE / "sr_oracle.cpp"
 LIB = HERE / "liboracle.so"
 
 # Same POD layouts as the C ABI (imported only for the struct definitions).
-from sharpray_gb300._abi import (SR_COUNTER_COUNT, COUNTER_NAMES, TRIANGLE_FLOATS, SrAovs, SrComposeParams, SrFog,
-                                 SrMaterial, SrRenderParams, SrShape, SrSkyProcedural, SrTransform, SrView)
+from sharpray_gb300._abi import (SR_COUNTER_COUNT, COUNTER_NAMES, TRIANGLE_FLOATS, SrAovImageParams, SrAovs,
+                                 SrComposeParams, SrFog, SrFont, SrMaterial, SrRenderParams, SrShape, SrSkyProcedural,
+                                 SrTransform, SrView)
 
 CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread"]
 
@@ -71,6 +72,8 @@ def lib():
             "oracle_compose": (None, [C.POINTER(SrAovs), U, U, C.POINTER(SrComposeParams), P, C.c_int32]),
             "oracle_preview": (None, [C.POINTER(SrAovs), U, U, C.POINTER(SrComposeParams), P]),
             "oracle_denoise": (None, [C.POINTER(SrAovs), U, U, C.POINTER(SrComposeParams), P, C.c_int32]),
+            "oracle_aov_image": (None, [C.POINTER(SrAovs), U, U, C.c_int32, C.POINTER(SrAovImageParams), P]),
+            "oracle_overlay_draw": (I, [P, U, U, C.POINTER(SrView), P, P, U, P, U, C.POINTER(SrFont)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -198,6 +201,25 @@ def preview(aovs, params: SrComposeParams) -> np.ndarray:
     out = np.zeros((aovs.height, aovs.width, 3), np.uint8)
     c = aovs.to_c()
     lib().oracle_preview(C.byref(c), aovs.width, aovs.height, C.byref(params), _p(out))
+    return out
+
+
+def aov_image(aovs, kind: int, params: SrAovImageParams) -> np.ndarray:
+    """program.cs:211-263 AOV dump of one kind as (H, W, 3) RGB8."""
+    out = np.zeros((aovs.height, aovs.width, 3), np.uint8)
+    lib().oracle_aov_image(C.byref(aovs.to_c()), aovs.width, aovs.height, int(kind), C.byref(params), _p(out))
+    return out
+
+
+def overlay_draw(image: np.ndarray, view: SrView, depth, lines, texts, font: SrFont) -> np.ndarray:
+    """Overlay.Draw on a copy of `image` ((H, W, 3) uint8); lines / texts are ctypes arrays."""
+    out = np.ascontiguousarray(image, np.uint8).copy()
+    h, w = out.shape[:2]
+    d = None if depth is None else np.ascontiguousarray(depth, np.float32)
+    rc = lib().oracle_overlay_draw(_p(out), w, h, C.byref(view), _p(d), lines, len(lines) if lines else 0, texts,
+                                   len(texts) if texts else 0, C.byref(font))
+    if rc:
+        raise ValueError("overlay line end point outside the int range")
     return out
 
 

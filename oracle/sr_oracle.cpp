@@ -16,6 +16,7 @@
 //   Scene.Sample + helpers        scene.cs:576-810
 //   Renderer.Render + scheduling  renderer.cs:107-237
 //   Compositor                    compose.cs:57-266
+//   AOV dumps, Overlay            program.cs:211-263, overlay.cs:54-196, math.cs:261,1638-1663
 // in the reference's exact floating-point operation order: C# evaluates left to right, RyuJIT
 // never contracts a*b+c into an FMA (this file must be compiled with -ffp-contract=off), and
 // MathF.Min/Max follow IEEE 754:2019 minimum/maximum (NaN-propagating, -0 < +0), restated in
@@ -1965,6 +1966,192 @@ void oracle_denoise(const SrAovs* a, uint32_t w, uint32_t h, const SrComposePara
             o[0] = m.r, o[1] = m.g, o[2] = m.b;
         }
     });
+}
+
+// ---- AOV dumps (program.cs:211-263) and the debug overlay (overlay.cs:54-196) ------------------------
+
+// (byte)f as .NET 8 on x64 compiles it: cvttss2si to int (0x80000000 for NaN and out-of-range
+// values), then the low byte.
+static uint8_t dotnet_byte(float f) {
+    int32_t i = (f >= -2147483648.0f && f < 2147483648.0f) ? (int32_t)f : INT32_MIN;
+    return (uint8_t)(uint32_t)i;
+}
+
+void oracle_aov_image(const SrAovs* a, uint32_t w, uint32_t h, int32_t kind, const SrAovImageParams* p, uint8_t* rgb) {
+    const uint32_t n = w * h;
+    for (uint32_t i = 0; i != n; ++i) {
+        uint8_t* px = rgb + 3 * (size_t)i;
+        if (kind == SR_AOV_NORMAL) {
+            px[0] = dotnet_byte((a->normals[3 * i] * 0.5f + 0.5f) * 255.0f);
+            px[1] = dotnet_byte((a->normals[3 * i + 1] * 0.5f + 0.5f) * 255.0f);
+            px[2] = dotnet_byte((a->normals[3 * i + 2] * 0.5f + 0.5f) * 255.0f);
+        } else if (kind == SR_AOV_DEPTH) {
+            const float depth_max_inv = 1.0f / 25.0f;
+            float depth = a->depth[i];
+            if (std::isinf(depth)) {
+                px[0] = 255, px[1] = 0, px[2] = 0;  // Pixel.Red
+            } else {
+                px[0] = px[1] = px[2] = dotnet_byte(net_clamp(depth * depth_max_inv, 0.0f, 1.0f) * 255.0f);
+            }
+        } else if (kind == SR_AOV_VARIANCE) {
+            float t = a->variance[i] / (p->variance_threshold * 2.0f);
+            px[0] = px[1] = px[2] = dotnet_byte(net_clamp(t, 0.0f, 1.0f) * 255.0f);
+        } else if (kind == SR_AOV_SAMPLES) {
+            float log_range = std::log2(p->max_samples / (float)p->min_samples);
+            float frac = std::log2(a->samples[i] / (float)p->min_samples) / log_range;
+            px[0] = px[1] = px[2] = dotnet_byte(frac * 255.0f);
+        } else {
+            px[0] = dotnet_byte(std::fabs(std::fmod(a->uv[2 * i], 1.0f)) * 255.0f);
+            px[1] = dotnet_byte(std::fabs(std::fmod(a->uv[2 * i + 1], 1.0f)) * 255.0f);
+            px[2] = 0;
+        }
+    }
+}
+
+// View.Project math.cs:1638-1663.
+static bool oracle_view_project(const SrView& v, V3 world, float aspect, float& sx, float& sy, float& depth) {
+    Quat rot{v.transform.rot[0], v.transform.rot[1], v.transform.rot[2], v.transform.rot[3]};
+    V3 pos{v.transform.pos[0], v.transform.pos[1], v.transform.pos[2]};
+    V3 scale{v.transform.scale[0], v.transform.scale[1], v.transform.scale[2]};
+    V3 local = quat_inverse(rot) * (world - pos) / scale;
+    if (local.z <= v.near_plane) return false;
+    float tan_half_hor, tan_half_ver;
+    if (aspect >= 1.0f) {
+        tan_half_hor = std::tan(v.fov * 0.5f);
+        tan_half_ver = tan_half_hor / aspect;
+    } else {
+        tan_half_ver = std::tan(v.fov * 0.5f);
+        tan_half_hor = tan_half_ver * aspect;
+    }
+    V3 local_from_near{local.x, local.y, local.z - v.near_plane};
+    float ndc_x = (local_from_near.x / local_from_near.z) / tan_half_hor;
+    float ndc_y = (local_from_near.y / local_from_near.z) / tan_half_ver;
+    sx = (ndc_x + 1.0f) * 0.5f;
+    sy = (1.0f - ndc_y) * 0.5f;
+    depth = magnitude(local_from_near);
+    return true;
+}
+
+// Vec2.RoundToInt math.cs:261 (MathF.Round is round-half-even); false when (int) would overflow.
+static bool oracle_round_to_int(float v, int32_t& out) {
+    float r = std::rint(v);
+    if (!(r >= -2147483648.0f && r < 2147483648.0f)) return false;
+    out = (int32_t)r;
+    return true;
+}
+
+static void oracle_put_pixel(uint8_t* rgb, uint32_t w, uint32_t h, int32_t x, int32_t y, const uint8_t* value,
+                             const float* depth, float line_depth, bool test) {
+    if ((uint32_t)x >= w || (uint32_t)y >= h) return;  // Overlay.PixelIndex
+    size_t index = (size_t)y * w + x;
+    if (test && !(line_depth <= depth[index])) return;
+    std::memcpy(rgb + 3 * index, value, 3);
+}
+
+// RasterizeLine overlay.cs:102-149.
+static void oracle_rasterize_line(uint8_t* rgb, uint32_t w, uint32_t h, const float* depth, int32_t sx, int32_t sy,
+                                  int32_t ex, int32_t ey, float depth_a, float depth_b, const uint8_t* value) {
+    float depth_a_inv = 1.0f / depth_a;
+    float depth_b_inv = 1.0f / depth_b;
+    int span_x = std::abs(ex - sx);
+    int span_y = -std::abs(ey - sy);
+    int step_x = sx < ex ? 1 : -1;
+    int step_y = sy < ey ? 1 : -1;
+    int error = span_x + span_y;
+    int total_steps = std::max(span_x, -span_y);
+    int step = -1;
+    int cx = sx, cy = sy;
+    while (true) {
+        ++step;
+        float line_frac = total_steps > 0 ? (float)step / total_steps : 0.0f;
+        float line_depth = 1.0f / (depth_a_inv * (1.0f - line_frac) + depth_b_inv * line_frac);  // float.Lerp
+        oracle_put_pixel(rgb, w, h, cx, cy, value, depth, line_depth, depth != nullptr);
+        if (cx == ex && cy == ey) break;
+        int err2 = 2 * error;
+        if (err2 >= span_y) {
+            error += span_y;
+            cx += step_x;
+        }
+        if (err2 <= span_x) {
+            error += span_x;
+            cy += step_y;
+        }
+    }
+}
+
+// RasterizeText overlay.cs:151-196.
+static void oracle_rasterize_text(uint8_t* rgb, uint32_t w, uint32_t h, const char* text, int32_t x, int32_t y,
+                                  int32_t align, const SrFont& font, const uint8_t* value) {
+    std::vector<std::pair<size_t, size_t>> lines;  // [begin, end) ranges; at most 64
+    size_t len = std::strlen(text), begin = 0;
+    for (size_t i = 0; i < len && lines.size() < 63; ++i) {
+        if (text[i] == '\n') {
+            lines.push_back({begin, i});
+            begin = i + 1;
+        }
+    }
+    lines.push_back({begin, len});
+    if (align == SR_ALIGN_CENTER) {
+        int width = 0;
+        for (auto& r : lines) width = std::max(width, (int)(r.second - r.first));
+        x -= width * 8 / 2;
+        y -= (int)lines.size() * 8 / 2;
+    }
+    for (size_t li = 0; li < lines.size(); ++li) {
+        for (size_t i = lines[li].first; i < lines[li].second; ++i) {
+            int ch = (unsigned char)text[i];
+            if (ch < font.first_char || ch > font.last_char) continue;
+            int glyph_base = (ch - font.first_char) * 8;
+            for (int row = 0; row != 8; ++row) {
+                uint8_t bits = font.glyphs[glyph_base + row];
+                for (int col = 0; col != 8; ++col) {
+                    if ((bits & (0x80 >> col)) == 0) continue;
+                    oracle_put_pixel(rgb, w, h, x + (int)(i - lines[li].first) * 8 + col, y + (int)li * 8 + row,
+                                     value, nullptr, 0.0f, false);
+                }
+            }
+        }
+    }
+}
+
+// Overlay.Draw overlay.cs:54-96: lines, then world texts, then screen texts.  Returns 1 when a line
+// end point does not fit an int (where the reference's Math.Abs would throw).
+int oracle_overlay_draw(uint8_t* rgb, uint32_t w, uint32_t h, const SrView* view, const float* depth,
+                        const SrOverlayLine* lines, uint32_t nl, const SrOverlayText* texts, uint32_t nt,
+                        const SrFont* font) {
+    float aspect = (float)w / h;
+    for (uint32_t i = 0; i < nl; ++i) {
+        const SrOverlayLine& l = lines[i];
+        float ax, ay, da, bx, by, db;
+        if (!oracle_view_project(*view, {l.a[0], l.a[1], l.a[2]}, aspect, ax, ay, da)) continue;
+        if (!oracle_view_project(*view, {l.b[0], l.b[1], l.b[2]}, aspect, bx, by, db)) continue;
+        int32_t cax, cay, cbx, cby;
+        if (!oracle_round_to_int(ax * (float)w, cax) || !oracle_round_to_int(ay * (float)h, cay) ||
+            !oracle_round_to_int(bx * (float)w, cbx) || !oracle_round_to_int(by * (float)h, cby))
+            return 1;
+        float bias = 1.0f - l.depth_bias;
+        uint8_t value[3];
+        Compositor::to_pixel({l.color[0], l.color[1], l.color[2]}, value);
+        oracle_rasterize_line(rgb, w, h, l.depth_test ? depth : nullptr, cax, cay, cbx, cby, da * bias, db * bias,
+                              value);
+    }
+    for (int world = 1; world >= 0; --world) {
+        for (uint32_t i = 0; i < nt; ++i) {
+            const SrOverlayText& t = texts[i];
+            if ((t.in_world != 0) != (world == 1)) continue;
+            int32_t x = t.screen_pos[0], y = t.screen_pos[1];
+            if (world) {
+                float sx, sy, d;
+                if (!oracle_view_project(*view, {t.world_pos[0], t.world_pos[1], t.world_pos[2]}, aspect, sx, sy, d))
+                    continue;
+                if (!oracle_round_to_int(sx * (float)w, x) || !oracle_round_to_int(sy * (float)h, y)) continue;
+            }
+            uint8_t value[3];
+            Compositor::to_pixel({t.color[0], t.color[1], t.color[2]}, value);
+            oracle_rasterize_text(rgb, w, h, t.text, x, y, t.align, *font, value);
+        }
+    }
+    return 0;
 }
 
 }  // extern "C"

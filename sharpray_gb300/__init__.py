@@ -4,8 +4,9 @@ The native library ``libsharpray_gb300.so`` (C ABI in ``include/sharpray.h``) do
 this package is the Python host side above it, mirroring the reference's Scene / Renderer /
 Compositor classes (see :mod:`sharpray_gb300.api`).
 """
-from .api import (AABox, Aovs, Compositor, Context, Fog, Material, Mesh, Object, Quat, Renderer, Scene,
-                  SharpRayError, SkyProcedural, SkyTexture, Sphere, StateError, Texture, TextureFilter, Tonemapper,
-                  Transform, View, load_image, mesh_triangles, render_compose, render_params)
+from .api import (AABox, AovKind, Aovs, Compositor, Context, Fog, Font, Material, Mesh, Object, Overlay, Quat,
+                  Renderer, Scene, SharpRayError, SkyProcedural, SkyTexture, Sphere, StateError, Texture,
+                  TextureFilter, Tonemapper, Transform, View, aov_image, load_image, mesh_triangles, render_compose,
+                  render_params, save_image)
 
 __version__ = "0.1.0"

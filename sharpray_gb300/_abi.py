@@ -24,6 +24,8 @@ SR_SHAPE_MESH = 0
 SR_SHAPE_SPHERE = 1
 SR_SHAPE_AABOX = 2
 
+SR_AOV_NORMAL, SR_AOV_DEPTH, SR_AOV_VARIANCE, SR_AOV_SAMPLES, SR_AOV_UV = 0, 1, 2, 3, 4
+SR_ALIGN_TOP_LEFT, SR_ALIGN_CENTER = 0, 1
 SR_TEXTURE_SRGB = 0
 SR_TEXTURE_LINEAR = 1
 SR_TEXTURE_HDR = 2
@@ -106,6 +108,23 @@ class SrComposeParams(C.Structure):
                 ("denoise_fog_radius", C.c_float), ("denoise_fog_strength", C.c_float)]
 
 
+class SrAovImageParams(C.Structure):
+    _fields_ = [("variance_threshold", C.c_float), ("min_samples", C.c_uint32), ("max_samples", C.c_uint32)]
+
+
+class SrOverlayLine(C.Structure):
+    _fields_ = [("a", _f3), ("b", _f3), ("color", _f3), ("depth_test", C.c_int32), ("depth_bias", C.c_float)]
+
+
+class SrOverlayText(C.Structure):
+    _fields_ = [("text", C.c_char_p), ("in_world", C.c_int32), ("world_pos", _f3), ("screen_pos", C.c_int32 * 2),
+                ("color", _f3), ("align", C.c_int32)]
+
+
+class SrFont(C.Structure):
+    _fields_ = [("glyphs", C.c_void_p), ("first_char", C.c_int32), ("last_char", C.c_int32)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _U = C.c_uint32
@@ -154,6 +173,11 @@ PROTOTYPES = {
     "sr_compose_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
     "sr_compose_device_static": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
     "sr_preview": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P]),
+    "sr_aov_image": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P]),
+    "sr_aov_image_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P, _P]),
+    "sr_overlay_draw": (_I, [_P, _P, _U, _U, C.POINTER(SrView), _P, _P, _U, _P, _U, C.POINTER(SrFont)]),
+    "sr_overlay_draw_device": (_I, [_P, _P, _U, _U, C.POINTER(SrView), _P, _P, _U, _P, _U, C.POINTER(SrFont), _P]),
+    "sr_image_save": (_I, [C.c_char_p, _U, _U, _P]),
 }
 
 

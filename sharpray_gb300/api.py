@@ -38,7 +38,8 @@ from ._abi import (SharpRayError, SrAovs, SrComposeParams, SrFog, SrMaterial, Sr
 __all__ = [
     "Context", "Texture", "TextureFilter", "Mesh", "Sphere", "AABox", "Material", "Quat", "Transform", "Object",
     "SkyTexture", "SkyProcedural", "Fog", "Scene", "View", "Renderer", "Compositor", "Tonemapper",
-    "SharpRayError", "StateError", "load_image", "mesh_triangles",
+    "SharpRayError", "StateError", "load_image", "mesh_triangles", "AovKind", "aov_image", "save_image", "Font",
+    "Overlay",
 ]
 
 
@@ -604,21 +605,144 @@ class Compositor:
         p.denoise_fog_radius, p.denoise_fog_strength = float(self.denoise_fog_radius), float(self.denoise_fog_strength)
         return p
 
-    def compose(self, rend: Renderer) -> np.ndarray:
-        """Compositor.Compose compose.cs:74-99 -> (H, W, 3) uint8."""
+    def compose(self, rend: Renderer, overlay: Optional["Overlay"] = None) -> np.ndarray:
+        """Compositor.Compose compose.cs:74-99 -> (H, W, 3) uint8, then the overlay if given."""
         out = np.zeros((rend.height, rend.width, 3), np.uint8)
         a, p = rend.aovs.to_c(), self.to_c()
         ctx = rend.scene.ctx
         check(ctx._lib.sr_compose(ctx.handle, C.byref(a), rend.width, rend.height, C.byref(p), ptr(out)))
+        if overlay is not None:
+            overlay.draw(ctx, out, rend.view, rend.depth.reshape(rend.height, rend.width))
         return out
 
-    def preview(self, rend: Renderer) -> np.ndarray:
-        """Compositor.Preview compose.cs:57-65 (tonemap without denoise)."""
+    def preview(self, rend: Renderer, overlay: Optional["Overlay"] = None) -> np.ndarray:
+        """Compositor.Preview compose.cs:57-65 (tonemap without denoise), then the overlay if given."""
         out = np.zeros((rend.height, rend.width, 3), np.uint8)
         a, p = rend.aovs.to_c(), self.to_c()
         ctx = rend.scene.ctx
         check(ctx._lib.sr_preview(ctx.handle, C.byref(a), rend.width, rend.height, C.byref(p), ptr(out)))
+        if overlay is not None:
+            overlay.draw(ctx, out, rend.view, rend.depth.reshape(rend.height, rend.width))
         return out
+
+
+class AovKind(IntEnum):
+    Normal = _abi.SR_AOV_NORMAL
+    Depth = _abi.SR_AOV_DEPTH
+    Variance = _abi.SR_AOV_VARIANCE
+    Samples = _abi.SR_AOV_SAMPLES
+    Uv = _abi.SR_AOV_UV
+
+
+def aov_image(rend: Renderer, kind: AovKind) -> np.ndarray:
+    """The normal / depth / variance / samples / uv dumps of program.cs:211-263 as (H, W, 3) uint8,
+    with the renderer's own variance threshold and sample range."""
+    out = np.zeros((rend.height, rend.width, 3), np.uint8)
+    p = _abi.SrAovImageParams(rend.params.variance_threshold, rend.params.min_samples, rend.params.max_samples)
+    ctx = rend.scene.ctx
+    a = rend.aovs.to_c()
+    check(ctx._lib.sr_aov_image(ctx.handle, C.byref(a), rend.width, rend.height, int(kind), C.byref(p), ptr(out)))
+    return out
+
+
+def save_image(path, rgb8: np.ndarray) -> None:
+    """Image.Save image.cs:198-212: .tga, .ppm or .bmp by extension."""
+    img = np.ascontiguousarray(rgb8, np.uint8)
+    if img.ndim != 3 or img.shape[2] != 3:
+        raise ValueError("image must be (height, width, 3) uint8")
+    check(_abi.load().sr_image_save(str(path).encode(), img.shape[1], img.shape[0], ptr(img)))
+
+
+@dataclass
+class Font:
+    """An 8x8 bitmap font: glyphs[c - first_char] is 8 row bytes, most significant bit leftmost
+    (the layout of the reference's Font table, font.cs).  No font ships with the library."""
+    glyphs: np.ndarray
+    first_char: int = 32
+
+    def to_c(self) -> "_abi.SrFont":
+        g = np.ascontiguousarray(self.glyphs, np.uint8).reshape(-1, 8)
+        self._keep = g
+        return _abi.SrFont(g.ctypes.data, int(self.first_char), int(self.first_char) + g.shape[0] - 1)
+
+
+class Overlay:
+    """Debug overlay (overlay.cs): lines and boxes in world space, text in world or screen space,
+    drawn by the library into an RGB8 image (sr_overlay_draw)."""
+
+    TopLeft, Center = _abi.SR_ALIGN_TOP_LEFT, _abi.SR_ALIGN_CENTER
+
+    def __init__(self, font: Optional[Font] = None):
+        self.font = font
+        self.lines: list = []
+        self.texts: list = []
+
+    def add_line(self, a, b, color, depth_test: bool = True, depth_bias: float = 0.005) -> None:
+        self.lines.append((tuple(map(float, a)), tuple(map(float, b)), tuple(map(float, color)), bool(depth_test),
+                           float(depth_bias)))
+
+    def add_line_box(self, box: AABox, color, depth_test: bool = True, depth_bias: float = 0.005,
+                     rot: Optional[Quat] = None) -> None:
+        """AddLineBox overlay.cs:23-44 with Box.Corners math.cs:1086-1096 (float32)."""
+        lo, hi = np.asarray(box.min, np.float32), np.asarray(box.max, np.float32)
+        center, half = (lo + hi) * np.float32(0.5), (hi - lo) * np.float32(0.5)
+        q = rot if rot is not None else Quat.identity()
+        corners = []
+        for i in range(8):
+            v = np.array([half[0] if i & 1 else -half[0], half[1] if i & 2 else -half[1],
+                          half[2] if i & 4 else -half[2]], np.float32)
+            corners.append(center + _rotate_f32(q, v))
+        for i, j in ((0, 1), (2, 3), (4, 5), (6, 7), (0, 2), (1, 3), (4, 6), (5, 7), (0, 4), (1, 5), (2, 6), (3, 7)):
+            self.add_line(corners[i], corners[j], color, depth_test, depth_bias)
+
+    def add_text(self, text: str, pos, color, align: Optional[int] = None) -> None:
+        """A 3-component `pos` is a world position (default centred), a 2-component one a screen
+        pixel (default top-left), as the two AddText overloads of overlay.cs:46-52."""
+        world = len(pos) == 3
+        if align is None:
+            align = self.Center if world else self.TopLeft
+        self.texts.append((text.encode("latin-1", "replace"), world, tuple(pos), tuple(map(float, color)), int(align)))
+
+    def _c_arrays(self):
+        lines = (_abi.SrOverlayLine * max(1, len(self.lines)))()
+        for k, (a, b, c, dt, bias) in enumerate(self.lines):
+            lines[k].a[:], lines[k].b[:], lines[k].color[:] = a, b, c
+            lines[k].depth_test, lines[k].depth_bias = int(dt), bias
+        texts = (_abi.SrOverlayText * max(1, len(self.texts)))()
+        for k, (t, world, pos, c, align) in enumerate(self.texts):
+            texts[k].text, texts[k].in_world, texts[k].align = t, int(world), align
+            if world:
+                texts[k].world_pos[:] = [float(x) for x in pos]
+            else:
+                texts[k].screen_pos[:] = [int(x) for x in pos]
+            texts[k].color[:] = c
+        return lines, texts
+
+    def draw(self, ctx: Context, image: np.ndarray, view: View, depth: Optional[np.ndarray] = None) -> np.ndarray:
+        """Overlay.Draw overlay.cs:54-96 into `image` ((H, W, 3) uint8, modified in place)."""
+        if image.dtype != np.uint8 or image.ndim != 3 or image.shape[2] != 3 or not image.flags.c_contiguous:
+            raise ValueError("image must be a C-contiguous (height, width, 3) uint8 array")
+        h, w = image.shape[:2]
+        d = None if depth is None else np.ascontiguousarray(depth, np.float32).reshape(h * w)
+        lines, texts = self._c_arrays()
+        font = self.font.to_c() if self.font is not None else _abi.SrFont(None, 0, -1)
+        v = view.to_c()
+        check(ctx._lib.sr_overlay_draw(ctx.handle, ptr(image), w, h, C.byref(v), ptr(d), lines, len(self.lines),
+                                       texts, len(self.texts), C.byref(font) if self.font is not None else None))
+        return image
+
+
+def _rotate_f32(q: Quat, v: np.ndarray) -> np.ndarray:
+    """Quat * Vec3 math.cs:609-617 in float32."""
+    axis = np.array([q.x, q.y, q.z], np.float32)
+    w = np.float32(q.w)
+    sqr = np.float32(axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2])
+    d = np.float32(axis[0] * v[0] + axis[1] * v[1] + axis[2] * v[2])
+    a = axis * np.float32(d * np.float32(2))
+    b = v * np.float32(w * w - sqr)
+    c = np.array([axis[1] * v[2] - axis[2] * v[1], axis[2] * v[0] - axis[0] * v[2], axis[0] * v[1] - axis[1] * v[0]],
+                 np.float32) * np.float32(w * np.float32(2))
+    return (a + b + c).astype(np.float32)
 
 
 def render_compose(scene: Scene, view: View, width: int, height: int, block_size: int, min_samples: int,

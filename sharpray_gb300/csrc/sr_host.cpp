@@ -13,6 +13,7 @@
 #include "../../include/sharpray.h"
 #include "sr_bvh.h"
 #include "sr_bvh_build.h"
+#include "sr_image.h"
 #include "sr_ingest.h"
 #include "sr_kernels.h"
 #include "sr_layout.h"
@@ -107,6 +108,8 @@ struct SrContext {
     // compose resources
     DevBuf compose_scratch, compose_tables, compose_io;
     std::vector<float> table_host;
+    // AOV images and overlay (host-buffer entry points stage through image_io)
+    DevBuf image_io, overlay_scratch;
 };
 
 struct SrScene {
@@ -1335,5 +1338,173 @@ SR_API int sr_scene_object_info(SrScene* s, uint32_t index, SrTransform* transfo
 SR_API int sr_scene_object_count(SrScene* s, uint32_t* count) {
     if (!s || !count) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     *count = (uint32_t)s->objects.size();
+    return SR_OK;
+}
+
+// ---- AOV images, overlay, image files (sr_image.cpp, sr_overlay.cu) --------------------------------
+
+static int aov_image_impl(SrContext* ctx, const DevAovs& d, uint32_t w, uint32_t h, int32_t kind,
+                          const SrAovImageParams* p, uint8_t* d_rgb, uint8_t* d_lut, cudaStream_t st) {
+    float var_div = 1.0f, min_s = 1.0f, log_range = 1.0f;
+    uint32_t lut_n = 0;
+    if (kind == SR_AOV_VARIANCE) var_div = p->variance_threshold * 2.0f;
+    if (kind == SR_AOV_SAMPLES) {
+        std::vector<uint8_t> lut = samples_table(p->min_samples, p->max_samples, &log_range);
+        lut_n = (uint32_t)lut.size();
+        min_s = (float)p->min_samples;
+        SR_CUDA(cudaMemcpyAsync(d_lut, lut.data(), lut.size(), cudaMemcpyHostToDevice, st), "copy samples table");
+    }
+    SR_CUDA(launch_aov_image(d, w * h, kind, var_div, d_lut, lut_n, min_s, log_range, d_rgb, st), "aov image");
+    (void)ctx;
+    return SR_OK;
+}
+
+static int aov_image_check(const SrAovs* a, int32_t kind, const SrAovImageParams* p) {
+    if (!a) return fail(SR_ERR_INVALID_ARG, "NULL AOVs");
+    const void* plane = kind == SR_AOV_NORMAL ? (const void*)a->normals
+                      : kind == SR_AOV_DEPTH ? (const void*)a->depth
+                      : kind == SR_AOV_VARIANCE ? (const void*)a->variance
+                      : kind == SR_AOV_SAMPLES ? (const void*)a->samples
+                      : kind == SR_AOV_UV ? (const void*)a->uv : nullptr;
+    if (kind < SR_AOV_NORMAL || kind > SR_AOV_UV) return fail(SR_ERR_INVALID_ARG, "bad AOV kind %d", kind);
+    if (!plane) return fail(SR_ERR_INVALID_ARG, "the AOV plane of kind %d is NULL", kind);
+    if ((kind == SR_AOV_VARIANCE || kind == SR_AOV_SAMPLES) && !p)
+        return fail(SR_ERR_INVALID_ARG, "AOV kind %d needs parameters", kind);
+    if (kind == SR_AOV_SAMPLES && (p->min_samples == 0 || p->max_samples < p->min_samples || p->max_samples > (1u << 24)))
+        return fail(SR_ERR_INVALID_ARG, "need 0 < min_samples <= max_samples <= 2^24");
+    return SR_OK;
+}
+
+SR_API int sr_aov_image(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, int32_t kind,
+                        const SrAovImageParams* p, uint8_t* rgb) {
+    if (!ctx || !rgb) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = aov_image_check(a, kind, p)) return rc;
+    if (ctx->device < 0) return fail(SR_ERR_STATE, "context has no device");
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    const size_t n = (size_t)w * h;
+    const size_t lut_bytes = kind == SR_AOV_SAMPLES ? (size_t)p->max_samples + 2 : 0;
+    SR_CUDA(ctx->image_io.reserve(n * 12 + n * 3 + lut_bytes + 256), "alloc AOV image io");
+    char* b = ctx->image_io.as<char>();
+    DevAovs d{};
+    size_t plane_bytes = 0;
+    const void* src = nullptr;
+    switch (kind) {
+        case SR_AOV_NORMAL: d.normals = (float*)b, src = a->normals, plane_bytes = n * 12; break;
+        case SR_AOV_DEPTH: d.depth = (float*)b, src = a->depth, plane_bytes = n * 4; break;
+        case SR_AOV_VARIANCE: d.variance = (float*)b, src = a->variance, plane_bytes = n * 4; break;
+        case SR_AOV_SAMPLES: d.samples = (uint32_t*)b, src = a->samples, plane_bytes = n * 4; break;
+        default: d.uv = (float*)b, src = a->uv, plane_bytes = n * 8; break;
+    }
+    uint8_t* d_rgb = (uint8_t*)(b + n * 12);
+    uint8_t* d_lut = d_rgb + n * 3;
+    if (n) SR_CUDA(cudaMemcpyAsync(b, src, plane_bytes, cudaMemcpyHostToDevice, st), "copy AOV plane");
+    if (int rc = aov_image_impl(ctx, d, w, h, kind, p, d_rgb, d_lut, st)) return rc;
+    if (n) SR_CUDA(cudaMemcpyAsync(rgb, d_rgb, n * 3, cudaMemcpyDeviceToHost, st), "copy pixels");
+    SR_CUDA(cudaStreamSynchronize(st), "aov image");
+    return SR_OK;
+}
+
+SR_API int sr_aov_image_device(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, int32_t kind,
+                               const SrAovImageParams* p, uint8_t* d_rgb, void* stream) {
+    if (!ctx || !d_rgb) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = aov_image_check(a, kind, p)) return rc;
+    if (ctx->device < 0) return fail(SR_ERR_STATE, "context has no device");
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    DevAovs d{a->radiance, a->radiance_fog, a->normals, a->uv, a->depth, a->samples, a->variance};
+    const size_t lut_bytes = kind == SR_AOV_SAMPLES ? (size_t)p->max_samples + 2 : 16;
+    SR_CUDA(ctx->overlay_scratch.reserve(lut_bytes), "alloc samples table");
+    return aov_image_impl(ctx, d, w, h, kind, p, d_rgb, ctx->overlay_scratch.as<uint8_t>(), st);
+}
+
+// Plans on the host, then stages ops, colours and the font next to the owner plane in `scratch`.
+static int overlay_impl(SrContext* ctx, DevBuf& scratch, uint8_t* d_rgb, uint32_t w, uint32_t h, const SrView* view,
+                        const float* d_depth, const SrOverlayLine* lines, uint32_t nl, const SrOverlayText* texts,
+                        uint32_t nt, const SrFont* font, cudaStream_t st) {
+    OverlayPlan plan;
+    try {
+        plan = plan_overlay(w, h, *view, lines, nl, texts, nt, font);
+    } catch (const ImageError& e) {
+        return fail(SR_ERR_INVALID_ARG, "%s", e.what());
+    }
+    const size_t n = (size_t)w * h;
+    const size_t font_bytes = font && font->glyphs ? (size_t)(font->last_char - font->first_char + 1) * 8 : 0;
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t o_owner = 0, o_lines = up(n * 4), o_glyphs = o_lines + up(plan.lines.size() * sizeof(OverlayLineOp));
+    const size_t o_colors = o_glyphs + up(plan.glyphs.size() * sizeof(OverlayGlyphOp));
+    const size_t o_font = o_colors + up(plan.colors.size() * 4), total = o_font + up(font_bytes) + 256;
+    SR_CUDA(scratch.reserve(total), "alloc overlay scratch");
+    char* b = scratch.as<char>();
+    if (!plan.lines.empty())
+        SR_CUDA(cudaMemcpyAsync(b + o_lines, plan.lines.data(), plan.lines.size() * sizeof(OverlayLineOp),
+                                cudaMemcpyHostToDevice, st), "copy overlay lines");
+    if (!plan.glyphs.empty())
+        SR_CUDA(cudaMemcpyAsync(b + o_glyphs, plan.glyphs.data(), plan.glyphs.size() * sizeof(OverlayGlyphOp),
+                                cudaMemcpyHostToDevice, st), "copy overlay glyphs");
+    if (!plan.colors.empty())
+        SR_CUDA(cudaMemcpyAsync(b + o_colors, plan.colors.data(), plan.colors.size() * 4, cudaMemcpyHostToDevice, st),
+                "copy overlay colours");
+    if (font_bytes)
+        SR_CUDA(cudaMemcpyAsync(b + o_font, font->glyphs, font_bytes, cudaMemcpyHostToDevice, st), "copy font");
+    SR_CUDA(launch_overlay((const OverlayLineOp*)(b + o_lines), (uint32_t)plan.lines.size(),
+                           (const OverlayGlyphOp*)(b + o_glyphs), (uint32_t)plan.glyphs.size(),
+                           (const uint8_t*)(b + o_font), (const uint32_t*)(b + o_colors), d_depth, w, h,
+                           (int32_t*)(b + o_owner), d_rgb, st),
+            "overlay");
+    (void)ctx;
+    return SR_OK;
+}
+
+static int overlay_check(SrContext* ctx, const void* rgb, uint32_t w, uint32_t h, const SrView* view,
+                         const SrOverlayLine* lines, uint32_t nl, const SrOverlayText* texts, uint32_t nt,
+                         const SrFont* font) {
+    if (!ctx || !rgb || !view) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (w == 0 || h == 0) return fail(SR_ERR_INVALID_ARG, "empty image");
+    if ((nl && !lines) || (nt && !texts)) return fail(SR_ERR_INVALID_ARG, "NULL overlay entries");
+    if (nt && (!font || !font->glyphs)) return fail(SR_ERR_INVALID_ARG, "overlay text needs a font");
+    if (font && font->glyphs && !(0 <= font->first_char && font->first_char <= font->last_char && font->last_char <= 255))
+        return fail(SR_ERR_INVALID_ARG, "font range must be 0 <= first_char <= last_char <= 255");
+    for (uint32_t i = 0; i < nt; ++i)
+        if (!texts[i].text) return fail(SR_ERR_INVALID_ARG, "overlay text %u is NULL", i);
+    if (ctx->device < 0) return fail(SR_ERR_STATE, "context has no device");
+    return SR_OK;
+}
+
+SR_API int sr_overlay_draw(SrContext* ctx, uint8_t* rgb, uint32_t w, uint32_t h, const SrView* view,
+                           const float* depth, const SrOverlayLine* lines, uint32_t nl, const SrOverlayText* texts,
+                           uint32_t nt, const SrFont* font) {
+    if (int rc = overlay_check(ctx, rgb, w, h, view, lines, nl, texts, nt, font)) return rc;
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = ctx->stream;
+    const size_t n = (size_t)w * h;
+    SR_CUDA(ctx->image_io.reserve(n * 3 + n * 4 + 512), "alloc overlay io");
+    uint8_t* d_rgb = ctx->image_io.as<uint8_t>();
+    float* d_depth = depth ? (float*)(d_rgb + ((n * 3 + 255) & ~(size_t)255)) : nullptr;
+    SR_CUDA(cudaMemcpyAsync(d_rgb, rgb, n * 3, cudaMemcpyHostToDevice, st), "copy image");
+    if (depth) SR_CUDA(cudaMemcpyAsync(d_depth, depth, n * 4, cudaMemcpyHostToDevice, st), "copy depth");
+    if (int rc = overlay_impl(ctx, ctx->overlay_scratch, d_rgb, w, h, view, d_depth, lines, nl, texts, nt, font, st))
+        return rc;
+    SR_CUDA(cudaMemcpyAsync(rgb, d_rgb, n * 3, cudaMemcpyDeviceToHost, st), "copy image");
+    SR_CUDA(cudaStreamSynchronize(st), "overlay");
+    return SR_OK;
+}
+
+SR_API int sr_overlay_draw_device(SrContext* ctx, uint8_t* d_rgb, uint32_t w, uint32_t h, const SrView* view,
+                                  const float* d_depth, const SrOverlayLine* lines, uint32_t nl,
+                                  const SrOverlayText* texts, uint32_t nt, const SrFont* font, void* stream) {
+    if (int rc = overlay_check(ctx, d_rgb, w, h, view, lines, nl, texts, nt, font)) return rc;
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    return overlay_impl(ctx, ctx->overlay_scratch, d_rgb, w, h, view, d_depth, lines, nl, texts, nt, font, st);
+}
+
+SR_API int sr_image_save(const char* path, uint32_t w, uint32_t h, const uint8_t* rgb) {
+    if (!path || (!rgb && w && h)) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    try {
+        save_image(path, w, h, rgb);
+    } catch (const ImageError& e) {
+        return fail(SR_ERR_IO, "%s", e.what());
+    }
     return SR_OK;
 }

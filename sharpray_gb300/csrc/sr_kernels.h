@@ -46,4 +46,24 @@ cudaError_t launch_compose_static(int device, const DevAovs& in, uint32_t width,
                                   const ComposeConsts& k, float rp_inv, float rpf_inv, float fog_strength,
                                   uint8_t* rgb8, cudaStream_t stream, size_t* needed_bytes);
 
+// AOV visualisation to RGB8 (sr_overlay.cu).  `lut` maps sample counts below lut_n to bytes.
+cudaError_t launch_aov_image(const DevAovs& in, uint32_t n, int32_t kind, float variance_div, const uint8_t* lut,
+                             uint32_t lut_n, float min_samples, float log_range, uint8_t* rgb8, cudaStream_t stream);
+
+// Overlay draw (sr_overlay.cu): lines and glyphs prepared on the host; `entry` is the draw-order
+// index, `colors[entry]` the packed RGB8 (r | g << 8 | b << 16); `owner` is a w*h int32 scratch.
+struct OverlayLineOp {
+    int32_t ax, ay, bx, by;
+    float inv_a, inv_b;  // 1 / biased depth at a and b
+    int32_t depth_test, entry;
+};
+struct OverlayGlyphOp {
+    int32_t x, y;   // top-left pixel of the 8x8 cell
+    int32_t glyph;  // row index into the font table
+    int32_t entry;
+};
+cudaError_t launch_overlay(const OverlayLineOp* lines, uint32_t line_count, const OverlayGlyphOp* glyph_ops,
+                           uint32_t glyph_count, const uint8_t* glyphs, const uint32_t* colors, const float* depth,
+                           uint32_t width, uint32_t height, int32_t* owner, uint8_t* rgb8, cudaStream_t stream);
+
 }  // namespace sr
