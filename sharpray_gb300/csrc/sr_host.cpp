@@ -785,7 +785,7 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         // queues per group slot: ray entries (32 B) trace x2 + shadow x2, 4-byte event 3 x2 + late x2 +
         // resolve; arrays start on 256 bytes
         const size_t rec = sizeof(Rec);
-        size_t bytes = n * (10 * rec + 16 + 4 * rec + 9 * 4) + (3 + 9 * kWaveGroups) * 256 +
+        size_t bytes = n * (10 * rec + 16 + 4 * rec + 12 * 4 + 1) + (4 + 10 * kWaveGroups) * 256 +
                        kWaveGroups * kWaveCounters * sizeof(uint32_t);
         SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
         s->wave_slots = (uint32_t)n;
@@ -800,6 +800,7 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
     Rec* recs = (Rec*)take(n, 6 * rec);
     Rec* pix = (Rec*)take(n, 4 * rec);
     float4* medium = (float4*)take(n, 16);
+    uint8_t* ev_mark = (uint8_t*)take(n, 1);
     for (int g = 0; g < kWaveGroups; ++g) {
         WaveState& w = s->ws[g];
         const size_t m = group_slots[g];
@@ -819,6 +820,9 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         w.q_shadow[1] = (Rec*)take(m, rec);
         w.q_late[0] = (uint32_t*)take(m, 4);
         w.q_late[1] = (uint32_t*)take(m, 4);
+        w.q_sorted = (uint32_t*)take(m, 3 * 4);
+        w.rec_stride = (uint32_t)n;
+        w.ev_mark = ev_mark;
     }
     for (int g = 0; g < kWaveGroups; ++g) s->ws[g].counts = (uint32_t*)p + g * kWaveCounters;
     return SR_OK;

@@ -62,8 +62,12 @@ enum : int { EV_FOG = 0, EV_MISS = 1, EV_SURF = 2 };
 // record (WaveState::pix, four per slot).
 enum : int { R_RAY = 0, R_HIT = 1, R_PATH = 2, R_RNG = 3, R_SH0 = 4, R_SH1 = 5 };
 enum : int { X_PRIM = 0, X_ACC = 1 };
-__device__ __forceinline__ size_t rix(uint32_t s, int k) { return 6 * (size_t)s + k; }
-__device__ __forceinline__ size_t pix(uint32_t s, int k) { return 4 * (size_t)s + k; }
+__device__ __forceinline__ size_t rix(const WaveState& W, uint32_t s, int k) {
+    return SR_REC_SOA ? (size_t)k * W.rec_stride + s : 6 * (size_t)s + k;
+}
+__device__ __forceinline__ size_t pix(const WaveState& W, uint32_t s, int k) {
+    return SR_REC_SOA ? (size_t)k * W.rec_stride + s : 4 * (size_t)s + k;
+}
 
 // Record loads and stores (one place to change how path state is moved).
 __device__ __forceinline__ Rec ld_rec(const Rec* p) { return *p; }
@@ -142,10 +146,11 @@ __device__ __forceinline__ Rec rng_rec(const Rng& r, Col fog) {
 }
 
 // Start of a sample: the camera ray and a reset path (scene.cs:633-638).
-__device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, const Ray& ray, const Rng& rng) {
-    st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
-    st_rec(&W.rec[rix(s, R_PATH)], Rec{make_float4(0.f, 0.f, 0.f, 0.f), make_float4(1.f, 1.f, 1.f, fbits(0u))});
-    st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, black()));
+__device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, const Ray& ray, const Rng& rng,
+                                             float sdist = 0.f) {
+    st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, sdist)});
+    st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(0.f, 0.f, 0.f, 0.f), make_float4(1.f, 1.f, 1.f, fbits(0u))});
+    st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, black()));
 }
 
 __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevParams P) {
@@ -162,15 +167,15 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
             Ray ray = camera_ray(V, P, x, y, rng);
             begin_sample(W, s, ray, rng);
             float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-            st_rec(&W.pix[pix(s, X_ACC)], Rec{z, z});
-            st_rec(&W.pix[pix(s, X_ACC + 1)], Rec{z, z});
-            st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{z, z});  // counts and sample index start at 0 (int bits)
+            st_rec(&W.pix[pix(W, s, X_ACC)], Rec{z, z});
+            st_rec(&W.pix[pix(W, s, X_ACC + 1)], Rec{z, z});
+            st_rec(&W.pix[pix(W, s, X_ACC + 2)], Rec{z, z});  // counts and sample index start at 0 (int bits)
         }
     }
     uint32_t off[1];
     block_offsets<1>({&W.counts[kCountTrace]}, {valid}, sh, 0u, off);
     if (valid) {
-        Rec r = ld_rec(&W.rec[rix(s, R_RAY)]);
+        Rec r = ld_rec(&W.rec[rix(W, s, R_RAY)]);
         W.q_trace[0][off[0]] = ray_entry(s, V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z}, 0u);
     }
 }
@@ -187,19 +192,15 @@ __device__ __forceinline__ int segment_event(const DevScene& S, const Ray& ray, 
 }
 
 // A new path ray (scatter or camera ray): -1 when it needs the next trace kernel's traversal; when
-// it misses both root children of the scene BVH -- the first thing the traversal tests -- its
-// empty closest hit is written here, as the trace kernel would write it, and its segment's event
-// is returned.
+// it misses both root children of the scene BVH -- the first thing the traversal tests -- it has
+// no hit, and its segment's event is returned with the fog scatter distance in `sdist` (the
+// caller stores it with the ray, as the trace kernel does).
 template <bool COUNT>
-__device__ __forceinline__ int next_segment(const WaveState& W, const DevScene& S, uint32_t s, const Ray& ray, Rng& rng,
-                                            Ctr& c) {
+__device__ __forceinline__ int next_segment(const DevScene& S, const Ray& ray, Rng& rng, Ctr& c, float& sdist) {
+    sdist = 0.f;
     if (!misses_scene<COUNT, false>(S, ray, c)) return -1;
     SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-    float sdist;
-    int ev = segment_event(S, ray, false, 0.f, rng, sdist);
-    st_rec(&W.rec[rix(s, R_HIT)], Rec{make_float4(__int_as_float(-1), __int_as_float(-1), __int_as_float(0x7f800000), 0.f),
-                            make_float4(0.f, 0.f, sdist, 0.f)});
-    return ev;
+    return segment_event(S, ray, false, 0.f, rng, sdist);
 }
 
 // Per-warp staging of the persistent loop's appends to NQ queues: entries collect in a shared
@@ -361,15 +362,17 @@ __device__ __forceinline__ int extend_answer(const WaveState& W, const DevScene&
     float sdist = 0.f;
     int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
     if (S.has_fog) {
-        Rec g = ld_rec(&W.rec[rix(s, R_RNG)]);
+        Rec g = ld_rec(&W.rec[rix(W, s, R_RNG)]);
         Rng rng = rng_of(g);
         ev = segment_event(S, ray, h.obj >= 0, h.dist, rng, sdist);
-        st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, Col{g.b.y, g.b.z, g.b.w}));
+        st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, Col{g.b.y, g.b.z, g.b.w}));
     }
-    st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                      make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
-    st_rec(&W.rec[rix(s, R_HIT)], Rec{make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
-                                      make_float4(h.u, h.v, sdist, 0.f)});
+    // the fog scatter distance travels with the ray; only a surface event needs the hit record
+    st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                                      make_float4(ray.d.x, ray.d.y, ray.d.z, sdist)});
+    if (ev == EV_SURF)
+        st_rec(&W.rec[rix(W, s, R_HIT)], Rec{make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
+                                          make_float4(h.u, h.v, 0.f, 0.f)});
     return ev;
 }
 
@@ -390,6 +393,9 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveSta
         W.counts[kCountEvent + 3 * nxt + EV_FOG] = 0;
         W.counts[kCountEvent + 3 * nxt + EV_MISS] = 0;
         W.counts[kCountEvent + 3 * nxt + EV_SURF] = 0;
+        W.counts[kCountSorted + EV_FOG] = 0;  // this bounce's sorted queues are filled after the trace
+        W.counts[kCountSorted + EV_MISS] = 0;
+        W.counts[kCountSorted + EV_SURF] = 0;
     }
     __shared__ uint32_t ring[kBlockWarps][3 * 64];
     WarpStage<3> stage;
@@ -412,7 +418,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveSta
                 tr = 1.0f;
                 if (S.has_fog) tr = 1.0f * fog_transmittance_inf(S, ray);
             }
-            st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr, tr, tr, 0.f));
+            st4(&W.rec[rix(W, s, R_SH0)].a, make_float4(tr, tr, tr, 0.f));
             return -1;
         },
         [&](uint32_t s, int ev) { stage.add(eq, ec, s, ev); });
@@ -427,7 +433,7 @@ __device__ __forceinline__ void shadow_trace(const WaveState& W, const DevScene&
                                              Ctr& c, uint32_t* err) {
     Col tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
     if (max_component(tr) > 0.0f && S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
-    st4(&W.rec[rix(s, R_SH0)].a, make_float4(tr.r, tr.g, tr.b, 0.f));
+    st4(&W.rec[rix(W, s, R_SH0)].a, make_float4(tr.r, tr.g, tr.b, 0.f));
 }
 
 // Shadow rays of the previous bounce in scenes with transparent materials, where a shadow ray is a
@@ -452,10 +458,10 @@ __global__ void __launch_bounds__(128) k_wave_shadow_loop(WaveState W, DevScene 
 template <bool COUNT, bool GENERAL>
 __device__ __forceinline__ void add_nee(const WaveState& W, const DevScene& S, uint32_t s, uint32_t pflags,
                                         Col& radiance, Col& fog, Ctr& c) {
-    Rec r0 = ld_rec(&W.rec[rix(s, R_SH0)]);
+    Rec r0 = ld_rec(&W.rec[rix(W, s, R_SH0)]);
     Col tr = col3(r0.a);
     if (max_component(tr) > 0.0f) {
-        Rec r1 = ld_rec(&W.rec[rix(s, R_SH1)]);
+        Rec r1 = ld_rec(&W.rec[rix(W, s, R_SH1)]);
         V3 ldir{r0.b.x, r0.b.y, r0.b.z};
         Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * col3(r1.a) * r1.a.w / r0.b.w;
         Col add = contrib * col3(r1.b);
@@ -483,7 +489,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
                                                 int ev, Ctr& c) {
     SegOut o;
         SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
-        Rec rr = ld_rec(&W.rec[rix(s, R_RAY)]), pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
+        Rec rr = ld_rec(&W.rec[rix(W, s, R_RAY)]), pr = ld_rec(&W.rec[rix(W, s, R_PATH)]), gr = ld_rec(&W.rec[rix(W, s, R_RNG)]);
         Rng rng = rng_of(gr);
         Col fog{gr.b.y, gr.b.z, gr.b.w};
         uint32_t bounce = ibits(rr.a.w);
@@ -500,9 +506,9 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
             // Fog and surface events share one light sample, one Russian-roulette draw and then
             // scatter, in that RNG order (scene.cs:654-726).
             const bool fog_event = ev == EV_FOG;
-            const Rec hr = ld_rec(&W.rec[rix(s, R_HIT)]);
             SurfHit sh;
             if (!fog_event) {
+                const Rec hr = ld_rec(&W.rec[rix(W, s, R_HIT)]);
                 Hit hit{__float_as_int(hr.a.x), __float_as_int(hr.a.y), hr.a.z, hr.a.w, hr.b.x, hr.b.y};
                 surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
             }
@@ -513,7 +519,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
             V3 pos;
             if (fog_event) {
                 energy = energy * col3(S.fog_color);
-                pos = ray_at(ray, hr.b.z);
+                pos = ray_at(ray, rr.b.w);  // the fog scatter distance
             } else {
                 bias = fmaxf(1e-4f, dist * 1e-4f);
                 pos = ray_at(ray, dist - bias);
@@ -521,7 +527,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
                 radiance = radiance + su.radiance * energy;
                 if (bounce == 0) {
                     pflags |= PF_PRIMARY;
-                    st_rec(&W.pix[pix(s, X_PRIM)], Rec{make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
+                    st_rec(&W.pix[pix(W, s, X_PRIM)], Rec{make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
                                  make_float4(su.uv.x, su.uv.y, 0.f, 0.f)});
                 }
             }
@@ -573,9 +579,9 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
                         o.shadow = true;
                         o.sh_o = pos;
                         o.sh_d = ldir;
-                        st_rec(&W.rec[rix(s, R_SH0)], Rec{make_float4(pos.x, pos.y, pos.z, 0.f),
+                        st_rec(&W.rec[rix(W, s, R_SH0)], Rec{make_float4(pos.x, pos.y, pos.z, 0.f),
                                                           make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
-                        st_rec(&W.rec[rix(s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
+                        st_rec(&W.rec[rix(W, s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
                                                           make_float4(energy.r, energy.g, energy.b, 0.f)});
                     }
                 }
@@ -614,20 +620,67 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
         }
         if (!terminate && ++bounce == P.bounces + 1) terminate = true;
         o.live = !terminate;
-        st_rec(&W.rec[rix(s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
+        st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
                      make_float4(energy.r, energy.g, energy.b, fbits(pflags))});
         if (o.live) {
-            o.next = next_segment<COUNT>(W, S, s, ray, rng, c);
+            float sd;
+            o.next = next_segment<COUNT>(S, ray, rng, c, sd);
             o.nx_o = ray.o;
             o.nx_d = ray.d;
             o.nx_bounce = bounce;
             // a traced ray's record is written by the trace kernel together with its hit
             if (o.next >= 0)
-                st_rec(&W.rec[rix(s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                                  make_float4(ray.d.x, ray.d.y, ray.d.z, 0.f)});
+                st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                                                  make_float4(ray.d.x, ray.d.y, ray.d.z, sd)});
         }
-        st_rec(&W.rec[rix(s, R_RNG)], rng_rec(rng, fog));
+        st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, fog));
     return o;
+}
+
+// The event queues of this bounce in slot order, so that the shade kernels' neighbouring threads
+// work on neighbouring slots: k_event_mark tags each queued slot with its event, k_event_sort
+// scans the slots in order and appends each tagged slot to its event's sorted queue (one atomic
+// per block and event; inside a block's run the order is the slot order), clearing the tags.
+__global__ void __launch_bounds__(256) k_event_mark(WaveState W, int cur) {
+    const uint32_t* ecount = W.counts + kCountEvent + 3 * cur;
+    const uint32_t n0 = ecount[0], n1 = ecount[1], n2 = ecount[2];
+    const uint32_t total = n0 + n1 + n2;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        const uint32_t ev = k < n0 ? 0u : (k < n0 + n1 ? 1u : 2u);
+        const uint32_t i = k - (ev == 0 ? 0u : (ev == 1 ? n0 : n0 + n1));
+        const uint32_t s = W.q_event[cur][(size_t)ev * W.slots + i];
+        W.ev_mark[s] = (uint8_t)(1u + ev);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_event_sort(WaveState W) {
+    __shared__ uint32_t warp_n[3][8];
+    __shared__ uint32_t base[3];
+    const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;  // group-local slot index
+    const uint32_t s = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);
+    const uint32_t m = li < W.slots ? W.ev_mark[s] : 0u;
+    if (m) W.ev_mark[s] = 0;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t rank[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, m == (uint32_t)(e + 1));
+        rank[e] = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) warp_n[e][warp] = __popc(bal);
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        uint32_t t = 0;
+        for (int w = 0; w < 8; ++w) t += warp_n[threadIdx.x][w];
+        base[threadIdx.x] = t ? atomicAdd(&W.counts[kCountSorted + threadIdx.x], t) : 0u;
+    }
+    __syncthreads();
+    if (m) {
+        const int e = (int)m - 1;
+        uint32_t off = base[e] + rank[e];
+        for (uint32_t w = 0; w < warp; ++w) off += warp_n[e][w];
+        W.q_sorted[(size_t)e * W.slots + off] = s;
+    }
 }
 
 // One segment of every live path with event EVK, or of all live paths (EVK = -1) with warps
@@ -661,7 +714,8 @@ __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveS
             ev = EV_SURF, i = k - pfog - pmiss, cnt = nsurf;
         }
         const bool valid = i < cnt;
-        const uint32_t s = valid ? W.q_event[cur][(size_t)ev * W.slots + i] : 0u;
+        const uint32_t* const q = SR_SORT_EVENTS ? W.q_sorted : W.q_event[cur];
+        const uint32_t s = valid ? q[(size_t)ev * W.slots + i] : 0u;
         SegOut o;
         if (valid) {
             o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
@@ -692,12 +746,12 @@ template <bool COUNT, bool GENERAL>
 __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevScene& S, const DevView& V,
                                                   const DevParams& P, const DevAovs& out, uint32_t s, Ctr& c) {
     SegOut o;
-        Rec pr = ld_rec(&W.rec[rix(s, R_PATH)]), gr = ld_rec(&W.rec[rix(s, R_RNG)]);
+        Rec pr = ld_rec(&W.rec[rix(W, s, R_PATH)]), gr = ld_rec(&W.rec[rix(W, s, R_RNG)]);
         uint32_t pflags = ibits(pr.b.w);
         Col radiance = col3(pr.a);
         Col radiance_fog{gr.b.y, gr.b.z, gr.b.w};
         if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, radiance_fog, c);
-        Rec c0 = ld_rec(&W.pix[pix(s, X_ACC)]), c1 = ld_rec(&W.pix[pix(s, X_ACC + 1)]), c2 = ld_rec(&W.pix[pix(s, X_ACC + 2)]);
+        Rec c0 = ld_rec(&W.pix[pix(W, s, X_ACC)]), c1 = ld_rec(&W.pix[pix(W, s, X_ACC + 1)]), c2 = ld_rec(&W.pix[pix(W, s, X_ACC + 2)]);
         float4 a0 = c0.a, a1 = c0.b, a2 = c1.a, a3 = c1.b, a4 = c2.a, a5 = c2.b;
         a0.x += radiance.r, a0.y += radiance.g, a0.z += radiance.b;
         a1.x += radiance_fog.r, a1.y += radiance_fog.g, a1.z += radiance_fog.b;
@@ -710,7 +764,7 @@ __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevS
         uint32_t ncount = ibits(a4.y), dcount = ibits(a4.z);
         uint32_t si = ibits(a4.w);
         if (pflags & PF_PRIMARY) {
-            Rec pm = ld_rec(&W.pix[pix(s, X_PRIM)]);
+            Rec pm = ld_rec(&W.pix[pix(W, s, X_PRIM)]);
             float4 pn = pm.a;
             a2.x += pn.x, a2.y += pn.y, a2.z += pn.z;
             a3.x = pn.x, a3.y = pn.y, a3.z = pn.z;
@@ -747,16 +801,17 @@ __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevS
         } else {
             Rng rng = rng_of(gr);
             Ray ray = camera_ray(V, P, x, y, rng);
-            o.next = next_segment<COUNT>(W, S, s, ray, rng, c);
-            begin_sample(W, s, ray, rng);
+            float sd;
+            o.next = next_segment<COUNT>(S, ray, rng, c, sd);
+            begin_sample(W, s, ray, rng, sd);
             o.live = true;
             o.nx_o = ray.o;
             o.nx_d = ray.d;
         }
         a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
-        st_rec(&W.pix[pix(s, X_ACC)], Rec{a0, a1});
-        st_rec(&W.pix[pix(s, X_ACC + 1)], Rec{a2, a3});
-        st_rec(&W.pix[pix(s, X_ACC + 2)], Rec{a4, a5});
+        st_rec(&W.pix[pix(W, s, X_ACC)], Rec{a0, a1});
+        st_rec(&W.pix[pix(W, s, X_ACC + 1)], Rec{a2, a3});
+        st_rec(&W.pix[pix(W, s, X_ACC + 2)], Rec{a4, a5});
     return o;
 }
 
@@ -851,8 +906,8 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
     if (group >= 0) {
         const WaveState W = G.W[group];
         // the slot's shadow ray queued for the next bounce, if any: traced first
-        if (ibits(ld_rec(&W.rec[rix(s, R_PATH)]).b.w) & PF_NEE) {
-            Rec r0 = ld_rec(&W.rec[rix(s, R_SH0)]);
+        if (ibits(ld_rec(&W.rec[rix(W, s, R_PATH)]).b.w) & PF_NEE) {
+            Rec r0 = ld_rec(&W.rec[rix(W, s, R_SH0)]);
             shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(V3{r0.a.x, r0.a.y, r0.a.z}, V3{r0.b.x, r0.b.y, r0.b.z}), c,
                                          err);
         }
@@ -915,6 +970,10 @@ static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cuda
     }
     k_wave_finalize<COUNT, GENERAL, true><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
                                                                            L.counters);
+    if (SR_SORT_EVENTS) {
+        k_event_mark<<<L.grid_mark, 256, 0, st>>>(W, cur);
+        k_event_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W);
+    }
     if (SR_SPLIT_SHADE) {
         k_wave_shade<COUNT, GENERAL, EV_FOG><<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
         k_wave_shade<COUNT, GENERAL, EV_MISS><<<L.grid_shade[1], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
@@ -987,10 +1046,12 @@ void wave_grid_sizes(WaveLaunch& L, int sms) {
     L.grid_shade[0] = b[3];
     L.grid_shade[1] = b[4];
     L.grid_shade[2] = b[5];
+    L.grid_mark = sms * 8;
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(L.W[0].counts, 0, (size_t)L.groups * kWaveCounters * sizeof(uint32_t), st);
+    if (e == cudaSuccess && SR_SORT_EVENTS) e = cudaMemsetAsync(L.W[0].ev_mark, 0, L.W[0].rec_stride, st);
     if (e != cudaSuccess) return e;
     for (int g = 0; g < L.groups; ++g)
         if (L.W[g].slots) k_wave_init<<<(L.W[g].slots + 127) / 128, 128, 0, st>>>(L.W[g], L.V, L.P);

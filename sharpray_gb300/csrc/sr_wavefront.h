@@ -34,9 +34,9 @@ struct WaveState {
     uint32_t groups;   // number of groups
     // records of all groups, indexed by the global slot (tile * 32 + lane)
     Rec* rec;          // path records, six sectors per slot (192 bytes, 64-byte aligned):
-                       //   ray  a: origin, bounce index (int bits)      b: direction, -
+                       //   ray  a: origin, bounce index (int bits)      b: direction, fog scatter distance
                        //   hit  a: object, triangle (int bits), world distance, local distance
-                       //        b: barycentric u, v, fog scatter distance, -
+                       //        b: barycentric u, v, -, -  (written for surface events only)
                        //   path a: radiance, pdf of the last scatter    b: throughput, path flags (int bits)
                        //   rng  a: RNG words s0..s3 (bits)              b: RNG counter s4 (bits), fog radiance
                        //   sh0  a: shadow origin (then transmittance)   b: shadow direction, light pdf
@@ -56,10 +56,23 @@ struct WaveState {
     uint32_t* q_late[2];    // finished samples whose last shadow ray is still to trace (ping-pong)
     uint32_t* q_resolve;    // finished samples without a shadow ray to trace
     uint32_t* counts;       // this group's counters, kCount* below
+    uint32_t rec_stride;    // slots of all groups (record kind k of slot s at k * rec_stride + s)
+    uint8_t* ev_mark;       // per global slot, 1 + its event while this bounce's queues are sorted
+    uint32_t* q_sorted;     // this bounce's event queues in slot order, three of `slots` entries
 };
 
+// Path and pixel records as one array per record kind (SR_REC_SOA = 1) or six / four records per
+// slot back to back (0).  With event queues in slot order (SR_SORT_EVENTS = 1) neighbouring
+// threads of the shade and finalize kernels then touch neighbouring records.
+#ifndef SR_REC_SOA
+#define SR_REC_SOA 0
+#endif
+#ifndef SR_SORT_EVENTS
+#define SR_SORT_EVENTS 1
+#endif
+
 // Number of 32-bit counters at WaveState::counts, and their layout.
-constexpr int kWaveCounters = 16;
+constexpr int kWaveCounters = 20;
 enum : int {
     kCountResolve = 0,     // samples finished this bounce without a shadow ray to trace
     kCountIter = 1,        // bounces run by the device loop
@@ -68,6 +81,7 @@ enum : int {
     kCountShadow = 6,      // + parity: shadow-queue length
     kCountLate = 8,        // + parity: late finished samples
     kCountEvent = 10,      // + 3 * parity + event: event-queue lengths
+    kCountSorted = 16,     // + event: fill cursors of the slot-ordered event queues
 };
 // Paths alive for the bounce of the given parity: queued for a traversal, with a known event, or
 // finished with their last shadow ray still to trace.
@@ -90,6 +104,7 @@ struct WaveLaunch {
     unsigned long long* counters;
     int grid_trace, grid_shadow, grid_finalize;
     int grid_shade[3];  // per event kernel (fog, miss, surface), or [0] for the sorted kernel
+    int grid_mark;      // k_event_mark (grid-stride over the event queues)
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
     uint32_t tail_paths;  // the bounce loop stops when at most this many paths are live; the tail
@@ -112,7 +127,7 @@ struct WaveGroups {
 #ifndef SR_SPLIT_SHADE
 #define SR_SPLIT_SHADE 1
 #endif
-constexpr int kWaveKernelsPerBounce = SR_SPLIT_SHADE ? 6 : 4;
+constexpr int kWaveKernelsPerBounce = (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 2 : 0);
 
 void wave_grid_sizes(WaveLaunch& L, int sms);
 // Counters of every group (contiguous, kWaveCounters per group) cleared, first camera rays.
