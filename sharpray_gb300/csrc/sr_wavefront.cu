@@ -130,12 +130,11 @@ __device__ __forceinline__ void push_block(uint32_t* const (&q)[NQ], uint32_t* c
         if (pred[i]) q[i][off[i]] = value;
 }
 
-// Ray-queue entries carry the ray itself (origin + slot, direction + bounce index), so that a
-// traversal kernel starts a ray with one coalesced load instead of a queue load followed by a
-// scattered record load.
-__device__ __forceinline__ Rec ray_entry(uint32_t slot, V3 o, V3 d, uint32_t bounce) {
-    return {make_float4(o.x, o.y, o.z, __int_as_float((int)slot)),
-            make_float4(d.x, d.y, d.z, __int_as_float((int)bounce))};
+// Ray-queue entries carry the ray itself (origin + slot, direction + the path ray's fog scatter
+// distance), so that a traversal kernel starts a ray with one coalesced load instead of a queue
+// load followed by a scattered record load.
+__device__ __forceinline__ Rec ray_entry(uint32_t slot, V3 o, V3 d, float fog_t) {
+    return {make_float4(o.x, o.y, o.z, __int_as_float((int)slot)), make_float4(d.x, d.y, d.z, fog_t)};
 }
 
 __device__ __forceinline__ Rng rng_of(const Rec& g) {
@@ -143,6 +142,16 @@ __device__ __forceinline__ Rng rng_of(const Rec& g) {
 }
 __device__ __forceinline__ Rec rng_rec(const Rng& r, Col fog) {
     return {make_float4(fbits(r.s0), fbits(r.s1), fbits(r.s2), fbits(r.s3)), make_float4(fbits(r.s4), fog.r, fog.g, fog.b)};
+}
+
+// The fog free-flight draw of a path ray (Fog.ScatterDistance scene.cs:478-496 without its end
+// test): the scatter distance, or +inf when the ray cannot scatter (or the scene has no fog, in
+// which case nothing is drawn).  The segment scatters when this is nearer than its closest hit.
+__device__ __forceinline__ float fog_scatter_t(const DevScene& S, const Ray& ray, Rng& rng) {
+    const float inf = __int_as_float(0x7f800000);
+    float t = inf;
+    if (S.has_fog && !fog_scatter_distance(S, ray, inf, rng, t)) t = inf;
+    return t;
 }
 
 // Start of a sample: the camera ray and a reset path (scene.cs:633-638).
@@ -153,7 +162,7 @@ __device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, con
     st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, black()));
 }
 
-__global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevParams P) {
+__global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevScene S, DevView V, DevParams P) {
     __shared__ uint32_t sh[2][1][kBlockWarps + 1];
     const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;  // index among this group's slots
     const uint32_t s = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);
@@ -165,7 +174,7 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
         if (valid) {
             Rng rng = rng_seed(x, y);
             Ray ray = camera_ray(V, P, x, y, rng);
-            begin_sample(W, s, ray, rng);
+            begin_sample(W, s, ray, rng, fog_scatter_t(S, ray, rng));
             float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
             st_rec(&W.pix[pix(W, s, X_ACC)], Rec{z, z});
             st_rec(&W.pix[pix(W, s, X_ACC + 1)], Rec{z, z});
@@ -176,31 +185,26 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevView V, DevPa
     block_offsets<1>({&W.counts[kCountTrace]}, {valid}, sh, 0u, off);
     if (valid) {
         Rec r = ld_rec(&W.rec[rix(W, s, R_RAY)]);
-        W.q_trace[0][off[0]] = ray_entry(s, V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z}, 0u);
+        W.q_trace[0][off[0]] = ray_entry(s, V3{r.a.x, r.a.y, r.a.z}, V3{r.b.x, r.b.y, r.b.z}, r.b.w);
     }
 }
 
 // The event of a segment whose closest hit is known (scene.cs:654-738 decides in this order):
 // with fog set, the free-flight distance is drawn first -- the segment's first RNG draw -- and wins
 // if it is shorter than the hit; else a hit is a surface event and no hit a miss.
-__device__ __forceinline__ int segment_event(const DevScene& S, const Ray& ray, bool has_hit, float hit_dist, Rng& rng,
-                                             float& sdist) {
-    sdist = 0.f;
-    if (S.has_fog && fog_scatter_distance(S, ray, has_hit ? hit_dist : __int_as_float(0x7f800000), rng, sdist))
-        return EV_FOG;
+__device__ __forceinline__ int segment_event(float fog_t, bool has_hit, float hit_dist) {
+    if (fog_t < (has_hit ? hit_dist : __int_as_float(0x7f800000))) return EV_FOG;
     return has_hit ? EV_SURF : EV_MISS;
 }
 
-// A new path ray (scatter or camera ray): -1 when it needs the next trace kernel's traversal; when
-// it misses both root children of the scene BVH -- the first thing the traversal tests -- it has
-// no hit, and its segment's event is returned with the fog scatter distance in `sdist` (the
-// caller stores it with the ray, as the trace kernel does).
+// A new path ray (scatter or camera ray) with fog scatter distance fog_t: -1 when it needs the
+// next trace kernel's traversal; when it misses both root children of the scene BVH -- the first
+// thing the traversal tests -- it has no hit, and its segment's event is returned.
 template <bool COUNT>
-__device__ __forceinline__ int next_segment(const DevScene& S, const Ray& ray, Rng& rng, Ctr& c, float& sdist) {
-    sdist = 0.f;
+__device__ __forceinline__ int next_segment(const DevScene& S, const Ray& ray, float fog_t, Ctr& c) {
     if (!misses_scene<COUNT, false>(S, ray, c)) return -1;
     SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-    return segment_event(S, ray, false, 0.f, rng, sdist);
+    return segment_event(fog_t, false, 0.f);
 }
 
 // Per-warp staging of the persistent loop's appends to NQ queues: entries collect in a shared
@@ -289,9 +293,9 @@ constexpr int kLeafWait = SR_LEAF_WAIT;
 
 // Persistent ray loop: lanes take entries [fetch counter) of the concatenation of two ray queues
 // -- q0 closest-hit queries, q1 occlusion queries -- until both are exhausted; `start(any)` is
-// called as a query begins, `finish(slot, tag, any, hit, ray)` (tag: the entry's bounce index)
-// stores its answer and returns an output code that `emit(slot, code)` (all lanes together, -1 =
-// none) passes on.
+// called as a query begins, `finish(slot, tag, any, hit, ray)` (tag: the bits of the entry's fog
+// scatter distance) stores its answer and returns an output code that `emit(slot, code)` (all
+// lanes together, -1 = none) passes on.
 // Each round runs the node visits of all lanes together (up to kNodeBurst), then one leaf action
 // of each lane that waits for one: leaf actions are long and differ between lanes, so batching
 // them keeps warps from running each one with a single lane.  Finished lanes are answered in a
@@ -355,21 +359,11 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
     }
 }
 
-// The closest hit of slot s's ray (at bounce index `bounce`) is known: store the ray and its hit
-// (one whole 64-byte record pair) and decide the segment's event.
-__device__ __forceinline__ int extend_answer(const WaveState& W, const DevScene& S, uint32_t s, const Hit& h,
-                                             const Ray& ray, uint32_t bounce) {
-    float sdist = 0.f;
-    int ev = h.obj >= 0 ? EV_SURF : EV_MISS;
-    if (S.has_fog) {
-        Rec g = ld_rec(&W.rec[rix(W, s, R_RNG)]);
-        Rng rng = rng_of(g);
-        ev = segment_event(S, ray, h.obj >= 0, h.dist, rng, sdist);
-        st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, Col{g.b.y, g.b.z, g.b.w}));
-    }
-    // the fog scatter distance travels with the ray; only a surface event needs the hit record
-    st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                      make_float4(ray.d.x, ray.d.y, ray.d.z, sdist)});
+// The closest hit of slot s's path ray (fog scatter distance fog_t) is known: decide the
+// segment's event and store the hit a surface event needs.  (The ray record was written when the
+// ray was made.)
+__device__ __forceinline__ int extend_answer(const WaveState& W, uint32_t s, const Hit& h, float fog_t) {
+    const int ev = segment_event(fog_t, h.obj >= 0, h.dist);
     if (ev == EV_SURF)
         st_rec(&W.rec[rix(W, s, R_HIT)], Rec{make_float4(__int_as_float(h.obj), __int_as_float(h.tri), h.dist, h.tl),
                                           make_float4(h.u, h.v, 0.f, 0.f)});
@@ -412,7 +406,8 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveSta
         &W.counts[kCountTraceFetch], c, err,
         [&](bool any) { SR_COUNT(c, any ? SR_COUNTER_SCENE_OCCLUDE : SR_COUNTER_SCENE_TRACE, 1); },
         [&](uint32_t s, uint32_t bounce, bool any, const Hit& h, const Ray& ray) {
-            if (!any) return extend_answer(W, S, s, h, ray, bounce);
+            (void)ray;
+            if (!any) return extend_answer(W, s, h, __uint_as_float(bounce));
             float tr = 0.0f;
             if (h.obj < 0) {
                 tr = 1.0f;
@@ -479,7 +474,7 @@ struct SegOut {
     int next = -1;
     V3 sh_o{0.f, 0.f, 0.f}, sh_d{0.f, 0.f, 0.f};  // the shadow ray, when traced
     V3 nx_o{0.f, 0.f, 0.f}, nx_d{0.f, 0.f, 0.f};  // the next ray, when traced
-    uint32_t nx_bounce = 0;                        // ... and its bounce index
+    float nx_t = 0.f;                              // ... and its fog scatter distance
 };
 
 // One segment of path slot s whose event is ev (scene.cs:640-738): first the NEE contribution of
@@ -623,15 +618,15 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
         st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
                      make_float4(energy.r, energy.g, energy.b, fbits(pflags))});
         if (o.live) {
-            float sd;
-            o.next = next_segment<COUNT>(S, ray, rng, c, sd);
+            // the next segment's fog free-flight draw: the reference makes it right after the
+            // traversal, which draws nothing, so drawing it now keeps the RNG sequence
+            const float ft = fog_scatter_t(S, ray, rng);
+            o.next = next_segment<COUNT>(S, ray, ft, c);
             o.nx_o = ray.o;
             o.nx_d = ray.d;
-            o.nx_bounce = bounce;
-            // a traced ray's record is written by the trace kernel together with its hit
-            if (o.next >= 0)
-                st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                                  make_float4(ray.d.x, ray.d.y, ray.d.z, sd)});
+            o.nx_t = ft;
+            st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
+                                              make_float4(ray.d.x, ray.d.y, ray.d.z, ft)});
         }
         st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, fog));
     return o;
@@ -730,12 +725,12 @@ __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveS
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve],
                           &W.counts[kCountLate + nxt], &W.counts[kCountShadow + nxt]},
                          pred, sh, round++, off);
-        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_bounce);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_t);
         if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
         if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
         if (pred[3]) W.q_resolve[off[3]] = s;
         if (pred[4]) W.q_late[nxt][off[4]] = s;
-        if (pred[5]) W.q_shadow[nxt][off[5]] = ray_entry(s, o.sh_o, o.sh_d, 0u);
+        if (pred[5]) W.q_shadow[nxt][off[5]] = ray_entry(s, o.sh_o, o.sh_d, 0.f);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -801,12 +796,13 @@ __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevS
         } else {
             Rng rng = rng_of(gr);
             Ray ray = camera_ray(V, P, x, y, rng);
-            float sd;
-            o.next = next_segment<COUNT>(S, ray, rng, c, sd);
-            begin_sample(W, s, ray, rng, sd);
+            const float ft = fog_scatter_t(S, ray, rng);
+            o.next = next_segment<COUNT>(S, ray, ft, c);
+            begin_sample(W, s, ray, rng, ft);
             o.live = true;
             o.nx_o = ray.o;
             o.nx_d = ray.d;
+            o.nx_t = ft;
         }
         a4.y = fbits(ncount), a4.z = fbits(dcount), a4.w = fbits(si);
         st_rec(&W.pix[pix(W, s, X_ACC)], Rec{a0, a1});
@@ -847,7 +843,7 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
         block_offsets<3>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
                          pred, sh, round++, off);
-        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, 0u);
+        if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_t);
         if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
         if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
     }
@@ -870,7 +866,8 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     int group = -1, ev = -1;
-    uint32_t s = 0, bounce = 0;
+    uint32_t s = 0;
+    float rt = 0.f;
     V3 ro{0.f, 0.f, 0.f}, rd{0.f, 0.f, 0.f};  // the ray of a segment that needs a traversal
     for (int g = 0; g < G.groups && group < 0; ++g) {
         const WaveState& Wg = G.W[g];
@@ -879,7 +876,7 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
             group = g;
             Rec e = Wg.q_trace[cur][k];
             s = (uint32_t)__float_as_int(e.a.w);
-            bounce = (uint32_t)__float_as_int(e.b.w);
+            rt = e.b.w;
             ro = V3{e.a.x, e.a.y, e.a.z};
             rd = V3{e.b.x, e.b.y, e.b.z};
             break;
@@ -925,7 +922,7 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
                 if (ev < 0) {
                     Ray ray = make_ray(ro, rd);
                     SR_COUNT(c, SR_COUNTER_SCENE_TRACE, 1);
-                    ev = extend_answer(W, S, s, scene_closest<COUNT, GENERAL>(S, ray, c, err), ray, bounce);
+                    ev = extend_answer(W, s, scene_closest<COUNT, GENERAL>(S, ray, c, err), rt);
                 }
                 o = shade_segment<COUNT, GENERAL>(W, S, P, s, ev, c);
                 if (o.shadow) shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(o.sh_o, o.sh_d), c, err);
@@ -935,7 +932,7 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
                 if (!o.live) break;
             }
             ev = o.next;
-            ro = o.nx_o, rd = o.nx_d, bounce = o.nx_bounce;
+            ro = o.nx_o, rd = o.nx_d, rt = o.nx_t;
         }
     }
     flush_counters<COUNT>(c, counters);
@@ -1054,7 +1051,7 @@ cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {
     if (e == cudaSuccess && SR_SORT_EVENTS) e = cudaMemsetAsync(L.W[0].ev_mark, 0, L.W[0].rec_stride, st);
     if (e != cudaSuccess) return e;
     for (int g = 0; g < L.groups; ++g)
-        if (L.W[g].slots) k_wave_init<<<(L.W[g].slots + 127) / 128, 128, 0, st>>>(L.W[g], L.V, L.P);
+        if (L.W[g].slots) k_wave_init<<<(L.W[g].slots + 127) / 128, 128, 0, st>>>(L.W[g], L.S, L.V, L.P);
     return cudaGetLastError();
 }
 
