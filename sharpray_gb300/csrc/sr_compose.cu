@@ -7,7 +7,10 @@
 // and {normal.xyz, depth}, plus {fog.rgb, 0}, so that every filter tap is two 128-bit loads and
 // the neighbour luminance is not recomputed per tap.  The taps of a pixel are visited in the
 // reference order (rows top to bottom, columns left to right) so the weighted sums accumulate
-// in the same order; the spatial weights exp(-d^2 / 2r^2) come from a host-evaluated table.
+// in the same order; the spatial weights exp(-d^2 / 2r^2) come from a host-evaluated table.  Per
+// tap the normal, depth and luminance Gaussians are one fast exponential of their summed
+// exponents and the sums accumulate with fused multiply-adds: the filter is the reference's up to
+// float rounding (images agree within one code value).
 #include <cuda_runtime.h>
 
 #include "sr_device.cuh"
@@ -92,20 +95,25 @@ __global__ void __launch_bounds__(128) k_compose(const float4* __restrict__ p_ra
                     if (has_n != nh_n || has_d != nh_d) continue;
                     float4 q0 = __ldg(prow + kx);
                     float w = dw * __ldg(wrow + kx);
-                    if (has_n && w > 0.0f) {
-                        V3 nd = cn - nn;
-                        w *= expf(-mag_sqr(nd) * k.normal_limit_inv);
-                    }
-                    if (has_d && w > 0.0f) {
-                        float dd = cd - q1.w;
-                        w *= expf(-(dd * dd) * k.depth_limit_inv);
-                    }
+                    // the normal, depth and luminance Gaussians of compose.cs:165-190 as one
+                    // exponential of the summed exponents (equal up to rounding; a weight the
+                    // reference zeroes by underflow stays zero)
                     if (w > 0.0f) {
+                        float e = 0.0f;
+                        if (has_n) {
+                            V3 nd = cn - nn;
+                            e = mag_sqr(nd) * k.normal_limit_inv;
+                        }
+                        if (has_d) {
+                            float dd = cd - q1.w;
+                            e = __fmaf_rn(dd * dd, k.depth_limit_inv, e);
+                        }
                         float ld = fmaxf(0.0f, q0.w - lum);
-                        w *= expf(-(ld * ld) * k.lum_limit_inv);
+                        e = __fmaf_rn(ld * ld, k.lum_limit_inv, e);
+                        w *= __expf(-e);
                     }
                     wsum += w;
-                    rsum = rsum + col3(q0) * w;
+                    rsum = Col{__fmaf_rn(q0.x, w, rsum.r), __fmaf_rn(q0.y, w, rsum.g), __fmaf_rn(q0.z, w, rsum.b)};
                 }
             }
             main = rsum / wsum;
@@ -126,8 +134,9 @@ __global__ void __launch_bounds__(128) k_compose(const float4* __restrict__ p_ra
                 for (int kx = kx0; kx <= kx1; ++kx) {
                     if (kx == 0 && ky == 0) continue;
                     float w = __ldg(wrow + kx);
+                    float4 f = __ldg(frow + kx);
                     wsum += w;
-                    rsum = rsum + col3(__ldg(frow + kx)) * w;
+                    rsum = Col{__fmaf_rn(f.x, w, rsum.r), __fmaf_rn(f.y, w, rsum.g), __fmaf_rn(f.z, w, rsum.b)};
                 }
             }
             fog = rsum / wsum;
