@@ -803,9 +803,16 @@ SR_DEV uint32_t cdf_sample(const float* cdf, const uint32_t* guide, uint32_t n, 
     return min(lo, n - 1);
 }
 
-// ISky.LightDirRand (SkyTexture scene.cs:408-416, SunProcedural scene.cs:314-323).
+// The direction toward the centre of sky texel (x, y) (SkyTexture.LightDirRand scene.cs:412-415).
+SR_DEV V3 sky_texel_dir(const DevSky& k, const DevTexture& t, uint32_t x, uint32_t y) {
+    V2 uv{((float)(int)x + 0.5f) / (float)(int)t.width, ((float)(int)y + 0.5f) / (float)(int)t.height};
+    return quat_rotate(k.rot, from_equirect_uv(uv));
+}
+
+// ISky.LightDirRand (SkyTexture scene.cs:408-416, SunProcedural scene.cs:314-323).  `texel` is the
+// sampled texel of a texture sky (-1 otherwise), whose radiance sky_light_radiance then reads.
 template <bool COUNT, bool GENERAL = true>
-SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr& c) {
+SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, int& texel, Ctr& c) {
     const DevSky& k = S.sky;
     if (!GENERAL || k.kind == 0) {
         if (k.cdf_total <= 0.0f) return false;
@@ -815,11 +822,13 @@ SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr
         uint32_t y = cdf_sample<COUNT>(k.cdf_marginal, k.guide_marginal, t.height, u.y, c);
         size_t row = (size_t)y * (t.width + 1);
         uint32_t x = cdf_sample<COUNT>(k.cdf_cond + row, k.guide_cond + row, t.width, u.x, c);
-        V2 uv{((float)(int)x + 0.5f) / (float)(int)t.width, ((float)(int)y + 0.5f) / (float)(int)t.height};
-        dir = quat_rotate(k.rot, from_equirect_uv(uv));
-        pdf = luminance(col3(ldg4(S.texels + t.offset + (size_t)y * t.width + x))) * k.pdf_scale;
+        dir = sky_texel_dir(k, t, x, y);
+        texel = (int)((size_t)y * t.width + x);
+        pdf = k.center ? ldg4(k.center + texel).w
+                       : luminance(col3(ldg4(S.texels + t.offset + (size_t)y * t.width + x))) * k.pdf_scale;
         return pdf > 0.0f;
     }
+    texel = -1;
     float phi = (kPi * 2.0f) * rng_float(rng);
     float blend = sqrtf(rng_float(rng));
     float z = k.sun_cos + (1.0f - k.sun_cos) * blend;
@@ -829,6 +838,24 @@ SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr
     dir = quat_rotate(k.sun_rot, V3{cp * st, sp * st, z});
     pdf = blend / k.sun_pdf_denom;
     return true;
+}
+
+template <bool COUNT, bool GENERAL = true>
+SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr& c) {
+    int texel;
+    return sky_light_rand<COUNT, GENERAL>(S, rng, dir, pdf, texel, c);
+}
+
+// Sky radiance toward a light sample's direction: for a sampled texel of a texture sky the value
+// evaluated at scene build (the same sky_radiance of the same direction, so the same bits), one
+// 16-byte load next to the pdf just read instead of a bilinear lookup.
+template <bool COUNT, bool GENERAL = true>
+SR_DEV Col sky_light_radiance(const DevScene& S, int texel, V3 dir, Ctr& c) {
+    if (texel >= 0 && S.sky.center) {
+        SR_COUNT(c, SR_COUNTER_TEX_SAMPLE, 1);
+        return col3(ldg4(S.sky.center + texel));
+    }
+    return sky_radiance<COUNT, GENERAL>(S, dir, c);
 }
 
 // ---- fog (scene.cs:445-496) -----------------------------------------------------------------------

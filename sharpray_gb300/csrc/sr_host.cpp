@@ -133,7 +133,7 @@ struct SrScene {
     BvhHost tlas;
     // device state
     DevScene dev{};
-    DevBuf nodes, tris, attrs, objs, mats, texs, texels, cdf_marginal, cdf_cond, guide_marginal, guide_cond;
+    DevBuf nodes, tris, attrs, objs, mats, texs, texels, cdf_marginal, cdf_cond, guide_marginal, guide_cond, sky_center;
     DevBuf err, counters;
     DevBuf aovs;  // staging for sr_render
     DevBuf rays_io;
@@ -675,6 +675,15 @@ SR_API int sr_scene_build(SrScene* s) {
         d.fog_falloff = s->fog.height_falloff;
         d.fog_g = s->fog.anisotropy;
         d.fog_color = mk4(s->fog.color[0], s->fog.color[1], s->fog.color[2], 0);
+    }
+    d.sky.center = nullptr;
+    if (ctx->device >= 0 && s->sky_kind == 0 && sky.cdf_total > 0.0f) {
+        const TextureHost& t = *ctx->textures[s->sky_texture];
+        const size_t n = (size_t)t.width * t.height;
+        SR_CUDA(s->sky_center.reserve(n * sizeof(float4)), "alloc sky table");
+        SR_CUDA(launch_sky_table(d, s->sky_center.as<float4>(), (uint32_t)n, st), "sky table");
+        SR_CUDA(cudaStreamSynchronize(st), "sky table");
+        d.sky.center = s->sky_center.as<float4>();
     }
     s->built = true;
     return SR_OK;

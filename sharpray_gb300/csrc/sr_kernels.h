@@ -21,6 +21,9 @@ struct DevAovs {
 cudaError_t launch_render(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& out,
                           unsigned long long* counters, uint32_t* err, cudaStream_t stream);
 
+// Sky table of a texture sky (DevSky::center), `texels` = width x height (sr_render.cu).
+cudaError_t launch_sky_table(const DevScene& S, float4* out, uint32_t texels, cudaStream_t stream);
+
 // Closest hit per world ray (sr_render.cu).
 cudaError_t launch_trace(const DevScene& S, const float* rays, uint32_t n, int32_t* obj, int32_t* tri, float* dist,
                          float* uv, uint32_t* err, cudaStream_t stream);

@@ -71,6 +71,8 @@ struct SR_ALIGN16 DevSky {
     const float* cdf_cond;           // height * (width + 1) floats
     const uint32_t* guide_marginal;  // height + 1 bucket bounds of the marginal search
     const uint32_t* guide_cond;      // height * (width + 1) bucket bounds of the row searches
+    const float4* center;            // per texel: the sky radiance toward its centre (xyz) and its light
+                                     // pdf (w), evaluated on the device at scene build (null: none)
     float4 top, middle, bottom, sun_dir, sun_radiance, sun_rot;
 };
 

@@ -192,6 +192,29 @@ cudaError_t launch_render(const DevScene& S, const DevView& V, const DevParams& 
     return cudaGetLastError();
 }
 
+// Per texel of a texture sky: the radiance toward the texel's centre -- the direction a light
+// sample of that texel takes -- and the texel's light pdf (SkyTexture.LightDirRand scene.cs:408-416),
+// with the functions the path code uses, so a light sample reads one record instead of a bilinear
+// lookup.
+__global__ void k_sky_table(DevScene S, float4* out) {
+    const DevSky& k = S.sky;
+    const DevTexture& t = S.textures[k.texture];
+    const uint32_t n = t.width * t.height;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % t.width, y = i / t.width;
+        Ctr c;
+        const Col L = sky_radiance<false, true>(S, sky_texel_dir(k, t, x, y), c);
+        const float pdf = luminance(col3(ldg4(S.texels + t.offset + (size_t)y * t.width + x))) * k.pdf_scale;
+        out[i] = make_float4(L.r, L.g, L.b, pdf);
+    }
+}
+
+cudaError_t launch_sky_table(const DevScene& S, float4* out, uint32_t texels, cudaStream_t stream) {
+    if (texels == 0) return cudaSuccess;
+    k_sky_table<<<(texels + 255) / 256 < 4096 ? (texels + 255) / 256 : 4096, 256, 0, stream>>>(S, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_trace(const DevScene& S, const float* rays, uint32_t n, int32_t* obj, int32_t* tri, float* dist,
                          float* uv, uint32_t* err, cudaStream_t stream) {
     if (n == 0) return cudaSuccess;

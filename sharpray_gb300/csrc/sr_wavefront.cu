@@ -458,7 +458,8 @@ __device__ __forceinline__ void add_nee(const WaveState& W, const DevScene& S, u
     if (max_component(tr) > 0.0f) {
         Rec r1 = ld_rec(&W.rec[rix(W, s, R_SH1)]);
         V3 ldir{r0.b.x, r0.b.y, r0.b.z};
-        Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * col3(r1.a) * r1.a.w / r0.b.w;
+        Col contrib = sky_light_radiance<COUNT, GENERAL>(S, __float_as_int(r1.b.w), ldir, c) * tr * col3(r1.a) * r1.a.w /
+                      r0.b.w;
         Col add = contrib * col3(r1.b);
         if (pflags & PF_NEE_FOG)
             fog = fog + add;
@@ -531,7 +532,8 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
             // added next segment (before anything of that segment touches the radiance)
             V3 ldir;
             float lpdf;
-            if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) && lpdf > 0.0f) {
+            int texel;
+            if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, texel, c) && lpdf > 0.0f) {
                 bool emit = true;
                 Col w3;
                 float mis;
@@ -561,7 +563,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
                         if (S.has_fog) t = 1.0f * fog_transmittance_inf(S, shadow);
                         Col tr = gray(t);
                         if (max_component(tr) > 0.0f) {
-                            Col contrib = sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * w3 * mis / lpdf;
+                            Col contrib = sky_light_radiance<COUNT, GENERAL>(S, texel, ldir, c) * tr * w3 * mis / lpdf;
                             Col add = contrib * energy;
                             if (to_fog)
                                 fog = fog + add;
@@ -577,7 +579,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
                         st_rec(&W.rec[rix(W, s, R_SH0)], Rec{make_float4(pos.x, pos.y, pos.z, 0.f),
                                                           make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
                         st_rec(&W.rec[rix(W, s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
-                                                          make_float4(energy.r, energy.g, energy.b, 0.f)});
+                                                          make_float4(energy.r, energy.g, energy.b, __int_as_float(texel))});
                     }
                 }
             }

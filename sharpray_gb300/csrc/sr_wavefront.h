@@ -40,7 +40,8 @@ struct WaveState {
                        //   path a: radiance, pdf of the last scatter    b: throughput, path flags (int bits)
                        //   rng  a: RNG words s0..s3 (bits)              b: RNG counter s4 (bits), fog radiance
                        //   sh0  a: shadow origin (then transmittance)   b: shadow direction, light pdf
-                       //   sh1  a: reflectance or phase pdf, MIS weight b: throughput at the light sample
+                       //   sh1  a: reflectance or phase pdf, MIS weight b: throughput at the light sample,
+                       //                                                  sampled sky texel (int bits)
     Rec* pix;          // pixel records, four sectors per slot:
                        //   prim a: primary-hit normal, depth            b: primary-hit uv, -, -
                        //   acc0 a: radiance sum, luminance sum          b: fog radiance sum, luminance^2 sum
