@@ -289,6 +289,14 @@ constexpr int kRefill = SR_REFILL;
 #endif
 constexpr int shade_min_blocks(int ev) { return ev == 0 || ev == 1 ? SR_SHADE_FOG_MIN_BLOCKS : SR_SHADE_MIN_BLOCKS; }
 constexpr int kNodeBurst = SR_NODE_BURST;
+// Order in which the persistent loop takes queries (bit 2: occlusion queue first; bits 0 / 1:
+// closest-hit / occlusion queue from its end).  A bounce's traversal kernel ends with a ramp-down
+// in which SMs run out of queries while a few long ones finish, so the order matters: the default
+// 5 takes the shadow rays first, then the path rays from the end of their queue (camera rays and
+// surface bounces first, fog scatters last) -- measured 2 % faster than queue order on C2.
+#ifndef SR_TRACE_ORDER
+#define SR_TRACE_ORDER 5
+#endif
 constexpr int kLeafWait = SR_LEAF_WAIT;
 
 // Persistent ray loop: lanes take entries [fetch counter) of the concatenation of two ray queues
@@ -330,8 +338,12 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
             if (!busy) {
                 uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
                 if (idx < n) {
-                    const bool any = idx >= n0;
-                    Rec e = any ? q1[idx - n0] : q0[idx];
+                    // fetch order: bit 2 of SR_TRACE_ORDER puts the occlusion queue first, bits 0
+                    // and 1 walk the closest-hit / occlusion queue from its end
+                    const bool sfirst = (SR_TRACE_ORDER & 4) != 0;
+                    const bool any = sfirst ? idx < n1 : idx >= n0;
+                    const uint32_t j = sfirst ? (any ? idx : idx - n1) : (any ? idx - n0 : idx);
+                    Rec e = any ? q1[(SR_TRACE_ORDER & 2) ? n1 - 1 - j : j] : q0[(SR_TRACE_ORDER & 1) ? n0 - 1 - j : j];
                     slot = (uint32_t)__float_as_int(e.a.w);
                     tag = (uint32_t)__float_as_int(e.b.w);
                     start(any);
