@@ -69,6 +69,9 @@ __device__ __forceinline__ size_t pix(const WaveState& W, uint32_t s, int k) {
     return SR_REC_SOA ? (size_t)k * W.rec_stride + s : 4 * (size_t)s + k;
 }
 
+// Tag of a slot whose event `ev` is shaded by the bounce of parity `parity` (0: none).
+__device__ __forceinline__ uint8_t event_mark(int ev, int parity) { return (uint8_t)(1 + ev + 3 * parity); }
+
 // Record loads and stores (one place to change how path state is moved).
 __device__ __forceinline__ Rec ld_rec(const Rec* p) { return *p; }
 __device__ __forceinline__ void st_rec(Rec* p, const Rec& v) { *p = v; }
@@ -428,7 +431,10 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveSta
             st4(&W.rec[rix(W, s, R_SH0)].a, make_float4(tr, tr, tr, 0.f));
             return -1;
         },
-        [&](uint32_t s, int ev) { stage.add(eq, ec, s, ev); });
+        [&](uint32_t s, int ev) {
+            stage.add(eq, ec, s, ev);
+            if (ev >= 0) W.ev_mark[s] = event_mark(ev, cur);
+        });
     stage.flush(eq, ec);
     flush_counters<COUNT>(c, counters);
 }
@@ -647,35 +653,40 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
 }
 
 // The event queues of this bounce in slot order, so that the shade kernels' neighbouring threads
-// work on neighbouring slots: k_event_mark tags each queued slot with its event, k_event_sort
-// scans the slots in order and appends each tagged slot to its event's sorted queue (one atomic
-// per block and event; inside a block's run the order is the slot order), clearing the tags.
-__global__ void __launch_bounds__(256) k_event_mark(WaveState W, int cur) {
-    const uint32_t* ecount = W.counts + kCountEvent + 3 * cur;
-    const uint32_t n0 = ecount[0], n1 = ecount[1], n2 = ecount[2];
-    const uint32_t total = n0 + n1 + n2;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
-        const uint32_t ev = k < n0 ? 0u : (k < n0 + n1 ? 1u : 2u);
-        const uint32_t i = k - (ev == 0 ? 0u : (ev == 1 ? n0 : n0 + n1));
-        const uint32_t s = W.q_event[cur][(size_t)ev * W.slots + i];
-        W.ev_mark[s] = (uint8_t)(1u + ev);
-    }
-}
-
-__global__ void __launch_bounds__(256) k_event_sort(WaveState W) {
+// work on neighbouring slots: every producer of an event also tags the slot with the event and
+// the parity of the bounce that shades it (event_mark), and k_event_sort scans the slots in order
+// -- four per thread -- appending each slot tagged for this bounce to its event's sorted queue
+// (one atomic per block and event; inside a block's run the order is the slot order) and
+// clearing its tag.  Tags for the next bounce (from a late finalize) are left in place.
+__global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur) {
     __shared__ uint32_t warp_n[3][8];
     __shared__ uint32_t base[3];
-    const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;  // group-local slot index
-    const uint32_t s = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);
-    const uint32_t m = li < W.slots ? W.ev_mark[s] : 0u;
-    if (m) W.ev_mark[s] = 0;
+    const uint32_t li = 4u * (blockIdx.x * blockDim.x + threadIdx.x);  // group-local slot index
+    const uint32_t s0 = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);  // 4 consecutive slots
+    uint32_t ev4[4];
+    uint32_t cnt[3] = {0, 0, 0};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        uint32_t m = li + j < W.slots ? W.ev_mark[s0 + j] : 0u;
+        const uint32_t e = m - 1u - 3u * (uint32_t)cur;  // event of this bounce, else >= 3
+        ev4[j] = e < 3u ? e : 3u;
+        if (e < 3u) {
+            W.ev_mark[s0 + j] = 0;
+            ++cnt[e];
+        }
+    }
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t rank[3];
+    uint32_t pre[3];
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
-        const uint32_t bal = __ballot_sync(0xffffffffu, m == (uint32_t)(e + 1));
-        rank[e] = __popc(bal & ((1u << lane) - 1u));
-        if (lane == 0) warp_n[e][warp] = __popc(bal);
+        uint32_t v = cnt[e];  // inclusive warp scan
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
+            if (lane >= (uint32_t)d) v += t;
+        }
+        pre[e] = v - cnt[e];
+        if (lane == 31) warp_n[e][warp] = v;
     }
     __syncthreads();
     if (threadIdx.x < 3) {
@@ -684,11 +695,16 @@ __global__ void __launch_bounds__(256) k_event_sort(WaveState W) {
         base[threadIdx.x] = t ? atomicAdd(&W.counts[kCountSorted + threadIdx.x], t) : 0u;
     }
     __syncthreads();
-    if (m) {
-        const int e = (int)m - 1;
-        uint32_t off = base[e] + rank[e];
-        for (uint32_t w = 0; w < warp; ++w) off += warp_n[e][w];
-        W.q_sorted[(size_t)e * W.slots + off] = s;
+    uint32_t off[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        off[e] = base[e] + pre[e];
+        for (uint32_t w = 0; w < warp; ++w) off[e] += warp_n[e][w];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t e = ev4[j];
+        if (e < 3u) W.q_sorted[(size_t)e * W.slots + off[e]++] = s0 + j;
     }
 }
 
@@ -740,8 +756,8 @@ __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveS
                           &W.counts[kCountLate + nxt], &W.counts[kCountShadow + nxt]},
                          pred, sh, round++, off);
         if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_t);
-        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
-        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
+        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s, W.ev_mark[s] = event_mark(EV_FOG, nxt);
+        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s, W.ev_mark[s] = event_mark(EV_MISS, nxt);
         if (pred[3]) W.q_resolve[off[3]] = s;
         if (pred[4]) W.q_late[nxt][off[4]] = s;
         if (pred[5]) W.q_shadow[nxt][off[5]] = ray_entry(s, o.sh_o, o.sh_d, 0.f);
@@ -858,8 +874,8 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
                          pred, sh, round++, off);
         if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_t);
-        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s;
-        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s;
+        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s, W.ev_mark[s] = event_mark(EV_FOG, nxt);
+        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s, W.ev_mark[s] = event_mark(EV_MISS, nxt);
     }
     flush_counters<COUNT>(c, counters);
 }
@@ -981,10 +997,7 @@ static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cuda
     }
     k_wave_finalize<COUNT, GENERAL, true><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
                                                                            L.counters);
-    if (SR_SORT_EVENTS) {
-        k_event_mark<<<L.grid_mark, 256, 0, st>>>(W, cur);
-        k_event_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W);
-    }
+    if (SR_SORT_EVENTS) k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, st>>>(W, cur);
     if (SR_SPLIT_SHADE) {
         k_wave_shade<COUNT, GENERAL, EV_FOG><<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
         k_wave_shade<COUNT, GENERAL, EV_MISS><<<L.grid_shade[1], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters);
@@ -1057,7 +1070,6 @@ void wave_grid_sizes(WaveLaunch& L, int sms) {
     L.grid_shade[0] = b[3];
     L.grid_shade[1] = b[4];
     L.grid_shade[2] = b[5];
-    L.grid_mark = sms * 8;
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {

@@ -58,7 +58,7 @@ struct WaveState {
     uint32_t* q_resolve;    // finished samples without a shadow ray to trace
     uint32_t* counts;       // this group's counters, kCount* below
     uint32_t rec_stride;    // slots of all groups (record kind k of slot s at k * rec_stride + s)
-    uint8_t* ev_mark;       // per global slot, 1 + its event while this bounce's queues are sorted
+    uint8_t* ev_mark;       // per global slot, 1 + event + 3 x parity of the bounce that shades it
     uint32_t* q_sorted;     // this bounce's event queues in slot order, three of `slots` entries
 };
 
@@ -105,7 +105,6 @@ struct WaveLaunch {
     unsigned long long* counters;
     int grid_trace, grid_shadow, grid_finalize;
     int grid_shade[3];  // per event kernel (fog, miss, surface), or [0] for the sorted kernel
-    int grid_mark;      // k_event_mark (grid-stride over the event queues)
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
     uint32_t tail_paths;  // the bounce loop stops when at most this many paths are live; the tail
@@ -128,7 +127,7 @@ struct WaveGroups {
 #ifndef SR_SPLIT_SHADE
 #define SR_SPLIT_SHADE 1
 #endif
-constexpr int kWaveKernelsPerBounce = (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 2 : 0);
+constexpr int kWaveKernelsPerBounce = (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 1 : 0);
 
 void wave_grid_sizes(WaveLaunch& L, int sms);
 // Counters of every group (contiguous, kWaveCounters per group) cleared, first camera rays.
