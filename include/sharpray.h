@@ -319,6 +319,15 @@ SR_API int sr_compose_device_static(SrContext* ctx, const SrAovs* device_aovs, u
 SR_API int sr_preview(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height,
                       const SrComposeParams* params, uint8_t* host_rgb8);
 
+/* Batched rendering (no counterpart in the reference, which renders one scene at a time): `count`
+ * distinct built scenes of one context, each with its view, parameters and device AOV planes
+ * (as sr_render_device), rendered by one CUDA graph launch on `stream` that holds one bounce
+ * loop per scene, run side by side.  Each scene's AOVs equal what sr_render_device gives it.  The
+ * graph is kept on the context and reused while the batch's scenes, views, parameters and
+ * buffers stay the same. */
+SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const SrRenderParams* params,
+                           const SrAovs* device_outs, uint32_t count, void* stream);
+
 /* ---- asset ingest (host-side file parsing) ------------------------------------------------- */
 /* Image.Load (image.cs:214-273: uncompressed 24-bit TrueColor / 8-bit Grayscale .tga, rows top-down)
  * or ImageHdr.Load (image.cs:307-382: Radiance .hdr, "-Y h +X w", new-style RLE or flat): sizes

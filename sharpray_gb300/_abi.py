@@ -173,6 +173,7 @@ PROTOTYPES = {
     "sr_compose_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
     "sr_compose_device_static": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
     "sr_preview": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P]),
+    "sr_render_batch": (_I, [_P, _P, _P, _P, _U, _P]),
     "sr_aov_image": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P]),
     "sr_aov_image_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P, _P]),
     "sr_overlay_draw": (_I, [_P, _P, _U, _U, C.POINTER(SrView), _P, _P, _U, _P, _U, C.POINTER(SrFont)]),

@@ -39,7 +39,7 @@ __all__ = [
     "Context", "Texture", "TextureFilter", "Mesh", "Sphere", "AABox", "Material", "Quat", "Transform", "Object",
     "SkyTexture", "SkyProcedural", "Fog", "Scene", "View", "Renderer", "Compositor", "Tonemapper",
     "SharpRayError", "StateError", "load_image", "mesh_triangles", "AovKind", "aov_image", "save_image", "Font",
-    "Overlay",
+    "Overlay", "render_batch",
 ]
 
 
@@ -759,6 +759,27 @@ def render_compose(scene: Scene, view: View, width: int, height: int, block_size
     a = C.byref(aovs.to_c()) if aovs is not None else None
     check(scene._lib.sr_render_compose(scene.handle, C.byref(v), C.byref(p), C.byref(cp), a, ptr(image)))
     return image, aovs
+
+
+def render_batch(scenes: Sequence["Scene"], views: Sequence["View"], params: Sequence[SrRenderParams],
+                 device_aovs: Sequence[SrAovs], stream: Optional[int] = None) -> None:
+    """sr_render_batch: several built scenes, each with its view, render parameters
+    (`render_params(...)`) and device AOV planes (an `SrAovs` of device pointers), in one graph
+    launch on `stream` (a CUDA stream handle; None = the context's).  Asynchronous."""
+    n = len(scenes)
+    if not (len(views) == len(params) == len(device_aovs) == n):
+        raise ValueError("scenes, views, params and device_aovs must have the same length")
+    if n == 0:
+        return
+    for s in scenes:
+        if not s.built:
+            s.build()
+    arr_s = (C.c_void_p * n)(*[s.handle.value for s in scenes])
+    arr_v = (_abi.SrView * n)(*[v.to_c() for v in views])
+    arr_p = (SrRenderParams * n)(*params)
+    arr_a = (SrAovs * n)(*device_aovs)
+    lib = scenes[0]._lib
+    check(lib.sr_render_batch(arr_s, arr_v, arr_p, arr_a, n, C.c_void_p(stream) if stream else None))
 
 
 def load_image(path) -> np.ndarray:

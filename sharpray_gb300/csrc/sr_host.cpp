@@ -110,6 +110,10 @@ struct SrContext {
     std::vector<float> table_host;
     // AOV images and overlay (host-buffer entry points stage through image_io)
     DevBuf image_io, overlay_scratch;
+    // batched rendering: the graph of the last batch and the launch descriptions baked into it
+    cudaStream_t batch_capture = nullptr;
+    cudaGraphExec_t batch_exec = nullptr;
+    std::vector<WaveLaunch> batch_launch;
 };
 
 struct SrScene {
@@ -291,6 +295,8 @@ SR_API int sr_ctx_destroy(SrContext* ctx) {
     if (ctx->device >= 0) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
+        if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
+        if (ctx->batch_capture) cudaStreamDestroy(ctx->batch_capture);
         cudaStreamDestroy(ctx->stream);
     }
     delete ctx;
@@ -837,8 +843,10 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
     return SR_OK;
 }
 
-static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& out,
-                            unsigned long long* ctr, cudaStream_t st, bool graph) {
+// The wavefront state of scene s reserved and initialised on `st` (first camera rays) for one
+// render, and the launch description of its bounce kernels in L.
+static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& out,
+                        unsigned long long* ctr, cudaStream_t st, WaveLaunch& L) {
     uint32_t tiles_x = (dp.width + 7) / 8, tiles_y = (dp.height + 3) / 4;
     int rc = wave_reserve(s, tiles_x, tiles_y);
     if (rc) return rc;
@@ -849,7 +857,6 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
     if (!s->sms) {
         SR_CUDA(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->ctx->device), "device query");
     }
-    WaveLaunch L;
     std::memset(&L, 0, sizeof(L));  // padding bytes take part in the graph-reuse comparison
     for (int g = 0; g < kWaveGroups; ++g) L.W[g] = s->ws[g];
     L.groups = kWaveGroups;
@@ -867,6 +874,13 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
     for (int g = 0; g < kWaveGroups; ++g) all_slots += s->ws[g].slots;
     L.tail_paths = SR_TAIL_DIV > 0 ? all_slots / SR_TAIL_DIV : 0;
     SR_CUDA(wave_init(L, st), "wavefront init");
+    return SR_OK;
+}
+
+static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& out,
+                            unsigned long long* ctr, cudaStream_t st, bool graph) {
+    WaveLaunch L;
+    if (int rc = wave_prepare(s, dv, dp, out, ctr, st, L)) return rc;
     if (graph) {
         if (!s->capture_stream) SR_CUDA(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking), "stream");
         if (s->graph_exec && std::memcmp(&s->graph_launch, &L, sizeof(L)) != 0) {
@@ -931,6 +945,60 @@ SR_API int sr_render_device(SrScene* s, const SrView* view, const SrRenderParams
     cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
     DevAovs d{out->radiance, out->radiance_fog, out->normals, out->uv, out->depth, out->samples, out->variance};
     return render_into(s, view, params, d, st);
+}
+
+SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const SrRenderParams* params,
+                           const SrAovs* outs, uint32_t count, void* stream) {
+    if (!scenes || !views || !params || !outs) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (count == 0) return SR_OK;
+    SrContext* ctx = scenes[0] ? scenes[0]->ctx : nullptr;
+    for (uint32_t i = 0; i < count; ++i) {
+        SrScene* s = scenes[i];
+        if (!s) return fail(SR_ERR_INVALID_ARG, "scene %u is NULL", i);
+        if (s->ctx != ctx) return fail(SR_ERR_INVALID_ARG, "scene %u belongs to another context", i);
+        if (int rc = need_device(s)) return rc;
+        for (uint32_t j = 0; j < i; ++j)
+            if (scenes[j] == s) return fail(SR_ERR_INVALID_ARG, "scene %u appears twice in the batch", i);
+        const SrAovs& o = outs[i];
+        if (!o.radiance || !o.radiance_fog || !o.normals || !o.uv || !o.depth || !o.samples || !o.variance)
+            return fail(SR_ERR_INVALID_ARG, "batch entry %u needs all seven AOV planes", i);
+    }
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    std::vector<WaveLaunch> Ls(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        SrScene* s = scenes[i];
+        DevView dv;
+        DevParams dp;
+        if (int rc = make_view(&views[i], &params[i], dv, dp)) return rc;
+        unsigned long long* ctr = nullptr;
+        if (s->counting) {
+            ctr = s->counters.as<unsigned long long>();
+            SR_CUDA(cudaMemsetAsync(ctr, 0, SR_COUNTER_COUNT * sizeof(unsigned long long), st), "clear counters");
+        }
+        const SrAovs& o = outs[i];
+        DevAovs d{o.radiance, o.radiance_fog, o.normals, o.uv, o.depth, o.samples, o.variance};
+        std::memset(&Ls[i], 0, sizeof(WaveLaunch));
+        if (int rc = wave_prepare(s, dv, dp, d, ctr, st, Ls[i])) return rc;
+        s->last_mode = SR_RENDER_WAVEFRONT_GRAPH;
+    }
+    if (!ctx->batch_capture) SR_CUDA(cudaStreamCreateWithFlags(&ctx->batch_capture, cudaStreamNonBlocking), "stream");
+    const bool same = ctx->batch_exec && ctx->batch_launch.size() == count &&
+                      std::memcmp(ctx->batch_launch.data(), Ls.data(), count * sizeof(WaveLaunch)) == 0;
+    if (!same) {
+        if (ctx->batch_exec) {
+            SR_CUDA(cudaStreamSynchronize(st), "sync before graph rebuild");
+            cudaGraphExecDestroy(ctx->batch_exec);
+            ctx->batch_exec = nullptr;
+        }
+        SrScene* s0 = scenes[0];  // side streams and fork events (used only with several slot groups)
+        SR_CUDA(wave_build_graph_batch(Ls.data(), (int)count, ctx->batch_capture, s0->side_streams, s0->fork_events,
+                                       &ctx->batch_exec),
+                "build batch graph");
+        ctx->batch_launch = Ls;
+    }
+    SR_CUDA(cudaGraphLaunch(ctx->batch_exec, st), "launch batch graph");
+    return SR_OK;
 }
 
 // Device AOV planes (56 B per pixel) plus an RGB8 image, cached on the scene.

@@ -1105,14 +1105,20 @@ cudaError_t wave_tail(const WaveLaunch& L, int cur, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, const cudaStream_t* side,
-                             const cudaEvent_t* fork, cudaGraphExec_t* exec_out) {
+// One graph holding, per launch description, the device-side bounce loop (a conditional WHILE node
+// whose body is two bounces and the loop condition) followed by its tail kernel.  The branches of
+// different descriptions have no edges between them, so the GPU runs them side by side: one
+// scene's small bounces and kernel ramp-downs overlap another's work.
+cudaError_t wave_build_graph_batch(const WaveLaunch* Ls, int n, cudaStream_t capture_stream, const cudaStream_t* side,
+                                   const cudaEvent_t* fork, cudaGraphExec_t* exec_out) {
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaGraphCreate(&graph, 0);
     if (e != cudaSuccess) return e;
-    cudaGraphConditionalHandle handle;
-    e = cudaGraphConditionalHandleCreate(&handle, graph, 1u, cudaGraphCondAssignDefault);
-    if (e == cudaSuccess) {
+    for (int i = 0; i < n && e == cudaSuccess; ++i) {
+        const WaveLaunch& L = Ls[i];
+        cudaGraphConditionalHandle handle;
+        e = cudaGraphConditionalHandleCreate(&handle, graph, 1u, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) break;
         cudaGraphNodeParams cp = {};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = handle;
@@ -1120,33 +1126,32 @@ cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, c
         cp.conditional.size = 1;
         cudaGraphNode_t node;
         e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
-        if (e == cudaSuccess) {
-            cudaGraph_t body = cp.conditional.phGraph_out[0];
-            e = cudaStreamBeginCaptureToGraph(capture_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-            if (e == cudaSuccess) {
-                // two bounces per group on parallel branches, joined before the loop condition
-                cudaError_t e1 = launch_bounces(L, 0, 2, capture_stream, side, fork);
-                k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.tail_paths, L.max_iters,
-                                                             L.err);
-                cudaGraph_t captured = nullptr;
-                cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
-                e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : cudaGetLastError());
-            }
-            if (e == cudaSuccess) {
-                // after the loop: the tail kernel over the paths left (parity 0 after whole bodies)
-                e = cudaStreamBeginCaptureToGraph(capture_stream, graph, &node, nullptr, 1, cudaStreamCaptureModeRelaxed);
-                if (e == cudaSuccess) {
-                    cudaError_t e1 = wave_tail(L, 0, capture_stream);
-                    cudaGraph_t captured = nullptr;
-                    cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
-                    e = e1 != cudaSuccess ? e1 : e2;
-                }
-            }
-        }
+        if (e != cudaSuccess) break;
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(capture_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) break;
+        // two bounces per group on parallel branches, joined before the loop condition
+        cudaError_t e1 = launch_bounces(L, 0, 2, capture_stream, side, fork);
+        k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.tail_paths, L.max_iters, L.err);
+        cudaGraph_t captured = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
+        e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : cudaGetLastError());
+        if (e != cudaSuccess) break;
+        // after the loop: the tail kernel over the paths left (parity 0 after whole bodies)
+        e = cudaStreamBeginCaptureToGraph(capture_stream, graph, &node, nullptr, 1, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) break;
+        e1 = wave_tail(L, 0, capture_stream);
+        e2 = cudaStreamEndCapture(capture_stream, &captured);
+        e = e1 != cudaSuccess ? e1 : e2;
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(exec_out, graph, 0);
     cudaGraphDestroy(graph);
     return e;
+}
+
+cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, const cudaStream_t* side,
+                             const cudaEvent_t* fork, cudaGraphExec_t* exec_out) {
+    return wave_build_graph_batch(&L, 1, capture_stream, side, fork, exec_out);
 }
 
 }  // namespace sr

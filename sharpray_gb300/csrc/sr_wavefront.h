@@ -139,5 +139,8 @@ cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st, const cud
 cudaError_t wave_tail(const WaveLaunch& L, int cur, cudaStream_t st);
 cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, const cudaStream_t* side,
                              const cudaEvent_t* fork, cudaGraphExec_t* exec_out);
+// One graph with an independent bounce loop + tail per launch description (batched rendering).
+cudaError_t wave_build_graph_batch(const WaveLaunch* Ls, int n, cudaStream_t capture_stream, const cudaStream_t* side,
+                                   const cudaEvent_t* fork, cudaGraphExec_t* exec_out);
 
 }  // namespace sr

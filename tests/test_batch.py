@@ -1,0 +1,104 @@
+"""Batched rendering (sr_render_batch): several scenes of one context in one graph launch, each
+scene's AOVs bit-identical to its own sr_render_device render; the cached graph is reused for an
+identical batch and rebuilt for a different one; invalid batches are refused."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from sharpray_gb300 import Context, SharpRayError, _abi, render_batch, render_params, synth
+
+pytestmark = pytest.mark.gpu
+
+PLANES = (("radiance", 3, "float32"), ("radiance_fog", 3, "float32"), ("normals", 3, "float32"), ("uv", 2, "float32"),
+          ("depth", 1, "float32"), ("samples", 1, "int32"), ("variance", 1, "float32"))
+
+
+def device_aovs(torch, n):
+    bufs = {k: torch.zeros(n * c, dtype=getattr(torch, t), device="cuda") for k, c, t in PLANES}
+    a = _abi.SrAovs(*[bufs[k].data_ptr() for k, _, _ in PLANES])
+    return bufs, a
+
+
+def host(bufs):
+    return {k: v.cpu().numpy().copy() for k, v in bufs.items()}
+
+
+def same(a, b):
+    for k in a:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+
+
+@pytest.fixture(scope="module")
+def batch_scenes():
+    torch = pytest.importorskip("torch")
+    ctx = Context(0)
+    descs = [synth.config_c1(40, 32, 4), synth.config_features(36, 28, 3), synth.config_procedural(24, 20, 5),
+             synth.config_c2(48, 27, 2, rings=60, rock_rings=20, env=(128, 64))]
+    descs[1].min_samples = 1  # adaptive stop in one of them
+    scenes = []
+    for d in descs:
+        s = d.instantiate(ctx)
+        s.build()
+        scenes.append(s)
+    return torch, ctx, descs, scenes
+
+
+def render_single(torch, ctx, d, s):
+    bufs, a = device_aovs(torch, d.width * d.height)
+    v, p = d.view.to_c(), render_params(*d.render_args())
+    _abi.check(ctx._lib.sr_render_device(s.handle, C.byref(v), C.byref(p), C.byref(a), None))
+    torch.cuda.synchronize()  # the device, so also the context's own stream
+    return bufs
+
+
+def test_batch_matches_single_renders(batch_scenes):
+    torch, ctx, descs, scenes = batch_scenes
+    stream = torch.cuda.current_stream().cuda_stream
+    singles = []
+    for d, s in zip(descs, scenes):
+        bufs, a = device_aovs(torch, d.width * d.height)
+        v, p = d.view.to_c(), render_params(*d.render_args())
+        _abi.check(ctx._lib.sr_render_device(s.handle, C.byref(v), C.byref(p), C.byref(a), C.c_void_p(stream)))
+        torch.cuda.synchronize()
+        singles.append(host(bufs))
+    outs = [device_aovs(torch, d.width * d.height) for d in descs]
+    params = [render_params(*d.render_args()) for d in descs]
+    for _ in range(2):  # the second launch reuses the cached graph
+        for bufs, _a in outs:
+            for t in bufs.values():
+                t.zero_()
+        render_batch(scenes, [d.view for d in descs], params, [a for _b, a in outs], stream=stream)
+        torch.cuda.synchronize()
+        for (bufs, _a), ref in zip(outs, singles):
+            same(host(bufs), ref)
+    assert int(singles[1]["samples"].min()) < descs[1].spp  # the adaptive scene did stop early
+
+
+def test_batch_subset_and_order(batch_scenes):
+    """A different batch (other scenes, other order) rebuilds the graph and still matches."""
+    torch, ctx, descs, scenes = batch_scenes
+    stream = torch.cuda.current_stream().cuda_stream
+    order = [3, 0]
+    outs = [device_aovs(torch, descs[i].width * descs[i].height) for i in order]
+    render_batch([scenes[i] for i in order], [descs[i].view for i in order],
+                 [render_params(*descs[i].render_args()) for i in order], [a for _b, a in outs], stream=stream)
+    torch.cuda.synchronize()
+    for i, (bufs, _a) in zip(order, outs):
+        ref = render_single(torch, ctx, descs[i], scenes[i])
+        same(host(bufs), host(ref))
+
+
+def test_batch_rejects_duplicates_and_missing_planes(batch_scenes):
+    torch, ctx, descs, scenes = batch_scenes
+    _b, a = device_aovs(torch, descs[0].width * descs[0].height)
+    p = render_params(*descs[0].render_args())
+    with pytest.raises(SharpRayError):
+        render_batch([scenes[0], scenes[0]], [descs[0].view] * 2, [p, p], [a, a])
+    bad = _abi.SrAovs(a.radiance, a.radiance_fog, a.normals, a.uv, a.depth, a.samples, None)
+    with pytest.raises(SharpRayError):
+        render_batch([scenes[0]], [descs[0].view], [p], [bad])
+    other = synth.config_c1(16, 16, 1).instantiate(Context(0))
+    other.build()
+    with pytest.raises(SharpRayError):
+        render_batch([scenes[0], other], [descs[0].view] * 2, [p, p], [a, a])
