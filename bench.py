@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=0, help="render mode: 0 auto, 1 megakernel, 2 wavefront, 3 graph")
     ap.add_argument("--variants", action="store_true", help="also time every render mode once")
+    ap.add_argument("--batch-scenes", type=int, default=32,
+                    help="scenes of the batched workload timed batched vs one after another (0: skip)")
     ap.add_argument("--profile-once", action="store_true",
                     help="set up, render + compose exactly once, exit (for ncu captures)")
     return ap.parse_args()
@@ -168,6 +170,64 @@ def cpu_oracle_sample(desc, target_s: float, threads: int):
     rows, dt = oracle_bands(scene, view, params, threads, desc.height, per_band)
     samples = rows * desc.width * desc.spp
     return samples / dt, rows, dt
+
+
+def measure_batch(ctx, count: int, stream, sp) -> dict:
+    """The batched workload (synth.config_batch: `count` scenes of uneven size, resolution and spp)
+    rendered by one sr_render_batch graph launch vs the same scenes one sr_render_device call
+    after another on the same stream; both give bit-identical images (so equal relMSE)."""
+    import ctypes as C
+
+    import torch
+    from sharpray_gb300 import _abi, render_batch, render_params, synth
+    t0 = time.perf_counter()
+    descs = synth.config_batch(count, seed=3)
+    scenes, outs, params, views, keep = [], [], [], [], []
+    for d in descs:
+        sc = d.instantiate(ctx)
+        sc.build()
+        n = d.width * d.height
+        dev = {k: torch.empty(n * c, dtype=torch.int32 if k == "samples" else torch.float32, device="cuda")
+               for k, c in (("radiance", 3), ("radiance_fog", 3), ("normals", 3), ("uv", 2), ("depth", 1),
+                            ("samples", 1), ("variance", 1))}
+        keep.append(dev)
+        scenes.append(sc)
+        outs.append(_abi.SrAovs(*[dev[k].data_ptr() for k in ("radiance", "radiance_fog", "normals", "uv", "depth",
+                                                               "samples", "variance")]))
+        params.append(render_params(*d.render_args()))
+        views.append(d.view)
+    setup = time.perf_counter() - t0
+    samples = sum(d.width * d.height * d.spp for d in descs)
+    lib = ctx._lib
+
+    def plain():
+        for sc, v, p, o in zip(scenes, views, params, outs):
+            vc = v.to_c()
+            _abi.check(lib.sr_render_device(sc.handle, C.byref(vc), C.byref(p), C.byref(o), sp))
+
+    def batch():
+        render_batch(scenes, views, params, outs, stream=stream.cuda_stream)
+
+    res = {}
+    for label, fn in (("plain", plain), ("batched", batch)):
+        fn()  # warm-up (builds the graphs)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(2):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        res[label] = a.elapsed_time(b) / 2 / 1000.0
+    tris = [d.triangle_count for d in descs]
+    return {"workload": f"{count} scenes (synth.config_batch, seed 3): triangles {min(tris)}-{max(tris)}, "
+                        "256x256-1920x1080, 4/16/64 spp, depth 4-8, fog on half",
+            "samples_per_step": samples, "unit": UNIT,
+            "value": samples / res["batched"], "plain_value": samples / res["plain"],
+            "batched_ms": 1000 * res["batched"], "plain_ms": 1000 * res["plain"],
+            "speedup": res["plain"] / res["batched"], "setup_s": round(setup, 1),
+            "note": "batched: one graph launch, one bounce loop per scene side by side; plain: one "
+                    "graph-captured render per scene, back to back; images bit-identical"}
 
 
 def run_reference(args):
@@ -327,6 +387,10 @@ def run_ours(args):
             variants[label] = samples_per_step / (a.elapsed_time(b) / 1000.0)
         scene.set_render_mode(args.mode)
 
+    batched = None
+    if args.batch_scenes > 0 and rank == 0:
+        batched = measure_batch(ctx, args.batch_scenes, stream, sp)
+
     # end to end through the public API with pinned host outputs
     host = Aovs(W, H)
     pinned = {}
@@ -400,6 +464,7 @@ def run_ours(args):
             "render_mode": {0: "auto (wavefront graph)", 1: "megakernel", 2: "wavefront host loop",
                             3: "wavefront graph"}[args.mode],
             "variants_samples_per_s": variants,
+            "batched": batched,
             "clocks": clocks.summary(),
             "counters_per_step": counters,
             # closest-hit + shadow queries per second (SceneTrace + SceneOcclude counters)

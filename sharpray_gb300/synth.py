@@ -402,6 +402,41 @@ def config_c2(width: int = 1920, height: int = 1080, spp: int = 64, rings: int =
     return d
 
 
+def config_batch(count: int = 32, seed: int = 3) -> list:
+    """Batched workload: `count` independent scenes, each one fBm-displaced sphere (CreateSphere
+    topology) with a triangle count log-uniform in [1k, 1M], a resolution from {256x256, 512x512,
+    1024x768, 1920x1080}, spp from {4, 16, 64}, depth U{4..8}, fog (0.02) on for half; one GGX
+    material per scene (roughness U[0.05, 1], metallic Bernoulli(0.3), albedo U[0.1, 0.9]^3) and a
+    256x128 HDR env with a sun lobe; seed 3."""
+    rng = np.random.default_rng(seed)
+    sizes = [(256, 256), (512, 512), (1024, 768), (1920, 1080)]
+    out = []
+    for i in range(count):
+        tris = math.exp(rng.uniform(math.log(1e3), math.log(1e6)))
+        rings = max(8, int(round(math.sqrt(tris / 2.0))))
+        w, h = sizes[int(rng.integers(len(sizes)))]
+        spp = int(rng.choice([4, 16, 64]))
+        bounces = int(rng.integers(4, 9))
+        fog = bool(rng.random() < 0.5)
+        pos, uv = uv_sphere(rings, rings, amplitude=0.1, seed=seed * 1000 + i)
+        d = SceneDesc(f"batch{i}_{2 * rings * rings}tris_{w}x{h}_{spp}spp")
+        d.meshes = [MeshDesc(pos, uv)]
+        d.textures = [TextureDesc(_rgbe_texels(sky_env(256, 128, seed=seed * 1000 + i, sun_peak=200.0,
+                                                       sun_sigma_deg=2.0, lognormal_sigma=1.0)))]
+        d.sky = ("texture", 0, 1.0, 0.0)
+        d.objects = [ObjectDesc("sphere", Transform(),
+                                {"albedo": tuple(float(x) for x in rng.uniform(0.1, 0.9, 3)),
+                                 "roughness": float(rng.uniform(0.05, 1.0)), "metallic": float(rng.random() < 0.3)},
+                                ("mesh", 0))]
+        if fog:
+            d.fog = Fog(0.02, (0.8, 0.75, 0.6), 0.6, 0.01)
+        cam = (0.0, 0.8, -3.0)
+        d.view = View(Transform(cam, look_rotation(cam, (0.0, 0.0, 0.0))), math.radians(55.0), 0.1)
+        d.width, d.height, d.spp, d.bounces = w, h, spp, bounces
+        out.append(d)
+    return out
+
+
 def config_features(width: int = 48, height: int = 40, spp: int = 8, seed: int = 5) -> SceneDesc:
     """Small scene touching every shading branch: textured/normal-mapped/point-filtered materials,
     transparent (refractive) sphere, metal box, emissive object, instanced transformed mesh, fog."""
