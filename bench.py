@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=0, help="render mode: 0 auto, 1 megakernel, 2 wavefront, 3 graph")
     ap.add_argument("--variants", action="store_true", help="also time every render mode once")
+    ap.add_argument("--autotune-spp", type=int, default=8,
+                    help="spp of the autotuner's trial renders at setup (0: default launch geometry)")
     ap.add_argument("--batch-scenes", type=int, default=32,
                     help="scenes of the batched workload timed batched vs one after another (0: skip)")
     ap.add_argument("--profile-once", action="store_true",
@@ -332,6 +334,14 @@ def run_ours(args):
         ctx.build_bvh(tb, 1.0, 0.5, 8, where=where)
         bvh_s[label + "_s"] = round(time.perf_counter() - t0, 4)
 
+    # autotuner (setup, untimed): launch geometry of the wavefront kernels for this scene
+    tuning = None
+    if args.autotune_spp > 0 and args.mode in (0, 3):
+        t0 = time.perf_counter()
+        tuning = scene.autotune(desc.view, params, trial_spp=args.autotune_spp)
+        tuning["trial_spp"] = args.autotune_spp
+        tuning["seconds"] = round(time.perf_counter() - t0, 2)
+
     # work counters of one render (untimed) -> algorithmic bytes per launch
     scene.set_counting(True)
     render()
@@ -465,6 +475,7 @@ def run_ours(args):
                             3: "wavefront graph"}[args.mode],
             "variants_samples_per_s": variants,
             "batched": batched,
+            "autotune": tuning,
             "clocks": clocks.summary(),
             "counters_per_step": counters,
             # closest-hit + shadow queries per second (SceneTrace + SceneOcclude counters)

@@ -328,6 +328,26 @@ SR_API int sr_preview(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, u
 SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const SrRenderParams* params,
                            const SrAovs* device_outs, uint32_t count, void* stream);
 
+/* Launch geometry of the wavefront kernels (no counterpart in the reference): blocks per SM of the
+ * traversal, fog-shade and surface-shade kernels (0 = as many as fit; never more) and the live-path
+ * count slots / tail_divisor at which the tail kernel takes over (0 = the built-in 16).  Results
+ * do not depend on it. */
+typedef struct SrTuning {
+    int32_t trace_blocks_per_sm;
+    int32_t fog_shade_blocks_per_sm;
+    int32_t surface_shade_blocks_per_sm;
+    uint32_t tail_divisor;
+    float ms;          /* sr_scene_autotune: trial render time of the chosen setting */
+    float default_ms;  /* sr_scene_autotune: trial render time of the defaults */
+} SrTuning;
+SR_API int sr_scene_set_tuning(SrScene* scene, const SrTuning* tuning); /* NULL = defaults */
+SR_API int sr_scene_get_tuning(SrScene* scene, SrTuning* tuning);
+/* Autotuner: renders `params` at trial_spp samples per pixel under candidate launch geometries
+ * (traversal blocks per SM: all that fit, one or two fewer; fog-shade blocks: all, two fewer; tail
+ * hand-over at slots / 8, 16 or 32), keeps the fastest on the scene and reports it. */
+SR_API int sr_scene_autotune(SrScene* scene, const SrView* view, const SrRenderParams* params, uint32_t trial_spp,
+                             SrTuning* chosen);
+
 /* ---- asset ingest (host-side file parsing) ------------------------------------------------- */
 /* Image.Load (image.cs:214-273: uncompressed 24-bit TrueColor / 8-bit Grayscale .tga, rows top-down)
  * or ImageHdr.Load (image.cs:307-382: Radiance .hdr, "-Y h +X w", new-style RLE or flat): sizes

@@ -108,6 +108,12 @@ class SrComposeParams(C.Structure):
                 ("denoise_fog_radius", C.c_float), ("denoise_fog_strength", C.c_float)]
 
 
+class SrTuning(C.Structure):
+    _fields_ = [("trace_blocks_per_sm", C.c_int32), ("fog_shade_blocks_per_sm", C.c_int32),
+                ("surface_shade_blocks_per_sm", C.c_int32), ("tail_divisor", C.c_uint32), ("ms", C.c_float),
+                ("default_ms", C.c_float)]
+
+
 class SrAovImageParams(C.Structure):
     _fields_ = [("variance_threshold", C.c_float), ("min_samples", C.c_uint32), ("max_samples", C.c_uint32)]
 
@@ -174,6 +180,9 @@ PROTOTYPES = {
     "sr_compose_device_static": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
     "sr_preview": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P]),
     "sr_render_batch": (_I, [_P, _P, _P, _P, _U, _P]),
+    "sr_scene_set_tuning": (_I, [_P, _P]),
+    "sr_scene_get_tuning": (_I, [_P, C.POINTER(SrTuning)]),
+    "sr_scene_autotune": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), _U, C.POINTER(SrTuning)]),
     "sr_aov_image": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P]),
     "sr_aov_image_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P, _P]),
     "sr_overlay_draw": (_I, [_P, _P, _U, _U, C.POINTER(SrView), _P, _P, _U, _P, _U, C.POINTER(SrFont)]),

@@ -426,6 +426,25 @@ class Scene:
         check(self._lib.sr_scene_build(self.handle))
         self.built = True
 
+    def set_tuning(self, trace_blocks_per_sm: int = 0, fog_shade_blocks_per_sm: int = 0,
+                   surface_shade_blocks_per_sm: int = 0, tail_divisor: int = 0) -> None:
+        """Launch geometry of the wavefront kernels (0 = default); results do not depend on it."""
+        t = _abi.SrTuning(trace_blocks_per_sm, fog_shade_blocks_per_sm, surface_shade_blocks_per_sm, tail_divisor,
+                          0.0, 0.0)
+        check(self._lib.sr_scene_set_tuning(self.handle, C.byref(t)))
+
+    def autotune(self, view: "View", params: SrRenderParams, trial_spp: int = 8) -> dict:
+        """sr_scene_autotune: times candidate launch geometries on `params` at trial_spp samples per
+        pixel and keeps the fastest; returns it with the trial times (ms) of it and of the defaults."""
+        if not self.built:
+            self.build()
+        t = _abi.SrTuning()
+        v = view.to_c()
+        check(self._lib.sr_scene_autotune(self.handle, C.byref(v), C.byref(params), int(trial_spp), C.byref(t)))
+        return {"trace_blocks_per_sm": t.trace_blocks_per_sm, "fog_shade_blocks_per_sm": t.fog_shade_blocks_per_sm,
+                "surface_shade_blocks_per_sm": t.surface_shade_blocks_per_sm, "tail_divisor": t.tail_divisor,
+                "ms": t.ms, "default_ms": t.default_ms}
+
     def load_obj(self, path, transform: Optional["Transform"] = None, material: Optional["Material"] = None,
                  smooth_normals: bool = True) -> int:
         """ObjLoader.Load(path, scene, config) obj.cs:139-259: adds one object per OBJ group; returns

@@ -155,6 +155,8 @@ struct SrScene {
     WaveLaunch graph_launch{};  // launch parameters baked into graph_exec
     uint32_t* counts_host = nullptr;  // pinned
     int sms = 0;
+    WaveTune tune{};  // launch geometry (sr_scene_set_tuning / sr_scene_autotune)
+    DevBuf tune_aovs;  // autotune's scratch AOV planes
     int last_mode = 0;                // render mode of the last render
     uint32_t last_host_iters = 0;     // bounces run by the host loop
     bool last_tail = false;           // the host loop launched the tail kernel
@@ -867,12 +869,13 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     L.err = s->err.as<uint32_t>();
     L.counters = ctr;
     L.general = s->dev.general;
-    wave_grid_sizes(L, s->sms);
+    wave_grid_sizes(L, s->sms, &s->tune);
     uint64_t cap = (uint64_t)dp.max_samples * (dp.bounces + 1) + 4;
     L.max_iters = (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap);
     uint32_t all_slots = 0;
     for (int g = 0; g < kWaveGroups; ++g) all_slots += s->ws[g].slots;
-    L.tail_paths = SR_TAIL_DIV > 0 ? all_slots / SR_TAIL_DIV : 0;
+    const uint32_t tail_div = s->tune.tail_div ? s->tune.tail_div : (uint32_t)SR_TAIL_DIV;
+    L.tail_paths = tail_div > 0 ? all_slots / tail_div : 0;
     SR_CUDA(wave_init(L, st), "wavefront init");
     return SR_OK;
 }
@@ -998,6 +1001,100 @@ SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const Sr
         ctx->batch_launch = Ls;
     }
     SR_CUDA(cudaGraphLaunch(ctx->batch_exec, st), "launch batch graph");
+    return SR_OK;
+}
+
+SR_API int sr_scene_set_tuning(SrScene* s, const SrTuning* t) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    if (t && (t->trace_blocks_per_sm < 0 || t->fog_shade_blocks_per_sm < 0 || t->surface_shade_blocks_per_sm < 0))
+        return fail(SR_ERR_INVALID_ARG, "blocks per SM must be >= 0");
+    s->tune = t ? WaveTune{t->trace_blocks_per_sm, t->fog_shade_blocks_per_sm, t->surface_shade_blocks_per_sm,
+                           t->tail_divisor}
+                : WaveTune{};
+    return SR_OK;
+}
+
+SR_API int sr_scene_get_tuning(SrScene* s, SrTuning* t) {
+    if (!s || !t) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    std::memset(t, 0, sizeof(*t));
+    t->trace_blocks_per_sm = s->tune.trace_per_sm;
+    t->fog_shade_blocks_per_sm = s->tune.fog_per_sm;
+    t->surface_shade_blocks_per_sm = s->tune.surface_per_sm;
+    t->tail_divisor = s->tune.tail_div;
+    return SR_OK;
+}
+
+// Times `params` at trial_spp samples per pixel under each candidate launch geometry -- traversal
+// blocks per SM (all that fit, one or two fewer), fog-shade blocks per SM (all that fit, two
+// fewer), tail hand-over (slots / 8, 16, 32) -- and keeps the fastest on the scene.
+SR_API int sr_scene_autotune(SrScene* s, const SrView* view, const SrRenderParams* params, uint32_t trial_spp,
+                             SrTuning* out) {
+    if (!s || !view || !params) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    if (trial_spp == 0) return fail(SR_ERR_INVALID_ARG, "trial_spp must be > 0");
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    SrRenderParams p = *params;
+    p.min_samples = p.max_samples = trial_spp;
+    const size_t n = (size_t)p.width * p.height;
+    SR_CUDA(s->tune_aovs.reserve(n * 56 + 256), "alloc autotune AOVs");
+    char* b = s->tune_aovs.as<char>();
+    DevAovs d;
+    d.radiance = (float*)b;
+    d.radiance_fog = d.radiance + 3 * n;
+    d.normals = d.radiance_fog + 3 * n;
+    d.uv = d.normals + 3 * n;
+    d.depth = d.uv + 2 * n;
+    d.samples = (uint32_t*)(d.depth + n);
+    d.variance = (float*)(d.samples + n);
+    int tr = 0, fog = 0, surf = 0;
+    wave_occupancy(s->dev.general != 0, &tr, &fog, &surf);
+    cudaEvent_t e0, e1;
+    SR_CUDA(cudaEventCreate(&e0), "event");
+    SR_CUDA(cudaEventCreate(&e1), "event");
+    const int32_t saved_mode = s->render_mode;
+    const WaveTune saved = s->tune;
+    s->render_mode = SR_RENDER_WAVEFRONT_GRAPH;
+    float best_ms = 0.0f, default_ms = 0.0f;
+    WaveTune best{};
+    int rc = SR_OK;
+    const int trace_c[3] = {0, tr - 1, tr - 2}, fog_c[2] = {0, fog - 2};
+    const uint32_t tail_c[3] = {16, 8, 32};
+    for (int a = 0; a < 3 && !rc; ++a)
+        for (int f = 0; f < 2 && !rc; ++f)
+            for (int t = 0; t < 3 && !rc; ++t) {
+                if (trace_c[a] < 0 || fog_c[f] < 0) continue;
+                if ((a > 0 && trace_c[a] < 1) || (f > 0 && fog_c[f] < 1)) continue;
+                s->tune = WaveTune{trace_c[a], fog_c[f], 0, tail_c[t]};
+                rc = render_into(s, view, &p, d, st);  // warm-up (builds the graph)
+                if (!rc) rc = cudaEventRecord(e0, st) == cudaSuccess ? SR_OK : fail(SR_ERR_CUDA, "event");
+                for (int k = 0; k < 2 && !rc; ++k) rc = render_into(s, view, &p, d, st);
+                if (!rc) rc = cudaEventRecord(e1, st) == cudaSuccess ? SR_OK : fail(SR_ERR_CUDA, "event");
+                if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(SR_ERR_CUDA, "autotune render");
+                if (rc) break;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms *= 0.5f;
+                if (a == 0 && f == 0 && t == 0) default_ms = ms;
+                if (best_ms == 0.0f || ms < best_ms) best_ms = ms, best = s->tune;
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s->render_mode = saved_mode;
+    if (rc) {
+        s->tune = saved;
+        return rc;
+    }
+    if (int erc = check_device_error(s)) {
+        s->tune = saved;
+        return erc;
+    }
+    s->tune = best;
+    if (out) {
+        sr_scene_get_tuning(s, out);
+        out->ms = best_ms;
+        out->default_ms = default_ms;
+    }
     return SR_OK;
 }
 

@@ -1057,12 +1057,27 @@ static void occupancy(int* b) {
     }
 }
 
-void wave_grid_sizes(WaveLaunch& L, int sms) {
+void wave_occupancy(bool general, int* trace, int* fog, int* surface) {
+    int b[6] = {0, 0, 0, 0, 0, 0};
+    if (general)
+        occupancy<true>(b);
+    else
+        occupancy<false>(b);
+    *trace = b[0], *fog = b[3], *surface = b[5];
+}
+
+void wave_grid_sizes(WaveLaunch& L, int sms, const WaveTune* tune) {
     int b[6] = {0, 0, 0, 0, 0, 0};
     if (L.general)
         occupancy<true>(b);
     else
         occupancy<false>(b);
+    if (tune) {  // a tuned count never exceeds what fits
+        auto pick = [](int want, int fit) { return want > 0 && want < fit ? want : fit; };
+        b[0] = pick(tune->trace_per_sm, b[0]);
+        b[3] = pick(tune->fog_per_sm, b[3]);
+        b[5] = pick(tune->surface_per_sm, b[5]);
+    }
     for (int& v : b) v = sms * (v > 0 ? v : 1);
     L.grid_trace = b[0];
     L.grid_shadow = b[1];

@@ -129,7 +129,16 @@ struct WaveGroups {
 #endif
 constexpr int kWaveKernelsPerBounce = (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 1 : 0);
 
-void wave_grid_sizes(WaveLaunch& L, int sms);
+// Launch geometry chosen at run time (0 = the default: as many blocks per SM as fit).
+struct WaveTune {
+    int trace_per_sm;     // persistent traversal kernel
+    int fog_per_sm;       // fog-event shade kernel
+    int surface_per_sm;   // surface-event shade kernel
+    uint32_t tail_div;    // the tail kernel takes over at slots / tail_div live paths (0 = SR_TAIL_DIV)
+};
+// Resident blocks per SM of the traversal, fog-shade and surface-shade kernels.
+void wave_occupancy(bool general, int* trace, int* fog, int* surface);
+void wave_grid_sizes(WaveLaunch& L, int sms, const WaveTune* tune = nullptr);
 // Counters of every group (contiguous, kWaveCounters per group) cleared, first camera rays.
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st);
 // One bounce of every group: group 0 on `st`, the others on `side` streams forked from and

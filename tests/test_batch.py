@@ -102,3 +102,18 @@ def test_batch_rejects_duplicates_and_missing_planes(batch_scenes):
     other.build()
     with pytest.raises(SharpRayError):
         render_batch([scenes[0], other], [descs[0].view] * 2, [p, p], [a, a])
+
+
+def test_tuning_leaves_results_unchanged(batch_scenes):
+    """Launch geometry (set by hand or by the autotuner) changes timing only, never the AOVs."""
+    torch, ctx, descs, scenes = batch_scenes
+    d, s = descs[3], scenes[3]
+    ref = host(render_single(torch, ctx, d, s))
+    for tune in ((3, 4, 2, 8), (1, 1, 1, 64), (0, 0, 0, 0)):
+        s.set_tuning(*tune)
+        same(host(render_single(torch, ctx, d, s)), ref)
+    chosen = s.autotune(d.view, render_params(*d.render_args()), trial_spp=2)
+    assert chosen["ms"] > 0 and chosen["default_ms"] > 0 and chosen["ms"] <= chosen["default_ms"]
+    assert chosen["tail_divisor"] in (8, 16, 32)
+    same(host(render_single(torch, ctx, d, s)), ref)
+    s.set_tuning()

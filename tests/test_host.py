@@ -118,3 +118,16 @@ def test_device_bvh_build_needs_a_device(host_ctx):
         host_ctx.set_bvh_build(_abi.SR_BVH_BUILD_DEVICE)
     with pytest.raises(StateError):
         host_ctx.build_bvh(np.zeros((4, 6), np.float32), 1.0, 0.5, 8, where=_abi.SR_BVH_BUILD_DEVICE)
+
+
+def test_tuning_validation(host_ctx):
+    import ctypes as C
+
+    from sharpray_gb300 import Scene, SharpRayError, _abi
+    s = Scene(host_ctx)
+    s.set_tuning(3, 4, 2, 8)
+    t = _abi.SrTuning()
+    _abi.check(host_ctx._lib.sr_scene_get_tuning(s.handle, C.byref(t)))
+    assert (t.trace_blocks_per_sm, t.fog_shade_blocks_per_sm, t.surface_shade_blocks_per_sm, t.tail_divisor) == (3, 4, 2, 8)
+    with pytest.raises(SharpRayError):
+        s.set_tuning(-1)
