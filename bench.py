@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--variants", action="store_true", help="also time every render mode once")
     ap.add_argument("--autotune-spp", type=int, default=8,
                     help="spp of the autotuner's trial renders at setup (0: default launch geometry)")
+    ap.add_argument("--batch-autotune-spp", type=int, default=0,
+                    help="autotune each batched scene with trial renders at this spp (0: defaults)")
     ap.add_argument("--batch-scenes", type=int, default=32,
                     help="scenes of the batched workload timed batched vs one after another (0: skip)")
     ap.add_argument("--profile-once", action="store_true",
@@ -174,7 +176,7 @@ def cpu_oracle_sample(desc, target_s: float, threads: int):
     return samples / dt, rows, dt
 
 
-def measure_batch(ctx, count: int, stream, sp) -> dict:
+def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
     """The batched workload (synth.config_batch: `count` scenes of uneven size, resolution and spp)
     rendered by one sr_render_batch graph launch vs the same scenes one sr_render_device call
     after another on the same stream; both give bit-identical images (so equal relMSE)."""
@@ -199,6 +201,11 @@ def measure_batch(ctx, count: int, stream, sp) -> dict:
         params.append(render_params(*d.render_args()))
         views.append(d.view)
     setup = time.perf_counter() - t0
+    tuned = 0
+    if tune_spp > 0:  # each scene's launch geometry from the autotuner (setup, untimed)
+        for sc, d, p in zip(scenes, descs, params):
+            t = sc.autotune(d.view, p, trial_spp=min(tune_spp, d.spp))
+            tuned += int(t["ms"] < t["default_ms"])
     samples = sum(d.width * d.height * d.spp for d in descs)
     lib = ctx._lib
 
@@ -228,6 +235,7 @@ def measure_batch(ctx, count: int, stream, sp) -> dict:
             "value": samples / res["batched"], "plain_value": samples / res["plain"],
             "batched_ms": 1000 * res["batched"], "plain_ms": 1000 * res["plain"],
             "speedup": res["plain"] / res["batched"], "setup_s": round(setup, 1),
+            "autotuned_scenes": tuned if tune_spp > 0 else None,
             "note": "batched: one graph launch, one bounce loop per scene side by side; plain: one "
                     "graph-captured render per scene, back to back; images bit-identical"}
 
@@ -399,7 +407,7 @@ def run_ours(args):
 
     batched = None
     if args.batch_scenes > 0 and rank == 0:
-        batched = measure_batch(ctx, args.batch_scenes, stream, sp)
+        batched = measure_batch(ctx, args.batch_scenes, stream, sp, args.batch_autotune_spp)
 
     # end to end through the public API with pinned host outputs
     host = Aovs(W, H)
