@@ -191,6 +191,8 @@ SR_API const char* sr_last_error_message(void);
  * device == -1 creates a host-only context: meshes, BVH builds/exports and scene BVH builds
  * work, every entry point that needs the GPU returns SR_ERR_STATE. */
 SR_API int sr_ctx_create(int device, SrContext** out_ctx);
+/* Scenes still alive keep the context alive: it is freed when the last of them is destroyed (the
+ * context itself must not be used after this call). */
 SR_API int sr_ctx_destroy(SrContext* ctx);
 
 /* ---- host-side ingest (no device work) --------------------------------------------------- */
@@ -347,6 +349,24 @@ SR_API int sr_scene_get_tuning(SrScene* scene, SrTuning* tuning);
  * hand-over at slots / 8, 16 or 32), keeps the fastest on the scene and reports it. */
 SR_API int sr_scene_autotune(SrScene* scene, const SrView* view, const SrRenderParams* params, uint32_t trial_spp,
                              SrTuning* chosen);
+
+/* ---- derivatives (no counterpart in the reference, which renders forward only) ------------- */
+/* Path-replay adjoint: the gradient of the image loss sum over pixels and channels of
+ * (radiance + radiance_fog - target)^2 with respect to the texels of albedo texture `texture`,
+ * for the image that sr_render_device produced with the same scene, view and params (`forward`:
+ * its radiance, radiance_fog and samples planes, device pointers).  `target` is a device
+ * width x height x 3 image; the gradient is ADDED into `grad` (device, texture width x height x 3).
+ * `replay` (device, width x height x 3, may be NULL) receives the replayed radiance + radiance_fog,
+ * which equals the forward image.  Sampled directions, roulette decisions, pdfs and MIS weights
+ * are held fixed (detached); the BRDF values and scatter weights are differentiated.  Scenes with
+ * transparent materials and params->bounces > 16 are refused.  Runs asynchronously on `stream`. */
+SR_API int sr_adjoint_albedo(SrScene* scene, const SrView* view, const SrRenderParams* params,
+                             const SrAovs* forward, const float* target, int32_t texture, float* grad,
+                             float* replay, void* stream);
+/* Replaces the texels of texture `texture` (rgb floats, its width x height) in a built scene's
+ * device copy, e.g. one step of inverse rendering.  The context's texture and other scenes are left
+ * as they are.  The scene's sky texture is refused (its light distribution is built from it). */
+SR_API int sr_scene_update_texture(SrScene* scene, int32_t texture, const float* texels_rgb);
 
 /* ---- asset ingest (host-side file parsing) ------------------------------------------------- */
 /* Image.Load (image.cs:214-273: uncompressed 24-bit TrueColor / 8-bit Grayscale .tga, rows top-down)

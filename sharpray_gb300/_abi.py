@@ -188,6 +188,9 @@ PROTOTYPES = {
     "sr_overlay_draw": (_I, [_P, _P, _U, _U, C.POINTER(SrView), _P, _P, _U, _P, _U, C.POINTER(SrFont)]),
     "sr_overlay_draw_device": (_I, [_P, _P, _U, _U, C.POINTER(SrView), _P, _P, _U, _P, _U, C.POINTER(SrFont), _P]),
     "sr_image_save": (_I, [C.c_char_p, _U, _U, _P]),
+    "sr_adjoint_albedo": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P, C.c_int32,
+                               _P, _P, _P]),
+    "sr_scene_update_texture": (_I, [_P, C.c_int32, _P]),
 }
 
 

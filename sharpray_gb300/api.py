@@ -445,6 +445,13 @@ class Scene:
                 "surface_shade_blocks_per_sm": t.surface_shade_blocks_per_sm, "tail_divisor": t.tail_divisor,
                 "ms": t.ms, "default_ms": t.default_ms}
 
+    def update_texture(self, texture, texels: np.ndarray) -> None:
+        """sr_scene_update_texture: new rgb texels (the texture's height x width x 3) for the built
+        scene's device copy of `texture` (a Texture or its id)."""
+        tid = texture.id if isinstance(texture, Texture) else int(texture)
+        t = np.ascontiguousarray(texels, dtype=np.float32)
+        check(self._lib.sr_scene_update_texture(self.handle, tid, ptr(t)))
+
     def load_obj(self, path, transform: Optional["Transform"] = None, material: Optional["Material"] = None,
                  smooth_normals: bool = True) -> int:
         """ObjLoader.Load(path, scene, config) obj.cs:139-259: adds one object per OBJ group; returns
@@ -799,6 +806,18 @@ def render_batch(scenes: Sequence["Scene"], views: Sequence["View"], params: Seq
     arr_a = (SrAovs * n)(*device_aovs)
     lib = scenes[0]._lib
     check(lib.sr_render_batch(arr_s, arr_v, arr_p, arr_a, n, C.c_void_p(stream) if stream else None))
+
+
+def adjoint_albedo(scene: "Scene", view: "View", params: SrRenderParams, forward: SrAovs, target: int,
+                   texture, grad: int, replay: Optional[int] = None, stream: Optional[int] = None) -> None:
+    """sr_adjoint_albedo: adds d/d(texels of `texture`) of sum (radiance + radiance_fog - target)^2
+    into `grad` for the image `forward` (device AOV planes of sr_render_device with the same scene,
+    view and params).  target / grad / replay are device pointers; asynchronous on `stream`."""
+    tid = texture.id if isinstance(texture, Texture) else int(texture)
+    v = view.to_c()
+    check(scene._lib.sr_adjoint_albedo(scene.handle, C.byref(v), C.byref(params), C.byref(forward), C.c_void_p(target),
+                                       tid, C.c_void_p(grad), C.c_void_p(replay) if replay else None,
+                                       C.c_void_p(stream) if stream else None))
 
 
 def load_image(path) -> np.ndarray:

@@ -1,0 +1,284 @@
+// sr_adjoint.cu — path-replay adjoint of a rendered image with respect to the texels of an albedo
+// (colour) texture: the gradient of the loss sum_pixels |I - T|^2, I = radiance + radiance_fog, for
+// a target image T.  No counterpart in the reference (it has no derivatives).
+//
+// One thread per pixel replays the pixel's samples exactly as the per-pixel path loop renders
+// them (the same RNG stream and the same functions, so the same paths and the same radiance --
+// the kernel also returns the replayed image for the caller to check), recording per vertex the
+// throughput, what the vertex adds to the radiance and the scatter weight.  A reverse sweep over
+// the vertices then carries the adjoint of the throughput back to the camera: through the scatter
+// weights, the luminance clamp of the indirect throughput and the Russian-roulette division (both
+// differentiated as functions of the throughput), and into the albedo of each surface vertex,
+// whose texture lookup passes it on to the four bilinear texels (atomic adds).
+//
+// Differentiated: the BRDF values of the light samples and the scatter weights with respect to
+// the albedo (diffuse term and, for metallic surfaces, the Fresnel base).  Held fixed ("detached"),
+// as path replay does: the sampled directions, lobe choices, Russian-roulette decisions and the
+// pdfs and MIS weights (which depend on the albedo only through the Fresnel base of metallic
+// surfaces).  For non-metallic surfaces the gradient is therefore the exact derivative of the
+// renderer's own estimator at fixed random numbers wherever no roulette decision or clamp
+// threshold is crossed.  Scenes with transparent materials are refused by the host entry point.
+#include <cuda_runtime.h>
+
+#include "sr_kernels.h"
+#include "sr_path.cuh"
+
+namespace sr {
+
+constexpr int kAdjMaxVertices = 17;  // bounces <= 16
+
+enum : int { AV_FOG = 0, AV_SURF = 1, AV_SURF_END = 2, AV_SKY = 3, AV_FOG_END = 4 };
+
+struct AdjVertex {
+    Col e_in;   // throughput entering the vertex
+    Col e_rr;   // throughput after the Russian roulette (surface), or after the fog colour (fog)
+    Col add;    // radiance added per unit throughput (emission + light sample; fog light sample; sky)
+    Col dadd;   // d add / d albedo, per channel
+    Col s;      // scatter weight (surface)
+    Col ds;     // d s / d albedo, per channel
+    Col pre;    // e_rr * s before the luminance clamp
+    float rr;   // survival probability divided by (1: none)
+    float clamp_max;
+    V2 uv;
+    int kind;
+    int material;
+};
+
+// d opaque_eval / d albedo (per channel), pdfs held fixed.
+__device__ Col opaque_eval_dalbedo(const Surface& s, V3 view, V3 light) {
+    float ndl = dot(s.normal, light);
+    if (ndl <= 0.0f) return black();
+    float ndv = fmaxf(1e-4f, dot(s.normal, view));
+    float rs = fmaxf(s.roughness * s.roughness, 1e-4f);
+    Col base = base_reflectivity(s.f0, s.albedo, s.metallic);
+    V3 half = normalize_or(view + light, s.normal);
+    float ndh = dot(s.normal, half);
+    float hdv = dot(half, view);
+    // fresnel(x, base) = base + (1 - base) (1 - x)^5, base = f0 + (albedo - f0) metallic
+    float xh = 1.0f - hdv, xv = 1.0f - ndv;
+    float dfh = s.metallic * (1.0f - xh * xh * xh * xh * xh);
+    float dfv = s.metallic * (1.0f - xv * xv * xv * xv * xv);
+    float g = smith_g1(ndv, rs) * smith_g1(ndl, rs);
+    float dspec = ggx_d(ndh, rs) * dfh * g / (4.0f * ndv);
+    Col fv = fresnel(ndv, base);
+    float k = (1.0f - s.metallic) * (ndl / kPi);
+    Col ddiff{((1.0f - fv.r) - s.albedo.r * dfv) * k, ((1.0f - fv.g) - s.albedo.g * dfv) * k,
+              ((1.0f - fv.b) - s.albedo.b * dfv) * k};
+    return (gray(dspec) + ddiff) * (1.0f - s.transparency);
+}
+
+// Scene.SampleSkyDirect (sample_sky_direct in sr_path.cuh) returning also d/d albedo.
+__device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos, V3 view, Rng& rng, Ctr& c,
+                                     uint32_t* err, Col& dnee) {
+    dnee = black();
+    V3 ldir;
+    float lpdf;
+    Col tr;
+    if (!sample_sky_light<false>(S, pos, rng, ldir, lpdf, tr, c, err)) return black();
+    V3 n = dot(s.normal, view) >= 0.0f ? s.normal : -s.normal;
+    if (dot(n, ldir) <= 0.0f) return black();
+    V3 ng = dot(s.normal_geo, view) >= 0.0f ? s.normal_geo : -s.normal_geo;
+    if (dot(ng, ldir) <= 0.0f) return black();
+    Col refl = opaque_eval(s, view, ldir);
+    float spdf = opaque_pdf(s, view, ldir, specular_probability(s, view));
+    float mis = power_heuristic(lpdf, spdf);
+    Col sky = sky_radiance<false>(S, ldir, c);
+    dnee = sky * tr * opaque_eval_dalbedo(s, view, ldir) * mis / lpdf;
+    return sky * tr * refl * mis / lpdf;
+}
+
+// Adjoint of x -> x / p, p = min(1, max component of x), at x (when p < 1).
+__device__ Col rr_adjoint(Col x, float p, Col a) {
+    if (!(p < 1.0f)) return a;
+    int m = (x.r >= x.g && x.r >= x.b) ? 0 : (x.g >= x.b ? 1 : 2);
+    float d = (x.r * a.r + x.g * a.g + x.b * a.b) / (p * p);
+    Col r = a / p;
+    if (m == 0) r.r -= d;
+    else if (m == 1) r.g -= d;
+    else r.b -= d;
+    return r;
+}
+
+// Adjoint of x -> x * (max / lum(x)) when lum(x) > max.
+__device__ Col clamp_adjoint(Col x, float max, Col a) {
+    float lum = luminance(x);
+    if (!(lum > max)) return a;
+    float k = max / lum;
+    float d = (x.r * a.r + x.g * a.g + x.b * a.b) / lum;
+    return Col{k * (a.r - 0.2126f * d), k * (a.g - 0.7152f * d), k * (a.b - 0.0722f * d)};
+}
+
+// sample_path (sr_render.cu) recording the vertices; rad / fog as the forward pass sums them.
+__device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t bounces, float indirect_clamp,
+                             AdjVertex* v, Col& radiance, Col& radiance_fog, Ctr& c, uint32_t* err) {
+    radiance = black();
+    radiance_fog = black();
+    Col energy = white();
+    bool has_spdf = false;
+    float spdf = 0.0f;
+    const float inf = __int_as_float(0x7f800000);
+    int n = 0;
+    for (uint32_t i = 0; i != bounces + 1; ++i) {
+        SurfHit hit;
+        bool has_hit = trace_surface<false>(S, ray, hit, c, err);
+        float sdist;
+        AdjVertex& x = v[n++];
+        x.e_in = energy;
+        x.rr = 1.0f;
+        x.clamp_max = indirect_clamp;
+        x.dadd = black();
+        x.ds = black();
+        if (S.has_fog && fog_scatter_distance(S, ray, has_hit ? hit.dist : inf, rng, sdist)) {
+            x.kind = AV_FOG;
+            energy = energy * col3(S.fog_color);
+            x.e_rr = energy;
+            x.add = sample_sky_direct_fog<false>(S, ray_at(ray, sdist), ray.d, rng, c, err);
+            Col srad = x.add * energy;
+            if (i == 0)
+                radiance_fog = radiance_fog + srad;
+            else
+                radiance = radiance + srad;
+            if (i >= 3) x.rr = fminf(1.0f, max_component(energy));
+            if (russian_roulette(energy, i, rng)) {
+                x.kind = AV_FOG_END;
+                break;
+            }
+            V3 sdir = hg_scatter_dir(ray.d, S.fog_g, rng);
+            has_spdf = true;
+            spdf = hg_pdf(dot(ray.d, sdir), S.fog_g);
+            ray = make_ray(ray_at(ray, sdist), sdir);
+        } else if (has_hit) {
+            const Surface& s = hit.surf;
+            float dist = hit.dist;
+            V3 view = -ray.d;
+            float bias = fmaxf(1e-4f, dist * 1e-4f);
+            V3 pos = ray_at(ray, dist - bias);
+            x.kind = AV_SURF;
+            x.uv = s.uv;
+            x.material = hit.material;
+            radiance = radiance + s.radiance * energy;
+            Col dnee;
+            Col nee = sample_sky_direct_adj(S, s, pos, view, rng, c, err, dnee);
+            radiance = radiance + nee * energy;
+            x.add = s.radiance + nee;
+            x.dadd = dnee;
+            if (i >= 3) x.rr = fminf(1.0f, max_component(energy));
+            if (russian_roulette(energy, i, rng)) {
+                x.kind = AV_SURF_END;
+                break;
+            }
+            x.e_rr = energy;
+            Scatter sc = surface_scatter(s, ray.d, view, rng);
+            x.s = sc.weight;
+            x.ds = opaque_eval_dalbedo(s, view, sc.dir) / fmaxf(sc.pdf, 1e-6f);
+            energy = energy * sc.weight;
+            x.pre = energy;
+            energy = clamp_luminance(energy, indirect_clamp);
+            has_spdf = sc.has_pdf;
+            spdf = sc.pdf;
+            ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
+        } else {
+            x.kind = AV_SKY;
+            float mis = has_spdf ? power_heuristic(spdf, sky_light_pdf(S, ray.d)) : 1.0f;
+            x.add = sky_radiance<false>(S, ray.d, c) * mis;
+            radiance = radiance + x.add * energy;
+            break;
+        }
+    }
+    return n;
+}
+
+// Passes d loss / d albedo at a surface vertex to the albedo texture's texels (the bilinear or
+// point lookup of Texture.Sample texture.cs:39-69, times the material's albedo).
+__device__ void scatter_albedo_grad(const DevScene& S, int material, V2 uv, Col g, int tex, float* grad) {
+    const DevMaterial& m = S.materials[material];
+    if (m.tex[0] != tex) return;
+    const DevTexture& t = S.textures[tex];
+    Col ga = g * col3(m.albedo_rough);
+    float u = uv.x * t.tiling_x;
+    u -= floorf(u);
+    float vv = uv.y * t.tiling_y;
+    vv -= floorf(vv);
+    const uint32_t w = t.width, h = t.height;
+    auto add = [&](uint32_t x, uint32_t y, float wt) {
+        float* p = grad + 3 * ((size_t)y * w + x);
+        atomicAdd(p, ga.r * wt);
+        atomicAdd(p + 1, ga.g * wt);
+        atomicAdd(p + 2, ga.b * wt);
+    };
+    if (t.filter == 1) {
+        add((uint32_t)(u * (float)w) % w, (uint32_t)(vv * (float)h) % h, 1.0f);
+        return;
+    }
+    float fx = u * (float)(w - 1), fy = vv * (float)(h - 1);
+    uint32_t x0 = (uint32_t)fx, y0 = (uint32_t)fy;
+    uint32_t x1 = (x0 + 1) % w, y1 = (y0 + 1) % h;
+    float tx = fx - (float)x0, ty = fy - (float)y0;
+    add(x0, y0, (1.0f - tx) * (1.0f - ty));
+    add(x1, y0, tx * (1.0f - ty));
+    add(x0, y1, (1.0f - tx) * ty);
+    add(x1, y1, tx * ty);
+}
+
+__global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, DevParams P, DevAovs fwd,
+                                                       const float* target, int tex, float* grad, float* replay,
+                                                       uint32_t* err) {
+    const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7), y = blockIdx.y * 8 + (threadIdx.x >> 3);
+    if (x >= P.width || y >= P.height) return;
+    const size_t i = (size_t)y * P.width + x;
+    const uint32_t count = fwd.samples[i];
+    const uint32_t taken = count < P.max_samples ? count : P.max_samples;  // the loop's off-by-one
+    const float inv = 1.0f / (float)count;
+    Col G{2.0f * (fwd.radiance[3 * i] + fwd.radiance_fog[3 * i] - target[3 * i]) * inv,
+          2.0f * (fwd.radiance[3 * i + 1] + fwd.radiance_fog[3 * i + 1] - target[3 * i + 1]) * inv,
+          2.0f * (fwd.radiance[3 * i + 2] + fwd.radiance_fog[3 * i + 2] - target[3 * i + 2]) * inv};
+    Ctr c;
+    AdjVertex v[kAdjMaxVertices];
+    Rng rng = rng_seed(x, y);
+    Col rad_sum = black(), fog_sum = black();
+    for (uint32_t si = 0; si < taken; ++si) {
+        Ray ray = camera_ray(V, P, x, y, rng);
+        Col rad, fog;
+        const int n = replay_sample(S, ray, rng, P.bounces, P.indirect_clamp, v, rad, fog, c, err);
+        rad_sum = rad_sum + rad;
+        fog_sum = fog_sum + fog;
+        // reverse sweep: a = d loss / d (throughput leaving the vertex)
+        Col a = black();
+        for (int k = n - 1; k >= 0; --k) {
+            const AdjVertex& q = v[k];
+            Col a_in;
+            if (q.kind == AV_SKY) {
+                a_in = G * q.add;
+            } else if (q.kind == AV_FOG || q.kind == AV_FOG_END) {
+                // e_rr = e_in * fog colour; add * e_rr; then the roulette divides e_rr
+                Col a_rr = (q.kind == AV_FOG ? rr_adjoint(q.e_rr, q.rr, a) : black()) + G * q.add;
+                a_in = a_rr * col3(S.fog_color);
+            } else if (q.kind == AV_SURF_END) {
+                a_in = G * q.add;
+                scatter_albedo_grad(S, q.material, q.uv, G * q.e_in * q.dadd, tex, grad);
+            } else {
+                const Col a_pre = clamp_adjoint(q.pre, q.clamp_max, a);
+                const Col a_s = q.e_rr * a_pre;
+                a_in = rr_adjoint(q.e_in, q.rr, q.s * a_pre) + G * q.add;
+                scatter_albedo_grad(S, q.material, q.uv, a_s * q.ds + G * q.e_in * q.dadd, tex, grad);
+            }
+            a = a_in;
+        }
+    }
+    if (replay) {
+        const Col r = rad_sum / (float)count, f = fog_sum / (float)count;
+        replay[3 * i] = r.r + f.r;
+        replay[3 * i + 1] = r.g + f.g;
+        replay[3 * i + 2] = r.b + f.b;
+    }
+}
+
+cudaError_t launch_adjoint_albedo(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
+                                  const float* target, int texture, float* grad, float* replay, uint32_t* err,
+                                  cudaStream_t stream) {
+    dim3 grid((P.width + 7) / 8, (P.height + 7) / 8);
+    k_adjoint_albedo<<<grid, 64, 0, stream>>>(S, V, P, fwd, target, texture, grad, replay, err);
+    return cudaGetLastError();
+}
+
+}  // namespace sr

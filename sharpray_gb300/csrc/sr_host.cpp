@@ -2,6 +2,7 @@
 // upload, render and compose entry points.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -114,6 +115,10 @@ struct SrContext {
     cudaStream_t batch_capture = nullptr;
     cudaGraphExec_t batch_exec = nullptr;
     std::vector<WaveLaunch> batch_launch;
+    // live scenes; sr_ctx_destroy with scenes still alive only marks the context closed, and the
+    // last sr_scene_destroy frees it (finalisers may run in any order)
+    std::vector<SrScene*> scenes;
+    bool closed = false;
 };
 
 struct SrScene {
@@ -157,6 +162,8 @@ struct SrScene {
     int sms = 0;
     WaveTune tune{};  // launch geometry (sr_scene_set_tuning / sr_scene_autotune)
     DevBuf tune_aovs;  // autotune's scratch AOV planes
+    std::vector<uint64_t> tex_offset;  // first texel of each texture in `texels` (textures present at build)
+    DevBuf tex_stage;                   // sr_scene_update_texture staging
     int last_mode = 0;                // render mode of the last render
     uint32_t last_host_iters = 0;     // bounces run by the host loop
     bool last_tail = false;           // the host loop launched the tail kernel
@@ -292,8 +299,7 @@ SR_API int sr_ctx_create(int device, SrContext** out_ctx) {
     return SR_OK;
 }
 
-SR_API int sr_ctx_destroy(SrContext* ctx) {
-    if (!ctx) return SR_OK;
+static void ctx_free(SrContext* ctx) {
     if (ctx->device >= 0) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
@@ -302,6 +308,12 @@ SR_API int sr_ctx_destroy(SrContext* ctx) {
         cudaStreamDestroy(ctx->stream);
     }
     delete ctx;
+}
+
+SR_API int sr_ctx_destroy(SrContext* ctx) {
+    if (!ctx) return SR_OK;
+    ctx->closed = true;
+    if (ctx->scenes.empty()) ctx_free(ctx);
     return SR_OK;
 }
 
@@ -398,19 +410,29 @@ SR_API int sr_mesh_bvh_export(SrContext* ctx, int32_t mesh, float* node_bounds, 
 
 SR_API int sr_scene_create(SrContext* ctx, SrScene** out_scene) {
     if (!ctx || !out_scene) return fail(SR_ERR_INVALID_ARG, "sr_scene_create: NULL argument");
+    if (ctx->closed) return fail(SR_ERR_STATE, "context destroyed");
     SrScene* s = new SrScene();
     s->ctx = ctx;
+    ctx->scenes.push_back(s);
     *out_scene = s;
     return SR_OK;
 }
 
 SR_API int sr_scene_destroy(SrScene* scene) {
     if (!scene) return SR_OK;
-    if (scene->ctx->device >= 0) {
-        cudaSetDevice(scene->ctx->device);
-        cudaStreamSynchronize(scene->ctx->stream);
+    SrContext* ctx = scene->ctx;
+    if (ctx->device >= 0) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+    }
+    if (ctx->batch_exec) {  // the cached batch graph may hold this scene's buffers
+        cudaGraphExecDestroy(ctx->batch_exec);
+        ctx->batch_exec = nullptr;
+        ctx->batch_launch.clear();
     }
     delete scene;
+    ctx->scenes.erase(std::find(ctx->scenes.begin(), ctx->scenes.end(), scene));
+    if (ctx->closed && ctx->scenes.empty()) ctx_free(ctx);
     return SR_OK;
 }
 
@@ -552,12 +574,14 @@ SR_API int sr_scene_build(SrScene* s) {
     // Textures (all of the context's, so ids stay valid).
     std::vector<DevTexture> texs(ctx->textures.size());
     std::vector<float4> texels;
+    s->tex_offset.assign(ctx->textures.size(), 0);
     for (size_t i = 0; i < ctx->textures.size(); ++i) {
         const TextureHost& t = *ctx->textures[i];
         DevTexture& d = texs[i];
         std::memset(&d, 0, sizeof(d));
         d.width = t.width, d.height = t.height, d.filter = t.filter, d.tiling_x = t.tiling_x, d.tiling_y = t.tiling_y;
         d.offset = texels.size();
+        s->tex_offset[i] = texels.size();
         for (size_t k = 0; k < (size_t)t.width * t.height; ++k)
             texels.push_back(mk4(t.texels[3 * k], t.texels[3 * k + 1], t.texels[3 * k + 2], 0.0f));
     }
@@ -1684,5 +1708,46 @@ SR_API int sr_image_save(const char* path, uint32_t w, uint32_t h, const uint8_t
     } catch (const ImageError& e) {
         return fail(SR_ERR_IO, "%s", e.what());
     }
+    return SR_OK;
+}
+
+SR_API int sr_adjoint_albedo(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
+                             const float* target, int32_t texture, float* grad, float* replay, void* stream) {
+    if (!s || !fwd || !target || !grad) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    if (!fwd->radiance || !fwd->radiance_fog || !fwd->samples)
+        return fail(SR_ERR_INVALID_ARG, "sr_adjoint_albedo needs the forward radiance, radiance_fog and samples planes");
+    if (texture < 0 || (size_t)texture >= s->tex_offset.size())
+        return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
+    if (s->dev.has_transparent) return fail(SR_ERR_STATE, "sr_adjoint_albedo does not support transparent materials");
+    DevView dv;
+    DevParams dp;
+    if (int rc = make_view(view, params, dv, dp)) return rc;
+    if (dp.bounces > 16) return fail(SR_ERR_INVALID_ARG, "sr_adjoint_albedo supports at most 16 bounces");
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
+    SR_CUDA(launch_adjoint_albedo(s->dev, dv, dp, f, target, texture, grad, replay, s->err.as<uint32_t>(), st),
+            "adjoint launch");
+    return SR_OK;
+}
+
+SR_API int sr_scene_update_texture(SrScene* s, int32_t texture, const float* texels_rgb) {
+    if (!s || !texels_rgb) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    if (texture < 0 || (size_t)texture >= s->tex_offset.size())
+        return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
+    if (s->sky_kind == 0 && s->sky_texture == texture)
+        return fail(SR_ERR_INVALID_ARG, "texture %d is the sky texture", texture);
+    const TextureHost& t = *s->ctx->textures[texture];
+    const size_t n = (size_t)t.width * t.height;
+    std::vector<float4> rec(n);
+    for (size_t k = 0; k < n; ++k) rec[k] = mk4(texels_rgb[3 * k], texels_rgb[3 * k + 1], texels_rgb[3 * k + 2], 0.0f);
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = s->ctx->stream;
+    SR_CUDA(cudaMemcpyAsync(s->texels.as<float4>() + s->tex_offset[texture], rec.data(), n * sizeof(float4),
+                            cudaMemcpyHostToDevice, st),
+            "upload texels");
+    SR_CUDA(cudaStreamSynchronize(st), "upload texels");
     return SR_OK;
 }

@@ -19,6 +19,7 @@ struct Fragment {
 struct SurfHit {
     Surface surf;
     float dist;
+    int32_t material;  // index into DevScene::materials
 };
 
 // The Surface of a scene hit: Scene.Trace after the BVH query (scene.cs:608-621): inflate the
@@ -55,6 +56,7 @@ __device__ __forceinline__ void surface_from_hit(const DevScene& S, const Ray& r
     s.tangent = {tdir.x, tdir.y, tdir.z, h.tan.w};
     s.uv = h.uv;
     out.dist = h.dist;
+    out.material = o.index;
 }
 
 // Scene.Trace scene.cs:602-625.

@@ -1,0 +1,184 @@
+"""Path-replay adjoint (sr_adjoint_albedo) against central finite differences of the renderer's own
+image loss, and sr_scene_update_texture against a scene built from scratch.
+
+The loss is L = sum over pixels and channels of (radiance + radiance_fog - target)^2.  At fixed
+random numbers the renderer's estimator is a smooth function of the albedo texels of a
+non-metallic surface (directions, lobe choices and pdfs do not depend on them), so central
+differences of L through sr_scene_update_texture + sr_render_device check the adjoint directly.
+Roulette decisions can flip under a perturbation; where that happens the finite differences at
+eps and 2 eps disagree and that texel channel is left out (the tests require most to be checked).
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from sharpray_gb300 import (Context, Fog, Quat, SharpRayError, Transform, View, _abi, adjoint_albedo, render_params,
+                            synth)
+from sharpray_gb300.synth import MeshDesc, ObjectDesc, SceneDesc, TextureDesc, look_rotation
+
+pytestmark = pytest.mark.gpu
+
+PLANES = (("radiance", 3, "float32"), ("radiance_fog", 3, "float32"), ("normals", 3, "float32"), ("uv", 2, "float32"),
+          ("depth", 1, "float32"), ("samples", 1, "int32"), ("variance", 1, "float32"))
+
+
+def adjoint_scene(fog: bool, bounces: int, clamp: float, w=40, h=30, spp=3) -> SceneDesc:
+    """Textured ground and blob sharing one bilinear albedo texture (different material albedos,
+    tiling 2 on the blob), a point-filtered texture on a second blob, an untextured rock."""
+    rng = np.random.default_rng(7)
+    gpos, guv = synth.ground_quad(3.0, -1.0)
+    bpos, buv = synth.uv_sphere(10, 14, amplitude=0.1, seed=2)
+    rpos, ruv = synth.uv_sphere(8, 10, amplitude=0.2, seed=4)
+    d = SceneDesc("adjoint")
+    d.meshes = [MeshDesc(gpos, guv, smooth_normals=False), MeshDesc(bpos, buv), MeshDesc(rpos, ruv)]
+    d.textures = [TextureDesc(synth._rgbe_texels(synth.sky_env(64, 32, seed=3, sun_peak=20.0, sun_sigma_deg=6.0))),
+                  TextureDesc(rng.uniform(0.2, 0.9, (6, 8, 3)).astype(np.float32), 0, (1.0, 1.0)),
+                  TextureDesc(rng.uniform(0.2, 0.9, (4, 4, 3)).astype(np.float32), 1, (1.0, 1.0))]
+    d.sky = ("texture", 0, 1.0, 0.3)
+    d.objects = [
+        ObjectDesc("ground", Transform(), {"albedo": (0.9, 0.8, 0.7), "roughness": 0.7, "color_texture": 1},
+                   ("mesh", 0)),
+        ObjectDesc("blob", Transform((-0.6, -0.2, 0.8), Quat.identity(), (0.7, 0.7, 0.7)),
+                   {"albedo": (1.0, 0.9, 0.8), "roughness": 0.4, "color_texture": 1}, ("mesh", 1)),
+        ObjectDesc("pointblob", Transform((0.9, -0.4, 0.4), Quat.angle_axis(0.5, (0.0, 1.0, 0.0)), (0.5, 0.5, 0.5)),
+                   {"albedo": (0.8, 0.8, 0.8), "roughness": 0.5, "color_texture": 2}, ("mesh", 1)),
+        ObjectDesc("rock", Transform((0.2, -0.7, -0.6), Quat.identity(), (0.3, 0.3, 0.3)),
+                   {"albedo": (0.5, 0.5, 0.45), "roughness": 0.6}, ("mesh", 2)),
+    ]
+    # the blob's tiling: a second TextureDesc would be a second texture, so tile through its uvs
+    d.meshes[1] = MeshDesc(bpos, buv * np.float32(2.0))
+    if fog:
+        d.fog = Fog(0.08, (0.8, 0.75, 0.7), 0.5, 0.2)
+    cam = (0.0, 0.9, -3.2)
+    d.view = View(Transform(cam, look_rotation(cam, (0.0, -0.4, 0.5))), math.radians(55.0), 0.1)
+    d.width, d.height, d.spp, d.bounces = w, h, spp, bounces
+    d.min_samples = spp
+    d.variance_threshold = 0.0  # every pixel takes spp samples (count spp + 1, the loop's off-by-one)
+    d.indirect_clamp = clamp
+    return d
+
+
+class Rig:
+    def __init__(self, torch, d: SceneDesc):
+        self.torch, self.d = torch, d
+        self.ctx = Context(0)
+        self.scene = d.instantiate(self.ctx)
+        self.scene.build()
+        self.tex = self.scene._keepalive[0]
+        n = d.width * d.height
+        self.bufs = {k: torch.zeros(n * c, dtype=getattr(torch, t), device="cuda") for k, c, t in PLANES}
+        self.aovs = _abi.SrAovs(*[self.bufs[k].data_ptr() for k, _, _ in PLANES])
+        self.params = render_params(*d.render_args())
+
+    def image(self) -> np.ndarray:
+        v = self.d.view.to_c()
+        _abi.check(self.ctx._lib.sr_render_device(self.scene.handle, C.byref(v), C.byref(self.params),
+                                                  C.byref(self.aovs), None))
+        self.torch.cuda.synchronize()
+        return (self.bufs["radiance"] + self.bufs["radiance_fog"]).cpu().numpy()
+
+    def loss(self, target: np.ndarray) -> float:
+        r = self.image().astype(np.float64) - target.astype(np.float64)
+        return float(np.dot(r, r))
+
+    def gradient(self, target: np.ndarray, tex_index: int):
+        torch = self.torch
+        self.image()
+        t = self.tex[tex_index]
+        grad = torch.zeros(t.height * t.width * 3, dtype=torch.float32, device="cuda")
+        replay = torch.zeros(self.d.width * self.d.height * 3, dtype=torch.float32, device="cuda")
+        tgt = torch.from_numpy(target).cuda()
+        adjoint_albedo(self.scene, self.d.view, self.params, self.aovs, tgt.data_ptr(), t, grad.data_ptr(),
+                       replay.data_ptr())
+        torch.cuda.synchronize()
+        fwd = (self.bufs["radiance"] + self.bufs["radiance_fog"]).cpu().numpy()
+        return grad.cpu().numpy().reshape(t.height, t.width, 3), replay.cpu().numpy(), fwd
+
+
+def check_against_fd(rig: Rig, tex_index: int, picks: int, seed: int, eps: float, min_checked: int):
+    target = (rig.image() * np.float32(0.6) + np.float32(0.05)).astype(np.float32)
+    grad, replay, fwd = rig.gradient(target, tex_index)
+    assert np.array_equal(replay.view(np.uint32), fwd.view(np.uint32)), "replay must reproduce the forward image"
+    tex = rig.tex[tex_index]
+    base = rig.d.textures[tex_index].texels.copy()
+    rng = np.random.default_rng(seed)
+    scale = float(np.abs(grad).max())
+    assert scale > 0.0
+    # texel channels with the largest gradients plus random ones
+    flat = np.argsort(-np.abs(grad).ravel())[: picks // 2].tolist()
+    flat += rng.choice(grad.size, picks - len(flat), replace=False).tolist()
+    checked = 0
+    for f in flat:
+        y, x, ch = np.unravel_index(f, grad.shape)
+        fds = []
+        for e in (eps, 2.0 * eps):
+            vals = []
+            for sgn in (1.0, -1.0):
+                t = base.copy()
+                t[y, x, ch] += np.float32(sgn * e)
+                rig.scene.update_texture(tex, t)
+                vals.append(rig.loss(target))
+            fds.append((vals[0] - vals[1]) / (2.0 * e))
+        rig.scene.update_texture(tex, base)
+        if abs(fds[0] - fds[1]) > 0.02 * max(abs(fds[0]), 1e-3 * scale):
+            continue  # a roulette decision flipped inside the step
+        checked += 1
+        g = float(grad[y, x, ch])
+        assert abs(g - fds[0]) <= 0.02 * abs(fds[0]) + 2e-3 * scale, (y, x, ch, g, fds)
+    assert checked >= min_checked, f"only {checked} of {len(flat)} texel channels had stable differences"
+    # the scene is back to its own texture
+    assert np.array_equal(rig.image().view(np.uint32), fwd.view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def torch_mod():
+    return pytest.importorskip("torch")
+
+
+@pytest.mark.parametrize("fog,clamp", [(False, 10.0), (True, 10.0), (False, 0.6)])
+def test_adjoint_matches_finite_differences_two_bounces(torch_mod, fog, clamp):
+    """Two bounces: no roulette; the clamp case exercises the clamp's Jacobian."""
+    rig = Rig(torch_mod, adjoint_scene(fog, 2, clamp))
+    check_against_fd(rig, 1, picks=10, seed=1, eps=1e-2, min_checked=10)
+    check_against_fd(rig, 2, picks=6, seed=2, eps=1e-2, min_checked=6)
+
+
+def test_adjoint_matches_finite_differences_with_roulette(torch_mod):
+    """Six bounces with fog: roulette from the fourth vertex on (divisions by the survival
+    probability, differentiated as a function of the throughput)."""
+    rig = Rig(torch_mod, adjoint_scene(True, 6, 3.0))
+    check_against_fd(rig, 1, picks=10, seed=3, eps=2e-4, min_checked=6)
+
+
+def test_update_texture_equals_fresh_build(torch_mod):
+    d = adjoint_scene(True, 3, 10.0)
+    rig = Rig(torch_mod, d)
+    new = np.random.default_rng(11).uniform(0.1, 1.0, d.textures[1].texels.shape).astype(np.float32)
+    rig.scene.update_texture(rig.tex[1], new)
+    got = rig.image()
+    d2 = adjoint_scene(True, 3, 10.0)
+    d2.textures[1] = TextureDesc(new, 0, (1.0, 1.0))
+    fresh = Rig(torch_mod, d2)
+    assert np.array_equal(got.view(np.uint32), fresh.image().view(np.uint32))
+
+
+def test_adjoint_rejects(torch_mod):
+    torch = torch_mod
+    rig = Rig(torch, adjoint_scene(False, 2, 10.0, w=8, h=8, spp=1))
+    with pytest.raises(SharpRayError):  # the sky texture
+        rig.scene.update_texture(rig.tex[0], rig.d.textures[0].texels)
+    tgt = torch.zeros(8 * 8 * 3, device="cuda")
+    g = torch.zeros(6 * 8 * 3, device="cuda")
+    deep = render_params(8, 8, 32, 1, 1, 0.0, 17, 10.0)
+    with pytest.raises(SharpRayError):
+        adjoint_albedo(rig.scene, rig.d.view, deep, rig.aovs, tgt.data_ptr(), rig.tex[1], g.data_ptr())
+    with pytest.raises(SharpRayError):
+        adjoint_albedo(rig.scene, rig.d.view, rig.params, rig.aovs, tgt.data_ptr(), 99, g.data_ptr())
+    glass = synth.config_features(8, 8, 1)  # has a transparent sphere
+    gs = glass.instantiate(Context(0))
+    gs.build()
+    with pytest.raises(SharpRayError):
+        adjoint_albedo(gs, glass.view, render_params(*glass.render_args()), rig.aovs, tgt.data_ptr(), 1,
+                       g.data_ptr())

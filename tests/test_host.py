@@ -131,3 +131,14 @@ def test_tuning_validation(host_ctx):
     assert (t.trace_blocks_per_sm, t.fog_shade_blocks_per_sm, t.surface_shade_blocks_per_sm, t.tail_divisor) == (3, 4, 2, 8)
     with pytest.raises(SharpRayError):
         s.set_tuning(-1)
+
+
+def test_context_outlived_by_scene(native_lib):
+    """Destroying a context before its scenes (finalisers run in any order) defers the free."""
+    import ctypes as C
+    from sharpray_gb300 import _abi
+    ctx, sc = C.c_void_p(), C.c_void_p()
+    _abi.check(native_lib.sr_ctx_create(-1, C.byref(ctx)))
+    _abi.check(native_lib.sr_scene_create(ctx, C.byref(sc)))
+    _abi.check(native_lib.sr_ctx_destroy(ctx))
+    _abi.check(native_lib.sr_scene_destroy(sc))
