@@ -58,6 +58,8 @@ def parse():
                     help="autotune each batched scene with trial renders at this spp (0: defaults)")
     ap.add_argument("--batch-scenes", type=int, default=32,
                     help="scenes of the batched workload timed batched vs one after another (0: skip)")
+    ap.add_argument("--adjoint-checks", type=int, default=64,
+                    help="adjoint workload: texel channels checked by finite differences (-1: skip the workload)")
     ap.add_argument("--profile-once", action="store_true",
                     help="set up, render + compose exactly once, exit (for ncu captures)")
     return ap.parse_args()
@@ -240,6 +242,106 @@ def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
                     "graph-captured render per scene, back to back; images bit-identical"}
 
 
+def measure_adjoint(checks: int, reps: int = 5) -> dict:
+    """The differentiable workload (synth.config_c4): forward render, then the path-replay adjoint of
+    L = sum (I - T)^2 for the albedo texture, T rendered from the textures perturbed by N(0, 0.05).
+    grads/s = texel-channel gradients produced per second (the texture's h x w x 3 per adjoint pass).
+    `checks` random (texel, channel) pairs that the image depends on are compared with central
+    differences of L (h = 1e-3 and 2e-3, common random numbers through sr_scene_update_texture_device);
+    a pair whose two differences disagree by > 2 % saw a roulette decision flip and is not scored."""
+    import ctypes as C
+
+    import torch
+    import numpy as np
+    from sharpray_gb300 import Context, _abi, adjoint_albedo, render_params, synth
+    from sharpray_gb300.autograd import device_aovs
+    d = synth.config_c4()
+    ctx = Context(0)
+    sc = d.instantiate(ctx)
+    sc.build()
+    tex_a, tex_r = sc._keepalive[0][1], sc._keepalive[0][2]
+    p = render_params(*d.render_args())
+    v = d.view.to_c()
+    st = torch.cuda.Stream()
+    sp = C.c_void_p(st.cuda_stream)
+    bufs, aovs = device_aovs(d.width, d.height)
+    lib = ctx._lib
+    base_a = torch.from_numpy(d.textures[1].texels).cuda()
+    base_r = torch.from_numpy(d.textures[2].texels).cuda()
+    g = torch.Generator(device="cpu").manual_seed(4)
+    st.wait_stream(torch.cuda.current_stream())  # the planes and base textures above
+
+    def render():
+        _abi.check(lib.sr_render_device(sc.handle, C.byref(v), C.byref(p), C.byref(aovs), sp))
+
+    def image():
+        return bufs["radiance"] + bufs["radiance_fog"]
+
+    with torch.cuda.stream(st):
+        noise = lambda t: (t + 0.05 * torch.randn(t.shape, generator=g).cuda()).clamp(0.0, 1.0)
+        sc.update_texture_device(tex_a, noise(base_a).contiguous().data_ptr(), st.cuda_stream)
+        sc.update_texture_device(tex_r, noise(base_r).contiguous().data_ptr(), st.cuda_stream)
+        render()
+        target = image().clone()
+        sc.update_texture_device(tex_a, base_a.data_ptr(), st.cuda_stream)
+        sc.update_texture_device(tex_r, base_r.data_ptr(), st.cuda_stream)
+        grad = torch.zeros_like(base_a)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        fwd_ms, adj_ms = [], []
+        for i in range(reps + 1):
+            ev[0].record(st)
+            render()
+            ev[1].record(st)
+            d_img = 2.0 * (image() - target)
+            grad.zero_()
+            e2 = torch.cuda.Event(enable_timing=True)
+            e2.record(st)
+            adjoint_albedo(sc, d.view, p, aovs, d_img.data_ptr(), tex_a, grad.data_ptr(), None, st.cuda_stream)
+            ev[2].record(st)
+            st.synchronize()
+            if i:  # the first pass is a warm-up
+                fwd_ms.append(ev[0].elapsed_time(ev[1]))
+                adj_ms.append(e2.elapsed_time(ev[2]))
+        loss0 = float(((image().double() - target.double()) ** 2).sum())
+
+        def loss_at(y, x, c, delta):
+            t = base_a.clone()
+            t[y, x, c] += delta
+            sc.update_texture_device(tex_a, t.data_ptr(), st.cuda_stream)
+            render()
+            return float(((image().double() - target.double()) ** 2).sum())
+
+        seen = (grad.abs().sum(dim=2) > 0).nonzero().cpu().numpy()
+        rng = np.random.default_rng(4)
+        picks = seen[rng.choice(len(seen), min(checks, len(seen)), replace=False)] if checks > 0 else []
+        rel, skipped = [], 0
+        for y, x in picks:
+            c = int(rng.integers(3))
+            fd = [(loss_at(y, x, c, h) - loss_at(y, x, c, -h)) / (2 * h) for h in (1e-3, 2e-3)]
+            if abs(fd[0] - fd[1]) > 0.02 * abs(fd[0]):
+                skipped += 1
+                continue
+            rel.append(abs(float(grad[y, x, c]) - fd[0]) / max(abs(fd[0]), 1e-12))
+        sc.update_texture_device(tex_a, base_a.data_ptr(), st.cuda_stream)
+        st.synchronize()
+    n_grad = base_a.numel()
+    adj_s = statistics.median(adj_ms) / 1000.0
+    fwd_s = statistics.median(fwd_ms) / 1000.0
+    samples = d.width * d.height * d.spp
+    rel_a = np.array(rel) if rel else np.zeros(0)
+    return {"workload": f"{d.name}: {d.triangle_count} triangles, 512x512 albedo + roughness textures, depth 6, "
+                        "L2 loss vs textures + N(0, 0.05)",
+            "grads_per_s": n_grad / adj_s, "unit": "texel-channel gradients/s",
+            "adjoint_ms": 1000 * adj_s, "forward_ms": 1000 * fwd_s,
+            "replayed_samples_per_s": samples / adj_s, "forward_samples_per_s": samples / fwd_s,
+            "loss": loss0, "fd_checked": len(rel), "fd_skipped_roulette_flip": skipped,
+            "fd_rel_err_median": float(np.median(rel_a)) if len(rel_a) else None,
+            "fd_rel_err_max": float(rel_a.max()) if len(rel_a) else None,
+            "fd_within_1pct": float((rel_a <= 0.01).mean()) if len(rel_a) else None,
+            "note": "gradient w.r.t. the albedo texture; sampling, roulette decisions, pdfs and MIS detached "
+                    "(path replay); FD: central, h = 1e-3, common random numbers"}
+
+
 def run_reference(args):
     rank, _, world = dist_info()
     if rank != 0:
@@ -409,6 +511,10 @@ def run_ours(args):
     if args.batch_scenes > 0 and rank == 0:
         batched = measure_batch(ctx, args.batch_scenes, stream, sp, args.batch_autotune_spp)
 
+    adjoint = None
+    if args.adjoint_checks >= 0 and rank == 0:
+        adjoint = measure_adjoint(args.adjoint_checks)
+
     # end to end through the public API with pinned host outputs
     host = Aovs(W, H)
     pinned = {}
@@ -484,6 +590,7 @@ def run_ours(args):
             "variants_samples_per_s": variants,
             "batched": batched,
             "autotune": tuning,
+            "adjoint": adjoint,
             "clocks": clocks.summary(),
             "counters_per_step": counters,
             # closest-hit + shadow queries per second (SceneTrace + SceneOcclude counters)

@@ -351,22 +351,25 @@ SR_API int sr_scene_autotune(SrScene* scene, const SrView* view, const SrRenderP
                              SrTuning* chosen);
 
 /* ---- derivatives (no counterpart in the reference, which renders forward only) ------------- */
-/* Path-replay adjoint: the gradient of the image loss sum over pixels and channels of
- * (radiance + radiance_fog - target)^2 with respect to the texels of albedo texture `texture`,
- * for the image that sr_render_device produced with the same scene, view and params (`forward`:
- * its radiance, radiance_fog and samples planes, device pointers).  `target` is a device
- * width x height x 3 image; the gradient is ADDED into `grad` (device, texture width x height x 3).
- * `replay` (device, width x height x 3, may be NULL) receives the replayed radiance + radiance_fog,
- * which equals the forward image.  Sampled directions, roulette decisions, pdfs and MIS weights
- * are held fixed (detached); the BRDF values and scatter weights are differentiated.  Scenes with
- * transparent materials and params->bounces > 16 are refused.  Runs asynchronously on `stream`. */
+/* Path-replay adjoint: for the image I = radiance + radiance_fog that sr_render_device produced
+ * with the same scene, view and params (`forward`: its radiance, radiance_fog and samples planes,
+ * device pointers) and the gradient d_image = dL/dI of any loss L (device, width x height x 3;
+ * for L = sum (I - target)^2 it is 2 (I - target)), ADDS dL/d(texels of albedo texture
+ * `texture`) into `grad` (device, texture width x height x 3).  `replay` (device, width x height x 3,
+ * may be NULL) receives the replayed image, which equals I.  Sampled directions, roulette
+ * decisions, pdfs and MIS weights are held fixed (detached); the BRDF values and scatter weights
+ * are differentiated.  Scenes with transparent materials and params->bounces > 16 are refused.
+ * Runs asynchronously on `stream`. */
 SR_API int sr_adjoint_albedo(SrScene* scene, const SrView* view, const SrRenderParams* params,
-                             const SrAovs* forward, const float* target, int32_t texture, float* grad,
+                             const SrAovs* forward, const float* d_image, int32_t texture, float* grad,
                              float* replay, void* stream);
 /* Replaces the texels of texture `texture` (rgb floats, its width x height) in a built scene's
  * device copy, e.g. one step of inverse rendering.  The context's texture and other scenes are left
  * as they are.  The scene's sky texture is refused (its light distribution is built from it). */
 SR_API int sr_scene_update_texture(SrScene* scene, int32_t texture, const float* texels_rgb);
+/* The same from device memory, asynchronously on `stream`. */
+SR_API int sr_scene_update_texture_device(SrScene* scene, int32_t texture, const float* d_texels_rgb,
+                                          void* stream);
 
 /* ---- asset ingest (host-side file parsing) ------------------------------------------------- */
 /* Image.Load (image.cs:214-273: uncompressed 24-bit TrueColor / 8-bit Grayscale .tga, rows top-down)

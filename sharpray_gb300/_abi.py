@@ -191,6 +191,7 @@ PROTOTYPES = {
     "sr_adjoint_albedo": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P, C.c_int32,
                                _P, _P, _P]),
     "sr_scene_update_texture": (_I, [_P, C.c_int32, _P]),
+    "sr_scene_update_texture_device": (_I, [_P, C.c_int32, _P, _P]),
 }
 
 

@@ -452,6 +452,13 @@ class Scene:
         t = np.ascontiguousarray(texels, dtype=np.float32)
         check(self._lib.sr_scene_update_texture(self.handle, tid, ptr(t)))
 
+    def update_texture_device(self, texture, d_texels: int, stream: Optional[int] = None) -> None:
+        """sr_scene_update_texture_device: the same from a device pointer (float32 h x w x 3),
+        asynchronous on `stream`."""
+        tid = texture.id if isinstance(texture, Texture) else int(texture)
+        check(self._lib.sr_scene_update_texture_device(self.handle, tid, C.c_void_p(d_texels),
+                                                       C.c_void_p(stream) if stream else None))
+
     def load_obj(self, path, transform: Optional["Transform"] = None, material: Optional["Material"] = None,
                  smooth_normals: bool = True) -> int:
         """ObjLoader.Load(path, scene, config) obj.cs:139-259: adds one object per OBJ group; returns
@@ -808,16 +815,17 @@ def render_batch(scenes: Sequence["Scene"], views: Sequence["View"], params: Seq
     check(lib.sr_render_batch(arr_s, arr_v, arr_p, arr_a, n, C.c_void_p(stream) if stream else None))
 
 
-def adjoint_albedo(scene: "Scene", view: "View", params: SrRenderParams, forward: SrAovs, target: int,
+def adjoint_albedo(scene: "Scene", view: "View", params: SrRenderParams, forward: SrAovs, d_image: int,
                    texture, grad: int, replay: Optional[int] = None, stream: Optional[int] = None) -> None:
-    """sr_adjoint_albedo: adds d/d(texels of `texture`) of sum (radiance + radiance_fog - target)^2
-    into `grad` for the image `forward` (device AOV planes of sr_render_device with the same scene,
-    view and params).  target / grad / replay are device pointers; asynchronous on `stream`."""
+    """sr_adjoint_albedo: adds dL/d(texels of `texture`) into `grad`, given d_image = dL/dI for the
+    image I = radiance + radiance_fog of `forward` (device AOV planes of sr_render_device with the
+    same scene, view and params).  d_image / grad / replay are device pointers (float32, H x W x 3
+    and the texture's h x w x 3); asynchronous on `stream`."""
     tid = texture.id if isinstance(texture, Texture) else int(texture)
     v = view.to_c()
-    check(scene._lib.sr_adjoint_albedo(scene.handle, C.byref(v), C.byref(params), C.byref(forward), C.c_void_p(target),
-                                       tid, C.c_void_p(grad), C.c_void_p(replay) if replay else None,
-                                       C.c_void_p(stream) if stream else None))
+    check(scene._lib.sr_adjoint_albedo(scene.handle, C.byref(v), C.byref(params), C.byref(forward),
+                                       C.c_void_p(d_image), tid, C.c_void_p(grad),
+                                       C.c_void_p(replay) if replay else None, C.c_void_p(stream) if stream else None))
 
 
 def load_image(path) -> np.ndarray:

@@ -1,6 +1,6 @@
 // sr_adjoint.cu — path-replay adjoint of a rendered image with respect to the texels of an albedo
-// (colour) texture: the gradient of the loss sum_pixels |I - T|^2, I = radiance + radiance_fog, for
-// a target image T.  No counterpart in the reference (it has no derivatives).
+// (colour) texture: given dL/dI for the image I = radiance + radiance_fog of a render, the gradient
+// dL/d(texels).  No counterpart in the reference (it has no derivatives).
 //
 // One thread per pixel replays the pixel's samples exactly as the per-pixel path loop renders
 // them (the same RNG stream and the same functions, so the same paths and the same radiance --
@@ -221,7 +221,7 @@ __device__ void scatter_albedo_grad(const DevScene& S, int material, V2 uv, Col 
 }
 
 __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, DevParams P, DevAovs fwd,
-                                                       const float* target, int tex, float* grad, float* replay,
+                                                       const float* d_image, int tex, float* grad, float* replay,
                                                        uint32_t* err) {
     const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7), y = blockIdx.y * 8 + (threadIdx.x >> 3);
     if (x >= P.width || y >= P.height) return;
@@ -229,9 +229,7 @@ __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, De
     const uint32_t count = fwd.samples[i];
     const uint32_t taken = count < P.max_samples ? count : P.max_samples;  // the loop's off-by-one
     const float inv = 1.0f / (float)count;
-    Col G{2.0f * (fwd.radiance[3 * i] + fwd.radiance_fog[3 * i] - target[3 * i]) * inv,
-          2.0f * (fwd.radiance[3 * i + 1] + fwd.radiance_fog[3 * i + 1] - target[3 * i + 1]) * inv,
-          2.0f * (fwd.radiance[3 * i + 2] + fwd.radiance_fog[3 * i + 2] - target[3 * i + 2]) * inv};
+    Col G{d_image[3 * i] * inv, d_image[3 * i + 1] * inv, d_image[3 * i + 2] * inv};
     Ctr c;
     AdjVertex v[kAdjMaxVertices];
     Rng rng = rng_seed(x, y);
@@ -274,10 +272,26 @@ __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, De
 }
 
 cudaError_t launch_adjoint_albedo(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
-                                  const float* target, int texture, float* grad, float* replay, uint32_t* err,
+                                  const float* d_image, int texture, float* grad, float* replay, uint32_t* err,
                                   cudaStream_t stream) {
     dim3 grid((P.width + 7) / 8, (P.height + 7) / 8);
-    k_adjoint_albedo<<<grid, 64, 0, stream>>>(S, V, P, fwd, target, texture, grad, replay, err);
+    k_adjoint_albedo<<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err);
+    return cudaGetLastError();
+}
+
+// rgb float triples -> the texel records (rgb + pad) of one texture.
+__global__ void k_texels_from_rgb(const float* __restrict__ rgb, float4* __restrict__ out, size_t n) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+        float4 t;
+        t.x = rgb[3 * k], t.y = rgb[3 * k + 1], t.z = rgb[3 * k + 2], t.w = 0.0f;
+        out[k] = t;
+    }
+}
+
+cudaError_t launch_texels_from_rgb(const float* rgb, float4* out, size_t n, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    size_t blocks = (n + 255) / 256;
+    k_texels_from_rgb<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(rgb, out, n);
     return cudaGetLastError();
 }
 

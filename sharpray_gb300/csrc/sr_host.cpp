@@ -1712,8 +1712,8 @@ SR_API int sr_image_save(const char* path, uint32_t w, uint32_t h, const uint8_t
 }
 
 SR_API int sr_adjoint_albedo(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
-                             const float* target, int32_t texture, float* grad, float* replay, void* stream) {
-    if (!s || !fwd || !target || !grad) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+                             const float* d_image, int32_t texture, float* grad, float* replay, void* stream) {
+    if (!s || !fwd || !d_image || !grad) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     if (int rc = need_device(s)) return rc;
     if (!fwd->radiance || !fwd->radiance_fog || !fwd->samples)
         return fail(SR_ERR_INVALID_ARG, "sr_adjoint_albedo needs the forward radiance, radiance_fog and samples planes");
@@ -1727,18 +1727,23 @@ SR_API int sr_adjoint_albedo(SrScene* s, const SrView* view, const SrRenderParam
     SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
     cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
     DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
-    SR_CUDA(launch_adjoint_albedo(s->dev, dv, dp, f, target, texture, grad, replay, s->err.as<uint32_t>(), st),
+    SR_CUDA(launch_adjoint_albedo(s->dev, dv, dp, f, d_image, texture, grad, replay, s->err.as<uint32_t>(), st),
             "adjoint launch");
     return SR_OK;
 }
 
-SR_API int sr_scene_update_texture(SrScene* s, int32_t texture, const float* texels_rgb) {
-    if (!s || !texels_rgb) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+static int updatable_texture(SrScene* s, int32_t texture) {
     if (int rc = need_device(s)) return rc;
     if (texture < 0 || (size_t)texture >= s->tex_offset.size())
         return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
     if (s->sky_kind == 0 && s->sky_texture == texture)
         return fail(SR_ERR_INVALID_ARG, "texture %d is the sky texture", texture);
+    return SR_OK;
+}
+
+SR_API int sr_scene_update_texture(SrScene* s, int32_t texture, const float* texels_rgb) {
+    if (!s || !texels_rgb) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = updatable_texture(s, texture)) return rc;
     const TextureHost& t = *s->ctx->textures[texture];
     const size_t n = (size_t)t.width * t.height;
     std::vector<float4> rec(n);
@@ -1749,5 +1754,17 @@ SR_API int sr_scene_update_texture(SrScene* s, int32_t texture, const float* tex
                             cudaMemcpyHostToDevice, st),
             "upload texels");
     SR_CUDA(cudaStreamSynchronize(st), "upload texels");
+    return SR_OK;
+}
+
+SR_API int sr_scene_update_texture_device(SrScene* s, int32_t texture, const float* d_texels_rgb, void* stream) {
+    if (!s || !d_texels_rgb) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = updatable_texture(s, texture)) return rc;
+    const TextureHost& t = *s->ctx->textures[texture];
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    SR_CUDA(launch_texels_from_rgb(d_texels_rgb, s->texels.as<float4>() + s->tex_offset[texture],
+                                   (size_t)t.width * t.height, st),
+            "update texels");
     return SR_OK;
 }

@@ -437,6 +437,43 @@ def config_batch(count: int = 32, seed: int = 3) -> list:
     return out
 
 
+def value_noise_float(size: int, seed: int, lo: float, hi: float, channels: int = 3, cells: int = 16) -> np.ndarray:
+    """Float32 value noise in [lo, hi], (size, size, channels) (the same field as value_noise_rgba8,
+    unquantised)."""
+    yy, xx = np.meshgrid(np.arange(size) + 0.5, np.arange(size) + 0.5, indexing="ij")
+    p = np.stack([xx * cells / size, yy * cells / size, np.zeros_like(xx)], axis=-1)
+    out = np.empty((size, size, channels), np.float32)
+    for c in range(channels):
+        n = 0.6 * value_noise3(p, seed + c) + 0.4 * value_noise3(p * 4.0, seed + 10 + c)
+        out[..., c] = lo + (hi - lo) * np.clip(n, 0.0, 1.0)
+    return out
+
+
+def config_c4(width: int = 512, height: int = 512, spp: int = 16, rings: int = 316, tex: int = 512,
+              seed: int = 4) -> SceneDesc:
+    """Differentiable workload: 512x512, 16 spp, depth 6; fBm-displaced sphere (CreateSphere topology
+    316x316 = 199,712 triangles) with a 512x512 float RGB albedo texture (value noise in [0.1, 0.9])
+    and a 512x512 roughness texture (value noise in [0.05, 1]), metallic 0; 512x256 HDR env with a
+    sun lobe; no fog; seed 4.  Texture 1 is the albedo, texture 2 the roughness."""
+    pos, uv = uv_sphere(rings, rings, amplitude=0.1, seed=seed)
+    d = SceneDesc(f"c4_adjoint_{width}x{height}_{spp}spp")
+    d.meshes = [MeshDesc(pos, uv)]
+    rough = value_noise_float(tex, seed + 50, 0.05, 1.0, channels=1)
+    d.textures = [TextureDesc(_rgbe_texels(sky_env(512, 256, seed=seed, sun_peak=100.0, sun_sigma_deg=3.0,
+                                                   lognormal_sigma=0.5))),
+                  TextureDesc(value_noise_float(tex, seed, 0.1, 0.9)),
+                  TextureDesc(np.repeat(rough, 3, axis=2))]
+    d.sky = ("texture", 0, 1.0, 0.0)
+    d.objects = [ObjectDesc("sphere", Transform(), {"albedo": (1.0, 1.0, 1.0), "roughness": 1.0, "metallic": 0.0,
+                                                    "color_texture": 1, "roughness_texture": 2}, ("mesh", 0))]
+    cam = (0.0, 0.4, -2.9)
+    d.view = View(Transform(cam, look_rotation(cam, (0.0, 0.0, 0.0))), math.radians(50.0), 0.1)
+    d.width, d.height, d.spp, d.bounces = width, height, spp, 6
+    d.min_samples = spp
+    d.variance_threshold = 0.0
+    return d
+
+
 def config_features(width: int = 48, height: int = 40, spp: int = 8, seed: int = 5) -> SceneDesc:
     """Small scene touching every shading branch: textured/normal-mapped/point-filtered materials,
     transparent (refractive) sphere, metal box, emissive object, instanced transformed mesh, fog."""

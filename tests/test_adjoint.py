@@ -1,5 +1,6 @@
 """Path-replay adjoint (sr_adjoint_albedo) against central finite differences of the renderer's own
-image loss, and sr_scene_update_texture against a scene built from scratch.
+image loss, sr_scene_update_texture(_device) against a scene built from scratch, and the PyTorch
+autograd wrapper (an inverse-rendering run that recovers a texture).
 
 The loss is L = sum over pixels and channels of (radiance + radiance_fog - target)^2.  At fixed
 random numbers the renderer's estimator is a smooth function of the albedo texels of a
@@ -17,6 +18,9 @@ import pytest
 from sharpray_gb300 import (Context, Fog, Quat, SharpRayError, Transform, View, _abi, adjoint_albedo, render_params,
                             synth)
 from sharpray_gb300.synth import MeshDesc, ObjectDesc, SceneDesc, TextureDesc, look_rotation
+
+torch_lib = pytest.importorskip("torch")
+from sharpray_gb300.autograd import current_stream_handle  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -89,9 +93,9 @@ class Rig:
         t = self.tex[tex_index]
         grad = torch.zeros(t.height * t.width * 3, dtype=torch.float32, device="cuda")
         replay = torch.zeros(self.d.width * self.d.height * 3, dtype=torch.float32, device="cuda")
-        tgt = torch.from_numpy(target).cuda()
-        adjoint_albedo(self.scene, self.d.view, self.params, self.aovs, tgt.data_ptr(), t, grad.data_ptr(),
-                       replay.data_ptr())
+        d_image = 2.0 * (self.bufs["radiance"] + self.bufs["radiance_fog"] - torch.from_numpy(target).cuda())
+        adjoint_albedo(self.scene, self.d.view, self.params, self.aovs, d_image.data_ptr(), t, grad.data_ptr(),
+                       replay.data_ptr(), current_stream_handle())
         torch.cuda.synchronize()
         fwd = (self.bufs["radiance"] + self.bufs["radiance_fog"]).cpu().numpy()
         return grad.cpu().numpy().reshape(t.height, t.width, 3), replay.cpu().numpy(), fwd
@@ -162,6 +166,11 @@ def test_update_texture_equals_fresh_build(torch_mod):
     d2.textures[1] = TextureDesc(new, 0, (1.0, 1.0))
     fresh = Rig(torch_mod, d2)
     assert np.array_equal(got.view(np.uint32), fresh.image().view(np.uint32))
+    # the device-pointer update, on torch's stream
+    rig.scene.update_texture(rig.tex[1], d.textures[1].texels)
+    dev = torch_mod.from_numpy(new).cuda()
+    rig.scene.update_texture_device(rig.tex[1], dev.data_ptr(), current_stream_handle())
+    assert np.array_equal(rig.image().view(np.uint32), got.view(np.uint32))
 
 
 def test_adjoint_rejects(torch_mod):
@@ -182,3 +191,45 @@ def test_adjoint_rejects(torch_mod):
     with pytest.raises(SharpRayError):
         adjoint_albedo(gs, glass.view, render_params(*glass.render_args()), rig.aovs, tgt.data_ptr(), 1,
                        g.data_ptr())
+
+
+def test_autograd_matches_adjoint_and_recovers_texture(torch_mod):
+    """render_albedo's backward is the adjoint; Adam on the texels from a perturbed start brings the
+    image loss and the texture error down."""
+    torch = torch_mod
+    from sharpray_gb300.autograd import render_albedo
+    d = adjoint_scene(False, 3, 10.0, w=48, h=36, spp=4)
+    rig = Rig(torch, d)
+    tex = rig.tex[1]
+    truth = torch.from_numpy(d.textures[1].texels).cuda()
+    target = render_albedo(rig.scene, d.view, rig.params, tex, truth).detach().clone()
+    start = (truth + 0.15 * torch.from_numpy(np.random.default_rng(5).standard_normal(truth.shape)
+                                            .astype(np.float32)).cuda()).clamp(0.05, 1.0)
+    x = start.clone().requires_grad_(True)
+    loss = ((render_albedo(rig.scene, d.view, rig.params, tex, x) - target) ** 2).sum()
+    loss.backward()
+    # the same gradient straight from the adjoint entry point
+    rig.scene.update_texture(tex, start.cpu().numpy())
+    img = torch.from_numpy(rig.image()).cuda()
+    g = torch.zeros_like(x)
+    d_image = 2.0 * (img - target.reshape(-1))
+    adjoint_albedo(rig.scene, d.view, rig.params, rig.aovs, d_image.data_ptr(), tex, g.data_ptr(), None,
+                   current_stream_handle())
+    torch.cuda.synchronize()
+    assert torch.allclose(x.grad, g, rtol=1e-5, atol=1e-6 * float(g.abs().max()))
+    opt = torch.optim.Adam([x], lr=0.02)
+    first = None
+    for _ in range(60):
+        opt.zero_grad()
+        loss = ((render_albedo(rig.scene, d.view, rig.params, tex, x) - target) ** 2).sum()
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            x.clamp_(0.0, 1.5)
+        first = first if first is not None else float(loss)
+    final = float(((render_albedo(rig.scene, d.view, rig.params, tex, x.detach()) - target) ** 2).sum())
+    assert final < 0.1 * first, (first, final)
+    seen = g.abs().sum(dim=2) > 0  # texels that the image depends on
+    err0 = float(((start - truth)[seen] ** 2).mean()) ** 0.5
+    err1 = float(((x.detach() - truth)[seen] ** 2).mean()) ** 0.5
+    assert err1 < 0.6 * err0, (err0, err1)

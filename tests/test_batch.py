@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from sharpray_gb300 import Context, SharpRayError, _abi, render_batch, render_params, synth
+from sharpray_gb300.autograd import current_stream_handle
 
 pytestmark = pytest.mark.gpu
 
@@ -54,7 +55,7 @@ def render_single(torch, ctx, d, s):
 
 def test_batch_matches_single_renders(batch_scenes):
     torch, ctx, descs, scenes = batch_scenes
-    stream = torch.cuda.current_stream().cuda_stream
+    stream = current_stream_handle()
     singles = []
     for d, s in zip(descs, scenes):
         bufs, a = device_aovs(torch, d.width * d.height)
@@ -78,7 +79,7 @@ def test_batch_matches_single_renders(batch_scenes):
 def test_batch_subset_and_order(batch_scenes):
     """A different batch (other scenes, other order) rebuilds the graph and still matches."""
     torch, ctx, descs, scenes = batch_scenes
-    stream = torch.cuda.current_stream().cuda_stream
+    stream = current_stream_handle()
     order = [3, 0]
     outs = [device_aovs(torch, descs[i].width * descs[i].height) for i in order]
     render_batch([scenes[i] for i in order], [descs[i].view for i in order],

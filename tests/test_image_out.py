@@ -104,7 +104,8 @@ def test_aov_image_device_entry(gpu_ctx, oracle_mod):
     p = _abi.SrAovImageParams(0.075, 4, 64)
     for kind in AovKind:
         out = torch.zeros((a.height, a.width, 3), dtype=torch.uint8, device="cuda")
-        stream = torch.cuda.current_stream().cuda_stream
+        from sharpray_gb300.autograd import current_stream_handle
+        stream = current_stream_handle()
         _abi.check(gpu_ctx._lib.sr_aov_image_device(gpu_ctx.handle, C.byref(da), a.width, a.height, int(kind),
                                                     C.byref(p), out.data_ptr(), C.c_void_p(stream)))
         assert np.array_equal(out.cpu().numpy(), oracle_mod.aov_image(a, int(kind), p)), kind
