@@ -60,6 +60,8 @@ def parse():
                     help="scenes of the batched workload timed batched vs one after another (0: skip)")
     ap.add_argument("--adjoint-checks", type=int, default=64,
                     help="adjoint workload: texel channels checked by finite differences (-1: skip the workload)")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="run only the adjoint workload (--steps timed passes, --adjoint-checks FD checks)")
     ap.add_argument("--profile-once", action="store_true",
                     help="set up, render + compose exactly once, exit (for ncu captures)")
     return ap.parse_args()
@@ -606,6 +608,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.adjoint_only:
+        print(json.dumps({"adjoint": measure_adjoint(max(args.adjoint_checks, 0), reps=max(args.steps, 1))}),
+              flush=True)
     else:
         run_ours(args)
 

@@ -68,13 +68,14 @@ __device__ Col opaque_eval_dalbedo(const Surface& s, V3 view, V3 light) {
 }
 
 // Scene.SampleSkyDirect (sample_sky_direct in sr_path.cuh) returning also d/d albedo.
+template <bool GENERAL>
 __device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos, V3 view, Rng& rng, Ctr& c,
                                      uint32_t* err, Col& dnee) {
     dnee = black();
     V3 ldir;
     float lpdf;
     Col tr;
-    if (!sample_sky_light<false>(S, pos, rng, ldir, lpdf, tr, c, err)) return black();
+    if (!sample_sky_light<false, GENERAL>(S, pos, rng, ldir, lpdf, tr, c, err)) return black();
     V3 n = dot(s.normal, view) >= 0.0f ? s.normal : -s.normal;
     if (dot(n, ldir) <= 0.0f) return black();
     V3 ng = dot(s.normal_geo, view) >= 0.0f ? s.normal_geo : -s.normal_geo;
@@ -82,7 +83,7 @@ __device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos
     Col refl = opaque_eval(s, view, ldir);
     float spdf = opaque_pdf(s, view, ldir, specular_probability(s, view));
     float mis = power_heuristic(lpdf, spdf);
-    Col sky = sky_radiance<false>(S, ldir, c);
+    Col sky = sky_radiance<false, GENERAL>(S, ldir, c);
     dnee = sky * tr * opaque_eval_dalbedo(s, view, ldir) * mis / lpdf;
     return sky * tr * refl * mis / lpdf;
 }
@@ -109,6 +110,7 @@ __device__ Col clamp_adjoint(Col x, float max, Col a) {
 }
 
 // sample_path (sr_render.cu) recording the vertices; rad / fog as the forward pass sums them.
+template <bool GENERAL>
 __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t bounces, float indirect_clamp,
                              AdjVertex* v, Col& radiance, Col& radiance_fog, Ctr& c, uint32_t* err) {
     radiance = black();
@@ -120,7 +122,7 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
     int n = 0;
     for (uint32_t i = 0; i != bounces + 1; ++i) {
         SurfHit hit;
-        bool has_hit = trace_surface<false>(S, ray, hit, c, err);
+        bool has_hit = trace_surface<false, GENERAL>(S, ray, hit, c, err);
         float sdist;
         AdjVertex& x = v[n++];
         x.e_in = energy;
@@ -132,7 +134,7 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.kind = AV_FOG;
             energy = energy * col3(S.fog_color);
             x.e_rr = energy;
-            x.add = sample_sky_direct_fog<false>(S, ray_at(ray, sdist), ray.d, rng, c, err);
+            x.add = sample_sky_direct_fog<false, GENERAL>(S, ray_at(ray, sdist), ray.d, rng, c, err);
             Col srad = x.add * energy;
             if (i == 0)
                 radiance_fog = radiance_fog + srad;
@@ -158,7 +160,7 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.material = hit.material;
             radiance = radiance + s.radiance * energy;
             Col dnee;
-            Col nee = sample_sky_direct_adj(S, s, pos, view, rng, c, err, dnee);
+            Col nee = sample_sky_direct_adj<GENERAL>(S, s, pos, view, rng, c, err, dnee);
             radiance = radiance + nee * energy;
             x.add = s.radiance + nee;
             x.dadd = dnee;
@@ -168,7 +170,7 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
                 break;
             }
             x.e_rr = energy;
-            Scatter sc = surface_scatter(s, ray.d, view, rng);
+            Scatter sc = surface_scatter<GENERAL>(s, ray.d, view, rng);
             x.s = sc.weight;
             x.ds = opaque_eval_dalbedo(s, view, sc.dir) / fmaxf(sc.pdf, 1e-6f);
             energy = energy * sc.weight;
@@ -179,8 +181,8 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
         } else {
             x.kind = AV_SKY;
-            float mis = has_spdf ? power_heuristic(spdf, sky_light_pdf(S, ray.d)) : 1.0f;
-            x.add = sky_radiance<false>(S, ray.d, c) * mis;
+            float mis = has_spdf ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
+            x.add = sky_radiance<false, GENERAL>(S, ray.d, c) * mis;
             radiance = radiance + x.add * energy;
             break;
         }
@@ -220,6 +222,7 @@ __device__ void scatter_albedo_grad(const DevScene& S, int material, V2 uv, Col 
     add(x1, y1, tx * ty);
 }
 
+template <bool GENERAL>
 __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, DevParams P, DevAovs fwd,
                                                        const float* d_image, int tex, float* grad, float* replay,
                                                        uint32_t* err) {
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, De
     for (uint32_t si = 0; si < taken; ++si) {
         Ray ray = camera_ray(V, P, x, y, rng);
         Col rad, fog;
-        const int n = replay_sample(S, ray, rng, P.bounces, P.indirect_clamp, v, rad, fog, c, err);
+        const int n = replay_sample<GENERAL>(S, ray, rng, P.bounces, P.indirect_clamp, v, rad, fog, c, err);
         rad_sum = rad_sum + rad;
         fog_sum = fog_sum + fog;
         // reverse sweep: a = d loss / d (throughput leaving the vertex)
@@ -275,7 +278,12 @@ cudaError_t launch_adjoint_albedo(const DevScene& S, const DevView& V, const Dev
                                   const float* d_image, int texture, float* grad, float* replay, uint32_t* err,
                                   cudaStream_t stream) {
     dim3 grid((P.width + 7) / 8, (P.height + 7) / 8);
-    k_adjoint_albedo<<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err);
+    // scenes of meshes under a texture sky without transparency or normal maps take the lean
+    // instantiation, as the wavefront kernels do (same results, far less code)
+    if (S.general)
+        k_adjoint_albedo<true><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err);
+    else
+        k_adjoint_albedo<false><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err);
     return cudaGetLastError();
 }
 

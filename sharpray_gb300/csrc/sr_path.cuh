@@ -101,12 +101,12 @@ __device__ Col shadow_transmittance(const DevScene& S, Ray ray, Ctr& c, uint32_t
 }
 
 // Scene.SampleSkyLight scene.cs:758-772.
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 __device__ bool sample_sky_light(const DevScene& S, V3 pos, Rng& rng, V3& ldir, float& lpdf, Col& tr, Ctr& c,
                                  uint32_t* err) {
-    if (!sky_light_rand<COUNT>(S, rng, ldir, lpdf, c) || lpdf <= 0.0f) return false;
+    if (!sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, c) || lpdf <= 0.0f) return false;
     Ray shadow = make_ray(pos, ldir);
-    tr = shadow_transmittance<COUNT>(S, shadow, c, err);
+    tr = shadow_transmittance<COUNT, GENERAL>(S, shadow, c, err);
     if (max_component(tr) <= 0.0f) return false;
     if (S.has_fog) tr = tr * fog_transmittance_inf(S, shadow);
     return true;
@@ -130,15 +130,15 @@ __device__ Col sample_sky_direct(const DevScene& S, const Surface& s, V3 pos, V3
 }
 
 // Scene.SampleSkyDirectFog scene.cs:796-810.
-template <bool COUNT>
+template <bool COUNT, bool GENERAL = true>
 __device__ Col sample_sky_direct_fog(const DevScene& S, V3 pos, V3 rdir, Rng& rng, Ctr& c, uint32_t* err) {
     V3 ldir;
     float lpdf;
     Col tr;
-    if (!sample_sky_light<COUNT>(S, pos, rng, ldir, lpdf, tr, c, err)) return black();
+    if (!sample_sky_light<COUNT, GENERAL>(S, pos, rng, ldir, lpdf, tr, c, err)) return black();
     float fog_pdf = hg_pdf(dot(rdir, ldir), S.fog_g);
     float mis = power_heuristic(lpdf, fog_pdf);
-    return sky_radiance<COUNT>(S, ldir, c) * tr * fog_pdf * mis / lpdf;
+    return sky_radiance<COUNT, GENERAL>(S, ldir, c) * tr * fog_pdf * mis / lpdf;
 }
 
 // Scene.RussianRoulette scene.cs:744-756.
