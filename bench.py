@@ -60,6 +60,8 @@ def parse():
                     help="scenes of the batched workload timed batched vs one after another (0: skip)")
     ap.add_argument("--adjoint-checks", type=int, default=64,
                     help="adjoint workload: texel channels checked by finite differences (-1: skip the workload)")
+    ap.add_argument("--inverse-steps", type=int, default=200,
+                    help="Adam steps of the inverse-rendering run (0: skip)")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the adjoint workload (--steps timed passes, --adjoint-checks FD checks)")
     ap.add_argument("--profile-once", action="store_true",
@@ -344,6 +346,64 @@ def measure_adjoint(checks: int, reps: int = 5) -> dict:
                     "(path replay); FD: central, h = 1e-3, common random numbers"}
 
 
+def measure_inverse(steps: int, views: int = 4, size: int = 256, spp: int = 8) -> dict:
+    """Inverse rendering on the differentiable workload's scene (synth.config_c4 geometry, 512x512
+    albedo texture): `views` orbit cameras (size x size, spp, depth 6) render targets with the true
+    texture; starting from flat grey, `steps` Adam steps (lr 0.02, texels clamped to [0, 1]) through
+    sharpray_gb300.autograd.render_albedo minimise the summed L2 image loss.  Reports the time per
+    step (all views' forward renders and adjoints) and the texture RMSE on the texels the views see."""
+    import torch
+    from sharpray_gb300 import Context, Transform, View, render_params, synth
+    from sharpray_gb300.autograd import render_albedo
+    d = synth.config_c4(size, size, spp)
+    ctx = Context(0)
+    sc = d.instantiate(ctx)
+    sc.build()
+    tex = sc._keepalive[0][1]
+    p = render_params(*d.render_args())
+    cams = []
+    for k in range(views):
+        ang = 2.0 * math.pi * k / views
+        pos = (2.9 * math.sin(ang), 0.4, -2.9 * math.cos(ang))
+        cams.append(View(Transform(pos, synth.look_rotation(pos, (0.0, 0.0, 0.0))), d.view.fov, d.view.near))
+    truth = torch.from_numpy(d.textures[1].texels).cuda()
+    with torch.no_grad():
+        targets = [render_albedo(sc, v, p, tex, truth).clone() for v in cams]
+    x = torch.full_like(truth, 0.5).requires_grad_(True)
+    opt = torch.optim.Adam([x], lr=0.02)
+
+    def step():
+        opt.zero_grad()
+        loss = sum(((render_albedo(sc, v, p, tex, x) - t) ** 2).sum() for v, t in zip(cams, targets))
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            x.clamp_(0.0, 1.0)
+        return loss
+
+    loss0 = float(step().detach())
+    seen = x.grad.abs().sum(dim=2) > 0
+    rmse = lambda: float(((x.detach() - truth)[seen] ** 2).mean()) ** 0.5
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps - 1):
+        loss = step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    with torch.no_grad():
+        final = float(sum(((render_albedo(sc, v, p, tex, x) - t) ** 2).sum() for v, t in zip(cams, targets)))
+    rmse_start = float(((torch.full_like(truth, 0.5) - truth)[seen] ** 2).mean()) ** 0.5
+    per_step = dt / max(steps - 1, 1)
+    return {"workload": f"{views} orbit views {size}x{size}, {spp} spp, depth 6, {d.triangle_count} triangles, "
+                        "512x512 albedo texture from flat grey",
+            "steps": steps, "ms_per_step": 1000 * per_step, "texel_grads_per_s": truth.numel() / per_step,
+            "path_samples_per_s": 2 * views * size * size * spp / per_step,
+            "loss_start": loss0, "loss_final": final, "texture_rmse_start": rmse_start, "texture_rmse_final": rmse(),
+            "seen_texels": int(seen.sum()),
+            "note": "per step: every view rendered (forward) and replayed (adjoint) through the torch.autograd "
+                    "wrapper; targets share the renderer's per-pixel random numbers"}
+
+
 def run_reference(args):
     rank, _, world = dist_info()
     if rank != 0:
@@ -516,6 +576,8 @@ def run_ours(args):
     adjoint = None
     if args.adjoint_checks >= 0 and rank == 0:
         adjoint = measure_adjoint(args.adjoint_checks)
+        if args.inverse_steps > 0:
+            adjoint["inverse_rendering"] = measure_inverse(args.inverse_steps)
 
     # end to end through the public API with pinned host outputs
     host = Aovs(W, H)
@@ -609,8 +671,10 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     elif args.adjoint_only:
-        print(json.dumps({"adjoint": measure_adjoint(max(args.adjoint_checks, 0), reps=max(args.steps, 1))}),
-              flush=True)
+        adj = measure_adjoint(max(args.adjoint_checks, 0), reps=max(args.steps, 1))
+        if args.inverse_steps > 0:
+            adj["inverse_rendering"] = measure_inverse(args.inverse_steps)
+        print(json.dumps({"adjoint": adj}), flush=True)
     else:
         run_ours(args)
 
