@@ -248,8 +248,9 @@ def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
 
 def measure_adjoint(checks: int, reps: int = 5) -> dict:
     """The differentiable workload (synth.config_c4): forward render, then the path-replay adjoint of
-    L = sum (I - T)^2 for the albedo texture, T rendered from the textures perturbed by N(0, 0.05).
-    grads/s = texel-channel gradients produced per second (the texture's h x w x 3 per adjoint pass).
+    L = sum (I - T)^2 for the albedo texture (and, timed only, for the roughness texture), T rendered
+    from the textures perturbed by N(0, 0.05).  grads/s = texel-channel gradients produced per second
+    (the albedo texture's h x w x 3 per adjoint pass; h x w for the roughness).
     `checks` random (texel, channel) pairs that the image depends on are compared with central
     differences of L (h = 1e-3 and 2e-3, common random numbers through sr_scene_update_texture_device);
     a pair whose two differences disagree by > 2 % saw a roulette decision flip and is not scored."""
@@ -257,7 +258,7 @@ def measure_adjoint(checks: int, reps: int = 5) -> dict:
 
     import torch
     import numpy as np
-    from sharpray_gb300 import Context, _abi, adjoint_albedo, render_params, synth
+    from sharpray_gb300 import Context, _abi, adjoint_albedo, adjoint_texture, render_params, synth
     from sharpray_gb300.autograd import device_aovs
     d = synth.config_c4()
     ctx = Context(0)
@@ -307,6 +308,19 @@ def measure_adjoint(checks: int, reps: int = 5) -> dict:
                 fwd_ms.append(ev[0].elapsed_time(ev[1]))
                 adj_ms.append(e2.elapsed_time(ev[2]))
         loss0 = float(((image().double() - target.double()) ** 2).sum())
+        # the roughness texture's gradient (same replay, GGX / Smith derivatives; channel 0)
+        grad_r = torch.zeros_like(base_r)
+        rough_ms = []
+        for i in range(reps + 1):
+            grad_r.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            adjoint_texture(sc, d.view, p, aovs, d_img.data_ptr(), tex_r, grad_r.data_ptr(), _abi.SR_ADJOINT_ROUGHNESS,
+                            None, st.cuda_stream)
+            e1.record(st)
+            st.synchronize()
+            if i:
+                rough_ms.append(e0.elapsed_time(e1))
 
         def loss_at(y, x, c, delta):
             t = base_a.clone()
@@ -337,6 +351,8 @@ def measure_adjoint(checks: int, reps: int = 5) -> dict:
                         "L2 loss vs textures + N(0, 0.05)",
             "grads_per_s": n_grad / adj_s, "unit": "texel-channel gradients/s",
             "adjoint_ms": 1000 * adj_s, "forward_ms": 1000 * fwd_s,
+            "roughness_adjoint_ms": statistics.median(rough_ms),
+            "roughness_grads_per_s": (n_grad // 3) / (statistics.median(rough_ms) / 1000.0),
             "replayed_samples_per_s": samples / adj_s, "forward_samples_per_s": samples / fwd_s,
             "loss": loss0, "fd_checked": len(rel), "fd_skipped_roulette_flip": skipped,
             "fd_rel_err_median": float(np.median(rel_a)) if len(rel_a) else None,

@@ -363,6 +363,14 @@ SR_API int sr_scene_autotune(SrScene* scene, const SrView* view, const SrRenderP
 SR_API int sr_adjoint_albedo(SrScene* scene, const SrView* view, const SrRenderParams* params,
                              const SrAovs* forward, const float* d_image, int32_t texture, float* grad,
                              float* replay, void* stream);
+/* The same for either parameter a texture can set: SR_ADJOINT_ALBEDO (the colour lookup; the
+ * gradient fills all three channels) or SR_ADJOINT_ROUGHNESS (the roughness lookup, which reads the
+ * red channel; the gradient fills channel 0).  For the roughness the sampled specular directions
+ * move with the parameter, so the detached gradient is exact in expectation, not per sample. */
+enum { SR_ADJOINT_ALBEDO = 0, SR_ADJOINT_ROUGHNESS = 1 };
+SR_API int sr_adjoint_texture(SrScene* scene, const SrView* view, const SrRenderParams* params,
+                              const SrAovs* forward, const float* d_image, int32_t texture, int32_t parameter,
+                              float* grad, float* replay, void* stream);
 /* Replaces the texels of texture `texture` (rgb floats, its width x height) in a built scene's
  * device copy, e.g. one step of inverse rendering.  The context's texture and other scenes are left
  * as they are.  The scene's sky texture is refused (its light distribution is built from it). */

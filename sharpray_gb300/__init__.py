@@ -6,7 +6,7 @@ Compositor classes (see :mod:`sharpray_gb300.api`).
 """
 from .api import (AABox, AovKind, Aovs, Compositor, Context, Fog, Font, Material, Mesh, Object, Overlay, Quat,
                   Renderer, Scene, SharpRayError, SkyProcedural, SkyTexture, Sphere, StateError, Texture,
-                  TextureFilter, Tonemapper, Transform, View, adjoint_albedo, aov_image, load_image, mesh_triangles,
+                  TextureFilter, Tonemapper, Transform, View, adjoint_albedo, adjoint_texture, aov_image, load_image, mesh_triangles,
                   render_batch, render_compose, render_params, save_image)
 
 __version__ = "0.1.0"

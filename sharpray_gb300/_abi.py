@@ -26,6 +26,7 @@ SR_SHAPE_AABOX = 2
 
 SR_AOV_NORMAL, SR_AOV_DEPTH, SR_AOV_VARIANCE, SR_AOV_SAMPLES, SR_AOV_UV = 0, 1, 2, 3, 4
 SR_ALIGN_TOP_LEFT, SR_ALIGN_CENTER = 0, 1
+SR_ADJOINT_ALBEDO, SR_ADJOINT_ROUGHNESS = 0, 1
 SR_TEXTURE_SRGB = 0
 SR_TEXTURE_LINEAR = 1
 SR_TEXTURE_HDR = 2
@@ -190,6 +191,8 @@ PROTOTYPES = {
     "sr_image_save": (_I, [C.c_char_p, _U, _U, _P]),
     "sr_adjoint_albedo": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P, C.c_int32,
                                _P, _P, _P]),
+    "sr_adjoint_texture": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P, C.c_int32,
+                                C.c_int32, _P, _P, _P]),
     "sr_scene_update_texture": (_I, [_P, C.c_int32, _P]),
     "sr_scene_update_texture_device": (_I, [_P, C.c_int32, _P, _P]),
 }

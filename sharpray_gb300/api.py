@@ -815,12 +815,25 @@ def render_batch(scenes: Sequence["Scene"], views: Sequence["View"], params: Seq
     check(lib.sr_render_batch(arr_s, arr_v, arr_p, arr_a, n, C.c_void_p(stream) if stream else None))
 
 
+def adjoint_texture(scene: "Scene", view: "View", params: SrRenderParams, forward: SrAovs, d_image: int,
+                    texture, grad: int, parameter: int = _abi.SR_ADJOINT_ALBEDO, replay: Optional[int] = None,
+                    stream: Optional[int] = None) -> None:
+    """sr_adjoint_texture: adds dL/d(texels of `texture`) into `grad`, given d_image = dL/dI for the
+    image I = radiance + radiance_fog of `forward` (device AOV planes of sr_render_device with the
+    same scene, view and params), for the texture as the albedo (SR_ADJOINT_ALBEDO) or the roughness
+    (SR_ADJOINT_ROUGHNESS: channel 0 of grad) lookup.  d_image / grad / replay are device pointers
+    (float32, H x W x 3 and the texture's h x w x 3); asynchronous on `stream`."""
+    tid = texture.id if isinstance(texture, Texture) else int(texture)
+    v = view.to_c()
+    check(scene._lib.sr_adjoint_texture(scene.handle, C.byref(v), C.byref(params), C.byref(forward),
+                                        C.c_void_p(d_image), tid, int(parameter), C.c_void_p(grad),
+                                        C.c_void_p(replay) if replay else None,
+                                        C.c_void_p(stream) if stream else None))
+
+
 def adjoint_albedo(scene: "Scene", view: "View", params: SrRenderParams, forward: SrAovs, d_image: int,
                    texture, grad: int, replay: Optional[int] = None, stream: Optional[int] = None) -> None:
-    """sr_adjoint_albedo: adds dL/d(texels of `texture`) into `grad`, given d_image = dL/dI for the
-    image I = radiance + radiance_fog of `forward` (device AOV planes of sr_render_device with the
-    same scene, view and params).  d_image / grad / replay are device pointers (float32, H x W x 3
-    and the texture's h x w x 3); asynchronous on `stream`."""
+    """sr_adjoint_albedo: adjoint_texture for the albedo lookup."""
     tid = texture.id if isinstance(texture, Texture) else int(texture)
     v = view.to_c()
     check(scene._lib.sr_adjoint_albedo(scene.handle, C.byref(v), C.byref(params), C.byref(forward),

@@ -1,6 +1,6 @@
 // sr_adjoint.cu — path-replay adjoint of a rendered image with respect to the texels of an albedo
-// (colour) texture: given dL/dI for the image I = radiance + radiance_fog of a render, the gradient
-// dL/d(texels).  No counterpart in the reference (it has no derivatives).
+// (colour) or roughness texture: given dL/dI for the image I = radiance + radiance_fog of a render,
+// the gradient dL/d(texels).  No counterpart in the reference (it has no derivatives).
 //
 // One thread per pixel replays the pixel's samples exactly as the per-pixel path loop renders
 // them (the same RNG stream and the same functions, so the same paths and the same radiance --
@@ -8,16 +8,18 @@
 // throughput, what the vertex adds to the radiance and the scatter weight.  A reverse sweep over
 // the vertices then carries the adjoint of the throughput back to the camera: through the scatter
 // weights, the luminance clamp of the indirect throughput and the Russian-roulette division (both
-// differentiated as functions of the throughput), and into the albedo of each surface vertex,
+// differentiated as functions of the throughput), and into the parameter of each surface vertex,
 // whose texture lookup passes it on to the four bilinear texels (atomic adds).
 //
 // Differentiated: the BRDF values of the light samples and the scatter weights with respect to
-// the albedo (diffuse term and, for metallic surfaces, the Fresnel base).  Held fixed ("detached"),
-// as path replay does: the sampled directions, lobe choices, Russian-roulette decisions and the
-// pdfs and MIS weights (which depend on the albedo only through the Fresnel base of metallic
-// surfaces).  For non-metallic surfaces the gradient is therefore the exact derivative of the
-// renderer's own estimator at fixed random numbers wherever no roulette decision or clamp
-// threshold is crossed.  Scenes with transparent materials are refused by the host entry point.
+// the parameter (albedo: the diffuse term and, for metallic surfaces, the Fresnel base;
+// roughness: the GGX distribution and Smith terms).  Held fixed ("detached"), as path replay does:
+// the sampled directions, lobe choices, Russian-roulette decisions and the pdfs and MIS weights.
+// For the albedo of non-metallic surfaces none of these depends on the parameter, so the gradient
+// is the exact derivative of the renderer's own estimator at fixed random numbers wherever no
+// roulette decision or clamp threshold is crossed.  The roughness moves the sampled specular
+// directions, so there the gradient is exact in expectation (d/dθ of the expected image) rather
+// than per sample.  Scenes with transparent materials are refused by the host entry point.
 #include <cuda_runtime.h>
 
 #include "sr_kernels.h"
@@ -33,9 +35,9 @@ struct AdjVertex {
     Col e_in;   // throughput entering the vertex
     Col e_rr;   // throughput after the Russian roulette (surface), or after the fog colour (fog)
     Col add;    // radiance added per unit throughput (emission + light sample; fog light sample; sky)
-    Col dadd;   // d add / d albedo, per channel
+    Col dadd;   // d add / d parameter (albedo: per channel; roughness: the rgb of d add / d roughness)
     Col s;      // scatter weight (surface)
-    Col ds;     // d s / d albedo, per channel
+    Col ds;     // d s / d parameter, likewise
     Col pre;    // e_rr * s before the luminance clamp
     float rr;   // survival probability divided by (1: none)
     float clamp_max;
@@ -67,8 +69,44 @@ __device__ Col opaque_eval_dalbedo(const Surface& s, V3 view, V3 light) {
     return (gray(dspec) + ddiff) * (1.0f - s.transparency);
 }
 
-// Scene.SampleSkyDirect (sample_sky_direct in sr_path.cuh) returning also d/d albedo.
-template <bool GENERAL>
+// d opaque_eval / d roughness, pdfs held fixed: only the specular term depends on it, through
+// rs = max(roughness^2, 1e-4) in the GGX distribution D = a2 / (pi d^2) (a2 = rs^2,
+// d = 1 - (n.h)^2 + (n.h)^2 a2) and in both Smith terms G1(x) = x / (x (1 - k) + k), k = rs / 2.
+__device__ Col opaque_eval_droughness(const Surface& s, V3 view, V3 light) {
+    float ndl = dot(s.normal, light);
+    if (ndl <= 0.0f) return black();
+    float rs = s.roughness * s.roughness;
+    if (!(rs > 1e-4f)) return black();  // rs sits at its floor
+    float ndv = fmaxf(1e-4f, dot(s.normal, view));
+    Col base = base_reflectivity(s.f0, s.albedo, s.metallic);
+    V3 half = normalize_or(view + light, s.normal);
+    float ndh = dot(s.normal, half);
+    float hdv = dot(half, view);
+    Col f = fresnel(hdv, base);
+    float a2 = rs * rs, nh2 = ndh * ndh;
+    float dd = (1.0f - nh2) + nh2 * a2;
+    float d_ggx = a2 / (kPi * dd * dd);
+    float dd_ggx = (dd - 2.0f * a2 * nh2) / (kPi * dd * dd * dd) * (2.0f * rs);  // d D / d rs
+    float k = rs * 0.5f;
+    float qv = ndv * (1.0f - k) + k, ql = ndl * (1.0f - k) + k;
+    float gv = ndv / qv, gl = ndl / ql;
+    float dgv = -0.5f * ndv * (1.0f - ndv) / (qv * qv), dgl = -0.5f * ndl * (1.0f - ndl) / (ql * ql);
+    float dspec = (dd_ggx * gv * gl + d_ggx * (dgv * gl + gv * dgl)) / (4.0f * ndv) * (2.0f * s.roughness);
+    return f * (dspec * (1.0f - s.transparency));
+}
+
+enum : int { ADJ_ALBEDO = 0, ADJ_ROUGHNESS = 1 };
+
+template <int PARAM>
+__device__ __forceinline__ Col opaque_eval_dparam(const Surface& s, V3 view, V3 light) {
+    if constexpr (PARAM == ADJ_ALBEDO)
+        return opaque_eval_dalbedo(s, view, light);
+    else
+        return opaque_eval_droughness(s, view, light);
+}
+
+// Scene.SampleSkyDirect (sample_sky_direct in sr_path.cuh) returning also its derivative.
+template <bool GENERAL, int PARAM>
 __device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos, V3 view, Rng& rng, Ctr& c,
                                      uint32_t* err, Col& dnee) {
     dnee = black();
@@ -84,7 +122,7 @@ __device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos
     float spdf = opaque_pdf(s, view, ldir, specular_probability(s, view));
     float mis = power_heuristic(lpdf, spdf);
     Col sky = sky_radiance<false, GENERAL>(S, ldir, c);
-    dnee = sky * tr * opaque_eval_dalbedo(s, view, ldir) * mis / lpdf;
+    dnee = sky * tr * opaque_eval_dparam<PARAM>(s, view, ldir) * mis / lpdf;
     return sky * tr * refl * mis / lpdf;
 }
 
@@ -110,7 +148,7 @@ __device__ Col clamp_adjoint(Col x, float max, Col a) {
 }
 
 // sample_path (sr_render.cu) recording the vertices; rad / fog as the forward pass sums them.
-template <bool GENERAL>
+template <bool GENERAL, int PARAM>
 __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t bounces, float indirect_clamp,
                              AdjVertex* v, Col& radiance, Col& radiance_fog, Ctr& c, uint32_t* err) {
     radiance = black();
@@ -160,7 +198,7 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.material = hit.material;
             radiance = radiance + s.radiance * energy;
             Col dnee;
-            Col nee = sample_sky_direct_adj<GENERAL>(S, s, pos, view, rng, c, err, dnee);
+            Col nee = sample_sky_direct_adj<GENERAL, PARAM>(S, s, pos, view, rng, c, err, dnee);
             radiance = radiance + nee * energy;
             x.add = s.radiance + nee;
             x.dadd = dnee;
@@ -172,7 +210,7 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.e_rr = energy;
             Scatter sc = surface_scatter<GENERAL>(s, ray.d, view, rng);
             x.s = sc.weight;
-            x.ds = opaque_eval_dalbedo(s, view, sc.dir) / fmaxf(sc.pdf, 1e-6f);
+            x.ds = opaque_eval_dparam<PARAM>(s, view, sc.dir) / fmaxf(sc.pdf, 1e-6f);
             energy = energy * sc.weight;
             x.pre = energy;
             energy = clamp_luminance(energy, indirect_clamp);
@@ -190,13 +228,18 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
     return n;
 }
 
-// Passes d loss / d albedo at a surface vertex to the albedo texture's texels (the bilinear or
-// point lookup of Texture.Sample texture.cs:39-69, times the material's albedo).
-__device__ void scatter_albedo_grad(const DevScene& S, int material, V2 uv, Col g, int tex, float* grad) {
+// Passes the derivative at a surface vertex to the texels of the texture lookup that set the
+// parameter (the bilinear or point lookup of Texture.Sample texture.cs:39-69): for the albedo
+// g = dL/d(albedo) per channel, times the material's albedo; for the roughness (the lookup's red
+// channel times the material's roughness) the sum of g's components times the material's roughness,
+// into the red channel.
+template <int PARAM>
+__device__ void scatter_texel_grad(const DevScene& S, int material, V2 uv, Col g, int tex, float* grad) {
     const DevMaterial& m = S.materials[material];
-    if (m.tex[0] != tex) return;
+    if (m.tex[PARAM == ADJ_ALBEDO ? 0 : 1] != tex) return;
     const DevTexture& t = S.textures[tex];
-    Col ga = g * col3(m.albedo_rough);
+    const Col ga = PARAM == ADJ_ALBEDO ? g * col3(m.albedo_rough)
+                                       : Col{(g.r + g.g + g.b) * m.albedo_rough.w, 0.0f, 0.0f};
     float u = uv.x * t.tiling_x;
     u -= floorf(u);
     float vv = uv.y * t.tiling_y;
@@ -205,8 +248,10 @@ __device__ void scatter_albedo_grad(const DevScene& S, int material, V2 uv, Col 
     auto add = [&](uint32_t x, uint32_t y, float wt) {
         float* p = grad + 3 * ((size_t)y * w + x);
         atomicAdd(p, ga.r * wt);
-        atomicAdd(p + 1, ga.g * wt);
-        atomicAdd(p + 2, ga.b * wt);
+        if (PARAM == ADJ_ALBEDO) {
+            atomicAdd(p + 1, ga.g * wt);
+            atomicAdd(p + 2, ga.b * wt);
+        }
     };
     if (t.filter == 1) {
         add((uint32_t)(u * (float)w) % w, (uint32_t)(vv * (float)h) % h, 1.0f);
@@ -222,8 +267,8 @@ __device__ void scatter_albedo_grad(const DevScene& S, int material, V2 uv, Col 
     add(x1, y1, tx * ty);
 }
 
-template <bool GENERAL>
-__global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, DevParams P, DevAovs fwd,
+template <bool GENERAL, int PARAM>
+__global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, DevParams P, DevAovs fwd,
                                                        const float* d_image, int tex, float* grad, float* replay,
                                                        uint32_t* err) {
     const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7), y = blockIdx.y * 8 + (threadIdx.x >> 3);
@@ -240,7 +285,7 @@ __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, De
     for (uint32_t si = 0; si < taken; ++si) {
         Ray ray = camera_ray(V, P, x, y, rng);
         Col rad, fog;
-        const int n = replay_sample<GENERAL>(S, ray, rng, P.bounces, P.indirect_clamp, v, rad, fog, c, err);
+        const int n = replay_sample<GENERAL, PARAM>(S, ray, rng, P.bounces, P.indirect_clamp, v, rad, fog, c, err);
         rad_sum = rad_sum + rad;
         fog_sum = fog_sum + fog;
         // reverse sweep: a = d loss / d (throughput leaving the vertex)
@@ -256,12 +301,12 @@ __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, De
                 a_in = a_rr * col3(S.fog_color);
             } else if (q.kind == AV_SURF_END) {
                 a_in = G * q.add;
-                scatter_albedo_grad(S, q.material, q.uv, G * q.e_in * q.dadd, tex, grad);
+                scatter_texel_grad<PARAM>(S, q.material, q.uv, G * q.e_in * q.dadd, tex, grad);
             } else {
                 const Col a_pre = clamp_adjoint(q.pre, q.clamp_max, a);
                 const Col a_s = q.e_rr * a_pre;
                 a_in = rr_adjoint(q.e_in, q.rr, q.s * a_pre) + G * q.add;
-                scatter_albedo_grad(S, q.material, q.uv, a_s * q.ds + G * q.e_in * q.dadd, tex, grad);
+                scatter_texel_grad<PARAM>(S, q.material, q.uv, a_s * q.ds + G * q.e_in * q.dadd, tex, grad);
             }
             a = a_in;
         }
@@ -274,16 +319,26 @@ __global__ void __launch_bounds__(64) k_adjoint_albedo(DevScene S, DevView V, De
     }
 }
 
-cudaError_t launch_adjoint_albedo(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
-                                  const float* d_image, int texture, float* grad, float* replay, uint32_t* err,
-                                  cudaStream_t stream) {
+cudaError_t launch_adjoint_texture(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
+                                   const float* d_image, int texture, int parameter, float* grad, float* replay,
+                                   uint32_t* err, cudaStream_t stream) {
     dim3 grid((P.width + 7) / 8, (P.height + 7) / 8);
     // scenes of meshes under a texture sky without transparency or normal maps take the lean
     // instantiation, as the wavefront kernels do (same results, far less code)
-    if (S.general)
-        k_adjoint_albedo<true><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err);
-    else
-        k_adjoint_albedo<false><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err);
+#define SR_ADJ_LAUNCH(G, PR) \
+    k_adjoint_texture<G, PR><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err)
+    if (parameter == ADJ_ALBEDO) {
+        if (S.general)
+            SR_ADJ_LAUNCH(true, ADJ_ALBEDO);
+        else
+            SR_ADJ_LAUNCH(false, ADJ_ALBEDO);
+    } else {
+        if (S.general)
+            SR_ADJ_LAUNCH(true, ADJ_ROUGHNESS);
+        else
+            SR_ADJ_LAUNCH(false, ADJ_ROUGHNESS);
+    }
+#undef SR_ADJ_LAUNCH
     return cudaGetLastError();
 }
 

@@ -1711,25 +1711,34 @@ SR_API int sr_image_save(const char* path, uint32_t w, uint32_t h, const uint8_t
     return SR_OK;
 }
 
-SR_API int sr_adjoint_albedo(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
-                             const float* d_image, int32_t texture, float* grad, float* replay, void* stream) {
+SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
+                              const float* d_image, int32_t texture, int32_t parameter, float* grad, float* replay,
+                              void* stream) {
     if (!s || !fwd || !d_image || !grad) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     if (int rc = need_device(s)) return rc;
     if (!fwd->radiance || !fwd->radiance_fog || !fwd->samples)
-        return fail(SR_ERR_INVALID_ARG, "sr_adjoint_albedo needs the forward radiance, radiance_fog and samples planes");
+        return fail(SR_ERR_INVALID_ARG, "the adjoint needs the forward radiance, radiance_fog and samples planes");
     if (texture < 0 || (size_t)texture >= s->tex_offset.size())
         return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
-    if (s->dev.has_transparent) return fail(SR_ERR_STATE, "sr_adjoint_albedo does not support transparent materials");
+    if (parameter != SR_ADJOINT_ALBEDO && parameter != SR_ADJOINT_ROUGHNESS)
+        return fail(SR_ERR_INVALID_ARG, "unknown adjoint parameter %d", parameter);
+    if (s->dev.has_transparent) return fail(SR_ERR_STATE, "the adjoint does not support transparent materials");
     DevView dv;
     DevParams dp;
     if (int rc = make_view(view, params, dv, dp)) return rc;
-    if (dp.bounces > 16) return fail(SR_ERR_INVALID_ARG, "sr_adjoint_albedo supports at most 16 bounces");
+    if (dp.bounces > 16) return fail(SR_ERR_INVALID_ARG, "the adjoint supports at most 16 bounces");
     SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
     cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
     DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
-    SR_CUDA(launch_adjoint_albedo(s->dev, dv, dp, f, d_image, texture, grad, replay, s->err.as<uint32_t>(), st),
+    SR_CUDA(launch_adjoint_texture(s->dev, dv, dp, f, d_image, texture, parameter, grad, replay,
+                                   s->err.as<uint32_t>(), st),
             "adjoint launch");
     return SR_OK;
+}
+
+SR_API int sr_adjoint_albedo(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
+                             const float* d_image, int32_t texture, float* grad, float* replay, void* stream) {
+    return sr_adjoint_texture(s, view, params, fwd, d_image, texture, SR_ADJOINT_ALBEDO, grad, replay, stream);
 }
 
 static int updatable_texture(SrScene* s, int32_t texture) {

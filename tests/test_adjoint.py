@@ -15,8 +15,8 @@ import math
 import numpy as np
 import pytest
 
-from sharpray_gb300 import (Context, Fog, Quat, SharpRayError, Transform, View, _abi, adjoint_albedo, render_params,
-                            synth)
+from sharpray_gb300 import (Context, Fog, Quat, SharpRayError, Transform, View, _abi, adjoint_albedo, adjoint_texture,
+                            render_params, synth)
 from sharpray_gb300.synth import MeshDesc, ObjectDesc, SceneDesc, TextureDesc, look_rotation
 
 torch_lib = pytest.importorskip("torch")
@@ -239,3 +239,56 @@ def test_autograd_matches_adjoint_and_recovers_texture(torch_mod):
     err0 = float(((start - truth)[seen] ** 2).mean()) ** 0.5
     err1 = float(((x.detach() - truth)[seen] ** 2).mean()) ** 0.5
     assert err1 < 0.6 * err0, (err0, err1)
+
+
+def roughness_scene(spp: int) -> SceneDesc:
+    """adjoint_scene with a 4x4 roughness texture (its red channel) on the ground and the blob."""
+    d = adjoint_scene(False, 2, 10.0, w=64, h=48, spp=spp)
+    rough = np.random.default_rng(9).uniform(0.25, 0.8, (4, 4, 3)).astype(np.float32)
+    d.textures.append(TextureDesc(rough, 0, (1.0, 1.0)))
+    for o in d.objects[:2]:
+        o.material["roughness"] = 1.0
+        o.material["roughness_texture"] = 3
+    return d
+
+
+def test_roughness_adjoint_matches_finite_differences_in_expectation(torch_mod):
+    """The roughness moves the sampled specular directions, so the detached (path-replay) gradient
+    equals the derivative of the expected image, not of each sample: with a linear loss
+    L = sum w * I at 256 spp it is compared with central differences over every texel."""
+    torch = torch_mod
+    d = roughness_scene(256)
+    rig = Rig(torch, d)
+    tex = rig.tex[3]
+    w = torch.from_numpy(np.random.default_rng(3).uniform(0.5, 1.5, d.width * d.height * 3)
+                         .astype(np.float32)).cuda()
+    rig.image()
+    grad = torch.zeros(4 * 4 * 3, device="cuda")
+    adjoint_texture(rig.scene, d.view, rig.params, rig.aovs, w.data_ptr(), tex, grad.data_ptr(),
+                    _abi.SR_ADJOINT_ROUGHNESS, None, current_stream_handle())
+    torch.cuda.synchronize()
+    g = grad.cpu().numpy().reshape(4, 4, 3)
+    assert np.all(g[..., 1:] == 0.0)  # the roughness lookup reads channel 0 only
+    base = d.textures[3].texels.copy()
+    wn = w.cpu().numpy().astype(np.float64)
+
+    def loss(t):
+        rig.scene.update_texture(tex, t)
+        return float(np.dot(rig.image().astype(np.float64), wn))
+
+    h = 0.02
+    fd = np.zeros((4, 4))
+    for y in range(4):
+        for x in range(4):
+            tp, tm = base.copy(), base.copy()
+            tp[y, x, 0] += h
+            tm[y, x, 0] -= h
+            fd[y, x] = (loss(tp) - loss(tm)) / (2 * h)
+    rig.scene.update_texture(tex, base)
+    ga = g[..., 0].astype(np.float64)
+    rel = np.linalg.norm(ga - fd) / np.linalg.norm(fd)
+    corr = np.corrcoef(ga.ravel(), fd.ravel())[0, 1]
+    # measured on GB300: correlation 0.999, relative L2 error 0.064 (the renderer's claimed scatter
+    # pdf is not exactly its sampling density -- directions are folded to the geometric side -- so
+    # the detached gradient misses a small part of the expectation's derivative)
+    assert corr > 0.98 and rel < 0.15, (ga.round(2).tolist(), fd.round(2).tolist(), rel, corr)
