@@ -363,14 +363,18 @@ SR_API int sr_scene_autotune(SrScene* scene, const SrView* view, const SrRenderP
 SR_API int sr_adjoint_albedo(SrScene* scene, const SrView* view, const SrRenderParams* params,
                              const SrAovs* forward, const float* d_image, int32_t texture, float* grad,
                              float* replay, void* stream);
-/* The same for either parameter a texture can set: SR_ADJOINT_ALBEDO (the colour lookup; the
- * gradient fills all three channels) or SR_ADJOINT_ROUGHNESS (the roughness lookup, which reads the
- * red channel; the gradient fills channel 0).  For the roughness the sampled specular directions
- * move with the parameter, so the detached gradient is exact in expectation, not per sample. */
-enum { SR_ADJOINT_ALBEDO = 0, SR_ADJOINT_ROUGHNESS = 1 };
+/* The same for SR_ADJOINT_ALBEDO (a texture as the colour lookup; the gradient fills all three
+ * channels), SR_ADJOINT_ROUGHNESS (a texture as the roughness lookup, which reads the red channel;
+ * the gradient fills channel 0) or SR_ADJOINT_FOG_DENSITY (the scene's fog density; `texture` is
+ * ignored and `grad` is one float).  The roughness moves the sampled specular directions and the
+ * density the sampled scatter distances, so for these two the detached gradient is the derivative
+ * of the expected image (score terms for the density), not of each sample. */
+enum { SR_ADJOINT_ALBEDO = 0, SR_ADJOINT_ROUGHNESS = 1, SR_ADJOINT_FOG_DENSITY = 2 };
 SR_API int sr_adjoint_texture(SrScene* scene, const SrView* view, const SrRenderParams* params,
                               const SrAovs* forward, const float* d_image, int32_t texture, int32_t parameter,
                               float* grad, float* replay, void* stream);
+/* Sets the fog density of a built scene with fog (> 0), e.g. one step of inverse rendering. */
+SR_API int sr_scene_update_fog_density(SrScene* scene, float density);
 /* Replaces the texels of texture `texture` (rgb floats, its width x height) in a built scene's
  * device copy, e.g. one step of inverse rendering.  The context's texture and other scenes are left
  * as they are.  The scene's sky texture is refused (its light distribution is built from it). */

@@ -26,7 +26,7 @@ SR_SHAPE_AABOX = 2
 
 SR_AOV_NORMAL, SR_AOV_DEPTH, SR_AOV_VARIANCE, SR_AOV_SAMPLES, SR_AOV_UV = 0, 1, 2, 3, 4
 SR_ALIGN_TOP_LEFT, SR_ALIGN_CENTER = 0, 1
-SR_ADJOINT_ALBEDO, SR_ADJOINT_ROUGHNESS = 0, 1
+SR_ADJOINT_ALBEDO, SR_ADJOINT_ROUGHNESS, SR_ADJOINT_FOG_DENSITY = 0, 1, 2
 SR_TEXTURE_SRGB = 0
 SR_TEXTURE_LINEAR = 1
 SR_TEXTURE_HDR = 2
@@ -194,6 +194,7 @@ PROTOTYPES = {
     "sr_adjoint_texture": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P, C.c_int32,
                                 C.c_int32, _P, _P, _P]),
     "sr_scene_update_texture": (_I, [_P, C.c_int32, _P]),
+    "sr_scene_update_fog_density": (_I, [_P, C.c_float]),
     "sr_scene_update_texture_device": (_I, [_P, C.c_int32, _P, _P]),
 }
 

@@ -452,6 +452,10 @@ class Scene:
         t = np.ascontiguousarray(texels, dtype=np.float32)
         check(self._lib.sr_scene_update_texture(self.handle, tid, ptr(t)))
 
+    def update_fog_density(self, density: float) -> None:
+        """sr_scene_update_fog_density: the built scene's fog density (its fog must exist)."""
+        check(self._lib.sr_scene_update_fog_density(self.handle, float(density)))
+
     def update_texture_device(self, texture, d_texels: int, stream: Optional[int] = None) -> None:
         """sr_scene_update_texture_device: the same from a device pointer (float32 h x w x 3),
         asynchronous on `stream`."""
@@ -821,9 +825,10 @@ def adjoint_texture(scene: "Scene", view: "View", params: SrRenderParams, forwar
     """sr_adjoint_texture: adds dL/d(texels of `texture`) into `grad`, given d_image = dL/dI for the
     image I = radiance + radiance_fog of `forward` (device AOV planes of sr_render_device with the
     same scene, view and params), for the texture as the albedo (SR_ADJOINT_ALBEDO) or the roughness
-    (SR_ADJOINT_ROUGHNESS: channel 0 of grad) lookup.  d_image / grad / replay are device pointers
-    (float32, H x W x 3 and the texture's h x w x 3); asynchronous on `stream`."""
-    tid = texture.id if isinstance(texture, Texture) else int(texture)
+    (SR_ADJOINT_ROUGHNESS: channel 0 of grad) lookup, or for the fog density (SR_ADJOINT_FOG_DENSITY:
+    `texture` ignored, grad one float).  d_image / grad / replay are device pointers (float32,
+    H x W x 3 and the texture's h x w x 3); asynchronous on `stream`."""
+    tid = -1 if texture is None else (texture.id if isinstance(texture, Texture) else int(texture))
     v = view.to_c()
     check(scene._lib.sr_adjoint_texture(scene.handle, C.byref(v), C.byref(params), C.byref(forward),
                                         C.c_void_p(d_image), tid, int(parameter), C.c_void_p(grad),

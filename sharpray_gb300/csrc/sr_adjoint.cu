@@ -37,7 +37,8 @@ struct AdjVertex {
     Col add;    // radiance added per unit throughput (emission + light sample; fog light sample; sky)
     Col dadd;   // d add / d parameter (albedo: per channel; roughness: the rgb of d add / d roughness)
     Col s;      // scatter weight (surface)
-    Col ds;     // d s / d parameter, likewise
+    Col ds;     // d s / d parameter, likewise (fog density: ds.r holds the score of the segment into
+                // the vertex, d log(its sampling weight) / d density; s does not depend on it)
     Col pre;    // e_rr * s before the luminance clamp
     float rr;   // survival probability divided by (1: none)
     float clamp_max;
@@ -95,14 +96,31 @@ __device__ Col opaque_eval_droughness(const Surface& s, V3 view, V3 light) {
     return f * (dspec * (1.0f - s.transparency));
 }
 
-enum : int { ADJ_ALBEDO = 0, ADJ_ROUGHNESS = 1 };
+enum : int { ADJ_ALBEDO = 0, ADJ_ROUGHNESS = 1, ADJ_FOG_DENSITY = 2 };
+
+// Optical depth per unit fog density along r over [0, t] (t may be +inf): the integral of
+// exp(-falloff * height) that Fog.OpticalDepth scales by the density (fog_transmittance_inf).
+__device__ float fog_depth_unit(const DevScene& S, const Ray& r, float t) {
+    const float hd = r.d.y, hs = r.o.y;
+    const float es = sr_exp(-S.fog_falloff * hs);
+    if (fabsf(hd) < 1e-6f) return es * t;
+    return (es - sr_exp(-S.fog_falloff * (hs + t * hd))) / (S.fog_falloff * hd);
+}
+
+// d/d density of a quantity proportional to exp(-density * depth): -depth times it; zero where the
+// depth is infinite (the quantity is then exactly zero and so is the limit of its derivative).
+__device__ __forceinline__ Col fog_depth_derivative(Col value, float depth) {
+    return isfinite(depth) ? value * -depth : black();
+}
 
 template <int PARAM>
 __device__ __forceinline__ Col opaque_eval_dparam(const Surface& s, V3 view, V3 light) {
     if constexpr (PARAM == ADJ_ALBEDO)
         return opaque_eval_dalbedo(s, view, light);
-    else
+    else if constexpr (PARAM == ADJ_ROUGHNESS)
         return opaque_eval_droughness(s, view, light);
+    else
+        return black();
 }
 
 // Scene.SampleSkyDirect (sample_sky_direct in sr_path.cuh) returning also its derivative.
@@ -122,9 +140,34 @@ __device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos
     float spdf = opaque_pdf(s, view, ldir, specular_probability(s, view));
     float mis = power_heuristic(lpdf, spdf);
     Col sky = sky_radiance<false, GENERAL>(S, ldir, c);
-    dnee = sky * tr * opaque_eval_dparam<PARAM>(s, view, ldir) * mis / lpdf;
-    return sky * tr * refl * mis / lpdf;
+    Col nee = sky * tr * refl * mis / lpdf;
+    if constexpr (PARAM == ADJ_FOG_DENSITY) {  // the shadow ray's fog transmittance exp(-density * depth)
+        if (S.has_fog)
+            dnee = fog_depth_derivative(nee, fog_depth_unit(S, make_ray(pos, ldir), __int_as_float(0x7f800000)));
+    } else {
+        dnee = sky * tr * opaque_eval_dparam<PARAM>(s, view, ldir) * mis / lpdf;
+    }
+    return nee;
 }
+
+// Scene.SampleSkyDirectFog (sample_sky_direct_fog in sr_path.cuh) returning also d/d density.
+template <bool GENERAL, int PARAM>
+__device__ Col sample_sky_direct_fog_adj(const DevScene& S, V3 pos, V3 rdir, Rng& rng, Ctr& c, uint32_t* err,
+                                         Col& dadd) {
+    dadd = black();
+    V3 ldir;
+    float lpdf;
+    Col tr;
+    if (!sample_sky_light<false, GENERAL>(S, pos, rng, ldir, lpdf, tr, c, err)) return black();
+    float fog_pdf = hg_pdf(dot(rdir, ldir), S.fog_g);
+    float mis = power_heuristic(lpdf, fog_pdf);
+    Col out = sky_radiance<false, GENERAL>(S, ldir, c) * tr * fog_pdf * mis / lpdf;
+    if constexpr (PARAM == ADJ_FOG_DENSITY)
+        dadd = fog_depth_derivative(out, fog_depth_unit(S, make_ray(pos, ldir), __int_as_float(0x7f800000)));
+    return out;
+}
+
+__device__ __forceinline__ float sum3(Col c) { return c.r + c.g + c.b; }
 
 // Adjoint of x -> x / p, p = min(1, max component of x), at x (when p < 1).
 __device__ Col rr_adjoint(Col x, float p, Col a) {
@@ -170,9 +213,11 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
         x.ds = black();
         if (S.has_fog && fog_scatter_distance(S, ray, has_hit ? hit.dist : inf, rng, sdist)) {
             x.kind = AV_FOG;
+            if constexpr (PARAM == ADJ_FOG_DENSITY)  // score of a scatter at sdist: 1/density - depth
+                x.ds.r = 1.0f / S.fog_density - fog_depth_unit(S, ray, sdist);
             energy = energy * col3(S.fog_color);
             x.e_rr = energy;
-            x.add = sample_sky_direct_fog<false, GENERAL>(S, ray_at(ray, sdist), ray.d, rng, c, err);
+            x.add = sample_sky_direct_fog_adj<GENERAL, PARAM>(S, ray_at(ray, sdist), ray.d, rng, c, err, x.dadd);
             Col srad = x.add * energy;
             if (i == 0)
                 radiance_fog = radiance_fog + srad;
@@ -196,6 +241,8 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.kind = AV_SURF;
             x.uv = s.uv;
             x.material = hit.material;
+            if constexpr (PARAM == ADJ_FOG_DENSITY)  // score of passing the fog up to the surface
+                if (S.has_fog) x.ds.r = -fog_depth_unit(S, ray, dist);
             radiance = radiance + s.radiance * energy;
             Col dnee;
             Col nee = sample_sky_direct_adj<GENERAL, PARAM>(S, s, pos, view, rng, c, err, dnee);
@@ -210,7 +257,8 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.e_rr = energy;
             Scatter sc = surface_scatter<GENERAL>(s, ray.d, view, rng);
             x.s = sc.weight;
-            x.ds = opaque_eval_dparam<PARAM>(s, view, sc.dir) / fmaxf(sc.pdf, 1e-6f);
+            if constexpr (PARAM != ADJ_FOG_DENSITY)
+                x.ds = opaque_eval_dparam<PARAM>(s, view, sc.dir) / fmaxf(sc.pdf, 1e-6f);
             energy = energy * sc.weight;
             x.pre = energy;
             energy = clamp_luminance(energy, indirect_clamp);
@@ -219,6 +267,11 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
         } else {
             x.kind = AV_SKY;
+            if constexpr (PARAM == ADJ_FOG_DENSITY)  // score of passing the fog to infinity
+                if (S.has_fog) {
+                    const float depth = fog_depth_unit(S, ray, inf);
+                    x.ds.r = isfinite(depth) ? -depth : 0.0f;  // an escape needs a finite depth
+                }
             float mis = has_spdf ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
             x.add = sky_radiance<false, GENERAL>(S, ray.d, c) * mis;
             radiance = radiance + x.add * energy;
@@ -282,6 +335,7 @@ __global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, D
     AdjVertex v[kAdjMaxVertices];
     Rng rng = rng_seed(x, y);
     Col rad_sum = black(), fog_sum = black();
+    float g_density = 0.0f;  // this pixel's d loss / d fog density
     for (uint32_t si = 0; si < taken; ++si) {
         Ray ray = camera_ray(V, P, x, y, rng);
         Col rad, fog;
@@ -299,18 +353,30 @@ __global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, D
                 // e_rr = e_in * fog colour; add * e_rr; then the roulette divides e_rr
                 Col a_rr = (q.kind == AV_FOG ? rr_adjoint(q.e_rr, q.rr, a) : black()) + G * q.add;
                 a_in = a_rr * col3(S.fog_color);
+                if constexpr (PARAM == ADJ_FOG_DENSITY) g_density += sum3(G * q.e_rr * q.dadd);
             } else if (q.kind == AV_SURF_END) {
                 a_in = G * q.add;
-                scatter_texel_grad<PARAM>(S, q.material, q.uv, G * q.e_in * q.dadd, tex, grad);
+                if constexpr (PARAM == ADJ_FOG_DENSITY)
+                    g_density += sum3(G * q.e_in * q.dadd);
+                else
+                    scatter_texel_grad<PARAM>(S, q.material, q.uv, G * q.e_in * q.dadd, tex, grad);
             } else {
                 const Col a_pre = clamp_adjoint(q.pre, q.clamp_max, a);
                 const Col a_s = q.e_rr * a_pre;
                 a_in = rr_adjoint(q.e_in, q.rr, q.s * a_pre) + G * q.add;
-                scatter_texel_grad<PARAM>(S, q.material, q.uv, a_s * q.ds + G * q.e_in * q.dadd, tex, grad);
+                if constexpr (PARAM == ADJ_FOG_DENSITY)
+                    g_density += sum3(G * q.e_in * q.dadd);
+                else
+                    scatter_texel_grad<PARAM>(S, q.material, q.uv, a_s * q.ds + G * q.e_in * q.dadd, tex, grad);
             }
+            // the segment into the vertex scales e_in by its sampling weight, whose derivative is
+            // the weight times the score
+            if constexpr (PARAM == ADJ_FOG_DENSITY) g_density += q.ds.r * sum3(a_in * q.e_in);
             a = a_in;
         }
     }
+    if constexpr (PARAM == ADJ_FOG_DENSITY)
+        if (g_density != 0.0f) atomicAdd(grad, g_density);
     if (replay) {
         const Col r = rad_sum / (float)count, f = fog_sum / (float)count;
         replay[3 * i] = r.r + f.r;
@@ -332,11 +398,16 @@ cudaError_t launch_adjoint_texture(const DevScene& S, const DevView& V, const De
             SR_ADJ_LAUNCH(true, ADJ_ALBEDO);
         else
             SR_ADJ_LAUNCH(false, ADJ_ALBEDO);
-    } else {
+    } else if (parameter == ADJ_ROUGHNESS) {
         if (S.general)
             SR_ADJ_LAUNCH(true, ADJ_ROUGHNESS);
         else
             SR_ADJ_LAUNCH(false, ADJ_ROUGHNESS);
+    } else {
+        if (S.general)
+            SR_ADJ_LAUNCH(true, ADJ_FOG_DENSITY);
+        else
+            SR_ADJ_LAUNCH(false, ADJ_FOG_DENSITY);
     }
 #undef SR_ADJ_LAUNCH
     return cudaGetLastError();

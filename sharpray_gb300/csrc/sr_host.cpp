@@ -1718,10 +1718,14 @@ SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderPara
     if (int rc = need_device(s)) return rc;
     if (!fwd->radiance || !fwd->radiance_fog || !fwd->samples)
         return fail(SR_ERR_INVALID_ARG, "the adjoint needs the forward radiance, radiance_fog and samples planes");
-    if (texture < 0 || (size_t)texture >= s->tex_offset.size())
-        return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
-    if (parameter != SR_ADJOINT_ALBEDO && parameter != SR_ADJOINT_ROUGHNESS)
+    if (parameter != SR_ADJOINT_ALBEDO && parameter != SR_ADJOINT_ROUGHNESS && parameter != SR_ADJOINT_FOG_DENSITY)
         return fail(SR_ERR_INVALID_ARG, "unknown adjoint parameter %d", parameter);
+    if (parameter == SR_ADJOINT_FOG_DENSITY) {
+        if (!s->dev.has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
+        texture = -1;
+    } else if (texture < 0 || (size_t)texture >= s->tex_offset.size()) {
+        return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
+    }
     if (s->dev.has_transparent) return fail(SR_ERR_STATE, "the adjoint does not support transparent materials");
     DevView dv;
     DevParams dp;
@@ -1739,6 +1743,16 @@ SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderPara
 SR_API int sr_adjoint_albedo(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
                              const float* d_image, int32_t texture, float* grad, float* replay, void* stream) {
     return sr_adjoint_texture(s, view, params, fwd, d_image, texture, SR_ADJOINT_ALBEDO, grad, replay, stream);
+}
+
+SR_API int sr_scene_update_fog_density(SrScene* s, float density) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!s->built) return fail(SR_ERR_STATE, "Scene not built");
+    if (!s->has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
+    if (!(density > 0.0f) || !std::isfinite(density)) return fail(SR_ERR_INVALID_ARG, "fog density must be > 0");
+    s->fog.density = density;
+    s->dev.fog_density = density;  // kernels take the scene by value; a cached graph is rebuilt
+    return SR_OK;
 }
 
 static int updatable_texture(SrScene* s, int32_t texture) {

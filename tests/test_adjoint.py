@@ -292,3 +292,39 @@ def test_roughness_adjoint_matches_finite_differences_in_expectation(torch_mod):
     # pdf is not exactly its sampling density -- directions are folded to the geometric side -- so
     # the detached gradient misses a small part of the expectation's derivative)
     assert corr > 0.98 and rel < 0.15, (ga.round(2).tolist(), fd.round(2).tolist(), rel, corr)
+
+
+def test_fog_density_adjoint_matches_finite_differences_in_expectation(torch_mod):
+    """The density sets the sampled scatter distances, so its replay gradient carries score terms
+    (1/density - depth at a scatter, -depth where a segment or shadow ray passes the fog) and equals
+    the derivative of the expected image: compared with central differences of a linear loss at
+    256 spp (sr_scene_update_fog_density)."""
+    torch = torch_mod
+    d = adjoint_scene(True, 2, 10.0, w=64, h=48, spp=256)
+    rig = Rig(torch, d)
+    w = torch.from_numpy(np.random.default_rng(4).uniform(0.5, 1.5, d.width * d.height * 3)
+                         .astype(np.float32)).cuda()
+    rig.image()
+    grad = torch.zeros(1, device="cuda")
+    adjoint_texture(rig.scene, d.view, rig.params, rig.aovs, w.data_ptr(), None, grad.data_ptr(),
+                    _abi.SR_ADJOINT_FOG_DENSITY, None, current_stream_handle())
+    torch.cuda.synchronize()
+    g = float(grad.cpu()[0])
+    wn = w.cpu().numpy().astype(np.float64)
+    sigma, h = d.fog.density, 0.05 * d.fog.density
+
+    def loss(s):
+        rig.scene.update_fog_density(s)
+        return float(np.dot(rig.image().astype(np.float64), wn))
+
+    fd = (loss(sigma + h) - loss(sigma - h)) / (2 * h)
+    rig.scene.update_fog_density(sigma)
+    print("fog density adjoint", g, "fd", fd)
+    assert g != 0.0 and abs(g - fd) <= 0.1 * abs(fd), (g, fd)
+    # not for a scene without fog
+    nofog = Rig(torch, adjoint_scene(False, 2, 10.0, w=8, h=8, spp=1))
+    with pytest.raises(SharpRayError):
+        adjoint_texture(nofog.scene, nofog.d.view, nofog.params, nofog.aovs, w.data_ptr(), None, grad.data_ptr(),
+                        _abi.SR_ADJOINT_FOG_DENSITY)
+    with pytest.raises(SharpRayError):
+        nofog.scene.update_fog_density(0.1)
