@@ -894,7 +894,9 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     L.counters = ctr;
     L.general = s->dev.general;
     wave_grid_sizes(L, s->sms, &s->tune);
-    uint64_t cap = (uint64_t)dp.max_samples * (dp.bounces + 1) + 4;
+    // a runaway guard, not a budget: a pixel's samples run one after another, each taking up to
+    // bounces + 2 iterations (the last segment's shadow ray is traced one bounce later)
+    uint64_t cap = ((uint64_t)dp.max_samples + 1) * ((uint64_t)dp.bounces + 2) * 2 + 8;
     L.max_iters = (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap);
     uint32_t all_slots = 0;
     for (int g = 0; g < kWaveGroups; ++g) all_slots += s->ws[g].slots;

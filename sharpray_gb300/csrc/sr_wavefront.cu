@@ -969,8 +969,8 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
 }
 
 // Condition of the device-side bounce loop: continue while more than `tail` paths of all groups
-// are live (the rest go to the tail kernel) and the bounce cap (max_samples * (bounces + 1) per
-// pixel, plus slack) is not reached.  `counts` holds the groups' counters one after another.
+// are live (the rest go to the tail kernel) and the bounce cap (a runaway guard of twice
+// (max_samples + 1) * (bounces + 2) per pixel) is not reached.  `counts` holds the groups' counters one after another.
 __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, int groups, uint32_t tail,
                                 uint32_t max_iters, uint32_t* err) {
     uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
