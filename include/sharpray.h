@@ -321,6 +321,12 @@ SR_API int sr_compose_device_static(SrContext* ctx, const SrAovs* device_aovs, u
 SR_API int sr_preview(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height,
                       const SrComposeParams* params, uint8_t* host_rgb8);
 
+/* Renderer.Tick (renderer.cs:98-105) without blocking: (finished pixels, pixels) of the scene's
+ * last render launch (sr_render_device, sr_render_compose, sr_render_batch; sr_render returns
+ * finished).  The wavefront renderer publishes the count every two bounces; the megakernel render
+ * mode reports 0 until it completes.  Never waits for the GPU. */
+SR_API int sr_render_progress(SrScene* scene, uint32_t* done, uint32_t* total);
+
 /* Batched rendering (no counterpart in the reference, which renders one scene at a time): `count`
  * distinct built scenes of one context, each with its view, parameters and device AOV planes
  * (as sr_render_device), rendered by one CUDA graph launch on `stream` that holds one bounce

@@ -452,6 +452,13 @@ class Scene:
         t = np.ascontiguousarray(texels, dtype=np.float32)
         check(self._lib.sr_scene_update_texture(self.handle, tid, ptr(t)))
 
+    def progress(self) -> tuple:
+        """sr_render_progress: (finished pixels, pixels) of the last render launch, without waiting
+        (Renderer.Tick's (Step, Total), renderer.cs:98-105, at pixel granularity)."""
+        d, t = C.c_uint32(), C.c_uint32()
+        check(self._lib.sr_render_progress(self.handle, C.byref(d), C.byref(t)))
+        return d.value, t.value
+
     def update_fog_density(self, density: float) -> None:
         """sr_scene_update_fog_density: the built scene's fog density (its fog must exist)."""
         check(self._lib.sr_scene_update_fog_density(self.handle, float(density)))

@@ -159,6 +159,12 @@ struct SrScene {
     cudaGraphExec_t graph_exec = nullptr;
     WaveLaunch graph_launch{};  // launch parameters baked into graph_exec
     uint32_t* counts_host = nullptr;  // pinned
+    // render progress (sr_render_progress): finished pixels published by the device loop into a
+    // host-mapped word, and an event after the last render's launches
+    uint32_t* progress_host = nullptr;
+    uint32_t* progress_dev = nullptr;
+    cudaEvent_t progress_event = nullptr;
+    uint32_t progress_total = 0;
     int sms = 0;
     WaveTune tune{};  // launch geometry (sr_scene_set_tuning / sr_scene_autotune)
     DevBuf tune_aovs;  // autotune's scratch AOV planes
@@ -175,6 +181,8 @@ struct SrScene {
         for (cudaEvent_t& e : fork_events)
             if (e) cudaEventDestroy(e);
         if (counts_host) cudaFreeHost(counts_host);
+        if (progress_host) cudaFreeHost(progress_host);
+        if (progress_event) cudaEventDestroy(progress_event);
     }
 };
 
@@ -902,6 +910,7 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     for (int g = 0; g < kWaveGroups; ++g) all_slots += s->ws[g].slots;
     const uint32_t tail_div = s->tune.tail_div ? s->tune.tail_div : (uint32_t)SR_TAIL_DIV;
     L.tail_paths = tail_div > 0 ? all_slots / tail_div : 0;
+    L.progress = s->progress_dev;
     SR_CUDA(wave_init(L, st), "wavefront init");
     return SR_OK;
 }
@@ -933,8 +942,12 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
         SR_CUDA(wave_bounce(L, cur, st, s->side_streams, s->fork_events), "wavefront bounce");
         SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws[0].counts, count_bytes, cudaMemcpyDeviceToHost, st), "read live count");
         SR_CUDA(cudaStreamSynchronize(st), "wavefront bounce");
-        uint32_t live = 0;
-        for (int g = 0; g < kWaveGroups; ++g) live += wave_live(s->counts_host + g * kWaveCounters, cur ^ 1);
+        uint32_t live = 0, done = 0;
+        for (int g = 0; g < kWaveGroups; ++g) {
+            live += wave_live(s->counts_host + g * kWaveCounters, cur ^ 1);
+            done += s->counts_host[g * kWaveCounters + kCountDone];
+        }
+        if (s->progress_host) *(volatile uint32_t*)s->progress_host = done;
         if (live <= L.tail_paths) {
             s->last_host_iters = it + 1;
             s->last_tail = live > 0;
@@ -942,6 +955,18 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
             break;
         }
     }
+    return SR_OK;
+}
+
+// Progress of the render about to be launched on scene s: the host-mapped word cleared, the total.
+static int progress_begin(SrScene* s, uint32_t pixels) {
+    if (!s->progress_host) {
+        SR_CUDA(cudaHostAlloc(&s->progress_host, sizeof(uint32_t), cudaHostAllocMapped), "pinned alloc");
+        SR_CUDA(cudaHostGetDevicePointer((void**)&s->progress_dev, s->progress_host, 0), "mapped pointer");
+    }
+    if (!s->progress_event) SR_CUDA(cudaEventCreateWithFlags(&s->progress_event, cudaEventDisableTiming), "event");
+    *(volatile uint32_t*)s->progress_host = 0;
+    s->progress_total = pixels;
     return SR_OK;
 }
 
@@ -957,11 +982,31 @@ static int render_into(SrScene* s, const SrView* view, const SrRenderParams* par
     }
     int mode = s->render_mode == SR_RENDER_AUTO ? SR_RENDER_WAVEFRONT_GRAPH : s->render_mode;
     s->last_mode = mode;
+    if (int rc = progress_begin(s, dp.width * dp.height)) return rc;
     if (mode == SR_RENDER_MEGAKERNEL) {
         SR_CUDA(launch_render(s->dev, dv, dp, out, ctr, s->err.as<uint32_t>(), st), "render launch");
-        return SR_OK;
+    } else if (int rc = render_wavefront(s, dv, dp, out, ctr, st, mode == SR_RENDER_WAVEFRONT_GRAPH)) {
+        return rc;
     }
-    return render_wavefront(s, dv, dp, out, ctr, st, mode == SR_RENDER_WAVEFRONT_GRAPH);
+    SR_CUDA(cudaEventRecord(s->progress_event, st), "progress event");
+    return SR_OK;
+}
+
+SR_API int sr_render_progress(SrScene* s, uint32_t* done, uint32_t* total) {
+    if (!s || !done || !total) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    *total = s->progress_total;
+    *done = 0;
+    if (!s->progress_event) return SR_OK;  // nothing rendered yet
+    cudaError_t q = cudaEventQuery(s->progress_event);
+    if (q == cudaSuccess) {
+        *done = s->progress_total;
+    } else if (q == cudaErrorNotReady) {
+        uint32_t d = *(volatile uint32_t*)s->progress_host;
+        *done = d < s->progress_total ? d : s->progress_total;
+    } else {
+        SR_CUDA(q, "progress query");
+    }
+    return SR_OK;
 }
 
 SR_API int sr_render_device(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* out,
@@ -1008,6 +1053,7 @@ SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const Sr
         const SrAovs& o = outs[i];
         DevAovs d{o.radiance, o.radiance_fog, o.normals, o.uv, o.depth, o.samples, o.variance};
         std::memset(&Ls[i], 0, sizeof(WaveLaunch));
+        if (int rc = progress_begin(s, dp.width * dp.height)) return rc;
         if (int rc = wave_prepare(s, dv, dp, d, ctr, st, Ls[i])) return rc;
         s->last_mode = SR_RENDER_WAVEFRONT_GRAPH;
     }
@@ -1027,6 +1073,7 @@ SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const Sr
         ctx->batch_launch = Ls;
     }
     SR_CUDA(cudaGraphLaunch(ctx->batch_exec, st), "launch batch graph");
+    for (uint32_t i = 0; i < count; ++i) SR_CUDA(cudaEventRecord(scenes[i]->progress_event, st), "progress event");
     return SR_OK;
 }
 

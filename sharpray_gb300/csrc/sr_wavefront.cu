@@ -765,6 +765,12 @@ __global__ void __launch_bounds__(128, shade_min_blocks(EVK)) k_wave_shade(WaveS
     flush_counters<COUNT>(c, counters);
 }
 
+// One more finished pixel per calling thread (warp-aggregated: one atomic per converged group).
+__device__ __forceinline__ void count_pixel_done(uint32_t* counter) {
+    const unsigned m = __activemask();
+    if ((int)(threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(counter, (uint32_t)__popc(m));
+}
+
 // End of the sample in slot s: the pending NEE contribution of its last segment, the pixel
 // statistics and the adaptive stop (renderer.cs:173-212), then the next camera ray or the AOVs.
 template <bool COUNT, bool GENERAL>
@@ -823,6 +829,7 @@ __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevS
             out.depth[i] = dcount > 0 ? a4.x / (float)dcount : __int_as_float(0x7f800000);
             out.samples[i] = count;
             out.variance[i] = var;
+            count_pixel_done(W.counts + kCountDone);
         } else {
             Rng rng = rng_of(gr);
             Ray ray = camera_ray(V, P, x, y, rng);
@@ -972,11 +979,15 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
 // are live (the rest go to the tail kernel) and the bounce cap (a runaway guard of twice
 // (max_samples + 1) * (bounces + 2) per pixel) is not reached.  `counts` holds the groups' counters one after another.
 __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, int groups, uint32_t tail,
-                                uint32_t max_iters, uint32_t* err) {
+                                uint32_t max_iters, uint32_t* err, uint32_t* progress) {
     uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
     counts[kCountIter] = it;
-    uint32_t live = 0;
-    for (int g = 0; g < groups; ++g) live += wave_live(counts + g * kWaveCounters, 0);  // next bounce: parity 0
+    uint32_t live = 0, done = 0;
+    for (int g = 0; g < groups; ++g) {
+        live += wave_live(counts + g * kWaveCounters, 0);  // next bounce: parity 0
+        done += counts[g * kWaveCounters + kCountDone];
+    }
+    if (progress) *(volatile uint32_t*)progress = done;  // host-mapped: read by sr_render_progress
     bool more = live > tail;
     if (more && it >= max_iters) {
         atomicOr(err, SR_DEVERR_LOOP);
@@ -1147,7 +1158,8 @@ cudaError_t wave_build_graph_batch(const WaveLaunch* Ls, int n, cudaStream_t cap
         if (e != cudaSuccess) break;
         // two bounces per group on parallel branches, joined before the loop condition
         cudaError_t e1 = launch_bounces(L, 0, 2, capture_stream, side, fork);
-        k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.tail_paths, L.max_iters, L.err);
+        k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.tail_paths, L.max_iters, L.err,
+                                                     L.progress);
         cudaGraph_t captured = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
         e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : cudaGetLastError());

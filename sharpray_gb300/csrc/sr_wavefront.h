@@ -78,6 +78,7 @@ enum : int {
     kCountResolve = 0,     // samples finished this bounce without a shadow ray to trace
     kCountIter = 1,        // bounces run by the device loop
     kCountTraceFetch = 2,  // the trace kernel's fetch cursor
+    kCountDone = 3,        // pixels whose AOVs are written (render progress)
     kCountTrace = 4,       // + parity: trace-queue length
     kCountShadow = 6,      // + parity: shadow-queue length
     kCountLate = 8,        // + parity: late finished samples
@@ -109,6 +110,7 @@ struct WaveLaunch {
     uint32_t max_iters;
     uint32_t tail_paths;  // the bounce loop stops when at most this many paths are live; the tail
                           // kernel then finishes them, one thread per slot
+    uint32_t* progress;   // host-mapped word the device loop publishes finished pixels to (or null)
 };
 
 // Every group's state, as one kernel argument.
