@@ -301,6 +301,12 @@ SR_API int sr_scene_counters(SrScene* scene, uint64_t* counters_out);
  * FilterFog :206-245, Tonemap :247-266, Color.ToPixel math.cs:127-136). */
 SR_API int sr_compose(SrContext* ctx, const SrAovs* host_aovs, uint32_t width, uint32_t height,
                       const SrComposeParams* params, uint8_t* host_rgb8);
+/* Filter + FilterFog without the tonemap: the denoised linear radiance + fog (the colour that
+ * Tonemap receives, compose.cs:93) into `device_linear` (width*height*3 floats), and the RGB8
+ * image into `device_rgb8` too unless it is NULL.  Device AOVs as sr_compose_device, on `stream`. */
+SR_API int sr_compose_float_device(SrContext* ctx, const SrAovs* device_aovs, uint32_t width, uint32_t height,
+                                   const SrComposeParams* params, float* device_linear, uint8_t* device_rgb8,
+                                   void* stream);
 /* Same on device buffers (radiance, radiance_fog, normals, depth, variance are read) on `stream`. */
 SR_API int sr_compose_device(SrContext* ctx, const SrAovs* device_aovs, uint32_t width, uint32_t height,
                              const SrComposeParams* params, uint8_t* device_rgb8, void* stream);

@@ -179,6 +179,7 @@ PROTOTYPES = {
     "sr_compose": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P]),
     "sr_compose_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
     "sr_compose_device_static": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
+    "sr_compose_float_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P, _P]),
     "sr_preview": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P]),
     "sr_render_batch": (_I, [_P, _P, _P, _P, _U, _P]),
     "sr_render_progress": (_I, [_P, C.POINTER(_U), C.POINTER(_U)]),

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128) k_compose(const float4* __restrict__ p_ra
                                                  const float4* __restrict__ p_fog, const float* __restrict__ variance,
                                                  uint32_t width, uint32_t height, ComposeConsts k,
                                                  const float* __restrict__ spatial, const float* __restrict__ fog_spatial,
-                                                 int denoise, uint8_t* rgb8) {
+                                                 int denoise, uint8_t* rgb8, float* linear) {
     int x = blockIdx.x * 32 + (threadIdx.x & 31);
     int y = blockIdx.y * 4 + (threadIdx.x >> 5);
     if (x >= (int)width || y >= (int)height) return;
@@ -142,12 +142,14 @@ __global__ void __launch_bounds__(128) k_compose(const float4* __restrict__ p_ra
             fog = rsum / wsum;
         }
     }
-    tonemap(k, main + fog, rgb8 + ci * 3);
+    const Col total = main + fog;
+    if (linear) linear[3 * ci] = total.r, linear[3 * ci + 1] = total.g, linear[3 * ci + 2] = total.b;
+    if (rgb8) tonemap(k, total, rgb8 + ci * 3);
 }
 
 cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, const ComposeConsts& k,
                            const float* spatial, const float* fog_spatial, bool denoise, uint8_t* rgb8,
-                           float4* scratch, cudaStream_t stream) {
+                           float4* scratch, cudaStream_t stream, float* linear) {
     uint32_t n = width * height;
     if (n == 0) return cudaSuccess;
     float4* p_rad = scratch;
@@ -156,7 +158,7 @@ cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, c
     k_pack<<<(n + 255) / 256, 256, 0, stream>>>(in, n, p_rad, p_geo, p_fog);
     dim3 grid((width + 31) / 32, (height + 3) / 4);
     k_compose<<<grid, 128, 0, stream>>>(p_rad, p_geo, p_fog, in.variance, width, height, k, spatial, fog_spatial,
-                                        denoise ? 1 : 0, rgb8);
+                                        denoise ? 1 : 0, rgb8, linear);
     return cudaGetLastError();
 }
 

@@ -820,7 +820,8 @@ static int make_view(const SrView* v, const SrRenderParams* p, DevView& dv, DevP
 }
 
 static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t h, const SrComposeParams* p,
-                        bool denoise, uint8_t* rgb8, cudaStream_t st);
+                        bool denoise, uint8_t* rgb8, cudaStream_t st,
+                        float* linear = nullptr);
 
 // Allocates the wavefront path state for a tiles_x x tiles_y grid of 8x4 slot tiles: the records
 // of every slot, then each group's queues, then every group's counters (one block, carved).
@@ -1285,7 +1286,7 @@ static void build_table(std::vector<float>& out, int radius, float inv, float sc
 }
 
 static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t h, const SrComposeParams* p,
-                        bool denoise, uint8_t* rgb8, cudaStream_t st) {
+                        bool denoise, uint8_t* rgb8, cudaStream_t st, float* linear) {
     if (!p) return fail(SR_ERR_INVALID_ARG, "params is NULL");
     if (ctx->device < 0) return fail(SR_ERR_STATE, "host-only context (device -1) cannot run device work");
     if (w == 0 || h == 0) return fail(SR_ERR_INVALID_ARG, "empty image");
@@ -1319,9 +1320,21 @@ static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t 
     size_t n = (size_t)w * h;
     SR_CUDA(ctx->compose_scratch.reserve(n * 3 * sizeof(float4)), "alloc compose scratch");
     const float* d_tab = ctx->compose_tables.as<float>();
-    SR_CUDA(launch_compose(in, w, h, k, d_tab, d_tab + fog_off, denoise, rgb8, ctx->compose_scratch.as<float4>(), st),
+    SR_CUDA(launch_compose(in, w, h, k, d_tab, d_tab + fog_off, denoise, rgb8, ctx->compose_scratch.as<float4>(), st,
+                           linear),
             "compose launch");
     return SR_OK;
+}
+
+SR_API int sr_compose_float_device(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p,
+                                   float* device_linear, uint8_t* device_rgb8, void* stream) {
+    if (!ctx || !a || !device_linear) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (!a->radiance || !a->radiance_fog || !a->normals || !a->depth || !a->variance)
+        return fail(SR_ERR_INVALID_ARG, "compose needs radiance, radiance_fog, normals, depth and variance");
+    SR_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    DevAovs d{a->radiance, a->radiance_fog, a->normals, a->uv, a->depth, a->samples, a->variance};
+    return compose_impl(ctx, d, w, h, p, true, device_rgb8, st, device_linear);
 }
 
 SR_API int sr_compose_device(SrContext* ctx, const SrAovs* a, uint32_t w, uint32_t h, const SrComposeParams* p,

@@ -48,9 +48,11 @@ struct ComposeConsts {
     float lum_limit_inv, normal_limit_inv, depth_limit_inv;
     int32_t radius, fog_radius;
 };
+// `linear` (optional, width x height x 3): the filtered radiance + fog before exposure and tonemap;
+// rgb8 may be null when only that is wanted.
 cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, const ComposeConsts& k,
                            const float* spatial, const float* fog_spatial, bool denoise, uint8_t* rgb8,
-                           float4* scratch, cudaStream_t stream);
+                           float4* scratch, cudaStream_t stream, float* linear = nullptr);
 
 // Compositing that allocates nothing: packed planes live in a fixed device array of sr_compose.cu
 // (bands of rows); spatial weights are evaluated per tap.  Returns cudaErrorInvalidValue when the
