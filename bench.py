@@ -62,6 +62,8 @@ def parse():
                     help="adjoint workload: texel channels checked by finite differences (-1: skip the workload)")
     ap.add_argument("--inverse-steps", type=int, default=200,
                     help="Adam steps of the inverse-rendering run (0: skip)")
+    ap.add_argument("--c5-steps", type=int, default=0,
+                    help="--adjoint-only: also time this many steps of the 16-view 768x768 differentiable workload")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the adjoint workload (--steps timed passes, --adjoint-checks FD checks)")
     ap.add_argument("--profile-once", action="store_true",
@@ -420,6 +422,95 @@ def measure_inverse(steps: int, views: int = 4, size: int = 256, spp: int = 8) -
                     "wrapper; targets share the renderer's per-pixel random numbers"}
 
 
+def measure_inverse_c5(steps: int, views: int = 16) -> dict:
+    """The batched + differentiable configuration (synth.config_c5: 16 orbit views, 768x768, 32 spp,
+    depth 8, 500,000 triangles, 1024x1024 albedo + roughness textures, fog): per step every view is
+    rendered and its image gradient replayed once for the albedo texture, the roughness texture and
+    the fog density together (sr_adjoint_all), then one Adam step updates all three (from flat grey
+    textures and 1.5x the density).
+    Reports the time per step after one warm-up step; `steps` timed steps."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+    from sharpray_gb300 import Context, Transform, View, _abi, render_params, synth
+    from sharpray_gb300.autograd import device_aovs
+    t_setup = time.perf_counter()
+    d = synth.config_c5()
+    ctx = Context(0)
+    ctx.set_bvh_build(_abi.SR_BVH_BUILD_DEVICE)
+    sc = d.instantiate(ctx)
+    sc.build()
+    tex_a, tex_r = sc._keepalive[0][1], sc._keepalive[0][2]
+    p = render_params(*d.render_args())
+    cams = []
+    for k in range(views):
+        ang = 2.0 * math.pi * k / views
+        pos = (2.9 * math.sin(ang), 0.4 + 0.6 * math.sin(3.0 * ang), -2.9 * math.cos(ang))
+        cams.append(View(Transform(pos, synth.look_rotation(pos, (0.0, 0.0, 0.0))), d.view.fov, d.view.near).to_c())
+    truth_a = torch.from_numpy(d.textures[1].texels).cuda()
+    truth_r = torch.from_numpy(d.textures[2].texels).cuda()
+    sigma = d.fog.density
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    bufs, aovs = device_aovs(d.width, d.height)
+    lib = ctx._lib
+    with torch.cuda.stream(st):
+        def render(v):
+            _abi.check(lib.sr_render_device(sc.handle, C.byref(v), C.byref(p), C.byref(aovs),
+                                            C.c_void_p(st.cuda_stream)))
+            return bufs["radiance"] + bufs["radiance_fog"]
+
+        targets = [render(v).clone() for v in cams]
+        xa = torch.full_like(truth_a, 0.5).requires_grad_(True)
+        xr = torch.full_like(truth_r, 0.5).requires_grad_(True)
+        xs = torch.tensor([1.5 * sigma], device="cuda", requires_grad=True)
+        opt = torch.optim.Adam([{"params": [xa, xr], "lr": 0.02}, {"params": [xs], "lr": 0.002}])
+        losses = []
+
+        def step():
+            sc.update_texture_device(tex_a, xa.detach().data_ptr(), st.cuda_stream)
+            sc.update_texture_device(tex_r, xr.detach().data_ptr(), st.cuda_stream)
+            sc.update_fog_density(float(xs.detach()))
+            ga, gr, gs = torch.zeros_like(xa), torch.zeros_like(xr), torch.zeros_like(xs)
+            loss = torch.zeros((), dtype=torch.float64, device="cuda")
+            for v, t in zip(cams, targets):
+                img = render(v)
+                diff = img - t
+                loss += (diff.double() ** 2).sum()
+                d_img = 2.0 * diff
+                _abi.check(lib.sr_adjoint_all(sc.handle, C.byref(v), C.byref(p), C.byref(aovs),
+                                              C.c_void_p(d_img.data_ptr()), tex_a.id, C.c_void_p(ga.data_ptr()),
+                                              tex_r.id, C.c_void_p(gr.data_ptr()), C.c_void_p(gs.data_ptr()), None,
+                                              C.c_void_p(st.cuda_stream)))
+            xa.grad, xr.grad, xs.grad = ga, gr, gs
+            opt.step()
+            with torch.no_grad():
+                xa.clamp_(0.0, 1.0)
+                xr.clamp_(0.05, 1.0)
+                xs.clamp_(1e-3, 1.0)
+            losses.append(loss)
+
+        step()  # warm-up
+        st.synchronize()
+        setup_s = time.perf_counter() - t_setup
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step()
+        st.synchronize()
+        dt = (time.perf_counter() - t0) / max(steps, 1)
+    n_grads = truth_a.numel() + truth_r.shape[0] * truth_r.shape[1] + 1
+    samples = views * d.width * d.height * d.spp
+    return {"workload": f"{views} orbit views {d.width}x{d.height}, {d.spp} spp, depth 8, "
+                        f"{d.triangle_count} triangles, 1024x1024 albedo + roughness textures, fog 0.03",
+            "timed_steps": steps, "ms_per_step": 1000 * dt, "texel_grads_per_s": n_grads / dt,
+            "path_samples_per_s": samples * 2 / dt, "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
+            "fog_density": {"true": sigma, "start": 1.5 * sigma, "after": float(xs.detach())},
+            "setup_s": round(setup_s, 1),
+            "note": "per step: each view rendered once (wavefront graph) and replayed once for all three "
+                    "gradients (sr_adjoint_all); path_samples_per_s counts both passes"}
+
+
 def run_reference(args):
     rank, _, world = dist_info()
     if rank != 0:
@@ -690,6 +781,8 @@ def main():
         adj = measure_adjoint(max(args.adjoint_checks, 0), reps=max(args.steps, 1))
         if args.inverse_steps > 0:
             adj["inverse_rendering"] = measure_inverse(args.inverse_steps)
+        if args.c5_steps > 0:
+            adj["batched_differentiable"] = measure_inverse_c5(args.c5_steps)
         print(json.dumps({"adjoint": adj}), flush=True)
     else:
         run_ours(args)

@@ -385,6 +385,12 @@ enum { SR_ADJOINT_ALBEDO = 0, SR_ADJOINT_ROUGHNESS = 1, SR_ADJOINT_FOG_DENSITY =
 SR_API int sr_adjoint_texture(SrScene* scene, const SrView* view, const SrRenderParams* params,
                               const SrAovs* forward, const float* d_image, int32_t texture, int32_t parameter,
                               float* grad, float* replay, void* stream);
+/* All three from one replay (one kernel launch instead of three): the albedo texture's gradient
+ * into albedo_grad, the roughness texture's into roughness_grad (channel 0) and the fog density's
+ * into fog_density_grad[0]; a NULL gradient skips its part. */
+SR_API int sr_adjoint_all(SrScene* scene, const SrView* view, const SrRenderParams* params, const SrAovs* forward,
+                          const float* d_image, int32_t albedo_texture, float* albedo_grad, int32_t roughness_texture,
+                          float* roughness_grad, float* fog_density_grad, float* replay, void* stream);
 /* Sets the fog density of a built scene with fog (> 0), e.g. one step of inverse rendering. */
 SR_API int sr_scene_update_fog_density(SrScene* scene, float density);
 /* Replaces the texels of texture `texture` (rgb floats, its width x height) in a built scene's

@@ -195,6 +195,8 @@ PROTOTYPES = {
                                _P, _P, _P]),
     "sr_adjoint_texture": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P, C.c_int32,
                                 C.c_int32, _P, _P, _P]),
+    "sr_adjoint_all": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.POINTER(SrAovs), _P, C.c_int32, _P,
+                            C.c_int32, _P, _P, _P, _P]),
     "sr_scene_update_texture": (_I, [_P, C.c_int32, _P]),
     "sr_scene_update_fog_density": (_I, [_P, C.c_float]),
     "sr_scene_update_texture_device": (_I, [_P, C.c_int32, _P, _P]),

@@ -22,6 +22,8 @@
 // than per sample.  Scenes with transparent materials are refused by the host entry point.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "sr_kernels.h"
 #include "sr_path.cuh"
 
@@ -31,11 +33,24 @@ constexpr int kAdjMaxVertices = 17;  // bounces <= 16
 
 enum : int { AV_FOG = 0, AV_SURF = 1, AV_SURF_END = 2, AV_SKY = 3, AV_FOG_END = 4 };
 
+enum : int { ADJ_ALBEDO = 0, ADJ_ROUGHNESS = 1, ADJ_FOG_DENSITY = 2, ADJ_ALL = 3 };
+
+// The roughness and fog-density derivatives of a vertex, kept besides the albedo ones when one
+// replay serves all three parameters.
+struct AdjExtra {
+    Col dadd_r;   // d add / d roughness
+    Col ds_r;     // d s / d roughness
+    Col dadd_f;   // d add / d fog density
+    float score;  // d log(sampling weight of the segment into the vertex) / d fog density
+};
+struct AdjNone {};
+
+template <int PARAM>
 struct AdjVertex {
     Col e_in;   // throughput entering the vertex
     Col e_rr;   // throughput after the Russian roulette (surface), or after the fog colour (fog)
     Col add;    // radiance added per unit throughput (emission + light sample; fog light sample; sky)
-    Col dadd;   // d add / d parameter (albedo: per channel; roughness: the rgb of d add / d roughness)
+    Col dadd;   // d add / d parameter (albedo: per channel; roughness, density: the rgb of d add / d p)
     Col s;      // scatter weight (surface)
     Col ds;     // d s / d parameter, likewise (fog density: ds.r holds the score of the segment into
                 // the vertex, d log(its sampling weight) / d density; s does not depend on it)
@@ -45,7 +60,34 @@ struct AdjVertex {
     V2 uv;
     int kind;
     int material;
+    std::conditional_t<PARAM == ADJ_ALL, AdjExtra, AdjNone> ex;
 };
+
+template <int PARAM> constexpr bool kAdjAlbedo = PARAM == ADJ_ALBEDO || PARAM == ADJ_ALL;
+template <int PARAM> constexpr bool kAdjRough = PARAM == ADJ_ROUGHNESS || PARAM == ADJ_ALL;
+template <int PARAM> constexpr bool kAdjFog = PARAM == ADJ_FOG_DENSITY || PARAM == ADJ_ALL;
+
+// Where each parameter's derivatives sit in a record.
+template <int PARAM>
+__device__ __forceinline__ Col dadd_rough(const AdjVertex<PARAM>& q) {
+    if constexpr (PARAM == ADJ_ALL) return q.ex.dadd_r; else return q.dadd;
+}
+template <int PARAM>
+__device__ __forceinline__ Col ds_rough(const AdjVertex<PARAM>& q) {
+    if constexpr (PARAM == ADJ_ALL) return q.ex.ds_r; else return q.ds;
+}
+template <int PARAM>
+__device__ __forceinline__ Col dadd_fog(const AdjVertex<PARAM>& q) {
+    if constexpr (PARAM == ADJ_ALL) return q.ex.dadd_f; else return q.dadd;
+}
+template <int PARAM>
+__device__ __forceinline__ float score_of(const AdjVertex<PARAM>& q) {
+    if constexpr (PARAM == ADJ_ALL) return q.ex.score; else return q.ds.r;
+}
+template <int PARAM>
+__device__ __forceinline__ void set_score(AdjVertex<PARAM>& x, float score) {
+    if constexpr (PARAM == ADJ_ALL) x.ex.score = score; else x.ds.r = score;
+}
 
 // d opaque_eval / d albedo (per channel), pdfs held fixed.
 __device__ Col opaque_eval_dalbedo(const Surface& s, V3 view, V3 light) {
@@ -96,8 +138,6 @@ __device__ Col opaque_eval_droughness(const Surface& s, V3 view, V3 light) {
     return f * (dspec * (1.0f - s.transparency));
 }
 
-enum : int { ADJ_ALBEDO = 0, ADJ_ROUGHNESS = 1, ADJ_FOG_DENSITY = 2 };
-
 // Optical depth per unit fog density along r over [0, t] (t may be +inf): the integral of
 // exp(-falloff * height) that Fog.OpticalDepth scales by the density (fog_transmittance_inf).
 __device__ float fog_depth_unit(const DevScene& S, const Ray& r, float t) {
@@ -113,21 +153,16 @@ __device__ __forceinline__ Col fog_depth_derivative(Col value, float depth) {
     return isfinite(depth) ? value * -depth : black();
 }
 
-template <int PARAM>
-__device__ __forceinline__ Col opaque_eval_dparam(const Surface& s, V3 view, V3 light) {
-    if constexpr (PARAM == ADJ_ALBEDO)
-        return opaque_eval_dalbedo(s, view, light);
-    else if constexpr (PARAM == ADJ_ROUGHNESS)
-        return opaque_eval_droughness(s, view, light);
-    else
-        return black();
-}
+// d nee / d albedo (per channel), d roughness, d fog density.
+struct NeeDeriv {
+    Col a, r, f;
+};
 
-// Scene.SampleSkyDirect (sample_sky_direct in sr_path.cuh) returning also its derivative.
+// Scene.SampleSkyDirect (sample_sky_direct in sr_path.cuh) returning also its derivatives.
 template <bool GENERAL, int PARAM>
 __device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos, V3 view, Rng& rng, Ctr& c,
-                                     uint32_t* err, Col& dnee) {
-    dnee = black();
+                                     uint32_t* err, NeeDeriv& dn) {
+    dn.a = dn.r = dn.f = black();
     V3 ldir;
     float lpdf;
     Col tr;
@@ -141,11 +176,11 @@ __device__ Col sample_sky_direct_adj(const DevScene& S, const Surface& s, V3 pos
     float mis = power_heuristic(lpdf, spdf);
     Col sky = sky_radiance<false, GENERAL>(S, ldir, c);
     Col nee = sky * tr * refl * mis / lpdf;
-    if constexpr (PARAM == ADJ_FOG_DENSITY) {  // the shadow ray's fog transmittance exp(-density * depth)
+    if constexpr (kAdjAlbedo<PARAM>) dn.a = sky * tr * opaque_eval_dalbedo(s, view, ldir) * mis / lpdf;
+    if constexpr (kAdjRough<PARAM>) dn.r = sky * tr * opaque_eval_droughness(s, view, ldir) * mis / lpdf;
+    if constexpr (kAdjFog<PARAM>) {  // the shadow ray's fog transmittance exp(-density * depth)
         if (S.has_fog)
-            dnee = fog_depth_derivative(nee, fog_depth_unit(S, make_ray(pos, ldir), __int_as_float(0x7f800000)));
-    } else {
-        dnee = sky * tr * opaque_eval_dparam<PARAM>(s, view, ldir) * mis / lpdf;
+            dn.f = fog_depth_derivative(nee, fog_depth_unit(S, make_ray(pos, ldir), __int_as_float(0x7f800000)));
     }
     return nee;
 }
@@ -162,7 +197,7 @@ __device__ Col sample_sky_direct_fog_adj(const DevScene& S, V3 pos, V3 rdir, Rng
     float fog_pdf = hg_pdf(dot(rdir, ldir), S.fog_g);
     float mis = power_heuristic(lpdf, fog_pdf);
     Col out = sky_radiance<false, GENERAL>(S, ldir, c) * tr * fog_pdf * mis / lpdf;
-    if constexpr (PARAM == ADJ_FOG_DENSITY)
+    if constexpr (kAdjFog<PARAM>)
         dadd = fog_depth_derivative(out, fog_depth_unit(S, make_ray(pos, ldir), __int_as_float(0x7f800000)));
     return out;
 }
@@ -193,7 +228,7 @@ __device__ Col clamp_adjoint(Col x, float max, Col a) {
 // sample_path (sr_render.cu) recording the vertices; rad / fog as the forward pass sums them.
 template <bool GENERAL, int PARAM>
 __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t bounces, float indirect_clamp,
-                             AdjVertex* v, Col& radiance, Col& radiance_fog, Ctr& c, uint32_t* err) {
+                             AdjVertex<PARAM>* v, Col& radiance, Col& radiance_fog, Ctr& c, uint32_t* err) {
     radiance = black();
     radiance_fog = black();
     Col energy = white();
@@ -205,19 +240,25 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
         SurfHit hit;
         bool has_hit = trace_surface<false, GENERAL>(S, ray, hit, c, err);
         float sdist;
-        AdjVertex& x = v[n++];
+        AdjVertex<PARAM>& x = v[n++];
         x.e_in = energy;
         x.rr = 1.0f;
         x.clamp_max = indirect_clamp;
         x.dadd = black();
         x.ds = black();
+        if constexpr (PARAM == ADJ_ALL) x.ex = AdjExtra{black(), black(), black(), 0.0f};
         if (S.has_fog && fog_scatter_distance(S, ray, has_hit ? hit.dist : inf, rng, sdist)) {
             x.kind = AV_FOG;
-            if constexpr (PARAM == ADJ_FOG_DENSITY)  // score of a scatter at sdist: 1/density - depth
-                x.ds.r = 1.0f / S.fog_density - fog_depth_unit(S, ray, sdist);
+            if constexpr (kAdjFog<PARAM>)  // score of a scatter at sdist: 1/density - depth
+                set_score(x, 1.0f / S.fog_density - fog_depth_unit(S, ray, sdist));
             energy = energy * col3(S.fog_color);
             x.e_rr = energy;
-            x.add = sample_sky_direct_fog_adj<GENERAL, PARAM>(S, ray_at(ray, sdist), ray.d, rng, c, err, x.dadd);
+            Col dfog;
+            x.add = sample_sky_direct_fog_adj<GENERAL, PARAM>(S, ray_at(ray, sdist), ray.d, rng, c, err, dfog);
+            if constexpr (PARAM == ADJ_ALL)
+                x.ex.dadd_f = dfog;
+            else if constexpr (PARAM == ADJ_FOG_DENSITY)
+                x.dadd = dfog;
             Col srad = x.add * energy;
             if (i == 0)
                 radiance_fog = radiance_fog + srad;
@@ -241,14 +282,20 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.kind = AV_SURF;
             x.uv = s.uv;
             x.material = hit.material;
-            if constexpr (PARAM == ADJ_FOG_DENSITY)  // score of passing the fog up to the surface
-                if (S.has_fog) x.ds.r = -fog_depth_unit(S, ray, dist);
+            if constexpr (kAdjFog<PARAM>)  // score of passing the fog up to the surface
+                if (S.has_fog) set_score(x, -fog_depth_unit(S, ray, dist));
             radiance = radiance + s.radiance * energy;
-            Col dnee;
-            Col nee = sample_sky_direct_adj<GENERAL, PARAM>(S, s, pos, view, rng, c, err, dnee);
+            NeeDeriv dn;
+            Col nee = sample_sky_direct_adj<GENERAL, PARAM>(S, s, pos, view, rng, c, err, dn);
             radiance = radiance + nee * energy;
             x.add = s.radiance + nee;
-            x.dadd = dnee;
+            if constexpr (PARAM == ADJ_ALL) {
+                x.dadd = dn.a;
+                x.ex.dadd_r = dn.r;
+                x.ex.dadd_f = dn.f;
+            } else {
+                x.dadd = PARAM == ADJ_ALBEDO ? dn.a : (PARAM == ADJ_ROUGHNESS ? dn.r : dn.f);
+            }
             if (i >= 3) x.rr = fminf(1.0f, max_component(energy));
             if (russian_roulette(energy, i, rng)) {
                 x.kind = AV_SURF_END;
@@ -257,8 +304,10 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             x.e_rr = energy;
             Scatter sc = surface_scatter<GENERAL>(s, ray.d, view, rng);
             x.s = sc.weight;
-            if constexpr (PARAM != ADJ_FOG_DENSITY)
-                x.ds = opaque_eval_dparam<PARAM>(s, view, sc.dir) / fmaxf(sc.pdf, 1e-6f);
+            const float ipdf = 1.0f / fmaxf(sc.pdf, 1e-6f);
+            if constexpr (kAdjAlbedo<PARAM>) x.ds = opaque_eval_dalbedo(s, view, sc.dir) * ipdf;
+            if constexpr (PARAM == ADJ_ROUGHNESS) x.ds = opaque_eval_droughness(s, view, sc.dir) * ipdf;
+            if constexpr (PARAM == ADJ_ALL) x.ex.ds_r = opaque_eval_droughness(s, view, sc.dir) * ipdf;
             energy = energy * sc.weight;
             x.pre = energy;
             energy = clamp_luminance(energy, indirect_clamp);
@@ -267,10 +316,10 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
             ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
         } else {
             x.kind = AV_SKY;
-            if constexpr (PARAM == ADJ_FOG_DENSITY)  // score of passing the fog to infinity
+            if constexpr (kAdjFog<PARAM>)
                 if (S.has_fog) {
                     const float depth = fog_depth_unit(S, ray, inf);
-                    x.ds.r = isfinite(depth) ? -depth : 0.0f;  // an escape needs a finite depth
+                    set_score(x, isfinite(depth) ? -depth : 0.0f);  // an escape needs a finite depth
                 }
             float mis = has_spdf ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
             x.add = sky_radiance<false, GENERAL>(S, ray.d, c) * mis;
@@ -288,6 +337,7 @@ __device__ int replay_sample(const DevScene& S, Ray ray, Rng& rng, uint32_t boun
 // into the red channel.
 template <int PARAM>
 __device__ void scatter_texel_grad(const DevScene& S, int material, V2 uv, Col g, int tex, float* grad) {
+    if (tex < 0 || !grad) return;
     const DevMaterial& m = S.materials[material];
     if (m.tex[PARAM == ADJ_ALBEDO ? 0 : 1] != tex) return;
     const DevTexture& t = S.textures[tex];
@@ -320,10 +370,22 @@ __device__ void scatter_texel_grad(const DevScene& S, int material, V2 uv, Col g
     add(x1, y1, tx * ty);
 }
 
+// Where the gradients go: an albedo texture and its gradient, a roughness texture and its
+// gradient, the fog density's gradient (one float); texture -1 or a null pointer skips a part.
+struct AdjTargets {
+    int tex_a;
+    float* grad_a;
+    int tex_r;
+    float* grad_r;
+    float* grad_f;
+};
+
+// One thread per pixel: replay, then the reverse sweep.  Register caps: 128 for the lean
+// instantiation (8 blocks of 64 per SM), 168 for the general one.
 template <bool GENERAL, int PARAM>
-__global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, DevParams P, DevAovs fwd,
-                                                       const float* d_image, int tex, float* grad, float* replay,
-                                                       uint32_t* err) {
+__global__ void __launch_bounds__(64, GENERAL ? 6 : 8)
+    k_adjoint(DevScene S, DevView V, DevParams P, DevAovs fwd, const float* d_image, AdjTargets T, float* replay,
+              uint32_t* err) {
     const uint32_t x = blockIdx.x * 8 + (threadIdx.x & 7), y = blockIdx.y * 8 + (threadIdx.x >> 3);
     if (x >= P.width || y >= P.height) return;
     const size_t i = (size_t)y * P.width + x;
@@ -332,7 +394,7 @@ __global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, D
     const float inv = 1.0f / (float)count;
     Col G{d_image[3 * i] * inv, d_image[3 * i + 1] * inv, d_image[3 * i + 2] * inv};
     Ctr c;
-    AdjVertex v[kAdjMaxVertices];
+    AdjVertex<PARAM> v[kAdjMaxVertices];
     Rng rng = rng_seed(x, y);
     Col rad_sum = black(), fog_sum = black();
     float g_density = 0.0f;  // this pixel's d loss / d fog density
@@ -345,7 +407,7 @@ __global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, D
         // reverse sweep: a = d loss / d (throughput leaving the vertex)
         Col a = black();
         for (int k = n - 1; k >= 0; --k) {
-            const AdjVertex& q = v[k];
+            const AdjVertex<PARAM>& q = v[k];
             Col a_in;
             if (q.kind == AV_SKY) {
                 a_in = G * q.add;
@@ -353,30 +415,32 @@ __global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, D
                 // e_rr = e_in * fog colour; add * e_rr; then the roulette divides e_rr
                 Col a_rr = (q.kind == AV_FOG ? rr_adjoint(q.e_rr, q.rr, a) : black()) + G * q.add;
                 a_in = a_rr * col3(S.fog_color);
-                if constexpr (PARAM == ADJ_FOG_DENSITY) g_density += sum3(G * q.e_rr * q.dadd);
-            } else if (q.kind == AV_SURF_END) {
-                a_in = G * q.add;
-                if constexpr (PARAM == ADJ_FOG_DENSITY)
-                    g_density += sum3(G * q.e_in * q.dadd);
-                else
-                    scatter_texel_grad<PARAM>(S, q.material, q.uv, G * q.e_in * q.dadd, tex, grad);
+                if constexpr (kAdjFog<PARAM>) g_density += sum3(G * q.e_rr * dadd_fog(q));
             } else {
-                const Col a_pre = clamp_adjoint(q.pre, q.clamp_max, a);
-                const Col a_s = q.e_rr * a_pre;
-                a_in = rr_adjoint(q.e_in, q.rr, q.s * a_pre) + G * q.add;
-                if constexpr (PARAM == ADJ_FOG_DENSITY)
-                    g_density += sum3(G * q.e_in * q.dadd);
-                else
-                    scatter_texel_grad<PARAM>(S, q.material, q.uv, a_s * q.ds + G * q.e_in * q.dadd, tex, grad);
+                const Col ge = G * q.e_in;
+                Col a_s = black();  // d loss / d (scatter weight); none after a roulette end
+                if (q.kind == AV_SURF_END) {
+                    a_in = G * q.add;
+                } else {
+                    const Col a_pre = clamp_adjoint(q.pre, q.clamp_max, a);
+                    a_s = q.e_rr * a_pre;
+                    a_in = rr_adjoint(q.e_in, q.rr, q.s * a_pre) + G * q.add;
+                }
+                if constexpr (kAdjAlbedo<PARAM>)
+                    scatter_texel_grad<ADJ_ALBEDO>(S, q.material, q.uv, a_s * q.ds + ge * q.dadd, T.tex_a, T.grad_a);
+                if constexpr (kAdjRough<PARAM>)
+                    scatter_texel_grad<ADJ_ROUGHNESS>(S, q.material, q.uv, a_s * ds_rough(q) + ge * dadd_rough(q),
+                                                      T.tex_r, T.grad_r);
+                if constexpr (kAdjFog<PARAM>) g_density += sum3(ge * dadd_fog(q));
             }
             // the segment into the vertex scales e_in by its sampling weight, whose derivative is
             // the weight times the score
-            if constexpr (PARAM == ADJ_FOG_DENSITY) g_density += q.ds.r * sum3(a_in * q.e_in);
+            if constexpr (kAdjFog<PARAM>) g_density += score_of(q) * sum3(a_in * q.e_in);
             a = a_in;
         }
     }
-    if constexpr (PARAM == ADJ_FOG_DENSITY)
-        if (g_density != 0.0f) atomicAdd(grad, g_density);
+    if constexpr (kAdjFog<PARAM>)
+        if (T.grad_f && g_density != 0.0f) atomicAdd(T.grad_f, g_density);
     if (replay) {
         const Col r = rad_sum / (float)count, f = fog_sum / (float)count;
         replay[3 * i] = r.r + f.r;
@@ -385,29 +449,25 @@ __global__ void __launch_bounds__(64) k_adjoint_texture(DevScene S, DevView V, D
     }
 }
 
-cudaError_t launch_adjoint_texture(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
-                                   const float* d_image, int texture, int parameter, float* grad, float* replay,
-                                   uint32_t* err, cudaStream_t stream) {
+cudaError_t launch_adjoint(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
+                           const float* d_image, int parameter, int tex_a, float* grad_a, int tex_r, float* grad_r,
+                           float* grad_f, float* replay, uint32_t* err, cudaStream_t stream) {
     dim3 grid((P.width + 7) / 8, (P.height + 7) / 8);
+    const AdjTargets T{tex_a, grad_a, tex_r, grad_r, grad_f};
     // scenes of meshes under a texture sky without transparency or normal maps take the lean
     // instantiation, as the wavefront kernels do (same results, far less code)
-#define SR_ADJ_LAUNCH(G, PR) \
-    k_adjoint_texture<G, PR><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, texture, grad, replay, err)
-    if (parameter == ADJ_ALBEDO) {
-        if (S.general)
-            SR_ADJ_LAUNCH(true, ADJ_ALBEDO);
-        else
-            SR_ADJ_LAUNCH(false, ADJ_ALBEDO);
-    } else if (parameter == ADJ_ROUGHNESS) {
-        if (S.general)
-            SR_ADJ_LAUNCH(true, ADJ_ROUGHNESS);
-        else
-            SR_ADJ_LAUNCH(false, ADJ_ROUGHNESS);
-    } else {
-        if (S.general)
-            SR_ADJ_LAUNCH(true, ADJ_FOG_DENSITY);
-        else
-            SR_ADJ_LAUNCH(false, ADJ_FOG_DENSITY);
+#define SR_ADJ_LAUNCH(PR)                                                                           \
+    do {                                                                                            \
+        if (S.general)                                                                              \
+            k_adjoint<true, PR><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, T, replay, err);    \
+        else                                                                                        \
+            k_adjoint<false, PR><<<grid, 64, 0, stream>>>(S, V, P, fwd, d_image, T, replay, err);   \
+    } while (0)
+    switch (parameter) {
+    case ADJ_ALBEDO: SR_ADJ_LAUNCH(ADJ_ALBEDO); break;
+    case ADJ_ROUGHNESS: SR_ADJ_LAUNCH(ADJ_ROUGHNESS); break;
+    case ADJ_FOG_DENSITY: SR_ADJ_LAUNCH(ADJ_FOG_DENSITY); break;
+    default: SR_ADJ_LAUNCH(ADJ_ALL); break;
     }
 #undef SR_ADJ_LAUNCH
     return cudaGetLastError();

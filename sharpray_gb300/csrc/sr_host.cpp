@@ -1773,31 +1773,66 @@ SR_API int sr_image_save(const char* path, uint32_t w, uint32_t h, const uint8_t
     return SR_OK;
 }
 
-SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
-                              const float* d_image, int32_t texture, int32_t parameter, float* grad, float* replay,
-                              void* stream) {
-    if (!s || !fwd || !d_image || !grad) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+// Checks shared by the adjoint entry points; dv / dp / st out.
+static int adjoint_prepare(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
+                           const float* d_image, void* stream, DevView& dv, DevParams& dp, cudaStream_t& st) {
+    if (!s || !fwd || !d_image) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     if (int rc = need_device(s)) return rc;
     if (!fwd->radiance || !fwd->radiance_fog || !fwd->samples)
         return fail(SR_ERR_INVALID_ARG, "the adjoint needs the forward radiance, radiance_fog and samples planes");
-    if (parameter != SR_ADJOINT_ALBEDO && parameter != SR_ADJOINT_ROUGHNESS && parameter != SR_ADJOINT_FOG_DENSITY)
-        return fail(SR_ERR_INVALID_ARG, "unknown adjoint parameter %d", parameter);
-    if (parameter == SR_ADJOINT_FOG_DENSITY) {
-        if (!s->dev.has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
-        texture = -1;
-    } else if (texture < 0 || (size_t)texture >= s->tex_offset.size()) {
-        return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
-    }
     if (s->dev.has_transparent) return fail(SR_ERR_STATE, "the adjoint does not support transparent materials");
-    DevView dv;
-    DevParams dp;
     if (int rc = make_view(view, params, dv, dp)) return rc;
     if (dp.bounces > 16) return fail(SR_ERR_INVALID_ARG, "the adjoint supports at most 16 bounces");
     SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
-    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    return SR_OK;
+}
+
+static bool scene_texture(SrScene* s, int32_t texture) {
+    return texture >= 0 && (size_t)texture < s->tex_offset.size();
+}
+
+SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
+                              const float* d_image, int32_t texture, int32_t parameter, float* grad, float* replay,
+                              void* stream) {
+    if (!grad) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (parameter != SR_ADJOINT_ALBEDO && parameter != SR_ADJOINT_ROUGHNESS && parameter != SR_ADJOINT_FOG_DENSITY)
+        return fail(SR_ERR_INVALID_ARG, "unknown adjoint parameter %d", parameter);
+    DevView dv;
+    DevParams dp;
+    cudaStream_t st;
+    if (int rc = adjoint_prepare(s, view, params, fwd, d_image, stream, dv, dp, st)) return rc;
+    if (parameter == SR_ADJOINT_FOG_DENSITY) {
+        if (!s->dev.has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
+    } else if (!scene_texture(s, texture)) {
+        return fail(SR_ERR_INVALID_ARG, "texture %d is not part of the scene", texture);
+    }
     DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
-    SR_CUDA(launch_adjoint_texture(s->dev, dv, dp, f, d_image, texture, parameter, grad, replay,
-                                   s->err.as<uint32_t>(), st),
+    const bool a = parameter == SR_ADJOINT_ALBEDO, r = parameter == SR_ADJOINT_ROUGHNESS;
+    SR_CUDA(launch_adjoint(s->dev, dv, dp, f, d_image, parameter, a ? texture : -1, a ? grad : nullptr,
+                           r ? texture : -1, r ? grad : nullptr, a || r ? nullptr : grad, replay,
+                           s->err.as<uint32_t>(), st),
+            "adjoint launch");
+    return SR_OK;
+}
+
+SR_API int sr_adjoint_all(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
+                          const float* d_image, int32_t albedo_texture, float* albedo_grad, int32_t roughness_texture,
+                          float* roughness_grad, float* fog_density_grad, float* replay, void* stream) {
+    DevView dv;
+    DevParams dp;
+    cudaStream_t st;
+    if (int rc = adjoint_prepare(s, view, params, fwd, d_image, stream, dv, dp, st)) return rc;
+    if (albedo_grad && !scene_texture(s, albedo_texture))
+        return fail(SR_ERR_INVALID_ARG, "albedo texture %d is not part of the scene", albedo_texture);
+    if (roughness_grad && !scene_texture(s, roughness_texture))
+        return fail(SR_ERR_INVALID_ARG, "roughness texture %d is not part of the scene", roughness_texture);
+    if (fog_density_grad && !s->dev.has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
+    if (!albedo_grad && !roughness_grad && !fog_density_grad) return SR_OK;
+    DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
+    SR_CUDA(launch_adjoint(s->dev, dv, dp, f, d_image, 3, albedo_grad ? albedo_texture : -1, albedo_grad,
+                           roughness_grad ? roughness_texture : -1, roughness_grad, fog_density_grad, replay,
+                           s->err.as<uint32_t>(), st),
             "adjoint launch");
     return SR_OK;
 }

@@ -24,13 +24,14 @@ cudaError_t launch_render(const DevScene& S, const DevView& V, const DevParams& 
 // Sky table of a texture sky (DevSky::center), `texels` = width x height (sr_render.cu).
 cudaError_t launch_sky_table(const DevScene& S, float4* out, uint32_t texels, cudaStream_t stream);
 
-// Path-replay adjoint: dL/d(texels of texture `texture`, as the albedo (parameter 0) or roughness
-// (parameter 1) lookup) for dL/dI = d_image (width x height x 3, I = radiance + radiance_fog),
-// added into grad (texture width x height x 3); replay (optional) gets the re-rendered image
-// (sr_adjoint.cu).
-cudaError_t launch_adjoint_texture(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
-                                   const float* d_image, int texture, int parameter, float* grad, float* replay,
-                                   uint32_t* err, cudaStream_t stream);
+// Path-replay adjoint (sr_adjoint.cu) for dL/dI = d_image (width x height x 3, I = radiance +
+// radiance_fog): parameter 0 adds dL/d(texels of albedo texture tex_a) into grad_a, 1 dL/d(texels
+// of roughness texture tex_r) into grad_r (channel 0), 2 dL/d(fog density) into grad_f[0], 3 all
+// three from one replay (a -1 texture or null gradient skips a part); replay (optional) gets the
+// re-rendered image.
+cudaError_t launch_adjoint(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& fwd,
+                           const float* d_image, int parameter, int tex_a, float* grad_a, int tex_r, float* grad_r,
+                           float* grad_f, float* replay, uint32_t* err, cudaStream_t stream);
 // rgb float triples -> texel records (sr_adjoint.cu).
 cudaError_t launch_texels_from_rgb(const float* rgb, float4* out, size_t n, cudaStream_t stream);
 

@@ -474,6 +474,33 @@ def config_c4(width: int = 512, height: int = 512, spp: int = 16, rings: int = 3
     return d
 
 
+def config_c5(width: int = 768, height: int = 768, spp: int = 32, rings: int = 500, tex: int = 1024,
+              seed: int = 5) -> SceneDesc:
+    """Batched + differentiable workload, one view of it: 768x768, 32 spp, depth 8; fBm sphere
+    (CreateSphere topology 500x500 = 500,000 triangles) with 1024x1024 albedo (value noise in
+    [0.1, 0.9]) and roughness (value noise in [0.05, 1]) textures, metallic 0; near-homogeneous fog
+    (density 0.03, falloff 0.01); 1024x512 HDR env; seed 5.  Texture 1 is the albedo, texture 2 the
+    roughness; the other views orbit the sphere (bench.py)."""
+    pos, uv = uv_sphere(rings, rings, amplitude=0.1, seed=seed)
+    d = SceneDesc(f"c5_differentiable_{width}x{height}_{spp}spp")
+    d.meshes = [MeshDesc(pos, uv)]
+    rough = value_noise_float(tex, seed + 50, 0.05, 1.0, channels=1)
+    d.textures = [TextureDesc(_rgbe_texels(sky_env(1024, 512, seed=seed, sun_peak=100.0, sun_sigma_deg=3.0,
+                                                   lognormal_sigma=0.5))),
+                  TextureDesc(value_noise_float(tex, seed, 0.1, 0.9)),
+                  TextureDesc(np.repeat(rough, 3, axis=2))]
+    d.sky = ("texture", 0, 1.0, 0.0)
+    d.objects = [ObjectDesc("sphere", Transform(), {"albedo": (1.0, 1.0, 1.0), "roughness": 1.0, "metallic": 0.0,
+                                                    "color_texture": 1, "roughness_texture": 2}, ("mesh", 0))]
+    d.fog = Fog(0.03, (0.8, 0.75, 0.6), 0.6, 0.01)
+    cam = (0.0, 0.4, -2.9)
+    d.view = View(Transform(cam, look_rotation(cam, (0.0, 0.0, 0.0))), math.radians(50.0), 0.1)
+    d.width, d.height, d.spp, d.bounces = width, height, spp, 8
+    d.min_samples = spp
+    d.variance_threshold = 0.0
+    return d
+
+
 def config_features(width: int = 48, height: int = 40, spp: int = 8, seed: int = 5) -> SceneDesc:
     """Small scene touching every shading branch: textured/normal-mapped/point-filtered materials,
     transparent (refractive) sphere, metal box, emissive object, instanced transformed mesh, fog."""

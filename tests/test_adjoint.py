@@ -328,3 +328,40 @@ def test_fog_density_adjoint_matches_finite_differences_in_expectation(torch_mod
                         _abi.SR_ADJOINT_FOG_DENSITY)
     with pytest.raises(SharpRayError):
         nofog.scene.update_fog_density(0.1)
+
+
+def test_adjoint_all_equals_separate_passes(torch_mod):
+    """sr_adjoint_all (one replay) gives the albedo, roughness and fog-density gradients of the three
+    single-parameter passes (up to the order of the atomic additions)."""
+    import ctypes as C
+    torch = torch_mod
+    d = roughness_scene(8)
+    d.fog = Fog(0.08, (0.8, 0.75, 0.7), 0.5, 0.2)
+    rig = Rig(torch, d)
+    rig.image()
+    w = torch.from_numpy(np.random.default_rng(6).uniform(-1.0, 1.0, d.width * d.height * 3)
+                         .astype(np.float32)).cuda()
+    ta, tr = rig.tex[1], rig.tex[3]
+    sep = [torch.zeros(ta.height * ta.width * 3, device="cuda"), torch.zeros(tr.height * tr.width * 3, device="cuda"),
+           torch.zeros(1, device="cuda")]
+    st = current_stream_handle()
+    for g, tex, kind in zip(sep, (ta, tr, None), (_abi.SR_ADJOINT_ALBEDO, _abi.SR_ADJOINT_ROUGHNESS,
+                                                   _abi.SR_ADJOINT_FOG_DENSITY)):
+        adjoint_texture(rig.scene, d.view, rig.params, rig.aovs, w.data_ptr(), tex, g.data_ptr(), kind, None, st)
+    both = [torch.zeros_like(g) for g in sep]
+    v = d.view.to_c()
+    _abi.check(rig.ctx._lib.sr_adjoint_all(rig.scene.handle, C.byref(v), C.byref(rig.params), C.byref(rig.aovs),
+                                           C.c_void_p(w.data_ptr()), ta.id, C.c_void_p(both[0].data_ptr()), tr.id,
+                                           C.c_void_p(both[1].data_ptr()), C.c_void_p(both[2].data_ptr()), None,
+                                           C.c_void_p(st)))
+    torch.cuda.synchronize()
+    for a, b in zip(sep, both):
+        assert float(a.abs().max()) > 0.0
+        assert torch.allclose(a, b, rtol=1e-4, atol=1e-5 * float(a.abs().max())), float((a - b).abs().max())
+    # a null gradient skips its part; a fog gradient needs fog
+    only = torch.zeros_like(sep[1])
+    _abi.check(rig.ctx._lib.sr_adjoint_all(rig.scene.handle, C.byref(v), C.byref(rig.params), C.byref(rig.aovs),
+                                           C.c_void_p(w.data_ptr()), -1, None, tr.id, C.c_void_p(only.data_ptr()),
+                                           None, None, C.c_void_p(st)))
+    torch.cuda.synchronize()
+    assert torch.allclose(only, sep[1], rtol=1e-4, atol=1e-5 * float(sep[1].abs().max()))
