@@ -43,3 +43,25 @@ def test_progress_during_async_render(mode):
     host = Aovs(d.width, d.height)
     _abi.check(ctx._lib.sr_render(sc.handle, C.byref(v), C.byref(p), C.byref(host.to_c())))
     assert sc.progress() == (total, total)
+
+
+def test_progress_of_batched_renders():
+    """Each scene of an sr_render_batch launch reports its own progress, finished after the graph."""
+    torch = pytest.importorskip("torch")
+    from sharpray_gb300 import render_batch
+    from sharpray_gb300.autograd import current_stream_handle, device_aovs
+    ctx = Context(0)
+    descs = [synth.config_c1(40, 24, 4), synth.config_procedural(24, 20, 3)]
+    scenes, outs, keep = [], [], []
+    for d in descs:
+        sc = d.instantiate(ctx)
+        sc.build()
+        bufs, a = device_aovs(d.width, d.height)
+        scenes.append(sc)
+        outs.append(a)
+        keep.append(bufs)
+    render_batch(scenes, [d.view for d in descs], [render_params(*d.render_args()) for d in descs], outs,
+                 stream=current_stream_handle())
+    torch.cuda.synchronize()
+    for sc, d in zip(scenes, descs):
+        assert sc.progress() == (d.width * d.height, d.width * d.height)
