@@ -997,8 +997,48 @@ __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* cou
 }
 
 // ---- launchers ------------------------------------------------------------------------------------
+// The trace queue of parity cur reordered in place by ray-direction octant (sign bits of d) within
+// each chunk of 256 entries, keeping the producer order inside an octant, so that the lanes of a
+// traversal warp take rays heading the same way.  Results are per slot, so the order of the queue
+// does not change them.
+__global__ void __launch_bounds__(256) k_trace_octant_sort(WaveState W, int cur) {
+    __shared__ uint32_t wcount[8][8];  // [warp][octant]
+    __shared__ uint32_t base[8][8];
+    const uint32_t len = W.counts[kCountTrace + cur];
+    const uint32_t start = blockIdx.x * 256u;
+    if (start >= len) return;  // uniform over the block
+    const uint32_t i = start + threadIdx.x;
+    const bool valid = i < len;
+    Rec e;
+    int oct = 8;  // none
+    if (valid) {
+        e = ld_rec(&W.q_trace[cur][i]);
+        oct = (e.b.x < 0.0f ? 1 : 0) | (e.b.y < 0.0f ? 2 : 0) | (e.b.z < 0.0f ? 4 : 0);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    uint32_t rank = 0;
+    for (int o = 0; o < 8; ++o) {
+        const unsigned m = __ballot_sync(0xffffffffu, oct == o);
+        if (oct == o) rank = __popc(m & below);
+        if (lane == 0) wcount[warp][o] = __popc(m);
+    }
+    __syncthreads();  // every entry of the chunk is in registers before any is written back
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int o = 0; o < 8; ++o)
+            for (int w = 0; w < 8; ++w) {
+                base[w][o] = acc;
+                acc += wcount[w][o];
+            }
+    }
+    __syncthreads();
+    if (valid) st_rec(&W.q_trace[cur][start + base[warp][oct] + rank], e);
+}
+
 template <bool COUNT, bool GENERAL>
 static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st) {
+    if (SR_TRACE_OCTANT_SORT) k_trace_octant_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W, cur);
     const bool loop_shadows = GENERAL && L.S.has_transparent;
     if (loop_shadows) {
         k_wave_trace<COUNT, GENERAL, false><<<L.grid_trace, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);

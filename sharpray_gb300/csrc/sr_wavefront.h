@@ -129,7 +129,13 @@ struct WaveGroups {
 #ifndef SR_SPLIT_SHADE
 #define SR_SPLIT_SHADE 1
 #endif
-constexpr int kWaveKernelsPerBounce = (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 1 : 0);
+// Trace queue reordered by ray-direction octant within chunks of 256 entries before each traversal
+// (1) or left in producer order (0).
+#ifndef SR_TRACE_OCTANT_SORT
+#define SR_TRACE_OCTANT_SORT 0
+#endif
+constexpr int kWaveKernelsPerBounce =
+    (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 1 : 0) + (SR_TRACE_OCTANT_SORT ? 1 : 0);
 
 // Launch geometry chosen at run time (0 = the default: as many blocks per SM as fit).
 struct WaveTune {
