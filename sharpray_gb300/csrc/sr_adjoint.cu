@@ -1,6 +1,7 @@
 // sr_adjoint.cu — path-replay adjoint of a rendered image with respect to the texels of an albedo
-// (colour) or roughness texture: given dL/dI for the image I = radiance + radiance_fog of a render,
-// the gradient dL/d(texels).  No counterpart in the reference (it has no derivatives).
+// (colour) or roughness texture and the fog density: given dL/dI for the image I = radiance +
+// radiance_fog of a render, the gradients dL/d(texels) and dL/d(density), one parameter per launch
+// or all three from one replay.  No counterpart in the reference (it has no derivatives).
 //
 // One thread per pixel replays the pixel's samples exactly as the per-pixel path loop renders
 // them (the same RNG stream and the same functions, so the same paths and the same radiance --
@@ -18,8 +19,10 @@
 // For the albedo of non-metallic surfaces none of these depends on the parameter, so the gradient
 // is the exact derivative of the renderer's own estimator at fixed random numbers wherever no
 // roulette decision or clamp threshold is crossed.  The roughness moves the sampled specular
-// directions, so there the gradient is exact in expectation (d/dθ of the expected image) rather
-// than per sample.  Scenes with transparent materials are refused by the host entry point.
+// directions and the density the sampled scatter distances, so there the gradient is exact in
+// expectation (d/dθ of the expected image) rather than per sample; for the density it carries the
+// score terms of the free-flight sampling.  Scenes with transparent materials are refused by the
+// host entry point.
 #include <cuda_runtime.h>
 
 #include <type_traits>
