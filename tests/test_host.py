@@ -142,3 +142,32 @@ def test_context_outlived_by_scene(native_lib):
     _abi.check(native_lib.sr_scene_create(ctx, C.byref(sc)))
     _abi.check(native_lib.sr_ctx_destroy(ctx))
     _abi.check(native_lib.sr_scene_destroy(sc))
+
+
+def test_progress_adjoint_and_update_validation(host_ctx):
+    """Argument and state checks of the progress, adjoint, texture/fog update and float-compose entry
+    points (none reaches the GPU)."""
+    import ctypes as C
+
+    from sharpray_gb300 import Scene, SharpRayError, StateError, _abi
+    lib = host_ctx._lib
+    s = Scene(host_ctx)
+    assert s.progress() == (0, 0)  # nothing launched
+    d, t = C.c_uint32(), C.c_uint32()
+    with pytest.raises(SharpRayError):
+        _abi.check(lib.sr_render_progress(s.handle, None, C.byref(t)))
+    with pytest.raises(StateError):  # not built
+        s.update_fog_density(0.1)
+    with pytest.raises(StateError):
+        s.update_texture(0, np.zeros((1, 1, 3), np.float32))
+    v, p, a = _abi.SrView(), _abi.SrRenderParams(), _abi.SrAovs()
+    g = (C.c_float * 3)()
+    for call in (lambda: lib.sr_adjoint_texture(s.handle, C.byref(v), C.byref(p), C.byref(a), g, 0, 0, g, None, None),
+                 lambda: lib.sr_adjoint_all(s.handle, C.byref(v), C.byref(p), C.byref(a), g, 0, g, -1, None, None,
+                                            None, None),
+                 lambda: lib.sr_adjoint_texture(s.handle, C.byref(v), C.byref(p), None, g, 0, 0, g, None, None),
+                 lambda: lib.sr_adjoint_texture(s.handle, C.byref(v), C.byref(p), C.byref(a), g, 0, 7, g, None,
+                                                None),
+                 lambda: lib.sr_compose_float_device(host_ctx.handle, C.byref(a), 4, 4, None, None, None, None)):
+        with pytest.raises(SharpRayError):
+            _abi.check(call())
