@@ -28,10 +28,13 @@ PLANES = (("radiance", 3, "float32"), ("radiance_fog", 3, "float32"), ("normals"
           ("depth", 1, "float32"), ("samples", 1, "int32"), ("variance", 1, "float32"))
 
 
-def adjoint_scene(fog: bool, bounces: int, clamp: float, w=40, h=30, spp=3, general: bool = False) -> SceneDesc:
+def adjoint_scene(fog: bool, bounces: int, clamp: float, w=40, h=30, spp=3, general: bool = False,
+                  metal: bool = False) -> SceneDesc:
     """Textured ground and blob sharing one bilinear albedo texture (different material albedos,
     tiling 2 on the blob), a point-filtered texture on a second blob, an untextured rock; `general`
-    adds an analytic sphere with the bilinear texture (the kernels' general instantiation)."""
+    adds an analytic sphere with the bilinear texture (the kernels' general instantiation); `metal`
+    makes the textured blob fully metallic (its albedo then enters through the Fresnel base; the
+    lobe probability clamps to a constant, so sampling still does not depend on the albedo)."""
     rng = np.random.default_rng(7)
     gpos, guv = synth.ground_quad(3.0, -1.0)
     bpos, buv = synth.uv_sphere(10, 14, amplitude=0.1, seed=2)
@@ -52,6 +55,8 @@ def adjoint_scene(fog: bool, bounces: int, clamp: float, w=40, h=30, spp=3, gene
         ObjectDesc("rock", Transform((0.2, -0.7, -0.6), Quat.identity(), (0.3, 0.3, 0.3)),
                    {"albedo": (0.5, 0.5, 0.45), "roughness": 0.6}, ("mesh", 2)),
     ]
+    if metal:
+        d.objects[1].material["metallic"] = 1.0
     if general:
         d.objects.append(ObjectDesc("ball", Transform(), {"albedo": (0.7, 0.9, 0.8), "roughness": 0.5,
                                                           "color_texture": 1}, ("sphere", (0.6, -0.75, -0.3), 0.25)))
@@ -145,12 +150,14 @@ def torch_mod():
     return pytest.importorskip("torch")
 
 
-@pytest.mark.parametrize("fog,clamp,general", [(False, 10.0, False), (True, 10.0, False), (False, 0.6, False),
-                                               (True, 10.0, True)])
-def test_adjoint_matches_finite_differences_two_bounces(torch_mod, fog, clamp, general):
+@pytest.mark.parametrize("fog,clamp,general,metal", [(False, 10.0, False, False), (True, 10.0, False, False),
+                                                     (False, 0.6, False, False), (True, 10.0, True, False),
+                                                     (False, 10.0, False, True)])
+def test_adjoint_matches_finite_differences_two_bounces(torch_mod, fog, clamp, general, metal):
     """Two bounces: no roulette; the clamp case exercises the clamp's Jacobian; `general` runs the
-    kernels' general instantiation (an analytic sphere in the scene)."""
-    rig = Rig(torch_mod, adjoint_scene(fog, 2, clamp, general=general))
+    kernels' general instantiation (an analytic sphere in the scene); `metal` the Fresnel-base
+    derivative."""
+    rig = Rig(torch_mod, adjoint_scene(fog, 2, clamp, general=general, metal=metal))
     check_against_fd(rig, 1, picks=10, seed=1, eps=1e-2, min_checked=10)
     check_against_fd(rig, 2, picks=6, seed=2, eps=1e-2, min_checked=6)
 
