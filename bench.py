@@ -64,6 +64,9 @@ def parse():
                     help="Adam steps of the inverse-rendering run (0: skip)")
     ap.add_argument("--c5-steps", type=int, default=0,
                     help="--adjoint-only: also time this many steps of the 16-view 768x768 differentiable workload")
+    ap.add_argument("--joint-steps", type=int, default=0,
+                    help="--adjoint-only: Adam steps recovering albedo, roughness and fog density jointly on a small "
+                         "version of the 16-view workload")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the adjoint workload (--steps timed passes, --adjoint-checks FD checks)")
     ap.add_argument("--profile-once", action="store_true",
@@ -422,13 +425,15 @@ def measure_inverse(steps: int, views: int = 4, size: int = 256, spp: int = 8) -
                     "wrapper; targets share the renderer's per-pixel random numbers"}
 
 
-def measure_inverse_c5(steps: int, views: int = 16) -> dict:
+def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 32, rings: int = 500,
+                       tex: int = 1024, lr_tex: float = 0.02, lr_density: float = 0.002) -> dict:
     """The batched + differentiable configuration (synth.config_c5: 16 orbit views, 768x768, 32 spp,
-    depth 8, 500,000 triangles, 1024x1024 albedo + roughness textures, fog): per step every view is
-    rendered and its image gradient replayed once for the albedo texture, the roughness texture and
-    the fog density together (sr_adjoint_all), then one Adam step updates all three (from flat grey
-    textures and 1.5x the density).
-    Reports the time per step after one warm-up step; `steps` timed steps."""
+    depth 8, 500,000 triangles, 1024x1024 albedo + roughness textures, fog; smaller with the
+    arguments): per step every view is rendered and its image gradient replayed once for the albedo
+    texture, the roughness texture and the fog density together (sr_adjoint_all), then one Adam step
+    updates all three (from flat grey textures and 1.5x the density).  Reports the time per step
+    after one warm-up step over `steps` timed steps, and the texture errors (albedo rgb, roughness
+    channel 0, on the texels the views see) before and after."""
     import ctypes as C
 
     import numpy as np
@@ -436,7 +441,7 @@ def measure_inverse_c5(steps: int, views: int = 16) -> dict:
     from sharpray_gb300 import Context, Transform, View, _abi, render_params, synth
     from sharpray_gb300.autograd import device_aovs
     t_setup = time.perf_counter()
-    d = synth.config_c5()
+    d = synth.config_c5(size, size, spp, rings=rings, tex=tex)
     ctx = Context(0)
     ctx.set_bvh_build(_abi.SR_BVH_BUILD_DEVICE)
     sc = d.instantiate(ctx)
@@ -465,7 +470,7 @@ def measure_inverse_c5(steps: int, views: int = 16) -> dict:
         xa = torch.full_like(truth_a, 0.5).requires_grad_(True)
         xr = torch.full_like(truth_r, 0.5).requires_grad_(True)
         xs = torch.tensor([1.5 * sigma], device="cuda", requires_grad=True)
-        opt = torch.optim.Adam([{"params": [xa, xr], "lr": 0.02}, {"params": [xs], "lr": 0.002}])
+        opt = torch.optim.Adam([{"params": [xa, xr], "lr": lr_tex}, {"params": [xs], "lr": lr_density}])
         losses = []
 
         def step():
@@ -493,6 +498,14 @@ def measure_inverse_c5(steps: int, views: int = 16) -> dict:
 
         step()  # warm-up
         st.synchronize()
+        # well-observed texels: first-step gradient at least 5 % of the 99th percentile (texels seen
+        # only at grazing angles or through reflections get weak, noisy gradients)
+        ga0, gr0 = xa.grad.abs().sum(dim=2), xr.grad[..., 0].abs()
+        seen_a = ga0 >= 0.05 * torch.quantile(ga0[ga0 > 0], 0.99)
+        seen_r = gr0 >= 0.05 * torch.quantile(gr0[gr0 > 0], 0.99)
+        rmse = lambda x, t, m: float(((x.detach() - t)[m] ** 2).mean()) ** 0.5
+        rmse_start = (rmse(torch.full_like(truth_a, 0.5), truth_a, seen_a),
+                      rmse(torch.full_like(truth_r, 0.5)[..., 0], truth_r[..., 0], seen_r))
         setup_s = time.perf_counter() - t_setup
         t0 = time.perf_counter()
         for _ in range(steps):
@@ -502,10 +515,13 @@ def measure_inverse_c5(steps: int, views: int = 16) -> dict:
     n_grads = truth_a.numel() + truth_r.shape[0] * truth_r.shape[1] + 1
     samples = views * d.width * d.height * d.spp
     return {"workload": f"{views} orbit views {d.width}x{d.height}, {d.spp} spp, depth 8, "
-                        f"{d.triangle_count} triangles, 1024x1024 albedo + roughness textures, fog 0.03",
+                        f"{d.triangle_count} triangles, {tex}x{tex} albedo + roughness textures, fog 0.03",
             "timed_steps": steps, "ms_per_step": 1000 * dt, "texel_grads_per_s": n_grads / dt,
             "path_samples_per_s": samples * 2 / dt, "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
             "fog_density": {"true": sigma, "start": 1.5 * sigma, "after": float(xs.detach())},
+            "albedo_rmse": {"start": rmse_start[0], "after": rmse(xa, truth_a, seen_a), "texels": int(seen_a.sum())},
+            "roughness_rmse": {"start": rmse_start[1], "after": rmse(xr[..., 0], truth_r[..., 0], seen_r),
+                               "texels": int(seen_r.sum())},
             "setup_s": round(setup_s, 1),
             "note": "per step: each view rendered once (wavefront graph) and replayed once for all three "
                     "gradients (sr_adjoint_all); path_samples_per_s counts both passes"}
@@ -783,6 +799,9 @@ def main():
             adj["inverse_rendering"] = measure_inverse(args.inverse_steps)
         if args.c5_steps > 0:
             adj["batched_differentiable"] = measure_inverse_c5(args.c5_steps)
+        if args.joint_steps > 0:  # the same pipeline small enough to run to convergence
+            adj["joint_recovery"] = measure_inverse_c5(args.joint_steps, views=4, size=192, spp=8, rings=150,
+                                                       tex=128, lr_tex=0.005, lr_density=0.001)
         print(json.dumps({"adjoint": adj}), flush=True)
     else:
         run_ours(args)
