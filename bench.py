@@ -426,14 +426,18 @@ def measure_inverse(steps: int, views: int = 4, size: int = 256, spp: int = 8) -
 
 
 def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 32, rings: int = 500,
-                       tex: int = 1024, lr_tex: float = 0.02, lr_density: float = 0.002) -> dict:
+                       tex: int = 1024, lr_tex: float = 0.02, lr_density: float = 0.002,
+                       target_spp_factor: int = 4) -> dict:
     """The batched + differentiable configuration (synth.config_c5: 16 orbit views, 768x768, 32 spp,
     depth 8, 500,000 triangles, 1024x1024 albedo + roughness textures, fog; smaller with the
     arguments): per step every view is rendered and its image gradient replayed once for the albedo
     texture, the roughness texture and the fog density together (sr_adjoint_all), then one Adam step
-    updates all three (from flat grey textures and 1.5x the density).  Reports the time per step
-    after one warm-up step over `steps` timed steps, and the texture errors (albedo rgb, roughness
-    channel 0, on the texels the views see) before and after."""
+    updates all three (from flat grey textures and 1.5x the density).  The targets are rendered
+    once at target_spp_factor x spp; every step renders with a fresh random-number stream and
+    replays with another (sr_scene_set_seed), so that dL/dI and dI/dθ come from independent samples
+    and the gradient is an unbiased estimate for the expected image.
+    Reports the time per step after one warm-up step over `steps` timed steps, and the texture errors
+    (albedo rgb, roughness channel 0, on the well-observed texels) before and after."""
     import ctypes as C
 
     import numpy as np
@@ -466,7 +470,12 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
                                             C.c_void_p(st.cuda_stream)))
             return bufs["radiance"] + bufs["radiance_fog"]
 
-        targets = [render(v).clone() for v in cams]
+        p_step = p
+        p = render_params(d.width, d.height, d.block_size, spp * target_spp_factor, spp * target_spp_factor,
+                          d.variance_threshold, d.bounces, d.indirect_clamp)
+        targets = [render(v).clone() for v in cams]  # reference stream (seed 0), more samples
+        p = p_step
+        seed = [0]
         xa = torch.full_like(truth_a, 0.5).requires_grad_(True)
         xr = torch.full_like(truth_r, 0.5).requires_grad_(True)
         xs = torch.tensor([1.5 * sigma], device="cuda", requires_grad=True)
@@ -474,16 +483,19 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
         losses = []
 
         def step():
+            seed[0] += 2
             sc.update_texture_device(tex_a, xa.detach().data_ptr(), st.cuda_stream)
             sc.update_texture_device(tex_r, xr.detach().data_ptr(), st.cuda_stream)
             sc.update_fog_density(float(xs.detach()))
             ga, gr, gs = torch.zeros_like(xa), torch.zeros_like(xr), torch.zeros_like(xs)
             loss = torch.zeros((), dtype=torch.float64, device="cuda")
             for v, t in zip(cams, targets):
+                sc.set_seed(seed[0])  # the image and dL/dI from one stream ...
                 img = render(v)
                 diff = img - t
                 loss += (diff.double() ** 2).sum()
                 d_img = 2.0 * diff
+                sc.set_seed(seed[0] + 1)  # ... the replay from another (every pixel takes spp samples)
                 _abi.check(lib.sr_adjoint_all(sc.handle, C.byref(v), C.byref(p), C.byref(aovs),
                                               C.c_void_p(d_img.data_ptr()), tex_a.id, C.c_void_p(ga.data_ptr()),
                                               tex_r.id, C.c_void_p(gr.data_ptr()), C.c_void_p(gs.data_ptr()), None,
@@ -523,8 +535,9 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
             "roughness_rmse": {"start": rmse_start[1], "after": rmse(xr[..., 0], truth_r[..., 0], seen_r),
                                "texels": int(seen_r.sum())},
             "setup_s": round(setup_s, 1),
-            "note": "per step: each view rendered once (wavefront graph) and replayed once for all three "
-                    "gradients (sr_adjoint_all); path_samples_per_s counts both passes"}
+            "note": "per step: each view rendered once (wavefront graph, a fresh random-number stream) and "
+                    "replayed once for all three gradients (sr_adjoint_all, an independent stream); "
+                    "path_samples_per_s counts both passes; targets at %dx the spp" % target_spp_factor}
 
 
 def run_reference(args):
@@ -801,7 +814,7 @@ def main():
             adj["batched_differentiable"] = measure_inverse_c5(args.c5_steps)
         if args.joint_steps > 0:  # the same pipeline small enough to run to convergence
             adj["joint_recovery"] = measure_inverse_c5(args.joint_steps, views=4, size=192, spp=8, rings=150,
-                                                       tex=128, lr_tex=0.005, lr_density=0.001)
+                                                       tex=128, lr_tex=0.005, lr_density=0.001, target_spp_factor=8)
         print(json.dumps({"adjoint": adj}), flush=True)
     else:
         run_ours(args)

@@ -342,6 +342,12 @@ SR_API int sr_render_progress(SrScene* scene, uint32_t* done, uint32_t* total);
 SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const SrRenderParams* params,
                            const SrAovs* device_outs, uint32_t count, void* stream);
 
+/* Random-number stream of the scene's renders and adjoints (an extension; the reference seeds
+ * Rng(x, y) per pixel): 0, the default, is the reference's stream; any other value gives every
+ * pixel an independent stream, e.g. fresh samples for each step of stochastic inverse rendering or
+ * for progressive accumulation.  An adjoint replays the stream the scene has when it runs. */
+SR_API int sr_scene_set_seed(SrScene* scene, uint32_t seed);
+
 /* Launch geometry of the wavefront kernels (no counterpart in the reference): blocks per SM of the
  * traversal, fog-shade and surface-shade kernels (0 = as many as fit; never more) and the live-path
  * count slots / tail_divisor at which the tail kernel takes over (0 = the built-in 16).  Results

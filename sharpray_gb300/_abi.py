@@ -184,6 +184,7 @@ PROTOTYPES = {
     "sr_render_batch": (_I, [_P, _P, _P, _P, _U, _P]),
     "sr_render_progress": (_I, [_P, C.POINTER(_U), C.POINTER(_U)]),
     "sr_scene_set_tuning": (_I, [_P, _P]),
+    "sr_scene_set_seed": (_I, [_P, _U]),
     "sr_scene_get_tuning": (_I, [_P, C.POINTER(SrTuning)]),
     "sr_scene_autotune": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), _U, C.POINTER(SrTuning)]),
     "sr_aov_image": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P]),

@@ -459,6 +459,10 @@ class Scene:
         check(self._lib.sr_render_progress(self.handle, C.byref(d), C.byref(t)))
         return d.value, t.value
 
+    def set_seed(self, seed: int) -> None:
+        """sr_scene_set_seed: random-number stream of renders and adjoints (0 = the reference's)."""
+        check(self._lib.sr_scene_set_seed(self.handle, int(seed)))
+
     def update_fog_density(self, density: float) -> None:
         """sr_scene_update_fog_density: the built scene's fog density (its fog must exist)."""
         check(self._lib.sr_scene_update_fog_density(self.handle, float(density)))

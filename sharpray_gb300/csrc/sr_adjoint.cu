@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(64, GENERAL ? 6 : 8)
     Col G{d_image[3 * i] * inv, d_image[3 * i + 1] * inv, d_image[3 * i + 2] * inv};
     Ctr c;
     AdjVertex<PARAM> v[kAdjMaxVertices];
-    Rng rng = rng_seed(x, y);
+    Rng rng = rng_seed(x, y, P.seed);
     Col rad_sum = black(), fog_sum = black();
     float g_density = 0.0f;  // this pixel's d loss / d fog density
     for (uint32_t si = 0; si < taken; ++si) {

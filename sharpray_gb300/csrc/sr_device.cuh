@@ -138,8 +138,11 @@ SR_DEV uint64_t split_mix64(uint64_t& state) {
     r = (r ^ (r >> 27)) * 0x94d049bb133111ebULL;
     return r ^ (r >> 31);
 }
-SR_DEV Rng rng_seed(uint32_t a, uint32_t b) {
+// Rng(a, b) (math.cs:1665-1743); `stream` != 0 selects another, independent stream per (a, b) (an
+// extension: 0 is the reference's seeding).
+SR_DEV Rng rng_seed(uint32_t a, uint32_t b, uint32_t stream = 0) {
     uint64_t seed = ((uint64_t)a << 32) | b;
+    if (stream) seed ^= (uint64_t)stream * 0x9E3779B97F4A7C15ull;
     uint64_t v1 = split_mix64(seed);
     uint64_t v2 = split_mix64(seed);
     return {(uint32_t)v1, (uint32_t)(v1 >> 32), (uint32_t)v2, (uint32_t)(v2 >> 32), 0u};

@@ -167,6 +167,7 @@ struct SrScene {
     uint32_t progress_total = 0;
     int sms = 0;
     WaveTune tune{};  // launch geometry (sr_scene_set_tuning / sr_scene_autotune)
+    uint32_t seed = 0;  // random-number stream of renders and adjoints (sr_scene_set_seed)
     DevBuf tune_aovs;  // autotune's scratch AOV planes
     std::vector<uint64_t> tex_offset;  // first texel of each texture in `texels` (textures present at build)
     DevBuf tex_stage;                   // sr_scene_update_texture staging
@@ -816,6 +817,8 @@ static int make_view(const SrView* v, const SrRenderParams* p, DevView& dv, DevP
     dp.variance_threshold = p->variance_threshold;
     dp.indirect_clamp = p->indirect_clamp;
     dp.aspect = aspect;
+    dp.seed = 0;
+    dp.pad[0] = dp.pad[1] = dp.pad[2] = 0;
     return SR_OK;
 }
 
@@ -912,7 +915,7 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     const uint32_t tail_div = s->tune.tail_div ? s->tune.tail_div : (uint32_t)SR_TAIL_DIV;
     L.tail_paths = tail_div > 0 ? all_slots / tail_div : 0;
     L.progress = s->progress_dev;
-    SR_CUDA(wave_init(L, st), "wavefront init");
+    SR_CUDA(wave_init(L, st, s->seed), "wavefront init");
     return SR_OK;
 }
 
@@ -985,7 +988,9 @@ static int render_into(SrScene* s, const SrView* view, const SrRenderParams* par
     s->last_mode = mode;
     if (int rc = progress_begin(s, dp.width * dp.height)) return rc;
     if (mode == SR_RENDER_MEGAKERNEL) {
-        SR_CUDA(launch_render(s->dev, dv, dp, out, ctr, s->err.as<uint32_t>(), st), "render launch");
+        DevParams pm = dp;
+        pm.seed = s->seed;
+        SR_CUDA(launch_render(s->dev, dv, pm, out, ctr, s->err.as<uint32_t>(), st), "render launch");
     } else if (int rc = render_wavefront(s, dv, dp, out, ctr, st, mode == SR_RENDER_WAVEFRONT_GRAPH)) {
         return rc;
     }
@@ -1075,6 +1080,12 @@ SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const Sr
     }
     SR_CUDA(cudaGraphLaunch(ctx->batch_exec, st), "launch batch graph");
     for (uint32_t i = 0; i < count; ++i) SR_CUDA(cudaEventRecord(scenes[i]->progress_event, st), "progress event");
+    return SR_OK;
+}
+
+SR_API int sr_scene_set_seed(SrScene* s, uint32_t seed) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    s->seed = seed;
     return SR_OK;
 }
 
@@ -1783,6 +1794,7 @@ static int adjoint_prepare(SrScene* s, const SrView* view, const SrRenderParams*
     if (s->dev.has_transparent) return fail(SR_ERR_STATE, "the adjoint does not support transparent materials");
     if (int rc = make_view(view, params, dv, dp)) return rc;
     if (dp.bounces > 16) return fail(SR_ERR_INVALID_ARG, "the adjoint supports at most 16 bounces");
+    dp.seed = s->seed;  // replay the forward render's random numbers
     SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
     st = stream ? (cudaStream_t)stream : s->ctx->stream;
     return SR_OK;

@@ -107,6 +107,8 @@ struct SR_ALIGN16 DevParams {
     uint32_t width, height, min_samples, max_samples;
     uint32_t bounces;
     float variance_threshold, indirect_clamp, aspect;
+    uint32_t seed;  // random-number stream of the render (0: the reference's Rng(x, y))
+    uint32_t pad[3];
 };
 
 }  // namespace sr

@@ -85,7 +85,7 @@ __device__ Fragment sample_path(const DevScene& S, Ray ray, Rng& rng, uint32_t b
 template <bool COUNT>
 __device__ void render_pixel(const DevScene& S, const DevView& V, const DevParams& P, const DevAovs& out, uint32_t x,
                              uint32_t y, Ctr& c, uint32_t* err) {
-    Rng rng = rng_seed(x, y);
+    Rng rng = rng_seed(x, y, P.seed);
     Col rad_sum = black(), fog_sum = black();
     float lum_sum = 0.f, lum_sqr = 0.f, surf_sum = 0.f, surf_sqr = 0.f;
     V3 nsum{0.f, 0.f, 0.f}, nfb{0.f, 0.f, 0.f};

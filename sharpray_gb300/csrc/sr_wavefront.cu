@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevScene S, DevV
         slot_pixel(W, s, x, y);
         valid = x < P.width && y < P.height;
         if (valid) {
-            Rng rng = rng_seed(x, y);
+            Rng rng = rng_seed(x, y, P.seed);
             Ray ray = camera_ray(V, P, x, y, rng);
             begin_sample(W, s, ray, rng, fog_scatter_t(S, ray, rng));
             float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1138,12 +1138,14 @@ void wave_grid_sizes(WaveLaunch& L, int sms, const WaveTune* tune) {
     L.grid_shade[2] = b[5];
 }
 
-cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st) {
+cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st, uint32_t seed) {
+    DevParams P = L.P;  // the seed only reaches the first camera rays, outside any cached graph
+    P.seed = seed;
     cudaError_t e = cudaMemsetAsync(L.W[0].counts, 0, (size_t)L.groups * kWaveCounters * sizeof(uint32_t), st);
     if (e == cudaSuccess && SR_SORT_EVENTS) e = cudaMemsetAsync(L.W[0].ev_mark, 0, L.W[0].rec_stride, st);
     if (e != cudaSuccess) return e;
     for (int g = 0; g < L.groups; ++g)
-        if (L.W[g].slots) k_wave_init<<<(L.W[g].slots + 127) / 128, 128, 0, st>>>(L.W[g], L.S, L.V, L.P);
+        if (L.W[g].slots) k_wave_init<<<(L.W[g].slots + 127) / 128, 128, 0, st>>>(L.W[g], L.S, L.V, P);
     return cudaGetLastError();
 }
 

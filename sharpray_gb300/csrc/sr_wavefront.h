@@ -148,7 +148,8 @@ struct WaveTune {
 void wave_occupancy(bool general, int* trace, int* fog, int* surface);
 void wave_grid_sizes(WaveLaunch& L, int sms, const WaveTune* tune = nullptr);
 // Counters of every group (contiguous, kWaveCounters per group) cleared, first camera rays.
-cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st);
+// Counters cleared and the first camera rays of every slot, drawn from random-number stream `seed`.
+cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st, uint32_t seed = 0);
 // One bounce of every group: group 0 on `st`, the others on `side` streams forked from and
 // joined back to `st` with the events in `fork` (one per group).
 cudaError_t wave_bounce(const WaveLaunch& L, int cur, cudaStream_t st, const cudaStream_t* side, const cudaEvent_t* fork);
