@@ -398,6 +398,7 @@ class Scene:
         self.sky = None
         self.fog: Optional[Fog] = None
         self.built = False
+        self.seed = 0  # random-number stream (set_seed)
 
     def set_sky(self, sky) -> None:
         if isinstance(sky, SkyTexture):
@@ -462,6 +463,7 @@ class Scene:
     def set_seed(self, seed: int) -> None:
         """sr_scene_set_seed: random-number stream of renders and adjoints (0 = the reference's)."""
         check(self._lib.sr_scene_set_seed(self.handle, int(seed)))
+        self.seed = int(seed)
 
     def update_fog_density(self, density: float) -> None:
         """sr_scene_update_fog_density: the built scene's fog density (its fog must exist)."""

@@ -153,6 +153,11 @@ def test_progress_adjoint_and_update_validation(host_ctx):
     lib = host_ctx._lib
     s = Scene(host_ctx)
     assert s.progress() == (0, 0)  # nothing launched
+    assert s.seed == 0
+    s.set_seed(9)
+    assert s.seed == 9
+    with pytest.raises(SharpRayError):
+        _abi.check(lib.sr_scene_set_seed(None, 1))
     d, t = C.c_uint32(), C.c_uint32()
     with pytest.raises(SharpRayError):
         _abi.check(lib.sr_render_progress(s.handle, None, C.byref(t)))
