@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=0, help="render mode: 0 auto, 1 megakernel, 2 wavefront, 3 graph")
-    ap.add_argument("--variants", action="store_true", help="also time every render mode once")
+    ap.add_argument("--variants", action="store_true", help="also time the megakernel render mode")
     ap.add_argument("--autotune-spp", type=int, default=8,
                     help="spp of the autotuner's trial renders at setup (0: default launch geometry)")
     ap.add_argument("--batch-autotune-spp", type=int, default=0,
@@ -152,39 +152,66 @@ def aggregate(samples_per_rank_step: int, steps: int, world: int, rank_seconds: 
 def algorithmic_bytes(c: dict, pixels: int) -> int:
     """Bytes the reference algorithm must touch per render (data-structure sizes of the reference):
     32 B per BVH node test, 36 B per triangle test, 40 B per instance test, 108 B per inflated hit,
-    48 B per bilinear texture sample (4 float3 texels), 4 B per CDF probe, 56 B AOV write per pixel."""
+    48 B per bilinear material-texture sample (4 float3 texels), 48 B per environment radiance
+    lookup (SkyTexture.Radiance: a bilinear sample of the env map), 4 B per CDF probe, 56 B AOV
+    write per pixel."""
     return int(32 * (c["tlas_node"] + c["blas_node"]) + 36 * c["blas_shape"] + 40 * c["tlas_shape"]
-               + 108 * c["hit_inflate"] + 48 * c["tex_sample"] + 4 * c["cdf_probe"] + 56 * pixels)
+               + 108 * c["hit_inflate"] + 48 * c["tex_sample"] + 48 * c["env_lookup"] + 4 * c["cdf_probe"]
+               + 56 * pixels)
 
 
 def oracle_bands(scene, view, params, threads: int, height: int, rows_per_band: int, bands: int = 16,
-                 shift: int = 0):
+                 shift: int = 0, keep: bool = False):
     """Renders `bands` evenly spaced bands of `rows_per_band` image rows with the CPU oracle (a
     stratified sample of the frame: rows differ widely in cost, sky vs. geometry).  Returns the
-    rows rendered and the seconds taken."""
+    rows rendered, the seconds taken and (keep) the list of (y0, y1, radiance + fog radiance rows)."""
     r = max(1, min(rows_per_band, height // bands))
     spans = []
     for b in range(bands):
         y0 = int((b + 0.5) * height / bands) - r // 2 + shift * r
         y0 = max(0, min(height - r, y0))
         spans.append((y0, y0 + r))
+    kept = []
     t0 = time.perf_counter()
     for y0, y1 in spans:
-        scene.render(view, params, threads, rows=(y0, y1))
-    return r * len(spans), time.perf_counter() - t0
+        a, _ = scene.render(view, params, threads, rows=(y0, y1))
+        if keep:
+            w = params.width
+            kept.append((y0, y1, (a.radiance + a.radiance_fog)[y0 * w:y1 * w].copy()))
+    return r * len(spans), time.perf_counter() - t0, kept
+
+
+def band_parity(kept, frame) -> dict:
+    """The GPU frame (radiance + fog radiance, pixels x 3) against the oracle's bands of the same
+    frame: the project's image bar (relMSE < 1e-4, per-pixel relative error < 1e-3 on >= 99.5 %)."""
+    import numpy as np
+    w = None
+    got, want = [], []
+    for y0, y1, rows in kept:
+        w = len(rows) // (y1 - y0)
+        got.append(frame[y0 * w:y1 * w])
+        want.append(rows)
+    g, r = np.concatenate(got).astype(np.float64), np.concatenate(want).astype(np.float64)
+    err = np.abs(g - r).max(axis=1) / np.maximum(np.abs(r).max(axis=1), 1e-3)
+    rel = float(np.mean((g - r) ** 2 / (r ** 2 + 1e-2)))
+    frac = float((err < 1e-3).mean())
+    return {"pixels": int(len(err)), "rel_mse": rel, "frac_within_1e-3": frac,
+            "pass": bool(rel < 1e-4 and frac >= 0.995),
+            "bar": "relMSE < 1e-4 and per-pixel relative error < 1e-3 on >= 99.5 % of pixels"}
 
 
 def cpu_oracle_sample(desc, target_s: float, threads: int):
-    """Times the CPU oracle on a stratified row sample of the workload sized for ~target_s seconds."""
+    """Times the CPU oracle on a stratified row sample of the workload sized for ~target_s seconds;
+    also returns the rows it rendered, for the parity check against the GPU frame."""
     from oracle import oracle
     from sharpray_gb300 import render_params
     scene = oracle.instantiate(desc)
     view, params = desc.view.to_c(), render_params(*desc.render_args())
-    rows1, dt1 = oracle_bands(scene, view, params, threads, desc.height, 1)
+    rows1, dt1, _ = oracle_bands(scene, view, params, threads, desc.height, 1)
     per_band = int(max(1, round(target_s / max(dt1, 1e-3))))
-    rows, dt = oracle_bands(scene, view, params, threads, desc.height, per_band)
+    rows, dt, kept = oracle_bands(scene, view, params, threads, desc.height, per_band, keep=True)
     samples = rows * desc.width * desc.spp
-    return samples / dt, rows, dt
+    return samples / dt, rows, dt, kept
 
 
 def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
@@ -225,11 +252,20 @@ def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
             vc = v.to_c()
             _abi.check(lib.sr_render_device(sc.handle, C.byref(vc), C.byref(p), C.byref(o), sp))
 
+    def plain_host_loop():  # one launch per bounce kernel, driven by the host
+        for sc in scenes:
+            sc.set_render_mode(_abi.SR_RENDER_WAVEFRONT)
+        try:
+            plain()
+        finally:
+            for sc in scenes:
+                sc.set_render_mode(_abi.SR_RENDER_AUTO)
+
     def batch():
         render_batch(scenes, views, params, outs, stream=stream.cuda_stream)
 
     res = {}
-    for label, fn in (("plain", plain), ("batched", batch)):
+    for label, fn in (("plain", plain), ("plain_host_loop", plain_host_loop), ("batched", batch)):
         fn()  # warm-up (builds the graphs)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -244,11 +280,15 @@ def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
                         "256x256-1920x1080, 4/16/64 spp, depth 4-8, fog on half",
             "samples_per_step": samples, "unit": UNIT,
             "value": samples / res["batched"], "plain_value": samples / res["plain"],
+            "plain_host_loop_value": samples / res["plain_host_loop"],
             "batched_ms": 1000 * res["batched"], "plain_ms": 1000 * res["plain"],
-            "speedup": res["plain"] / res["batched"], "setup_s": round(setup, 1),
+            "plain_host_loop_ms": 1000 * res["plain_host_loop"],
+            "speedup": res["plain"] / res["batched"], "speedup_vs_host_loop": res["plain_host_loop"] / res["batched"],
+            "setup_s": round(setup, 1),
             "autotuned_scenes": tuned if tune_spp > 0 else None,
             "note": "batched: one graph launch, one bounce loop per scene side by side; plain: one "
-                    "graph-captured render per scene, back to back; images bit-identical"}
+                    "graph-captured render per scene, back to back; plain_host_loop: one render per scene "
+                    "with one launch per bounce kernel from the host; images bit-identical"}
 
 
 def measure_adjoint(checks: int, reps: int = 5) -> dict:
@@ -508,22 +548,25 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
                 xs.clamp_(1e-3, 1.0)
             losses.append(loss)
 
-        step()  # warm-up
-        st.synchronize()
-        # well-observed texels: first-step gradient at least 5 % of the 99th percentile (texels seen
-        # only at grazing angles or through reflections get weak, noisy gradients)
-        ga0, gr0 = xa.grad.abs().sum(dim=2), xr.grad[..., 0].abs()
-        seen_a = ga0 >= 0.05 * torch.quantile(ga0[ga0 > 0], 0.99)
-        seen_r = gr0 >= 0.05 * torch.quantile(gr0[gr0 > 0], 0.99)
-        rmse = lambda x, t, m: float(((x.detach() - t)[m] ** 2).mean()) ** 0.5
-        rmse_start = (rmse(torch.full_like(truth_a, 0.5), truth_a, seen_a),
-                      rmse(torch.full_like(truth_r, 0.5)[..., 0], truth_r[..., 0], seen_r))
-        setup_s = time.perf_counter() - t_setup
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            step()
-        st.synchronize()
-        dt = (time.perf_counter() - t0) / max(steps, 1)
+        try:
+            step()  # warm-up
+            st.synchronize()
+            # well-observed texels: first-step gradient at least 5 % of the 99th percentile (texels
+            # seen only at grazing angles or through reflections get weak, noisy gradients)
+            ga0, gr0 = xa.grad.abs().sum(dim=2), xr.grad[..., 0].abs()
+            seen_a = ga0 >= 0.05 * torch.quantile(ga0[ga0 > 0], 0.99)
+            seen_r = gr0 >= 0.05 * torch.quantile(gr0[gr0 > 0], 0.99)
+            rmse = lambda x, t, m: float(((x.detach() - t)[m] ** 2).mean()) ** 0.5
+            rmse_start = (rmse(torch.full_like(truth_a, 0.5), truth_a, seen_a),
+                          rmse(torch.full_like(truth_r, 0.5)[..., 0], truth_r[..., 0], seen_r))
+            setup_s = time.perf_counter() - t_setup
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                step()
+            st.synchronize()
+            dt = (time.perf_counter() - t0) / max(steps, 1)
+        finally:
+            sc.set_seed(0)  # later users of the scene render from the reference's stream
     n_grads = truth_a.numel() + truth_r.shape[0] * truth_r.shape[1] + 1
     samples = views * d.width * d.height * d.spp
     return {"workload": f"{views} orbit views {d.width}x{d.height}, {d.spp} spp, depth 8, "
@@ -551,13 +594,13 @@ def run_reference(args):
     scene = oracle.instantiate(desc)
     view, params = desc.view.to_c(), render_params(*desc.render_args())
     # calibrate a stratified row sample of ~2 s per step so the whole run stays within minutes
-    rows1, dt1 = oracle_bands(scene, view, params, threads, desc.height, 1)
+    rows1, dt1, _ = oracle_bands(scene, view, params, threads, desc.height, 1)
     per_band = int(max(1, round(2.0 / max(dt1, 1e-3))))
     for _ in range(args.warmup):
         oracle_bands(scene, view, params, threads, desc.height, 1)
     times, rows = [], 0
     for s in range(args.steps):
-        rows, dt = oracle_bands(scene, view, params, threads, desc.height, per_band, shift=s % 2)
+        rows, dt, _ = oracle_bands(scene, view, params, threads, desc.height, per_band, shift=s % 2)
         times.append(dt)
     samples = rows * desc.width * desc.spp * args.steps
     value = samples / sum(times)
@@ -690,20 +733,24 @@ def run_ours(args):
 
     value, total_s = aggregate(samples_per_step, args.steps, world, sum(step_ms) / 1000.0, reduce_max)
 
-    variants = None
-    if args.variants:
-        variants = {}
-        for mode, label in ((1, "megakernel"), (2, "wavefront_host_loop"), (3, "wavefront_graph")):
-            scene.set_render_mode(mode)
+    # render modes on the same frame (identical images): the graph-captured device bounce loop
+    # against the plain one-launch-per-bounce host loop, two renders each after a warm-up; the
+    # megakernel (one thread per pixel) with --variants
+    variants = {}
+    modes = ((2, "wavefront_host_loop"), (3, "wavefront_graph")) + (((1, "megakernel"),) if args.variants else ())
+    for mode, label in modes:
+        scene.set_render_mode(mode)
+        render()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(2):
             render()
-            torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            render()
-            b.record(stream)
-            torch.cuda.synchronize()
-            variants[label] = samples_per_step / (a.elapsed_time(b) / 1000.0)
-        scene.set_render_mode(args.mode)
+        b.record(stream)
+        torch.cuda.synchronize()
+        variants[label] = samples_per_step / (a.elapsed_time(b) / 2000.0)
+    scene.set_render_mode(args.mode)
+    variants["graph_over_host_loop"] = variants["wavefront_graph"] / variants["wavefront_host_loop"]
 
     batched = None
     if args.batch_scenes > 0 and rank == 0:
@@ -751,13 +798,18 @@ def run_ours(args):
         except Exception:
             traffic = None
 
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, rows, dt = cpu_oracle_sample(desc, args.cpu_seconds, threads)
+        v, rows, dt, kept = cpu_oracle_sample(desc, args.cpu_seconds, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{rows} rows in 16 evenly spaced bands x {W} px x {desc.spp} spp of the same frame "
                          f"({dt:.1f} s)"}
+        # the timed frame (AOVs of the last render; every render of this scene is the same) against
+        # the oracle's rows of it
+        frame = (dev["radiance"] + dev["radiance_fog"]).view(-1, 3).cpu().numpy()
+        parity = band_parity(kept, frame)
+        parity["sample"] = cpu["sample"]
 
     if rank == 0:
         out = {
@@ -784,6 +836,7 @@ def run_ours(args):
                          "note": "per frame of the path tracer; alg bytes from the kernels' own work "
                                  "counters sized by the reference's records"},
             "cpu_baseline": cpu,
+            "parity_vs_oracle": parity,
             "gpu_launches": launches,
             "render_mode": {0: "auto (wavefront graph)", 1: "megakernel", 2: "wavefront host loop",
                             3: "wavefront graph"}[args.mode],

@@ -174,9 +174,10 @@ enum {
     SR_COUNTER_BLAS_NODE,         /* mesh BVH box tests                 (bvh.cs:189)     */
     SR_COUNTER_BLAS_SHAPE,        /* triangle tests                     (bvh.cs:203)     */
     SR_COUNTER_HIT_INFLATE,       /* closest hits inflated              (mesh.cs:57)     */
-    SR_COUNTER_TEX_SAMPLE,        /* Texture.Sample calls               (texture.cs:39)  */
+    SR_COUNTER_TEX_SAMPLE,        /* material Texture.Sample calls      (texture.cs:39)  */
     SR_COUNTER_CDF_PROBE,         /* Cdf1 search probes performed       (cdf.cs:40-52)   */
     SR_COUNTER_LIGHT_SAMPLE,      /* sky-texture light samples (Cdf2)   (scene.cs:408)   */
+    SR_COUNTER_ENV_LOOKUP,        /* SkyTexture.Radiance lookups        (scene.cs:406)   */
     SR_COUNTER_COUNT
 };
 
@@ -347,11 +348,20 @@ SR_API int sr_render_batch(SrScene* const* scenes, const SrView* views, const Sr
  * pixel an independent stream, e.g. fresh samples for each step of stochastic inverse rendering or
  * for progressive accumulation.  An adjoint replays the stream the scene has when it runs. */
 SR_API int sr_scene_set_seed(SrScene* scene, uint32_t seed);
+/* The scene's current random-number stream (what sr_scene_set_seed last set; 0 by default), e.g.
+ * for a wrapper that must replay a render with the stream it was made with. */
+SR_API int sr_scene_get_seed(SrScene* scene, uint32_t* seed);
 
 /* Launch geometry of the wavefront kernels (no counterpart in the reference): blocks per SM of the
  * traversal, fog-shade and surface-shade kernels (0 = as many as fit; never more) and the live-path
  * count slots / tail_divisor at which the tail kernel takes over (0 = the built-in 16).  Results
- * do not depend on it. */
+ * do not depend on it.
+ * Two loop caps (0 = the built-in runaway guards) bound the work of one render: the iterations of
+ * the wavefront bounce loop and the actions (node visits, leaf steps) of one traversal.  A render
+ * or trace that reaches either ends early and returns SR_ERR_DEVICE naming the loop cap (error
+ * word 2); the kernels return normally and the context stays usable.  The reference has no such
+ * guard (its Tick loop waits without a timeout, renderer.cs:98-105); lowering them is how failure
+ * detection is exercised without a fault. */
 typedef struct SrTuning {
     int32_t trace_blocks_per_sm;
     int32_t fog_shade_blocks_per_sm;
@@ -359,6 +369,8 @@ typedef struct SrTuning {
     uint32_t tail_divisor;
     float ms;          /* sr_scene_autotune: trial render time of the chosen setting */
     float default_ms;  /* sr_scene_autotune: trial render time of the defaults */
+    uint32_t max_bounce_iterations; /* wavefront bounce-loop cap (0 = (max_samples + 1) * (bounces + 2) * 2 + 8) */
+    uint32_t max_traversal_steps;   /* per-traversal action cap (0 = 2^24) */
 } SrTuning;
 SR_API int sr_scene_set_tuning(SrScene* scene, const SrTuning* tuning); /* NULL = defaults */
 SR_API int sr_scene_get_tuning(SrScene* scene, SrTuning* tuning);

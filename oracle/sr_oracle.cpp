@@ -869,7 +869,10 @@ struct Sky {
         sun_pdf_denom = kPi * (1.0f - sun_angle_cos);
     }
     Col radiance(V3 dir, Counters* ctr) const {
-        if (kind == 0) return tex->sample(equirect_uv(rot_inv * dir), ctr) * multiplier;
+        if (kind == 0) {
+            if (ctr) ctr->add(SR_COUNTER_ENV_LOOKUP);
+            return tex->sample(equirect_uv(rot_inv * dir), nullptr) * multiplier;
+        }
         const float bias = 0.0001f;
         float top_b = 1.0f - std::pow(net_min(1.0f, 1.0f + bias - dir.y), 4.0f);
         float bot_b = 1.0f - std::pow(net_min(1.0f, 1.0f + bias + dir.y), 40.0f);

@@ -44,7 +44,7 @@ SR_TONEMAP_LINEAR_SMOOTH = 1
 
 COUNTER_NAMES = [
     "sample", "sample_bounce", "scene_trace", "scene_occlude", "tlas_node", "tlas_shape", "blas_node",
-    "blas_shape", "hit_inflate", "tex_sample", "cdf_probe", "light_sample",
+    "blas_shape", "hit_inflate", "tex_sample", "cdf_probe", "light_sample", "env_lookup",
 ]
 SR_COUNTER_COUNT = len(COUNTER_NAMES)
 
@@ -112,7 +112,7 @@ class SrComposeParams(C.Structure):
 class SrTuning(C.Structure):
     _fields_ = [("trace_blocks_per_sm", C.c_int32), ("fog_shade_blocks_per_sm", C.c_int32),
                 ("surface_shade_blocks_per_sm", C.c_int32), ("tail_divisor", C.c_uint32), ("ms", C.c_float),
-                ("default_ms", C.c_float)]
+                ("default_ms", C.c_float), ("max_bounce_iterations", C.c_uint32), ("max_traversal_steps", C.c_uint32)]
 
 
 class SrAovImageParams(C.Structure):
@@ -185,6 +185,7 @@ PROTOTYPES = {
     "sr_render_progress": (_I, [_P, C.POINTER(_U), C.POINTER(_U)]),
     "sr_scene_set_tuning": (_I, [_P, _P]),
     "sr_scene_set_seed": (_I, [_P, _U]),
+    "sr_scene_get_seed": (_I, [_P, C.POINTER(_U)]),
     "sr_scene_get_tuning": (_I, [_P, C.POINTER(SrTuning)]),
     "sr_scene_autotune": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), _U, C.POINTER(SrTuning)]),
     "sr_aov_image": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.c_int32, C.POINTER(SrAovImageParams), _P]),

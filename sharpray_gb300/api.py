@@ -398,7 +398,6 @@ class Scene:
         self.sky = None
         self.fog: Optional[Fog] = None
         self.built = False
-        self.seed = 0  # random-number stream (set_seed)
 
     def set_sky(self, sky) -> None:
         if isinstance(sky, SkyTexture):
@@ -428,11 +427,20 @@ class Scene:
         self.built = True
 
     def set_tuning(self, trace_blocks_per_sm: int = 0, fog_shade_blocks_per_sm: int = 0,
-                   surface_shade_blocks_per_sm: int = 0, tail_divisor: int = 0) -> None:
-        """Launch geometry of the wavefront kernels (0 = default); results do not depend on it."""
+                   surface_shade_blocks_per_sm: int = 0, tail_divisor: int = 0, max_bounce_iterations: int = 0,
+                   max_traversal_steps: int = 0) -> None:
+        """Launch geometry of the wavefront kernels (0 = default); results do not depend on it.
+        The two caps (0 = the built-in runaway guards) end a render that exceeds them with
+        SR_ERR_DEVICE (loop cap) instead of running on."""
         t = _abi.SrTuning(trace_blocks_per_sm, fog_shade_blocks_per_sm, surface_shade_blocks_per_sm, tail_divisor,
-                          0.0, 0.0)
+                          0.0, 0.0, max_bounce_iterations, max_traversal_steps)
         check(self._lib.sr_scene_set_tuning(self.handle, C.byref(t)))
+
+    def get_tuning(self) -> dict:
+        """sr_scene_get_tuning: the scene's current launch geometry and loop caps."""
+        t = _abi.SrTuning()
+        check(self._lib.sr_scene_get_tuning(self.handle, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in _abi.SrTuning._fields_ if f not in ("ms", "default_ms")}
 
     def autotune(self, view: "View", params: SrRenderParams, trial_spp: int = 8) -> dict:
         """sr_scene_autotune: times candidate launch geometries on `params` at trial_spp samples per
@@ -461,9 +469,23 @@ class Scene:
         return d.value, t.value
 
     def set_seed(self, seed: int) -> None:
-        """sr_scene_set_seed: random-number stream of renders and adjoints (0 = the reference's)."""
-        check(self._lib.sr_scene_set_seed(self.handle, int(seed)))
-        self.seed = int(seed)
+        """sr_scene_set_seed: random-number stream of renders and adjoints (0 = the reference's).
+        The stream is a 32-bit value: seeds outside [0, 2^32) are rejected."""
+        seed = int(seed)
+        if not 0 <= seed <= 0xFFFFFFFF:
+            raise ValueError(f"seed must be in [0, 2^32), got {seed}")
+        check(self._lib.sr_scene_set_seed(self.handle, seed))
+
+    def get_seed(self) -> int:
+        """sr_scene_get_seed: the stream the scene's renders use now (also after a direct
+        sr_scene_set_seed call through the C ABI)."""
+        v = C.c_uint32()
+        check(self._lib.sr_scene_get_seed(self.handle, C.byref(v)))
+        return v.value
+
+    @property
+    def seed(self) -> int:
+        return self.get_seed()
 
     def update_fog_density(self, density: float) -> None:
         """sr_scene_update_fog_density: the built scene's fog density (its fog must exist)."""

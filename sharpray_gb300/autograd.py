@@ -53,7 +53,7 @@ class TextureRender(torch.autograd.Function):
         check(scene._lib.sr_render_device(scene.handle, C.byref(v), C.byref(params), C.byref(aovs),
                                           C.c_void_p(stream)))
         ctx.scene, ctx.view, ctx.params, ctx.texture, ctx.parameter = scene, view, params, texture, parameter
-        ctx.seed = scene.seed  # the replay must use the forward's random-number stream
+        ctx.seed = scene.get_seed()  # the replay must use the forward's random-number stream
         ctx.bufs, ctx.aovs = bufs, aovs
         ctx.save_for_backward(texels)
         return (bufs["radiance"] + bufs["radiance_fog"]).view(params.height, params.width, 3)
@@ -66,7 +66,7 @@ class TextureRender(torch.autograd.Function):
         ctx.scene.update_texture_device(ctx.texture, texels.data_ptr(), stream)
         g_img = grad_image.contiguous().to(torch.float32)
         grad = torch.zeros_like(texels)
-        seed = ctx.scene.seed
+        seed = ctx.scene.get_seed()
         ctx.scene.set_seed(ctx.seed)  # and its random-number stream
         try:
             adjoint_texture(ctx.scene, ctx.view, ctx.params, ctx.aovs, g_img.data_ptr(), ctx.texture,

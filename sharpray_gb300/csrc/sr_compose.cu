@@ -11,6 +11,7 @@
 // tap the normal, depth and luminance Gaussians are one fast exponential of their summed
 // exponents and the sums accumulate with fused multiply-adds: the filter is the reference's up to
 // float rounding (images agree within one code value).
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include "sr_device.cuh"
@@ -327,21 +328,27 @@ cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, c
 static constexpr size_t kStaticScratchBytes = size_t(32) << 20;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-// Device address of g_static_scratch, resolved once per device with that device current.
+// Device address of g_static_scratch, resolved once per device with that device current.  Host
+// threads making their first call on one device at the same time may both resolve it; they store
+// the same value, and the atomic entries make that a benign race instead of a data race.
 static constexpr int kMaxDevices = 64;
-static float4* g_static_scratch_addr[kMaxDevices];
+static std::atomic<float4*> g_static_scratch_addr[kMaxDevices];
 
 static cudaError_t static_scratch(int device, float4** out) {
     if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
-    if (!g_static_scratch_addr[device]) {
+    float4* addr = g_static_scratch_addr[device].load(std::memory_order_acquire);
+    if (!addr) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e != cudaSuccess) return e;
-        g_static_scratch_addr[device] = (float4*)p;
+        addr = (float4*)p;
+        g_static_scratch_addr[device].store(addr, std::memory_order_release);
     }
-    *out = g_static_scratch_addr[device];
+    *out = addr;
     return cudaSuccess;
 }
+
+size_t compose_static_capacity() { return kStaticScratchBytes; }
 
 // Packs image rows [row0, row0 + rows) into band-local planes.
 __global__ void k_pack_band(DevAovs in, uint32_t width, uint32_t row0, uint32_t rows, float4* p_rad, float4* p_geo,
@@ -447,12 +454,13 @@ __global__ void __launch_bounds__(128) k_compose_band(const float4* __restrict__
 
 cudaError_t launch_compose_static(int device, const DevAovs& in, uint32_t width, uint32_t height,
                                   const ComposeConsts& k, float rp_inv, float rpf_inv, float fog_strength,
-                                  uint8_t* rgb8, cudaStream_t stream, size_t* needed_bytes) {
+                                  uint8_t* rgb8, cudaStream_t stream, size_t* needed_bytes, bool* too_large) {
     uint32_t halo = (uint32_t)(k.radius > k.fog_radius ? k.radius : k.fog_radius);
     const size_t row_bytes = (size_t)width * 3 * sizeof(float4);
     size_t rows_cap = kStaticScratchBytes / row_bytes;
     *needed_bytes = (size_t)(2 * halo + 2) * row_bytes;
-    if (rows_cap < 2 * (size_t)halo + 2) return cudaErrorInvalidValue;  // caller reports the limit
+    *too_large = rows_cap < 2 * (size_t)halo + 2;
+    if (*too_large) return cudaErrorInvalidValue;  // nothing launched; the caller reports the limit
     float4* base = nullptr;
     cudaError_t e = static_scratch(device, &base);
     if (e != cudaSuccess) return e;

@@ -250,9 +250,37 @@ struct StackEntry {
     float t;
 };
 constexpr int kStackSize = 128;  // bvh.cs:172 stackalloc size; depth cap 64 keeps use <= 65.
-// Upper bound on node pops of one traversal.  A well-formed tree of N nodes needs at most N pops;
-// the cap only turns a malformed tree into an error word instead of a hang.
-constexpr uint32_t kMaxPops = 1u << 24;
+
+// Traversal stacks.  LocalStack is a per-thread array in local memory.  SplitStack keeps the first
+// N entries of each thread's stack in shared memory and the rest in a per-thread local array.  Its
+// shared words are laid out [entry][word][thread of the block], so the 32 lanes of a warp always
+// touch 32 different banks, whatever stack depth each lane is at; local memory interleaves the
+// threads of a warp word by word, so lanes at different depths touch different 128-byte lines.
+struct LocalStack {
+    StackEntry* a;
+    SR_DEV StackEntry get(int i) const { return a[i]; }
+    SR_DEV void set(int i, const StackEntry& e) { a[i] = e; }
+};
+template <int N, int BLOCK>
+struct SplitStack {
+    uint32_t* sm;   // this thread's first word: the block's shared array + threadIdx.x
+    StackEntry* a;  // entries N and up
+    SR_DEV StackEntry get(int i) const {
+        if (i >= N) return a[i - N];
+        const uint32_t* p = sm + (size_t)i * 3 * BLOCK;
+        return {(int)p[0], (int)p[BLOCK], __uint_as_float(p[2 * BLOCK])};
+    }
+    SR_DEV void set(int i, const StackEntry& e) {
+        if (i >= N) {
+            a[i - N] = e;
+            return;
+        }
+        uint32_t* p = sm + (size_t)i * 3 * BLOCK;
+        p[0] = (uint32_t)e.child;
+        p[BLOCK] = (uint32_t)e.count;
+        p[2 * BLOCK] = __float_as_uint(e.t);
+    }
+};
 
 // Read-only scene data (BVH nodes, triangles, attributes, texels, CDF tables) goes through the
 // non-coherent path.  SR_SCENE_HINT = 1 adds the L2 eviction priority evict_last so that the path
@@ -498,8 +526,10 @@ struct SceneQuery {
             state = (has_node || sp > 0) ? QS_NODE : QS_DONE;
     }
 
-    SR_DEV bool count_action(uint32_t* err) {
-        if (++pops > kMaxPops) {
+    // Every action counts against the scene's cap (DevScene::max_actions); past it the query ends
+    // with the error word set, so a malformed tree (or a test's low cap) ends in an error, not a hang.
+    SR_DEV bool count_action(const DevScene& S, uint32_t* err) {
+        if (++pops > S.max_actions) {
             atomicOr(err, SR_DEVERR_LOOP);
             state = QS_DONE;
             return false;
@@ -507,10 +537,10 @@ struct SceneQuery {
         return true;
     }
 
-    template <bool COUNT>
-    SR_DEV void node_action(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
-        if (!count_action(err)) return;
-        StackEntry e = has_node ? node : stack[--sp];
+    template <bool COUNT, typename STK>
+    SR_DEV void node_action(const DevScene& S, STK& stack, Ctr& c, uint32_t* err) {
+        if (!count_action(S, err)) return;
+        StackEntry e = has_node ? node : stack.get(--sp);
         has_node = false;
         if (!ANY && e.t >= cur_best) {
             next_state();
@@ -536,7 +566,7 @@ struct SceneQuery {
                     return;
                 }
                 bool a_first = ta < tb;
-                stack[sp++] = a_first ? eb : ea;
+                stack.set(sp++, a_first ? eb : ea);
                 node = a_first ? ea : eb;
                 has_node = true;
             } else if (pa || pb) {
@@ -557,10 +587,10 @@ struct SceneQuery {
         }
     }
 
-    template <bool COUNT>
-    SR_DEV void leaf_action(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
+    template <bool COUNT, typename STK>
+    SR_DEV void leaf_action(const DevScene& S, STK& stack, Ctr& c, uint32_t* err) {
         const float inf = __int_as_float(0x7f800000);
-        if (!count_action(err)) return;
+        if (!count_action(S, err)) return;
         if (state == QS_TRI) {
             // the whole mesh leaf, in leaf order (bvh.cs:203-212)
             for (; tri_left > 0; ++tri_next, --tri_left) {
@@ -631,8 +661,8 @@ struct SceneQuery {
     }
 
     // One action of whatever kind is next; true when the query is answered.
-    template <bool COUNT>
-    SR_DEV bool step(const DevScene& S, StackEntry* stack, Ctr& c, uint32_t* err) {
+    template <bool COUNT, typename STK>
+    SR_DEV bool step(const DevScene& S, STK& stack, Ctr& c, uint32_t* err) {
         if (state == QS_NODE)
             node_action<COUNT>(S, stack, c, err);
         else if (state != QS_DONE)
@@ -662,7 +692,8 @@ SR_DEV bool misses_scene(const DevScene& S, const Ray& r, Ctr& c) {
 
 template <bool COUNT, bool ANY, bool GENERAL = true>
 SR_DEV Hit scene_traverse(const DevScene& S, const Ray& wr, Ctr& c, uint32_t* err) {
-    StackEntry stack[kSceneStack];
+    StackEntry entries[kSceneStack];
+    LocalStack stack{entries};
     SceneQuery<ANY, GENERAL> q;
     q.init(S, wr);
     while (!q.template step<COUNT>(S, stack, c, err)) {
@@ -754,7 +785,10 @@ SR_DEV V3 from_equirect_uv(V2 uv) {
 template <bool COUNT, bool GENERAL = true>
 SR_DEV Col sky_radiance(const DevScene& S, V3 dir, Ctr& c) {
     const DevSky& k = S.sky;
-    if (!GENERAL || k.kind == 0) return tex_sample<COUNT>(S, k.texture, equirect_uv(quat_rotate(k.rot_inv, dir)), c) * k.multiplier;
+    if (!GENERAL || k.kind == 0) {
+        SR_COUNT(c, SR_COUNTER_ENV_LOOKUP, 1);
+        return tex_sample<false>(S, k.texture, equirect_uv(quat_rotate(k.rot_inv, dir)), c) * k.multiplier;
+    }
     const float bias = 0.0001f;
     float top_b = 1.0f - sr_pow(fminf(1.0f, 1.0f + bias - dir.y), 4.0f);
     float bot_b = 1.0f - sr_pow(fminf(1.0f, 1.0f + bias + dir.y), 40.0f);
@@ -855,7 +889,7 @@ SR_DEV bool sky_light_rand(const DevScene& S, Rng& rng, V3& dir, float& pdf, Ctr
 template <bool COUNT, bool GENERAL = true>
 SR_DEV Col sky_light_radiance(const DevScene& S, int texel, V3 dir, Ctr& c) {
     if (texel >= 0 && S.sky.center) {
-        SR_COUNT(c, SR_COUNTER_TEX_SAMPLE, 1);
+        SR_COUNT(c, SR_COUNTER_ENV_LOOKUP, 1);
         return col3(ldg4(S.sky.center + texel));
     }
     return sky_radiance<COUNT, GENERAL>(S, dir, c);

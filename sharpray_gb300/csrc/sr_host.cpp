@@ -711,6 +711,7 @@ SR_API int sr_scene_build(SrScene* s) {
     for (const auto& o : s->objects)
         if (o.shape.kind != SR_SHAPE_MESH || o.mat.normal_texture >= 0) general = true;
     d.general = general ? 1 : 0;
+    d.max_actions = kDefaultMaxActions;
     if (s->has_fog) {
         d.fog_density = s->fog.density;
         d.fog_falloff = s->fog.height_falloff;
@@ -745,6 +746,13 @@ SR_API int sr_scene_bvh_export(SrScene* s, float* node_bounds, int32_t* node_lin
     return SR_OK;
 }
 
+// The scene as a kernel argument: its device description with the tuned traversal cap.
+static DevScene launch_scene(const SrScene* s) {
+    DevScene d = s->dev;
+    if (s->tune.max_actions) d.max_actions = s->tune.max_actions;
+    return d;
+}
+
 static int need_device(SrScene* s) {
     if (!s->built) return fail(SR_ERR_STATE, "Scene not built");
     if (s->ctx->device < 0) return fail(SR_ERR_STATE, "host-only context (device -1) cannot run device work");
@@ -777,7 +785,7 @@ SR_API int sr_scene_trace(SrScene* s, const float* rays, uint32_t count, int32_t
     float* d_dist = (float*)(d_tri + count);
     float* d_uv = d_dist + count;
     SR_CUDA(cudaMemcpyAsync(d_rays, rays, in_b, cudaMemcpyHostToDevice, st), "copy rays");
-    SR_CUDA(launch_trace(s->dev, d_rays, count, d_obj, d_tri, d_dist, d_uv, s->err.as<uint32_t>(), st), "trace launch");
+    SR_CUDA(launch_trace(launch_scene(s), d_rays, count, d_obj, d_tri, d_dist, d_uv, s->err.as<uint32_t>(), st), "trace launch");
     SR_CUDA(cudaMemcpyAsync(out_object, d_obj, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
     SR_CUDA(cudaMemcpyAsync(out_triangle, d_tri, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
     SR_CUDA(cudaMemcpyAsync(out_dist, d_dist, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
@@ -898,7 +906,7 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     std::memset(&L, 0, sizeof(L));  // padding bytes take part in the graph-reuse comparison
     for (int g = 0; g < kWaveGroups; ++g) L.W[g] = s->ws[g];
     L.groups = kWaveGroups;
-    L.S = s->dev;
+    L.S = launch_scene(s);
     L.V = dv;
     L.P = dp;
     L.out = out;
@@ -909,6 +917,7 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     // a runaway guard, not a budget: a pixel's samples run one after another, each taking up to
     // bounces + 2 iterations (the last segment's shadow ray is traced one bounce later)
     uint64_t cap = ((uint64_t)dp.max_samples + 1) * ((uint64_t)dp.bounces + 2) * 2 + 8;
+    if (s->tune.max_iters && s->tune.max_iters < cap) cap = s->tune.max_iters;
     L.max_iters = (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap);
     uint32_t all_slots = 0;
     for (int g = 0; g < kWaveGroups; ++g) all_slots += s->ws[g].slots;
@@ -941,7 +950,8 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
     const size_t count_bytes = kWaveGroups * kWaveCounters * sizeof(uint32_t);
     if (!s->counts_host) SR_CUDA(cudaMallocHost(&s->counts_host, count_bytes), "pinned alloc");
     for (uint32_t it = 0;; ++it) {
-        if (it >= L.max_iters) return fail(SR_ERR_DEVICE, "wavefront loop exceeded %u bounces", L.max_iters);
+        if (it >= L.max_iters)
+            return fail(SR_ERR_DEVICE, "wavefront loop exceeded %u bounces (error word 0x2, loop cap)", L.max_iters);
         int cur = (int)(it & 1u);
         SR_CUDA(wave_bounce(L, cur, st, s->side_streams, s->fork_events), "wavefront bounce");
         SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws[0].counts, count_bytes, cudaMemcpyDeviceToHost, st), "read live count");
@@ -990,7 +1000,7 @@ static int render_into(SrScene* s, const SrView* view, const SrRenderParams* par
     if (mode == SR_RENDER_MEGAKERNEL) {
         DevParams pm = dp;
         pm.seed = s->seed;
-        SR_CUDA(launch_render(s->dev, dv, pm, out, ctr, s->err.as<uint32_t>(), st), "render launch");
+        SR_CUDA(launch_render(launch_scene(s), dv, pm, out, ctr, s->err.as<uint32_t>(), st), "render launch");
     } else if (int rc = render_wavefront(s, dv, dp, out, ctr, st, mode == SR_RENDER_WAVEFRONT_GRAPH)) {
         return rc;
     }
@@ -1089,12 +1099,18 @@ SR_API int sr_scene_set_seed(SrScene* s, uint32_t seed) {
     return SR_OK;
 }
 
+SR_API int sr_scene_get_seed(SrScene* s, uint32_t* seed) {
+    if (!s || !seed) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    *seed = s->seed;
+    return SR_OK;
+}
+
 SR_API int sr_scene_set_tuning(SrScene* s, const SrTuning* t) {
     if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
     if (t && (t->trace_blocks_per_sm < 0 || t->fog_shade_blocks_per_sm < 0 || t->surface_shade_blocks_per_sm < 0))
         return fail(SR_ERR_INVALID_ARG, "blocks per SM must be >= 0");
     s->tune = t ? WaveTune{t->trace_blocks_per_sm, t->fog_shade_blocks_per_sm, t->surface_shade_blocks_per_sm,
-                           t->tail_divisor}
+                           t->tail_divisor, t->max_bounce_iterations, t->max_traversal_steps}
                 : WaveTune{};
     return SR_OK;
 }
@@ -1106,6 +1122,8 @@ SR_API int sr_scene_get_tuning(SrScene* s, SrTuning* t) {
     t->fog_shade_blocks_per_sm = s->tune.fog_per_sm;
     t->surface_shade_blocks_per_sm = s->tune.surface_per_sm;
     t->tail_divisor = s->tune.tail_div;
+    t->max_bounce_iterations = s->tune.max_iters;
+    t->max_traversal_steps = s->tune.max_actions;
     return SR_OK;
 }
 
@@ -1150,7 +1168,7 @@ SR_API int sr_scene_autotune(SrScene* s, const SrView* view, const SrRenderParam
             for (int t = 0; t < 3 && !rc; ++t) {
                 if (trace_c[a] < 0 || fog_c[f] < 0) continue;
                 if ((a > 0 && trace_c[a] < 1) || (f > 0 && fog_c[f] < 1)) continue;
-                s->tune = WaveTune{trace_c[a], fog_c[f], 0, tail_c[t]};
+                s->tune = WaveTune{trace_c[a], fog_c[f], 0, tail_c[t], saved.max_iters, saved.max_actions};
                 rc = render_into(s, view, &p, d, st);  // warm-up (builds the graph)
                 if (!rc) rc = cudaEventRecord(e0, st) == cudaSuccess ? SR_OK : fail(SR_ERR_CUDA, "event");
                 for (int k = 0; k < 2 && !rc; ++k) rc = render_into(s, view, &p, d, st);
@@ -1388,13 +1406,14 @@ SR_API int sr_compose_device_static(SrContext* ctx, const SrAovs* a, uint32_t w,
         return fail(SR_ERR_INVALID_ARG, "denoise radius out of range");
     DevAovs d{a->radiance, a->radiance_fog, a->normals, a->uv, a->depth, a->samples, a->variance};
     size_t needed = 0;
+    bool too_large = false;
     cudaError_t e = launch_compose_static(ctx->device, d, w, h, k, 1.0f / (rp * rp * 2.0f), 1.0f / (rpf * rpf * 2.0f),
-                                          p->denoise_fog_strength, device_rgb8, st, &needed);
-    if (e == cudaErrorInvalidValue)
+                                          p->denoise_fog_strength, device_rgb8, st, &needed, &too_large);
+    if (too_large)
         return fail(SR_ERR_INVALID_ARG,
                     "sr_compose_device_static: a %u-pixel-wide image with filter radius %d needs %zu bytes of "
-                    "scratch per band, more than the fixed 33554432-byte scratch array",
-                    w, k.radius > k.fog_radius ? k.radius : k.fog_radius, needed);
+                    "scratch per band, more than the fixed %zu-byte scratch array",
+                    w, k.radius > k.fog_radius ? k.radius : k.fog_radius, needed, compose_static_capacity());
     SR_CUDA(e, "compose (static scratch)");
     return SR_OK;
 }
@@ -1821,7 +1840,7 @@ SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderPara
     }
     DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
     const bool a = parameter == SR_ADJOINT_ALBEDO, r = parameter == SR_ADJOINT_ROUGHNESS;
-    SR_CUDA(launch_adjoint(s->dev, dv, dp, f, d_image, parameter, a ? texture : -1, a ? grad : nullptr,
+    SR_CUDA(launch_adjoint(launch_scene(s), dv, dp, f, d_image, parameter, a ? texture : -1, a ? grad : nullptr,
                            r ? texture : -1, r ? grad : nullptr, a || r ? nullptr : grad, replay,
                            s->err.as<uint32_t>(), st),
             "adjoint launch");
@@ -1842,7 +1861,7 @@ SR_API int sr_adjoint_all(SrScene* s, const SrView* view, const SrRenderParams* 
     if (fog_density_grad && !s->dev.has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
     if (!albedo_grad && !roughness_grad && !fog_density_grad) return SR_OK;
     DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
-    SR_CUDA(launch_adjoint(s->dev, dv, dp, f, d_image, 3, albedo_grad ? albedo_texture : -1, albedo_grad,
+    SR_CUDA(launch_adjoint(launch_scene(s), dv, dp, f, d_image, 3, albedo_grad ? albedo_texture : -1, albedo_grad,
                            roughness_grad ? roughness_texture : -1, roughness_grad, fog_density_grad, replay,
                            s->err.as<uint32_t>(), st),
             "adjoint launch");

@@ -56,11 +56,14 @@ cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, c
                            float4* scratch, cudaStream_t stream, float* linear = nullptr);
 
 // Compositing that allocates nothing: packed planes live in a fixed device array of sr_compose.cu
-// (bands of rows); spatial weights are evaluated per tap.  Returns cudaErrorInvalidValue when the
-// image is too wide for the array (needed_bytes then holds the size one band would need).
+// (bands of rows); spatial weights are evaluated per tap.  When the image is too wide for the array
+// it launches nothing, sets *too_large and returns cudaErrorInvalidValue (needed_bytes then holds
+// the size one band would need); any other error is a CUDA failure of the lookup or a launch.
 cudaError_t launch_compose_static(int device, const DevAovs& in, uint32_t width, uint32_t height,
                                   const ComposeConsts& k, float rp_inv, float rpf_inv, float fog_strength,
-                                  uint8_t* rgb8, cudaStream_t stream, size_t* needed_bytes);
+                                  uint8_t* rgb8, cudaStream_t stream, size_t* needed_bytes, bool* too_large);
+// Bytes of the fixed array launch_compose_static works in.
+size_t compose_static_capacity();
 
 // AOV visualisation to RGB8 (sr_overlay.cu).  `lut` maps sample counts below lut_n to bytes.
 cudaError_t launch_aov_image(const DevAovs& in, uint32_t n, int32_t kind, float variance_div, const uint8_t* lut,

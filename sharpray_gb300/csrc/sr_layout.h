@@ -28,9 +28,13 @@
 namespace sr {
 
 enum : uint32_t {
-    SR_DEVERR_STACK = 1u,  // traversal stack would exceed 128 entries
-    SR_DEVERR_LOOP = 2u,   // a traversal or shadow loop exceeded its iteration cap
+    SR_DEVERR_STACK = 1u,  // traversal stack would exceed its capacity
+    SR_DEVERR_LOOP = 2u,   // a traversal, shadow or bounce loop exceeded its iteration cap
 };
+// Default cap on the actions (node visits, leaf steps) of one traversal.  A well-formed tree of N
+// nodes needs at most about 2N; the cap turns a malformed tree into an error word instead of a
+// hang.  A scene's tuning can lower it (SrTuning::max_traversal_steps).
+constexpr uint32_t kDefaultMaxActions = 1u << 24;
 
 struct SR_ALIGN16 DevObject {
     float4 pos_kind;    // transform position, shape kind (int bits)
@@ -91,7 +95,8 @@ struct SR_ALIGN16 DevScene {
     int32_t object_count;
     int32_t general;  // needs the general kernels (analytic shapes, transparency, normal maps,
                       // procedural sky); 0 = meshes + texture sky only
-    int32_t pad1[3];
+    uint32_t max_actions;  // cap on the actions of one traversal (kDefaultMaxActions unless tuned)
+    int32_t pad1[2];
     float fog_density, fog_falloff, fog_g, pad;
     float4 fog_color;
 };

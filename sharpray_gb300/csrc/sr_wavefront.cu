@@ -301,6 +301,14 @@ constexpr int kNodeBurst = SR_NODE_BURST;
 #define SR_TRACE_ORDER 5
 #endif
 constexpr int kLeafWait = SR_LEAF_WAIT;
+// Threads per block of the traversal kernel.
+constexpr int kTraceBlock = 128;
+// Traversal stack entries per lane kept in shared memory (0: the whole stack in local memory).
+// Shared words are laid out so that a warp's stack accesses never conflict; each entry costs
+// 12 bytes per thread, 1.5 KB per block.
+#ifndef SR_SMEM_STACK
+#define SR_SMEM_STACK 0
+#endif
 
 // Persistent ray loop: lanes take entries [fetch counter) of the concatenation of two ray queues
 // -- q0 closest-hit queries, q1 occlusion queries -- until both are exhausted; `start(any)` is
@@ -316,7 +324,15 @@ template <bool COUNT, bool GENERAL, typename Start, typename Finish, typename Em
 __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec* q0, uint32_t n0, const Rec* q1,
                                                    uint32_t n1, uint32_t* fetch, Ctr& c, uint32_t* err, Start start,
                                                    Finish finish, Emit emit) {
-    StackEntry stack[kSceneStack];
+#if SR_SMEM_STACK > 0
+    // the first SR_SMEM_STACK entries of every lane's stack in shared memory, the rest local
+    __shared__ uint32_t stack_words[SR_SMEM_STACK * 3 * kTraceBlock];
+    StackEntry entries[kSceneStack - SR_SMEM_STACK];
+    SplitStack<SR_SMEM_STACK, kTraceBlock> stack{stack_words + threadIdx.x, entries};
+#else
+    StackEntry entries[kSceneStack];
+    LocalStack stack{entries};
+#endif
     SceneQuery<false, GENERAL, true> sq;
     const uint32_t n = n0 + n1;
     bool busy = false, pending = false, exhausted = false;
@@ -496,159 +512,205 @@ struct SegOut {
     float nx_t = 0.f;                              // ... and its fog scatter distance
 };
 
-// One segment of path slot s whose event is ev (scene.cs:640-738): first the NEE contribution of
-// the previous segment, then the event's logic; the new path state is stored.
+// The state a path carries from segment to segment (its ray and fog scatter distance, bounce index,
+// flags, accumulated radiance and fog radiance, throughput, last scatter pdf, random numbers), in
+// registers while one shade call runs its segments.
+struct PathRegs {
+    Ray ray;
+    float fog_t;
+    uint32_t bounce, pflags;
+    Col radiance, energy, fog;
+    float spdf;
+    Rng rng;
+};
+
+// A segment of path slot s whose event is ev (scene.cs:640-738), on the path state in p: the
+// event's logic, then the next ray's fog free-flight draw and, when that ray misses the scene's
+// root boxes, its segment's event (o.next).  FOG_OR_MISS = true compiles only what fog scatter
+// and miss events need (the events a chained segment can have: its ray misses the root boxes).
+template <bool COUNT, bool GENERAL, bool FOG_OR_MISS>
+__device__ __forceinline__ SegOut shade_event(const WaveState& W, const DevScene& S, const DevParams& P, uint32_t s,
+                                              int ev, PathRegs& p, Ctr& c) {
+    SegOut o;
+    SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
+    if (p.bounce == 0) SR_COUNT(c, SR_COUNTER_SAMPLE, 1);
+    Ray& ray = p.ray;
+    Col& energy = p.energy;
+    const uint32_t bounce = p.bounce;
+    bool terminate = false;
+    if (ev != EV_MISS) {
+        // Fog and surface events share one light sample, one Russian-roulette draw and then
+        // scatter, in that RNG order (scene.cs:654-726).
+        const bool fog_event = FOG_OR_MISS || ev == EV_FOG;
+        SurfHit sh;
+        if (!fog_event) {
+            const Rec hr = ld_rec(&W.rec[rix(W, s, R_HIT)]);
+            Hit hit{__float_as_int(hr.a.x), __float_as_int(hr.a.y), hr.a.z, hr.a.w, hr.b.x, hr.b.y};
+            surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
+        }
+        const Surface& su = sh.surf;
+        const float dist = sh.dist;
+        const V3 view = -ray.d;
+        float bias = 0.0f;
+        V3 pos;
+        if (fog_event) {
+            energy = energy * col3(S.fog_color);
+            pos = ray_at(ray, p.fog_t);  // the fog scatter distance
+        } else {
+            bias = fmaxf(1e-4f, dist * 1e-4f);
+            pos = ray_at(ray, dist - bias);
+            if (GENERAL && (p.pflags & PF_MEDIUM)) energy = energy * beer_law(col3(W.medium[s]), dist);
+            p.radiance = p.radiance + su.radiance * energy;
+            if (bounce == 0) {
+                p.pflags |= PF_PRIMARY;
+                st_rec(&W.pix[pix(W, s, X_PRIM)], Rec{make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
+                                                     make_float4(su.uv.x, su.uv.y, 0.f, 0.f)});
+            }
+        }
+        // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
+        // a shadow ray that needs a traversal goes to the shadow kernel and its contribution is
+        // added next segment (before anything of that segment touches the radiance)
+        V3 ldir;
+        float lpdf;
+        int texel;
+        if (sky_light_rand<COUNT, GENERAL>(S, p.rng, ldir, lpdf, texel, c) && lpdf > 0.0f) {
+            bool emit = true;
+            Col w3;
+            float mis;
+            if (fog_event) {
+                float fog_pdf = hg_pdf(dot(ray.d, ldir), S.fog_g);
+                mis = power_heuristic(lpdf, fog_pdf);
+                w3 = gray(fog_pdf);
+            } else {
+                V3 nn = dot(su.normal, view) >= 0.0f ? su.normal : -su.normal;
+                V3 ng = dot(su.normal_geo, view) >= 0.0f ? su.normal_geo : -su.normal_geo;
+                emit = dot(nn, ldir) > 0.0f && dot(ng, ldir) > 0.0f;
+                if (emit) {
+                    w3 = opaque_eval(su, view, ldir);
+                    mis = power_heuristic(lpdf, opaque_pdf(su, view, ldir, specular_probability(su, view)));
+                }
+            }
+            if (emit) {
+                const bool to_fog = fog_event && bounce == 0;
+                Ray shadow = make_ray(pos, ldir);
+                const bool any = !GENERAL || !S.has_transparent;
+                if (any ? misses_scene<COUNT, true>(S, shadow, c) : misses_scene<COUNT, false>(S, shadow, c)) {
+                    // a shadow ray that misses the scene's root boxes is unoccluded: its
+                    // transmittance is the fog's alone, and the light sample's contribution is
+                    // added at once, as SampleSkyDirect(Fog) forms it
+                    SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
+                    float t = 1.0f;
+                    if (S.has_fog) t = 1.0f * fog_transmittance_inf(S, shadow);
+                    Col tr = gray(t);
+                    if (max_component(tr) > 0.0f) {
+                        Col contrib = sky_light_radiance<COUNT, GENERAL>(S, texel, ldir, c) * tr * w3 * mis / lpdf;
+                        Col add = contrib * energy;
+                        if (to_fog)
+                            p.fog = p.fog + add;
+                        else
+                            p.radiance = p.radiance + add;
+                    }
+                } else {
+                    // traced by the shadow kernel; the contribution is added next segment
+                    p.pflags |= PF_NEE | (to_fog ? PF_NEE_FOG : 0u);
+                    o.shadow = true;
+                    o.sh_o = pos;
+                    o.sh_d = ldir;
+                    st_rec(&W.rec[rix(W, s, R_SH0)], Rec{make_float4(pos.x, pos.y, pos.z, 0.f),
+                                                      make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
+                    st_rec(&W.rec[rix(W, s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
+                                                      make_float4(energy.r, energy.g, energy.b, __int_as_float(texel))});
+                }
+            }
+        }
+        if (russian_roulette(energy, bounce, p.rng)) {
+            terminate = true;
+        } else if (fog_event) {
+            V3 sdir = hg_scatter_dir(ray.d, S.fog_g, p.rng);
+            p.pflags |= PF_SPDF;
+            p.spdf = hg_pdf(dot(ray.d, sdir), S.fog_g);
+            ray = make_ray(pos, sdir);
+        } else {
+            Scatter sc = surface_scatter<GENERAL>(su, ray.d, view, p.rng);
+            energy = energy * sc.weight;
+            energy = clamp_luminance(energy, P.indirect_clamp);
+            bool enter = dot(sc.dir, su.normal_geo) < 0.0f;
+            if (GENERAL && sc.refracted) {
+                if (enter) {
+                    p.pflags |= PF_MEDIUM;
+                    W.medium[s] = make_float4(su.albedo.r, su.albedo.g, su.albedo.b, 0.f);
+                } else {
+                    p.pflags &= ~PF_MEDIUM;
+                }
+            } else if (!enter) {
+                p.pflags &= ~PF_MEDIUM;
+            }
+            p.pflags = sc.has_pdf ? (p.pflags | PF_SPDF) : (p.pflags & ~PF_SPDF);
+            p.spdf = sc.pdf;
+            ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
+        }
+    } else {
+        // miss: sky radiance with the MIS weight of the last scatter (scene.cs:728-738)
+        float mis = (p.pflags & PF_SPDF) ? power_heuristic(p.spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
+        p.radiance = p.radiance + sky_radiance<COUNT, GENERAL>(S, ray.d, c) * mis * energy;
+        terminate = true;
+    }
+    if (!terminate && ++p.bounce == P.bounces + 1) terminate = true;
+    o.live = !terminate;
+    if (o.live) {
+        // the next segment's fog free-flight draw: the reference makes it right after the
+        // traversal, which draws nothing, so drawing it now keeps the RNG sequence
+        p.fog_t = fog_scatter_t(S, ray, p.rng);
+        o.next = next_segment<COUNT>(S, ray, p.fog_t, c);
+        o.nx_o = ray.o;
+        o.nx_d = ray.d;
+        o.nx_t = p.fog_t;
+    }
+    return o;
+}
+
+// Segments of a path whose next event is already known run back to back (SR_CHAIN_SEGMENTS = 1):
+// while a segment's new ray misses the scene's root boxes (its event is a fog scatter or a miss,
+// decided on the spot) and no shadow ray waits for a traversal, the same shade call goes on with
+// the next segment, with the path state in registers, instead of storing it and queueing the
+// slot for the next bounce.  In foggy scenes most segments scatter far outside the scene, so
+// runs of such segments are common.  Each path's operations and their order are unchanged, so
+// images are identical either way; only the records stored and the bounces run change.
+#ifndef SR_CHAIN_SEGMENTS
+#define SR_CHAIN_SEGMENTS 1
+#endif
+
+// Path slot s from its stored state through its segment with event ev -- first the NEE
+// contribution of the previous segment if its shadow ray was traced since -- and, chaining, the
+// segments after it that need no traversal; then the new path state is stored.
 template <bool COUNT, bool GENERAL>
 __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevScene& S, const DevParams& P, uint32_t s,
                                                 int ev, Ctr& c) {
-    SegOut o;
-        SR_COUNT(c, SR_COUNTER_SAMPLE_BOUNCE, 1);
-        Rec rr = ld_rec(&W.rec[rix(W, s, R_RAY)]), pr = ld_rec(&W.rec[rix(W, s, R_PATH)]), gr = ld_rec(&W.rec[rix(W, s, R_RNG)]);
-        Rng rng = rng_of(gr);
-        Col fog{gr.b.y, gr.b.z, gr.b.w};
-        uint32_t bounce = ibits(rr.a.w);
-        uint32_t pflags = ibits(pr.b.w);
-        if (bounce == 0) SR_COUNT(c, SR_COUNTER_SAMPLE, 1);
-        Ray ray = make_ray(V3{rr.a.x, rr.a.y, rr.a.z}, V3{rr.b.x, rr.b.y, rr.b.z});
-        Col radiance = col3(pr.a);
-        float spdf = pr.a.w;
-        Col energy = col3(pr.b);
-        if (pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, pflags, radiance, fog, c);
-        pflags &= ~(PF_NEE | PF_NEE_FOG);
-        bool terminate = false;
-        if (ev != EV_MISS) {
-            // Fog and surface events share one light sample, one Russian-roulette draw and then
-            // scatter, in that RNG order (scene.cs:654-726).
-            const bool fog_event = ev == EV_FOG;
-            SurfHit sh;
-            if (!fog_event) {
-                const Rec hr = ld_rec(&W.rec[rix(W, s, R_HIT)]);
-                Hit hit{__float_as_int(hr.a.x), __float_as_int(hr.a.y), hr.a.z, hr.a.w, hr.b.x, hr.b.y};
-                surface_from_hit<COUNT, GENERAL>(S, ray, hit, sh, c);
-            }
-            const Surface& su = sh.surf;
-            const float dist = sh.dist;
-            const V3 view = -ray.d;
-            float bias = 0.0f;
-            V3 pos;
-            if (fog_event) {
-                energy = energy * col3(S.fog_color);
-                pos = ray_at(ray, rr.b.w);  // the fog scatter distance
-            } else {
-                bias = fmaxf(1e-4f, dist * 1e-4f);
-                pos = ray_at(ray, dist - bias);
-                if (GENERAL && (pflags & PF_MEDIUM)) energy = energy * beer_law(col3(W.medium[s]), dist);
-                radiance = radiance + su.radiance * energy;
-                if (bounce == 0) {
-                    pflags |= PF_PRIMARY;
-                    st_rec(&W.pix[pix(W, s, X_PRIM)], Rec{make_float4(su.normal.x, su.normal.y, su.normal.z, dist),
-                                 make_float4(su.uv.x, su.uv.y, 0.f, 0.f)});
-                }
-            }
-            // NEE toward the sky (SampleSkyDirectFog scene.cs:796-810 / SampleSkyDirect :774-794);
-            // a shadow ray that needs a traversal goes to the shadow kernel and its contribution is
-            // added next segment (before anything of that segment touches the radiance)
-            V3 ldir;
-            float lpdf;
-            int texel;
-            if (sky_light_rand<COUNT, GENERAL>(S, rng, ldir, lpdf, texel, c) && lpdf > 0.0f) {
-                bool emit = true;
-                Col w3;
-                float mis;
-                if (fog_event) {
-                    float fog_pdf = hg_pdf(dot(ray.d, ldir), S.fog_g);
-                    mis = power_heuristic(lpdf, fog_pdf);
-                    w3 = gray(fog_pdf);
-                } else {
-                    V3 nn = dot(su.normal, view) >= 0.0f ? su.normal : -su.normal;
-                    V3 ng = dot(su.normal_geo, view) >= 0.0f ? su.normal_geo : -su.normal_geo;
-                    emit = dot(nn, ldir) > 0.0f && dot(ng, ldir) > 0.0f;
-                    if (emit) {
-                        w3 = opaque_eval(su, view, ldir);
-                        mis = power_heuristic(lpdf, opaque_pdf(su, view, ldir, specular_probability(su, view)));
-                    }
-                }
-                if (emit) {
-                    const bool to_fog = fog_event && bounce == 0;
-                    Ray shadow = make_ray(pos, ldir);
-                    const bool any = !GENERAL || !S.has_transparent;
-                    if (any ? misses_scene<COUNT, true>(S, shadow, c) : misses_scene<COUNT, false>(S, shadow, c)) {
-                        // a shadow ray that misses the scene's root boxes is unoccluded: its
-                        // transmittance is the fog's alone, and the light sample's contribution is
-                        // added at once, as SampleSkyDirect(Fog) forms it
-                        SR_COUNT(c, SR_COUNTER_SCENE_OCCLUDE, 1);
-                        float t = 1.0f;
-                        if (S.has_fog) t = 1.0f * fog_transmittance_inf(S, shadow);
-                        Col tr = gray(t);
-                        if (max_component(tr) > 0.0f) {
-                            Col contrib = sky_light_radiance<COUNT, GENERAL>(S, texel, ldir, c) * tr * w3 * mis / lpdf;
-                            Col add = contrib * energy;
-                            if (to_fog)
-                                fog = fog + add;
-                            else
-                                radiance = radiance + add;
-                        }
-                    } else {
-                        // traced by the shadow kernel; the contribution is added next segment
-                        pflags |= PF_NEE | (to_fog ? PF_NEE_FOG : 0u);
-                        o.shadow = true;
-                        o.sh_o = pos;
-                        o.sh_d = ldir;
-                        st_rec(&W.rec[rix(W, s, R_SH0)], Rec{make_float4(pos.x, pos.y, pos.z, 0.f),
-                                                          make_float4(ldir.x, ldir.y, ldir.z, lpdf)});
-                        st_rec(&W.rec[rix(W, s, R_SH1)], Rec{make_float4(w3.r, w3.g, w3.b, mis),
-                                                          make_float4(energy.r, energy.g, energy.b, __int_as_float(texel))});
-                    }
-                }
-            }
-            if (russian_roulette(energy, bounce, rng)) {
-                terminate = true;
-            } else if (fog_event) {
-                V3 sdir = hg_scatter_dir(ray.d, S.fog_g, rng);
-                pflags |= PF_SPDF;
-                spdf = hg_pdf(dot(ray.d, sdir), S.fog_g);
-                ray = make_ray(pos, sdir);
-            } else {
-                Scatter sc = surface_scatter<GENERAL>(su, ray.d, view, rng);
-                energy = energy * sc.weight;
-                energy = clamp_luminance(energy, P.indirect_clamp);
-                bool enter = dot(sc.dir, su.normal_geo) < 0.0f;
-                if (GENERAL && sc.refracted) {
-                    if (enter) {
-                        pflags |= PF_MEDIUM;
-                        W.medium[s] = make_float4(su.albedo.r, su.albedo.g, su.albedo.b, 0.f);
-                    } else {
-                        pflags &= ~PF_MEDIUM;
-                    }
-                } else if (!enter) {
-                    pflags &= ~PF_MEDIUM;
-                }
-                pflags = sc.has_pdf ? (pflags | PF_SPDF) : (pflags & ~PF_SPDF);
-                spdf = sc.pdf;
-                ray = make_ray(ray_at(ray, dist) + sc.dir * bias, sc.dir);
-            }
-        } else {
-            // miss: sky radiance with the MIS weight of the last scatter (scene.cs:728-738)
-            float mis = (pflags & PF_SPDF) ? power_heuristic(spdf, sky_light_pdf<GENERAL>(S, ray.d)) : 1.0f;
-            radiance = radiance + sky_radiance<COUNT, GENERAL>(S, ray.d, c) * mis * energy;
-            terminate = true;
-        }
-        if (!terminate && ++bounce == P.bounces + 1) terminate = true;
-        o.live = !terminate;
-        st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(radiance.r, radiance.g, radiance.b, spdf),
-                     make_float4(energy.r, energy.g, energy.b, fbits(pflags))});
-        if (o.live) {
-            // the next segment's fog free-flight draw: the reference makes it right after the
-            // traversal, which draws nothing, so drawing it now keeps the RNG sequence
-            const float ft = fog_scatter_t(S, ray, rng);
-            o.next = next_segment<COUNT>(S, ray, ft, c);
-            o.nx_o = ray.o;
-            o.nx_d = ray.d;
-            o.nx_t = ft;
-            st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(bounce)),
-                                              make_float4(ray.d.x, ray.d.y, ray.d.z, ft)});
-        }
-        st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, fog));
+    const Rec rr = ld_rec(&W.rec[rix(W, s, R_RAY)]), pr = ld_rec(&W.rec[rix(W, s, R_PATH)]),
+              gr = ld_rec(&W.rec[rix(W, s, R_RNG)]);
+    PathRegs p;
+    p.rng = rng_of(gr);
+    p.fog = Col{gr.b.y, gr.b.z, gr.b.w};
+    p.bounce = ibits(rr.a.w);
+    p.pflags = ibits(pr.b.w);
+    p.ray = make_ray(V3{rr.a.x, rr.a.y, rr.a.z}, V3{rr.b.x, rr.b.y, rr.b.z});
+    p.fog_t = rr.b.w;
+    p.radiance = col3(pr.a);
+    p.spdf = pr.a.w;
+    p.energy = col3(pr.b);
+    if (p.pflags & PF_NEE) add_nee<COUNT, GENERAL>(W, S, s, p.pflags, p.radiance, p.fog, c);
+    p.pflags &= ~(PF_NEE | PF_NEE_FOG);
+    SegOut o = shade_event<COUNT, GENERAL, false>(W, S, P, s, ev, p, c);
+    if (SR_CHAIN_SEGMENTS) {
+        // at most bounces + 1 segments per sample: every segment advances the bounce index
+        while (o.live && !o.shadow && o.next >= 0) o = shade_event<COUNT, GENERAL, true>(W, S, P, s, o.next, p, c);
+    }
+    st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(p.radiance.r, p.radiance.g, p.radiance.b, p.spdf),
+                                          make_float4(p.energy.r, p.energy.g, p.energy.b, fbits(p.pflags))});
+    if (o.live)
+        st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(p.ray.o.x, p.ray.o.y, p.ray.o.z, fbits(p.bounce)),
+                                             make_float4(p.ray.d.x, p.ray.d.y, p.ray.d.z, p.fog_t)});
+    st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(p.rng, p.fog));
     return o;
 }
 

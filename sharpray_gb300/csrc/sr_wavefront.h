@@ -143,6 +143,8 @@ struct WaveTune {
     int fog_per_sm;       // fog-event shade kernel
     int surface_per_sm;   // surface-event shade kernel
     uint32_t tail_div;    // the tail kernel takes over at slots / tail_div live paths (0 = SR_TAIL_DIV)
+    uint32_t max_iters;   // bounce-loop cap (0 = the runaway guard)
+    uint32_t max_actions; // per-traversal action cap (0 = kDefaultMaxActions)
 };
 // Resident blocks per SM of the traversal, fog-shade and surface-shade kernels.
 void wave_occupancy(bool general, int* trace, int* fog, int* surface);

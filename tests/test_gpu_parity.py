@@ -255,9 +255,13 @@ def test_adaptive_sampling_wavefront(built, oracle_mod):
     args = (d.width, d.height, 32, 2, 16, 0.2, 4, 10.0)
     rend = Renderer(g, d.view, *args)
     ref, _ = o.render(d.view.to_c(), render_params(*args))
-    assert (rend.samples == ref.samples).mean() >= 0.97
+    assert (rend.samples == ref.samples).mean() >= 0.995
     assert rend.samples.min() >= 2 and rend.samples.max() <= 17
     assert len(np.unique(rend.samples)) > 2, "threshold should stop some pixels early"
     tot, tref = rend.radiance + rend.radiance_fog, ref.radiance + ref.radiance_fog
     err = np.abs(tot - tref).max(axis=1) / np.maximum(np.abs(tref).max(axis=1), 1e-3)
-    assert (err < 1e-3).mean() >= 0.95
+    # the project's image bar: a pixel whose stop decision differs shows up here as well
+    frac = float((err < 1e-3).mean())
+    assert frac >= 0.995, f"only {frac:.4f} of pixels within 1e-3 ({(rend.samples != ref.samples).sum()} pixels " \
+                          f"stopped after a different sample count)"
+    assert rel_mse(tot, tref) < 1e-4

@@ -156,8 +156,24 @@ def test_progress_adjoint_and_update_validation(host_ctx):
     assert s.seed == 0
     s.set_seed(9)
     assert s.seed == 9
+    # the getter reads the C scene, so a direct call through the ABI is seen too
+    _abi.check(lib.sr_scene_set_seed(s.handle, 0xFFFFFFFF))
+    assert s.get_seed() == 0xFFFFFFFF
+    for bad in (-1, 1 << 32):
+        with pytest.raises(ValueError):
+            s.set_seed(bad)
+    assert s.get_seed() == 0xFFFFFFFF
+    s.set_seed(0)
     with pytest.raises(SharpRayError):
         _abi.check(lib.sr_scene_set_seed(None, 1))
+    with pytest.raises(SharpRayError):
+        _abi.check(lib.sr_scene_get_seed(s.handle, None))
+    # loop caps round-trip through the tuning (the renders that hit them are GPU tests)
+    s.set_tuning(max_bounce_iterations=6, max_traversal_steps=40)
+    t = s.get_tuning()
+    assert (t["max_bounce_iterations"], t["max_traversal_steps"]) == (6, 40)
+    s.set_tuning()
+    assert s.get_tuning()["max_traversal_steps"] == 0
     d, t = C.c_uint32(), C.c_uint32()
     with pytest.raises(SharpRayError):
         _abi.check(lib.sr_render_progress(s.handle, None, C.byref(t)))
