@@ -74,6 +74,8 @@ def lib():
             "oracle_denoise": (None, [C.POINTER(SrAovs), U, U, C.POINTER(SrComposeParams), P, C.c_int32]),
             "oracle_aov_image": (None, [C.POINTER(SrAovs), U, U, C.c_int32, C.POINTER(SrAovImageParams), P]),
             "oracle_overlay_draw": (I, [P, U, U, C.POINTER(SrView), P, P, U, P, U, C.POINTER(SrFont)]),
+            "oracle_adjoint": (I, [P, C.POINTER(SrView), C.POINTER(SrRenderParams), C.c_int32, P, P, C.c_int32, P,
+                                   C.c_int32, P, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -175,6 +177,24 @@ class OracleScene:
         uv = np.empty((n, 2), np.float32)
         self.L.oracle_scene_trace(self.h, _p(r), n, _p(obj), _p(tri), _p(dist), _p(uv), threads or os.cpu_count())
         return {"object": obj, "triangle": tri, "dist": dist, "uv": uv}
+
+    def adjoint(self, view: SrView, params: SrRenderParams, d_image: np.ndarray, samples: np.ndarray,
+                tex_albedo: int = -1, albedo_shape=None, tex_roughness: int = -1, roughness_shape=None,
+                threads: int = 0):
+        """FP64 path-replay adjoint (oracle_adjoint): for dL/dI = d_image (h x w x 3) and the forward
+        render's sample counts, returns (dL/d albedo texels (th, tw, 3) or None, dL/d roughness texels
+        (th, tw, 3; channel 0) or None, dL/d fog density, replayed image (h*w, 3)), all in double."""
+        d = np.ascontiguousarray(d_image, np.float32).reshape(-1)
+        smp = np.ascontiguousarray(samples, np.uint32).reshape(-1)
+        ga = np.zeros((*albedo_shape, 3), np.float64) if tex_albedo >= 0 else None
+        gr = np.zeros((*roughness_shape, 3), np.float64) if tex_roughness >= 0 else None
+        gf = np.zeros(1, np.float64)
+        rep = np.zeros((params.width * params.height, 3), np.float32)
+        rc = self.L.oracle_adjoint(self.h, C.byref(view), C.byref(params), threads or os.cpu_count(), _p(d), _p(smp),
+                                   tex_albedo, _p(ga), tex_roughness, _p(gr), _p(gf), _p(rep))
+        if rc:
+            raise RuntimeError(self.L.oracle_last_error().decode())
+        return ga, gr, float(gf[0]), rep
 
     def render(self, view: SrView, params: SrRenderParams, threads: int = 0, rows=None, counters: bool = False):
         """AOV planes of rows [y0, y1) (others stay zero) and optionally the work counters."""

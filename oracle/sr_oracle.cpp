@@ -1277,11 +1277,12 @@ struct Scene {
     }
 
     // Scene.Trace scene.cs:602-625.
-    bool trace(const Ray& ray, SurfaceHit* out, Counters* ctr) const {
+    bool trace(const Ray& ray, SurfaceHit* out, Counters* ctr, int* obj_out = nullptr) const {
         if (ctr) ctr->add(SR_COUNTER_SCENE_TRACE);
         ShapeHit hit;
         int idx, tri;
         if (!intersect(ray, &hit, &idx, &tri, ctr)) return false;
+        if (obj_out) *obj_out = idx;
         const Material& mat = objects[idx].mat;
         Col albedo = sample_albedo(mat, hit.uv, ctr);
         const Texture* rt = tex(mat.rough_tex);
@@ -1655,6 +1656,397 @@ void parallel_for(int n, int threads, Fn fn) {
             }
         });
     for (auto& th : pool) th.join();
+}
+
+// ---- FP64 path-replay adjoint ------------------------------------------------------------------
+//
+// The double-precision reference for the GPU's path-replay adjoint.  The reference renderer has no
+// derivatives; this restates the replay estimator of dL/dθ, for θ = the texels of an albedo texture,
+// the texels of a roughness texture (its red channel) and the fog density, given dL/dI for the
+// image I = radiance + radiance_fog.  Paths are replayed in float with the reference's arithmetic --
+// the same random numbers and the same paths as Scene::sample -- while every derivative is taken in
+// double by forward-mode dual numbers through the reference's formulas: OpaqueEval (scene.cs:76-101
+// with brdf.cs:12-57), the fog's optical depth and free-flight density (scene.cs:445-496),
+// ClampLuminance (math.cs:121-125) and RussianRoulette (scene.cs:744-756).  The chain from the
+// camera to every vertex runs backwards in double.  Held fixed, as path replay does: the sampled
+// directions, lobe choices, roulette decisions, pdfs and MIS weights.  The free-flight sampling of
+// every segment contributes the score d log p / d density of its sampled event (a scatter at t,
+// reaching a surface, or escaping to the sky).  Scenes with transparent materials are not covered
+// (the GPU adjoint refuses them).
+
+struct Dual {
+    double v, d;
+};
+inline Dual dual(double v, double d = 0.0) { return {v, d}; }
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+inline Dual dexp(Dual a) {
+    double e = std::exp(a.v);
+    return {e, a.d * e};
+}
+inline Dual dlog(Dual a) { return {std::log(a.v), a.d / a.v}; }
+struct DCol {
+    Dual c[3];
+};
+inline DCol dcol(Col x) { return {{dual(x.r), dual(x.g), dual(x.b)}}; }
+inline double cval(Col x, int i) { return i == 0 ? x.r : (i == 1 ? x.g : x.b); }
+
+struct V3d {
+    double x, y, z;
+};
+inline V3d v3d(V3 v) { return {v.x, v.y, v.z}; }
+inline double dotd(V3d a, V3d b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3d normalize_or_d(V3d v, V3d fb) {
+    double m = dotd(v, v);
+    if (!(m >= 1e-12)) return fb;
+    double k = 1.0 / std::sqrt(m);
+    return {v.x * k, v.y * k, v.z * k};
+}
+
+// Brdf.Fresnel, GgxD, SmithG1 (brdf.cs:22-57) over duals.
+inline Dual fresnel_dual(double n_dot_v, Dual base) {
+    double x = 1.0 - n_dot_v;
+    double x5 = x * x * x * x * x;
+    return base + (dual(1.0) - base) * dual(x5);
+}
+inline Dual ggx_d_dual(double n_dot_h, Dual rs) {
+    Dual a2 = rs * rs;
+    double nh2 = n_dot_h * n_dot_h;
+    Dual d = dual(1.0 - nh2) + dual(nh2) * a2;
+    return a2 / (dual(M_PI) * d * d);
+}
+inline Dual smith_g1_dual(double n_dot_x, Dual rs) {
+    Dual k = rs / dual(2.0);
+    return dual(n_dot_x) / (dual(n_dot_x) * (dual(1.0) - k) + k);
+}
+
+// Surface.OpaqueEval (scene.cs:76-101) in double over a dual albedo and roughness; the branch
+// decisions (light behind the surface, the roughness floor) are the float surface's.
+DCol opaque_eval_dual(const Surface& s, V3 view, V3 light, const DCol& albedo, Dual roughness) {
+    DCol out{{dual(0), dual(0), dual(0)}};
+    if (dot(s.normal, light) <= 0.0f) return out;
+    const V3d n = v3d(s.normal), v = v3d(view), l = v3d(light);
+    const double n_dot_l = dotd(n, l);
+    const double n_dot_v = std::max(1e-4, dotd(n, v));
+    Dual r2 = roughness * roughness;
+    Dual rs = s.roughness * s.roughness > 1e-4f ? r2 : dual(1e-4);
+    const double f0 = std::pow(((double)s.ior - 1.0) / ((double)s.ior + 1.0), 2.0);
+    const V3d half = normalize_or_d({v.x + l.x, v.y + l.y, v.z + l.z}, n);
+    const double n_dot_h = dotd(n, half), h_dot_v = dotd(half, v);
+    Dual g = smith_g1_dual(n_dot_v, rs) * smith_g1_dual(n_dot_l, rs);
+    Dual dterm = ggx_d_dual(n_dot_h, rs) * g / dual(4.0 * n_dot_v);
+    const double m = s.metallic, tr = 1.0 - (double)s.transparency;
+    for (int i = 0; i < 3; ++i) {
+        Dual base = dual(f0) + (albedo.c[i] - dual(f0)) * dual(m);  // Color.Lerp(f0, albedo, metallic)
+        Dual spec = dterm * fresnel_dual(h_dot_v, base);
+        Dual diff = (dual(1.0) - fresnel_dual(n_dot_v, base)) * albedo.c[i] * dual((1.0 - m) * (n_dot_l / M_PI));
+        out.c[i] = (spec + diff) * dual(tr);
+    }
+    return out;
+}
+
+// Fog.OpticalDepth (scene.cs:452-467) over [start, end] in double with a dual density.
+Dual optical_depth_dual(const Fog& f, const Ray& r, double start, double end, Dual density) {
+    const double hd = r.dir.y, ho = r.origin.y, k = f.height_falloff;
+    const double hs = ho + start * hd;
+    const double es = std::exp(-k * hs);
+    if (std::fabs(r.dir.y) < 1e-6f) return density * dual(es * (end - start));
+    const double ee = std::isinf(end) ? (end * hd > 0 ? 0.0 : INFINITY) : std::exp(-k * (ho + end * hd));
+    return density * dual((es - ee) / (k * hd));
+}
+
+// Albedo + roughness derivatives of one BRDF evaluation: d eval / d albedo (channel i only moves
+// channel i of eval: this takes the diagonal) and d eval / d roughness, both in double.
+void eval_derivatives(const Surface& s, V3 view, V3 light, double d_alb[3], double d_rough[3]) {
+    for (int i = 0; i < 3; ++i) {
+        DCol a = dcol(s.albedo);
+        a.c[i].d = 1.0;
+        d_alb[i] = opaque_eval_dual(s, view, light, a, dual(s.roughness)).c[i].d;
+    }
+    DCol e = opaque_eval_dual(s, view, light, dcol(s.albedo), dual(s.roughness, 1.0));
+    for (int i = 0; i < 3; ++i) d_rough[i] = e.c[i].d;
+}
+
+enum { AJ_FOG = 0, AJ_SURF = 1, AJ_SURF_END = 2, AJ_SKY = 3, AJ_FOG_END = 4 };
+struct AdjVertex64 {
+    int kind;
+    uint32_t bounce;
+    Col e_in;       // throughput entering the vertex (float, as the forward has it)
+    Col s;          // scatter weight (surface)
+    double add[3];  // radiance added per unit throughput
+    double dadd_a[3], dadd_r[3], dadd_f[3];  // d add / d albedo channel, d roughness, d density
+    double ds_a[3], ds_r[3];                 // d s / d albedo channel, d roughness
+    double score;   // d log(density of the sampled segment into the vertex) / d fog density
+    float clamp_max;
+    V2 uv;
+    int object;
+};
+
+// Scene.RussianRoulette's division (scene.cs:744-756) over duals: x / min(1, max component of x)
+// from bounce 3 on; the survival value's branch is the float forward's.
+inline DCol roulette_dual(const DCol& x, Col xf, uint32_t bounce) {
+    if (bounce < 3) return x;
+    float p = net_min(1.0f, max_component(xf));
+    if (!(p < 1.0f)) return x;
+    const int m = (xf.r >= xf.g && xf.r >= xf.b) ? 0 : (xf.g >= xf.b ? 1 : 2);
+    Dual pd = x.c[m];
+    return {{x.c[0] / pd, x.c[1] / pd, x.c[2] / pd}};
+}
+// Color.ClampLuminance (math.cs:121-125) over duals; the branch is the float forward's.
+inline DCol clamp_dual(const DCol& x, Col xf, float max) {
+    if (!(luminance(xf) > max)) return x;
+    Dual lum = dual(0.2126) * x.c[0] + dual(0.7152) * x.c[1] + dual(0.0722) * x.c[2];
+    Dual k = dual(max) / lum;
+    return {{x.c[0] * k, x.c[1] * k, x.c[2] * k}};
+}
+
+struct Adjoint64 {
+    const Scene& sc;
+    Dual density;  // the fog density, as a dual seeded 1 (d / d density)
+
+    // d log p / d density of a segment's free flight (scene.cs:469-496 samples t with density
+    // sigma(t) exp(-tau(0, t))): a scatter at t, or no scatter before `end` (a surface or the sky).
+    double score_scatter(const Ray& r, float t) const {
+        const double y = r.origin.y + (double)t * r.dir.y;
+        Dual log_sigma = dlog(density) - dual(sc.fog.height_falloff * y);
+        return (log_sigma - optical_depth_dual(sc.fog, r, 0.0, t, density)).d;
+    }
+    double score_pass(const Ray& r, double end) const {
+        Dual tau = optical_depth_dual(sc.fog, r, 0.0, end, density);
+        return std::isfinite(tau.v) ? -tau.d : 0.0;
+    }
+    // d/d density of the shadow ray's fog transmittance exp(-tau(0, inf)), relative to its value.
+    double transmittance_log_derivative(const Ray& shadow) const {
+        Dual tau = optical_depth_dual(sc.fog, shadow, 0.0, INFINITY, density);
+        return std::isfinite(tau.v) ? -tau.d : 0.0;
+    }
+
+    // Scene::sample replayed, recording the vertices (returns their number); the float arithmetic
+    // and RNG draws are sample()'s, so radiance / radiance_fog come out the same.
+    int replay(Ray ray, Rng& rng, uint32_t bounces, float indirect_clamp, AdjVertex64* v, Col& radiance,
+               Col& radiance_fog) const {
+        radiance = kBlack;
+        radiance_fog = kBlack;
+        Col energy = kWhite;
+        bool has_scatter_pdf = false;
+        float scatter_pdf = 0.0f;
+        int n = 0;
+        for (uint32_t i = 0; i != bounces + 1; ++i) {
+            SurfaceHit hit;
+            int obj = -1;
+            bool has_hit = sc.trace(ray, &hit, nullptr, &obj);
+            float scatter_dist;
+            AdjVertex64& x = v[n++];
+            x = AdjVertex64{};
+            x.bounce = i;
+            x.e_in = energy;
+            x.clamp_max = indirect_clamp;
+            if (sc.has_fog && sc.fog.scatter_distance(ray, 0.0f, has_hit ? hit.dist : kInf, rng, &scatter_dist)) {
+                x.kind = AJ_FOG;
+                x.score = score_scatter(ray, scatter_dist);
+                energy = energy * sc.fog.color;
+                // Scene.SampleSkyDirectFog scene.cs:796-810
+                V3 pos = ray_at(ray, scatter_dist);
+                Col nee = kBlack;
+                SampleLight light;
+                Col tr;
+                if (sc.sample_sky_light(pos, rng, &light, &tr, nullptr)) {
+                    float fog_pdf = hg_pdf(dot(ray.dir, light.dir), sc.fog.anisotropy);
+                    float mis = power_heuristic(light.pdf, fog_pdf);
+                    nee = sc.sky.radiance(light.dir, nullptr) * tr * fog_pdf * mis / light.pdf;
+                    const double dl = transmittance_log_derivative(make_ray(pos, light.dir));
+                    for (int c = 0; c < 3; ++c) x.dadd_f[c] = cval(nee, c) * dl;
+                }
+                for (int c = 0; c < 3; ++c) x.add[c] = cval(nee, c);
+                Col scatter_rad = nee * energy;
+                if (i == 0)
+                    radiance_fog = radiance_fog + scatter_rad;
+                else
+                    radiance = radiance + scatter_rad;
+                if (Scene::russian_roulette(energy, i, rng)) {
+                    x.kind = AJ_FOG_END;
+                    break;
+                }
+                V3 sdir = hg_scatter_dir(ray.dir, sc.fog.anisotropy, rng);
+                has_scatter_pdf = true;
+                scatter_pdf = hg_pdf(dot(ray.dir, sdir), sc.fog.anisotropy);
+                ray = make_ray(ray_at(ray, scatter_dist), sdir);
+            } else if (has_hit) {
+                const Surface& surf = hit.surf;
+                float dist = hit.dist;
+                V3 view = -ray.dir;
+                float dist_bias = net_max(1e-4f, dist * 1e-4f);
+                V3 hit_pos = ray_at(ray, dist - dist_bias);
+                x.kind = AJ_SURF;
+                x.uv = surf.uv;
+                x.object = obj;
+                if (sc.has_fog) x.score = score_pass(ray, dist);
+                radiance = radiance + surf.radiance * energy;
+                // Scene.SampleSkyDirect scene.cs:774-794
+                Col nee = kBlack;
+                SampleLight light;
+                Col tr;
+                if (sc.sample_sky_light(hit_pos, rng, &light, &tr, nullptr)) {
+                    V3 nn = dot(surf.normal, view) >= 0.0f ? surf.normal : -surf.normal;
+                    V3 ng = dot(surf.normal_geo, view) >= 0.0f ? surf.normal_geo : -surf.normal_geo;
+                    if (dot(nn, light.dir) > 0.0f && dot(ng, light.dir) > 0.0f) {
+                        Col refl = surf.opaque_eval(view, light.dir);
+                        float mis = power_heuristic(light.pdf, surf.opaque_pdf(view, light.dir));
+                        Col sky = sc.sky.radiance(light.dir, nullptr);
+                        nee = sky * tr * refl * mis / light.pdf;
+                        double da[3], dr[3];
+                        eval_derivatives(surf, view, light.dir, da, dr);
+                        const double dl = sc.has_fog ? transmittance_log_derivative(make_ray(hit_pos, light.dir)) : 0.0;
+                        for (int c = 0; c < 3; ++c) {
+                            const double k = cval(sky, c) * cval(tr, c) * (double)mis / (double)light.pdf;
+                            x.dadd_a[c] = k * da[c];
+                            x.dadd_r[c] = k * dr[c];
+                            x.dadd_f[c] = cval(nee, c) * dl;
+                        }
+                    }
+                }
+                radiance = radiance + nee * energy;
+                for (int c = 0; c < 3; ++c) x.add[c] = cval(surf.radiance, c) + cval(nee, c);
+                if (Scene::russian_roulette(energy, i, rng)) {
+                    x.kind = AJ_SURF_END;
+                    break;
+                }
+                SampleScatter scat = surf.scatter(ray.dir, view, rng);
+                x.s = scat.weight;
+                double da[3], dr[3];
+                eval_derivatives(surf, view, scat.dir, da, dr);
+                const double ipdf = 1.0 / (double)net_max(scat.pdf, 1e-6f);
+                for (int c = 0; c < 3; ++c) {
+                    x.ds_a[c] = da[c] * ipdf;
+                    x.ds_r[c] = dr[c] * ipdf;
+                }
+                energy = energy * scat.weight;
+                energy = clamp_luminance(energy, indirect_clamp);
+                has_scatter_pdf = scat.has_pdf;
+                scatter_pdf = scat.pdf;
+                ray = make_ray(ray_at(ray, dist) + scat.dir * dist_bias, scat.dir);
+            } else {
+                x.kind = AJ_SKY;
+                if (sc.has_fog) x.score = score_pass(ray, INFINITY);
+                float mis = 1.0f;
+                if (has_scatter_pdf) {
+                    auto l = sc.sky.light_dir(ray.dir);
+                    mis = power_heuristic(scatter_pdf, l ? l->pdf : 0.0f);
+                }
+                Col add = sc.sky.radiance(ray.dir, nullptr) * mis;
+                for (int c = 0; c < 3; ++c) x.add[c] = cval(add, c);
+                radiance = radiance + add * energy;
+                break;
+            }
+        }
+        return n;
+    }
+};
+
+// The texels (and bilinear weights) Texture.Sample (texture.cs:39-69) reads at uv.
+int texel_footprint(const Texture& t, V2 coord, uint32_t idx[4], double w[4]) {
+    float u = coord.x * t.tiling.x;
+    u -= std::floor(u);
+    float v = coord.y * t.tiling.y;
+    v -= std::floor(v);
+    if (t.filter == 1) {
+        uint32_t x = (uint32_t)(u * (float)t.width) % t.width;
+        uint32_t y = (uint32_t)(v * (float)t.height) % t.height;
+        idx[0] = y * t.width + x;
+        w[0] = 1.0;
+        return 1;
+    }
+    float fx = u * (float)(t.width - 1), fy = v * (float)(t.height - 1);
+    uint32_t x0 = (uint32_t)fx, y0 = (uint32_t)fy;
+    uint32_t x1 = (x0 + 1) % t.width, y1 = (y0 + 1) % t.height;
+    double tx = (double)fx - (double)x0, ty = (double)fy - (double)y0;
+    idx[0] = y0 * t.width + x0, w[0] = (1 - tx) * (1 - ty);
+    idx[1] = y0 * t.width + x1, w[1] = tx * (1 - ty);
+    idx[2] = y1 * t.width + x0, w[2] = (1 - tx) * ty;
+    idx[3] = y1 * t.width + x1, w[3] = tx * ty;
+    return 4;
+}
+
+// Per-thread gradient sums.
+struct AdjSums {
+    std::vector<double> a, r;
+    double f = 0.0;
+};
+
+// Reverse sweep over one sample's vertices; G = dL/dI / sample count of the pixel.
+void adjoint_sweep(const Scene& sc, const AdjVertex64* v, int n, const double G[3], int tex_a, int tex_r,
+                   AdjSums& out) {
+    double a[3] = {0, 0, 0};  // d loss / d (throughput leaving the vertex)
+    for (int k = n - 1; k >= 0; --k) {
+        const AdjVertex64& q = v[k];
+        double a_in[3];
+        for (int c = 0; c < 3; ++c) a_in[c] = G[c] * q.add[c];
+        if (q.kind == AJ_FOG || q.kind == AJ_FOG_END) {
+            const Col fc = sc.fog.color;
+            const Col ef = q.e_in * fc;
+            double a_f[3] = {a_in[0], a_in[1], a_in[2]};  // d loss / d (throughput after the fog colour)
+            if (q.kind == AJ_FOG)
+                for (int j = 0; j < 3; ++j) {  // column j of d roulette(ef) / d ef
+                    DCol x = dcol(ef);
+                    x.c[j].d = 1.0;
+                    DCol y = roulette_dual(x, ef, q.bounce);
+                    for (int c = 0; c < 3; ++c) a_f[j] += a[c] * y.c[c].d;
+                }
+            for (int c = 0; c < 3; ++c) {
+                a_in[c] = a_f[c] * cval(fc, c);
+                out.f += G[c] * cval(ef, c) * q.dadd_f[c];
+            }
+        } else if (q.kind == AJ_SURF || q.kind == AJ_SURF_END) {
+            const bool scatters = q.kind == AJ_SURF;
+            Col rr_f = q.e_in;  // the roulette's float output (as the forward divides)
+            if (q.bounce >= 3) {
+                float p = net_min(1.0f, max_component(q.e_in));
+                if (p < 1.0f) rr_f = q.e_in / p;
+            }
+            const Col pre_f = rr_f * q.s;
+            if (scatters)
+                for (int j = 0; j < 3; ++j) {  // column j of d clamp(roulette(e) * s) / d e
+                    DCol x = dcol(q.e_in);
+                    x.c[j].d = 1.0;
+                    DCol y = roulette_dual(x, q.e_in, q.bounce);
+                    for (int c = 0; c < 3; ++c) y.c[c] = y.c[c] * dual(cval(q.s, c));
+                    y = clamp_dual(y, pre_f, q.clamp_max);
+                    for (int c = 0; c < 3; ++c) a_in[j] += a[c] * y.c[c].d;
+                }
+            // d loss / d parameter at this vertex: through the light sample and the scatter weight
+            auto through_scatter = [&](const double ds[3]) {
+                if (!scatters) return 0.0;
+                DCol y;
+                for (int c = 0; c < 3; ++c) y.c[c] = dual(cval(rr_f, c)) * dual(cval(q.s, c), ds[c]);
+                y = clamp_dual(y, pre_f, q.clamp_max);
+                return a[0] * y.c[0].d + a[1] * y.c[1].d + a[2] * y.c[2].d;
+            };
+            const Material& m = sc.objects[q.object].mat;
+            uint32_t idx[4];
+            double w[4];
+            if (tex_a >= 0 && m.color_tex == tex_a) {
+                const int nt = texel_footprint(*sc.textures[tex_a], q.uv, idx, w);
+                for (int c = 0; c < 3; ++c) {
+                    double ds[3] = {0, 0, 0};
+                    ds[c] = q.ds_a[c];
+                    const double g = G[c] * cval(q.e_in, c) * q.dadd_a[c] + through_scatter(ds);
+                    for (int t = 0; t < nt; ++t) out.a[3 * idx[t] + c] += g * cval(m.albedo, c) * w[t];
+                }
+            }
+            if (tex_r >= 0 && m.rough_tex == tex_r) {
+                const int nt = texel_footprint(*sc.textures[tex_r], q.uv, idx, w);
+                double g = through_scatter(q.ds_r);
+                for (int c = 0; c < 3; ++c) g += G[c] * cval(q.e_in, c) * q.dadd_r[c];
+                for (int t = 0; t < nt; ++t) out.r[3 * idx[t]] += g * m.roughness * w[t];
+            }
+            for (int c = 0; c < 3; ++c) out.f += G[c] * cval(q.e_in, c) * q.dadd_f[c];
+        }
+        // the segment into the vertex: its sampling density's score times everything downstream
+        out.f += q.score * (a_in[0] * q.e_in.r + a_in[1] * q.e_in.g + a_in[2] * q.e_in.b);
+        for (int c = 0; c < 3; ++c) a[c] = a_in[c];
+    }
 }
 
 }  // namespace
@@ -2155,6 +2547,72 @@ int oracle_overlay_draw(uint8_t* rgb, uint32_t w, uint32_t h, const SrView* view
         }
     }
     return 0;
+}
+
+// FP64 path-replay adjoint (see "FP64 path-replay adjoint" above): for dL/dI = d_image (h x w x 3)
+// of the image I = radiance + radiance_fog, with `samples` the forward render's sample counts (the
+// normalisation of each pixel), ADDS dL/d(texels of albedo texture tex_a) into grad_a (its w x h x
+// 3), dL/d(red texels of roughness texture tex_r) into grad_r (w x h x 3, channel 0) and dL/d(fog
+// density) into grad_f[0]; -1 / NULL skip a part.  `replay` (optional, h x w x 3) receives the
+// replayed image, which equals the render's radiance + radiance_fog.  Random-number stream 0 (the
+// reference's Rng(x, y)).
+int oracle_adjoint(void* sp, const SrView* v, const SrRenderParams* p, int32_t threads, const float* d_image,
+                   const uint32_t* samples, int32_t tex_a, double* grad_a, int32_t tex_r, double* grad_r,
+                   double* grad_f, float* replay) {
+    const Scene* s = (Scene*)sp;
+    if (!s->built) return fail(SR_ERR_STATE, "Scene not built");
+    for (const Object& o : s->objects)
+        if (o.mat.transparency > 0.0f) return fail(SR_ERR_STATE, "the adjoint does not cover transparent materials");
+    if (p->bounces > 16) return fail(SR_ERR_INVALID_ARG, "bounces must be <= 16");
+    const int nt = threads > 0 ? threads : 1;
+    const size_t na = tex_a >= 0 && grad_a ? (size_t)s->textures[tex_a]->width * s->textures[tex_a]->height * 3 : 0;
+    const size_t nr = tex_r >= 0 && grad_r ? (size_t)s->textures[tex_r]->width * s->textures[tex_r]->height * 3 : 0;
+    std::vector<AdjSums> sums(nt);
+    for (AdjSums& a : sums) {
+        a.a.assign(na, 0.0);
+        a.r.assign(nr, 0.0);
+    }
+    View view{to_transform(v->transform), v->fov, v->near_plane};
+    const float aspect = (float)p->width / (float)p->height;
+    Adjoint64 adj{*s, dual(s->has_fog ? s->fog.density : 1.0f, 1.0)};
+    parallel_for((int)p->height, nt, [&](int yi, int t) {
+        const uint32_t y = (uint32_t)yi;
+        AdjVertex64 verts[17];
+        for (uint32_t x = 0; x < p->width; ++x) {
+            const size_t i = (size_t)y * p->width + x;
+            const uint32_t count = samples[i];
+            const uint32_t taken = count < p->max_samples ? count : p->max_samples;  // the loop's off-by-one
+            double G[3];
+            for (int c = 0; c < 3; ++c) G[c] = (double)d_image[3 * i + c] / (double)count;
+            Rng rng(x, y);
+            Col rad_sum = kBlack, fog_sum = kBlack;
+            for (uint32_t si = 0; si < taken; ++si) {
+                // Renderer.Render's jitter (renderer.cs:167-176): x first, then y
+                float jx = rng.next_float();
+                float px = ((float)x + jx) / (float)p->width;
+                float jy = rng.next_float();
+                float py = ((float)y + jy) / (float)p->height;
+                Ray ray = view.ray({px, py}, aspect);
+                Col rad, fog;
+                const int n = adj.replay(ray, rng, p->bounces, p->indirect_clamp, verts, rad, fog);
+                rad_sum = rad_sum + rad;
+                fog_sum = fog_sum + fog;
+                adjoint_sweep(*s, verts, n, G, na ? tex_a : -1, nr ? tex_r : -1, sums[t]);
+            }
+            if (replay) {
+                Col r = rad_sum / (float)count, f = fog_sum / (float)count;
+                replay[3 * i] = r.r + f.r;
+                replay[3 * i + 1] = r.g + f.g;
+                replay[3 * i + 2] = r.b + f.b;
+            }
+        }
+    });
+    for (const AdjSums& a : sums) {
+        for (size_t k = 0; k < na; ++k) grad_a[k] += a.a[k];
+        for (size_t k = 0; k < nr; ++k) grad_r[k] += a.r[k];
+        if (grad_f) grad_f[0] += a.f;
+    }
+    return SR_OK;
 }
 
 }  // extern "C"

@@ -18,6 +18,7 @@ import pytest
 from sharpray_gb300 import (Context, Fog, Quat, SharpRayError, Transform, View, _abi, adjoint_albedo, adjoint_texture,
                             render_params, synth)
 from sharpray_gb300.synth import MeshDesc, ObjectDesc, SceneDesc, TextureDesc, look_rotation
+from tests.adjoint_scenes import adjoint_scene, roughness_scene
 
 torch_lib = pytest.importorskip("torch")
 from sharpray_gb300.autograd import current_stream_handle  # noqa: E402
@@ -26,51 +27,6 @@ pytestmark = pytest.mark.gpu
 
 PLANES = (("radiance", 3, "float32"), ("radiance_fog", 3, "float32"), ("normals", 3, "float32"), ("uv", 2, "float32"),
           ("depth", 1, "float32"), ("samples", 1, "int32"), ("variance", 1, "float32"))
-
-
-def adjoint_scene(fog: bool, bounces: int, clamp: float, w=40, h=30, spp=3, general: bool = False,
-                  metal: bool = False) -> SceneDesc:
-    """Textured ground and blob sharing one bilinear albedo texture (different material albedos,
-    tiling 2 on the blob), a point-filtered texture on a second blob, an untextured rock; `general`
-    adds an analytic sphere with the bilinear texture (the kernels' general instantiation); `metal`
-    makes the textured blob fully metallic (its albedo then enters through the Fresnel base; the
-    lobe probability clamps to a constant, so sampling still does not depend on the albedo)."""
-    rng = np.random.default_rng(7)
-    gpos, guv = synth.ground_quad(3.0, -1.0)
-    bpos, buv = synth.uv_sphere(10, 14, amplitude=0.1, seed=2)
-    rpos, ruv = synth.uv_sphere(8, 10, amplitude=0.2, seed=4)
-    d = SceneDesc("adjoint")
-    d.meshes = [MeshDesc(gpos, guv, smooth_normals=False), MeshDesc(bpos, buv), MeshDesc(rpos, ruv)]
-    d.textures = [TextureDesc(synth._rgbe_texels(synth.sky_env(64, 32, seed=3, sun_peak=20.0, sun_sigma_deg=6.0))),
-                  TextureDesc(rng.uniform(0.2, 0.9, (6, 8, 3)).astype(np.float32), 0, (1.0, 1.0)),
-                  TextureDesc(rng.uniform(0.2, 0.9, (4, 4, 3)).astype(np.float32), 1, (1.0, 1.0))]
-    d.sky = ("texture", 0, 1.0, 0.3)
-    d.objects = [
-        ObjectDesc("ground", Transform(), {"albedo": (0.9, 0.8, 0.7), "roughness": 0.7, "color_texture": 1},
-                   ("mesh", 0)),
-        ObjectDesc("blob", Transform((-0.6, -0.2, 0.8), Quat.identity(), (0.7, 0.7, 0.7)),
-                   {"albedo": (1.0, 0.9, 0.8), "roughness": 0.4, "color_texture": 1}, ("mesh", 1)),
-        ObjectDesc("pointblob", Transform((0.9, -0.4, 0.4), Quat.angle_axis(0.5, (0.0, 1.0, 0.0)), (0.5, 0.5, 0.5)),
-                   {"albedo": (0.8, 0.8, 0.8), "roughness": 0.5, "color_texture": 2}, ("mesh", 1)),
-        ObjectDesc("rock", Transform((0.2, -0.7, -0.6), Quat.identity(), (0.3, 0.3, 0.3)),
-                   {"albedo": (0.5, 0.5, 0.45), "roughness": 0.6}, ("mesh", 2)),
-    ]
-    if metal:
-        d.objects[1].material["metallic"] = 1.0
-    if general:
-        d.objects.append(ObjectDesc("ball", Transform(), {"albedo": (0.7, 0.9, 0.8), "roughness": 0.5,
-                                                          "color_texture": 1}, ("sphere", (0.6, -0.75, -0.3), 0.25)))
-    # the blob's tiling: a second TextureDesc would be a second texture, so tile through its uvs
-    d.meshes[1] = MeshDesc(bpos, buv * np.float32(2.0))
-    if fog:
-        d.fog = Fog(0.08, (0.8, 0.75, 0.7), 0.5, 0.2)
-    cam = (0.0, 0.9, -3.2)
-    d.view = View(Transform(cam, look_rotation(cam, (0.0, -0.4, 0.5))), math.radians(55.0), 0.1)
-    d.width, d.height, d.spp, d.bounces = w, h, spp, bounces
-    d.min_samples = spp
-    d.variance_threshold = 0.0  # every pixel takes spp samples (count spp + 1, the loop's off-by-one)
-    d.indirect_clamp = clamp
-    return d
 
 
 class Rig:
@@ -248,17 +204,6 @@ def test_autograd_matches_adjoint_and_recovers_texture(torch_mod):
     assert err1 < 0.6 * err0, (err0, err1)
 
 
-def roughness_scene(spp: int) -> SceneDesc:
-    """adjoint_scene with a 4x4 roughness texture (its red channel) on the ground and the blob."""
-    d = adjoint_scene(False, 2, 10.0, w=64, h=48, spp=spp)
-    rough = np.random.default_rng(9).uniform(0.25, 0.8, (4, 4, 3)).astype(np.float32)
-    d.textures.append(TextureDesc(rough, 0, (1.0, 1.0)))
-    for o in d.objects[:2]:
-        o.material["roughness"] = 1.0
-        o.material["roughness_texture"] = 3
-    return d
-
-
 def test_roughness_adjoint_matches_finite_differences_in_expectation(torch_mod):
     """The roughness moves the sampled specular directions, so the detached (path-replay) gradient
     equals the derivative of the expected image, not of each sample: with a linear loss
@@ -392,3 +337,65 @@ def test_seed_streams(torch_mod):
     rig.scene.set_render_mode(_abi.SR_RENDER_AUTO)
     rig.scene.set_seed(0)
     assert np.array_equal(rig.image().view(np.uint32), base.view(np.uint32))
+
+
+def grad_agreement(got: np.ndarray, want: np.ndarray) -> tuple:
+    """(relative L2 error, fraction of entries within 1e-3 relative + 1e-4 of the largest)."""
+    got, want = got.astype(np.float64).ravel(), want.astype(np.float64).ravel()
+    scale = float(np.abs(want).max())
+    rel_l2 = float(np.linalg.norm(got - want) / max(np.linalg.norm(want), 1e-300))
+    ok = np.abs(got - want) <= 1e-3 * np.abs(want) + 1e-4 * scale
+    return rel_l2, float(ok.mean())
+
+
+@pytest.mark.parametrize("fog,general", [(False, False), (True, False), (True, True)])
+def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general):
+    """The GPU adjoint (float, sr_adjoint_all: albedo texture, roughness texture, fog density from one
+    replay) against the oracle's FP64 replay adjoint on the same scene, dL/dI and sample counts.  The
+    two evaluate the same estimator -- the oracle with dual numbers in double through the reference's
+    formulas -- so they agree to float rounding wherever the two sides trace the same paths (rare paths
+    fork where the GPU's and the C runtime's transcendentals differ by an ulp).  Bars: relative L2
+    error < 1e-3 for each texture gradient and the density gradient within 1e-3; every texel channel
+    within 1e-3 relative (+ 1e-4 of the largest) on >= 99 %."""
+    import ctypes as C
+    torch = torch_mod
+    d = roughness_scene(4)
+    d.width, d.height = 48, 36
+    d.bounces = 5
+    d.indirect_clamp = 3.0
+    if fog:
+        d.fog = Fog(0.08, (0.8, 0.75, 0.7), 0.5, 0.2)
+    if general:  # an analytic sphere: the kernels' general instantiation
+        d.objects.append(ObjectDesc("ball", Transform(), {"albedo": (0.7, 0.9, 0.8), "roughness": 0.5,
+                                                          "color_texture": 1}, ("sphere", (0.6, -0.75, -0.3), 0.25)))
+    rig = Rig(torch, d)
+    img = rig.image()
+    target = (img * np.float32(0.6) + np.float32(0.05)).astype(np.float32)
+    d_image = (2.0 * (img - target)).astype(np.float32)
+    samples = rig.bufs["samples"].cpu().numpy().view(np.uint32)
+    ta, tr = rig.tex[1], rig.tex[3]
+    g = [torch.zeros(ta.height * ta.width * 3, device="cuda"), torch.zeros(tr.height * tr.width * 3, device="cuda"),
+         torch.zeros(1, device="cuda")]
+    replay = torch.zeros(d.width * d.height * 3, device="cuda")
+    di = torch.from_numpy(d_image).cuda()
+    v = d.view.to_c()
+    _abi.check(rig.ctx._lib.sr_adjoint_all(rig.scene.handle, C.byref(v), C.byref(rig.params), C.byref(rig.aovs),
+                                           C.c_void_p(di.data_ptr()), ta.id, C.c_void_p(g[0].data_ptr()), tr.id,
+                                           C.c_void_p(g[1].data_ptr()), C.c_void_p(g[2].data_ptr()),
+                                           C.c_void_p(replay.data_ptr()), C.c_void_p(current_stream_handle())))
+    torch.cuda.synchronize()
+    o = oracle_mod.instantiate(d)
+    ga, gr, gf, rep = o.adjoint(v, rig.params, d_image, samples, 1, (ta.height, ta.width), 3, (tr.height, tr.width))
+    # the replays follow the same paths: the image bar of the render parity tests
+    rp = replay.cpu().numpy().reshape(-1, 3).astype(np.float64)
+    err = np.abs(rp - rep).max(axis=1) / np.maximum(np.abs(rep).max(axis=1), 1e-3)
+    assert (err < 1e-3).mean() >= 0.995
+    for name, got, want in (("albedo", g[0].cpu().numpy(), ga), ("roughness", g[1].cpu().numpy().reshape(-1, 3)[:, 0],
+                                                                   gr.reshape(-1, 3)[:, 0])):
+        assert np.abs(want).max() > 0.0, name
+        rel_l2, frac = grad_agreement(got, want)
+        assert rel_l2 < 1e-3 and frac >= 0.99, (name, rel_l2, frac)
+    assert np.all(g[1].cpu().numpy().reshape(-1, 3)[:, 1:] == 0.0)
+    if fog:
+        gd = float(g[2].cpu().numpy()[0])
+        assert abs(gd - gf) <= 1e-3 * abs(gf), (gd, gf)

@@ -37,8 +37,8 @@ def test_bounce_loop_cap_reports_and_recovers(scene, mode):
         g.set_tuning(max_bounce_iterations=2)  # 4 spp x 5 segments need ~25 bounces
         with pytest.raises(SharpRayError) as e:
             render(d, g)
-        assert e.value.args[0] == _abi.SR_ERR_DEVICE
-        assert "loop cap" in e.value.args[1]
+        assert e.value.code == _abi.SR_ERR_DEVICE
+        assert "loop cap" in str(e.value)
         g.set_tuning()
         after = render(d, g)
     finally:
@@ -56,10 +56,10 @@ def test_traversal_cap_in_trace_and_render(scene, oracle_mod):
         g.set_tuning(max_traversal_steps=3)  # fewer actions than any hit needs
         with pytest.raises(SharpRayError) as e:
             g.trace(rays)
-        assert e.value.args[0] == _abi.SR_ERR_DEVICE and "loop cap" in e.value.args[1]
+        assert e.value.code == _abi.SR_ERR_DEVICE and "loop cap" in str(e.value)
         with pytest.raises(SharpRayError) as e:
             render(d, g)
-        assert e.value.args[0] == _abi.SR_ERR_DEVICE
+        assert e.value.code == _abi.SR_ERR_DEVICE
         g.set_tuning()
         got = g.trace(rays)
     finally:

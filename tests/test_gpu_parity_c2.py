@@ -26,7 +26,8 @@ BANDS, ROWS = 16, 2
 @pytest.fixture(scope="module")
 def c2(gpu_ctx, oracle_mod):
     d = synth.config_c2()
-    assert (d.width, d.height, d.spp, d.bounces, d.triangle_count) == (1920, 1080, 64, 8, 871200 + 64 * 5000)
+    # 871,200-triangle sphere + one 5,000-triangle rock mesh shared by 64 instances
+    assert (d.width, d.height, d.spp, d.bounces, d.triangle_count, len(d.objects)) == (1920, 1080, 64, 8, 876200, 65)
     g = d.instantiate(gpu_ctx)
     g.build()
     return d, g, oracle_mod.instantiate(d)
