@@ -409,6 +409,30 @@ SR_API int sr_adjoint_texture(SrScene* scene, const SrView* view, const SrRender
 SR_API int sr_adjoint_all(SrScene* scene, const SrView* view, const SrRenderParams* params, const SrAovs* forward,
                           const float* d_image, int32_t albedo_texture, float* albedo_grad, int32_t roughness_texture,
                           float* roughness_grad, float* fog_density_grad, float* replay, void* stream);
+/* How the adjoint entry points above replay a render's paths (no reference counterpart):
+ * SR_ADJOINT_REPLAY_WAVEFRONT (the default) renders them again with the wavefront kernels -- the
+ * same traversal, event queues and shading as sr_render_device -- recording each sample's path
+ * vertices in a device buffer (slots x (bounces + 1) x 128 bytes) and sweeping them back into the
+ * gradients when the sample ends; SR_ADJOINT_REPLAY_PIXEL replays each pixel's samples in one
+ * thread.  Both give the same gradients up to the order of float additions. */
+enum { SR_ADJOINT_REPLAY_WAVEFRONT = 0, SR_ADJOINT_REPLAY_PIXEL = 1 };
+SR_API int sr_scene_set_adjoint_replay(SrScene* scene, int32_t form);
+/* Path-vertex checkpointing (no reference counterpart): sr_render_device that also keeps every
+ * sample's path vertices on the device, so that sr_adjoint_checkpointed can differentiate this
+ * image without tracing it again.  The vertices take slots x max_samples x (bounces + 1) x 128 bytes
+ * (slots: width x height rounded up to 8 x 4 tiles), reported in *bytes_kept (may be NULL), and stay
+ * until the next checkpointed render or sr_scene_release_checkpoint.  The gradients are those of the
+ * rendered samples themselves (replay with another seed decorrelates them instead). */
+SR_API int sr_render_checkpointed(SrScene* scene, const SrView* view, const SrRenderParams* params,
+                                  const SrAovs* device_out, void* stream, uint64_t* bytes_kept);
+/* The adjoint of the last checkpointed render's image for dL/dI = d_image (device, width x height x 3):
+ * adds the gradients as sr_adjoint_all does, sweeping the kept vertices (no traversal).  That
+ * render's output planes must still hold it (its sample counts are read). */
+SR_API int sr_adjoint_checkpointed(SrScene* scene, const float* d_image, int32_t albedo_texture, float* albedo_grad,
+                                   int32_t roughness_texture, float* roughness_grad, float* fog_density_grad,
+                                   void* stream);
+/* Frees the vertices kept by sr_render_checkpointed. */
+SR_API int sr_scene_release_checkpoint(SrScene* scene);
 /* Sets the fog density of a built scene with fog (> 0), e.g. one step of inverse rendering. */
 SR_API int sr_scene_update_fog_density(SrScene* scene, float density);
 /* Replaces the texels of texture `texture` (rgb floats, its width x height) in a built scene's

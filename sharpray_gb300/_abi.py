@@ -27,6 +27,7 @@ SR_SHAPE_AABOX = 2
 SR_AOV_NORMAL, SR_AOV_DEPTH, SR_AOV_VARIANCE, SR_AOV_SAMPLES, SR_AOV_UV = 0, 1, 2, 3, 4
 SR_ALIGN_TOP_LEFT, SR_ALIGN_CENTER = 0, 1
 SR_ADJOINT_ALBEDO, SR_ADJOINT_ROUGHNESS, SR_ADJOINT_FOG_DENSITY = 0, 1, 2
+SR_ADJOINT_REPLAY_WAVEFRONT, SR_ADJOINT_REPLAY_PIXEL = 0, 1
 SR_TEXTURE_SRGB = 0
 SR_TEXTURE_LINEAR = 1
 SR_TEXTURE_HDR = 2
@@ -185,6 +186,10 @@ PROTOTYPES = {
     "sr_render_progress": (_I, [_P, C.POINTER(_U), C.POINTER(_U)]),
     "sr_scene_set_tuning": (_I, [_P, _P]),
     "sr_scene_set_seed": (_I, [_P, _U]),
+    "sr_scene_set_adjoint_replay": (_I, [_P, C.c_int32]),
+    "sr_render_checkpointed": (_I, [_P, _P, _P, _P, _P, C.POINTER(C.c_uint64)]),
+    "sr_adjoint_checkpointed": (_I, [_P, _P, C.c_int32, _P, C.c_int32, _P, _P, _P]),
+    "sr_scene_release_checkpoint": (_I, [_P]),
     "sr_scene_get_seed": (_I, [_P, C.POINTER(_U)]),
     "sr_scene_get_tuning": (_I, [_P, C.POINTER(SrTuning)]),
     "sr_scene_autotune": (_I, [_P, C.POINTER(SrView), C.POINTER(SrRenderParams), _U, C.POINTER(SrTuning)]),

@@ -487,6 +487,34 @@ class Scene:
     def seed(self) -> int:
         return self.get_seed()
 
+    def set_adjoint_replay(self, form: int) -> None:
+        """sr_scene_set_adjoint_replay: SR_ADJOINT_REPLAY_WAVEFRONT (default) or SR_ADJOINT_REPLAY_PIXEL."""
+        check(self._lib.sr_scene_set_adjoint_replay(self.handle, int(form)))
+
+    def render_checkpointed(self, view: "View", params: SrRenderParams, device_out: SrAovs,
+                            stream: Optional[int] = None) -> int:
+        """sr_render_checkpointed: sr_render_device keeping every sample's path vertices for
+        adjoint_checkpointed; returns the bytes they take."""
+        v = view.to_c()
+        n = C.c_uint64()
+        check(self._lib.sr_render_checkpointed(self.handle, C.byref(v), C.byref(params), C.byref(device_out),
+                                               C.c_void_p(stream) if stream else None, C.byref(n)))
+        return n.value
+
+    def adjoint_checkpointed(self, d_image: int, albedo_texture=None, albedo_grad: Optional[int] = None,
+                             roughness_texture=None, roughness_grad: Optional[int] = None,
+                             fog_density_grad: Optional[int] = None, stream: Optional[int] = None) -> None:
+        """sr_adjoint_checkpointed: the gradients of the last checkpointed render's image for
+        dL/dI = d_image (device pointers; a None gradient skips its part)."""
+        tid = lambda t: -1 if t is None else (t.id if isinstance(t, Texture) else int(t))
+        p = lambda x: C.c_void_p(x) if x else None
+        check(self._lib.sr_adjoint_checkpointed(self.handle, C.c_void_p(d_image), tid(albedo_texture), p(albedo_grad),
+                                                tid(roughness_texture), p(roughness_grad), p(fog_density_grad),
+                                                p(stream)))
+
+    def release_checkpoint(self) -> None:
+        check(self._lib.sr_scene_release_checkpoint(self.handle))
+
     def update_fog_density(self, density: float) -> None:
         """sr_scene_update_fog_density: the built scene's fog density (its fog must exist)."""
         check(self._lib.sr_scene_update_fog_density(self.handle, float(density)))

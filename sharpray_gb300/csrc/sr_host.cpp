@@ -174,8 +174,19 @@ struct SrScene {
     int last_mode = 0;                // render mode of the last render
     uint32_t last_host_iters = 0;     // bounces run by the host loop
     bool last_tail = false;           // the host loop launched the tail kernel
+    // adjoint passes of the wavefront kernels (sr_wave_adjoint.cu)
+    int32_t adjoint_replay = SR_ADJOINT_REPLAY_WAVEFRONT;  // sr_scene_set_adjoint_replay
+    DevBuf adj_vbuf, adj_pass;     // replay: vertex records (one sample per slot), the device AdjPass
+    DevBuf ckpt_vbuf, ckpt_vcount, ckpt_pass_dev;  // record: every sample's vertex records and counts
+    cudaGraphExec_t adj_graph_exec = nullptr;
+    WaveLaunch adj_graph_launch{};
+    // the last checkpointed render (sr_render_checkpointed), swept by sr_adjoint_checkpointed
+    bool ckpt_valid = false;
+    WaveLaunch ckpt_launch{};
+    AdjPass ckpt_pass{};
     ~SrScene() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (adj_graph_exec) cudaGraphExecDestroy(adj_graph_exec);
         if (capture_stream) cudaStreamDestroy(capture_stream);
         for (cudaStream_t& st : side_streams)
             if (st) cudaStreamDestroy(st);
@@ -928,23 +939,52 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     return SR_OK;
 }
 
+// A wavefront render of scene s; `adj` (with adj_mode kAdjReplay or kAdjRecord) makes it an adjoint
+// pass, whose AdjPass goes to the scene's device copy before the launches.  Forward renders and
+// adjoint passes keep separate cached graphs.
 static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& out,
-                            unsigned long long* ctr, cudaStream_t st, bool graph) {
+                            unsigned long long* ctr, cudaStream_t st, bool graph, int adj_mode = kAdjNone,
+                            AdjPass* adj = nullptr, WaveLaunch* launch_out = nullptr) {
     WaveLaunch L;
     if (int rc = wave_prepare(s, dv, dp, out, ctr, st, L)) return rc;
+    if (adj_mode != kAdjNone) {
+        // vertex records: one sample per slot (replay) or every sample (record, kept apart so that
+        // a replay pass does not overwrite a checkpoint)
+        const bool record = adj_mode == kAdjRecord;
+        const uint64_t kept = record ? dp.max_samples : 1u;
+        adj->vper = dp.bounces + 1;
+        adj->samples_kept = (uint32_t)kept;
+        const uint64_t recs = (uint64_t)s->wave_slots * kept * adj->vper;
+        DevBuf& vbuf = record ? s->ckpt_vbuf : s->adj_vbuf;
+        DevBuf& pass = record ? s->ckpt_pass_dev : s->adj_pass;
+        SR_CUDA(vbuf.reserve(recs * kAdjVertexF4 * sizeof(float4)), "alloc adjoint vertex records");
+        adj->vbuf = vbuf.as<float4>();
+        if (record) {
+            SR_CUDA(s->ckpt_vcount.reserve((size_t)s->wave_slots * kept), "alloc adjoint vertex counts");
+            adj->vcount = s->ckpt_vcount.as<uint8_t>();
+        }
+        SR_CUDA(pass.reserve(sizeof(AdjPass)), "alloc adjoint pass");
+        SR_CUDA(cudaMemcpyAsync(pass.ptr, adj, sizeof(AdjPass), cudaMemcpyHostToDevice, st), "upload adjoint pass");
+        L.adj_mode = adj_mode;
+        L.adj = pass.as<AdjPass>();
+        wave_adj_grid_sizes(L, s->sms);
+    }
+    if (launch_out) *launch_out = L;
     if (graph) {
+        cudaGraphExec_t& exec = adj_mode != kAdjNone ? s->adj_graph_exec : s->graph_exec;
+        WaveLaunch& baked = adj_mode != kAdjNone ? s->adj_graph_launch : s->graph_launch;
         if (!s->capture_stream) SR_CUDA(cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking), "stream");
-        if (s->graph_exec && std::memcmp(&s->graph_launch, &L, sizeof(L)) != 0) {
+        if (exec && std::memcmp(&baked, &L, sizeof(L)) != 0) {
             SR_CUDA(cudaStreamSynchronize(st), "sync before graph rebuild");
-            cudaGraphExecDestroy(s->graph_exec);
-            s->graph_exec = nullptr;
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
         }
-        if (!s->graph_exec) {
-            SR_CUDA(wave_build_graph(L, s->capture_stream, s->side_streams, s->fork_events, &s->graph_exec),
+        if (!exec) {
+            SR_CUDA(wave_build_graph(L, s->capture_stream, s->side_streams, s->fork_events, &exec),
                     "build bounce-loop graph");
-            std::memcpy(&s->graph_launch, &L, sizeof(L));
+            std::memcpy(&baked, &L, sizeof(L));
         }
-        SR_CUDA(cudaGraphLaunch(s->graph_exec, st), "launch bounce-loop graph");
+        SR_CUDA(cudaGraphLaunch(exec, st), "launch bounce-loop graph");
         return SR_OK;
     }
     const size_t count_bytes = kWaveGroups * kWaveCounters * sizeof(uint32_t);
@@ -1823,6 +1863,31 @@ static bool scene_texture(SrScene* s, int32_t texture) {
     return texture >= 0 && (size_t)texture < s->tex_offset.size();
 }
 
+// The adjoint of a finished render (forward planes f) in the scene's replay form: the wavefront
+// replay (sr_wave_adjoint.cu; host loop when the scene renders with one, else the graph) or the
+// per-pixel replay kernel (sr_adjoint.cu).  parameter 0-2 names one gradient, 3 all of them.
+static int run_adjoint(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& f, const float* d_image,
+                       int parameter, int tex_a, float* grad_a, int tex_r, float* grad_r, float* grad_f,
+                       float* replay, cudaStream_t st) {
+    if (s->adjoint_replay == SR_ADJOINT_REPLAY_PIXEL) {
+        SR_CUDA(launch_adjoint(launch_scene(s), dv, dp, f, d_image, parameter, tex_a, grad_a, tex_r, grad_r, grad_f,
+                               replay, s->err.as<uint32_t>(), st),
+                "adjoint launch");
+        return SR_OK;
+    }
+    AdjPass a{};
+    a.d_image = d_image;
+    a.fwd_samples = f.samples;
+    a.replay = replay;
+    a.tex_a = grad_a ? tex_a : -1;
+    a.grad_a = grad_a;
+    a.tex_r = grad_r ? tex_r : -1;
+    a.grad_r = grad_r;
+    a.grad_f = grad_f;
+    const DevAovs none{};  // a replay writes no AOVs
+    return render_wavefront(s, dv, dp, none, nullptr, st, s->render_mode != SR_RENDER_WAVEFRONT, kAdjReplay, &a);
+}
+
 SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
                               const float* d_image, int32_t texture, int32_t parameter, float* grad, float* replay,
                               void* stream) {
@@ -1840,11 +1905,8 @@ SR_API int sr_adjoint_texture(SrScene* s, const SrView* view, const SrRenderPara
     }
     DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
     const bool a = parameter == SR_ADJOINT_ALBEDO, r = parameter == SR_ADJOINT_ROUGHNESS;
-    SR_CUDA(launch_adjoint(launch_scene(s), dv, dp, f, d_image, parameter, a ? texture : -1, a ? grad : nullptr,
-                           r ? texture : -1, r ? grad : nullptr, a || r ? nullptr : grad, replay,
-                           s->err.as<uint32_t>(), st),
-            "adjoint launch");
-    return SR_OK;
+    return run_adjoint(s, dv, dp, f, d_image, parameter, a ? texture : -1, a ? grad : nullptr, r ? texture : -1,
+                       r ? grad : nullptr, a || r ? nullptr : grad, replay, st);
 }
 
 SR_API int sr_adjoint_all(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
@@ -1861,16 +1923,86 @@ SR_API int sr_adjoint_all(SrScene* s, const SrView* view, const SrRenderParams* 
     if (fog_density_grad && !s->dev.has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
     if (!albedo_grad && !roughness_grad && !fog_density_grad) return SR_OK;
     DevAovs f{fwd->radiance, fwd->radiance_fog, nullptr, nullptr, nullptr, fwd->samples, nullptr};
-    SR_CUDA(launch_adjoint(launch_scene(s), dv, dp, f, d_image, 3, albedo_grad ? albedo_texture : -1, albedo_grad,
-                           roughness_grad ? roughness_texture : -1, roughness_grad, fog_density_grad, replay,
-                           s->err.as<uint32_t>(), st),
-            "adjoint launch");
-    return SR_OK;
+    return run_adjoint(s, dv, dp, f, d_image, 3, albedo_grad ? albedo_texture : -1, albedo_grad,
+                       roughness_grad ? roughness_texture : -1, roughness_grad, fog_density_grad, replay, st);
 }
 
 SR_API int sr_adjoint_albedo(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* fwd,
                              const float* d_image, int32_t texture, float* grad, float* replay, void* stream) {
     return sr_adjoint_texture(s, view, params, fwd, d_image, texture, SR_ADJOINT_ALBEDO, grad, replay, stream);
+}
+
+SR_API int sr_scene_set_adjoint_replay(SrScene* s, int32_t form) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (form != SR_ADJOINT_REPLAY_WAVEFRONT && form != SR_ADJOINT_REPLAY_PIXEL)
+        return fail(SR_ERR_INVALID_ARG, "unknown adjoint replay form %d", form);
+    s->adjoint_replay = form;
+    return SR_OK;
+}
+
+SR_API int sr_render_checkpointed(SrScene* s, const SrView* view, const SrRenderParams* params, const SrAovs* out,
+                                  void* stream, uint64_t* bytes_kept) {
+    if (!s || !out || !params) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    if (!out->radiance || !out->radiance_fog || !out->normals || !out->uv || !out->depth || !out->samples || !out->variance)
+        return fail(SR_ERR_INVALID_ARG, "sr_render_checkpointed needs all seven AOV planes");
+    if (s->dev.has_transparent) return fail(SR_ERR_STATE, "the adjoint does not support transparent materials");
+    DevView dv;
+    DevParams dp;
+    if (int rc = make_view(view, params, dv, dp)) return rc;
+    if (dp.bounces > 16) return fail(SR_ERR_INVALID_ARG, "the adjoint supports at most 16 bounces");
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    if (int rc = progress_begin(s, dp.width * dp.height)) return rc;
+    s->ckpt_valid = false;
+    DevAovs d{out->radiance, out->radiance_fog, out->normals, out->uv, out->depth, out->samples, out->variance};
+    AdjPass a{};
+    WaveLaunch L;
+    if (int rc = render_wavefront(s, dv, dp, d, nullptr, st, s->render_mode != SR_RENDER_WAVEFRONT, kAdjRecord, &a, &L))
+        return rc;
+    SR_CUDA(cudaEventRecord(s->progress_event, st), "progress event");
+    a.fwd_samples = out->samples;  // the sweep's sample counts
+    s->ckpt_valid = true;
+    s->ckpt_launch = L;
+    s->ckpt_pass = a;
+    if (bytes_kept)
+        *bytes_kept = (uint64_t)s->wave_slots * a.samples_kept * (a.vper * kAdjVertexF4 * sizeof(float4) + 1);
+    return SR_OK;
+}
+
+SR_API int sr_adjoint_checkpointed(SrScene* s, const float* d_image, int32_t albedo_texture, float* albedo_grad,
+                                   int32_t roughness_texture, float* roughness_grad, float* fog_density_grad,
+                                   void* stream) {
+    if (!s || !d_image) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    if (!s->ckpt_valid) return fail(SR_ERR_STATE, "no checkpointed render on this scene (sr_render_checkpointed)");
+    if (albedo_grad && !scene_texture(s, albedo_texture))
+        return fail(SR_ERR_INVALID_ARG, "albedo texture %d is not part of the scene", albedo_texture);
+    if (roughness_grad && !scene_texture(s, roughness_texture))
+        return fail(SR_ERR_INVALID_ARG, "roughness texture %d is not part of the scene", roughness_texture);
+    if (fog_density_grad && !s->dev.has_fog) return fail(SR_ERR_STATE, "the scene has no fog");
+    if (!albedo_grad && !roughness_grad && !fog_density_grad) return SR_OK;
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->ctx->stream;
+    AdjPass a = s->ckpt_pass;
+    a.d_image = d_image;
+    a.tex_a = albedo_grad ? albedo_texture : -1;
+    a.grad_a = albedo_grad;
+    a.tex_r = roughness_grad ? roughness_texture : -1;
+    a.grad_r = roughness_grad;
+    a.grad_f = fog_density_grad;
+    SR_CUDA(cudaMemcpyAsync(s->ckpt_pass_dev.ptr, &a, sizeof(AdjPass), cudaMemcpyHostToDevice, st), "upload adjoint pass");
+    SR_CUDA(launch_adjoint_checkpoint(s->ckpt_launch, d_image, a.fwd_samples, st), "checkpoint sweep");
+    return SR_OK;
+}
+
+SR_API int sr_scene_release_checkpoint(SrScene* s) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (s->ctx->device >= 0) cudaSetDevice(s->ctx->device);
+    s->ckpt_valid = false;
+    s->ckpt_vbuf.release();
+    s->ckpt_vcount.release();
+    return SR_OK;
 }
 
 SR_API int sr_scene_update_fog_density(SrScene* s, float density) {

@@ -95,6 +95,31 @@ inline uint32_t wave_live(const uint32_t* counts, int parity) {
            counts[kCountEvent + 3 * parity + 2] + counts[kCountLate + parity];
 }
 
+// Adjoint modes of the wavefront kernels (instantiated in sr_wave_adjoint.cu).  kAdjReplay: the
+// render replays the paths of a finished render (same random numbers), records each sample's path
+// vertices in the slot's vertex buffer and, when the sample ends, sweeps them back into the
+// parameter gradients (dL/dI known).  kAdjRecord: a normal render that also keeps every sample's
+// vertices (path-vertex checkpointing), swept later by launch_adjoint_checkpoint.
+enum : int { kAdjNone = 0, kAdjReplay = 1, kAdjRecord = 2 };
+constexpr int kAdjVertexF4 = 8;     // float4s per vertex record
+constexpr int kAdjSampleShift = 8;  // record mode: the sample index rides in the path flags above bit 8
+
+// Where the adjoint kernels read and write, kept in device memory (one per scene) so that a cached
+// graph stays valid while the buffers change from call to call.
+struct AdjPass {
+    float4* vbuf;                 // vertex records: ((slot * samples_kept + sample) * vper + k) * 8 float4
+    uint32_t vper;                // vertices per sample (bounces + 1)
+    uint32_t samples_kept;        // samples kept per slot (replay 1, record max_samples)
+    uint8_t* vcount;              // record: vertices of each (slot, sample)
+    const float* d_image;         // replay: dL/dI (width x height x 3)
+    const uint32_t* fwd_samples;  // replay: sample counts of the render replayed
+    float* replay;                // replay: the re-rendered image (optional)
+    int32_t tex_a, tex_r;         // albedo / roughness texture (-1: none)
+    float* grad_a;                // dL/d(albedo texels), texture w x h x 3
+    float* grad_r;                // dL/d(roughness texels), texture w x h x 3 (channel 0)
+    float* grad_f;                // dL/d(fog density), one float
+};
+
 struct WaveLaunch {
     WaveState W[kWaveGroups];
     int groups;
@@ -111,6 +136,9 @@ struct WaveLaunch {
     uint32_t tail_paths;  // the bounce loop stops when at most this many paths are live; the tail
                           // kernel then finishes them, one thread per slot
     uint32_t* progress;   // host-mapped word the device loop publishes finished pixels to (or null)
+    int adj_mode;         // kAdj*: the kernels of an adjoint pass
+    const AdjPass* adj;   // device AdjPass of an adjoint pass
+    int grid_adj_shade[3], grid_adj_finalize;  // their grids
 };
 
 // Every group's state, as one kernel argument.
@@ -162,5 +190,16 @@ cudaError_t wave_build_graph(const WaveLaunch& L, cudaStream_t capture_stream, c
 // One graph with an independent bounce loop + tail per launch description (batched rendering).
 cudaError_t wave_build_graph_batch(const WaveLaunch* Ls, int n, cudaStream_t capture_stream, const cudaStream_t* side,
                                    const cudaEvent_t* fork, cudaGraphExec_t* exec_out);
+
+// The adjoint forms of a bounce's kernels after the traversal (sr_wave_adjoint.cu): the late
+// finalize (late = true) or the finalize, the shade kernels, the tail; grids from their occupancy.
+void wave_adj_finalize(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st, bool late);
+void wave_adj_shade(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st);
+cudaError_t wave_adj_tail(const WaveLaunch& L, int cur, cudaStream_t st);
+void wave_adj_grid_sizes(WaveLaunch& L, int sms);
+// Record mode's sweep: every kept sample of every slot, once dL/dI of the recorded render is known
+// (`samples`: that render's sample counts).
+cudaError_t launch_adjoint_checkpoint(const WaveLaunch& L, const float* d_image, const uint32_t* samples,
+                                      cudaStream_t st);
 
 }  // namespace sr

@@ -15,7 +15,7 @@ import math
 import numpy as np
 import pytest
 
-from sharpray_gb300 import (Context, Fog, Quat, SharpRayError, Transform, View, _abi, adjoint_albedo, adjoint_texture,
+from sharpray_gb300 import (Context, Fog, Quat, SharpRayError, StateError, Transform, View, _abi, adjoint_albedo, adjoint_texture,
                             render_params, synth)
 from sharpray_gb300.synth import MeshDesc, ObjectDesc, SceneDesc, TextureDesc, look_rotation
 from tests.adjoint_scenes import adjoint_scene, roughness_scene
@@ -348,8 +348,9 @@ def grad_agreement(got: np.ndarray, want: np.ndarray) -> tuple:
     return rel_l2, float(ok.mean())
 
 
+@pytest.mark.parametrize("form", [_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_ADJOINT_REPLAY_PIXEL])
 @pytest.mark.parametrize("fog,general", [(False, False), (True, False), (True, True)])
-def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general):
+def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general, form):
     """The GPU adjoint (float, sr_adjoint_all: albedo texture, roughness texture, fog density from one
     replay) against the oracle's FP64 replay adjoint on the same scene, dL/dI and sample counts.  The
     two evaluate the same estimator -- the oracle with dual numbers in double through the reference's
@@ -369,6 +370,7 @@ def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general):
         d.objects.append(ObjectDesc("ball", Transform(), {"albedo": (0.7, 0.9, 0.8), "roughness": 0.5,
                                                           "color_texture": 1}, ("sphere", (0.6, -0.75, -0.3), 0.25)))
     rig = Rig(torch, d)
+    rig.scene.set_adjoint_replay(form)
     img = rig.image()
     target = (img * np.float32(0.6) + np.float32(0.05)).astype(np.float32)
     d_image = (2.0 * (img - target)).astype(np.float32)
@@ -381,7 +383,7 @@ def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general):
     v = d.view.to_c()
     _abi.check(rig.ctx._lib.sr_adjoint_all(rig.scene.handle, C.byref(v), C.byref(rig.params), C.byref(rig.aovs),
                                            C.c_void_p(di.data_ptr()), ta.id, C.c_void_p(g[0].data_ptr()), tr.id,
-                                           C.c_void_p(g[1].data_ptr()), C.c_void_p(g[2].data_ptr()),
+                                           C.c_void_p(g[1].data_ptr()), C.c_void_p(g[2].data_ptr()) if fog else None,
                                            C.c_void_p(replay.data_ptr()), C.c_void_p(current_stream_handle())))
     torch.cuda.synchronize()
     o = oracle_mod.instantiate(d)
@@ -399,3 +401,95 @@ def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general):
     if fog:
         gd = float(g[2].cpu().numpy()[0])
         assert abs(gd - gf) <= 1e-3 * abs(gf), (gd, gf)
+
+
+def adjoint_all(rig, d_image, ta, tr, fog: bool, replay=None):
+    """sr_adjoint_all into fresh gradient buffers; returns (albedo, roughness, density) on the host."""
+    torch = rig.torch
+    g = [torch.zeros(ta.height * ta.width * 3, device="cuda"), torch.zeros(tr.height * tr.width * 3, device="cuda"),
+         torch.zeros(1, device="cuda")]
+    v = rig.d.view.to_c()
+    _abi.check(rig.ctx._lib.sr_adjoint_all(rig.scene.handle, C.byref(v), C.byref(rig.params), C.byref(rig.aovs),
+                                           C.c_void_p(d_image.data_ptr()), ta.id, C.c_void_p(g[0].data_ptr()), tr.id,
+                                           C.c_void_p(g[1].data_ptr()), C.c_void_p(g[2].data_ptr()) if fog else None,
+                                           C.c_void_p(replay.data_ptr()) if replay is not None else None,
+                                           C.c_void_p(current_stream_handle())))
+    torch.cuda.synchronize()
+    return [x.cpu().numpy() for x in g]
+
+
+def replay_rig(torch, fog: bool, general: bool, spp: int = 4):
+    d = roughness_scene(spp)
+    d.width, d.height = 40, 30
+    d.bounces = 6
+    d.indirect_clamp = 3.0
+    if fog:
+        d.fog = Fog(0.08, (0.8, 0.75, 0.7), 0.5, 0.2)
+    if general:
+        d.objects.append(ObjectDesc("ball", Transform(), {"albedo": (0.7, 0.9, 0.8), "roughness": 0.5,
+                                                          "color_texture": 1}, ("sphere", (0.6, -0.75, -0.3), 0.25)))
+    return Rig(torch, d)
+
+
+@pytest.mark.parametrize("fog,general", [(False, False), (True, False), (True, True)])
+def test_wavefront_replay_equals_pixel_replay(torch_mod, fog, general):
+    """The wavefront replay (the render's kernels recording vertices, swept at each sample's end) and the
+    per-pixel replay differentiate the same paths: replayed images bit-identical to the render, gradients
+    equal up to the order of the atomic additions; the host-loop and graph forms agree too."""
+    torch = torch_mod
+    rig = replay_rig(torch, fog, general)
+    img = rig.image()
+    d_image = torch.from_numpy((2.0 * (img - (img * np.float32(0.6) + np.float32(0.05)))).astype(np.float32)).cuda()
+    ta, tr = rig.tex[1], rig.tex[3]
+    out = {}
+    for form, mode in ((_abi.SR_ADJOINT_REPLAY_PIXEL, _abi.SR_RENDER_AUTO),
+                       (_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_RENDER_AUTO),
+                       (_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_RENDER_WAVEFRONT)):
+        rig.scene.set_adjoint_replay(form)
+        rig.scene.set_render_mode(mode)
+        replay = torch.zeros(rig.d.width * rig.d.height * 3, device="cuda")
+        out[(form, mode)] = adjoint_all(rig, d_image, ta, tr, fog, replay)
+        assert np.array_equal(replay.cpu().numpy().view(np.uint32), img.view(np.uint32)), (form, mode)
+    rig.scene.set_render_mode(_abi.SR_RENDER_AUTO)
+    ref = out[(_abi.SR_ADJOINT_REPLAY_PIXEL, _abi.SR_RENDER_AUTO)]
+    for key, got in out.items():
+        for k, (a, b) in enumerate(zip(got, ref)):
+            if k == 2 and not fog:
+                continue
+            scale = float(np.abs(b).max())
+            assert scale > 0.0, (key, k)
+            assert np.allclose(a, b, rtol=1e-4, atol=1e-5 * scale), (key, k, float(np.abs(a - b).max()), scale)
+
+
+@pytest.mark.parametrize("fog", [False, True])
+def test_checkpointed_adjoint_equals_replay(torch_mod, fog):
+    """sr_render_checkpointed renders the same image as sr_render_device and keeps every sample's vertices;
+    sr_adjoint_checkpointed then gives the gradients a replay of the same samples gives (no traversal)."""
+    torch = torch_mod
+    rig = replay_rig(torch, fog, False)
+    img = rig.image()
+    d_image = torch.from_numpy((2.0 * (img - (img * np.float32(0.6) + np.float32(0.05)))).astype(np.float32)).cuda()
+    ta, tr = rig.tex[1], rig.tex[3]
+    rig.scene.set_adjoint_replay(_abi.SR_ADJOINT_REPLAY_WAVEFRONT)
+    want = adjoint_all(rig, d_image, ta, tr, fog)
+    for b in rig.bufs.values():
+        b.zero_()
+    kept = rig.scene.render_checkpointed(rig.d.view, rig.params, rig.aovs, current_stream_handle())
+    torch.cuda.synchronize()
+    tiles = ((rig.d.width + 7) // 8) * ((rig.d.height + 3) // 4)
+    assert kept == tiles * 32 * rig.d.spp * ((rig.d.bounces + 1) * 128 + 1)
+    ck = (rig.bufs["radiance"] + rig.bufs["radiance_fog"]).cpu().numpy()
+    assert np.array_equal(ck.view(np.uint32), img.view(np.uint32)), "a checkpointed render is the same render"
+    g = [torch.zeros(ta.height * ta.width * 3, device="cuda"), torch.zeros(tr.height * tr.width * 3, device="cuda"),
+         torch.zeros(1, device="cuda")]
+    rig.scene.adjoint_checkpointed(d_image.data_ptr(), ta, g[0].data_ptr(), tr, g[1].data_ptr(),
+                                   g[2].data_ptr() if fog else None, current_stream_handle())
+    torch.cuda.synchronize()
+    for k, (a, b) in enumerate(zip([x.cpu().numpy() for x in g], want)):
+        if k == 2 and not fog:
+            continue
+        scale = float(np.abs(b).max())
+        assert scale > 0.0 and np.allclose(a, b, rtol=1e-4, atol=1e-5 * scale), (k, float(np.abs(a - b).max()), scale)
+    rig.scene.release_checkpoint()
+    with pytest.raises(StateError):
+        rig.scene.adjoint_checkpointed(d_image.data_ptr(), ta, g[0].data_ptr())
