@@ -490,6 +490,34 @@ struct SceneQuery {
 
     SR_DEV bool is_any() const { return ANY || (DYN && any_hit); }
 
+    // The query's state as kQueryWords words (and back), field by field so that it stays in
+    // registers; ray reciprocals are recomputed by make_ray, which gives the same bits.
+    static constexpr int kQueryWords = 36;
+    SR_DEV void save(uint32_t* w) const {
+        const float f[] = {wr.o.x, wr.o.y, wr.o.z, wr.d.x, wr.d.y, wr.d.z, cr.o.x, cr.o.y, cr.o.z, cr.d.x, cr.d.y,
+                           cr.d.z, cur_best, lscale, ob_u, ob_v, best.dist, best.tl, best.u, best.v, node.t};
+#pragma unroll
+        for (int i = 0; i < 21; ++i) w[i] = __float_as_uint(f[i]);
+        const int n[] = {best.obj, best.tri, node.child, node.count, sp, mesh_base, leaf_next, leaf_left, tri_next,
+                         tri_left, obj_pos, ob_tri, (int)pops, state,
+                         (in_mesh ? 1 : 0) | (has_node ? 2 : 0) | (any_hit ? 4 : 0)};
+#pragma unroll
+        for (int i = 0; i < 15; ++i) w[21 + i] = (uint32_t)n[i];
+    }
+    SR_DEV void load(const uint32_t* w) {
+        auto f = [&](int i) { return __uint_as_float(w[i]); };
+        wr = make_ray(V3{f(0), f(1), f(2)}, V3{f(3), f(4), f(5)});
+        cr = make_ray(V3{f(6), f(7), f(8)}, V3{f(9), f(10), f(11)});
+        cur_best = f(12), lscale = f(13), ob_u = f(14), ob_v = f(15);
+        best = Hit{(int)w[21], (int)w[22], f(16), f(17), f(18), f(19)};
+        node = StackEntry{(int)w[23], (int)w[24], f(20)};
+        sp = (int)w[25], mesh_base = (int)w[26], leaf_next = (int)w[27], leaf_left = (int)w[28];
+        tri_next = (int)w[29], tri_left = (int)w[30], obj_pos = (int)w[31], ob_tri = (int)w[32];
+        pops = w[33];
+        state = (int)w[34];
+        in_mesh = (w[35] & 1u) != 0, has_node = (w[35] & 2u) != 0, any_hit = (w[35] & 4u) != 0;
+    }
+
     SR_DEV void init(const DevScene& S, const Ray& r, bool any = false) {
         any_hit = any;
         const float inf = __int_as_float(0x7f800000);

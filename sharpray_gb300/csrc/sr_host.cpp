@@ -845,6 +845,13 @@ static int compose_impl(SrContext* ctx, const DevAovs& in, uint32_t w, uint32_t 
                         bool denoise, uint8_t* rgb8, cudaStream_t st,
                         float* linear = nullptr);
 
+// Closest-hit queries a traversal launch may set aside (per group and parity): 1/32 of the slots,
+// between 256 and 16384; kDeferBytes each (the query's state and a full traversal stack).
+static uint32_t defer_capacity(size_t slots) {
+    const size_t c = slots / 32;
+    return (uint32_t)(c < 256 ? 256 : (c > 16384 ? 16384 : c));
+}
+
 // Allocates the wavefront path state for a tiles_x x tiles_y grid of 8x4 slot tiles: the records
 // of every slot, then each group's queues, then every group's counters (one block, carved).
 static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
@@ -857,8 +864,8 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         // queues per group slot: ray entries (32 B) trace x2 + shadow x2, 4-byte event 3 x2 + late x2 +
         // resolve; arrays start on 256 bytes
         const size_t rec = sizeof(Rec);
-        size_t bytes = n * (10 * rec + 16 + 4 * rec + 12 * 4 + 1) + (4 + 10 * kWaveGroups) * 256 +
-                       kWaveGroups * kWaveCounters * sizeof(uint32_t);
+        size_t bytes = n * (10 * rec + 16 + 4 * rec + 12 * 4 + 1) + (4 + 12 * kWaveGroups) * 256 +
+                       kWaveGroups * (kWaveCounters * sizeof(uint32_t) + 2 * (size_t)defer_capacity(n) * kDeferBytes);
         SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
         s->wave_slots = (uint32_t)n;
     }
@@ -893,6 +900,9 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         w.q_late[0] = (uint32_t*)take(m, 4);
         w.q_late[1] = (uint32_t*)take(m, 4);
         w.q_sorted = (uint32_t*)take(m, 3 * 4);
+        w.defer_cap = defer_capacity(n);
+        w.defer[0] = (float4*)take(w.defer_cap, kDeferBytes);
+        w.defer[1] = (float4*)take(w.defer_cap, kDeferBytes);
         w.rec_stride = (uint32_t)n;
         w.ev_mark = ev_mark;
     }
@@ -998,7 +1008,7 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
         SR_CUDA(cudaStreamSynchronize(st), "wavefront bounce");
         uint32_t live = 0, done = 0;
         for (int g = 0; g < kWaveGroups; ++g) {
-            live += wave_live(s->counts_host + g * kWaveCounters, cur ^ 1);
+            live += wave_live(s->counts_host + g * kWaveCounters, cur ^ 1, s->ws[g].defer_cap);
             done += s->counts_host[g * kWaveCounters + kCountDone];
         }
         if (s->progress_host) *(volatile uint32_t*)s->progress_host = done;

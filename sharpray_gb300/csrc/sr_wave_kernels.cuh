@@ -260,10 +260,27 @@ constexpr int kLeafWait = SR_LEAF_WAIT;
 // them keeps warps from running each one with a single lane.  Finished lanes are answered in a
 // batch when the warp refills.  Every lane's own sequence of actions is unchanged, so results are
 // those of a plain loop over SceneQuery::step.
+// Closest-hit queries that are still running SR_DEFER_ROUNDS rounds after the queues ran out are
+// set aside -- their complete state (SceneQuery::save and the used stack entries) goes to a defer
+// buffer -- and the next bounce's traversal kernel resumes them before anything else, so that a
+// launch ends soon after its queues do instead of waiting for its longest queries while most SMs
+// idle.  A query's own sequence of actions is unchanged, so results are too; the path is shaded
+// one or more bounces later.  Occlusion queries are never set aside (their answer is needed by
+// this bounce's shading).  0: no deferral.
+#ifndef SR_DEFER_ROUNDS
+#define SR_DEFER_ROUNDS 0
+#endif
+// A deferred query's record: slot, fog tag and the query's words, then its stack entries.
+constexpr int kDeferHeadF4 = 10;  // 2 + SceneQuery::kQueryWords words, rounded up to float4s
+constexpr int kDeferF4 = kDeferHeadF4 + (3 * kSceneStack + 3) / 4;
+static_assert(kDeferF4 * sizeof(float4) == kDeferBytes, "host and device sizes of a defer record differ");
+
 template <bool COUNT, bool GENERAL, typename Start, typename Finish, typename Emit>
 __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec* q0, uint32_t n0, const Rec* q1,
                                                    uint32_t n1, uint32_t* fetch, Ctr& c, uint32_t* err, Start start,
-                                                   Finish finish, Emit emit) {
+                                                   Finish finish, Emit emit, const float4* din = nullptr,
+                                                   uint32_t nd = 0, float4* dout = nullptr, uint32_t* dcount = nullptr,
+                                                   uint32_t dcap = 0) {
 #if SR_SMEM_STACK > 0
     // the first SR_SMEM_STACK entries of every lane's stack in shared memory, the rest local
     constexpr int kTraceBlock = 128;  // threads per block of the traversal kernel
@@ -275,10 +292,12 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
     LocalStack stack{entries};
 #endif
     SceneQuery<false, GENERAL, true> sq;
-    const uint32_t n = n0 + n1;
+    static_assert(2 + SceneQuery<false, GENERAL, true>::kQueryWords <= 4 * kDeferHeadF4, "defer record header");
+    const uint32_t n = nd + n0 + n1;  // deferred queries first, then the two queues
     bool busy = false, pending = false, exhausted = false;
     uint32_t slot = 0, tag = 0;
     const int lane = threadIdx.x & 31;
+    [[maybe_unused]] uint32_t rounds_after = 0;  // rounds since this warp found the queues empty
     for (;;) {
         unsigned idle = __ballot_sync(0xffffffffu, !busy);
         int nidle = __popc(idle);
@@ -297,7 +316,18 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
             if (base + (uint32_t)nidle >= n) exhausted = true;
             if (!busy) {
                 uint32_t idx = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
-                if (idx < n) {
+                if (idx < nd) {  // a query set aside by the last launch: resumed where it stopped
+                    const float4* r = din + (size_t)idx * kDeferF4;
+                    const uint32_t* w = reinterpret_cast<const uint32_t*>(r);
+                    slot = w[0];
+                    tag = w[1];
+                    sq.load(w + 2);
+                    const uint32_t* se = reinterpret_cast<const uint32_t*>(r + kDeferHeadF4);
+                    for (int i = 0; i < sq.sp; ++i)
+                        stack.set(i, StackEntry{(int)se[3 * i], (int)se[3 * i + 1], __uint_as_float(se[3 * i + 2])});
+                    busy = true;
+                } else if (idx < n) {
+                    idx -= nd;
                     // fetch order: bit 2 of SR_TRACE_ORDER puts the occlusion queue first, bits 0
                     // and 1 walk the closest-hit / occlusion queue from its end
                     const bool sfirst = (SR_TRACE_ORDER & 4) != 0;
@@ -327,6 +357,22 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
         if (busy && sq.state == QS_DONE) {
             busy = false;
             pending = true;
+        }
+        if (SR_DEFER_ROUNDS > 0 && exhausted && ++rounds_after >= SR_DEFER_ROUNDS && busy && !sq.any_hit && dcap) {
+            const uint32_t d = atomicAdd(dcount, 1u);
+            if (d < dcap) {  // else the buffer is full and the query runs on here
+                float4* r = dout + (size_t)d * kDeferF4;
+                uint32_t* w = reinterpret_cast<uint32_t*>(r);
+                w[0] = slot;
+                w[1] = tag;
+                sq.save(w + 2);
+                uint32_t* se = reinterpret_cast<uint32_t*>(r + kDeferHeadF4);
+                for (int i = 0; i < sq.sp; ++i) {
+                    const StackEntry e = stack.get(i);
+                    se[3 * i] = (uint32_t)e.child, se[3 * i + 1] = (uint32_t)e.count, se[3 * i + 2] = __float_as_uint(e.t);
+                }
+                busy = false;  // set aside: no answer this launch
+            }
         }
     }
 }
@@ -391,7 +437,9 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveSta
         [&](uint32_t s, int ev) {
             stage.add(eq, ec, s, ev);
             if (ev >= 0) W.ev_mark[s] = event_mark(ev, cur);
-        });
+        },
+        W.defer[cur], wave_deferred(W.counts, W.defer_cap, cur), W.defer[nxt], &W.counts[kCountDefer + nxt],
+        W.defer_cap);
     stage.flush(eq, ec);
     flush_counters<COUNT>(c, counters);
 }
@@ -959,7 +1007,10 @@ template <bool COUNT, bool GENERAL, bool LATE, int ADJ = kAdjNone>
 __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, DevView V, DevParams P, DevAovs out,
                                                        int cur, uint32_t* err, unsigned long long* counters,
                                                        const AdjPass* A) {
-    if (!LATE && blockIdx.x == 0 && threadIdx.x == 0) W.counts[kCountTraceFetch] = 0;  // next trace's fetch cursor
+    if (!LATE && blockIdx.x == 0 && threadIdx.x == 0) {
+        W.counts[kCountTraceFetch] = 0;    // next trace's fetch cursor
+        W.counts[kCountDefer + cur] = 0;  // this bounce's traversal resumed these; the next one fills them
+    }
     __shared__ uint32_t sh[2][3][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
@@ -1047,6 +1098,18 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
             break;
         }
         k -= nl;
+        // queries set aside by the last traversal kernel: traced again from their ray (same answer)
+        const uint32_t nd = wave_deferred(Wg.counts, Wg.defer_cap, cur);
+        if (k < nd) {
+            group = g;
+            const uint32_t* w = reinterpret_cast<const uint32_t*>(Wg.defer[cur] + (size_t)k * kDeferF4);
+            s = w[0];
+            rt = __uint_as_float(w[1]);
+            ro = V3{__uint_as_float(w[2]), __uint_as_float(w[3]), __uint_as_float(w[4])};
+            rd = V3{__uint_as_float(w[5]), __uint_as_float(w[6]), __uint_as_float(w[7])};
+            break;
+        }
+        k -= nd;
     }
     if (group >= 0) {
         const WaveState W = G.W[group];

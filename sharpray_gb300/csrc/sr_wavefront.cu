@@ -132,12 +132,12 @@ __global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur) {
 // are live (the rest go to the tail kernel) and the bounce cap (a runaway guard of twice
 // (max_samples + 1) * (bounces + 2) per pixel) is not reached.  `counts` holds the groups' counters one after another.
 __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, int groups, uint32_t tail,
-                                uint32_t max_iters, uint32_t* err, uint32_t* progress) {
+                                uint32_t max_iters, uint32_t* err, uint32_t* progress, uint32_t defer_cap) {
     uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
     counts[kCountIter] = it;
     uint32_t live = 0, done = 0;
     for (int g = 0; g < groups; ++g) {
-        live += wave_live(counts + g * kWaveCounters, 0);  // next bounce: parity 0
+        live += wave_live(counts + g * kWaveCounters, 0, defer_cap);  // next bounce: parity 0
         done += counts[g * kWaveCounters + kCountDone];
     }
     if (progress) *(volatile uint32_t*)progress = done;  // host-mapped: read by sr_render_progress
@@ -367,7 +367,7 @@ cudaError_t wave_build_graph_batch(const WaveLaunch* Ls, int n, cudaStream_t cap
         // two bounces per group on parallel branches, joined before the loop condition
         cudaError_t e1 = launch_bounces(L, 0, 2, capture_stream, side, fork);
         k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.tail_paths, L.max_iters, L.err,
-                                                     L.progress);
+                                                     L.progress, L.W[0].defer_cap);
         cudaGraph_t captured = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(capture_stream, &captured);
         e = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : cudaGetLastError());

@@ -60,6 +60,10 @@ struct WaveState {
     uint32_t rec_stride;    // slots of all groups (record kind k of slot s at k * rec_stride + s)
     uint8_t* ev_mark;       // per global slot, 1 + event + 3 x parity of the bounce that shades it
     uint32_t* q_sorted;     // this bounce's event queues in slot order, three of `slots` entries
+    float4* defer[2];       // closest-hit queries the traversal kernel set aside at the end of its
+                            // launch (ping-pong by bounce parity), kDeferF4 float4 each: resumed
+                            // first by the next bounce's traversal kernel
+    uint32_t defer_cap;     // entries per defer buffer (0: no deferral)
 };
 
 // Path and pixel records as one array per record kind (SR_REC_SOA = 1) or six / four records per
@@ -72,8 +76,11 @@ struct WaveState {
 #define SR_SORT_EVENTS 1
 #endif
 
+// Bytes of one set-aside traversal (sr_wave_kernels.cuh, kDeferF4): the query's state and its stack.
+constexpr size_t kDeferBytes = 16 * (10 + (3 * 192 + 3) / 4);
+
 // Number of 32-bit counters at WaveState::counts, and their layout.
-constexpr int kWaveCounters = 20;
+constexpr int kWaveCounters = 22;
 enum : int {
     kCountResolve = 0,     // samples finished this bounce without a shadow ray to trace
     kCountIter = 1,        // bounces run by the device loop
@@ -84,15 +91,24 @@ enum : int {
     kCountLate = 8,        // + parity: late finished samples
     kCountEvent = 10,      // + 3 * parity + event: event-queue lengths
     kCountSorted = 16,     // + event: fill cursors of the slot-ordered event queues
+    kCountDefer = 19,      // + parity: queries set aside in defer[parity] (may exceed defer_cap)
 };
-// Paths alive for the bounce of the given parity: queued for a traversal, with a known event, or
-// finished with their last shadow ray still to trace.
+// Paths alive for the bounce of the given parity: queued for a traversal, with a known event,
+// finished with their last shadow ray still to trace, or with a traversal set aside.
 #if defined(__CUDACC__)
 __host__ __device__
 #endif
-inline uint32_t wave_live(const uint32_t* counts, int parity) {
+inline uint32_t wave_deferred(const uint32_t* counts, uint32_t cap, int parity) {
+    const uint32_t n = counts[kCountDefer + parity];
+    return n < cap ? n : cap;
+}
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline uint32_t wave_live(const uint32_t* counts, int parity, uint32_t defer_cap) {
     return counts[kCountTrace + parity] + counts[kCountEvent + 3 * parity] + counts[kCountEvent + 3 * parity + 1] +
-           counts[kCountEvent + 3 * parity + 2] + counts[kCountLate + parity];
+           counts[kCountEvent + 3 * parity + 2] + counts[kCountLate + parity] +
+           wave_deferred(counts, defer_cap, parity);
 }
 
 // Adjoint modes of the wavefront kernels (instantiated in sr_wave_adjoint.cu).  kAdjReplay: the

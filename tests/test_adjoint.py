@@ -8,6 +8,8 @@ non-metallic surface (directions, lobe choices and pdfs do not depend on them), 
 differences of L through sr_scene_update_texture + sr_render_device check the adjoint directly.
 Roulette decisions can flip under a perturbation; where that happens the finite differences at
 eps and 2 eps disagree and that texel channel is left out (the tests require most to be checked).
+The bar is 1 % of the difference quotient plus 1e-3 of the largest gradient; the exact comparison is
+against the oracle's FP64 adjoint (test_adjoint_matches_fp64_oracle).
 """
 import ctypes as C
 import math
@@ -95,7 +97,9 @@ def check_against_fd(rig: Rig, tex_index: int, picks: int, seed: int, eps: float
             continue  # a roulette decision flipped inside the step
         checked += 1
         g = float(grad[y, x, ch])
-        assert abs(g - fds[0]) <= 0.02 * abs(fds[0]) + 2e-3 * scale, (y, x, ch, g, fds)
+        # 1 % of the difference quotient, with a floor of 1e-3 of the largest gradient for texel
+        # channels whose quotient is near zero (float32 images round it there)
+        assert abs(g - fds[0]) <= 0.01 * abs(fds[0]) + 1e-3 * scale, (y, x, ch, g, fds)
     assert checked >= min_checked, f"only {checked} of {len(flat)} texel channels had stable differences"
     # the scene is back to its own texture
     assert np.array_equal(rig.image().view(np.uint32), fwd.view(np.uint32))
