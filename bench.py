@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--variants", action="store_true", help="also time the megakernel render mode")
     ap.add_argument("--autotune-spp", type=int, default=8,
                     help="spp of the autotuner's trial renders at setup (0: default launch geometry)")
-    ap.add_argument("--batch-autotune-spp", type=int, default=0,
+    ap.add_argument("--batch-autotune-spp", type=int, default=4,
                     help="autotune each batched scene with trial renders at this spp (0: defaults)")
     ap.add_argument("--batch-scenes", type=int, default=32,
                     help="scenes of the batched workload timed batched vs one after another (0: skip)")
@@ -241,11 +241,17 @@ def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
         params.append(render_params(*d.render_args()))
         views.append(d.view)
     setup = time.perf_counter() - t0
-    tuned = 0
+    tuned, choices = 0, []
+    t_tune = time.perf_counter()
     if tune_spp > 0:  # each scene's launch geometry from the autotuner (setup, untimed)
         for sc, d, p in zip(scenes, descs, params):
             t = sc.autotune(d.view, p, trial_spp=min(tune_spp, d.spp))
             tuned += int(t["ms"] < t["default_ms"])
+            choices.append({"scene": f"{d.width}x{d.height} {d.spp} spp {d.triangle_count} tris",
+                            "block": t["trace_block_threads"], "trace_per_sm": t["trace_blocks_per_sm"],
+                            "fog_per_sm": t["fog_shade_blocks_per_sm"], "tail_divisor": t["tail_divisor"],
+                            "gain": round(t["gain"], 4) if t["gain"] else None})
+    tune_s = time.perf_counter() - t_tune
     samples = sum(d.width * d.height * d.spp for d in descs)
     lib = ctx._lib
 
@@ -288,6 +294,7 @@ def measure_batch(ctx, count: int, stream, sp, tune_spp: int = 0) -> dict:
             "speedup": res["plain"] / res["batched"], "speedup_vs_host_loop": res["plain_host_loop"] / res["batched"],
             "setup_s": round(setup, 1),
             "autotuned_scenes": tuned if tune_spp > 0 else None,
+            "autotune": {"trial_spp": tune_spp, "seconds": round(tune_s, 1), "choices": choices} if tune_spp > 0 else None,
             "note": "batched: one graph launch, one bounce loop per scene side by side; plain: one "
                     "graph-captured render per scene, back to back; plain_host_loop: one render per scene "
                     "with one launch per bounce kernel from the host; images bit-identical"}

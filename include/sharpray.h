@@ -352,10 +352,11 @@ SR_API int sr_scene_set_seed(SrScene* scene, uint32_t seed);
  * for a wrapper that must replay a render with the stream it was made with. */
 SR_API int sr_scene_get_seed(SrScene* scene, uint32_t* seed);
 
-/* Launch geometry of the wavefront kernels (no counterpart in the reference): blocks per SM of the
- * traversal, fog-shade and surface-shade kernels (0 = as many as fit; never more) and the live-path
- * count slots / tail_divisor at which the tail kernel takes over (0 = the built-in 16).  Results
- * do not depend on it.
+/* Launch geometry of the wavefront kernels (no counterpart in the reference): threads per block of
+ * the traversal kernel (64, 128 or 256; 0 = 128), blocks per SM of the traversal, fog-shade and
+ * surface-shade kernels (0 = as many as fit; never more) and the live-path count slots /
+ * tail_divisor at which the tail kernel takes over (0 = the built-in 16).  Results do not depend
+ * on it.
  * Two loop caps (0 = the built-in runaway guards) bound the work of one render: the iterations of
  * the wavefront bounce loop and the actions (node visits, leaf steps) of one traversal.  A render
  * or trace that reaches either ends early and returns SR_ERR_DEVICE naming the loop cap (error
@@ -371,12 +372,16 @@ typedef struct SrTuning {
     float default_ms;  /* sr_scene_autotune: trial render time of the defaults */
     uint32_t max_bounce_iterations; /* wavefront bounce-loop cap (0 = (max_samples + 1) * (bounces + 2) * 2 + 8) */
     uint32_t max_traversal_steps;   /* per-traversal action cap (0 = 2^24) */
+    uint32_t trace_block_threads;   /* traversal kernel block size: 64, 128 or 256 (0 = 128) */
 } SrTuning;
 SR_API int sr_scene_set_tuning(SrScene* scene, const SrTuning* tuning); /* NULL = defaults */
 SR_API int sr_scene_get_tuning(SrScene* scene, SrTuning* tuning);
-/* Autotuner: renders `params` at trial_spp samples per pixel under candidate launch geometries
- * (traversal blocks per SM: all that fit, one or two fewer; fog-shade blocks: all, two fewer; tail
- * hand-over at slots / 8, 16 or 32), keeps the fastest on the scene and reports it. */
+/* Autotuner: renders `params` at trial_spp samples per pixel under candidate launch geometries, one
+ * dimension after another from the defaults -- traversal block size (128, 64, 256), traversal
+ * blocks per SM (all that fit, one or two fewer), fog-shade blocks per SM (all, two fewer), tail
+ * hand-over (slots / 16, 8, 32) -- keeping the fastest of each, and leaves the result on the scene
+ * (ms: its trial time; default_ms: the defaults').  The BVH node width is not a dimension: the
+ * traversal walks the reference's binary tree, whose child order the bit-exact hits rest on. */
 SR_API int sr_scene_autotune(SrScene* scene, const SrView* view, const SrRenderParams* params, uint32_t trial_spp,
                              SrTuning* chosen);
 

@@ -19,8 +19,8 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsharpray_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["sr_render.cu", "sr_wavefront.cu", "sr_wave_adjoint.cu", "sr_compose.cu", "sr_bvh_build.cu",
-                "sr_overlay.cu", "sr_adjoint.cu"]
+CUDA_SOURCES = ["sr_render.cu", "sr_wavefront.cu", "sr_wave_adjoint.cu", "sr_wave_trace.cu", "sr_compose.cu",
+                "sr_bvh_build.cu", "sr_overlay.cu", "sr_adjoint.cu"]
 HOST_SOURCES = ["sr_host.cpp", "sr_geometry.cpp", "sr_ingest.cpp", "sr_image.cpp"]
 
 

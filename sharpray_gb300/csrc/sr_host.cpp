@@ -1159,8 +1159,12 @@ SR_API int sr_scene_set_tuning(SrScene* s, const SrTuning* t) {
     if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
     if (t && (t->trace_blocks_per_sm < 0 || t->fog_shade_blocks_per_sm < 0 || t->surface_shade_blocks_per_sm < 0))
         return fail(SR_ERR_INVALID_ARG, "blocks per SM must be >= 0");
+    if (t && t->trace_block_threads != 0 && t->trace_block_threads != 64 && t->trace_block_threads != 128 &&
+        t->trace_block_threads != 256)
+        return fail(SR_ERR_INVALID_ARG, "trace_block_threads must be 64, 128 or 256 (or 0)");
     s->tune = t ? WaveTune{t->trace_blocks_per_sm, t->fog_shade_blocks_per_sm, t->surface_shade_blocks_per_sm,
-                           t->tail_divisor, t->max_bounce_iterations, t->max_traversal_steps}
+                           t->tail_divisor, t->max_bounce_iterations, t->max_traversal_steps,
+                           (int)t->trace_block_threads}
                 : WaveTune{};
     return SR_OK;
 }
@@ -1174,12 +1178,14 @@ SR_API int sr_scene_get_tuning(SrScene* s, SrTuning* t) {
     t->tail_divisor = s->tune.tail_div;
     t->max_bounce_iterations = s->tune.max_iters;
     t->max_traversal_steps = s->tune.max_actions;
+    t->trace_block_threads = (uint32_t)s->tune.trace_block;
     return SR_OK;
 }
 
-// Times `params` at trial_spp samples per pixel under each candidate launch geometry -- traversal
-// blocks per SM (all that fit, one or two fewer), fog-shade blocks per SM (all that fit, two
-// fewer), tail hand-over (slots / 8, 16, 32) -- and keeps the fastest on the scene.
+// Times `params` at trial_spp samples per pixel under candidate launch geometries, one dimension at a
+// time from the defaults (coordinate search): traversal block size, traversal blocks per SM,
+// fog-shade blocks per SM, tail hand-over; keeps the fastest of each dimension and leaves the
+// result on the scene.
 SR_API int sr_scene_autotune(SrScene* s, const SrView* view, const SrRenderParams* params, uint32_t trial_spp,
                              SrTuning* out) {
     if (!s || !view || !params) return fail(SR_ERR_INVALID_ARG, "NULL argument");
@@ -1208,29 +1214,48 @@ SR_API int sr_scene_autotune(SrScene* s, const SrView* view, const SrRenderParam
     const int32_t saved_mode = s->render_mode;
     const WaveTune saved = s->tune;
     s->render_mode = SR_RENDER_WAVEFRONT_GRAPH;
-    float best_ms = 0.0f, default_ms = 0.0f;
-    WaveTune best{};
     int rc = SR_OK;
-    const int trace_c[3] = {0, tr - 1, tr - 2}, fog_c[2] = {0, fog - 2};
-    const uint32_t tail_c[3] = {16, 8, 32};
-    for (int a = 0; a < 3 && !rc; ++a)
-        for (int f = 0; f < 2 && !rc; ++f)
-            for (int t = 0; t < 3 && !rc; ++t) {
-                if (trace_c[a] < 0 || fog_c[f] < 0) continue;
-                if ((a > 0 && trace_c[a] < 1) || (f > 0 && fog_c[f] < 1)) continue;
-                s->tune = WaveTune{trace_c[a], fog_c[f], 0, tail_c[t], saved.max_iters, saved.max_actions};
-                rc = render_into(s, view, &p, d, st);  // warm-up (builds the graph)
-                if (!rc) rc = cudaEventRecord(e0, st) == cudaSuccess ? SR_OK : fail(SR_ERR_CUDA, "event");
-                for (int k = 0; k < 2 && !rc; ++k) rc = render_into(s, view, &p, d, st);
-                if (!rc) rc = cudaEventRecord(e1, st) == cudaSuccess ? SR_OK : fail(SR_ERR_CUDA, "event");
-                if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(SR_ERR_CUDA, "autotune render");
-                if (rc) break;
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                ms *= 0.5f;
-                if (a == 0 && f == 0 && t == 0) default_ms = ms;
-                if (best_ms == 0.0f || ms < best_ms) best_ms = ms, best = s->tune;
-            }
+    // one trial: a warm-up render (builds the graph), then two timed renders
+    auto trial = [&](const WaveTune& t, float& ms) {
+        s->tune = t;
+        rc = render_into(s, view, &p, d, st);
+        if (!rc) rc = cudaEventRecord(e0, st) == cudaSuccess ? SR_OK : fail(SR_ERR_CUDA, "event");
+        for (int k = 0; k < 2 && !rc; ++k) rc = render_into(s, view, &p, d, st);
+        if (!rc) rc = cudaEventRecord(e1, st) == cudaSuccess ? SR_OK : fail(SR_ERR_CUDA, "event");
+        if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = fail(SR_ERR_CUDA, "autotune render");
+        ms = 0.0f;
+        if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+        ms *= 0.5f;
+        return rc == SR_OK;
+    };
+    WaveTune best{0, 0, 0, 16, saved.max_iters, saved.max_actions, 128};
+    float best_ms = 0.0f, default_ms = 0.0f;
+    if (trial(best, default_ms)) best_ms = default_ms;
+    auto consider = [&](WaveTune t) {
+        float ms = 0.0f;
+        if (!rc && trial(t, ms) && ms < best_ms) best_ms = ms, best = t;
+    };
+    for (int blk : {64, 256}) {  // traversal block size
+        WaveTune t = best;
+        t.trace_block = blk;
+        consider(t);
+    }
+    const int fit = best.trace_block == 128 ? tr : wave_trace_occupancy(s->dev.general != 0, best.trace_block);
+    for (int fewer : {1, 2}) {  // traversal blocks per SM: one or two fewer than fit
+        WaveTune t = best;
+        t.trace_per_sm = fit - fewer;
+        if (t.trace_per_sm >= 1) consider(t);
+    }
+    if (fog - 2 >= 1) {  // fog-shade blocks per SM
+        WaveTune t = best;
+        t.fog_per_sm = fog - 2;
+        consider(t);
+    }
+    for (uint32_t div : {8u, 32u}) {  // tail hand-over
+        WaveTune t = best;
+        t.tail_div = div;
+        consider(t);
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     s->render_mode = saved_mode;

@@ -393,9 +393,11 @@ __device__ __forceinline__ int extend_answer(const WaveState& W, uint32_t s, con
 // samples in the same persistent loop (any hit -> black in opaque scenes, else the fog
 // transmittance, written over the request's origin; SampleSkyLight scene.cs:758-772).  One loop
 // for both keeps the SMs busy while either kind's last long rays finish.
-template <bool COUNT, bool GENERAL, bool WITH_SHADOW>
-__global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveState W, DevScene S, int cur,
-                                                                          uint32_t* err, unsigned long long* counters) {
+// BLOCK: threads per block (64, 128 or 256, chosen at run time by the scene's tuning); the register
+// cap keeps SR_TRACE_MIN_BLOCKS x 128 threads resident per SM whatever the block size.
+template <bool COUNT, bool GENERAL, bool WITH_SHADOW, int BLOCK = 128>
+__global__ void __launch_bounds__(BLOCK, SR_TRACE_MIN_BLOCKS * 128 / BLOCK)
+    k_wave_trace(WaveState W, DevScene S, int cur, uint32_t* err, unsigned long long* counters) {
     const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         W.counts[kCountResolve] = 0;  // the next bounce's queues start empty
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS) k_wave_trace(WaveSta
         W.counts[kCountSorted + EV_MISS] = 0;
         W.counts[kCountSorted + EV_SURF] = 0;
     }
-    __shared__ uint32_t ring[kBlockWarps][3 * 64];
+    __shared__ uint32_t ring[BLOCK / 32][3 * 64];
     WarpStage<3> stage;
     stage.init(ring[threadIdx.x >> 5]);
     uint32_t* const eq[3] = {W.q_event[cur] + (size_t)EV_FOG * W.slots, W.q_event[cur] + (size_t)EV_MISS * W.slots,

@@ -193,12 +193,14 @@ template <bool COUNT, bool GENERAL>
 static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st) {
     if (SR_TRACE_OCTANT_SORT) k_trace_octant_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W, cur);
     const bool loop_shadows = GENERAL && L.S.has_transparent;
-    if (loop_shadows) {
+    if (!COUNT && L.trace_block != 128) {
+        wave_trace_block(L, W, cur, st, loop_shadows);
+    } else if (loop_shadows) {
         k_wave_trace<COUNT, GENERAL, false><<<L.grid_trace, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
-        k_wave_shadow_loop<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
     } else {
         k_wave_trace<COUNT, GENERAL, true><<<L.grid_trace, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
     }
+    if (loop_shadows) k_wave_shadow_loop<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
     // an adjoint pass runs the same traversal, then the recording forms of the other kernels
     if (L.adj_mode != kAdjNone)
         wave_adj_finalize(L, W, cur, st, true);
@@ -288,6 +290,12 @@ void wave_grid_sizes(WaveLaunch& L, int sms, const WaveTune* tune) {
         occupancy<true>(b);
     else
         occupancy<false>(b);
+    // the traversal kernel's block size (counting renders keep the default 128)
+    L.trace_block = 128;
+    if (tune && (tune->trace_block == 64 || tune->trace_block == 256) && !L.counters) {
+        L.trace_block = tune->trace_block;
+        b[0] = wave_trace_occupancy(L.general != 0, L.trace_block);
+    }
     if (tune) {  // a tuned count never exceeds what fits
         auto pick = [](int want, int fit) { return want > 0 && want < fit ? want : fit; };
         b[0] = pick(tune->trace_per_sm, b[0]);

@@ -146,6 +146,7 @@ struct WaveLaunch {
     uint32_t* err;
     unsigned long long* counters;
     int grid_trace, grid_shadow, grid_finalize;
+    int trace_block;    // threads per block of the traversal kernel (64, 128 or 256)
     int grid_shade[3];  // per event kernel (fog, miss, surface), or [0] for the sorted kernel
     int general;  // 1: kernels with analytic shapes, transparency/media, normal maps, procedural sky
     uint32_t max_iters;
@@ -189,6 +190,7 @@ struct WaveTune {
     uint32_t tail_div;    // the tail kernel takes over at slots / tail_div live paths (0 = SR_TAIL_DIV)
     uint32_t max_iters;   // bounce-loop cap (0 = the runaway guard)
     uint32_t max_actions; // per-traversal action cap (0 = kDefaultMaxActions)
+    int trace_block;      // threads per block of the traversal kernel: 64, 128 or 256 (0 = 128)
 };
 // Resident blocks per SM of the traversal, fog-shade and surface-shade kernels.
 void wave_occupancy(bool general, int* trace, int* fog, int* surface);
@@ -213,6 +215,9 @@ void wave_adj_finalize(const WaveLaunch& L, const WaveState& W, int cur, cudaStr
 void wave_adj_shade(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st);
 cudaError_t wave_adj_tail(const WaveLaunch& L, int cur, cudaStream_t st);
 void wave_adj_grid_sizes(WaveLaunch& L, int sms);
+// The traversal kernel at 64 or 256 threads per block (sr_wave_trace.cu) and its resident blocks per SM.
+void wave_trace_block(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st, bool loop_shadows);
+int wave_trace_occupancy(bool general, int block);
 // Record mode's sweep: every kept sample of every slot, once dL/dI of the recorded render is known
 // (`samples`: that render's sample counts).
 cudaError_t launch_adjoint_checkpoint(const WaveLaunch& L, const float* d_image, const uint32_t* samples,

@@ -113,8 +113,12 @@ def test_tuning_leaves_results_unchanged(batch_scenes):
     for tune in ((3, 4, 2, 8), (1, 1, 1, 64), (0, 0, 0, 0)):
         s.set_tuning(*tune)
         same(host(render_single(torch, ctx, d, s)), ref)
+    for threads in (64, 256):  # the traversal kernel's block size
+        for per_sm in (0, 2):
+            s.set_tuning(trace_blocks_per_sm=per_sm, trace_block_threads=threads)
+            same(host(render_single(torch, ctx, d, s)), ref)
     chosen = s.autotune(d.view, render_params(*d.render_args()), trial_spp=2)
     assert chosen["ms"] > 0 and chosen["default_ms"] > 0 and chosen["ms"] <= chosen["default_ms"]
-    assert chosen["tail_divisor"] in (8, 16, 32)
+    assert chosen["tail_divisor"] in (8, 16, 32) and chosen["trace_block_threads"] in (64, 128, 256)
     same(host(render_single(torch, ctx, d, s)), ref)
     s.set_tuning()

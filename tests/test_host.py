@@ -174,6 +174,11 @@ def test_progress_adjoint_and_update_validation(host_ctx):
     assert (t["max_bounce_iterations"], t["max_traversal_steps"]) == (6, 40)
     s.set_tuning()
     assert s.get_tuning()["max_traversal_steps"] == 0
+    s.set_tuning(trace_block_threads=256)
+    assert s.get_tuning()["trace_block_threads"] == 256
+    with pytest.raises(SharpRayError):
+        s.set_tuning(trace_block_threads=96)
+    s.set_tuning()
     d, t = C.c_uint32(), C.c_uint32()
     with pytest.raises(SharpRayError):
         _abi.check(lib.sr_render_progress(s.handle, None, C.byref(t)))
