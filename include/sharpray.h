@@ -95,12 +95,18 @@ typedef struct SrShape {
     float params[6];
 } SrShape;
 
-/* Reference: Fog scene.cs:438-442 (exponential height fog; height_falloff must be > 0). */
+/* Reference: Fog scene.cs:438-442: exponential height fog, density * exp(-height_falloff * y), for
+ * height_falloff > 0 (top_height is then ignored).  An extension without a reference counterpart:
+ * height_falloff == 0 gives a homogeneous medium of constant density below top_height (finite) and
+ * none above it -- bounded, because through an unbounded homogeneous medium no sky light would reach
+ * any point.  Its optical depth is density x the length of the segment below the top, and its
+ * free-flight draw is the reference's single exponential per segment. */
 typedef struct SrFog {
     float density;
     float color[3];
     float anisotropy;
     float height_falloff;
+    float top_height;
 } SrFog;
 
 /* Reference: SkyProcedural ctor scene.cs:341-354 + SunProcedural scene.cs:281-298. */

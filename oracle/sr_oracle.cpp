@@ -924,8 +924,30 @@ struct Fog {
     Col color;
     float anisotropy;
     float height_falloff;
+    float top_height;  // the homogeneous extension (height_falloff 0): the medium's top
     float density_at(float y) const { return density * std::exp(-height_falloff * y); }
+    // Homogeneous fog (height_falloff 0; an extension, no counterpart in the reference, whose
+    // formulas divide by the falloff): the part [enter, exit) of the ray below the top height.
+    bool slab_span(const Ray& ray, float* enter, float* exit) const {
+        const float hd = ray.dir.y, ho = ray.origin.y;
+        *enter = 0.0f;
+        *exit = kInf;
+        if (hd == 0.0f) return ho < top_height;
+        const float tc = (top_height - ho) / hd;
+        if (hd > 0.0f) {
+            *exit = tc;
+            return tc > 0.0f;
+        }
+        *enter = net_max(0.0f, tc);
+        return true;
+    }
     float optical_depth(const Ray& ray, float start, float end) const {
+        if (height_falloff == 0.0f) {  // density x the length of [start, end] below the top
+            float enter, exit;
+            if (!slab_span(ray, &enter, &exit)) return 0.0f;
+            const float a = net_max(start, enter), b = net_min(end, exit);
+            return b > a ? density * (b - a) : 0.0f;
+        }
         float hd = ray.dir.y;
         float hs = ray.origin.y + start * hd;
         float he = ray.origin.y + end * hd;
@@ -941,6 +963,16 @@ struct Fog {
         float hs = ho + start * hd;
         float u = rng.next_exponential();
         float t;
+        if (height_falloff == 0.0f) {  // the optical-depth budget spent at constant density
+            float enter, exit;
+            if (!slab_span(ray, &enter, &exit)) return false;
+            t = net_max(start, enter) + u / density;
+            if (t < exit && t < end) {
+                *t_out = t;
+                return true;
+            }
+            return false;
+        }
         if (std::fabs(hd) < 1e-6f) {
             float ds = density_at(hs);
             if (ds <= 0.0f) return false;
@@ -1749,6 +1781,12 @@ DCol opaque_eval_dual(const Surface& s, V3 view, V3 light, const DCol& albedo, D
 
 // Fog.OpticalDepth (scene.cs:452-467) over [start, end] in double with a dual density.
 Dual optical_depth_dual(const Fog& f, const Ray& r, double start, double end, Dual density) {
+    if (f.height_falloff == 0.0f) {  // homogeneous: density x the length of [start, end] below the top
+        float enter, exit;
+        if (!f.slab_span(r, &enter, &exit)) return dual(0.0);
+        const double a = std::max(start, (double)enter), b = std::min(end, (double)exit);
+        return density * dual(b > a ? b - a : 0.0);
+    }
     const double hd = r.dir.y, ho = r.origin.y, k = f.height_falloff;
     const double hs = ho + start * hd;
     const double es = std::exp(-k * hs);
@@ -2195,7 +2233,8 @@ void oracle_scene_set_sky_procedural(void* sp, const SrSkyProcedural* p) {
 void oracle_scene_set_fog(void* sp, const SrFog* f) {
     Scene* s = (Scene*)sp;
     s->has_fog = true;
-    s->fog = {f->density, {f->color[0], f->color[1], f->color[2]}, f->anisotropy, f->height_falloff};
+    s->fog = {f->density, {f->color[0], f->color[1], f->color[2]}, f->anisotropy, f->height_falloff,
+              f->height_falloff == 0.0f ? f->top_height : kInf};
 }
 
 // Object ctor scene.cs:214-225: world bounds from the rotated local bounds.

@@ -79,7 +79,8 @@ class SrShape(C.Structure):
 
 
 class SrFog(C.Structure):
-    _fields_ = [("density", C.c_float), ("color", _f3), ("anisotropy", C.c_float), ("height_falloff", C.c_float)]
+    _fields_ = [("density", C.c_float), ("color", _f3), ("anisotropy", C.c_float), ("height_falloff", C.c_float),
+                ("top_height", C.c_float)]
 
 
 class SrSkyProcedural(C.Structure):

@@ -372,15 +372,18 @@ class SkyProcedural:
 
 @dataclass
 class Fog:
-    """Exponential height fog (scene.cs:438-505).  ``height_falloff`` must be > 0."""
+    """Exponential height fog (scene.cs:438-505) for ``height_falloff`` > 0; with ``height_falloff``
+    0, a homogeneous medium below ``top_height`` (an extension; the top must be finite)."""
     density: float
     color: Sequence[float]
     anisotropy: float
     height_falloff: float
+    top_height: float = math.inf
 
     def to_c(self) -> SrFog:
         f = SrFog()
         f.density, f.anisotropy, f.height_falloff = float(self.density), float(self.anisotropy), float(self.height_falloff)
+        f.top_height = float(self.top_height)
         f.color[:] = [float(c) for c in self.color]
         return f
 

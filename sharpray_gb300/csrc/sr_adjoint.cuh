@@ -120,6 +120,12 @@ __device__ __forceinline__ Col opaque_eval_droughness(const Surface& s, V3 view,
 // Optical depth per unit fog density along r over [0, t] (t may be +inf): the integral of
 // exp(-falloff * height) that Fog.OpticalDepth scales by the density (fog_transmittance_inf).
 __device__ __forceinline__ float fog_depth_unit(const DevScene& S, const Ray& r, float t) {
+    if (S.fog_falloff == 0.0f) {  // homogeneous: the length of [0, t] below the top
+        float enter, exit;
+        if (!fog_slab_span(S, r, enter, exit)) return 0.0f;
+        const float e = fminf(t, exit);
+        return e > enter ? e - enter : 0.0f;
+    }
     const float hd = r.d.y, hs = r.o.y;
     const float es = sr_exp(-S.fog_falloff * hs);
     if (fabsf(hd) < 1e-6f) return es * t;

@@ -925,7 +925,28 @@ SR_DEV Col sky_light_radiance(const DevScene& S, int texel, V3 dir, Ctr& c) {
 
 // ---- fog (scene.cs:445-496) -----------------------------------------------------------------------
 SR_DEV float fog_density_at(const DevScene& S, float y) { return S.fog_density * sr_exp(-S.fog_falloff * y); }
+// Homogeneous fog (an extension for falloff 0, no reference counterpart): the part [enter, exit) of
+// ray r (t >= 0) below the medium's top height; false when the ray never is below it.
+SR_DEV bool fog_slab_span(const DevScene& S, const Ray& r, float& enter, float& exit) {
+    const float inf = __int_as_float(0x7f800000);
+    const float hd = r.d.y, ho = r.o.y;
+    enter = 0.0f;
+    exit = inf;
+    if (hd == 0.0f) return ho < S.fog_top;
+    const float tc = (S.fog_top - ho) / hd;  // where the ray crosses the top
+    if (hd > 0.0f) {
+        exit = tc;
+        return tc > 0.0f;
+    }
+    enter = fmaxf(0.0f, tc);
+    return true;
+}
 SR_DEV float fog_transmittance_inf(const DevScene& S, const Ray& r) {
+    if (S.fog_falloff == 0.0f) {  // homogeneous: density x the length below the top
+        float enter, exit;
+        if (!fog_slab_span(S, r, enter, exit)) return 1.0f;
+        return sr_exp(-(S.fog_density * (exit - enter)));
+    }
     // OpticalDepth over [0, +inf).
     float hd = r.d.y;
     float inf = __int_as_float(0x7f800000);
@@ -942,6 +963,16 @@ SR_DEV bool fog_scatter_distance(const DevScene& S, const Ray& r, float end, Rng
     float hs = ho + 0.0f * hd;
     float u = rng_exponential(rng);
     float t;
+    if (S.fog_falloff == 0.0f) {  // homogeneous: the optical-depth budget spent at constant density
+        float enter, exit;
+        if (!fog_slab_span(S, r, enter, exit)) return false;
+        t = enter + u / S.fog_density;
+        if (t < exit && t < end) {
+            t_out = t;
+            return true;
+        }
+        return false;
+    }
     if (fabsf(hd) < 1e-6f) {
         float ds = fog_density_at(S, hs);
         if (ds <= 0.0f) return false;

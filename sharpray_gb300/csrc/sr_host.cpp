@@ -478,8 +478,13 @@ SR_API int sr_scene_set_sky_procedural(SrScene* s, const SrSkyProcedural* sky) {
 SR_API int sr_scene_set_fog(SrScene* s, const SrFog* fog) {
     if (!s || !fog) return fail(SR_ERR_INVALID_ARG, "NULL argument");
     if (s->built) return fail(SR_ERR_STATE, "Scene already built");
-    if (!(fog->height_falloff > 0.0f))
-        return fail(SR_ERR_INVALID_ARG, "Fog height_falloff must be > 0 (the reference divides by it)");
+    if (!(fog->height_falloff >= 0.0f) || std::isinf(fog->height_falloff))
+        return fail(SR_ERR_INVALID_ARG, "Fog height_falloff must be finite and >= 0");
+    if (fog->height_falloff == 0.0f && !std::isfinite(fog->top_height))
+        return fail(SR_ERR_INVALID_ARG,
+                    "a homogeneous fog (height_falloff 0) needs a finite top_height: through an unbounded medium "
+                    "no sky light reaches the scene");
+    if (!(fog->density > 0.0f) || !std::isfinite(fog->density)) return fail(SR_ERR_INVALID_ARG, "Fog density must be > 0");
     if (!(fog->anisotropy > -1.0f && fog->anisotropy < 1.0f))
         return fail(SR_ERR_INVALID_ARG, "Fog anisotropy must be in (-1, 1)");
     s->has_fog = true;
@@ -726,6 +731,7 @@ SR_API int sr_scene_build(SrScene* s) {
     if (s->has_fog) {
         d.fog_density = s->fog.density;
         d.fog_falloff = s->fog.height_falloff;
+        d.fog_top = s->fog.height_falloff == 0.0f ? s->fog.top_height : __builtin_inff();
         d.fog_g = s->fog.anisotropy;
         d.fog_color = mk4(s->fog.color[0], s->fog.color[1], s->fog.color[2], 0);
     }

@@ -97,7 +97,8 @@ struct SR_ALIGN16 DevScene {
                       // procedural sky); 0 = meshes + texture sky only
     uint32_t max_actions;  // cap on the actions of one traversal (kDefaultMaxActions unless tuned)
     int32_t pad1[2];
-    float fog_density, fog_falloff, fog_g, pad;
+    float fog_density, fog_falloff, fog_g;
+    float fog_top;  // homogeneous fog (falloff 0): the medium's top height; +inf for the height fog
     float4 fog_color;
 };
 

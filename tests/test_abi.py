@@ -68,9 +68,17 @@ def test_no_mutation_after_build(host_ctx):
 
 
 def test_fog_height_falloff_must_be_positive(host_ctx):
+    """Height fog needs falloff > 0 (the reference divides by it); falloff 0 is the homogeneous
+    extension, which needs a finite top height."""
+    import math
     s = _tiny_scene(host_ctx)
-    with pytest.raises(SharpRayError, match="height_falloff"):
+    with pytest.raises(SharpRayError, match="top_height"):
         s.set_fog(Fog(0.02, (1, 1, 1), 0.6, 0.0))
+    for bad in (Fog(0.02, (1, 1, 1), 0.6, -0.1), Fog(0.02, (1, 1, 1), 0.6, math.inf), Fog(0.0, (1, 1, 1), 0.6, 0.1),
+                Fog(0.02, (1, 1, 1), 1.0, 0.1)):
+        with pytest.raises(SharpRayError):
+            s.set_fog(bad)
+    s.set_fog(Fog(0.02, (1, 1, 1), 0.6, 0.0, 2.5))  # bounded homogeneous medium
 
 
 def test_bad_ids_and_zero_scale(host_ctx):

@@ -353,7 +353,7 @@ def grad_agreement(got: np.ndarray, want: np.ndarray) -> tuple:
 
 
 @pytest.mark.parametrize("form", [_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_ADJOINT_REPLAY_PIXEL])
-@pytest.mark.parametrize("fog,general", [(False, False), (True, False), (True, True)])
+@pytest.mark.parametrize("fog,general", [(False, False), (True, False), (True, True), ("homogeneous", False)])
 def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general, form):
     """The GPU adjoint (float, sr_adjoint_all: albedo texture, roughness texture, fog density from one
     replay) against the oracle's FP64 replay adjoint on the same scene, dL/dI and sample counts.  The
@@ -368,7 +368,9 @@ def test_adjoint_matches_fp64_oracle(torch_mod, oracle_mod, fog, general, form):
     d.width, d.height = 48, 36
     d.bounces = 5
     d.indirect_clamp = 3.0
-    if fog:
+    if fog == "homogeneous":  # the extension: constant density below height 0.2
+        d.fog = Fog(0.15, (0.8, 0.75, 0.7), 0.5, 0.0, 0.2)
+    elif fog:
         d.fog = Fog(0.08, (0.8, 0.75, 0.7), 0.5, 0.2)
     if general:  # an analytic sphere: the kernels' general instantiation
         d.objects.append(ObjectDesc("ball", Transform(), {"albedo": (0.7, 0.9, 0.8), "roughness": 0.5,

@@ -51,7 +51,16 @@ SCENES = {
     # the image bar's own sample count: 1024 spp on small images
     "c1_1024spp": lambda: synth.config_c1(32, 32, 1024),
     "c2_1024spp": lambda: synth.config_c2(48, 32, 1024, rings=120, rock_rings=50, env=(256, 128)),
+    # the homogeneous-fog extension: constant density below height 0.5, the camera above it
+    "c2_homogeneous": lambda: homogeneous(synth.config_c2(48, 32, 16, rings=120, rock_rings=50, env=(256, 128))),
 }
+
+
+def homogeneous(d, density=0.05, top=0.5):
+    from sharpray_gb300 import Fog
+    d.fog = Fog(density, (0.8, 0.75, 0.6), 0.6, 0.0, top)
+    d.name += "_homogeneous_fog"
+    return d
 
 
 @pytest.fixture(scope="module")
@@ -85,7 +94,8 @@ def rel_mse(x, ref):
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-@pytest.mark.parametrize("name", ["c1", "features", "procedural", "c2_reduced", "c1_1024spp", "c2_1024spp"])
+@pytest.mark.parametrize("name", ["c1", "features", "procedural", "c2_reduced", "c1_1024spp", "c2_1024spp",
+                                  "c2_homogeneous"])
 def test_render_matches_oracle(built, name):
     d, g, o = built(name)
     rend = Renderer(g, d.view, *d.render_args())
@@ -231,7 +241,7 @@ def test_counters_track_oracle(built):
     assert c["scene_occlude"] <= oc["scene_occlude"]
 
 
-@pytest.mark.parametrize("name", ["c1", "features", "c2_reduced"])
+@pytest.mark.parametrize("name", ["c1", "features", "c2_reduced", "c2_homogeneous"])
 def test_render_modes_identical(built, name):
     """Megakernel, wavefront (host loop) and wavefront (device graph loop) run the same per-path
     arithmetic in the same order, so their AOVs are bit-identical."""
