@@ -592,7 +592,9 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
         xr = torch.full_like(truth_r, 0.5).requires_grad_(True)
         xs = torch.tensor([1.5 * sigma], device="cuda", requires_grad=True)
         opt = torch.optim.Adam([{"params": [xa, xr], "lr": lr_tex}, {"params": [xs], "lr": lr_density}])
+        base_lr = [g["lr"] for g in opt.param_groups]
         losses = []
+        n_step = [0]
 
         kept = [0]
 
@@ -626,6 +628,13 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
                                               tex_r.id, C.c_void_p(gr.data_ptr()), C.c_void_p(gs.data_ptr()), None,
                                               C.c_void_p(st.cuda_stream)))
             xa.grad, xr.grad, xs.grad = ga, gr, gs
+            # cosine decay of the learning rates over the run: the gradients are Monte Carlo
+            # estimates, and at a fixed rate Adam's normalised steps keep the texels moving by about
+            # the rate per step on the noise alone
+            decay = 0.5 * (1.0 + math.cos(math.pi * min(n_step[0], steps) / (steps + 1)))
+            for g, lr0 in zip(opt.param_groups, base_lr):
+                g["lr"] = lr0 * decay
+            n_step[0] += 1
             opt.step()
             with torch.no_grad():
                 xa.clamp_(0.0, 1.0)
@@ -662,6 +671,7 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
                         f"{d.triangle_count} triangles, {tex}x{tex} albedo + roughness textures, fog 0.03",
             "form": form, "vertex_record_bytes": vertex_bytes,
             "timed_steps": steps, "ms_per_step": 1000 * dt, "texel_grads_per_s": n_grads / dt,
+            "adam": {"lr_textures": lr_tex, "lr_density": lr_density, "schedule": "cosine decay to 0 over the run"},
             "path_samples_per_s": samples * (1 if form == "checkpoint" else 2) / dt,
             "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
             "fog_density": {"true": sigma, "start": 1.5 * sigma, "after": float(xs.detach())},

@@ -155,7 +155,7 @@ struct SrScene {
     WaveState ws[kWaveGroups]{};
     cudaStream_t capture_stream = nullptr;
     cudaStream_t side_streams[kWaveGroups > 1 ? kWaveGroups - 1 : 1] = {};  // groups 1.. of a bounce
-    cudaEvent_t fork_events[kWaveGroups] = {};                              // fork, then joins
+    cudaEvent_t fork_events[kWaveGroups + 1] = {};                          // fork, then joins
     cudaGraphExec_t graph_exec = nullptr;
     WaveLaunch graph_launch{};  // launch parameters baked into graph_exec
     uint32_t* counts_host = nullptr;  // pinned
@@ -868,9 +868,9 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
     if (s->wave_slots < n || !s->wave.ptr) {
         // 32-byte sectors: path records (6 per slot), pixel records (4 per slot); 16-byte medium;
         // queues per group slot: ray entries (32 B) trace x2 + shadow x2, 4-byte event 3 x2 + late x2 +
-        // resolve; arrays start on 256 bytes
+        // resolve x2 + sorted 3; arrays start on 256 bytes
         const size_t rec = sizeof(Rec);
-        size_t bytes = n * (10 * rec + 16 + 4 * rec + 12 * 4 + 1) + (4 + 12 * kWaveGroups) * 256 +
+        size_t bytes = n * (10 * rec + 16 + 4 * rec + 13 * 4 + 1) + (4 + 13 * kWaveGroups) * 256 +
                        kWaveGroups * (kWaveCounters * sizeof(uint32_t) + 2 * (size_t)defer_capacity(n) * kDeferBytes);
         SR_CUDA(s->wave.reserve(bytes), "alloc wavefront state");
         s->wave_slots = (uint32_t)n;
@@ -900,7 +900,8 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         w.q_trace[1] = (Rec*)take(m, rec);
         w.q_event[0] = (uint32_t*)take(m, 3 * 4);
         w.q_event[1] = (uint32_t*)take(m, 3 * 4);
-        w.q_resolve = (uint32_t*)take(m, 4);
+        w.q_resolve[0] = (uint32_t*)take(m, 4);
+        w.q_resolve[1] = (uint32_t*)take(m, 4);
         w.q_shadow[0] = (Rec*)take(m, rec);
         w.q_shadow[1] = (Rec*)take(m, rec);
         w.q_late[0] = (uint32_t*)take(m, 4);
@@ -923,8 +924,9 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     uint32_t tiles_x = (dp.width + 7) / 8, tiles_y = (dp.height + 3) / 4;
     int rc = wave_reserve(s, tiles_x, tiles_y);
     if (rc) return rc;
-    for (int g = 0; g + 1 < kWaveGroups; ++g)
-        if (!s->side_streams[g]) SR_CUDA(cudaStreamCreateWithFlags(&s->side_streams[g], cudaStreamNonBlocking), "stream");
+    // side streams: the other groups' bounces, or (one group) the ready phase of each bounce
+    for (cudaStream_t& side : s->side_streams)
+        if (!side) SR_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "stream");
     for (cudaEvent_t& e : s->fork_events)
         if (!e) SR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
     if (!s->sms) {

@@ -35,8 +35,12 @@ __device__ __forceinline__ size_t pix(const WaveState& W, uint32_t s, int k) {
     return SR_REC_SOA ? (size_t)k * W.rec_stride + s : 4 * (size_t)s + k;
 }
 
-// Tag of a slot whose event `ev` is shaded by the bounce of parity `parity` (0: none).
-__device__ __forceinline__ uint8_t event_mark(int ev, int parity) { return (uint8_t)(1 + ev + 3 * parity); }
+// Tag of a slot whose event `ev` is shaded by the bounce of parity `parity` (0: none); `wait`: the
+// event is decided by that bounce's traversal kernel or the path's shadow ray is traced there, so
+// it is shaded after that kernel (else it is ready at the bounce's start).
+__device__ __forceinline__ uint8_t event_mark(int ev, int parity, int wait) {
+    return (uint8_t)(1 + ev + 3 * parity + 6 * wait);
+}
 
 // Record loads and stores (one place to change how path state is moved).
 __device__ __forceinline__ Rec ld_rec(const Rec* p) { return *p; }
@@ -123,12 +127,26 @@ __device__ __forceinline__ float fog_scatter_t(const DevScene& S, const Ray& ray
     return t;
 }
 
+// The ray sector of a path record shares a 64-byte DRAM burst with the hit sector, which is dead
+// from the shading of a segment until the next traversal writes it.  SR_RAY_HIT_PAIR = 1 stores a
+// zero hit sector with every ray store, so that the burst is written whole instead of half.
+#ifndef SR_RAY_HIT_PAIR
+#define SR_RAY_HIT_PAIR 0
+#endif
+__device__ __forceinline__ void st_ray(const WaveState& W, uint32_t s, const Rec& ray) {
+    st_rec(&W.rec[rix(W, s, R_RAY)], ray);
+    if (SR_RAY_HIT_PAIR) {
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        st_rec(&W.rec[rix(W, s, R_HIT)], Rec{z, z});
+    }
+}
+
 // Start of a sample: the camera ray and a reset path (scene.cs:633-638).
 // `flags`: the path flags a sample starts with (an adjoint pass that keeps every sample's vertices
 // puts the sample index there).
 __device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, const Ray& ray, const Rng& rng,
                                              float sdist = 0.f, uint32_t flags = 0u) {
-    st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, sdist)});
+    st_ray(W, s, Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, sdist)});
     st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(0.f, 0.f, 0.f, 0.f), make_float4(1.f, 1.f, 1.f, fbits(flags))});
     st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, black()));
 }
@@ -266,7 +284,9 @@ constexpr int kLeafWait = SR_LEAF_WAIT;
 // launch ends soon after its queues do instead of waiting for its longest queries while most SMs
 // idle.  A query's own sequence of actions is unchanged, so results are too; the path is shaded
 // one or more bounces later.  Occlusion queries are never set aside (their answer is needed by
-// this bounce's shading).  0: no deferral.
+// this bounce's shading).  0: no deferral.  Measured on the 1080p fog workload (images identical):
+// 16 rounds +1.6 % and 4 rounds -7 % with the events shaded in one phase; 16 rounds -2 % with split
+// phases (SR_SPLIT_PHASES), whose ready phase already fills the ramp-down that deferral shortens.
 #ifndef SR_DEFER_ROUNDS
 #define SR_DEFER_ROUNDS 0
 #endif
@@ -398,19 +418,9 @@ __device__ __forceinline__ int extend_answer(const WaveState& W, uint32_t s, con
 template <bool COUNT, bool GENERAL, bool WITH_SHADOW, int BLOCK = 128>
 __global__ void __launch_bounds__(BLOCK, SR_TRACE_MIN_BLOCKS * 128 / BLOCK)
     k_wave_trace(WaveState W, DevScene S, int cur, uint32_t* err, unsigned long long* counters) {
+    // (the queues this kernel appends to were emptied by the last bounce's finalize kernel, so that
+    // the ready phase's kernels can run beside this one)
     const int nxt = cur ^ 1;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        W.counts[kCountResolve] = 0;  // the next bounce's queues start empty
-        W.counts[kCountTrace + nxt] = 0;
-        W.counts[kCountShadow + nxt] = 0;
-        W.counts[kCountLate + nxt] = 0;
-        W.counts[kCountEvent + 3 * nxt + EV_FOG] = 0;
-        W.counts[kCountEvent + 3 * nxt + EV_MISS] = 0;
-        W.counts[kCountEvent + 3 * nxt + EV_SURF] = 0;
-        W.counts[kCountSorted + EV_FOG] = 0;  // this bounce's sorted queues are filled after the trace
-        W.counts[kCountSorted + EV_MISS] = 0;
-        W.counts[kCountSorted + EV_SURF] = 0;
-    }
     __shared__ uint32_t ring[BLOCK / 32][3 * 64];
     WarpStage<3> stage;
     stage.init(ring[threadIdx.x >> 5]);
@@ -438,7 +448,7 @@ __global__ void __launch_bounds__(BLOCK, SR_TRACE_MIN_BLOCKS * 128 / BLOCK)
         },
         [&](uint32_t s, int ev) {
             stage.add(eq, ec, s, ev);
-            if (ev >= 0) W.ev_mark[s] = event_mark(ev, cur);
+            if (ev >= 0) W.ev_mark[s] = event_mark(ev, cur, 1);
         },
         W.defer[cur], wave_deferred(W.counts, W.defer_cap, cur), W.defer[nxt], &W.counts[kCountDefer + nxt],
         W.defer_cap);
@@ -816,27 +826,41 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
     st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(p.radiance.r, p.radiance.g, p.radiance.b, p.spdf),
                                           make_float4(p.energy.r, p.energy.g, p.energy.b, fbits(p.pflags))});
     if (o.live)
-        st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(p.ray.o.x, p.ray.o.y, p.ray.o.z, fbits(p.bounce)),
-                                             make_float4(p.ray.d.x, p.ray.d.y, p.ray.d.z, p.fog_t)});
+        st_ray(W, s, Rec{make_float4(p.ray.o.x, p.ray.o.y, p.ray.o.z, fbits(p.bounce)),
+                         make_float4(p.ray.d.x, p.ray.d.y, p.ray.d.z, p.fog_t)});
     st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(p.rng, p.fog));
     return o;
 }
 
-// One segment of every live path with event EVK, or of all live paths (EVK = -1) with warps
-// sorted by event: the index space is then the fog queue, the miss queue and the surface queue,
-// the first two padded to whole warps, so every warp runs one event's logic.
+// Events of phase `phase` of the bounce (0: the ready events, 1: the others; see SR_SPLIT_PHASES)
+// from the slot-ordered queues, or every event from the arrival-ordered ones (SR_SORT_EVENTS = 0).
+// Returns the event count and sets *first, its first entry in the sorted queue.
+__device__ __forceinline__ uint32_t phase_events(const WaveState& W, int cur, int phase, int ev, uint32_t* first) {
+    *first = 0;
+    if (!SR_SORT_EVENTS) return W.counts[kCountEvent + 3 * cur + ev];
+    if (phase == 0) return W.counts[kCountSorted + ev];
+    *first = W.counts[kCountSorted + ev];
+    return W.counts[kCountSortedLate + ev];
+}
+
+// One segment of every live path of the phase with event EVK, or of all its live paths (EVK = -1)
+// with warps sorted by event: the index space is then the fog queue, the miss queue and the surface
+// queue, the first two padded to whole warps, so every warp runs one event's logic.
 template <bool COUNT, bool GENERAL, int EVK, int ADJ = kAdjNone>
 __global__ void __launch_bounds__(128, ADJ != kAdjNone ? 4 : shade_min_blocks(EVK))
-    k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, uint32_t* err, unsigned long long* counters,
-                 const AdjPass* A) {
+    k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, int phase, uint32_t* err,
+                 unsigned long long* counters, const AdjPass* A) {
     __shared__ uint32_t sh[2][6][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     const int nxt = cur ^ 1;
-    const uint32_t* ecount = W.counts + kCountEvent + 3 * cur;
-    const uint32_t nfog = ecount[EV_FOG], nmiss = ecount[EV_MISS], nsurf = ecount[EV_SURF];
+    uint32_t first[3];
+    const uint32_t nfog = phase_events(W, cur, phase, EV_FOG, &first[EV_FOG]);
+    const uint32_t nmiss = phase_events(W, cur, phase, EV_MISS, &first[EV_MISS]);
+    const uint32_t nsurf = phase_events(W, cur, phase, EV_SURF, &first[EV_SURF]);
+    const uint32_t ecount[3] = {nfog, nmiss, nsurf};
     const uint32_t pfog = (nfog + 31u) & ~31u, pmiss = (nmiss + 31u) & ~31u;
     const uint32_t total = EVK >= 0 ? ecount[EVK] : pfog + pmiss + nsurf;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -855,25 +879,27 @@ __global__ void __launch_bounds__(128, ADJ != kAdjNone ? 4 : shade_min_blocks(EV
         }
         const bool valid = i < cnt;
         const uint32_t* const q = SR_SORT_EVENTS ? W.q_sorted : W.q_event[cur];
-        const uint32_t s = valid ? q[(size_t)ev * W.slots + i] : 0u;
+        const uint32_t s = valid ? q[(size_t)ev * W.slots + first[ev] + i] : 0u;
         SegOut o;
         if (valid) {
             o = shade_segment<COUNT, GENERAL, ADJ>(W, S, P, s, ev, c, A);
         }
         uint32_t* eq = W.q_event[nxt];
-        // finished samples wait for their last shadow ray (traced next bounce) when it has one
+        // finished samples wait for their last shadow ray (traced next bounce) when it has one; so
+        // does the next event of a path with a shadow ray queued
         const bool pred[6] = {valid && o.live && o.next < 0, valid && o.live && o.next == EV_FOG,
                               valid && o.live && o.next == EV_MISS, valid && !o.live && !o.shadow,
                               valid && !o.live && o.shadow, valid && o.shadow};
         uint32_t off[6];
         block_offsets<6>({&W.counts[kCountTrace + nxt], &W.counts[kCountEvent + 3 * nxt + EV_FOG],
-                          &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[kCountResolve],
+                          &W.counts[kCountEvent + 3 * nxt + EV_MISS], &W.counts[count_resolve(cur)],
                           &W.counts[kCountLate + nxt], &W.counts[kCountShadow + nxt]},
                          pred, sh, round++, off);
+        const int wait = o.shadow ? 1 : 0;
         if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_t);
-        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s, W.ev_mark[s] = event_mark(EV_FOG, nxt);
-        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s, W.ev_mark[s] = event_mark(EV_MISS, nxt);
-        if (pred[3]) W.q_resolve[off[3]] = s;
+        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s, W.ev_mark[s] = event_mark(EV_FOG, nxt, wait);
+        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s, W.ev_mark[s] = event_mark(EV_MISS, nxt, wait);
+        if (pred[3]) W.q_resolve[cur][off[3]] = s;
         if (pred[4]) W.q_late[nxt][off[4]] = s;
         if (pred[5]) W.q_shadow[nxt][off[5]] = ray_entry(s, o.sh_o, o.sh_d, 0.f);
     }
@@ -1009,18 +1035,30 @@ template <bool COUNT, bool GENERAL, bool LATE, int ADJ = kAdjNone>
 __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, DevView V, DevParams P, DevAovs out,
                                                        int cur, uint32_t* err, unsigned long long* counters,
                                                        const AdjPass* A) {
+    const int nxt = cur ^ 1;
     if (!LATE && blockIdx.x == 0 && threadIdx.x == 0) {
+        // The queues of this bounce's parity are consumed: empty them for the bounce after next,
+        // and the cursors and finished-sample queue of the next bounce (whose other queues this
+        // bounce has filled).  Done here, at the end of a bounce, so that the next bounce's ready
+        // phase and traversal kernel start together.
         W.counts[kCountTraceFetch] = 0;    // next trace's fetch cursor
         W.counts[kCountDefer + cur] = 0;  // this bounce's traversal resumed these; the next one fills them
+        W.counts[kCountTrace + cur] = 0;
+        W.counts[kCountShadow + cur] = 0;
+        W.counts[kCountLate + cur] = 0;
+        W.counts[kCountEvent + 3 * cur + EV_FOG] = 0;
+        W.counts[kCountEvent + 3 * cur + EV_MISS] = 0;
+        W.counts[kCountEvent + 3 * cur + EV_SURF] = 0;
+        W.counts[count_resolve(nxt)] = 0;
+        for (int e = 0; e < 3; ++e) W.counts[kCountSorted + e] = W.counts[kCountSortedLate + e] = 0;
     }
     __shared__ uint32_t sh[2][3][kBlockWarps + 1];
     uint32_t round = 0;
     Ctr c;
 #pragma unroll
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
-    const int nxt = cur ^ 1;
-    const uint32_t n = LATE ? W.counts[kCountLate + cur] : W.counts[kCountResolve];
-    const uint32_t* q = LATE ? W.q_late[cur] : W.q_resolve;
+    const uint32_t n = LATE ? W.counts[kCountLate + cur] : W.counts[count_resolve(cur)];
+    const uint32_t* q = LATE ? W.q_late[cur] : W.q_resolve[cur];
     const uint32_t stride = gridDim.x * blockDim.x;
     float g_density = 0.0f;  // adjoint replay: this thread's d loss / d fog density
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -1039,8 +1077,8 @@ __global__ void __launch_bounds__(128) k_wave_finalize(WaveState W, DevScene S, 
                           &W.counts[kCountEvent + 3 * nxt + EV_MISS]},
                          pred, sh, round++, off);
         if (pred[0]) W.q_trace[nxt][off[0]] = ray_entry(s, o.nx_o, o.nx_d, o.nx_t);
-        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s, W.ev_mark[s] = event_mark(EV_FOG, nxt);
-        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s, W.ev_mark[s] = event_mark(EV_MISS, nxt);
+        if (pred[1]) eq[(size_t)EV_FOG * W.slots + off[1]] = s, W.ev_mark[s] = event_mark(EV_FOG, nxt, 0);
+        if (pred[2]) eq[(size_t)EV_MISS * W.slots + off[2]] = s, W.ev_mark[s] = event_mark(EV_MISS, nxt, 0);
     }
     flush_counters<COUNT>(c, counters);
     if constexpr (ADJ == kAdjReplay) {  // every thread of the block gets here: one atomic per warp
@@ -1067,6 +1105,7 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
     for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     int group = -1, ev = -1;
+    bool resumed = false;  // a query set aside by the last traversal kernel
     uint32_t s = 0;
     float rt = 0.f;
     V3 ro{0.f, 0.f, 0.f}, rd{0.f, 0.f, 0.f};  // the ray of a segment that needs a traversal
@@ -1104,6 +1143,7 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
         const uint32_t nd = wave_deferred(Wg.counts, Wg.defer_cap, cur);
         if (k < nd) {
             group = g;
+            resumed = true;
             const uint32_t* w = reinterpret_cast<const uint32_t*>(Wg.defer[cur] + (size_t)k * kDeferF4);
             s = w[0];
             rt = __uint_as_float(w[1]);
@@ -1115,8 +1155,10 @@ __global__ void __launch_bounds__(128) k_wave_tail(WaveGroups G, DevScene S, Dev
     }
     if (group >= 0) {
         const WaveState W = G.W[group];
-        // the slot's shadow ray queued for the next bounce, if any: traced first
-        if (ibits(ld_rec(&W.rec[rix(W, s, R_PATH)]).b.w) & PF_NEE) {
+        // the slot's shadow ray queued for the next bounce, if any: traced first (a set-aside
+        // query's shadow ray was traced by the kernel that set it aside: its transmittance has
+        // replaced the ray's origin)
+        if (!resumed && (ibits(ld_rec(&W.rec[rix(W, s, R_PATH)]).b.w) & PF_NEE)) {
             Rec r0 = ld_rec(&W.rec[rix(W, s, R_SH0)]);
             shadow_trace<COUNT, GENERAL>(W, S, s, make_ray(V3{r0.a.x, r0.a.y, r0.a.z}, V3{r0.b.x, r0.b.y, r0.b.z}), c,
                                          err);

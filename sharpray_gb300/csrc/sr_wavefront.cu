@@ -73,12 +73,16 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevScene S, DevV
 }
 
 // The event queues of this bounce in slot order, so that the shade kernels' neighbouring threads
-// work on neighbouring slots: every producer of an event also tags the slot with the event and
-// the parity of the bounce that shades it (event_mark), and k_event_sort scans the slots in order
-// -- four per thread -- appending each slot tagged for this bounce to its event's sorted queue
-// (one atomic per block and event; inside a block's run the order is the slot order) and
-// clearing its tag.  Tags for the next bounce (from a late finalize) are left in place.
-__global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur) {
+// work on neighbouring slots: every producer of an event also tags the slot with the event, the
+// parity of the bounce that shades it and whether it waits for that bounce's traversal kernel
+// (event_mark), and k_event_sort scans the slots in order -- four per thread -- appending each slot
+// tagged for this bounce and phase to its event's sorted queue (one atomic per block and event;
+// inside a block's run the order is the slot order) and clearing its tag.  Phase 0 takes the ready
+// events (running beside the traversal kernel, which meanwhile tags other slots: a tag it has not
+// written yet reads as 0 or as a waiting tag, both left alone); phase 1 takes the rest of the
+// bounce's events and places them after phase 0's.  Tags for the next bounce (from a late finalize)
+// are left in place.
+__global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur, int phase) {
     __shared__ uint32_t warp_n[3][8];
     __shared__ uint32_t base[3];
     const uint32_t li = 4u * (blockIdx.x * blockDim.x + threadIdx.x);  // group-local slot index
@@ -87,8 +91,10 @@ __global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur) {
     uint32_t cnt[3] = {0, 0, 0};
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        uint32_t m = li + j < W.slots ? W.ev_mark[s0 + j] : 0u;
-        const uint32_t e = m - 1u - 3u * (uint32_t)cur;  // event of this bounce, else >= 3
+        const uint32_t m = li + j < W.slots ? W.ev_mark[s0 + j] : 0u;
+        // m = 1 + event + 3 x parity + 6 x wait: the event of this bounce and phase, else >= 3
+        const uint32_t t = phase == 0 ? m - 1u - 3u * (uint32_t)cur : (m > 6u ? m - 7u : m - 1u) - 3u * (uint32_t)cur;
+        const uint32_t e = m == 0u ? 3u : t;
         ev4[j] = e < 3u ? e : 3u;
         if (e < 3u) {
             W.ev_mark[s0 + j] = 0;
@@ -112,7 +118,9 @@ __global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur) {
     if (threadIdx.x < 3) {
         uint32_t t = 0;
         for (int w = 0; w < 8; ++w) t += warp_n[threadIdx.x][w];
-        base[threadIdx.x] = t ? atomicAdd(&W.counts[kCountSorted + threadIdx.x], t) : 0u;
+        const uint32_t first = phase == 0 ? 0u : W.counts[kCountSorted + threadIdx.x];
+        base[threadIdx.x] =
+            first + (t ? atomicAdd(&W.counts[(phase == 0 ? kCountSorted : kCountSortedLate) + threadIdx.x], t) : 0u);
     }
     __syncthreads();
     uint32_t off[3];
@@ -189,8 +197,49 @@ __global__ void __launch_bounds__(256) k_trace_octant_sort(WaveState W, int cur)
     if (valid) st_rec(&W.q_trace[cur][start + base[warp][oct] + rank], e);
 }
 
+// The shade kernels of one phase of a bounce (phase 0: the ready events, fog and miss only; a
+// surface event always comes from the traversal kernel).
 template <bool COUNT, bool GENERAL>
-static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st) {
+static void launch_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st) {
+    if (L.adj_mode != kAdjNone) {
+        wave_adj_shade(L, W, cur, phase, st);
+        return;
+    }
+    if (SR_SPLIT_SHADE) {
+        k_wave_shade<COUNT, GENERAL, EV_FOG><<<phase == 0 ? L.grid_ready[0] : L.grid_shade[0], 128, 0, st>>>(
+            W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
+        k_wave_shade<COUNT, GENERAL, EV_MISS><<<phase == 0 ? L.grid_ready[1] : L.grid_shade[1], 128, 0, st>>>(
+            W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
+        if (phase == 1)
+            k_wave_shade<COUNT, GENERAL, EV_SURF>
+                <<<L.grid_shade[2], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
+    } else {
+        k_wave_shade<COUNT, GENERAL, -1>
+            <<<phase == 0 ? L.grid_ready[0] : L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err,
+                                                                           L.counters, nullptr);
+    }
+}
+
+// One bounce of group W on stream st.  With split phases and a side stream, the ready phase (its
+// sort and shade kernels) runs on `side`, forked from st before the traversal kernel and joined
+// back before the other phase's sort (fork[0], fork[1]); without a side stream it runs first on st.
+template <bool COUNT, bool GENERAL>
+static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st,
+                                 cudaStream_t side, const cudaEvent_t* fork) {
+    if (kSplitPhases) {
+        cudaStream_t sa = side ? side : st;
+        if (side) {
+            cudaError_t e = cudaEventRecord(fork[0], st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork[0], 0);
+            if (e != cudaSuccess) return e;
+        }
+        k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, sa>>>(W, cur, 0);
+        launch_shade<COUNT, GENERAL>(L, W, cur, 0, sa);
+        if (side) {
+            cudaError_t e = cudaEventRecord(fork[1], side);
+            if (e != cudaSuccess) return e;
+        }
+    }
     if (SR_TRACE_OCTANT_SORT) k_trace_octant_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W, cur);
     const bool loop_shadows = GENERAL && L.S.has_transparent;
     if (!COUNT && L.trace_block != 128) {
@@ -207,59 +256,59 @@ static void launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cuda
     else
         k_wave_finalize<COUNT, GENERAL, true><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
                                                                                L.counters, nullptr);
-    if (SR_SORT_EVENTS) k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, st>>>(W, cur);
-    if (L.adj_mode != kAdjNone) {
-        wave_adj_shade(L, W, cur, st);
+    if (kSplitPhases && side) {
+        cudaError_t e = cudaStreamWaitEvent(st, fork[1], 0);
+        if (e != cudaSuccess) return e;
+    }
+    if (SR_SORT_EVENTS) k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, st>>>(W, cur, 1);
+    launch_shade<COUNT, GENERAL>(L, W, cur, 1, st);
+    if (L.adj_mode != kAdjNone)
         wave_adj_finalize(L, W, cur, st, false);
-        return;
-    }
-    if (SR_SPLIT_SHADE) {
-        k_wave_shade<COUNT, GENERAL, EV_FOG>
-            <<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters, nullptr);
-        k_wave_shade<COUNT, GENERAL, EV_MISS>
-            <<<L.grid_shade[1], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters, nullptr);
-        k_wave_shade<COUNT, GENERAL, EV_SURF>
-            <<<L.grid_shade[2], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters, nullptr);
-    } else {
-        k_wave_shade<COUNT, GENERAL, -1><<<L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, L.err, L.counters, nullptr);
-    }
-    k_wave_finalize<COUNT, GENERAL, false><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
-                                                                            L.counters, nullptr);
+    else
+        k_wave_finalize<COUNT, GENERAL, false><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
+                                                                                L.counters, nullptr);
+    return cudaSuccess;
 }
 
-static void launch_group_bounces(const WaveLaunch& L, const WaveState& W, int cur, int n, cudaStream_t st) {
-    for (int i = 0; i < n; ++i, cur ^= 1) {
-        if (L.general) {
-            if (L.counters)
-                launch_bounce<true, true>(L, W, cur, st);
-            else
-                launch_bounce<false, true>(L, W, cur, st);
-        } else {
-            if (L.counters)
-                launch_bounce<true, false>(L, W, cur, st);
-            else
-                launch_bounce<false, false>(L, W, cur, st);
-        }
+static cudaError_t launch_group_bounces(const WaveLaunch& L, const WaveState& W, int cur, int n, cudaStream_t st,
+                                        cudaStream_t side, const cudaEvent_t* fork) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < n && e == cudaSuccess; ++i, cur ^= 1) {
+        if (L.general)
+            e = L.counters ? launch_bounce<true, true>(L, W, cur, st, side, fork)
+                           : launch_bounce<false, true>(L, W, cur, st, side, fork);
+        else
+            e = L.counters ? launch_bounce<true, false>(L, W, cur, st, side, fork)
+                           : launch_bounce<false, false>(L, W, cur, st, side, fork);
     }
+    return e;
 }
 
-// n bounces of every group starting at parity cur: group 0 on st, group g on side[g - 1], forked
-// from st by fork[0] and joined back by fork[g].
+// n bounces of every group starting at parity cur.  One group: its bounces on st, the ready phases
+// on side[0] (fork[0], fork[1]).  Several groups: group 0 on st, group g on side[g - 1], forked from
+// st by fork[0] and joined back by fork[g]; each group's phases then run one after the other.
 static cudaError_t launch_bounces(const WaveLaunch& L, int cur, int n, cudaStream_t st, const cudaStream_t* side,
                                   const cudaEvent_t* fork) {
     cudaError_t e = cudaSuccess;
-    if (L.groups > 1) {
-        e = cudaEventRecord(fork[0], st);
-        for (int g = 1; g < L.groups && e == cudaSuccess; ++g) e = cudaStreamWaitEvent(side[g - 1], fork[0], 0);
-        if (e != cudaSuccess) return e;
+    if (L.groups == 1) {
+        e = launch_group_bounces(L, L.W[0], cur, n, st, side ? side[0] : nullptr, fork);
+        return e != cudaSuccess ? e : cudaGetLastError();
     }
-    for (int g = 0; g < L.groups; ++g) launch_group_bounces(L, L.W[g], cur, n, g == 0 ? st : side[g - 1]);
+    e = cudaEventRecord(fork[0], st);
+    for (int g = 1; g < L.groups && e == cudaSuccess; ++g) e = cudaStreamWaitEvent(side[g - 1], fork[0], 0);
+    if (e != cudaSuccess) return e;
+    for (int g = 0; g < L.groups && e == cudaSuccess; ++g)
+        e = launch_group_bounces(L, L.W[g], cur, n, g == 0 ? st : side[g - 1], nullptr, fork);
     for (int g = 1; g < L.groups && e == cudaSuccess; ++g) {
         e = cudaEventRecord(fork[g], side[g - 1]);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, fork[g], 0);
     }
     return e != cudaSuccess ? e : cudaGetLastError();
 }
+
+#ifndef SR_READY_BLOCKS
+#define SR_READY_BLOCKS 0
+#endif
 
 template <bool GENERAL>
 static void occupancy(int* b) {
@@ -309,6 +358,10 @@ void wave_grid_sizes(WaveLaunch& L, int sms, const WaveTune* tune) {
     L.grid_shade[0] = b[3];
     L.grid_shade[1] = b[4];
     L.grid_shade[2] = b[5];
+    // the ready phase's fog kernel shares the SMs with the traversal kernel: SR_READY_BLOCKS blocks
+    // per SM (0: as many as fit alone)
+    L.grid_ready[0] = SR_READY_BLOCKS > 0 && sms * SR_READY_BLOCKS < b[3] ? sms * SR_READY_BLOCKS : b[3];
+    L.grid_ready[1] = b[4];
 }
 
 cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st, uint32_t seed) {
