@@ -127,26 +127,12 @@ __device__ __forceinline__ float fog_scatter_t(const DevScene& S, const Ray& ray
     return t;
 }
 
-// The ray sector of a path record shares a 64-byte DRAM burst with the hit sector, which is dead
-// from the shading of a segment until the next traversal writes it.  SR_RAY_HIT_PAIR = 1 stores a
-// zero hit sector with every ray store, so that the burst is written whole instead of half.
-#ifndef SR_RAY_HIT_PAIR
-#define SR_RAY_HIT_PAIR 0
-#endif
-__device__ __forceinline__ void st_ray(const WaveState& W, uint32_t s, const Rec& ray) {
-    st_rec(&W.rec[rix(W, s, R_RAY)], ray);
-    if (SR_RAY_HIT_PAIR) {
-        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-        st_rec(&W.rec[rix(W, s, R_HIT)], Rec{z, z});
-    }
-}
-
 // Start of a sample: the camera ray and a reset path (scene.cs:633-638).
 // `flags`: the path flags a sample starts with (an adjoint pass that keeps every sample's vertices
 // puts the sample index there).
 __device__ __forceinline__ void begin_sample(const WaveState& W, uint32_t s, const Ray& ray, const Rng& rng,
                                              float sdist = 0.f, uint32_t flags = 0u) {
-    st_ray(W, s, Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, sdist)});
+    st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(ray.o.x, ray.o.y, ray.o.z, fbits(0u)), make_float4(ray.d.x, ray.d.y, ray.d.z, sdist)});
     st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(0.f, 0.f, 0.f, 0.f), make_float4(1.f, 1.f, 1.f, fbits(flags))});
     st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(rng, black()));
 }
@@ -826,8 +812,8 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
     st_rec(&W.rec[rix(W, s, R_PATH)], Rec{make_float4(p.radiance.r, p.radiance.g, p.radiance.b, p.spdf),
                                           make_float4(p.energy.r, p.energy.g, p.energy.b, fbits(p.pflags))});
     if (o.live)
-        st_ray(W, s, Rec{make_float4(p.ray.o.x, p.ray.o.y, p.ray.o.z, fbits(p.bounce)),
-                         make_float4(p.ray.d.x, p.ray.d.y, p.ray.d.z, p.fog_t)});
+        st_rec(&W.rec[rix(W, s, R_RAY)], Rec{make_float4(p.ray.o.x, p.ray.o.y, p.ray.o.z, fbits(p.bounce)),
+                                             make_float4(p.ray.d.x, p.ray.d.y, p.ray.d.z, p.fog_t)});
     st_rec(&W.rec[rix(W, s, R_RNG)], rng_rec(p.rng, p.fog));
     return o;
 }
