@@ -268,7 +268,8 @@ SR_API int sr_scene_bvh_export(SrScene* scene, float* node_bounds, int32_t* node
  * object's mesh (-1 for analytic shapes), world distance, barycentric u, v.  Replaces the
  * traversal of Scene.Trace (scene.cs:602-625 -> Bvh.Intersect bvh.cs:165-216 ->
  * Mesh.Intersect mesh.cs:51-62 -> TriangleLean.Intersect math.cs:1407-1435); used for the
- * bit-exact hit parity test. */
+ * bit-exact hit parity test.  The traversal is the wavefront renderer's persistent loop, or, in
+ * the megakernel render mode (sr_scene_set_render_mode), the megakernel's per-ray traversal. */
 SR_API int sr_scene_trace(SrScene* scene, const float* rays, uint32_t count, int32_t* out_object,
                           int32_t* out_triangle, float* out_dist, float* out_uv);
 

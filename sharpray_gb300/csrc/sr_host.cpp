@@ -793,8 +793,10 @@ SR_API int sr_scene_trace(SrScene* s, const float* rays, uint32_t count, int32_t
     if (int rc = need_device(s)) return rc;
     SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
     cudaStream_t st = s->ctx->stream;
+    // rays, then the four outputs, then (persistent form) ray-queue entries on 256 bytes and a cursor
     size_t in_b = (size_t)count * 6 * 4, out_b = (size_t)count * 5 * 4;
-    SR_CUDA(s->rays_io.reserve(in_b + out_b + 64), "alloc ray buffers");
+    const size_t q_off = (in_b + out_b + 255) & ~(size_t)255, q_b = (size_t)count * sizeof(Rec);
+    SR_CUDA(s->rays_io.reserve(q_off + q_b + 256), "alloc ray buffers");
     char* base = s->rays_io.as<char>();
     float* d_rays = (float*)base;
     int32_t* d_obj = (int32_t*)(base + in_b);
@@ -802,7 +804,19 @@ SR_API int sr_scene_trace(SrScene* s, const float* rays, uint32_t count, int32_t
     float* d_dist = (float*)(d_tri + count);
     float* d_uv = d_dist + count;
     SR_CUDA(cudaMemcpyAsync(d_rays, rays, in_b, cudaMemcpyHostToDevice, st), "copy rays");
-    SR_CUDA(launch_trace(launch_scene(s), d_rays, count, d_obj, d_tri, d_dist, d_uv, s->err.as<uint32_t>(), st), "trace launch");
+    if (s->render_mode == SR_RENDER_MEGAKERNEL) {
+        // one thread per ray through the megakernel's traversal
+        SR_CUDA(launch_trace(launch_scene(s), d_rays, count, d_obj, d_tri, d_dist, d_uv, s->err.as<uint32_t>(), st),
+                "trace launch");
+    } else {
+        // the wavefront renderer's persistent traversal loop
+        if (!s->sms) SR_CUDA(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->ctx->device), "device query");
+        const DevScene S = launch_scene(s);
+        SR_CUDA(launch_trace_persistent(S, S.general != 0, d_rays, count, (Rec*)(base + q_off),
+                                        (uint32_t*)(base + q_off + q_b), d_obj, d_tri, d_dist, d_uv,
+                                        s->err.as<uint32_t>(), s->sms, st),
+                "trace launch");
+    }
     SR_CUDA(cudaMemcpyAsync(out_object, d_obj, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
     SR_CUDA(cudaMemcpyAsync(out_triangle, d_tri, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");
     SR_CUDA(cudaMemcpyAsync(out_dist, d_dist, count * 4, cudaMemcpyDeviceToHost, st), "copy hits");

@@ -136,6 +136,58 @@ __global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur, int ph
     }
 }
 
+// Closest hits of world rays through the renderer's own persistent traversal loop (the ray
+// query of sr_scene_trace outside the megakernel render mode): the rays become ray-queue entries,
+// then one persistent launch answers them, each lane writing its query's result.
+__global__ void k_pack_rays(const float* rays, uint32_t n, Rec* q) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* r = rays + (size_t)i * 6;
+    q[i] = ray_entry(i, V3{r[0], r[1], r[2]}, V3{r[3], r[4], r[5]}, 0.f);
+}
+
+template <bool GENERAL>
+__global__ void __launch_bounds__(128, SR_TRACE_MIN_BLOCKS)
+    k_trace_rays_persistent(DevScene S, const Rec* q, uint32_t n, uint32_t* fetch, int32_t* obj, int32_t* tri,
+                            float* dist, float* uv, uint32_t* err) {
+    Ctr c;
+#pragma unroll
+    for (int i = 0; i < SR_COUNTER_COUNT; ++i) c.v[i] = 0;
+    persistent_queries<false, GENERAL>(
+        S, q, n, nullptr, 0u, fetch, c, err, [&](bool) {},
+        [&](uint32_t i, uint32_t, bool, const Hit& h, const Ray&) {
+            if (h.obj < 0) {
+                obj[i] = -1, tri[i] = -1, dist[i] = __int_as_float(0x7f800000), uv[2 * i] = 0.f, uv[2 * i + 1] = 0.f;
+            } else {
+                obj[i] = S.objects[h.obj].index;
+                tri[i] = h.tri >= 0 ? __float_as_int(__ldg(S.tris + 3 * h.tri).w) : -1;
+                dist[i] = h.dist, uv[2 * i] = h.u, uv[2 * i + 1] = h.v;
+            }
+            return -1;
+        },
+        [&](uint32_t, int) {});
+}
+
+cudaError_t launch_trace_persistent(const DevScene& S, bool general, const float* rays, uint32_t n, Rec* entries,
+                                    uint32_t* fetch, int32_t* obj, int32_t* tri, float* dist, float* uv,
+                                    uint32_t* err, int sms, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    k_pack_rays<<<(n + 127) / 128, 128, 0, st>>>(rays, n, entries);
+    int per_sm = 0;
+    if (general) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_rays_persistent<true>, 128, 0);
+        k_trace_rays_persistent<true><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(S, entries, n, fetch, obj, tri,
+                                                                                    dist, uv, err);
+    } else {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_rays_persistent<false>, 128, 0);
+        k_trace_rays_persistent<false><<<sms * (per_sm > 0 ? per_sm : 1), 128, 0, st>>>(S, entries, n, fetch, obj,
+                                                                                     tri, dist, uv, err);
+    }
+    return cudaGetLastError();
+}
+
 // Condition of the device-side bounce loop: continue while more than `tail` paths of all groups
 // are live (the rest go to the tail kernel) and the bounce cap (a runaway guard of twice
 // (max_samples + 1) * (bounces + 2) per pixel) is not reached.  `counts` holds the groups' counters one after another.

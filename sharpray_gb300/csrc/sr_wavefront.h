@@ -242,6 +242,11 @@ void wave_adj_finalize(const WaveLaunch& L, const WaveState& W, int cur, cudaStr
 void wave_adj_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st);
 cudaError_t wave_adj_tail(const WaveLaunch& L, int cur, cudaStream_t st);
 void wave_adj_grid_sizes(WaveLaunch& L, int sms);
+// Closest hits of n world rays (6 floats each, device) through the persistent traversal loop of the
+// wavefront renderer; `entries` (n ray-queue records) and `fetch` (one word) are scratch.
+cudaError_t launch_trace_persistent(const DevScene& S, bool general, const float* rays, uint32_t n, Rec* entries,
+                                    uint32_t* fetch, int32_t* obj, int32_t* tri, float* dist, float* uv,
+                                    uint32_t* err, int sms, cudaStream_t st);
 // The traversal kernel at 64 or 256 threads per block (sr_wave_trace.cu) and its resident blocks per SM.
 void wave_trace_block(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st, bool loop_shadows);
 int wave_trace_occupancy(bool general, int block);

@@ -77,11 +77,19 @@ def built(gpu_ctx, oracle_mod):
     return get
 
 
+@pytest.mark.parametrize("mode", [0, 1], ids=["persistent_loop", "per_ray"])
 @pytest.mark.parametrize("name", ["c1", "features", "procedural", "c2_reduced"])
-def test_closest_hit_bit_exact(built, name):
+def test_closest_hit_bit_exact(built, name, mode):
+    """Ray queries through the wavefront renderer's persistent traversal loop (render mode auto)
+    and through the megakernel's per-ray traversal (render mode 1)."""
     d, g, o = built(name)
     rays = np.concatenate([seeded_rays(20000, seed=11), camera_rays(d, 20000, seed=12)])
-    got, want = g.trace(rays), o.trace(rays)
+    g.set_render_mode(mode)
+    try:
+        got = g.trace(rays)
+    finally:
+        g.set_render_mode(0)
+    want = o.trace(rays)
     assert (want["object"] >= 0).sum() > 1000, "ray set should hit the scene"
     for k in ("object", "triangle"):
         assert np.array_equal(got[k], want[k]), f"{k}: {(got[k] != want[k]).sum()} mismatches"
