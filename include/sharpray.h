@@ -380,13 +380,19 @@ typedef struct SrTuning {
     uint32_t max_bounce_iterations; /* wavefront bounce-loop cap (0 = (max_samples + 1) * (bounces + 2) * 2 + 8) */
     uint32_t max_traversal_steps;   /* per-traversal action cap (0 = 2^24) */
     uint32_t trace_block_threads;   /* traversal kernel block size: 64, 128 or 256 (0 = 128) */
+    uint32_t max_slots;             /* path slots in flight, the wavefront queues' capacity, rounded up to
+                                     * 32 (0 = one per pixel).  With fewer slots than pixels a slot takes
+                                     * the next unclaimed pixel when its pixel is done: less path-state
+                                     * memory, fewer paths per bounce; results are unchanged.  Not applied
+                                     * to sr_render_checkpointed (its vertices are indexed by slot). */
 } SrTuning;
 SR_API int sr_scene_set_tuning(SrScene* scene, const SrTuning* tuning); /* NULL = defaults */
 SR_API int sr_scene_get_tuning(SrScene* scene, SrTuning* tuning);
 /* Autotuner: renders `params` at trial_spp samples per pixel under candidate launch geometries, one
  * dimension after another from the defaults -- traversal block size (128, 64, 256), traversal
  * blocks per SM (all that fit, one or two fewer), fog-shade blocks per SM (all, two fewer), tail
- * hand-over (slots / 16, 8, 32) -- keeping the fastest of each, and leaves the result on the scene
+ * hand-over (slots / 16, 8, 32), slot capacity (every pixel, a half, a quarter) -- keeping the
+ * fastest of each, and leaves the result on the scene
  * (ms: its trial time; default_ms: the defaults').  The BVH node width is not a dimension: the
  * traversal walks the reference's binary tree, whose child order the bit-exact hits rest on. */
 SR_API int sr_scene_autotune(SrScene* scene, const SrView* view, const SrRenderParams* params, uint32_t trial_spp,

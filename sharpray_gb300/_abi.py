@@ -115,7 +115,7 @@ class SrTuning(C.Structure):
     _fields_ = [("trace_blocks_per_sm", C.c_int32), ("fog_shade_blocks_per_sm", C.c_int32),
                 ("surface_shade_blocks_per_sm", C.c_int32), ("tail_divisor", C.c_uint32), ("ms", C.c_float),
                 ("default_ms", C.c_float), ("max_bounce_iterations", C.c_uint32), ("max_traversal_steps", C.c_uint32),
-                ("trace_block_threads", C.c_uint32)]
+                ("trace_block_threads", C.c_uint32), ("max_slots", C.c_uint32)]
 
 
 class SrAovImageParams(C.Structure):

@@ -154,8 +154,8 @@ struct SrScene {
     uint32_t wave_slots = 0;
     WaveState ws[kWaveGroups]{};
     cudaStream_t capture_stream = nullptr;
-    cudaStream_t side_streams[kWaveGroups > 1 ? kWaveGroups - 1 : 1] = {};  // groups 1.. of a bounce
-    cudaEvent_t fork_events[kWaveGroups + 1] = {};                          // fork, then joins
+    cudaStream_t side_streams[kSideStreams] = {};  // a bounce's parallel branches (or groups 1..)
+    cudaEvent_t fork_events[kForkEvents] = {};      // forks and joins
     cudaGraphExec_t graph_exec = nullptr;
     WaveLaunch graph_launch{};  // launch parameters baked into graph_exec
     uint32_t* counts_host = nullptr;  // pinned
@@ -872,10 +872,11 @@ static uint32_t defer_capacity(size_t slots) {
     return (uint32_t)(c < 256 ? 256 : (c > 16384 ? 16384 : c));
 }
 
-// Allocates the wavefront path state for a tiles_x x tiles_y grid of 8x4 slot tiles: the records
-// of every slot, then each group's queues, then every group's counters (one block, carved).
-static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
-    const uint32_t tiles = tiles_x * tiles_y;
+// Allocates the wavefront path state for `tiles` tiles of 32 slots over an image of pixel_tiles
+// 8x4 pixel tiles (tiles_x per row): the records of every slot, then each group's queues, then
+// every group's counters (one block, carved).  Fewer slot tiles than pixel tiles: slots claim the
+// pixels left over as theirs finish.
+static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t pixel_tiles, uint32_t tiles) {
     const size_t n = (size_t)tiles * 32;
     uint32_t group_slots[kWaveGroups];
     for (int g = 0; g < kWaveGroups; ++g) group_slots[g] = (uint32_t)(tiles > (uint32_t)g ? (tiles - g + kWaveGroups - 1) / kWaveGroups : 0) * 32;
@@ -905,6 +906,8 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         const size_t m = group_slots[g];
         w.slots = group_slots[g];
         w.tiles_x = tiles_x;
+        w.pixel_tiles = pixel_tiles;
+        w.dynamic = tiles < pixel_tiles ? 1u : 0u;
         w.group = (uint32_t)g;
         w.groups = kWaveGroups;
         w.rec = recs;
@@ -927,16 +930,26 @@ static int wave_reserve(SrScene* s, uint32_t tiles_x, uint32_t tiles_y) {
         w.rec_stride = (uint32_t)n;
         w.ev_mark = ev_mark;
     }
-    for (int g = 0; g < kWaveGroups; ++g) s->ws[g].counts = (uint32_t*)p + g * kWaveCounters;
+    for (int g = 0; g < kWaveGroups; ++g) {
+        s->ws[g].counts = (uint32_t*)p + g * kWaveCounters;
+        s->ws[g].pixel_cursor = (uint32_t*)p + kCountPixel;  // group 0's
+    }
     return SR_OK;
 }
 
 // The wavefront state of scene s reserved and initialised on `st` (first camera rays) for one
 // render, and the launch description of its bounce kernels in L.
+// `slot_cap`: whether the scene's slot capacity (WaveTune::max_slots) applies (not for renders that
+// keep every sample's vertices, which are indexed by slot).
 static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, const DevAovs& out,
-                        unsigned long long* ctr, cudaStream_t st, WaveLaunch& L) {
-    uint32_t tiles_x = (dp.width + 7) / 8, tiles_y = (dp.height + 3) / 4;
-    int rc = wave_reserve(s, tiles_x, tiles_y);
+                        unsigned long long* ctr, cudaStream_t st, WaveLaunch& L, bool slot_cap = true) {
+    const uint32_t tiles_x = (dp.width + 7) / 8, tiles_y = (dp.height + 3) / 4, pixel_tiles = tiles_x * tiles_y;
+    uint32_t tiles = pixel_tiles;
+    if (slot_cap && s->tune.max_slots) {
+        const uint32_t cap = (s->tune.max_slots + 31) / 32;
+        if (cap < tiles) tiles = cap;
+    }
+    int rc = wave_reserve(s, tiles_x, pixel_tiles, tiles);
     if (rc) return rc;
     // side streams: the other groups' bounces, or (one group) the ready phase of each bounce
     for (cudaStream_t& side : s->side_streams)
@@ -958,8 +971,10 @@ static int wave_prepare(SrScene* s, const DevView& dv, const DevParams& dp, cons
     L.general = s->dev.general;
     wave_grid_sizes(L, s->sms, &s->tune);
     // a runaway guard, not a budget: a pixel's samples run one after another, each taking up to
-    // bounces + 2 iterations (the last segment's shadow ray is traced one bounce later)
-    uint64_t cap = ((uint64_t)dp.max_samples + 1) * ((uint64_t)dp.bounces + 2) * 2 + 8;
+    // bounces + 2 iterations (the last segment's shadow ray is traced one bounce later), and a
+    // slot runs the pixels it claims one after another
+    const uint64_t rounds = (pixel_tiles + tiles - 1) / tiles;
+    uint64_t cap = (((uint64_t)dp.max_samples + 1) * ((uint64_t)dp.bounces + 2) * 2 + 8) * rounds;
     if (s->tune.max_iters && s->tune.max_iters < cap) cap = s->tune.max_iters;
     L.max_iters = (uint32_t)(cap > 0x7fffffffull ? 0x7fffffffull : cap);
     uint32_t all_slots = 0;
@@ -978,7 +993,7 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
                             unsigned long long* ctr, cudaStream_t st, bool graph, int adj_mode = kAdjNone,
                             AdjPass* adj = nullptr, WaveLaunch* launch_out = nullptr) {
     WaveLaunch L;
-    if (int rc = wave_prepare(s, dv, dp, out, ctr, st, L)) return rc;
+    if (int rc = wave_prepare(s, dv, dp, out, ctr, st, L, adj_mode != kAdjRecord)) return rc;
     if (adj_mode != kAdjNone) {
         // vertex records: one sample per slot (replay) or every sample (record, kept apart so that
         // a replay pass does not overwrite a checkpoint)
@@ -1186,7 +1201,7 @@ SR_API int sr_scene_set_tuning(SrScene* s, const SrTuning* t) {
         return fail(SR_ERR_INVALID_ARG, "trace_block_threads must be 64, 128 or 256 (or 0)");
     s->tune = t ? WaveTune{t->trace_blocks_per_sm, t->fog_shade_blocks_per_sm, t->surface_shade_blocks_per_sm,
                            t->tail_divisor, t->max_bounce_iterations, t->max_traversal_steps,
-                           (int)t->trace_block_threads}
+                           (int)t->trace_block_threads, t->max_slots}
                 : WaveTune{};
     return SR_OK;
 }
@@ -1201,13 +1216,14 @@ SR_API int sr_scene_get_tuning(SrScene* s, SrTuning* t) {
     t->max_bounce_iterations = s->tune.max_iters;
     t->max_traversal_steps = s->tune.max_actions;
     t->trace_block_threads = (uint32_t)s->tune.trace_block;
+    t->max_slots = s->tune.max_slots;
     return SR_OK;
 }
 
 // Times `params` at trial_spp samples per pixel under candidate launch geometries, one dimension at a
 // time from the defaults (coordinate search): traversal block size, traversal blocks per SM,
-// fog-shade blocks per SM, tail hand-over; keeps the fastest of each dimension and leaves the
-// result on the scene.
+// fog-shade blocks per SM, tail hand-over, slot capacity; keeps the fastest of each dimension and
+// leaves the result on the scene.
 SR_API int sr_scene_autotune(SrScene* s, const SrView* view, const SrRenderParams* params, uint32_t trial_spp,
                              SrTuning* out) {
     if (!s || !view || !params) return fail(SR_ERR_INVALID_ARG, "NULL argument");
@@ -1250,7 +1266,7 @@ SR_API int sr_scene_autotune(SrScene* s, const SrView* view, const SrRenderParam
         ms *= 0.5f;
         return rc == SR_OK;
     };
-    WaveTune best{0, 0, 0, 16, saved.max_iters, saved.max_actions, 128};
+    WaveTune best{0, 0, 0, 16, saved.max_iters, saved.max_actions, 128, 0};
     float best_ms = 0.0f, default_ms = 0.0f;
     if (trial(best, default_ms)) best_ms = default_ms;
     auto consider = [&](WaveTune t) {
@@ -1277,6 +1293,11 @@ SR_API int sr_scene_autotune(SrScene* s, const SrView* view, const SrRenderParam
         WaveTune t = best;
         t.tail_div = div;
         consider(t);
+    }
+    for (uint32_t part : {2u, 4u}) {  // slot capacity: half or a quarter of the pixels in flight
+        WaveTune t = best;
+        t.max_slots = (uint32_t)((n + part - 1) / part);
+        if (t.max_slots >= 32) consider(t);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

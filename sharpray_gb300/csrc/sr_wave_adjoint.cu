@@ -48,23 +48,25 @@ void wave_adj_finalize(const WaveLaunch& L, const WaveState& W, int cur, cudaStr
 // The shade kernels of one phase of a bounce (phase 0: the ready events, which are never surface
 // events).
 template <bool GENERAL, int ADJ>
-static void adj_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st) {
-    k_wave_shade<false, GENERAL, EV_FOG, ADJ>
-        <<<L.grid_adj_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, nullptr, L.adj);
-    k_wave_shade<false, GENERAL, EV_MISS, ADJ>
-        <<<L.grid_adj_shade[1], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, nullptr, L.adj);
-    if (phase == 1)
+static void adj_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st, int events) {
+    if (events & 1)
+        k_wave_shade<false, GENERAL, EV_FOG, ADJ>
+            <<<L.grid_adj_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, nullptr, L.adj);
+    if (events & 2)
+        k_wave_shade<false, GENERAL, EV_MISS, ADJ>
+            <<<L.grid_adj_shade[1], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, nullptr, L.adj);
+    if (phase == 1 && (events & 4))
         k_wave_shade<false, GENERAL, EV_SURF, ADJ>
             <<<L.grid_adj_shade[2], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, nullptr, L.adj);
 }
 
-void wave_adj_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st) {
+void wave_adj_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st, int events) {
     if (L.general)
-        L.adj_mode == kAdjReplay ? adj_shade<true, kAdjReplay>(L, W, cur, phase, st)
-                                 : adj_shade<true, kAdjRecord>(L, W, cur, phase, st);
+        L.adj_mode == kAdjReplay ? adj_shade<true, kAdjReplay>(L, W, cur, phase, st, events)
+                                 : adj_shade<true, kAdjRecord>(L, W, cur, phase, st, events);
     else
-        L.adj_mode == kAdjReplay ? adj_shade<false, kAdjReplay>(L, W, cur, phase, st)
-                                 : adj_shade<false, kAdjRecord>(L, W, cur, phase, st);
+        L.adj_mode == kAdjReplay ? adj_shade<false, kAdjReplay>(L, W, cur, phase, st, events)
+                                 : adj_shade<false, kAdjRecord>(L, W, cur, phase, st, events);
 }
 
 cudaError_t wave_adj_tail(const WaveLaunch& L, int cur, cudaStream_t st) {

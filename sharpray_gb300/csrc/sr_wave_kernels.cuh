@@ -50,11 +50,28 @@ __device__ __forceinline__ void st4(float4* p, float4 v) { *p = v; }
 __device__ __forceinline__ uint32_t ibits(float f) { return (uint32_t)__float_as_int(f); }
 __device__ __forceinline__ float fbits(uint32_t u) { return __int_as_float((int)u); }
 
-__device__ __forceinline__ void slot_pixel(const WaveState& W, uint32_t slot, uint32_t& x, uint32_t& y) {
-    // slots are laid out in 8x4 pixel tiles so that a warp's primary rays are neighbours
-    uint32_t tile = slot >> 5, lane = slot & 31u;
+// Pixel of tile-order index p: pixels are numbered in 8x4 tiles, so that the 32 slots of a warp
+// start on neighbouring pixels (slot s starts on pixel s).
+__device__ __forceinline__ void pixel_xy(const WaveState& W, uint32_t p, uint32_t& x, uint32_t& y) {
+    uint32_t tile = p >> 5, lane = p & 31u;
     x = (tile % W.tiles_x) * 8u + (lane & 7u);
     y = (tile / W.tiles_x) * 4u + (lane >> 3);
+}
+// The first pixel of a slot (every slot's pixel when there is one slot per pixel).
+__device__ __forceinline__ void slot_pixel(const WaveState& W, uint32_t slot, uint32_t& x, uint32_t& y) {
+    pixel_xy(W, slot, x, y);
+}
+// The next unclaimed pixel inside the image for a slot of a render with fewer slots than pixels
+// (~0u: none left).
+__device__ __forceinline__ uint32_t claim_pixel(const WaveState& W, const DevParams& P) {
+    const uint32_t end = W.pixel_tiles * 32u;
+    for (;;) {
+        const uint32_t p = atomicAdd(W.pixel_cursor, 1u);
+        if (p >= end) return ~0u;
+        uint32_t x, y;
+        pixel_xy(W, p, x, y);
+        if (x < P.width && y < P.height) return p;
+    }
 }
 
 // Appends of one grid-stride round to NQ queues (value to queue i where pred[i] holds), aggregated
@@ -298,7 +315,7 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
     LocalStack stack{entries};
 #endif
     SceneQuery<false, GENERAL, true> sq;
-    static_assert(2 + SceneQuery<false, GENERAL, true>::kQueryWords <= 4 * kDeferHeadF4, "defer record header");
+    static_assert(2 + decltype(sq)::kQueryWords <= 4 * kDeferHeadF4, "defer record header");
     const uint32_t n = nd + n0 + n1;  // deferred queries first, then the two queues
     bool busy = false, pending = false, exhausted = false;
     uint32_t slot = 0, tag = 0;
@@ -940,12 +957,13 @@ __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevS
             ncount++;
             a4.x += pn.w;
             dcount++;
-            if (ibits(a5.z) == 0u) a5 = make_float4(pm.b.x, pm.b.y, fbits(1u), 0.f);
+            if (ibits(a5.z) == 0u) a5 = make_float4(pm.b.x, pm.b.y, fbits(1u), a5.w);
         }
         bool done = false;
         uint32_t count = 0;
         uint32_t x, y;
-        slot_pixel(W, s, x, y);
+        const uint32_t pixel = W.dynamic ? ibits(a5.w) : s;
+        pixel_xy(W, pixel, x, y);
         if constexpr (ADJ == kAdjReplay) {
             // the replayed render takes the samples the replayed one took (renderer.cs:215's
             // off-by-one: a pixel whose loop ran out counts max_samples + 1), and this sample's
@@ -995,8 +1013,24 @@ __device__ __forceinline__ SegOut finalize_sample(const WaveState& W, const DevS
             out.samples[i] = count;
             out.variance[i] = var;
             count_pixel_done(W.counts + kCountDone);
-        } else {
-            Rng rng = rng_of(gr);
+        }
+        // the pixel's next sample, or (fewer slots than pixels) the first sample of the next
+        // unclaimed pixel, with that pixel's own random-number stream and fresh statistics
+        bool start = !done;
+        Rng rng = rng_of(gr);
+        if (done && W.dynamic) {
+            const uint32_t q = claim_pixel(W, P);
+            if (q != ~0u) {
+                pixel_xy(W, q, x, y);
+                const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+                a0 = a1 = a2 = a3 = a4 = z;
+                a5 = make_float4(0.f, 0.f, 0.f, fbits(q));
+                ncount = dcount = si = 0;
+                rng = rng_seed(x, y, W.pixel_cursor[kCountSeed - kCountPixel]);
+                start = true;
+            }
+        }
+        if (start) {
             Ray ray = camera_ray(V, P, x, y, rng);
             const float ft = fog_scatter_t(S, ray, rng);
             o.next = next_segment<COUNT>(S, ray, ft, c);

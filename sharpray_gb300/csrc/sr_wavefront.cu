@@ -45,15 +45,29 @@
 
 namespace sr {
 
+// The pixel cursor of a render with fewer slots than pixels -- the pixels after the slots' own --
+// and the render's random-number stream, which the finalize kernels seed claimed pixels from.
+__global__ void k_wave_cursor(uint32_t* cursor, uint32_t first, uint32_t seed) {
+    cursor[0] = first;
+    cursor[kCountSeed - kCountPixel] = seed;
+}
+
 __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevScene S, DevView V, DevParams P) {
     __shared__ uint32_t sh[2][1][kBlockWarps + 1];
     const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;  // index among this group's slots
     const uint32_t s = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);
     bool valid = false;
     if (li < W.slots) {
-        uint32_t x, y;
-        slot_pixel(W, s, x, y);
+        // slot s starts on pixel s (or, with fewer slots than pixels, on the next unclaimed pixel
+        // when pixel s lies outside the image)
+        uint32_t x, y, p = s;
+        pixel_xy(W, p, x, y);
         valid = x < P.width && y < P.height;
+        if (!valid && W.dynamic) {
+            p = claim_pixel(W, P);
+            valid = p != ~0u;
+            if (valid) pixel_xy(W, p, x, y);
+        }
         if (valid) {
             Rng rng = rng_seed(x, y, P.seed);
             Ray ray = camera_ray(V, P, x, y, rng);
@@ -61,7 +75,8 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevScene S, DevV
             float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
             st_rec(&W.pix[pix(W, s, X_ACC)], Rec{z, z});
             st_rec(&W.pix[pix(W, s, X_ACC + 1)], Rec{z, z});
-            st_rec(&W.pix[pix(W, s, X_ACC + 2)], Rec{z, z});  // counts and sample index start at 0 (int bits)
+            // counts and sample index start at 0 (int bits); the pixel's tile-order index in the last word
+            st_rec(&W.pix[pix(W, s, X_ACC + 2)], Rec{z, make_float4(0.f, 0.f, 0.f, fbits(p))});
         }
     }
     uint32_t off[1];
@@ -250,47 +265,56 @@ __global__ void __launch_bounds__(256) k_trace_octant_sort(WaveState W, int cur)
 }
 
 // The shade kernels of one phase of a bounce (phase 0: the ready events, fog and miss only; a
-// surface event always comes from the traversal kernel).
+// surface event always comes from the traversal kernel); `events`: bit 0 fog, bit 1 miss, bit 2
+// surface.
 template <bool COUNT, bool GENERAL>
-static void launch_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st) {
+static void launch_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st, int events = 7) {
     if (L.adj_mode != kAdjNone) {
-        wave_adj_shade(L, W, cur, phase, st);
+        wave_adj_shade(L, W, cur, phase, st, events);
         return;
     }
     if (SR_SPLIT_SHADE) {
-        k_wave_shade<COUNT, GENERAL, EV_FOG><<<phase == 0 ? L.grid_ready[0] : L.grid_shade[0], 128, 0, st>>>(
-            W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
-        k_wave_shade<COUNT, GENERAL, EV_MISS><<<phase == 0 ? L.grid_ready[1] : L.grid_shade[1], 128, 0, st>>>(
-            W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
-        if (phase == 1)
+        if (events & 1)
+            k_wave_shade<COUNT, GENERAL, EV_FOG><<<phase == 0 ? L.grid_ready[0] : L.grid_shade[0], 128, 0, st>>>(
+                W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
+        if (events & 2)
+            k_wave_shade<COUNT, GENERAL, EV_MISS><<<phase == 0 ? L.grid_ready[1] : L.grid_shade[1], 128, 0, st>>>(
+                W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
+        if (phase == 1 && (events & 4))
             k_wave_shade<COUNT, GENERAL, EV_SURF>
                 <<<L.grid_shade[2], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
-    } else {
+    } else if (events == 7) {
         k_wave_shade<COUNT, GENERAL, -1>
             <<<phase == 0 ? L.grid_ready[0] : L.grid_shade[0], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err,
                                                                            L.counters, nullptr);
     }
 }
 
-// One bounce of group W on stream st.  With split phases and a side stream, the ready phase (its
-// sort and shade kernels) runs on `side`, forked from st before the traversal kernel and joined
-// back before the other phase's sort (fork[0], fork[1]); without a side stream it runs first on st.
+// `to` waits for the work queued on `from` so far (event ev).
+static cudaError_t stream_join(cudaStream_t to, cudaStream_t from, cudaEvent_t ev) {
+    cudaError_t e = cudaEventRecord(ev, from);
+    return e == cudaSuccess ? cudaStreamWaitEvent(to, ev, 0) : e;
+}
+
+// One bounce of group W on stream st.  With side streams (side[0..2], events fork[0..5]) its
+// kernels form this graph of branches; without them they run in the same order on st:
+//
+//   st:      trace ----------> [late finalize on side[1]] ---+
+//   side[0]:  sort + shade ready events ---+                  |
+//   st:                                    +-> sort rest -> fog + miss shade -+-> finalize
+//   side[2]:                                            +-> surface shade ----+
+//
+// Every branch touches its own slots (the ready events', the late samples', the waiting events'
+// by event), so the order between branches does not change any path.
 template <bool COUNT, bool GENERAL>
 static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st,
-                                 cudaStream_t side, const cudaEvent_t* fork) {
+                                 const cudaStream_t* side, const cudaEvent_t* fork) {
+    cudaError_t e = cudaSuccess;
     if (kSplitPhases) {
-        cudaStream_t sa = side ? side : st;
-        if (side) {
-            cudaError_t e = cudaEventRecord(fork[0], st);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(side, fork[0], 0);
-            if (e != cudaSuccess) return e;
-        }
+        cudaStream_t sa = side ? side[0] : st;
+        if (side && (e = stream_join(side[0], st, fork[0])) != cudaSuccess) return e;
         k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, sa>>>(W, cur, 0);
         launch_shade<COUNT, GENERAL>(L, W, cur, 0, sa);
-        if (side) {
-            cudaError_t e = cudaEventRecord(fork[1], side);
-            if (e != cudaSuccess) return e;
-        }
     }
     if (SR_TRACE_OCTANT_SORT) k_trace_octant_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W, cur);
     const bool loop_shadows = GENERAL && L.S.has_transparent;
@@ -302,18 +326,26 @@ static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cu
         k_wave_trace<COUNT, GENERAL, true><<<L.grid_trace, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
     }
     if (loop_shadows) k_wave_shadow_loop<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
-    // an adjoint pass runs the same traversal, then the recording forms of the other kernels
+    // the late finalize: the samples whose last shadow ray the traversal kernel just traced
+    const bool par = SR_PAR_SHADE && side != nullptr;
+    cudaStream_t sl = par ? side[1] : st;
+    if (par && (e = stream_join(side[1], st, fork[1])) != cudaSuccess) return e;
     if (L.adj_mode != kAdjNone)
-        wave_adj_finalize(L, W, cur, st, true);
+        wave_adj_finalize(L, W, cur, sl, true);
     else
-        k_wave_finalize<COUNT, GENERAL, true><<<L.grid_finalize, 128, 0, st>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
+        k_wave_finalize<COUNT, GENERAL, true><<<L.grid_finalize, 128, 0, sl>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
                                                                                L.counters, nullptr);
-    if (kSplitPhases && side) {
-        cudaError_t e = cudaStreamWaitEvent(st, fork[1], 0);
-        if (e != cudaSuccess) return e;
-    }
+    if (kSplitPhases && side && (e = stream_join(st, side[0], fork[2])) != cudaSuccess) return e;
     if (SR_SORT_EVENTS) k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, st>>>(W, cur, 1);
-    launch_shade<COUNT, GENERAL>(L, W, cur, 1, st);
+    if (par && SR_SPLIT_SHADE) {
+        if ((e = stream_join(side[2], st, fork[3])) != cudaSuccess) return e;
+        launch_shade<COUNT, GENERAL>(L, W, cur, 1, side[2], 4);
+        launch_shade<COUNT, GENERAL>(L, W, cur, 1, st, 3);
+        if ((e = stream_join(st, side[2], fork[4])) != cudaSuccess) return e;
+    } else {
+        launch_shade<COUNT, GENERAL>(L, W, cur, 1, st);
+    }
+    if (par && (e = stream_join(st, side[1], fork[5])) != cudaSuccess) return e;
     if (L.adj_mode != kAdjNone)
         wave_adj_finalize(L, W, cur, st, false);
     else
@@ -323,7 +355,7 @@ static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cu
 }
 
 static cudaError_t launch_group_bounces(const WaveLaunch& L, const WaveState& W, int cur, int n, cudaStream_t st,
-                                        cudaStream_t side, const cudaEvent_t* fork) {
+                                        const cudaStream_t* side, const cudaEvent_t* fork) {
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < n && e == cudaSuccess; ++i, cur ^= 1) {
         if (L.general)
@@ -336,14 +368,15 @@ static cudaError_t launch_group_bounces(const WaveLaunch& L, const WaveState& W,
     return e;
 }
 
-// n bounces of every group starting at parity cur.  One group: its bounces on st, the ready phases
-// on side[0] (fork[0], fork[1]).  Several groups: group 0 on st, group g on side[g - 1], forked from
-// st by fork[0] and joined back by fork[g]; each group's phases then run one after the other.
+// n bounces of every group starting at parity cur.  One group: its bounces on st, their parallel
+// branches on side[0..2] (events fork[0..5]).  Several groups: group 0 on st, group g on
+// side[g - 1], forked from st by fork[0] and joined back by fork[g]; each group's kernels then run
+// one after the other.
 static cudaError_t launch_bounces(const WaveLaunch& L, int cur, int n, cudaStream_t st, const cudaStream_t* side,
                                   const cudaEvent_t* fork) {
     cudaError_t e = cudaSuccess;
     if (L.groups == 1) {
-        e = launch_group_bounces(L, L.W[0], cur, n, st, side ? side[0] : nullptr, fork);
+        e = launch_group_bounces(L, L.W[0], cur, n, st, side, fork);
         return e != cudaSuccess ? e : cudaGetLastError();
     }
     e = cudaEventRecord(fork[0], st);
@@ -422,6 +455,7 @@ cudaError_t wave_init(const WaveLaunch& L, cudaStream_t st, uint32_t seed) {
     cudaError_t e = cudaMemsetAsync(L.W[0].counts, 0, (size_t)L.groups * kWaveCounters * sizeof(uint32_t), st);
     if (e == cudaSuccess && SR_SORT_EVENTS) e = cudaMemsetAsync(L.W[0].ev_mark, 0, L.W[0].rec_stride, st);
     if (e != cudaSuccess) return e;
+    if (L.W[0].dynamic) k_wave_cursor<<<1, 1, 0, st>>>(L.W[0].pixel_cursor, L.W[0].rec_stride, seed);
     for (int g = 0; g < L.groups; ++g)
         if (L.W[g].slots) k_wave_init<<<(L.W[g].slots + 127) / 128, 128, 0, st>>>(L.W[g], L.S, L.V, P);
     return cudaGetLastError();

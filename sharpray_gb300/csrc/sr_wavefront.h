@@ -63,6 +63,11 @@ struct WaveState {
                             // traversal kernel
     uint32_t* q_sorted;     // this bounce's event queues in slot order, three of `slots` entries:
                             // the ready events first, then the others
+    uint32_t pixel_tiles;   // 8x4 pixel tiles covering the image (slots / 32 when every pixel has one)
+    uint32_t dynamic;       // 1: fewer slots than pixels -- a slot whose pixel is done takes the next
+                            // unclaimed pixel (its tile-order index in the pixel record, acc2.b.w)
+    uint32_t* pixel_cursor; // next unclaimed pixel (tile-order index), shared by the groups; the
+                            // render's random-number stream in the word after it
     float4* defer[2];       // closest-hit queries the traversal kernel set aside at the end of its
                             // launch (ping-pong by bounce parity), kDeferF4 float4 each: resumed
                             // first by the next bounce's traversal kernel
@@ -97,7 +102,7 @@ constexpr size_t kDeferBytes = 16 * (10 + (3 * 192 + 3) / 4);
 constexpr bool kSplitPhases = SR_SPLIT_PHASES && SR_SORT_EVENTS;
 
 // Number of 32-bit counters at WaveState::counts, and their layout.
-constexpr int kWaveCounters = 25;
+constexpr int kWaveCounters = 27;
 enum : int {
     kCountResolve = 0,     // samples finished this bounce without a shadow ray to trace (parity 0;
                            // parity 1: kCountResolve1)
@@ -112,6 +117,9 @@ enum : int {
     kCountDefer = 19,      // + parity: queries set aside in defer[parity] (may exceed defer_cap)
     kCountResolve1 = 21,   // as kCountResolve, parity 1
     kCountSortedLate = 22, // + event: fill cursors of the slot-ordered queues, the other events
+    kCountPixel = 25,      // group 0: next unclaimed pixel of a render with fewer slots than pixels
+    kCountSeed = 26,       // group 0, same renders: the random-number stream of the render (the
+                           // bounce kernels' parameters stay seed-independent for graph reuse)
 };
 #if defined(__CUDACC__)
 __host__ __device__
@@ -205,6 +213,15 @@ struct WaveGroups {
 #ifndef SR_TRACE_OCTANT_SORT
 #define SR_TRACE_OCTANT_SORT 0
 #endif
+// Kernels of a bounce that touch disjoint slots run on parallel graph branches (SR_PAR_SHADE = 1):
+// the late finalize beside the ready phase's join and the waiting phase's sort, and the surface
+// shade beside the fog and miss shade kernels of the waiting phase.
+#ifndef SR_PAR_SHADE
+#define SR_PAR_SHADE 1
+#endif
+// Side streams and events a bounce's branches use (one group), or the other groups' streams.
+constexpr int kSideStreams = kWaveGroups > 3 ? kWaveGroups - 1 : 3;
+constexpr int kForkEvents = kWaveGroups + 1 > 6 ? kWaveGroups + 1 : 6;
 constexpr int kWaveKernelsPerBounce = (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 1 : 0) +
                                       (kSplitPhases ? (SR_SPLIT_SHADE ? 3 : 2) : 0) + (SR_TRACE_OCTANT_SORT ? 1 : 0);
 
@@ -217,6 +234,7 @@ struct WaveTune {
     uint32_t max_iters;   // bounce-loop cap (0 = the runaway guard)
     uint32_t max_actions; // per-traversal action cap (0 = kDefaultMaxActions)
     int trace_block;      // threads per block of the traversal kernel: 64, 128 or 256 (0 = 128)
+    uint32_t max_slots;   // path slots in flight (queue capacity; 0 = one per pixel)
 };
 // Resident blocks per SM of the traversal, fog-shade and surface-shade kernels.
 void wave_occupancy(bool general, int* trace, int* fog, int* surface);
@@ -239,7 +257,8 @@ cudaError_t wave_build_graph_batch(const WaveLaunch* Ls, int n, cudaStream_t cap
 // the late finalize (late = true) or the finalize, the shade kernels of a phase, the tail; grids
 // from their occupancy.
 void wave_adj_finalize(const WaveLaunch& L, const WaveState& W, int cur, cudaStream_t st, bool late);
-void wave_adj_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st);
+// `events`: bit 0 fog, bit 1 miss, bit 2 surface (phase 0 never has surface events).
+void wave_adj_shade(const WaveLaunch& L, const WaveState& W, int cur, int phase, cudaStream_t st, int events = 7);
 cudaError_t wave_adj_tail(const WaveLaunch& L, int cur, cudaStream_t st);
 void wave_adj_grid_sizes(WaveLaunch& L, int sms);
 // Closest hits of n world rays (6 floats each, device) through the persistent traversal loop of the

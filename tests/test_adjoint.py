@@ -448,16 +448,20 @@ def test_wavefront_replay_equals_pixel_replay(torch_mod, fog, general):
     d_image = torch.from_numpy((2.0 * (img - (img * np.float32(0.6) + np.float32(0.05)))).astype(np.float32)).cuda()
     ta, tr = rig.tex[1], rig.tex[3]
     out = {}
-    for form, mode in ((_abi.SR_ADJOINT_REPLAY_PIXEL, _abi.SR_RENDER_AUTO),
-                       (_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_RENDER_AUTO),
-                       (_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_RENDER_WAVEFRONT)):
+    # the last form replays with 96 slots for the 1200 pixels: slots claim pixels as theirs finish
+    for form, mode, slots in ((_abi.SR_ADJOINT_REPLAY_PIXEL, _abi.SR_RENDER_AUTO, 0),
+                              (_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_RENDER_AUTO, 0),
+                              (_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_RENDER_WAVEFRONT, 0),
+                              (_abi.SR_ADJOINT_REPLAY_WAVEFRONT, _abi.SR_RENDER_AUTO, 96)):
         rig.scene.set_adjoint_replay(form)
         rig.scene.set_render_mode(mode)
+        rig.scene.set_tuning(max_slots=slots)
         replay = torch.zeros(rig.d.width * rig.d.height * 3, device="cuda")
-        out[(form, mode)] = adjoint_all(rig, d_image, ta, tr, fog, replay)
-        assert np.array_equal(replay.cpu().numpy().view(np.uint32), img.view(np.uint32)), (form, mode)
+        out[(form, mode, slots)] = adjoint_all(rig, d_image, ta, tr, fog, replay)
+        assert np.array_equal(replay.cpu().numpy().view(np.uint32), img.view(np.uint32)), (form, mode, slots)
     rig.scene.set_render_mode(_abi.SR_RENDER_AUTO)
-    ref = out[(_abi.SR_ADJOINT_REPLAY_PIXEL, _abi.SR_RENDER_AUTO)]
+    rig.scene.set_tuning()
+    ref = out[(_abi.SR_ADJOINT_REPLAY_PIXEL, _abi.SR_RENDER_AUTO, 0)]
     for key, got in out.items():
         for k, (a, b) in enumerate(zip(got, ref)):
             if k == 2 and not fog:

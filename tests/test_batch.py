@@ -122,3 +122,28 @@ def test_tuning_leaves_results_unchanged(batch_scenes):
     assert chosen["tail_divisor"] in (8, 16, 32) and chosen["trace_block_threads"] in (64, 128, 256)
     same(host(render_single(torch, ctx, d, s)), ref)
     s.set_tuning()
+
+
+@pytest.mark.parametrize("index", [1, 3])
+def test_fewer_slots_than_pixels_leave_results_unchanged(batch_scenes, index):
+    """Slot capacity below the pixel count (slots claim the pixels left over as theirs finish, each
+    with the pixel's own random-number stream) gives the same AOVs, in every render mode, with the
+    reference's stream and with another one; the adaptive stop of the features scene included."""
+    torch, ctx, descs, scenes = batch_scenes
+    d, s = descs[index], scenes[index]
+    n = d.width * d.height
+    try:
+        for seed in (0, 7):
+            s.set_seed(seed)
+            s.set_tuning()
+            ref = host(render_single(torch, ctx, d, s))
+            for slots in (n // 3, 32, 45):  # a third (rounded up to 32), one warp, a non-multiple of 32
+                for mode in (_abi.SR_RENDER_AUTO, _abi.SR_RENDER_WAVEFRONT):
+                    s.set_render_mode(mode)
+                    s.set_tuning(max_slots=slots)
+                    same(host(render_single(torch, ctx, d, s)), ref)
+            s.set_render_mode(_abi.SR_RENDER_AUTO)
+    finally:
+        s.set_seed(0)
+        s.set_tuning()
+        s.set_render_mode(_abi.SR_RENDER_AUTO)
