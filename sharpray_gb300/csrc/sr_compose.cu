@@ -5,12 +5,13 @@
 //
 // A packing pass first turns the AOV planes into two float4 planes, {radiance.rgb, luminance}
 // and {normal.xyz, depth}, plus {fog.rgb, 0}, so that every filter tap is two 128-bit loads and
-// the neighbour luminance is not recomputed per tap.  The taps of a pixel are visited in the
-// reference order (rows top to bottom, columns left to right) so the weighted sums accumulate
-// in the same order; the spatial weights exp(-d^2 / 2r^2) come from a host-evaluated table.  Per
-// tap the normal, depth and luminance Gaussians are one fast exponential of their summed
-// exponents and the sums accumulate with fused multiply-adds: the filter is the reference's up to
-// float rounding (images agree within one code value).
+// the neighbour luminance is not recomputed per tap.  The packed luminance, normal and depth are
+// pre-scaled so that the normal, depth and luminance Gaussians of a tap are one base-2 exponential
+// of a sum of three squares, and the two neighbour classes of compose.cs:154-158 (normal present,
+// depth finite) ride in the sign bits of the packed luminance and depth.  The taps of a pixel are
+// visited in the reference order (rows top to bottom, columns left to right) so the weighted sums
+// accumulate in the same order; the spatial weights exp(-d^2 / 2r^2) come from a host-evaluated
+// table.  The filter is the reference's up to float rounding (images agree within one code value).
 #include <atomic>
 #include <cuda_runtime.h>
 
@@ -18,15 +19,6 @@
 #include "sr_kernels.h"
 
 namespace sr {
-
-__global__ void k_pack(DevAovs in, uint32_t n, float4* p_rad, float4* p_geo, float4* p_fog) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    Col r{in.radiance[3 * i], in.radiance[3 * i + 1], in.radiance[3 * i + 2]};
-    p_rad[i] = make_float4(r.r, r.g, r.b, luminance(r));
-    p_geo[i] = make_float4(in.normals[3 * i], in.normals[3 * i + 1], in.normals[3 * i + 2], in.depth[i]);
-    p_fog[i] = make_float4(in.radiance_fog[3 * i], in.radiance_fog[3 * i + 1], in.radiance_fog[3 * i + 2], 0.0f);
-}
 
 // Color.ToPixel math.cs:127-136.
 __device__ __forceinline__ void to_pixel(Col c, uint8_t* out) {
@@ -50,6 +42,136 @@ __device__ __forceinline__ void tonemap(const ComposeConsts& k, Col radiance, ui
     }
 }
 
+// Scale factors of the packed planes: the Gaussian exp(-x^2 * inv) of compose.cs:165-190 is
+// 2^-((s x)^2) with s = sqrt(inv * log2(e)).
+struct ComposeScales {
+    float n, d, l;  // normal, depth and luminance
+};
+constexpr uint32_t kSignBit = 0x80000000u;
+
+// Packed planes of pixel i: p_rad = {rgb, s_l * luminance}, p_geo = {s_n * normal, s_d * depth} and
+// p_fog = {fog rgb, 0}.  A pixel without a normal (|n|^2 == 0, compose.cs:140) stores a zero normal
+// and the luminance with its sign bit set; a pixel without a finite depth stores -0 as its depth.
+// Accepted neighbours are always of the centre's class, so a zero normal or depth stands only
+// where the reference skips that Gaussian, and luminance and depth are never negative, so their
+// magnitudes stay intact.
+__global__ void k_pack(DevAovs in, uint32_t n, ComposeScales sc, float4* p_rad, float4* p_geo, float4* p_fog) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Col r{in.radiance[3 * i], in.radiance[3 * i + 1], in.radiance[3 * i + 2]};
+    V3 nv{in.normals[3 * i], in.normals[3 * i + 1], in.normals[3 * i + 2]};
+    float d = in.depth[i];
+    const bool has_n = mag_sqr(nv) > 0.0f, has_d = !isinf(d);
+    const float l = sc.l * luminance(r);
+    p_rad[i] = make_float4(r.r, r.g, r.b, has_n ? l : __uint_as_float(__float_as_uint(l) | kSignBit));
+    const float gd = has_d ? sc.d * d : __uint_as_float(kSignBit);
+    p_geo[i] = has_n ? make_float4(sc.n * nv.x, sc.n * nv.y, sc.n * nv.z, gd) : make_float4(0.f, 0.f, 0.f, gd);
+    p_fog[i] = make_float4(in.radiance_fog[3 * i], in.radiance_fog[3 * i + 1], in.radiance_fog[3 * i + 2], 0.0f);
+}
+
+// 2^x (the hardware approximation; x <= 0 here).
+__device__ __forceinline__ float exp2_fast(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// The centre pixel of Filter (compose.cs:101-204) and its running sums.
+struct FilterCentre {
+    uint32_t cls_l, cls_d;  // sign-bit classes of the packed luminance and depth
+    float nx, ny, nz, d, l; // packed normal, depth and luminance magnitudes
+    float dw;               // denoise weight
+    float wsum;
+    Col rsum;
+};
+
+// One tap of Filter (compose.cs:150-198) for centre c: neighbour q0 = {rgb, packed luminance},
+// q1 = {packed normal, packed depth}, spatial weight ws.
+__device__ __forceinline__ void filter_tap(FilterCentre& c, const float4& q0, const float4& q1, float ws) {
+    // neighbours of another class are rejected (compose.cs:154-158)
+    if ((int)((__float_as_uint(q0.w) ^ c.cls_l) | (__float_as_uint(q1.w) ^ c.cls_d)) < 0) return;
+    const float dx = c.nx - q1.x, dy = c.ny - q1.y, dz = c.nz - q1.z;
+    const float dd = c.d - fabsf(q1.w);
+    const float dl = fmaxf(0.0f, fabsf(q0.w) - c.l);
+    float e = dx * dx;
+    e = __fmaf_rn(dy, dy, e);
+    e = __fmaf_rn(dz, dz, e);
+    e = __fmaf_rn(dd, dd, e);
+    e = __fmaf_rn(dl, dl, e);
+    const float w = (c.dw * ws) * exp2_fast(-e);
+    c.wsum += w;
+    c.rsum = Col{__fmaf_rn(q0.x, w, c.rsum.r), __fmaf_rn(q0.y, w, c.rsum.g), __fmaf_rn(q0.z, w, c.rsum.b)};
+}
+
+// Taps kx in [kx0, kx1] of one kernel row: prow / grow point at the row's column x, wrow at its
+// spatial weights (centre column at offset 0).
+__device__ __forceinline__ void filter_row(FilterCentre& c, const float4* __restrict__ prow,
+                                           const float4* __restrict__ grow, const float* __restrict__ wrow, int kx0,
+                                           int kx1) {
+#pragma unroll 1
+    for (int kx = kx0; kx <= kx1; ++kx) filter_tap(c, __ldg(prow + kx), __ldg(grow + kx), __ldg(wrow + kx));
+}
+
+// Columns kx in [kx0, kx1] of one image row for two vertically adjacent pixels a and b (MODE bit 0:
+// the column is a tap of a, bit 1: of b), each tap column loaded once for both; wa / wb point at
+// the row's spatial weights of each pixel's kernel.
+template <int MODE>
+__device__ __forceinline__ void filter_cols(FilterCentre& a, FilterCentre& b, const float4* __restrict__ prow,
+                                            const float4* __restrict__ grow, const float* __restrict__ wa,
+                                            const float* __restrict__ wb, int kx0, int kx1) {
+#pragma unroll 1
+    for (int kx = kx0; kx <= kx1; ++kx) {
+        const float4 q0 = __ldg(prow + kx), q1 = __ldg(grow + kx);
+        if (MODE & 1) filter_tap(a, q0, q1, __ldg(wa + kx));
+        if (MODE & 2) filter_tap(b, q0, q1, __ldg(wb + kx));
+    }
+}
+
+// FilterFog compose.cs:206-245 for pixel (x, y) with fog radiance `fog`.
+__device__ __forceinline__ Col filter_fog(const float4* __restrict__ p_fog, uint32_t width, uint32_t height,
+                                          const ComposeConsts& k, const float* __restrict__ fog_spatial, int x, int y,
+                                          Col fog) {
+    const int R = k.fog_radius;
+    const int side = 2 * R + 1;
+    const float* row_half = fog_spatial + side * side;
+    float wsum = 1.0f;
+    Col rsum = fog;
+    const int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
+    for (int ky = ky0; ky <= ky1; ++ky) {
+        const int hw = (int)__ldg(row_half + ky + R);
+        const int kx0 = max(-hw, -x), kx1 = min(hw, (int)width - 1 - x);
+        const float* wrow = fog_spatial + (ky + R) * side + R;
+        const float4* frow = p_fog + (size_t)(y + ky) * width + x;
+        for (int kx = kx0; kx <= kx1; ++kx) {
+            if (kx == 0 && ky == 0) continue;
+            const float w = __ldg(wrow + kx);
+            const float4 f = __ldg(frow + kx);
+            wsum += w;
+            rsum = Col{__fmaf_rn(f.x, w, rsum.r), __fmaf_rn(f.y, w, rsum.g), __fmaf_rn(f.z, w, rsum.b)};
+        }
+    }
+    return rsum / wsum;
+}
+
+// The centre of Filter for pixel ci (packed c0 = {rgb, packed luminance}, c1 = {packed normal,
+// depth}); false when its denoise weight takes the early out (compose.cs:125-131).
+__device__ __forceinline__ bool filter_centre(FilterCentre& c, const ComposeConsts& k, const float4& c0,
+                                              const float4& c1, float variance) {
+    const Col main = col3(c0);
+    const float lum = luminance(main);
+    const float boost = 1.0f + lum * k.lum_boost;
+    c.dw = fminf(variance * boost * k.strength, k.strength_max);
+    if (c.dw < 1e-4f) return false;
+    c.cls_l = __float_as_uint(c0.w) & kSignBit;
+    c.cls_d = __float_as_uint(c1.w) & kSignBit;
+    c.nx = c1.x, c.ny = c1.y, c.nz = c1.z;
+    c.d = fabsf(c1.w);
+    c.l = fabsf(c0.w);
+    c.wsum = 1.0f;
+    c.rsum = main;
+    return true;
+}
+
 // Table layout (host-built): for radius R, (2R+1)^2 spatial weights followed by 2R+1 row half-widths
 // (as floats) = the largest |kx| with kx^2 + ky^2 <= R^2.
 __global__ void __launch_bounds__(128) k_compose(const float4* __restrict__ p_rad, const float4* __restrict__ p_geo,
@@ -66,226 +188,127 @@ __global__ void __launch_bounds__(128) k_compose(const float4* __restrict__ p_ra
     Col fog = col3(__ldg(p_fog + ci));
     if (denoise) {
         // ---- Filter compose.cs:101-204 ----
-        float4 c1 = __ldg(p_geo + ci);
-        V3 cn = v3(c1);
-        float cd = c1.w;
-        bool has_n = mag_sqr(cn) > 0.0f;
-        bool has_d = !isinf(cd);
-        float lum = c0.w;
-        float boost = 1.0f + lum * k.lum_boost;
-        float dw = fminf(__ldg(variance + ci) * boost * k.strength, k.strength_max);
-        if (!(dw < 1e-4f)) {
-            int R = k.radius;
-            int side = 2 * R + 1;
+        FilterCentre c;
+        if (filter_centre(c, k, c0, __ldg(p_geo + ci), __ldg(variance + ci))) {
+            const int R = k.radius;
+            const int side = 2 * R + 1;
             const float* row_half = spatial + side * side;
-            float wsum = 1.0f;
-            Col rsum = main;
-            int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
+            const int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
             for (int ky = ky0; ky <= ky1; ++ky) {
-                int hw = (int)__ldg(row_half + ky + R);
-                int kx0 = max(-hw, -x), kx1 = min(hw, (int)width - 1 - x);
+                const int hw = (int)__ldg(row_half + ky + R);
+                const int kx0 = max(-hw, -x), kx1 = min(hw, (int)width - 1 - x);
                 const float* wrow = spatial + (ky + R) * side + R;
                 const float4* prow = p_rad + (size_t)(y + ky) * width + x;
                 const float4* grow = p_geo + (size_t)(y + ky) * width + x;
-                for (int kx = kx0; kx <= kx1; ++kx) {
-                    if (kx == 0 && ky == 0) continue;
-                    float4 q1 = __ldg(grow + kx);
-                    V3 nn = v3(q1);
-                    bool nh_n = mag_sqr(nn) > 0.0f;
-                    bool nh_d = !isinf(q1.w);
-                    if (has_n != nh_n || has_d != nh_d) continue;
-                    float4 q0 = __ldg(prow + kx);
-                    float w = dw * __ldg(wrow + kx);
-                    // the normal, depth and luminance Gaussians of compose.cs:165-190 as one
-                    // exponential of the summed exponents (equal up to rounding; a weight the
-                    // reference zeroes by underflow stays zero)
-                    if (w > 0.0f) {
-                        float e = 0.0f;
-                        if (has_n) {
-                            V3 nd = cn - nn;
-                            e = mag_sqr(nd) * k.normal_limit_inv;
-                        }
-                        if (has_d) {
-                            float dd = cd - q1.w;
-                            e = __fmaf_rn(dd * dd, k.depth_limit_inv, e);
-                        }
-                        float ld = fmaxf(0.0f, q0.w - lum);
-                        e = __fmaf_rn(ld * ld, k.lum_limit_inv, e);
-                        w *= __expf(-e);
-                    }
-                    wsum += w;
-                    rsum = Col{__fmaf_rn(q0.x, w, rsum.r), __fmaf_rn(q0.y, w, rsum.g), __fmaf_rn(q0.z, w, rsum.b)};
+                if (ky != 0) {
+                    filter_row(c, prow, grow, wrow, kx0, kx1);
+                } else {  // the centre itself is not a tap
+                    filter_row(c, prow, grow, wrow, kx0, -1);
+                    filter_row(c, prow, grow, wrow, 1, kx1);
                 }
             }
-            main = rsum / wsum;
+            main = c.rsum / c.wsum;
         }
-        // ---- FilterFog compose.cs:206-245 ----
-        {
-            int R = k.fog_radius;
-            int side = 2 * R + 1;
-            const float* row_half = fog_spatial + side * side;
-            float wsum = 1.0f;
-            Col rsum = fog;
-            int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
-            for (int ky = ky0; ky <= ky1; ++ky) {
-                int hw = (int)__ldg(row_half + ky + R);
-                int kx0 = max(-hw, -x), kx1 = min(hw, (int)width - 1 - x);
-                const float* wrow = fog_spatial + (ky + R) * side + R;
-                const float4* frow = p_fog + (size_t)(y + ky) * width + x;
-                for (int kx = kx0; kx <= kx1; ++kx) {
-                    if (kx == 0 && ky == 0) continue;
-                    float w = __ldg(wrow + kx);
-                    float4 f = __ldg(frow + kx);
-                    wsum += w;
-                    rsum = Col{__fmaf_rn(f.x, w, rsum.r), __fmaf_rn(f.y, w, rsum.g), __fmaf_rn(f.z, w, rsum.b)};
-                }
-            }
-            fog = rsum / wsum;
-        }
+        fog = filter_fog(p_fog, width, height, k, fog_spatial, x, y, fog);
     }
     const Col total = main + fog;
     if (linear) linear[3 * ci] = total.r, linear[3 * ci + 1] = total.g, linear[3 * ci + 2] = total.b;
     if (rgb8) tonemap(k, total, rgb8 + ci * 3);
 }
 
-// Two horizontally adjacent pixels per thread (SR_COMPOSE_PAIR = 1): the main filter walks the
-// union of both pixels' tap columns row by row, so every tap column's two float4 loads serve both
-// pixels; each pixel still takes exactly its own taps in the reference order, so the sums (and the
-// image) are those of k_compose.  Measured 0.6 % slower at 1920x1080 (the filter is bound by the
-// per-tap arithmetic, not by its loads), so it stays off.
-#ifndef SR_COMPOSE_PAIR
-#define SR_COMPOSE_PAIR 0
+// Two vertically adjacent pixels per thread (SR_COMPOSE_ROWS = 2): a = (x, y) and b = (x, y + 1)
+// walk the union of their kernel rows together, and each tap column of a row is loaded once for
+// both.  Each pixel still takes exactly its own taps in the reference order (per row: the columns
+// only the wider of the two kernels covers on the left, the shared columns, those on the right),
+// so its sums -- and the image -- are those of k_compose.
+#ifndef SR_COMPOSE_ROWS
+#define SR_COMPOSE_ROWS 2
 #endif
 
-struct FilterPx {
-    bool filter;  // the pixel's joint bilateral filter runs (weight above the early-out)
-    bool has_n, has_d;
-    V3 cn;
-    float cd, lum, dw, wsum;
-    Col rsum;
-};
-
-// One tap of Filter (compose.cs:150-198) for pixel p: neighbour q0 = {rgb, luminance},
-// q1 = {normal, depth}, spatial weight ws.
-__device__ __forceinline__ void filter_tap(FilterPx& p, const ComposeConsts& k, float4 q0, float4 q1, float ws) {
-    V3 nn = v3(q1);
-    bool nh_n = mag_sqr(nn) > 0.0f;
-    bool nh_d = !isinf(q1.w);
-    if (p.has_n != nh_n || p.has_d != nh_d) return;
-    float w = p.dw * ws;
-    if (w > 0.0f) {
-        float e = 0.0f;
-        if (p.has_n) {
-            V3 nd = p.cn - nn;
-            e = mag_sqr(nd) * k.normal_limit_inv;
-        }
-        if (p.has_d) {
-            float dd = p.cd - q1.w;
-            e = __fmaf_rn(dd * dd, k.depth_limit_inv, e);
-        }
-        float ld = fmaxf(0.0f, q0.w - p.lum);
-        e = __fmaf_rn(ld * ld, k.lum_limit_inv, e);
-        w *= __expf(-e);
-    }
-    p.wsum += w;
-    p.rsum = Col{__fmaf_rn(q0.x, w, p.rsum.r), __fmaf_rn(q0.y, w, p.rsum.g), __fmaf_rn(q0.z, w, p.rsum.b)};
-}
-
-// FilterFog compose.cs:206-245 for pixel (x, y).
-__device__ __forceinline__ Col filter_fog(const float4* __restrict__ p_fog, uint32_t width, uint32_t height,
-                                          const ComposeConsts& k, const float* __restrict__ fog_spatial, int x, int y,
-                                          Col fog) {
-    int R = k.fog_radius;
-    int side = 2 * R + 1;
-    const float* row_half = fog_spatial + side * side;
-    float wsum = 1.0f;
-    Col rsum = fog;
-    int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
-    for (int ky = ky0; ky <= ky1; ++ky) {
-        int hw = (int)__ldg(row_half + ky + R);
-        int kx0 = max(-hw, -x), kx1 = min(hw, (int)width - 1 - x);
-        const float* wrow = fog_spatial + (ky + R) * side + R;
-        const float4* frow = p_fog + (size_t)(y + ky) * width + x;
-        for (int kx = kx0; kx <= kx1; ++kx) {
-            if (kx == 0 && ky == 0) continue;
-            float w = __ldg(wrow + kx);
-            float4 f = __ldg(frow + kx);
-            wsum += w;
-            rsum = Col{__fmaf_rn(f.x, w, rsum.r), __fmaf_rn(f.y, w, rsum.g), __fmaf_rn(f.z, w, rsum.b)};
-        }
-    }
-    return rsum / wsum;
-}
-
-__global__ void __launch_bounds__(128) k_compose_pair(const float4* __restrict__ p_rad,
-                                                      const float4* __restrict__ p_geo,
-                                                      const float4* __restrict__ p_fog,
-                                                      const float* __restrict__ variance, uint32_t width,
-                                                      uint32_t height, ComposeConsts k,
-                                                      const float* __restrict__ spatial,
-                                                      const float* __restrict__ fog_spatial, int denoise,
-                                                      uint8_t* rgb8, float* linear) {
-    const int xa = 2 * (int)(blockIdx.x * 32 + (threadIdx.x & 31));
-    const int y = blockIdx.y * 4 + (threadIdx.x >> 5);
-    if (xa >= (int)width || y >= (int)height) return;
-    const bool b_live = xa + 1 < (int)width;
-    FilterPx px[2];
-    Col main[2], fog[2];
-    for (int j = 0; j < 2; ++j) {
-        px[j].filter = false;
-        if (j == 1 && !b_live) continue;
-        const size_t ci = (size_t)y * width + xa + j;
-        const float4 c0 = __ldg(p_rad + ci);
-        main[j] = col3(c0);
-        fog[j] = col3(__ldg(p_fog + ci));
-        if (!denoise) continue;
-        const float4 c1 = __ldg(p_geo + ci);
-        FilterPx& p = px[j];
-        p.cn = v3(c1);
-        p.cd = c1.w;
-        p.has_n = mag_sqr(p.cn) > 0.0f;
-        p.has_d = !isinf(p.cd);
-        p.lum = c0.w;
-        const float boost = 1.0f + p.lum * k.lum_boost;
-        p.dw = fminf(__ldg(variance + ci) * boost * k.strength, k.strength_max);
-        p.filter = !(p.dw < 1e-4f);
-        p.wsum = 1.0f;
-        p.rsum = main[j];
-    }
-    if (px[0].filter || px[1].filter) {
-        // ---- Filter compose.cs:101-204, both pixels over the union of their tap columns ----
-        const int R = k.radius;
-        const int side = 2 * R + 1;
-        const float* row_half = spatial + side * side;
-        const int xb = xa + 1;
-        const int ky0 = max(-R, -y), ky1 = min(R, (int)height - 1 - y);
-        for (int ky = ky0; ky <= ky1; ++ky) {
-            const int hw = (int)__ldg(row_half + ky + R);
-            const int c_lo = max(0, (px[0].filter ? xa : xb) - hw);
-            const int c_hi = min((int)width - 1, (px[1].filter ? xb : xa) + hw);
-            const float* wrow = spatial + (ky + R) * side + R;
-            const float4* prow = p_rad + (size_t)(y + ky) * width;
-            const float4* grow = p_geo + (size_t)(y + ky) * width;
-            for (int c = c_lo; c <= c_hi; ++c) {
-                const float4 q1 = __ldg(grow + c);
-                const float4 q0 = __ldg(prow + c);
-                const int ka = c - xa, kb = c - xb;
-                if (px[0].filter && ka <= hw && (ka != 0 || ky != 0)) filter_tap(px[0], k, q0, q1, __ldg(wrow + ka));
-                if (px[1].filter && kb >= -hw && (kb != 0 || ky != 0))
-                    filter_tap(px[1], k, q0, q1, __ldg(wrow + kb));
+__global__ void __launch_bounds__(128, 6) k_compose_rows2(const float4* __restrict__ p_rad,
+                                                       const float4* __restrict__ p_geo,
+                                                       const float4* __restrict__ p_fog,
+                                                       const float* __restrict__ variance, uint32_t width,
+                                                       uint32_t height, ComposeConsts k,
+                                                       const float* __restrict__ spatial,
+                                                       const float* __restrict__ fog_spatial, int denoise,
+                                                       uint8_t* rgb8, float* linear) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int y = 2 * (int)(blockIdx.y * 4 + (threadIdx.x >> 5));
+    if (x >= (int)width || y >= (int)height) return;
+    const bool b_in = y + 1 < (int)height;
+    const size_t ca = (size_t)y * width + x, cb = ca + width;
+    const float4 a0 = __ldg(p_rad + ca);
+    float4 b0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (b_in) b0 = __ldg(p_rad + cb);
+    Col main_a = col3(a0), main_b = col3(b0);
+    if (denoise) {
+        // ---- Filter compose.cs:101-204 for both pixels ----
+        FilterCentre A, B;
+        const bool fa = filter_centre(A, k, a0, __ldg(p_geo + ca), __ldg(variance + ca));
+        const bool fb = b_in && filter_centre(B, k, b0, __ldg(p_geo + cb), __ldg(variance + cb));
+        if (fa || fb) {
+            const int R = k.radius;
+            const int side = 2 * R + 1;
+            const float* row_half = spatial + side * side;
+            const int colmin = -x, colmax = (int)width - 1 - x;
+            // image rows y + ky for ky in [-R, R + 1]: row ky of a's kernel and row ky - 1 of b's
+            const int ky0 = max(-R, -y), ky1 = min(R + 1, (int)height - 1 - y);
+            for (int ky = ky0; ky <= ky1; ++ky) {
+                const int ka = ky, kb = ky - 1;
+                const int hwa = fa && ka <= R ? (int)__ldg(row_half + ka + R) : -1;
+                const int hwb = fb && kb >= -R ? (int)__ldg(row_half + kb + R) : -1;
+                const float* wa = spatial + (ka + R) * side + R;
+                const float* wb = spatial + (kb + R) * side + R;
+                const float4* prow = p_rad + (size_t)(y + ky) * width + x;
+                const float4* grow = p_geo + (size_t)(y + ky) * width + x;
+                // a pixel's own centre is not one of its taps
+                const int skip = (ka == 0 ? 1 : 0) | (kb == 0 ? 2 : 0);
+                auto run = [&](int mode, int k0, int k1) {
+                    if (k0 > k1 || mode == 0) return;
+                    auto cols = [&](int m, int c0, int c1) {
+                        if (c0 > c1) return;
+                        if (m == 1)
+                            filter_cols<1>(A, B, prow, grow, wa, wb, c0, c1);
+                        else if (m == 2)
+                            filter_cols<2>(A, B, prow, grow, wa, wb, c0, c1);
+                        else if (m == 3)
+                            filter_cols<3>(A, B, prow, grow, wa, wb, c0, c1);
+                    };
+                    if ((mode & skip) && k0 <= 0 && 0 <= k1) {
+                        cols(mode, k0, -1);
+                        cols(mode & ~skip, 0, 0);
+                        cols(mode, 1, k1);
+                    } else {
+                        cols(mode, k0, k1);
+                    }
+                };
+                const int hmin = min(hwa, hwb), hmax = max(hwa, hwb);
+                if (hmax < 0) continue;
+                const int wide = hwa > hwb ? 1 : 2;  // the pixel whose kernel row is wider
+                const int lo = max(-hmax, colmin), hi = min(hmax, colmax);
+                if (hmin < 0) {
+                    run(wide, lo, hi);
+                } else {
+                    const int clo = max(-hmin, colmin), chi = min(hmin, colmax);
+                    run(wide, lo, clo - 1);
+                    run(3, clo, chi);
+                    run(wide, chi + 1, hi);
+                }
             }
+            if (fa) main_a = A.rsum / A.wsum;
+            if (fb) main_b = B.rsum / B.wsum;
         }
-        for (int j = 0; j < 2; ++j)
-            if (px[j].filter) main[j] = px[j].rsum / px[j].wsum;
     }
-    for (int j = 0; j < 2; ++j) {
-        if (j == 1 && !b_live) break;
-        if (denoise) fog[j] = filter_fog(p_fog, width, height, k, fog_spatial, xa + j, y, fog[j]);
-        const size_t ci = (size_t)y * width + xa + j;
-        const Col total = main[j] + fog[j];
+    auto finish = [&](size_t ci, int py, const Col& m) {
+        Col fog = col3(__ldg(p_fog + ci));
+        if (denoise) fog = filter_fog(p_fog, width, height, k, fog_spatial, x, py, fog);
+        const Col total = m + fog;
         if (linear) linear[3 * ci] = total.r, linear[3 * ci + 1] = total.g, linear[3 * ci + 2] = total.b;
         if (rgb8) tonemap(k, total, rgb8 + ci * 3);
-    }
+    };
+    finish(ca, y, main_a);
+    if (b_in) finish(cb, y + 1, main_b);
 }
 
 cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, const ComposeConsts& k,
@@ -296,15 +319,18 @@ cudaError_t launch_compose(const DevAovs& in, uint32_t width, uint32_t height, c
     float4* p_rad = scratch;
     float4* p_geo = scratch + n;
     float4* p_fog = scratch + 2 * (size_t)n;
-    k_pack<<<(n + 255) / 256, 256, 0, stream>>>(in, n, p_rad, p_geo, p_fog);
-    if (SR_COMPOSE_PAIR) {
-        dim3 grid((width + 63) / 64, (height + 3) / 4);
-        k_compose_pair<<<grid, 128, 0, stream>>>(p_rad, p_geo, p_fog, in.variance, width, height, k, spatial,
-                                                 fog_spatial, denoise ? 1 : 0, rgb8, linear);
+    const float log2e = 1.4426950408889634f;
+    const ComposeScales sc{sqrtf(k.normal_limit_inv * log2e), sqrtf(k.depth_limit_inv * log2e),
+                           sqrtf(k.lum_limit_inv * log2e)};
+    k_pack<<<(n + 255) / 256, 256, 0, stream>>>(in, n, sc, p_rad, p_geo, p_fog);
+    if (SR_COMPOSE_ROWS == 2) {
+        dim3 grid((width + 31) / 32, (height + 7) / 8);
+        k_compose_rows2<<<grid, 128, 0, stream>>>(p_rad, p_geo, p_fog, in.variance, width, height, k, spatial,
+                                                  fog_spatial, denoise ? 1 : 0, rgb8, linear);
     } else {
         dim3 grid((width + 31) / 32, (height + 3) / 4);
-        k_compose<<<grid, 128, 0, stream>>>(p_rad, p_geo, p_fog, in.variance, width, height, k, spatial, fog_spatial,
-                                            denoise ? 1 : 0, rgb8, linear);
+        k_compose<<<grid, 128, 0, stream>>>(p_rad, p_geo, p_fog, in.variance, width, height, k, spatial,
+                                            fog_spatial, denoise ? 1 : 0, rgb8, linear);
     }
     return cudaGetLastError();
 }
