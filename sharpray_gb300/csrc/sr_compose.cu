@@ -115,11 +115,21 @@ __device__ __forceinline__ void filter_row(FilterCentre& c, const float4* __rest
 // Columns kx in [kx0, kx1] of one image row for two vertically adjacent pixels a and b (MODE bit 0:
 // the column is a tap of a, bit 1: of b), each tap column loaded once for both; wa / wb point at
 // the row's spatial weights of each pixel's kernel.
+// Unroll factor of the two-row kernel's column loop and its minimum resident blocks per SM (the
+// register cap).  Measured at 1920x1080: unroll 2 at 6 blocks (80 registers) 7.0 ms; unroll 1 at 6
+// or 8 blocks 7.5 ms; unroll 2 at 8 blocks (64 registers, spills) 8.2 ms.
+#ifndef SR_COMPOSE_COL_UNROLL
+#define SR_COMPOSE_COL_UNROLL 2
+#endif
+#ifndef SR_COMPOSE_MIN_BLOCKS
+#define SR_COMPOSE_MIN_BLOCKS 6
+#endif
+constexpr int kComposeColUnroll = SR_COMPOSE_COL_UNROLL;
 template <int MODE>
 __device__ __forceinline__ void filter_cols(FilterCentre& a, FilterCentre& b, const float4* __restrict__ prow,
                                             const float4* __restrict__ grow, const float* __restrict__ wa,
                                             const float* __restrict__ wb, int kx0, int kx1) {
-#pragma unroll 1
+#pragma unroll kComposeColUnroll
     for (int kx = kx0; kx <= kx1; ++kx) {
         const float4 q0 = __ldg(prow + kx), q1 = __ldg(grow + kx);
         if (MODE & 1) filter_tap(a, q0, q1, __ldg(wa + kx));
@@ -225,7 +235,7 @@ __global__ void __launch_bounds__(128) k_compose(const float4* __restrict__ p_ra
 #define SR_COMPOSE_ROWS 2
 #endif
 
-__global__ void __launch_bounds__(128, 6) k_compose_rows2(const float4* __restrict__ p_rad,
+__global__ void __launch_bounds__(128, SR_COMPOSE_MIN_BLOCKS) k_compose_rows2(const float4* __restrict__ p_rad,
                                                        const float4* __restrict__ p_geo,
                                                        const float4* __restrict__ p_fog,
                                                        const float* __restrict__ variance, uint32_t width,
