@@ -223,6 +223,37 @@ def test_compose_large_radius_and_reinhard(gpu_ctx, oracle_mod):
         assert (diff <= 1).mean() >= 0.999 and diff.max() <= 3
 
 
+def test_compose_neighbour_classes_and_odd_sizes(gpu_ctx, oracle_mod):
+    """All four neighbour classes of compose.cs:154-158 (normal present or not, depth finite or
+    not, including normals too small to square above zero), on odd and one-row / one-column
+    images: the device filter (two pixel rows per thread, classes in sign bits) against the
+    oracle's compositor."""
+    from sharpray_gb300 import _abi
+    import ctypes as C
+    rng = np.random.default_rng(11)
+    for w, h in ((37, 23), (5, 1), (1, 7), (64, 33)):
+        a = Aovs(w, h)
+        n = w * h
+        a.radiance[:] = rng.gamma(1.0, 0.5, size=(n, 3)).astype(np.float32)
+        a.radiance_fog[:] = rng.gamma(1.0, 0.05, size=(n, 3)).astype(np.float32)
+        nrm = rng.normal(size=(n, 3))
+        a.normals[:] = (nrm / np.linalg.norm(nrm, axis=1, keepdims=True)).astype(np.float32)
+        a.depth[:] = rng.uniform(1, 5, size=n).astype(np.float32)
+        cls = rng.integers(0, 4, size=n)
+        a.normals[cls & 1 == 1] = 0.0
+        tiny = (cls & 1 == 1) & (rng.random(n) < 0.3)
+        a.normals[tiny] = np.float32(1e-30)  # squares to zero: no normal, as in the reference
+        a.depth[cls & 2 == 2] = np.inf
+        a.variance[:] = rng.uniform(0, 0.3, size=n).astype(np.float32)
+        comp = Compositor(denoise_radius=0.3, exposure=1.1)
+        out = np.zeros((h, w, 3), np.uint8)
+        ac, pc = a.to_c(), comp.to_c()
+        _abi.check(gpu_ctx._lib.sr_compose(gpu_ctx.handle, C.byref(ac), w, h, C.byref(pc), out.ctypes.data))
+        ref = oracle_mod.compose(a, pc)
+        diff = np.abs(out.astype(int) - ref.astype(int))
+        assert (diff <= 1).mean() >= 0.999 and diff.max() <= 3, (w, h, (diff <= 1).mean(), diff.max())
+
+
 def test_render_compose_one_call(built):
     d, g, _ = built("features")
     comp = Compositor()
