@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--mode", type=int, default=0, help="render mode: 0 auto, 1 megakernel, 2 wavefront, 3 graph")
-    ap.add_argument("--variants", action="store_true", help="also time the megakernel render mode")
+    ap.add_argument("--no-megakernel", action="store_true",
+                    help="skip timing the megakernel render mode (one thread per pixel) among the render modes")
     ap.add_argument("--autotune-spp", type=int, default=8,
                     help="spp of the autotuner's trial renders at setup (0: default launch geometry)")
     ap.add_argument("--batch-autotune-spp", type=int, default=4,
@@ -856,9 +857,9 @@ def run_ours(args):
 
     # render modes on the same frame (identical images): the graph-captured device bounce loop
     # against the plain one-launch-per-bounce host loop, two renders each after a warm-up; the
-    # megakernel (one thread per pixel) with --variants
+    # megakernel (one thread per pixel) unless --no-megakernel
     variants = {}
-    modes = ((2, "wavefront_host_loop"), (3, "wavefront_graph")) + (((1, "megakernel"),) if args.variants else ())
+    modes = ((2, "wavefront_host_loop"), (3, "wavefront_graph")) + (() if args.no_megakernel else ((1, "megakernel"),))
     for mode, label in modes:
         scene.set_render_mode(mode)
         render()
