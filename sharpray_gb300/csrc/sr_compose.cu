@@ -112,9 +112,6 @@ __device__ __forceinline__ void filter_row(FilterCentre& c, const float4* __rest
     for (int kx = kx0; kx <= kx1; ++kx) filter_tap(c, __ldg(prow + kx), __ldg(grow + kx), __ldg(wrow + kx));
 }
 
-// Columns kx in [kx0, kx1] of one image row for two vertically adjacent pixels a and b (MODE bit 0:
-// the column is a tap of a, bit 1: of b), each tap column loaded once for both; wa / wb point at
-// the row's spatial weights of each pixel's kernel.
 // Unroll factor of the two-row kernel's column loop and its minimum resident blocks per SM (the
 // register cap).  Measured at 1920x1080: unroll 2 at 6 blocks (80 registers) 7.0 ms; unroll 1 at 6
 // or 8 blocks 7.5 ms; unroll 2 at 8 blocks (64 registers, spills) 8.2 ms.
@@ -125,6 +122,10 @@ __device__ __forceinline__ void filter_row(FilterCentre& c, const float4* __rest
 #define SR_COMPOSE_MIN_BLOCKS 6
 #endif
 constexpr int kComposeColUnroll = SR_COMPOSE_COL_UNROLL;
+
+// Columns kx in [kx0, kx1] of one image row for two vertically adjacent pixels a and b (MODE bit 0:
+// the column is a tap of a, bit 1: of b), each tap column loaded once for both; wa / wb point at
+// the row's spatial weights of each pixel's kernel.
 template <int MODE>
 __device__ __forceinline__ void filter_cols(FilterCentre& a, FilterCentre& b, const float4* __restrict__ prow,
                                             const float4* __restrict__ grow, const float* __restrict__ wa,
