@@ -22,6 +22,9 @@ enum : uint32_t {
 };
 // segment events (queue index)
 enum : int { EV_FOG = 0, EV_MISS = 1, EV_SURF = 2 };
+// Event selector of a shade kernel that shades both fog-scatter and miss events in one launch
+// (warps padded between the two queues so that each warp runs one event's logic).
+constexpr int EV_FOG_MISS = 3;
 
 // Sectors of a slot's path record (WaveState::rec, six per slot, 192 bytes on 64-byte boundaries:
 // {ray, hit}, {path, rng} and the shadow request each fill one 64-byte DRAM burst) and of its pixel
@@ -252,7 +255,9 @@ constexpr int kRefill = SR_REFILL;
 #ifndef SR_SHADE_FOG_MIN_BLOCKS
 #define SR_SHADE_FOG_MIN_BLOCKS 8
 #endif
-constexpr int shade_min_blocks(int ev) { return ev == 0 || ev == 1 ? SR_SHADE_FOG_MIN_BLOCKS : SR_SHADE_MIN_BLOCKS; }
+constexpr int shade_min_blocks(int ev) {
+    return ev == EV_FOG || ev == EV_MISS || ev == EV_FOG_MISS ? SR_SHADE_FOG_MIN_BLOCKS : SR_SHADE_MIN_BLOCKS;
+}
 constexpr int kNodeBurst = SR_NODE_BURST;
 // Order in which the persistent loop takes queries (bit 2: occlusion queue first; bits 0 / 1:
 // closest-hit / occlusion queue from its end).  A bounce's traversal kernel ends with a ramp-down
@@ -794,7 +799,7 @@ __device__ __forceinline__ SegOut shade_event(const WaveState& W, const DevScene
 // Path slot s from its stored state through its segment with event ev -- first the NEE
 // contribution of the previous segment if its shadow ray was traced since -- and, chaining, the
 // segments after it that need no traversal; then the new path state is stored.
-template <bool COUNT, bool GENERAL, int ADJ = kAdjNone>
+template <bool COUNT, bool GENERAL, int ADJ = kAdjNone, bool FOG_OR_MISS = false>
 __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevScene& S, const DevParams& P, uint32_t s,
                                                 int ev, Ctr& c, const AdjPass* A = nullptr) {
     const Rec rr = ld_rec(&W.rec[rix(W, s, R_RAY)]), pr = ld_rec(&W.rec[rix(W, s, R_PATH)]),
@@ -815,7 +820,7 @@ __device__ __forceinline__ SegOut shade_segment(const WaveState& W, const DevSce
         add_nee<COUNT, GENERAL, ADJ>(W, S, s, p.pflags, p.radiance, p.fog, c, vrec);
     }
     p.pflags &= ~(PF_NEE | PF_NEE_FOG);
-    SegOut o = shade_event<COUNT, GENERAL, false, ADJ>(W, S, P, s, ev, p, c, A);
+    SegOut o = shade_event<COUNT, GENERAL, FOG_OR_MISS, ADJ>(W, S, P, s, ev, p, c, A);
     if (SR_CHAIN_MIN_LANES > 0) {
         // at most bounces + 1 segments per sample: every segment advances the bounce index; the
         // lanes of the call vote each round, and all of them stop together
@@ -848,7 +853,9 @@ __device__ __forceinline__ uint32_t phase_events(const WaveState& W, int cur, in
 
 // One segment of every live path of the phase with event EVK, or of all its live paths (EVK = -1)
 // with warps sorted by event: the index space is then the fog queue, the miss queue and the surface
-// queue, the first two padded to whole warps, so every warp runs one event's logic.
+// queue, the first two padded to whole warps, so every warp runs one event's logic.  EVK =
+// EV_FOG_MISS: the fog queue (padded) and the miss queue in one launch, compiled with only the
+// fog and miss logic.
 template <bool COUNT, bool GENERAL, int EVK, int ADJ = kAdjNone>
 __global__ void __launch_bounds__(128, ADJ != kAdjNone ? 4 : shade_min_blocks(EVK))
     k_wave_shade(WaveState W, DevScene S, DevParams P, int cur, int phase, uint32_t* err,
@@ -865,17 +872,17 @@ __global__ void __launch_bounds__(128, ADJ != kAdjNone ? 4 : shade_min_blocks(EV
     const uint32_t nsurf = phase_events(W, cur, phase, EV_SURF, &first[EV_SURF]);
     const uint32_t ecount[3] = {nfog, nmiss, nsurf};
     const uint32_t pfog = (nfog + 31u) & ~31u, pmiss = (nmiss + 31u) & ~31u;
-    const uint32_t total = EVK >= 0 ? ecount[EVK] : pfog + pmiss + nsurf;
+    const uint32_t total = EVK == EV_FOG_MISS ? pfog + nmiss : EVK >= 0 ? ecount[EVK % 3] : pfog + pmiss + nsurf;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < total; base += stride) {
         const uint32_t k = base + threadIdx.x;
         int ev;
         uint32_t i, cnt;
-        if (EVK >= 0) {
+        if (EVK >= 0 && EVK != EV_FOG_MISS) {
             ev = EVK, i = k, cnt = total;
         } else if (k < pfog) {
             ev = EV_FOG, i = k, cnt = nfog;
-        } else if (k < pfog + pmiss) {
+        } else if (EVK == EV_FOG_MISS || k < pfog + pmiss) {
             ev = EV_MISS, i = k - pfog, cnt = nmiss;
         } else {
             ev = EV_SURF, i = k - pfog - pmiss, cnt = nsurf;
@@ -885,7 +892,7 @@ __global__ void __launch_bounds__(128, ADJ != kAdjNone ? 4 : shade_min_blocks(EV
         const uint32_t s = valid ? q[(size_t)ev * W.slots + first[ev] + i] : 0u;
         SegOut o;
         if (valid) {
-            o = shade_segment<COUNT, GENERAL, ADJ>(W, S, P, s, ev, c, A);
+            o = shade_segment<COUNT, GENERAL, ADJ, EVK == EV_FOG_MISS>(W, S, P, s, ev, c, A);
         }
         uint32_t* eq = W.q_event[nxt];
         // finished samples wait for their last shadow ray (traced next bounce) when it has one; so

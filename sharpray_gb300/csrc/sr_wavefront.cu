@@ -273,7 +273,13 @@ static void launch_shade(const WaveLaunch& L, const WaveState& W, int cur, int p
         wave_adj_shade(L, W, cur, phase, st, events);
         return;
     }
-    if (SR_SPLIT_SHADE) {
+    if (SR_SPLIT_SHADE && SR_FOG_MISS_ONE && (events & 3) == 3) {
+        k_wave_shade<COUNT, GENERAL, EV_FOG_MISS><<<phase == 0 ? L.grid_ready[0] : L.grid_shade[0], 128, 0, st>>>(
+            W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
+        if (phase == 1 && (events & 4))
+            k_wave_shade<COUNT, GENERAL, EV_SURF>
+                <<<L.grid_shade[2], 128, 0, st>>>(W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
+    } else if (SR_SPLIT_SHADE) {
         if (events & 1)
             k_wave_shade<COUNT, GENERAL, EV_FOG><<<phase == 0 ? L.grid_ready[0] : L.grid_shade[0], 128, 0, st>>>(
                 W, L.S, L.P, cur, phase, L.err, L.counters, nullptr);
@@ -401,7 +407,10 @@ static void occupancy(int* b) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[1], k_wave_shadow_loop<false, GENERAL>, 128, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[2], k_wave_finalize<false, GENERAL, false>, 128, 0);
     if (SR_SPLIT_SHADE) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shade<false, GENERAL, EV_FOG>, 128, 0);
+        if (SR_FOG_MISS_ONE)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shade<false, GENERAL, EV_FOG_MISS>, 128, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[3], k_wave_shade<false, GENERAL, EV_FOG>, 128, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[4], k_wave_shade<false, GENERAL, EV_MISS>, 128, 0);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b[5], k_wave_shade<false, GENERAL, EV_SURF>, 128, 0);
     } else {

@@ -222,8 +222,15 @@ struct WaveGroups {
 // Side streams and events a bounce's branches use (one group), or the other groups' streams.
 constexpr int kSideStreams = kWaveGroups > 3 ? kWaveGroups - 1 : 3;
 constexpr int kForkEvents = kWaveGroups + 1 > 6 ? kWaveGroups + 1 : 6;
-constexpr int kWaveKernelsPerBounce = (SR_SPLIT_SHADE ? 6 : 4) + (SR_SORT_EVENTS ? 1 : 0) +
-                                      (kSplitPhases ? (SR_SPLIT_SHADE ? 3 : 2) : 0) + (SR_TRACE_OCTANT_SORT ? 1 : 0);
+// The fog-scatter and miss events of a phase are shaded by one launch (SR_FOG_MISS_ONE = 1: warps
+// padded between the two queues) or by one launch each (0).
+#ifndef SR_FOG_MISS_ONE
+#define SR_FOG_MISS_ONE 1
+#endif
+constexpr int kShadeLaunches = SR_SPLIT_SHADE ? (SR_FOG_MISS_ONE ? 2 : 3) : 1;  // waiting phase
+constexpr int kReadyShadeLaunches = SR_SPLIT_SHADE && !SR_FOG_MISS_ONE ? 2 : 1;
+constexpr int kWaveKernelsPerBounce = 3 + kShadeLaunches + (SR_SORT_EVENTS ? 1 : 0) +
+                                      (kSplitPhases ? 1 + kReadyShadeLaunches : 0) + (SR_TRACE_OCTANT_SORT ? 1 : 0);
 
 // Launch geometry chosen at run time (0 = the default: as many blocks per SM as fit).
 struct WaveTune {
