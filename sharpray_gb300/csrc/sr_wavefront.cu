@@ -97,22 +97,57 @@ __global__ void __launch_bounds__(128) k_wave_init(WaveState W, DevScene S, DevV
 // written yet reads as 0 or as a waiting tag, both left alone); phase 1 takes the rest of the
 // bounce's events and places them after phase 0's.  Tags for the next bounce (from a late finalize)
 // are left in place.
-__global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur, int phase) {
-    __shared__ uint32_t warp_n[3][8];
+//
+// Slots one thread of k_event_sort scans (4, 8 or 16: consecutive slots of one 32-slot tile, their
+// tags read as one vector when they are all inside the group; the tags it takes are cleared byte
+// by byte, since the traversal kernel may be tagging the others).  Measured on the 1080p fog
+// workload (graph mode): 4 per thread 527.7, 8 525.8, 16 523.1 M samples/s -- the kernel wants
+// the parallelism more than fewer blocks and atomics.
+#ifndef SR_SORT_PER_THREAD
+#define SR_SORT_PER_THREAD 4
+#endif
+constexpr int kSortPerThread = SR_SORT_PER_THREAD;
+static_assert(kSortPerThread == 4 || kSortPerThread == 8 || kSortPerThread == 16, "k_event_sort slots per thread");
+constexpr int kSortBlock = 256;
+
+__global__ void __launch_bounds__(kSortBlock) k_event_sort(WaveState W, int cur, int phase) {
+    __shared__ uint32_t warp_n[3][kSortBlock / 32];
     __shared__ uint32_t base[3];
-    const uint32_t li = 4u * (blockIdx.x * blockDim.x + threadIdx.x);  // group-local slot index
-    const uint32_t s0 = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);  // 4 consecutive slots
-    uint32_t ev4[4];
+    constexpr int K = kSortPerThread;
+    const uint32_t li = K * (blockIdx.x * blockDim.x + threadIdx.x);  // group-local slot index
+    const uint32_t s0 = ((li >> 5) * W.groups + W.group) * 32u + (li & 31u);  // K consecutive slots
+    // the K tags (one byte each)
+    uint32_t tag[K / 4];
+    if (li + K <= W.slots) {
+        if constexpr (K == 16) {
+            const uint4 v = *reinterpret_cast<const uint4*>(W.ev_mark + s0);
+            tag[0] = v.x, tag[1] = v.y, tag[2] = v.z, tag[3] = v.w;
+        } else if constexpr (K == 8) {
+            const uint2 v = *reinterpret_cast<const uint2*>(W.ev_mark + s0);
+            tag[0] = v.x, tag[1] = v.y;
+        } else {
+            tag[0] = *reinterpret_cast<const uint32_t*>(W.ev_mark + s0);
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < K / 4; ++q) {
+            tag[q] = 0u;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (li + 4 * q + j < W.slots) tag[q] |= (uint32_t)W.ev_mark[s0 + 4 * q + j] << (8 * j);
+        }
+    }
+    uint32_t evs = 0;  // 2 bits per slot: the slot's event of this bounce and phase, 3 = none
     uint32_t cnt[3] = {0, 0, 0};
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const uint32_t m = li + j < W.slots ? W.ev_mark[s0 + j] : 0u;
+    for (int j = 0; j < K; ++j) {
+        const uint32_t m = (tag[j >> 2] >> (8 * (j & 3))) & 0xffu;
         // m = 1 + event + 3 x parity + 6 x wait: the event of this bounce and phase, else >= 3
         const uint32_t t = phase == 0 ? m - 1u - 3u * (uint32_t)cur : (m > 6u ? m - 7u : m - 1u) - 3u * (uint32_t)cur;
-        const uint32_t e = m == 0u ? 3u : t;
-        ev4[j] = e < 3u ? e : 3u;
+        const uint32_t e = m == 0u ? 3u : (t < 3u ? t : 3u);
+        evs |= e << (2 * j);
         if (e < 3u) {
-            W.ev_mark[s0 + j] = 0;
+            W.ev_mark[s0 + j] = 0;  // byte stores: other slots' tags may be written meanwhile
             ++cnt[e];
         }
     }
@@ -132,7 +167,7 @@ __global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur, int ph
     __syncthreads();
     if (threadIdx.x < 3) {
         uint32_t t = 0;
-        for (int w = 0; w < 8; ++w) t += warp_n[threadIdx.x][w];
+        for (int w = 0; w < kSortBlock / 32; ++w) t += warp_n[threadIdx.x][w];
         const uint32_t first = phase == 0 ? 0u : W.counts[kCountSorted + threadIdx.x];
         base[threadIdx.x] =
             first + (t ? atomicAdd(&W.counts[(phase == 0 ? kCountSorted : kCountSortedLate) + threadIdx.x], t) : 0u);
@@ -145,10 +180,14 @@ __global__ void __launch_bounds__(256) k_event_sort(WaveState W, int cur, int ph
         for (uint32_t w = 0; w < warp; ++w) off[e] += warp_n[e][w];
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const uint32_t e = ev4[j];
+    for (int j = 0; j < K; ++j) {
+        const uint32_t e = (evs >> (2 * j)) & 3u;
         if (e < 3u) W.q_sorted[(size_t)e * W.slots + off[e]++] = s0 + j;
     }
+}
+
+static unsigned sort_blocks(const WaveState& W) {
+    return (W.slots + kSortBlock * kSortPerThread - 1) / (kSortBlock * kSortPerThread);
 }
 
 // Closest hits of world rays through the renderer's own persistent traversal loop (the ray
@@ -319,7 +358,7 @@ static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cu
     if (kSplitPhases) {
         cudaStream_t sa = side ? side[0] : st;
         if (side && (e = stream_join(side[0], st, fork[0])) != cudaSuccess) return e;
-        k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, sa>>>(W, cur, 0);
+        k_event_sort<<<sort_blocks(W), kSortBlock, 0, sa>>>(W, cur, 0);
         launch_shade<COUNT, GENERAL>(L, W, cur, 0, sa);
     }
     if (SR_TRACE_OCTANT_SORT) k_trace_octant_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W, cur);
@@ -342,7 +381,7 @@ static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cu
         k_wave_finalize<COUNT, GENERAL, true><<<L.grid_finalize, 128, 0, sl>>>(W, L.S, L.V, L.P, L.out, cur, L.err,
                                                                                L.counters, nullptr);
     if (kSplitPhases && side && (e = stream_join(st, side[0], fork[2])) != cudaSuccess) return e;
-    if (SR_SORT_EVENTS) k_event_sort<<<(W.slots + 1023) / 1024, 256, 0, st>>>(W, cur, 1);
+    if (SR_SORT_EVENTS) k_event_sort<<<sort_blocks(W), kSortBlock, 0, st>>>(W, cur, 1);
     if (par && SR_SPLIT_SHADE) {
         if ((e = stream_join(side[2], st, fork[3])) != cudaSuccess) return e;
         launch_shade<COUNT, GENERAL>(L, W, cur, 1, side[2], 4);
