@@ -243,6 +243,11 @@ constexpr int kRefill = SR_REFILL;
 #ifndef SR_LEAF_WAIT
 #define SR_LEAF_WAIT 16
 #endif
+// The node burst takes one warp vote per node visit (1) or two (0: any lane with node work, then
+// the lanes waiting for a leaf action); both make the same decisions.
+#ifndef SR_BURST_ONE_VOTE
+#define SR_BURST_ONE_VOTE 1
+#endif
 // Shading runs as one kernel per event (SR_SPLIT_SHADE = 1): fog scatter, the most frequent
 // event in foggy scenes, then needs far fewer registers than surface shading and runs at higher
 // occupancy.  Minimum resident blocks per SM requested for each (caps their registers).
@@ -370,10 +375,23 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
                 }
             }
         }
-        if (!__any_sync(0xffffffffu, busy)) {
+        const unsigned busy_mask = __ballot_sync(0xffffffffu, busy);
+        if (!busy_mask) {
             if (exhausted) break;
             continue;
         }
+#if SR_BURST_ONE_VOTE
+        // one vote per node visit: the lanes waiting for a leaf action (or done); the busy lanes
+        // not among them have node work (a lane's busy flag does not change inside the burst)
+        unsigned waiting = __ballot_sync(0xffffffffu, busy && sq.state != QS_NODE);
+#pragma unroll 1
+        for (int k = 0; k < kNodeBurst; ++k) {
+            if (!(busy_mask & ~waiting)) break;
+            if (busy && sq.state == QS_NODE) sq.template node_action<COUNT>(S, stack, c, err);
+            waiting = __ballot_sync(0xffffffffu, busy && sq.state != QS_NODE);
+            if (__popc(waiting) >= kLeafWait) break;
+        }
+#else
 #pragma unroll 1
         for (int k = 0; k < kNodeBurst; ++k) {
             bool nodework = busy && sq.state == QS_NODE;
@@ -381,6 +399,7 @@ __device__ __forceinline__ void persistent_queries(const DevScene& S, const Rec*
             if (nodework) sq.template node_action<COUNT>(S, stack, c, err);
             if (__popc(__ballot_sync(0xffffffffu, busy && sq.state != QS_NODE)) >= kLeafWait) break;
         }
+#endif
         if (busy && sq.state != QS_NODE && sq.state != QS_DONE) sq.template leaf_action<COUNT>(S, stack, c, err);
         if (busy && sq.state == QS_DONE) {
             busy = false;
