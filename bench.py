@@ -163,6 +163,12 @@ def algorithmic_bytes(c: dict, pixels: int) -> int:
                + 56 * pixels)
 
 
+def traversal_bytes(c: dict) -> int:
+    """The share of algorithmic_bytes that the traversal kernel touches: node, triangle and
+    instance tests."""
+    return int(32 * (c["tlas_node"] + c["blas_node"]) + 36 * c["blas_shape"] + 40 * c["tlas_shape"])
+
+
 def oracle_bands(scene, view, params, threads: int, height: int, rows_per_band: int, bands: int = 16,
                  shift: int = 0, keep: bool = False):
     """Renders `bands` evenly spaced bands of `rows_per_band` image rows with the CPU oracle (a
@@ -872,6 +878,16 @@ def run_ours(args):
         b.record(stream)
         torch.cuda.synchronize()
         variants[label] = samples_per_step / (a.elapsed_time(b) / 2000.0)
+    # the dominant kernel, the traversal, timed live: one host-loop render with a CUDA-event pair
+    # around every bounce's traversal kernel on the render's stream
+    trace_timing = None
+    if args.mode in (0, 2, 3):
+        scene.set_render_mode(2)
+        scene.set_kernel_timing(True)
+        render()
+        torch.cuda.synchronize()
+        trace_timing = scene.trace_time()
+        scene.set_kernel_timing(False)
     scene.set_render_mode(args.mode)
     variants["graph_over_host_loop"] = variants["wavefront_graph"] / variants["wavefront_host_loop"]
 
@@ -913,13 +929,33 @@ def run_ours(args):
     alg = algorithmic_bytes(counters, n)
     kern_s = statistics.mean(render_ms) / 1000.0
     achieved = alg / kern_s / 1e9
-    traffic = None
+    traffic, trace_traffic, trace_ncu_launches = None, None, None
     tf = ROOT / "profiles" / "path_tracer_c2_traffic.json"
     if tf.exists() and (W, H, desc.spp) == (1920, 1080, 64):
         try:
-            traffic = json.loads(tf.read_text()).get("traffic_bytes_per_frame")
+            tj = json.loads(tf.read_text())
+            traffic = tj.get("traffic_bytes_per_frame")
+            trace_traffic = tj.get("trace_traffic_bytes_per_frame")
+            trace_ncu_launches = tj.get("trace_launches")
         except Exception:
             traffic = None
+    # roofline of the traversal kernel: the reference's bytes for its work (node, triangle and
+    # instance tests) per launch over its average launch time
+    trace_roof = None
+    if trace_timing and trace_timing["launches"] > 0:
+        nl = trace_timing["launches"]
+        trace_alg = traversal_bytes(counters)
+        trace_s = trace_timing["total_ms"] / 1000.0
+        trace_ach = trace_alg / trace_s / 1e9
+        trace_roof = {"bound": "hbm", "achieved": trace_ach, "peak": peak, "unit": "GB/s", "frac": trace_ach / peak,
+                      "traffic": trace_traffic / trace_ncu_launches if trace_traffic and trace_ncu_launches else None,
+                      "kernel": "k_wave_trace (persistent traversal: path rays + shadow rays of a bounce)",
+                      "launches": nl, "kernel_ms_per_launch": trace_timing["total_ms"] / nl,
+                      "alg_bytes_per_launch": trace_alg / nl, "peak_source": peak_kind,
+                      "note": "timed live with CUDA events around each traversal launch of a host-loop render "
+                              "of the same frame; alg bytes 32 per node test, 36 per triangle test, 40 per "
+                              "instance test from the kernels' work counters; traffic per launch from the ncu "
+                              "launch list of the same frame"}
 
     cpu, parity = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -950,7 +986,9 @@ def run_ours(args):
                        "wall_s_timed": round(wall, 3)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": H2D_PARAM_BYTES,
                     "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "roofline": trace_roof or {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                       "frac": achieved / peak, "traffic": traffic, "kernel": "frame"},
+            "roofline_frame": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": ("path tracer: k_render_pixels" if args.mode == 1 else
                                     "path tracer: k_wave_trace/finalize(late)/shade(fog,miss,surface)/finalize "

@@ -302,6 +302,15 @@ SR_API int sr_scene_render_info(SrScene* scene, uint32_t* kernel_launches, uint3
  * sr_scene_set_counting); counters_out has SR_COUNTER_COUNT entries. */
 SR_API int sr_scene_set_counting(SrScene* scene, int32_t enabled);
 SR_API int sr_scene_counters(SrScene* scene, uint64_t* counters_out);
+/* Traversal-kernel timing (no reference counterpart; the reference's Counters.TimeRender times
+ * whole renders): with timing enabled, a render in SR_RENDER_WAVEFRONT mode (the host loop)
+ * records CUDA events on its stream right before and after every bounce's traversal kernel.
+ * sr_scene_trace_time (synchronises) returns their summed duration in milliseconds and the number
+ * of traversal launches of the last such render or adjoint replay; 0 and 0 when the last render
+ * ran in another mode or without timing.  Other kernels of a bounce may run beside the traversal
+ * kernel on parallel branches, as in an untimed render. */
+SR_API int sr_scene_set_kernel_timing(SrScene* scene, int32_t enabled);
+SR_API int sr_scene_trace_time(SrScene* scene, float* total_ms, uint32_t* launches);
 
 /* ---- compositing ------------------------------------------------------------------------- */
 /* Joint bilateral denoise + fog blur + tonemap to RGB8 (width*height*3 bytes), host AOVs in,

@@ -179,6 +179,8 @@ PROTOTYPES = {
     "sr_scene_render_info": (_I, [_P, C.POINTER(_U), C.POINTER(_U)]),
     "sr_scene_set_counting": (_I, [_P, C.c_int32]),
     "sr_scene_counters": (_I, [_P, _P]),
+    "sr_scene_set_kernel_timing": (_I, [_P, C.c_int32]),
+    "sr_scene_trace_time": (_I, [_P, C.POINTER(C.c_float), C.POINTER(_U)]),
     "sr_compose": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P]),
     "sr_compose_device": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),
     "sr_compose_device_static": (_I, [_P, C.POINTER(SrAovs), _U, _U, C.POINTER(SrComposeParams), _P, _P]),

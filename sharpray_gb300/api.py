@@ -590,6 +590,16 @@ class Scene:
     def set_counting(self, enabled: bool) -> None:
         check(self._lib.sr_scene_set_counting(self.handle, int(enabled)))
 
+    def set_kernel_timing(self, enabled: bool) -> None:
+        """Time every traversal kernel of host-loop renders (render mode 2) with CUDA events."""
+        check(self._lib.sr_scene_set_kernel_timing(self.handle, int(enabled)))
+
+    def trace_time(self) -> dict:
+        """Summed traversal-kernel time (ms) and launches of the last timed host-loop render."""
+        ms, n = C.c_float(), C.c_uint32()
+        check(self._lib.sr_scene_trace_time(self.handle, C.byref(ms), C.byref(n)))
+        return {"total_ms": ms.value, "launches": n.value}
+
     def counters(self) -> dict:
         out = np.zeros(_abi.SR_COUNTER_COUNT, np.uint64)
         check(self._lib.sr_scene_counters(self.handle, ptr(out)))

@@ -174,6 +174,11 @@ struct SrScene {
     int last_mode = 0;                // render mode of the last render
     uint32_t last_host_iters = 0;     // bounces run by the host loop
     bool last_tail = false;           // the host loop launched the tail kernel
+    // traversal-kernel timing of host-loop renders (sr_scene_set_kernel_timing)
+    bool kernel_timing = false;
+    cudaEvent_t trace_ev[2] = {};
+    double trace_ms = 0.0;         // summed duration of the last host-loop render's traversal kernels
+    uint32_t trace_launches = 0;   // ... and their number
     // adjoint passes of the wavefront kernels (sr_wave_adjoint.cu)
     int32_t adjoint_replay = SR_ADJOINT_REPLAY_WAVEFRONT;  // sr_scene_set_adjoint_replay
     DevBuf adj_vbuf, adj_pass;     // replay: vertex records (one sample per slot), the device AdjPass
@@ -195,6 +200,8 @@ struct SrScene {
         if (counts_host) cudaFreeHost(counts_host);
         if (progress_host) cudaFreeHost(progress_host);
         if (progress_event) cudaEventDestroy(progress_event);
+        for (cudaEvent_t& e : trace_ev)
+            if (e) cudaEventDestroy(e);
     }
 };
 
@@ -1036,6 +1043,14 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
     }
     const size_t count_bytes = kWaveGroups * kWaveCounters * sizeof(uint32_t);
     if (!s->counts_host) SR_CUDA(cudaMallocHost(&s->counts_host, count_bytes), "pinned alloc");
+    s->trace_ms = 0.0;
+    s->trace_launches = 0;
+    if (s->kernel_timing) {  // an event pair around every bounce's traversal kernel, read after the bounce
+        for (cudaEvent_t& e : s->trace_ev)
+            if (!e) SR_CUDA(cudaEventCreate(&e), "event");
+        L.trace_ev[0] = s->trace_ev[0];
+        L.trace_ev[1] = s->trace_ev[1];
+    }
     for (uint32_t it = 0;; ++it) {
         if (it >= L.max_iters)
             return fail(SR_ERR_DEVICE, "wavefront loop exceeded %u bounces (error word 0x2, loop cap)", L.max_iters);
@@ -1043,6 +1058,12 @@ static int render_wavefront(SrScene* s, const DevView& dv, const DevParams& dp, 
         SR_CUDA(wave_bounce(L, cur, st, s->side_streams, s->fork_events), "wavefront bounce");
         SR_CUDA(cudaMemcpyAsync(s->counts_host, s->ws[0].counts, count_bytes, cudaMemcpyDeviceToHost, st), "read live count");
         SR_CUDA(cudaStreamSynchronize(st), "wavefront bounce");
+        if (L.trace_ev[0]) {
+            float ms = 0.0f;
+            SR_CUDA(cudaEventElapsedTime(&ms, L.trace_ev[0], L.trace_ev[1]), "traversal kernel time");
+            s->trace_ms += ms;
+            ++s->trace_launches;
+        }
         uint32_t live = 0, done = 0;
         for (int g = 0; g < kWaveGroups; ++g) {
             live += wave_live(s->counts_host + g * kWaveCounters, cur ^ 1, s->ws[g].defer_cap);
@@ -1395,6 +1416,23 @@ SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t*
         *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + (s->last_tail ? 1 : 0);
     }
     *bounce_iterations = iters;
+    return SR_OK;
+}
+
+SR_API int sr_scene_set_kernel_timing(SrScene* s, int32_t enabled) {
+    if (!s) return fail(SR_ERR_INVALID_ARG, "scene is NULL");
+    s->kernel_timing = enabled != 0;
+    return SR_OK;
+}
+
+SR_API int sr_scene_trace_time(SrScene* s, float* total_ms, uint32_t* launches) {
+    if (!s || !total_ms || !launches) return fail(SR_ERR_INVALID_ARG, "NULL argument");
+    if (int rc = need_device(s)) return rc;
+    SR_CUDA(cudaSetDevice(s->ctx->device), "cudaSetDevice");
+    SR_CUDA(cudaDeviceSynchronize(), "sync");
+    const bool timed = s->last_mode == SR_RENDER_WAVEFRONT;
+    *total_ms = timed ? (float)s->trace_ms : 0.0f;
+    *launches = timed ? s->trace_launches : 0u;
     return SR_OK;
 }
 

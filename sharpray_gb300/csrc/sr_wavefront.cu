@@ -362,6 +362,7 @@ static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cu
         launch_shade<COUNT, GENERAL>(L, W, cur, 0, sa);
     }
     if (SR_TRACE_OCTANT_SORT) k_trace_octant_sort<<<(W.slots + 255) / 256, 256, 0, st>>>(W, cur);
+    if (L.trace_ev[0] && (e = cudaEventRecord(L.trace_ev[0], st)) != cudaSuccess) return e;
     const bool loop_shadows = GENERAL && L.S.has_transparent;
     if (!COUNT && L.trace_block != 128) {
         wave_trace_block(L, W, cur, st, loop_shadows);
@@ -371,6 +372,7 @@ static cudaError_t launch_bounce(const WaveLaunch& L, const WaveState& W, int cu
         k_wave_trace<COUNT, GENERAL, true><<<L.grid_trace, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
     }
     if (loop_shadows) k_wave_shadow_loop<COUNT, GENERAL><<<L.grid_shadow, 128, 0, st>>>(W, L.S, cur, L.err, L.counters);
+    if (L.trace_ev[1] && (e = cudaEventRecord(L.trace_ev[1], st)) != cudaSuccess) return e;
     // the late finalize: the samples whose last shadow ray the traversal kernel just traced
     const bool par = SR_PAR_SHADE && side != nullptr;
     cudaStream_t sl = par ? side[1] : st;

@@ -188,6 +188,8 @@ struct WaveLaunch {
     uint32_t* progress;   // host-mapped word the device loop publishes finished pixels to (or null)
     int adj_mode;         // kAdj*: the kernels of an adjoint pass
     const AdjPass* adj;   // device AdjPass of an adjoint pass
+    cudaEvent_t trace_ev[2];  // host-loop renders with kernel timing: recorded on the launching stream
+                              // right before and after each bounce's traversal kernel (else null)
     int grid_adj_shade[3], grid_adj_finalize;  // their grids
 };
 

@@ -298,6 +298,34 @@ def test_render_modes_identical(built, name):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (mode, plane)
 
 
+def test_traversal_kernel_timing(built):
+    """sr_scene_set_kernel_timing: a host-loop render times one traversal kernel per bounce with
+    CUDA events and gives the same image as an untimed render; other render modes report none."""
+    import time
+
+    from sharpray_gb300 import _abi
+    d, g, _ = built("c2_reduced")
+    g.set_render_mode(_abi.SR_RENDER_WAVEFRONT)
+    plain = Renderer(g, d.view, *d.render_args())
+    g.set_kernel_timing(True)
+    try:
+        t0 = time.perf_counter()
+        timed = Renderer(g, d.view, *d.render_args())
+        wall_ms = 1e3 * (time.perf_counter() - t0)
+        t = g.trace_time()
+        info = g.render_info()
+        assert t["launches"] == info["bounce_iterations"] > 0
+        assert 0.0 < t["total_ms"] < wall_ms
+        for plane in ("radiance", "radiance_fog", "samples"):
+            assert np.array_equal(getattr(timed, plane).view(np.uint32), getattr(plain, plane).view(np.uint32))
+        g.set_render_mode(_abi.SR_RENDER_WAVEFRONT_GRAPH)
+        Renderer(g, d.view, *d.render_args())
+        assert g.trace_time() == {"total_ms": 0.0, "launches": 0}
+    finally:
+        g.set_kernel_timing(False)
+        g.set_render_mode(_abi.SR_RENDER_AUTO)
+
+
 def test_adaptive_sampling_wavefront(built, oracle_mod):
     """Adaptive stop (minSamples < maxSamples) through the wavefront loop matches the oracle."""
     d, g, o = built("c1")
