@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--joint-steps", type=int, default=0,
                     help="--adjoint-only: Adam steps recovering albedo, roughness and fog density jointly on a small "
                          "version of the 16-view workload")
+    ap.add_argument("--joint-smooth", type=float, default=0.0,
+                    help="--joint-steps: weight of a smoothness prior on both textures (0: none)")
     ap.add_argument("--adjoint-only", action="store_true",
                     help="run only the adjoint workload (--steps timed passes, --adjoint-checks FD checks)")
     ap.add_argument("--profile-once", action="store_true",
@@ -560,7 +562,7 @@ def measure_inverse(steps: int, views: int = 4, size: int = 256, spp: int = 8) -
 
 def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 32, rings: int = 500,
                        tex: int = 1024, lr_tex: float = 0.02, lr_density: float = 0.002,
-                       target_spp_factor: int = 4, form: str = "replay") -> dict:
+                       target_spp_factor: int = 4, form: str = "replay", smooth: float = 0.0) -> dict:
     """The batched + differentiable configuration (synth.config_c5: 16 orbit views, 768x768, 32 spp,
     depth 8, 500,000 triangles, 1024x1024 albedo + roughness textures, fog; smaller with the
     arguments): per step every view is rendered and its image gradient replayed once for the albedo
@@ -572,6 +574,8 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
     form "checkpoint" instead renders each view with sr_render_checkpointed (every sample's path
     vertices kept on the device) and sweeps them with sr_adjoint_checkpointed: no second traversal,
     at the memory of every sample's vertices, and dL/dI and dI/dθ from the same samples.
+    `smooth` > 0 adds a smoothness prior to the loss: smooth x the summed squared differences of
+    neighbouring texels (wrapping, as the textures repeat) of both textures.
     Reports the time per step after one warm-up step over `steps` timed steps, the vertex-record
     memory the form holds, and the texture errors (albedo rgb, roughness channel 0, on the
     well-observed texels) before and after."""
@@ -652,6 +656,12 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
                                               C.c_void_p(d_img.data_ptr()), tex_a.id, C.c_void_p(ga.data_ptr()),
                                               tex_r.id, C.c_void_p(gr.data_ptr()), C.c_void_p(gs.data_ptr()), None,
                                               C.c_void_p(st.cuda_stream)))
+            if smooth > 0.0:  # gradient of the smoothness prior: 2 smooth (4 x - its four neighbours)
+                for x, g, ch in ((xa, ga, slice(None)), (xr, gr, slice(0, 1))):
+                    v = x.detach()[..., ch]
+                    lap = 4.0 * v - (torch.roll(v, 1, 0) + torch.roll(v, -1, 0) + torch.roll(v, 1, 1) +
+                                     torch.roll(v, -1, 1))
+                    g[..., ch] += 2.0 * smooth * lap
             xa.grad, xr.grad, xs.grad = ga, gr, gs
             # cosine decay of the learning rates over the run: the gradients are Monte Carlo
             # estimates, and at a fixed rate Adam's normalised steps keep the texels moving by about
@@ -697,6 +707,7 @@ def measure_inverse_c5(steps: int, views: int = 16, size: int = 768, spp: int = 
             "form": form, "vertex_record_bytes": vertex_bytes,
             "timed_steps": steps, "ms_per_step": 1000 * dt, "texel_grads_per_s": n_grads / dt,
             "adam": {"lr_textures": lr_tex, "lr_density": lr_density, "schedule": "cosine decay to 0 over the run"},
+            "smoothness_prior": smooth,
             "path_samples_per_s": samples * (1 if form == "checkpoint" else 2) / dt,
             "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
             "fog_density": {"true": sigma, "start": 1.5 * sigma, "after": float(xs.detach())},
@@ -1031,7 +1042,8 @@ def main():
                                                                               form="checkpoint")
         if args.joint_steps > 0:  # the same pipeline small enough to run to convergence
             adj["joint_recovery"] = measure_inverse_c5(args.joint_steps, views=4, size=192, spp=8, rings=150,
-                                                       tex=128, lr_tex=0.005, lr_density=0.001, target_spp_factor=8)
+                                                       tex=128, lr_tex=0.005, lr_density=0.001, target_spp_factor=8,
+                                                       smooth=args.joint_smooth)
         print(json.dumps({"adjoint": adj}), flush=True)
     else:
         run_ours(args)
