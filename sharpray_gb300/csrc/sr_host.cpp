@@ -1409,9 +1409,8 @@ SR_API int sr_scene_render_info(SrScene* s, uint32_t* kernel_launches, uint32_t*
     uint32_t iters = s->last_host_iters;
     if (s->last_mode == SR_RENDER_WAVEFRONT_GRAPH) {
         SR_CUDA(cudaMemcpy(&iters, s->ws[0].counts + kCountIter, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read bounce count");
-        // init, the bounce kernels, one loop condition per 2 bounces
-        // init and bounce kernels per group, one loop condition per 2 bounces, the tail kernel
-        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + iters / 2 + 1;
+        // init and bounce kernels per group, one loop condition per loop body, the tail kernel
+        *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + iters / kGraphBounces + 1;
     } else {
         *kernel_launches = kWaveGroups * (1 + kWaveKernelsPerBounce * iters) + (s->last_tail ? 1 : 0);
     }

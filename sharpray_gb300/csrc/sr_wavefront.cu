@@ -247,7 +247,7 @@ cudaError_t launch_trace_persistent(const DevScene& S, bool general, const float
 // (max_samples + 1) * (bounces + 2) per pixel) is not reached.  `counts` holds the groups' counters one after another.
 __global__ void k_wave_continue(cudaGraphConditionalHandle handle, uint32_t* counts, int groups, uint32_t tail,
                                 uint32_t max_iters, uint32_t* err, uint32_t* progress, uint32_t defer_cap) {
-    uint32_t it = counts[kCountIter] + 2;  // two bounces per loop body
+    uint32_t it = counts[kCountIter] + kGraphBounces;  // bounces per loop body
     counts[kCountIter] = it;
     uint32_t live = 0, done = 0;
     for (int g = 0; g < groups; ++g) {
@@ -561,8 +561,8 @@ cudaError_t wave_build_graph_batch(const WaveLaunch* Ls, int n, cudaStream_t cap
         cudaGraph_t body = cp.conditional.phGraph_out[0];
         e = cudaStreamBeginCaptureToGraph(capture_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (e != cudaSuccess) break;
-        // two bounces per group on parallel branches, joined before the loop condition
-        cudaError_t e1 = launch_bounces(L, 0, 2, capture_stream, side, fork);
+        // kGraphBounces bounces per group on parallel branches, joined before the loop condition
+        cudaError_t e1 = launch_bounces(L, 0, kGraphBounces, capture_stream, side, fork);
         k_wave_continue<<<1, 1, 0, capture_stream>>>(handle, L.W[0].counts, L.groups, L.tail_paths, L.max_iters, L.err,
                                                      L.progress, L.W[0].defer_cap);
         cudaGraph_t captured = nullptr;

@@ -199,6 +199,13 @@ struct WaveGroups {
     int groups;
 };
 
+// Bounces per body of the graph's device-side loop (even: the tail after the loop takes parity 0).
+#ifndef SR_GRAPH_BOUNCES
+#define SR_GRAPH_BOUNCES 2
+#endif
+constexpr int kGraphBounces = SR_GRAPH_BOUNCES;
+static_assert(kGraphBounces % 2 == 0, "whole pairs of bounces per loop body");
+
 // The bounce loop hands over to the tail kernel at slots / SR_TAIL_DIV live paths (0: never).
 #ifndef SR_TAIL_DIV
 #define SR_TAIL_DIV 16
